@@ -1,0 +1,29 @@
+#!/bin/sh
+# Builds the oracle pin: PhiNum's own hot-path sources, compiled unchanged
+# from the reference tree (REF_DIR, default /root/reference) against the
+# single-rank MPI/FFTW shims in oracle/ref_shim/, into oracle/_ref/.
+#
+# Test infrastructure only.  Flags: no -ffast-math and no FP contraction, so
+# that the reference's FP64 arithmetic is plain IEEE round-to-nearest in
+# source order (the reference's own PBS scripts add -ffast-math, which only
+# reorders).  Exits 0 without building when the reference tree
+# is absent.
+set -e
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF_DIR="${REF_DIR:-/root/reference}"
+OUT="$HERE/_ref"
+if [ ! -f "$REF_DIR/dynamics.cpp" ]; then
+  echo "build_ref: reference tree not found at $REF_DIR; skipping"
+  exit 0
+fi
+mkdir -p "$OUT"
+CXXFLAGS="-std=gnu++14 -O2 -ffp-contract=off -fno-fast-math -fPIC -shared"
+build() {
+  name="$1"; shift
+  g++ $CXXFLAGS "$@" -I"$HERE/ref_shim" -I"$REF_DIR" "$HERE/ref_driver.cpp" -o "$OUT/$name"
+}
+build libphinum_ref_t0_f64.so -DPHN_REF_THEORY=0 -DPHN_REF_PRECISION=0 &
+build libphinum_ref_t1_f64.so -DPHN_REF_THEORY=1 -DPHN_REF_PRECISION=0 &
+build libphinum_ref_t0_f32.so -DPHN_REF_THEORY=0 -DPHN_REF_PRECISION=-1 &
+wait
+ls -1 "$OUT"

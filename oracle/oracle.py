@@ -1,0 +1,332 @@
+"""ctypes front end of the CPU oracle (phinum_oracle.c) and of the reference
+pin (oracle/_ref/libphinum_ref_*.so, built by oracle/build_ref.sh).
+
+TEST INFRASTRUCTURE.  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg import this module.  Arrays are float64 in the reference's
+layout: Nc*N*N*(N+2) values, index Nc*(x + N*y + N*N*z) + a, z-slabs 0 and
+N+1 are ghosts (lattice.cpp:76-78, util.cpp:34-37).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+MAX_NC = 4
+AVG_FIELDS = (["t"] + [f"phi{a}" for a in range(MAX_NC)] + [f"pi{a}" for a in range(MAX_NC)] +
+              ["phi2", "pi2", "phipi", "phi4", "phi6", "energy", "interaction", "charge",
+               "min_phi", "max_phi", "max_abs_phi", "min_pos", "max_pos", "max_abs_pos",
+               "gradient", "reserved0", "reserved1"])
+AVG_LEN = len(AVG_FIELDS)
+AVG = {k: i for i, k in enumerate(AVG_FIELDS)}
+ISLAND_FIELDS = ["index", "size", "volume", "pot_en", "kin_en", "grad_en", "av_phi",
+                 "peak_pos", "peak_value", "seed_pos"]
+ISL = {k: i for i, k in enumerate(ISLAND_FIELDS)}
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+_PD = ctypes.POINTER(ctypes.c_double)
+_PI = ctypes.POINTER(ctypes.c_int)
+
+
+@dataclass
+class Params:
+    """Reference run parameters (parameters.cpp:84-201)."""
+    N: int = 8
+    Nc: int = 1
+    theory: int = 0
+    mass_mode: int = 1
+    lambda_mode: int = -1
+    a: float = 0.25
+    dt: float = 0.08
+    T0: float = 0.0
+    m_sqr: float = 1.0
+    kappa: float = 3.0 ** 0.5
+    h: float = 0.0
+
+
+class _CParams(ctypes.Structure):
+    _fields_ = [("N", _I), ("Nc", _I), ("theory", _I), ("mass_mode", _I), ("lambda_mode", _I),
+                ("pad_", _I), ("a", _D), ("dt", _D), ("T0", _D), ("m_sqr", _D), ("kappa", _D),
+                ("h", _D)]
+
+
+class _CClock(ctypes.Structure):
+    _fields_ = [("tau", _D), ("dtau", _D), ("last_mom", _D), ("last_field", _D),
+                ("steps", _I), ("pad_", _I)]
+
+
+def _cp(p: Params) -> _CParams:
+    return _CParams(p.N, p.Nc, p.theory, p.mass_mode, p.lambda_mode, 0, p.a, p.dt, p.T0,
+                    p.m_sqr, p.kappa, p.h)
+
+
+def _ptr(a: np.ndarray, kind=_PD):
+    return a.ctypes.data_as(kind)
+
+
+def field_len(p: Params) -> int:
+    return p.Nc * p.N * p.N * (p.N + 2)
+
+
+def to_ref_layout(field: np.ndarray, Nc: int = 1) -> np.ndarray:
+    """[Nc][z][y][x] (or [z][y][x]) -> reference layout with ghost slabs."""
+    f = np.asarray(field, dtype=np.float64)
+    if f.ndim == 3:
+        f = f[None]
+    nc, n = f.shape[0], f.shape[1]
+    out = np.zeros((n + 2, n, n, nc))
+    out[1:n + 1] = np.moveaxis(f, 0, -1)
+    out[0] = out[n]
+    out[n + 1] = out[1]
+    return out.reshape(-1)
+
+
+def from_ref_layout(flat: np.ndarray, N: int, Nc: int = 1) -> np.ndarray:
+    """reference layout -> [Nc][z][y][x] interior."""
+    f = np.asarray(flat).reshape(N + 2, N, N, Nc)[1:N + 1]
+    return np.ascontiguousarray(np.moveaxis(f, -1, 0))
+
+
+# ----------------------------------------------------------------- build ---
+def lib_path(fast: bool = False) -> str:
+    return os.path.join(HERE, "libphinum_oracle_fast.so" if fast else "libphinum_oracle.so")
+
+
+def build(force: bool = False) -> None:
+    """Compile phinum_oracle.c twice: an exact build (no fast-math, no FP
+    contraction; the parity checker) and a timing build with the reference's
+    own optimisation flags minus the x86-only ones (run_PC.pbs:1)."""
+    src = os.path.join(HERE, "phinum_oracle.c")
+    variants = [
+        (lib_path(False), ["-O2", "-ffp-contract=off", "-fno-fast-math"]),
+        (lib_path(True), ["-O3", "-ffast-math", "-funroll-all-loops", "-fprefetch-loop-arrays"]),
+    ]
+    procs = []
+    for out, flags in variants:
+        if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
+                os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "phinum_oracle.h"))):
+            continue
+        for omp in (["-fopenmp"], []):
+            cmd = ["gcc", "-std=c99", "-fPIC", "-shared", *flags, *omp, src, "-o", out + ".tmp", "-lm"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode == 0:
+                os.replace(out + ".tmp", out)
+                break
+        else:
+            raise RuntimeError("oracle build failed:\n" + r.stderr)
+    del procs
+
+
+_libs: dict = {}
+
+
+def _load(fast: bool = False):
+    key = "fast" if fast else "exact"
+    if key not in _libs:
+        path = lib_path(fast)
+        if not os.path.exists(path):
+            build()
+        lib = ctypes.CDLL(path)
+        lib.orc_evolve.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock), _PD, _PD, _I, _I]
+        lib.orc_reset.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock)]
+        lib.orc_averages.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock), _PD, _PD, _PD]
+        lib.orc_run_loop.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock), _PD, _PD, _I, _D,
+                                     _PD, _I, _I]
+        lib.orc_run_loop.restype = _I
+        lib.orc_spectrum_bins.argtypes = [ctypes.POINTER(_CParams), _PI, _PD]
+        lib.orc_spectrum.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _PD, _PD, _PD, _PI]
+        lib.orc_spectrum.restype = _I
+        lib.orc_spectrum_columns.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _PD, _PI, _I, _PD]
+        lib.orc_islands.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _D, _I, _I, _PI, _PD, _I]
+        lib.orc_islands.restype = _I
+        lib.orc_site_energy.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, ctypes.c_long, _I, _I, _I]
+        lib.orc_site_energy.restype = _D
+        lib.orc_max_threads.restype = _I
+        _libs[key] = lib
+    return _libs[key]
+
+
+class Clock:
+    """numeric:: time keeping (tau, dtau, last kick/drift times, steps)."""
+
+    def __init__(self, p: Params, fast: bool = False):
+        self.p, self._c, self.fast = p, _CClock(), fast
+        _load(fast).orc_reset(ctypes.byref(_cp(p)), ctypes.byref(self._c))
+
+    @property
+    def tau(self) -> float:
+        return self._c.tau
+
+    @property
+    def steps(self) -> int:
+        return self._c.steps
+
+
+def max_threads(fast: bool = True) -> int:
+    return int(_load(fast).orc_max_threads())
+
+
+def evolve(p: Params, phi: np.ndarray, pi: np.ndarray, nsteps: int, clock: Clock | None = None,
+           nthreads: int = 1, fast: bool = False) -> Clock:
+    """n x evolve() in place on reference-layout float64 arrays."""
+    assert phi.dtype == np.float64 and pi.dtype == np.float64 and phi.flags.c_contiguous
+    assert phi.size == field_len(p) and pi.size == field_len(p)
+    clock = clock or Clock(p, fast)
+    _load(fast).orc_evolve(ctypes.byref(_cp(p)), ctypes.byref(clock._c), _ptr(phi), _ptr(pi),
+                           int(nsteps), int(nthreads))
+    return clock
+
+
+def averages(p: Params, phi: np.ndarray, pi: np.ndarray, clock: Clock | None = None) -> np.ndarray:
+    out = np.zeros(AVG_LEN)
+    _load().orc_averages(ctypes.byref(_cp(p)), ctypes.byref(clock._c) if clock else None, _ptr(phi),
+                         _ptr(pi), _ptr(out))
+    return out
+
+
+def run_loop(p: Params, phi: np.ndarray, pi: np.ndarray, nsteps: int, tso: float,
+             max_rows: int = 10000, nthreads: int = 1):
+    clock = Clock(p)
+    rows = np.zeros((max_rows, AVG_LEN))
+    n = _load().orc_run_loop(ctypes.byref(_cp(p)), ctypes.byref(clock._c), _ptr(phi), _ptr(pi),
+                             int(nsteps), float(tso), _ptr(rows), max_rows, int(nthreads))
+    return rows[:n], clock
+
+
+def spectrum_bins(p: Params):
+    nb, bs = _I(), _D()
+    _load().orc_spectrum_bins(ctypes.byref(_cp(p)), ctypes.byref(nb), ctypes.byref(bs))
+    return nb.value, bs.value
+
+
+def spectrum(p: Params, phi: np.ndarray, pi: np.ndarray):
+    nb, _ = spectrum_bins(p)
+    F, K, Q = (np.zeros(nb * p.Nc) for _ in range(3))
+    C = np.zeros(nb, dtype=np.int32)
+    r = _load().orc_spectrum(ctypes.byref(_cp(p)), _ptr(phi), _ptr(pi), _ptr(F), _ptr(K), _ptr(Q),
+                             _ptr(C, _PI))
+    if r < 0:
+        raise RuntimeError("bin array too small")
+    return F, K, Q, C
+
+
+def spectrum_columns(p: Params, F, K, Q, C) -> np.ndarray:
+    nb = C.size
+    cols = np.zeros((nb, 7))
+    _load().orc_spectrum_columns(ctypes.byref(_cp(p)), _ptr(F), _ptr(K), _ptr(Q),
+                                 _ptr(np.ascontiguousarray(C, dtype=np.int32), _PI), nb, _ptr(cols))
+    return cols
+
+
+def site_energy(p: Params, phi: np.ndarray, pi: np.ndarray) -> np.ndarray:
+    """rho(x) for every interior site, [z][y][x] (slow; small lattices only)."""
+    N = p.N
+    out = np.zeros((N, N, N))
+    lib = _load()
+    cp = ctypes.byref(_cp(p))
+    for z in range(N):
+        for y in range(N):
+            for x in range(N):
+                K = p.Nc * (x + N * y + N * N * (z + 1))
+                out[z, y, x] = lib.orc_site_energy(cp, _ptr(phi), _ptr(pi), K, x, y, z + 1)
+    return out
+
+
+def islands(p: Params, phi: np.ndarray, pi: np.ndarray, thres: float, mode: int = 0, zper: int = 0,
+            max_islands: int = 1 << 20):
+    """Returns (labels in reference layout, island records [n][10])."""
+    labels = np.zeros(field_len(p), dtype=np.int32)
+    recs = np.zeros((max_islands, len(ISLAND_FIELDS)))
+    n = _load().orc_islands(ctypes.byref(_cp(p)), _ptr(phi), _ptr(pi), float(thres), int(mode),
+                            int(zper), _ptr(labels, _PI), _ptr(recs), max_islands)
+    if n < 0:
+        raise MemoryError("oracle islands: allocation failed")
+    return labels, recs[:min(n, max_islands)]
+
+
+# ------------------------------------------------------ the reference pin ---
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def ref_path(theory: int = 0, precision: str = "f64") -> str:
+    return os.path.join(REF_DIR, f"libphinum_ref_t{theory}_{precision}.so")
+
+
+def ref_available(theory: int = 0, precision: str = "f64") -> bool:
+    return os.path.exists(ref_path(theory, precision))
+
+
+class Reference:
+    """The reference's own sources (single rank, shims) behind ctypes.  One
+    instance per process and variant: the reference keeps global state."""
+
+    def __init__(self, p: Params, precision: str = "f64"):
+        self.p = p
+        lib = ctypes.CDLL(ref_path(p.theory, precision))
+        lib.ref_init.argtypes = [_I, _I, _D, _D, _D, _I, _D, _I, _D, _D, _D]
+        lib.ref_init.restype = _I
+        lib.ref_set_fields.argtypes = [_PD, _PD]
+        lib.ref_get_fields.argtypes = [_PD, _PD]
+        lib.ref_evolve.argtypes = [_I]
+        lib.ref_time.argtypes = [_PD, _PI]
+        lib.ref_averages.argtypes = [_PD]
+        lib.ref_run_loop.argtypes = [_I, _D, _PD, _I]
+        lib.ref_run_loop.restype = _I
+        lib.ref_binsize.restype = _D
+        lib.ref_spectrum.argtypes = [_PD, _PD, _PD, _PI]
+        lib.ref_islands.argtypes = [_D, _PI, _PD, _I]
+        lib.ref_islands.restype = _I
+        self.lib = lib
+        r = lib.ref_init(p.N, p.Nc, p.a, p.dt, p.T0, p.mass_mode, p.m_sqr, p.lambda_mode, 1.0,
+                         p.kappa, p.h)
+        if r != 0:
+            raise RuntimeError(f"ref_init failed ({r}); one Reference per process")
+
+    def set_fields(self, phi, pi):
+        self.lib.ref_set_fields(_ptr(np.ascontiguousarray(phi, np.float64)),
+                                _ptr(np.ascontiguousarray(pi, np.float64)))
+
+    def get_fields(self):
+        n = field_len(self.p)
+        phi, pi = np.zeros(n), np.zeros(n)
+        self.lib.ref_get_fields(_ptr(phi), _ptr(pi))
+        return phi, pi
+
+    def reset(self):
+        self.lib.ref_reset()
+
+    def evolve(self, n: int):
+        self.lib.ref_evolve(int(n))
+
+    def time(self):
+        t, s = _D(), _I()
+        self.lib.ref_time(ctypes.byref(t), ctypes.byref(s))
+        return t.value, s.value
+
+    def averages(self) -> np.ndarray:
+        out = np.zeros(AVG_LEN)
+        self.lib.ref_averages(_ptr(out))
+        return out
+
+    def run_loop(self, nsteps: int, tso: float, max_rows: int = 10000) -> np.ndarray:
+        rows = np.zeros((max_rows, AVG_LEN))
+        n = self.lib.ref_run_loop(int(nsteps), float(tso), _ptr(rows), max_rows)
+        return rows[:n]
+
+    def spectrum(self):
+        nb = self.lib.ref_nbins()
+        F, K, Q = (np.zeros(nb * self.p.Nc) for _ in range(3))
+        C = np.zeros(nb, dtype=np.int32)
+        self.lib.ref_spectrum(_ptr(F), _ptr(K), _ptr(Q), _ptr(C, _PI))
+        return F, K, Q, C
+
+    def islands(self, thres: float, max_islands: int = 1 << 16):
+        labels = np.zeros(field_len(self.p), dtype=np.int32)
+        stats = np.zeros((max_islands, 8))
+        n = self.lib.ref_islands(float(thres), _ptr(labels, _PI), _ptr(stats), max_islands)
+        return labels, stats[:min(n, max_islands)]

@@ -1,0 +1,581 @@
+/*
+ * phinum_oracle.c -- CPU restatement of PhiNum's lattice hot path.
+ *
+ * TEST INFRASTRUCTURE.  This file is the oracle that the GPU path is checked
+ * against: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg (and its `--impl reference` arm) load it.  The product never links it
+ * and never falls back to it.
+ *
+ * It restates, in plain C and in the reference's own operation order, the
+ * functions on the path:
+ *   orc_evolve           reset()/evolve()/updateMomenta()/updateFields()/
+ *                        Communication::exchange()   dynamics.cpp:28-237,
+ *                                                     comm.cpp:63-78
+ *   orc_averages         CalculateExtrema() + CalculateVolumeAverages()
+ *                                                     fieldanalysis.cpp:319-699
+ *   orc_run_loop         main.cpp:685-699 with Print_AveragesExtrema()'s TSO
+ *                        cadence                      fieldanalysis.cpp:748-782
+ *   orc_spectrum         MomentumSpace::init/InitBCounts/
+ *                        Calculate_CorrelationFunctions, fftXtoP_direct
+ *                                                     momentumspace.cpp:32-278,
+ *                                                     clusterfft.cpp:185-225
+ *   orc_islands          is_island()/BFS()/Full_Analysis() scan
+ *                                                     islands.cpp:72-279,778-840
+ * for theories 0 (phi^4 + phi^6) and 1 (phi^4 + linear h), static box, one
+ * rank (z-slab count 1), Nc components interleaved innermost.
+ *
+ * Parity pin: the FP64 results are bit-identical to the reference's own
+ * sources compiled by oracle/build_ref.sh (checked against the committed
+ * fixtures in tests/golden/), provided this file is compiled without
+ * -ffast-math and with -ffp-contract=off (GCC contracts a*b+c into FMA by
+ * default on AArch64).  The spectrum uses this file's own FFT, so spectra
+ * agree with the reference to rounding, and bin counts exactly.
+ *
+ * Layout (util.cpp:34-37, lattice.cpp:76-78): a field holds
+ * Nc*N*N*(N+2) doubles, index Nc*(x + N*y + N*N*z) + a, z-slabs 0 and N+1
+ * are ghosts that mirror slabs N and 1.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "phinum_oracle.h"
+
+/* ---------------------------------------------------------------- helpers */
+static inline double sqr(double x) { return x * x; }              /* util.cpp:20-23 */
+static inline int mod(int i, int n) { return i >= 0 ? i % n : (n + i) % n; } /* util.cpp:12-18 */
+static inline long pos3(const orc_params *p, int x, int y, int z) {          /* util.cpp:34-37 */
+  return (long)p->Nc * x + (long)p->Nc * p->N * y + (long)p->Nc * p->N * p->N * z;
+}
+static inline long field_len(const orc_params *p) { return (long)p->Nc * p->N * p->N * (p->N + 2); }
+
+int orc_version(void) { return 3; }
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------ time keeping */
+/* reset(): dynamics.cpp:28-50 (static box). */
+void orc_reset(const orc_params *p, orc_clock *c) {
+  c->tau = p->T0;
+  c->dtau = p->dt * p->a;
+  c->last_mom = c->tau;
+  c->last_field = c->tau;
+  c->steps = 0;
+}
+
+/* Communication::exchange() with one rank: comm.cpp:63-78. */
+void orc_exchange(const orc_params *p, double *f) {
+  const long slab = (long)p->Nc * p->N * p->N;
+  memcpy(f + (long)(p->N + 1) * slab, f + slab, (size_t)slab * sizeof(double));
+  memcpy(f, f + (long)p->N * slab, (size_t)slab * sizeof(double));
+}
+
+/* updateMomenta(): dynamics.cpp:52-175 for theory 0 (:82-87) and 1 (:96-101),
+ * slabs z in [z0, z1). */
+static void update_momenta_slabs(const orc_params *p, const double *Phi, double *Pi,
+                                 double factor, int z0, int z1) {
+  const int N = p->N, Nc = p->Nc;
+  const double mass = p->m_sqr; /* BareM_sqr_long == BareM_sqr_trans == M_sqr (renormalization.cpp:8-9) */
+  for (int z = z0; z < z1; z++) {
+    long Kooo = pos3(p, 0, 0, z);
+    for (int y = 0; y < N; y++)
+      for (int x = 0; x < N; x++) {
+        double locPhiSqr = 0.0;
+        for (int a = 0; a < Nc; a++) locPhiSqr += sqr(Phi[Kooo + a]);
+        long Kuoo = pos3(p, mod(x + 1, N), y, z);
+        long Kouo = pos3(p, x, mod(y + 1, N), z);
+        long Koou = pos3(p, x, y, z + 1);
+        long Kdoo = pos3(p, mod(x - 1, N), y, z);
+        long Kodo = pos3(p, x, mod(y - 1, N), z);
+        long Kood = pos3(p, x, y, z - 1);
+        for (int a = 0; a < Nc; a++) {
+          double LapPhi = (Phi[Kuoo] + Phi[Kdoo] + Phi[Kouo] + Phi[Kodo] + Phi[Koou] + Phi[Kood] -
+                           6. * Phi[Kooo]) / sqr(p->a);
+          if (p->theory == 0) {
+            Pi[Kooo] += (LapPhi - ((double)p->mass_mode * mass +
+                                   (double)p->lambda_mode * (locPhiSqr / (6. * Nc)) +
+                                   (sqr(locPhiSqr / p->kappa) / (120. * Nc * Nc))) * Phi[Kooo]) * factor;
+          } else {
+            if (a == 0)
+              Pi[Kooo] += (LapPhi - p->h - ((double)p->mass_mode * mass +
+                                            (double)p->lambda_mode * (locPhiSqr / (6. * Nc))) * Phi[Kooo]) * factor;
+            else
+              Pi[Kooo] += (LapPhi - ((double)p->mass_mode * mass +
+                                     (double)p->lambda_mode * (locPhiSqr / (6. * Nc))) * Phi[Kooo]) * factor;
+          }
+          Kooo++; Kuoo++; Kouo++; Koou++; Kdoo++; Kodo++; Kood++;
+        }
+      }
+  }
+}
+
+/* evolve(): dynamics.cpp:196-237 (regime 0), nsteps times.  nthreads > 1
+ * splits the z-slabs over threads like `mpirun -np K` splits them over ranks;
+ * every site sees the same operations, so the result does not depend on it. */
+void orc_evolve(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int nsteps, int nthreads) {
+  const int N = p->N;
+  const long begin = pos3(p, 0, 0, 1), end = (long)p->Nc * N * N * (N + 1);
+  if (nthreads < 1) nthreads = 1;
+  for (int s = 0; s < nsteps; s++) {
+    c->tau += 0.5 * c->dtau;
+    const double fk = c->tau - c->last_mom;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+    for (int z = 1; z < N + 1; z++) update_momenta_slabs(p, Phi, Pi, fk, z, z + 1);
+    c->last_mom = c->tau;
+    c->tau += 0.5 * c->dtau;
+    const double fd = c->tau - c->last_field;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+    for (long K = begin; K < end; K++) Phi[K] += Pi[K] * fd; /* updateFields, dynamics.cpp:182-183 */
+    c->last_field = c->tau;
+    orc_exchange(p, Phi);
+    c->steps++;
+  }
+}
+
+/* ---------------------------------------------------------------- averages */
+/* CalculateExtrema(): fieldanalysis.cpp:319-397 (one rank). */
+static void extrema(const orc_params *p, const double *Phi, orc_row *o) {
+  const int Nc = p->Nc, N = p->N;
+  double maxPhi = -10000000.0, minPhi = 10000000.0, maxAbsPhi = 0.0;
+  long maxpos = -1, minpos = -1, maxAbspos = -1;
+  double AbsPhi = 0.;
+  for (long k = pos3(p, 0, 0, 1); k < (long)Nc * N * N * (N + 1); k++) {
+    AbsPhi += ((Phi[k]) * (Phi[k]));
+    if ((k + 1) % Nc == 0) {
+      AbsPhi = sqrt(AbsPhi);
+      if (AbsPhi > maxAbsPhi) {
+        maxAbsPhi = AbsPhi;
+        maxAbspos = k + 1 - Nc;
+      }
+      AbsPhi = 0;
+    }
+    if (Phi[k] > maxPhi) { maxPhi = Phi[k]; maxpos = k; }
+    if (Phi[k] < minPhi) { minPhi = Phi[k]; minpos = k; }
+  }
+  o->min_phi = minPhi;
+  o->max_phi = maxPhi;
+  o->max_abs_phi = maxAbsPhi;
+  o->min_pos = (double)minpos;
+  o->max_pos = (double)maxpos;
+  o->max_abs_pos = (double)maxAbspos;
+}
+
+/* CalculateVolumeAverages(): fieldanalysis.cpp:399-699, theories 0 and 1,
+ * static box, no charge / energy-density extras.  Also returns the gradient
+ * term GradPhiSqr/vol, which the reference keeps local. */
+static void volume_averages(const orc_params *p, const double *Phi, const double *Pi, orc_row *o) {
+  const int N = p->N, Nc = p->Nc;
+  const int vol = N * N * N;
+  const double mass = p->m_sqr;
+  double phi[ORC_MAX_NC], pi[ORC_MAX_NC];
+  for (int a = 0; a < Nc; a++) { phi[a] = 0.0; pi[a] = 0.0; }
+  double phi2 = 0., pi2 = 0., phi4 = 0., phi6 = 0., phipi = 0.;
+  double Interaction = 0., Charge = 0., Energy;
+  double GradPhiSqr = 0.0;
+  long Kooo = pos3(p, 0, 0, 1);
+  for (int z = 1; z < N + 1; z++)
+    for (int y = 0; y < N; y++)
+      for (int x = 0; x < N; x++) {
+        long Kuoo = pos3(p, mod(x + 1, N), y, z);
+        long Kouo = pos3(p, x, mod(y + 1, N), z);
+        long Koou = pos3(p, x, y, z + 1);
+        double locPhiSqr = 0.0;
+        double locPhi = 0.;
+        for (int a = 0; a < Nc; a++) {
+          phi[a] += Phi[Kooo]; pi[a] += Pi[Kooo];
+          phi2 += sqr(Phi[Kooo]); pi2 += sqr(Pi[Kooo]);
+          phipi += Phi[Kooo] * Pi[Kooo];
+          locPhiSqr += sqr(Phi[Kooo]);
+          locPhi += Phi[Kooo];
+          GradPhiSqr += (sqr(Phi[Kuoo] - Phi[Kooo]) / sqr(p->a) + sqr(Phi[Kouo] - Phi[Kooo]) / sqr(p->a) +
+                         sqr(Phi[Koou] - Phi[Kooo]) / sqr(p->a));
+          if (p->theory == 0) {
+            Interaction += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
+          } else {
+            if (a == 0)
+              Interaction += (p->h * Phi[Kooo] + (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]));
+            else
+              Interaction += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
+          }
+          Kooo++; Kuoo++; Kouo++; Koou++;
+        }
+        (void)locPhi;
+        phi4 += sqr(locPhiSqr);
+        phi6 += sqr(locPhiSqr) * locPhiSqr;
+        if (p->theory == 0)
+          Interaction += (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)) +
+                         (sqr(locPhiSqr) * locPhiSqr / (720.0 * Nc * Nc * p->kappa * p->kappa));
+        else
+          Interaction += (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc));
+      }
+  for (int a = 0; a < Nc; a++) { phi[a] /= (vol); pi[a] /= (vol); }
+  Charge = (0.5 * pi2 - GradPhiSqr / 6. - Interaction);
+  Energy = (0.5 * pi2 + 0.5 * GradPhiSqr + Interaction);
+  Energy /= (vol);
+  Interaction /= (vol);
+  Charge /= (vol);
+  phi2 /= (vol); pi2 /= (vol);
+  phi4 /= (vol);
+  phi6 /= (vol);
+  phipi /= (vol);
+  /* MPI_Reduce + "/nodes" with one rank (fieldanalysis.cpp:658-685) is the identity */
+  for (int a = 0; a < ORC_MAX_NC; a++) {
+    o->phi[a] = a < Nc ? phi[a] : 0.0;
+    o->pi[a] = a < Nc ? pi[a] : 0.0;
+  }
+  o->phi2 = phi2; o->pi2 = pi2; o->phipi = phipi; o->phi4 = phi4; o->phi6 = phi6;
+  o->energy = Energy; o->interaction = Interaction; o->charge = Charge;
+  o->gradient = GradPhiSqr / (vol);
+}
+
+void orc_averages(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, orc_row *o) {
+  memset(o, 0, sizeof(*o));
+  o->t = c ? c->tau : 0.0;
+  extrema(p, Phi, o);
+  volume_averages(p, Phi, Pi, o);
+}
+
+/* main.cpp:685-699 with an explicit step count; Print_AveragesExtrema()'s
+ * cadence (fieldanalysis.cpp:753-780): a row at step 0, then whenever
+ * tau >= LastSO + TSO, where LastSO advances by TSO.  Rows are stamped with
+ * LastSO, the time the reference prints.  Returns the number of rows. */
+int orc_run_loop(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int nsteps, double tso,
+                 orc_row *rows, int max_rows, int nthreads) {
+  int nrows = 0;
+  double last_so = 0.0;
+  orc_reset(p, c);
+  for (int count = 0; count < nsteps; count++) {
+    int due = 0;
+    if (c->steps == 0) {
+      last_so = c->tau;
+      due = 1;
+    } else if (!(c->tau < last_so + tso)) {
+      if (c->tau >= last_so + tso) last_so += tso;
+      due = 1;
+    }
+    if (due && nrows < max_rows) {
+      orc_averages(p, c, Phi, Pi, &rows[nrows]);
+      rows[nrows].t = last_so;
+      nrows++;
+    }
+    orc_evolve(p, c, Phi, Pi, 1, nthreads);
+  }
+  return nrows;
+}
+
+/* ---------------------------------------------------------------- spectrum */
+/* MomentumSpace::init (momentumspace.cpp:32-47): bin width and count. */
+void orc_spectrum_bins(const orc_params *p, int *nbins, double *binsize) {
+  double pTmin = (2.0 / (p->a)) * sin(acos(-1.) / p->N);
+  double pTmax = sqrt(3.0 * (4.0 / sqr(p->a)));
+  *binsize = pTmin;
+  *nbins = (int)(pTmax / pTmin + 0.5) + 2;
+}
+
+/* Lattice momentum along one axis for index n (momentumspace.cpp:222-235,
+ * the halved axis at :244 uses the positive branch only). */
+static double lattice_p(int n, int N, double a) {
+  if (n < N / 2 + 1) return 2.0 / (a) * sin(n * acos(-1.) / N);
+  return -2.0 / (a) * sin(n * acos(-1.) / N);
+}
+
+/* In-place complex DFT of length n with stride; radix-2 when n is a power of
+ * two, direct sum otherwise.  sign = -1 is the forward transform. */
+static void dft_line(double *re, double *im, int n, long stride, double *wr, double *wi) {
+  if (n <= 1) return;
+  const double two_pi = 6.283185307179586476925286766559;
+  if ((n & (n - 1)) == 0) {
+    for (int i = 1, j = 0; i < n; i++) {
+      int bit = n >> 1;
+      for (; j & bit; bit >>= 1) j ^= bit;
+      j ^= bit;
+      if (i < j) {
+        double t = re[i * stride]; re[i * stride] = re[j * stride]; re[j * stride] = t;
+        t = im[i * stride]; im[i * stride] = im[j * stride]; im[j * stride] = t;
+      }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+      int half = len >> 1;
+      for (int k = 0; k < half; k++) {
+        double ang = two_pi * (double)k / (double)len;
+        double cr = cos(ang), ci = -sin(ang);
+        for (int s = 0; s < n; s += len) {
+          long i0 = (long)(s + k) * stride, i1 = (long)(s + k + half) * stride;
+          double br = re[i1] * cr - im[i1] * ci;
+          double bi = re[i1] * ci + im[i1] * cr;
+          re[i1] = re[i0] - br; im[i1] = im[i0] - bi;
+          re[i0] += br; im[i0] += bi;
+        }
+      }
+    }
+    return;
+  }
+  for (int k = 0; k < n; k++) {
+    double sr = 0, si = 0;
+    for (int j = 0; j < n; j++) {
+      double ang = two_pi * (double)((long)k * j % n) / (double)n;
+      double cr = cos(ang), ci = -sin(ang);
+      sr += re[j * stride] * cr - im[j * stride] * ci;
+      si += re[j * stride] * ci + im[j * stride] * cr;
+    }
+    wr[k] = sr; wi[k] = si;
+  }
+  for (int k = 0; k < n; k++) { re[k * stride] = wr[k]; im[k * stride] = wi[k]; }
+}
+
+/* 3-D forward DFT of component `comp` of a field, scaled by a^3
+ * (fftXtoP_direct, clusterfft.cpp:185-225).  Output is the full complex
+ * spectrum, index kx + N*ky + N*N*kz. */
+static void forward_fft(const orc_params *p, const double *f, int comp, double *re, double *im) {
+  const int N = p->N;
+  const long NN = (long)N * N;
+  double *wr = (double *)malloc(sizeof(double) * N), *wi = (double *)malloc(sizeof(double) * N);
+  for (int z = 0; z < N; z++)
+    for (int y = 0; y < N; y++)
+      for (int x = 0; x < N; x++) {
+        re[x + N * y + NN * z] = f[comp + pos3(p, x, y, z + 1)];
+        im[x + N * y + NN * z] = 0.0;
+      }
+  for (long r = 0; r < NN; r++) dft_line(re + r * N, im + r * N, N, 1, wr, wi);
+  for (int z = 0; z < N; z++)
+    for (int x = 0; x < N; x++) dft_line(re + x + NN * z, im + x + NN * z, N, N, wr, wi);
+  for (long r = 0; r < NN; r++) dft_line(re + r, im + r, N, NN, wr, wi);
+  const double factor = (sqr(p->a) * p->a);
+  for (long i = 0; i < NN * N; i++) { re[i] *= factor; im[i] *= factor; }
+  free(wr); free(wi);
+}
+
+/* InitBCounts + Calculate_CorrelationFunctions (momentumspace.cpp:89-278):
+ * F/K/Q[bin*Nc + a] = sum over modes px, pz in [0,N), py in [0,N/2] of
+ * |Phi_p|^2, |Pi_p|^2, Re(Phi_p conj Pi_p), each counted twice unless py is 0
+ * or N/2; counts[bin] likewise.  py runs over lattice y (the reference's
+ * transposed FFT input puts y on the halved axis, clusterfft.cpp:198). */
+int orc_spectrum(const orc_params *p, const double *Phi, const double *Pi, double *F, double *K, double *Q,
+                 int *counts) {
+  const int N = p->N, Nc = p->Nc;
+  int nb;
+  double binsize;
+  orc_spectrum_bins(p, &nb, &binsize);
+  const long NN = (long)N * N, V = NN * N;
+  for (int k = 0; k < nb * Nc; k++) { F[k] = 0.; K[k] = 0.; Q[k] = 0.; }
+  for (int k = 0; k < nb; k++) counts[k] = 0;
+  double *fr = (double *)malloc(sizeof(double) * V), *fi = (double *)malloc(sizeof(double) * V);
+  double *gr = (double *)malloc(sizeof(double) * V), *gi = (double *)malloc(sizeof(double) * V);
+  int bad = 0;
+  for (int a = 0; a < Nc; a++) {
+    forward_fft(p, Phi, a, fr, fi);
+    forward_fft(p, Pi, a, gr, gi);
+    for (int pz = 0; pz < N; pz++) {
+      double nu = (pz == 0) ? 0 : lattice_p(pz, N, p->a);
+      for (int px = 0; px < N; px++) {
+        double ppx = lattice_p(px, N, p->a);
+        for (int py = 0; py < N / 2 + 1; py++) {
+          double ppy = 2.0 / (p->a) * sin(py * acos(-1.) / N);
+          double psqr = sqr(ppx) + sqr(ppy) + sqr(nu);
+          int bin = (int)(sqrt(psqr) / binsize + 0.5);
+          if (bin >= nb) { bad = 1; continue; }
+          long m = px + (long)N * py + NN * pz;
+          double af = hypot(fr[m], fi[m]), ak = hypot(gr[m], gi[m]);
+          double q = fr[m] * gr[m] + fi[m] * gi[m];
+          int w = (py != 0 && py != N / 2) ? 2 : 1;
+          for (int r = 0; r < w; r++) {
+            F[bin * Nc + a] += sqr(af);
+            K[bin * Nc + a] += sqr(ak);
+            Q[bin * Nc + a] += q;
+            if (a == 0) counts[bin]++;
+          }
+        }
+      }
+    }
+  }
+  free(fr); free(fi); free(gr); free(gi);
+  return bad ? -1 : nb;
+}
+
+/* Print_fp (momentumspace.cpp:280-384) per-bin columns, for bins with a
+ * non-zero count and F: p, count, omega, F/(L^3 count), K/(L^3 count),
+ * sqrt(FK)/(L^3 count), F p^3 /(2 pi^2 L^3 count).  cols[k*7 + ...]; rows of
+ * skipped bins are zero with count 0.  Components are averaged as :471-474. */
+void orc_spectrum_columns(const orc_params *p, const double *F, const double *K, const double *Q,
+                          const int *counts, int nb, double *cols) {
+  const int N = p->N, Nc = p->Nc;
+  double binsize;
+  int nbb;
+  orc_spectrum_bins(p, &nbb, &binsize);
+  double NormCorr = 1. / (sqr(N * p->a) * N * p->a);
+  for (int k = 0; k < nb; k++) {
+    double *c = cols + (long)k * 7;
+    for (int j = 0; j < 7; j++) c[j] = 0.0;
+    double norm2 = (counts[k] == 0 ? 0 : 1 / (double)(counts[k]));
+    double pabs = binsize * k;
+    if (norm2 != 0 && F[k * Nc] != 0) {
+      double FF = 0, KK = 0, QQ = 0;
+      for (int a = 0; a < Nc; a++) { FF += F[k * Nc + a]; KK += K[k * Nc + a]; QQ += Q[k * Nc + a]; }
+      FF /= Nc; KK /= Nc; QQ /= Nc;
+      (void)QQ;
+      c[0] = pabs;
+      c[1] = counts[k];
+      c[2] = sqrt(KK / FF);
+      c[3] = FF * NormCorr * norm2;
+      c[4] = KK * NormCorr * norm2;
+      c[5] = sqrt(FF * KK) * NormCorr * norm2;
+      c[6] = FF * NormCorr * norm2 * pabs * pabs * pabs / 2. / acos(-1.) / acos(-1.);
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ islands */
+/* Per-site energy density, the summand of the reference's Energy
+ * (fieldanalysis.cpp:437-471,571-579): 1/2 sum_a pi_a^2 + 1/2 sum_a grad_a
+ * + V.  Its lattice mean is the reference's Energy. */
+double orc_site_energy(const orc_params *p, const double *Phi, const double *Pi, long Kooo0, int x, int y, int z) {
+  const int N = p->N, Nc = p->Nc;
+  const double mass = p->m_sqr;
+  long Kooo = Kooo0;
+  long Kuoo = pos3(p, mod(x + 1, N), y, z), Kouo = pos3(p, x, mod(y + 1, N), z), Koou = pos3(p, x, y, z + 1);
+  double kin = 0., grad = 0., inter = 0., locPhiSqr = 0.;
+  for (int a = 0; a < Nc; a++) {
+    kin += sqr(Pi[Kooo]);
+    locPhiSqr += sqr(Phi[Kooo]);
+    grad += (sqr(Phi[Kuoo] - Phi[Kooo]) / sqr(p->a) + sqr(Phi[Kouo] - Phi[Kooo]) / sqr(p->a) +
+             sqr(Phi[Koou] - Phi[Kooo]) / sqr(p->a));
+    if (p->theory == 0)
+      inter += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
+    else if (a == 0)
+      inter += (p->h * Phi[Kooo] + (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]));
+    else
+      inter += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
+    Kooo++; Kuoo++; Kouo++; Koou++;
+  }
+  if (p->theory == 0)
+    inter += (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)) +
+             (sqr(locPhiSqr) * locPhiSqr / (720.0 * Nc * Nc * p->kappa * p->kappa));
+  else
+    inter += (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc));
+  return 0.5 * kin + 0.5 * grad + inter;
+}
+
+/* Mask: mode 0 is is_island() (islands.cpp:76): the first component at the
+ * site satisfies Phi^2/2 + Pi^2/2 > thres^2/2; mode 1 is the energy-density
+ * mask rho(x) > thres. */
+static unsigned char *make_mask(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode) {
+  const int N = p->N;
+  const long n = field_len(p);
+  unsigned char *m = (unsigned char *)calloc((size_t)n, 1);
+  for (int z = 1; z < N + 1; z++)
+    for (int y = 0; y < N; y++)
+      for (int x = 0; x < N; x++) {
+        long K = pos3(p, x, y, z);
+        if (mode == 0)
+          m[K] = (Phi[K] * Phi[K] * 0.5 + Pi[K] * Pi[K] * 0.5 > thres * thres * 0.5);
+        else
+          m[K] = orc_site_energy(p, Phi, Pi, K, x, y, z) > thres;
+      }
+  return m;
+}
+
+/* One BFS (islands.cpp:90-279, theory 0/1, static box) from seed P with label
+ * `flag`.  z is open (1..N) as on one rank (:224-236) unless zper. */
+static void bfs(const orc_params *p, const double *Phi, const double *Pi, const unsigned char *mask, int *b,
+                long *queue, long P, int flag, int zper, orc_island *B) {
+  const int N = p->N, Nc = p->Nc;
+  const double mass = p->m_sqr;
+  int NN = 0;
+  double cPotEn = 0., cGradEn = 0., cKinEn = 0., cavPhi = 0.;
+  long cnt = P;
+  long head = 0, tail = 0;
+  b[P] = flag;
+  queue[tail++] = P;
+  while (head < tail) {
+    long Kooo = queue[head++];
+    if (Phi[Kooo] * Phi[Kooo] > Phi[cnt] * Phi[cnt]) cnt = Kooo;
+    int z = (int)(Kooo / ((long)Nc * N * N));
+    int y = (int)((Kooo - (long)Nc * N * N * z) / ((long)Nc * N));
+    int x = (int)((Kooo - (long)Nc * N * N * z - (long)Nc * N * y) / Nc);
+    long Kuoo = pos3(p, mod(x + 1, N), y, z);
+    long Kdoo = pos3(p, mod(x - 1, N), y, z);
+    long Kouo = pos3(p, x, mod(y + 1, N), z);
+    long Kodo = pos3(p, x, mod(y - 1, N), z);
+    long Koou = pos3(p, x, y, z + 1);
+    long Kood = pos3(p, x, y, z - 1);
+    NN++;
+    cGradEn += 0.5 * (sqr(Phi[Kuoo] - Phi[Kooo]) + sqr(Phi[Kouo] - Phi[Kooo]) + sqr(Phi[Koou] - Phi[Kooo])) / sqr(p->a);
+    cKinEn += 0.5 * sqr(Pi[Kooo]);
+    if (p->theory == 0)
+      cPotEn += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]) +
+                (double)(p->lambda_mode) * (sqr(sqr(Phi[Kooo])) / (24.0 * Nc)) +
+                (sqr(sqr(Phi[Kooo])) * sqr(Phi[Kooo]) / (720.0 * Nc * Nc * p->kappa * p->kappa));
+    else
+      cPotEn += (p->h * Phi[Kooo] + (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]) +
+                 (double)(p->lambda_mode) * (sqr(sqr(Phi[Kooo])) / (24.0 * Nc)));
+    cavPhi += Phi[Kooo];
+    if (mask[Kuoo] && b[Kuoo] == -1) { b[Kuoo] = flag; queue[tail++] = Kuoo; }
+    if (mask[Kdoo] && b[Kdoo] == -1) { b[Kdoo] = flag; queue[tail++] = Kdoo; }
+    if (mask[Kouo] && b[Kouo] == -1) { b[Kouo] = flag; queue[tail++] = Kouo; }
+    if (mask[Kodo] && b[Kodo] == -1) { b[Kodo] = flag; queue[tail++] = Kodo; }
+    if (zper) {
+      long Kp = pos3(p, x, y, z == N ? 1 : z + 1), Km = pos3(p, x, y, z == 1 ? N : z - 1);
+      if (mask[Kp] && b[Kp] == -1) { b[Kp] = flag; queue[tail++] = Kp; }
+      if (mask[Km] && b[Km] == -1) { b[Km] = flag; queue[tail++] = Km; }
+    } else {
+      if (z < N)
+        if (mask[Koou] && b[Koou] == -1) { b[Koou] = flag; queue[tail++] = Koou; }
+      if (z > 1)
+        if (mask[Kood] && b[Kood] == -1) { b[Kood] = flag; queue[tail++] = Kood; }
+    }
+  }
+  cavPhi /= (double)(NN);
+  const double cell = p->a * p->a * p->a;
+  B->index = flag;
+  B->size = NN;
+  B->volume = NN * p->a * p->a * p->a;
+  B->pot_en = cPotEn * cell;
+  B->kin_en = cKinEn * cell;
+  B->grad_en = cGradEn * cell;
+  B->av_phi = cavPhi;
+  B->peak_pos = (double)cnt;
+  B->peak_value = Phi[cnt];
+  B->seed_pos = (double)P;
+}
+
+/* Full_Analysis() from an empty island history (islands.cpp:778-840): labels
+ * reset to -1, then every unlabelled mask site in linear order seeds a BFS.
+ * Island i gets label i, so labels follow each island's smallest site index.
+ * labels (may be NULL) uses the reference layout; islands[] receives at most
+ * max_islands records.  Returns the island count, or -1 on allocation failure. */
+int orc_islands(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode, int zper,
+                int *labels, orc_island *islands, int max_islands) {
+  const int N = p->N, Nc = p->Nc;
+  const long n = field_len(p);
+  unsigned char *mask = make_mask(p, Phi, Pi, thres, mode);
+  int *b = labels ? labels : (int *)malloc(sizeof(int) * (size_t)n);
+  long *queue = (long *)malloc(sizeof(long) * (size_t)n);
+  if (!mask || !b || !queue) return -1;
+  for (long k = 0; k < n; k++) b[k] = -1;
+  int count = 0;
+  orc_island scratch;
+  for (long K = pos3(p, 0, 0, 1); K < (long)Nc * N * N * (N + 1); K++)
+    if (mask[K] && b[K] == -1) {
+      orc_island *B = count < max_islands ? &islands[count] : &scratch;
+      bfs(p, Phi, Pi, mask, b, queue, K, count, zper, B);
+      count++;
+    }
+  free(mask);
+  free(queue);
+  if (!labels) free(b);
+  return count;
+}

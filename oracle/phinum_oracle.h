@@ -1,0 +1,74 @@
+/*
+ * phinum_oracle.h -- CPU restatement of PhiNum's lattice hot path.
+ * TEST INFRASTRUCTURE: see phinum_oracle.c.
+ */
+#ifndef PHINUM_ORACLE_H
+#define PHINUM_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAX_NC 4
+
+/* Run parameters, in the reference's own terms (parameters.cpp:84-201). */
+typedef struct orc_params {
+  int N;           /* N_t = N_eta: cubic lattice edge */
+  int Nc;          /* field components */
+  int theory;      /* 0: phi^4 + phi^6 (Kappa), 1: phi^4 + linear h */
+  int mass_mode;   /* Mass_Mode */
+  int lambda_mode; /* Lambda_Mode */
+  int pad_;
+  double a;        /* a_t = a_eta */
+  double dt;       /* dtBaseTrans: dtau = dt * a */
+  double T0;
+  double m_sqr;    /* M_sqr (= BareM_sqr_long/_trans without tadpole renormalisation) */
+  double kappa;    /* Kappa (theory 0) */
+  double h;        /* h (theory 1) */
+} orc_params;
+
+/* numeric:: and LocalLattice:: time keeping (dynamics.cpp:8-50). */
+typedef struct orc_clock {
+  double tau, dtau, last_mom, last_field;
+  int steps, pad_;
+} orc_clock;
+
+/* One SO row: CalculateVolumeAverages + CalculateExtrema outputs
+ * (lattice.cpp:44-58).  Positions are indices into the reference layout. */
+typedef struct orc_row {
+  double t;
+  double phi[ORC_MAX_NC], pi[ORC_MAX_NC];
+  double phi2, pi2, phipi, phi4, phi6;
+  double energy, interaction, charge;
+  double min_phi, max_phi, max_abs_phi;
+  double min_pos, max_pos, max_abs_pos;
+  double gradient; /* GradPhiSqr / vol: mean of sum_d (forward difference)^2 / a^2 */
+  double reserved[2];
+} orc_row;
+
+/* One island (struct island, islands.cpp:13-28, latest entries). */
+typedef struct orc_island {
+  double index, size, volume, pot_en, kin_en, grad_en, av_phi, peak_pos, peak_value, seed_pos;
+} orc_island;
+
+int orc_version(void);
+int orc_max_threads(void);
+void orc_reset(const orc_params *p, orc_clock *c);
+void orc_exchange(const orc_params *p, double *f);
+void orc_evolve(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int nsteps, int nthreads);
+void orc_averages(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, orc_row *o);
+int orc_run_loop(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int nsteps, double tso,
+                 orc_row *rows, int max_rows, int nthreads);
+void orc_spectrum_bins(const orc_params *p, int *nbins, double *binsize);
+int orc_spectrum(const orc_params *p, const double *Phi, const double *Pi, double *F, double *K, double *Q,
+                 int *counts);
+void orc_spectrum_columns(const orc_params *p, const double *F, const double *K, const double *Q,
+                          const int *counts, int nb, double *cols);
+double orc_site_energy(const orc_params *p, const double *Phi, const double *Pi, long K, int x, int y, int z);
+int orc_islands(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode, int zper,
+                int *labels, orc_island *islands, int max_islands);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

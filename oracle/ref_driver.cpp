@@ -1,0 +1,328 @@
+/*
+ * Oracle pin: PhiNum's own hot-path sources, compiled UNCHANGED from the
+ * reference tree against the single-rank shims in oracle/ref_shim/, behind a
+ * small extern "C" surface that the golden-vector generator
+ * (tests/golden/make_golden.py) drives through ctypes.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The result (oracle/_ref/libphinum_ref_*.so) is
+ * built by oracle/build_ref.sh in a container that holds the reference tree;
+ * it is never shipped, never linked into the product and never timed.
+ *
+ * What this file supplies in place of the reference's main.cpp and
+ * parameters.cpp:
+ *   - the parameter block (parameters.cpp:7-303 declares these names as
+ *     compile-time switches plus globals; the names must match because the
+ *     reference functions use them directly).  `theory` and `doubleprecision`
+ *     come from -DPHN_REF_THEORY / -DPHN_REF_PRECISION so that one recipe
+ *     builds every variant without editing a reference file;
+ *   - the run loop of main.cpp:685-699 with an explicit step count in place
+ *     of `tau < TMax` (an accumulated FP sum), and without the island,
+ *     false-vacuum and spectrum calls, which are exposed separately.
+ */
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <queue>
+#include <vector>
+#include <algorithm>
+#include <sys/stat.h>
+
+#include "mpi.h"
+#include "fftw3-mpi.h"
+
+using namespace std;
+
+/* ---- parameter block (stands in for parameters.cpp) ---------------------- */
+#define _PARAMETERS_CPP_
+
+#ifndef PHN_REF_THEORY
+#define PHN_REF_THEORY 0
+#endif
+#ifndef PHN_REF_PRECISION
+#define PHN_REF_PRECISION 0
+#endif
+
+#define doubleprecision PHN_REF_PRECISION
+#if (doubleprecision == -1)
+#define pseudo_double float
+#define MPI_PSEUDO_DOUBLE MPI_FLOAT
+#define really_double double
+#define p_fftw_complex fftwf_complex
+#define p_fftw_plan fftwf_plan
+#define p_fftw_mpi_init fftwf_mpi_init
+#define p_fftw_mpi_local_size_3d fftwf_mpi_local_size_3d
+#define p_fftw_alloc_real fftwf_alloc_real
+#define p_fftw_alloc_complex fftwf_alloc_complex
+#define p_fftw_mpi_plan_dft_r2c_3d fftwf_mpi_plan_dft_r2c_3d
+#define p_fftw_mpi_plan_dft_c2r_3d fftwf_mpi_plan_dft_c2r_3d
+#define p_fftw_destroy_plan fftwf_destroy_plan
+#define p_fftw_execute fftwf_execute
+#else
+#define pseudo_double double
+#define MPI_PSEUDO_DOUBLE MPI_DOUBLE
+#define really_double double
+#define p_fftw_complex fftw_complex
+#define p_fftw_plan fftw_plan
+#define p_fftw_mpi_init fftw_mpi_init
+#define p_fftw_mpi_local_size_3d fftw_mpi_local_size_3d
+#define p_fftw_alloc_real fftw_alloc_real
+#define p_fftw_alloc_complex fftw_alloc_complex
+#define p_fftw_mpi_plan_dft_r2c_3d fftw_mpi_plan_dft_r2c_3d
+#define p_fftw_mpi_plan_dft_c2r_3d fftw_mpi_plan_dft_c2r_3d
+#define p_fftw_destroy_plan fftw_destroy_plan
+#define p_fftw_execute fftw_execute
+#endif
+
+#define hardscale2 0
+#define EXPANSION 0
+#define withCorr 1
+#define withBins 1
+#define LAMBDA_MODE 1
+#define withcharge 0
+#define expansion 0
+#define finebin 0
+#define withEnergyPS 0
+#define islanddetect 1
+#define EnergybasedID 0
+#define theory PHN_REF_THEORY
+#define adjustDT 0
+#define initialize 3
+
+int runs = 1;
+int runID = 1;
+int nodes = 1;
+int ID = 0;
+
+int Nc = 1;
+int Mass_Mode = 1;
+pseudo_double M_sqr = 1.;
+int Lambda_Mode = -1;
+pseudo_double Lambda = 1.;
+pseudo_double Kappa = 2.;
+pseudo_double h = 0.;
+
+int renorm_tadpole = 0;
+int max_renSteps = 2000;
+pseudo_double tad_precision = 1e-6;
+
+pseudo_double a_t = 0.25;
+int N_t = 8;
+pseudo_double a_eta;
+int N_eta;
+pseudo_double T0 = 0;
+pseudo_double TMax = 1e30;
+pseudo_double TSO = 1.0;
+pseudo_double TMO = 1e30;
+pseudo_double dtBaseTrans = 0.08;
+pseudo_double dtBaseLong = 0.08;
+
+int justnoise = 0;
+pseudo_double QS = 1.;
+pseudo_double scale2 = 1.;
+pseudo_double Amplitude = 0.;
+pseudo_double chi = 1.;
+pseudo_double Noise = 0.5;
+pseudo_double phi0_0 = 0., phi0_1 = 0.;
+pseudo_double pi0_0 = 0., pi0_1 = 0.;
+pseudo_double M2_long = 0., M2_trans = 0.;
+
+int LASTRUN = 0;
+
+/* ---- the reference's own hot-path sources, unchanged ----------------------- */
+#include "lattice.cpp"
+#include "util.cpp"
+#include "comm.cpp"
+#include "dynamics.cpp"
+#include "fieldanalysis.cpp"
+#include "clusterfft.cpp"
+#include "momentumspace.cpp"
+#include "islands.cpp"
+#include "renormalization.cpp"
+
+/* ---- extern "C" surface for the golden-vector generator -------------------- */
+namespace {
+bool g_ready = false;
+size_t field_len() { return (size_t)Nc * N_t * N_t * (LocalLattice::N_eta_loc + 2); }
+}
+
+extern "C" {
+
+/* Layout of the averages record written by ref_averages / ref_run_loop. */
+enum { REF_MAX_NC = 4, REF_AVG_LEN = 1 + 2 * REF_MAX_NC + 14 + 3 };
+
+int ref_precision() { return doubleprecision; }
+int ref_theory() { return theory; }
+
+int ref_init(int N, int nc, double a, double dt, double t0, int mass_mode, double m_sqr,
+             int lambda_mode, double lambda, double kappa, double hlin) {
+  if (g_ready) return -1;
+  if (nc < 1 || nc > REF_MAX_NC) return -2;
+  N_t = N;
+  Nc = nc;
+  a_t = (pseudo_double)a;
+  dtBaseLong = (pseudo_double)dt;
+  T0 = (pseudo_double)t0;
+  Mass_Mode = mass_mode;
+  M_sqr = (pseudo_double)m_sqr;
+  Lambda_Mode = lambda_mode;
+  Lambda = (pseudo_double)lambda;
+  Kappa = (pseudo_double)kappa;
+  h = (pseudo_double)hlin;
+  /* CompleteParameters (parameters.cpp:398-411): cubic box, dt base */
+  a_eta = a_t;
+  N_eta = N_t;
+  dtBaseTrans = dtBaseLong;
+  LocalLattice::init();
+  FFT::init();
+  MomentumSpace::init();
+  island_analysis::init();
+  fix_tadpole();
+  reset();
+  g_ready = true;
+  return 0;
+}
+
+void ref_fin() {
+  if (!g_ready) return;
+  island_analysis::fin();
+  MomentumSpace::fin();
+  FFT::fin();
+  LocalLattice::fin();
+  g_ready = false;
+}
+
+/* Fields in the reference layout Nc*N*N*(N+2) (ghost z-slabs 0 and N+1);
+ * only the interior is read, then the ghosts are filled by exchange(). */
+void ref_set_fields(const double *phi, const double *pi) {
+  const size_t n = field_len();
+  for (size_t k = 0; k < n; ++k) {
+    LocalLattice::Phi[k] = (pseudo_double)phi[k];
+    LocalLattice::Pi[k] = (pseudo_double)pi[k];
+  }
+  Communication::exchange();
+}
+
+void ref_get_fields(double *phi, double *pi) {
+  const size_t n = field_len();
+  for (size_t k = 0; k < n; ++k) {
+    phi[k] = (double)LocalLattice::Phi[k];
+    pi[k] = (double)LocalLattice::Pi[k];
+  }
+}
+
+void ref_reset() { reset(); }
+
+void ref_evolve(int nsteps) {
+  for (int s = 0; s < nsteps; ++s) evolve();
+}
+
+void ref_time(double *tau, int *stepcount) {
+  *tau = (double)LocalLattice::tau;
+  *stepcount = numeric::total_stepcount;
+}
+
+static void record(double t, double *out) {
+  using namespace LocalLattice;
+  int i = 0;
+  out[i++] = t;
+  for (int a = 0; a < REF_MAX_NC; ++a) out[i++] = a < Nc ? (double)avgphi[a] : 0.0;
+  for (int a = 0; a < REF_MAX_NC; ++a) out[i++] = a < Nc ? (double)avgpi[a] : 0.0;
+  out[i++] = avgphi2;
+  out[i++] = avgpi2;
+  out[i++] = avgphipi;
+  out[i++] = avgphi4;
+  out[i++] = avgphi6;
+  out[i++] = avgEnergy;
+  out[i++] = avgInteraction;
+  out[i++] = avgCharge;
+  out[i++] = GlminPhi;
+  out[i++] = GlmaxPhi;
+  out[i++] = GlmaxAbsPhi;
+  out[i++] = (double)minpos;
+  out[i++] = (double)maxpos;
+  out[i++] = (double)maxAbspos;
+  out[i++] = 0.0;
+  out[i++] = 0.0;
+  out[i++] = 0.0;
+}
+
+int ref_avg_len() { return REF_AVG_LEN; }
+
+/* One CalculateExtrema + CalculateVolumeAverages pass on the current state. */
+void ref_averages(double *out) {
+  CalculateExtrema();
+  CalculateVolumeAverages();
+  record((double)LocalLattice::tau, out);
+}
+
+/* main.cpp:685-699 with an explicit step count: before every evolve() the
+ * reference's own Print_AveragesExtrema() decides (TSO cadence on the
+ * accumulated tau) whether to compute a row; each row computed is recorded.
+ * Returns the number of rows written (at most max_rows). */
+int ref_run_loop(int nsteps, double tso, double *rows, int max_rows) {
+  TSO = (pseudo_double)tso;
+  int nrows = 0;
+  int count = 0;
+  for (reset(); count < nsteps; evolve(), ++count) {
+    const bool due = !(numeric::total_stepcount > 0 &&
+                       LocalLattice::tau < numeric::LastSOoutput + TSO);
+    Print_AveragesExtrema();
+    if (due && nrows < max_rows) {
+      record((double)numeric::LastSOoutput, rows + (size_t)nrows * REF_AVG_LEN);
+      ++nrows;
+    }
+  }
+  return nrows;
+}
+
+int ref_nbins() { return MomentumSpace::nTBins; }
+double ref_binsize() { return (double)MomentumSpace::binsizeT; }
+
+/* Calculate_CorrelationFunctions (momentumspace.cpp:140-278) on the current
+ * fields; outputs TotalCorrF/K/Q[bin*Nc + a] and TotalBCounts[bin]. */
+void ref_spectrum(double *F, double *K, double *Q, int *counts) {
+  Calculate_CorrelationFunctions();
+  for (int k = 0; k < MomentumSpace::nTBins * Nc; ++k) {
+    F[k] = (double)MomentumSpace::TotalCorrF[k];
+    K[k] = (double)MomentumSpace::TotalCorrK[k];
+    Q[k] = (double)MomentumSpace::TotalCorrQ[k];
+  }
+  for (int k = 0; k < MomentumSpace::nTBins; ++k) counts[k] = MomentumSpace::TotalBCounts[k];
+}
+
+/* One Full_Analysis (islands.cpp:778-840) from an empty island history with
+ * the given threshold.  labels[] receives the reference's b[] array (the
+ * reference layout, -1 outside islands); stats[i*8 + ...] = index, V, PotEn,
+ * KinEn, GradEn, avPhi, peak position, Peak_value for each island found, in
+ * the reference's found_islands order.  Returns the island count. */
+int ref_islands(double thres, int *labels, double *stats, int max_islands) {
+  using namespace island_analysis;
+  island_analysis::fin();
+  island_analysis::init();
+  island_analysis::thres = (pseudo_double)thres;
+  Full_Analysis();
+  const size_t n = field_len();
+  for (size_t k = 0; k < n; ++k) labels[k] = b[k];
+  const int count = (int)found_islands.size();
+  for (int i = 0; i < count && i < max_islands; ++i) {
+    island &B = found_islands[(size_t)i];
+    double *s = stats + (size_t)i * 8;
+    s[0] = (double)B.index;
+    s[1] = (double)B.V.back();
+    s[2] = (double)B.PotEn.back();
+    s[3] = (double)B.KinEn.back();
+    s[4] = (double)B.GradEn.back();
+    s[5] = (double)B.avPhi.back();
+    s[6] = (double)B.center.back().pos;
+    s[7] = (double)B.Peak_value.back();
+  }
+  return count;
+}
+
+} /* extern "C" */

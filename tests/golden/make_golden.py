@@ -1,0 +1,116 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's OWN
+sources (oracle/_ref, built by oracle/build_ref.sh from the reference tree).
+
+    sh oracle/build_ref.sh && python tests/golden/make_golden.py
+
+Every case runs in a fresh process because the reference keeps its lattice in
+globals.  Inputs come from tests/golden/inputs.py (bit-reproducible on any
+platform), so the fixtures store seeds for the large cases and full arrays only
+for the small ones.  FP64 fields of the large cases are stored as SHA-256
+digests of their little-endian bytes: a bit-exact implementation reproduces
+them exactly.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+SQRT6 = 6.0 ** 0.5
+
+# Reference parameterisation of the two potentials (field rescaled by sqrt(6)):
+#   phi^6:        V = phi^2/2 - phi^4/4 + g phi^6/6, g = 0.1   -> theory 0,
+#                 Mmode=1, M=1, Lmode=-1, Kappa = sqrt(0.3/g) = sqrt(3)
+#   tilted DW:    V = (phi^2-1)^2/4 + eps phi, eps = 0.05       -> theory 1,
+#                 Mmode=-1, M=1, Lmode=1, h = sqrt(6) eps
+PHI6 = dict(theory=0, mass_mode=1, lambda_mode=-1, m_sqr=1.0, kappa=3.0 ** 0.5, h=0.0)
+TDW = dict(theory=1, mass_mode=-1, lambda_mode=1, m_sqr=1.0, kappa=1.0, h=SQRT6 * 0.05)
+
+CASES = {
+    # name: (params, seed, phi0, steps, tso, full arrays?, checkpoints)
+    "t0_n8": (dict(N=8, Nc=1, **PHI6), 1, SQRT6, 100, 0.25, True, (1, 10, 100)),
+    "t1_n8": (dict(N=8, Nc=1, **TDW), 2, -SQRT6, 100, 0.25, True, (1, 10, 100)),
+    "t0_n12": (dict(N=12, Nc=1, **PHI6), 3, SQRT6, 60, 0.3, True, (1, 60)),
+    "t0_n16_nc2": (dict(N=16, Nc=2, **PHI6), 4, SQRT6, 50, 0.25, True, (1, 50)),
+    "t1_n32": (dict(N=32, Nc=1, **TDW), 5, -SQRT6, 500, 1.0, False, (1, 100, 500)),
+    "c0_n64": (dict(N=64, Nc=1, **PHI6), 6, SQRT6, 2000, 1.0, False, (1, 500, 2000)),
+}
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def island_threshold(phi, pi) -> float:
+    """A threshold that puts about 12% of sites in the reference mask."""
+    r = np.sqrt(phi[0] ** 2 + pi[0] ** 2)
+    return float(np.quantile(r, 0.88))
+
+
+def run_case(name: str) -> None:
+    from oracle import oracle as O
+    import inputs
+    pd, seed, phi0, steps, tso, full, checkpoints = CASES[name]
+    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, seed, phi0=phi0)
+    R = O.Reference(p)
+    out = {"params": json.dumps(pd), "seed": seed, "phi0": phi0, "steps": steps, "tso": tso,
+           "a": p.a, "dt": p.dt}
+    if full:
+        out["phi_init"], out["pi_init"] = phi_i, pi_i
+    # SO rows over the whole run (main.cpp:685-699 cadence)
+    R.set_fields(O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc))
+    out["rows"] = R.run_loop(steps, tso)
+    # fields at the checkpoints (fresh start, explicit evolve counts)
+    R.set_fields(O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc))
+    R.reset()
+    done = 0
+    for c in checkpoints:
+        R.evolve(c - done)
+        done = c
+        ph, pp = R.get_fields()
+        phi_c, pi_c = O.from_ref_layout(ph, p.N, p.Nc), O.from_ref_layout(pp, p.N, p.Nc)
+        out[f"phi_sha_{c}"] = digest(phi_c)
+        out[f"pi_sha_{c}"] = digest(pi_c)
+        out[f"avg_{c}"] = R.averages()
+        if full:
+            out[f"phi_{c}"], out[f"pi_{c}"] = phi_c, pi_c
+    out["tau_end"], out["steps_end"] = R.time()
+    # spectrum and islands on the final state
+    F, K, Q, C = R.spectrum()
+    out["spec_F"], out["spec_K"], out["spec_Q"], out["spec_counts"] = F, K, Q, C
+    if p.Nc == 1:
+        thr = island_threshold(phi_c, pi_c)
+        labels, stats = R.islands(thr)
+        lab = O.from_ref_layout(labels.astype(np.float64), p.N, 1)[0].astype(np.int32)
+        out["island_thres"] = thr
+        out["island_stats"] = stats
+        out["island_labels_sha"] = hashlib.sha256(lab.astype("<i4").tobytes()).hexdigest()
+        if full:
+            out["island_labels"] = lab
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: rows={len(out['rows'])} islands={len(out.get('island_stats', []))}")
+
+
+def main() -> None:
+    from oracle import oracle as O
+    if len(sys.argv) > 2 and sys.argv[1] == "--case":
+        run_case(sys.argv[2])
+        return
+    if not O.ref_available(0) or not O.ref_available(1):
+        sys.exit("reference pin not built: run oracle/build_ref.sh first")
+    for name in CASES:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--case", name], check=True)
+
+
+if __name__ == "__main__":
+    main()
