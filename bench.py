@@ -1,0 +1,337 @@
+"""Benchmark of the lattice hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step" = one leapfrog step over the whole lattice): the phi^6
+oscillon potential (reference theory 0, Kappa = sqrt(3)) on a 512^3 periodic
+lattice, a = 0.25, dtau = 0.02, FP32 fields, with the volume averages and
+extrema fused into every 50th step (TSO = 1.0).  Inputs are seeded synthetic
+fields (homogeneous phi0 = sqrt(6) plus smoothed noise); 1.5 GB of fields, far
+above the 129 MB L2, so no flush is needed between steps.
+
+value     site-updates/s over K steps, fields resident in HBM, device time
+          (CUDA events on the handle's stream), max over ranks x ranks.
+e2e       the same metric through the C ABI with host buffers: each e2e
+          iteration uploads phi, pi (reference layout, FP64, pinned), runs one
+          TSO interval (50 steps + one SO row) and downloads phi, pi.
+roofline  the plain step kernel: 16 algorithmic bytes per site (read phi, pi;
+          write pi, phi') over its mean launch time, against the measured HBM
+          copy bandwidth in MEASURED_PEAKS.json.
+cpu_baseline / --impl reference
+          the CPU oracle (C restatement of the reference loop, FP64, the
+          reference's -O3 -ffast-math flags, OpenMP over z-slabs) on a bounded
+          number of steps of the same lattice.
+Multi-GPU: replicas only -- every rank evolves its own lattice; no collective
+on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+
+METRIC = "site-updates/s"
+N_MAIN = 512
+TSO_STEPS = 50
+BYTES_PER_SITE = {0: 32, 1: 16, 2: 32}  # FP64, FP32, compensated FP32
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class Dist:
+    """Barrier and max-reduce across ranks (gloo on CPU tensors); trivial at N=1."""
+
+    def __init__(self):
+        self.rank, self.local, self.world = env_rank()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx, self.samples, self.proc = gpu_index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for s in self.samples for j in range(4) if s[5 + j].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the plain FP32 step kernel at 512^3, from the
+    committed ncu summary (profiles/leapfrog_f32_512.md, line 'traffic_bytes_per_launch: X')."""
+    path = os.path.join(ROOT, "profiles", "leapfrog_f32_512.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+_FIELDS = {}
+
+
+def make_fields(N: int, seed: int = 2026):
+    """Seeded Gaussian fields with the configuration's spectrum (vacuum
+    amplitude 1/(2 omega L^3) per mode in the config's units, x6 in the
+    reference's, modes above k_max = pi/(2 dx) zeroed), in the reference layout."""
+    if N not in _FIELDS:
+        from phinum_gb300 import initial, layout
+        phi, pi = initial.gaussian_fields(N, a=0.25, phi0=6.0 ** 0.5, noise=3.0, scale2=2 * np.pi, seed=seed)
+        _FIELDS[N] = (layout.to_ref_layout(phi), layout.to_ref_layout(pi))
+    return _FIELDS[N]
+
+
+def measure_gpu(args, dist: Dist):
+    from phinum_gb300 import lattice as PL
+    from phinum_gb300 import _lib as L
+
+    N = N_MAIN
+    phi, pi = make_fields(N)
+    lib = L.load()
+    sites = N ** 3
+    out = {}
+
+    # ---------------------------------------------------------------- value
+    lat = PL.Lattice(PL.Params(N=N, precision=L.FP32))
+    lat.upload(phi, pi)
+    lat.run_loop(max(3, args.warmup), 1.0)
+    lat.synchronize()
+    n0, _, _ = lat.stats()
+    dist.barrier()
+    lat.synchronize()
+    with ClockSampler(dist.local) as cs:
+        t0 = time.perf_counter()
+        rows = lat.run_loop(args.steps, 1.0, max_rows=args.steps // TSO_STEPS + 2)
+        lat.synchronize()
+        wall = time.perf_counter() - t0
+    dist.barrier()
+    n1, ms, nsteps = lat.stats()
+    dev_s = dist.max(ms / 1e3)
+    out["value"] = sites * args.steps * dist.world / dev_s
+    out["ms_per_step"] = dev_s * 1e3 / args.steps
+    out["wall_s"] = wall
+    out["rows"] = int(rows.shape[0])
+    out["gpu_launches"] = int(n1 - n0)
+    out["clocks"] = cs.summary()
+    out["energy_drift"] = float(abs(rows[-1, 14] - rows[0, 14]) / abs(rows[0, 14])) if rows.shape[0] > 1 else None
+
+    # ------------------------------------------------- roofline: plain step
+    lat.evolve(20)
+    k_plain = max(50, min(400, args.steps))
+    lat.evolve(k_plain)
+    _, ms_plain, _ = lat.stats()
+    t_launch = ms_plain / 1e3 / k_plain
+    achieved = BYTES_PER_SITE[1] * sites / t_launch / 1e9
+    peak, kind = peaks()
+    out["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                       "frac": round(achieved / peak, 4), "traffic": traffic_from_profile(),
+                       "kernel": "phn::step_f32<1,0,0>", "peak_kind": f"{kind} hbm_gbs",
+                       "algorithmic_bytes_per_launch": BYTES_PER_SITE[1] * sites,
+                       "mean_launch_ms": round(t_launch * 1e3, 4)}
+    lat.close()
+
+    # ---------------------------------------------------------------- e2e
+    lat = PL.Lattice(PL.Params(N=N, precision=L.FP32))
+    for a in (phi, pi):
+        L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
+    hphi, hpi = np.empty_like(phi), np.empty_like(pi)
+    for a in (hphi, hpi):
+        L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
+    e2e_iters = 3
+
+    def e2e_iter():
+        lat.upload(phi, pi)
+        lat.run_loop(TSO_STEPS, 1.0, max_rows=2)
+        L.check(lib.phn_download(lat.h, hphi.ctypes.data_as(L._PD), hpi.ctypes.data_as(L._PD)))
+
+    e2e_iter()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_iters):
+        e2e_iter()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    out["e2e"] = {"value": sites * TSO_STEPS * e2e_iters * dist.world / e2e_s, "unit": METRIC,
+                  "h2d_bytes_per_step": int(phi.nbytes + pi.nbytes),
+                  "d2h_bytes_per_step": int(hphi.nbytes + hpi.nbytes + 26 * 8),
+                  "step": f"upload phi,pi (FP64 reference layout) + {TSO_STEPS} leapfrog steps with one fused "
+                          "SO row + download phi,pi"}
+    for a in (phi, pi, hphi, hpi):
+        lib.phn_unpin_host(a.ctypes.data)
+    lat.close()
+
+    # ------------------------------------------- the other precisions/sizes
+    also = {}
+    for label, n, prec, k in (("n256_fp32", 256, L.FP32, 400), ("n256_fp64", 256, L.FP64, 40),
+                              ("n512_fp64", 512, L.FP64, 10), ("n512_kahan_fp32", 512, L.FP32_KAHAN, 200)):
+        if args.quick and n == 512 and prec != L.FP32:
+            continue
+        ph, pp = (phi, pi) if n == N else make_fields(n)
+        lat = PL.Lattice(PL.Params(N=n, precision=prec))
+        lat.upload(ph, pp)
+        lat.evolve(3)
+        lat.evolve(k)
+        _, ms_k, _ = lat.stats()
+        t = ms_k / 1e3 / k
+        also[label] = {"site_updates_per_s": n ** 3 / t, "ms_per_step": t * 1e3,
+                       "hbm_gbs_algorithmic": BYTES_PER_SITE[prec] * n ** 3 / t / 1e9,
+                       "frac_of_measured_hbm": BYTES_PER_SITE[prec] * n ** 3 / t / 1e9 / peak}
+        lat.close()
+    out["also"] = also
+    return out
+
+
+def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int):
+    """The oracle's reference loop (FP64) on all host threads, bounded."""
+    from oracle import oracle as O
+    O.build()
+    p = O.Params(N=N)
+    phi, pi = make_fields(N)
+    nt = O.max_threads(True)
+    clock = O.Clock(p, fast=True)
+    O.evolve(p, phi, pi, 1, clock, nthreads=nt, fast=True)  # warm-up, page-in
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < steps_cap and time.perf_counter() - t0 < max_seconds:
+        O.evolve(p, phi, pi, 1, clock, nthreads=nt, fast=True)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return N ** 3 * steps / dt, nt, steps, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="skip the slow FP64/compensated extra lines")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    rank, local, world = env_rank()
+    config = {"workload": f"phi^6 oscillon (theory 0, Kappa=sqrt(3)), {N_MAIN}^3 periodic lattice, a=0.25, "
+                          f"dtau=0.02, leapfrog kick-drift with fused volume averages + extrema every "
+                          f"{TSO_STEPS} steps (TSO=1.0)",
+              "N": N_MAIN, "sites": N_MAIN ** 3, "tso_steps": TSO_STEPS,
+              "l2": "inputs larger than L2 (1.5 GB of fields vs 129 MB L2); no flush",
+              "parallelism": f"replicas x{args.gpus}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        rate, nt, steps, dt = cpu_reference_rate(N_MAIN, 45.0, max(1, args.steps))
+        line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": args.gpus,
+                "steps": steps, "warmup": 1, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": rate, "unit": METRIC, "cores": nt, "kind": "port",
+                                 "sample": f"{steps} steps of the {N_MAIN}^3 lattice, FP64, {nt} OpenMP threads "
+                                           f"over z-slabs, -O3 -ffast-math (reference flags)"},
+                "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        # one replica per GPU: this rank sees only its own device
+        os.environ["CUDA_DEVICE_ORDER"] = "PCI_BUS_ID"
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = Dist()
+    res = measure_gpu(args, dist)
+    line = {"metric": METRIC, "value": res["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": res["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+            "roofline": res["roofline"], "e2e": res["e2e"], "clocks": res["clocks"],
+            "gpu_launches": res["gpu_launches"], "also": res["also"],
+            "so_rows": res["rows"], "energy_drift_rel": res["energy_drift"]}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, nt, steps, dt = cpu_reference_rate(N_MAIN, 15.0, 200)
+        line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": nt, "kind": "port",
+                                "sample": f"{steps} steps of the {N_MAIN}^3 lattice ({dt:.1f} s), FP64, {nt} "
+                                          f"OpenMP threads over z-slabs, -O3 -ffast-math (reference flags)"}
+    if rank == 0:
+        print(json.dumps(line))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,169 @@
+/*
+ * phinum_gpu.h -- C ABI of the GB300 (sm_103a) implementation of PhiNum's
+ * lattice hot path: leapfrog evolution of (phi, pi) on a periodic cubic
+ * lattice with fused volume averages, the radial power spectrum after an R2C
+ * FFT, and island (connected-component) labelling.
+ *
+ * The reference exposes no FFI: its entry points are argument-less free
+ * functions over globals.  Each call below replaces one of them; the host
+ * keeps the reference's parameters and lattice layout and copies results
+ * into the same globals (see phinum_gb300/adapter/phinum_dynamics.cpp).
+ *
+ * Conventions
+ *   - Every function returns an int status: PHN_OK (0) or a negative
+ *     PHN_ERR_* code.  Nothing aborts or traps; phn_last_error() gives text.
+ *   - Host field arrays use the reference layout (lattice.cpp:76-78,
+ *     util.cpp:34-37): Nc*N*N*(N+2) doubles, index Nc*(x + N*y + N*N*z) + a,
+ *     z-slabs 0 and N+1 are ghost copies of slabs N and 1.  The caller owns
+ *     them; the handle owns its device copies.
+ *   - Positions reported (extrema, island peaks) are indices into that layout.
+ *   - One handle = one lattice on the current CUDA device, one stream.
+ *     Calls on a handle are not thread-safe; distinct handles are independent.
+ */
+#ifndef PHINUM_GPU_H
+#define PHINUM_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHN_ABI_VERSION 1
+#define PHN_MAX_NC 4
+
+enum {
+  PHN_OK = 0,
+  PHN_ERR_INVALID = -1,     /* bad argument or parameter */
+  PHN_ERR_CUDA = -2,        /* a CUDA runtime or cuFFT call failed */
+  PHN_ERR_NONFINITE = -3,   /* a reduction saw NaN or Inf in the fields */
+  PHN_ERR_TIMEOUT = -4,     /* a bounded device-side wait gave up */
+  PHN_ERR_NOMEM = -5,       /* device allocation failed or exceeds the size cap */
+  PHN_ERR_UNSUPPORTED = -6, /* valid in the reference, not provided here */
+  PHN_ERR_TRUNCATED = -7    /* output buffer smaller than the result */
+};
+
+enum {
+  PHN_FP64 = 0,      /* fields and arithmetic in FP64, in the reference's operation order */
+  PHN_FP32 = 1,      /* fields in FP32, FP64 reductions */
+  PHN_FP32_KAHAN = 2 /* fields in FP32 with compensated (Kahan) kick and drift, FP64 reductions */
+};
+
+enum {
+  PHN_ISLAND_REFERENCE = 0, /* is_island(): phi^2/2 + pi^2/2 > thres^2/2 (islands.cpp:76) */
+  PHN_ISLAND_ENERGY = 1     /* energy density rho(x) > thres, rho the summand of <E> */
+};
+
+/* Run parameters, in the reference's own terms (parameters.cpp:84-201). */
+typedef struct phn_params {
+  int N;           /* N_t = N_eta: lattice edge (cubic box) */
+  int Nc;          /* field components, 1..PHN_MAX_NC */
+  int theory;      /* 0: phi^4+phi^6 (Kappa), 1: phi^4 + linear h  (parameters.cpp:86-120) */
+  int mass_mode;   /* Mass_Mode */
+  int lambda_mode; /* Lambda_Mode */
+  int precision;   /* PHN_FP64 / PHN_FP32 / PHN_FP32_KAHAN */
+  double a;        /* a_t = a_eta */
+  double dt;       /* dtBaseTrans; dtau = dt * a (dynamics.cpp:42) */
+  double T0;       /* initial time */
+  double m_sqr;    /* M_sqr (bare masses without tadpole renormalisation) */
+  double kappa;    /* Kappa, theory 0 */
+  double h;        /* h, theory 1 */
+} phn_params;
+
+/* One SO row: the outputs of CalculateVolumeAverages + CalculateExtrema
+ * (lattice.cpp:44-58), as 26 doubles. */
+typedef struct phn_averages {
+  double t;                               /* time stamp (SO rows: LastSOoutput) */
+  double phi[PHN_MAX_NC], pi[PHN_MAX_NC]; /* avgphi[a], avgpi[a] */
+  double phi2, pi2, phipi, phi4, phi6;    /* avgphi2 ... avgphi6 */
+  double energy, interaction, charge;     /* avgEnergy, avgInteraction, avgCharge */
+  double min_phi, max_phi, max_abs_phi;   /* GlminPhi, GlmaxPhi, GlmaxAbsPhi */
+  double min_pos, max_pos, max_abs_pos;   /* minpos, maxpos, maxAbspos */
+  double gradient;                        /* GradPhiSqr / vol */
+  double nonfinite;                       /* number of non-finite phi/pi values seen */
+  double reserved;
+} phn_averages;
+
+/* One island (struct island, islands.cpp:13-28).  Islands are numbered by
+ * their smallest site index, which is the reference's seed order. */
+typedef struct phn_island {
+  double index, size, volume, pot_en, kin_en, grad_en, av_phi, peak_pos, peak_value, seed_pos;
+} phn_island;
+
+typedef struct phn_handle phn_handle;
+
+int phn_abi_version(void);
+const char *phn_last_error(void);
+int phn_device_count(int *count);
+
+/* LocalLattice::init + FFT::init + MomentumSpace::init + reset()
+ * (lattice.cpp:70-104, clusterfft.cpp:36-47, momentumspace.cpp:32-65,
+ * dynamics.cpp:28-50): allocates device fields (zeroed) on the current device. */
+int phn_create(const phn_params *params, phn_handle **out);
+/* LocalLattice::fin / FFT::fin / MomentumSpace::fin (lattice.cpp:107-117). */
+int phn_destroy(phn_handle *h);
+
+/* Replaces direct writes/reads of LocalLattice::Phi/Pi (lattice.cpp:77-78):
+ * host arrays in the reference layout; upload reads the interior only,
+ * download also fills the ghost slabs as Communication::exchange() would. */
+int phn_upload(phn_handle *h, const double *Phi, const double *Pi);
+int phn_download(phn_handle *h, double *Phi, double *Pi);
+
+/* reset() (dynamics.cpp:28-50): tau = T0, kick/drift clocks = tau, counters 0.
+ * The next evolve kicks by dtau/2 (dynamics.cpp:84). */
+int phn_reset(phn_handle *h);
+/* nsteps x evolve() (dynamics.cpp:196-237): updateMomenta + updateFields +
+ * exchange, fused into one kernel per step. */
+int phn_evolve(phn_handle *h, int nsteps);
+/* LocalLattice::tau and numeric::total_stepcount. */
+int phn_time(const phn_handle *h, double *tau, int *total_stepcount);
+
+/* CalculateExtrema() + CalculateVolumeAverages() (fieldanalysis.cpp:319-699)
+ * on the current state. */
+int phn_volume_averages(phn_handle *h, phn_averages *out);
+/* false_vacuum_decayed() (fieldanalysis.cpp:887-893) on the last averages. */
+int phn_false_vacuum_decayed(const phn_averages *avg, int theory, int *decayed);
+
+/* The run loop of main.cpp:685-699 with an explicit step count: reset(),
+ * then nsteps x { Print_AveragesExtrema() cadence (TSO on the accumulated tau,
+ * fieldanalysis.cpp:753-780); evolve() }.  The averages of a due row are
+ * fused into that step's kernel (zero extra passes over HBM).  Rows are
+ * stamped with LastSOoutput.  *nrows receives the number of rows; if more than
+ * max_rows were due the call returns PHN_ERR_TRUNCATED after writing max_rows. */
+int phn_run_loop(phn_handle *h, int nsteps, double tso, phn_averages *rows, int max_rows, int *nrows);
+
+/* MomentumSpace::init (momentumspace.cpp:40-47): bin count and width. */
+int phn_spectrum_bins(const phn_handle *h, int *nbins, double *binsize);
+/* fftXtoP_direct + Calculate_CorrelationFunctions (clusterfft.cpp:185-225,
+ * momentumspace.cpp:140-278) on the current state: TotalCorrF/K/Q[bin*Nc+a]
+ * and TotalBCounts[bin].  Arrays hold nbins*Nc (F, K, Q) and nbins (counts). */
+int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, int nbins);
+
+/* Full_Analysis() seeding from an empty history (islands.cpp:72-279,778-840):
+ * mask (mode), 6-connectivity, x and y periodic, z open as on one rank unless
+ * z_periodic.  labels (optional, reference layout, -1 outside islands) and up
+ * to max_out island records; *n_islands receives the total count.  Nc must
+ * be 1 (the reference's scan walks component-interleaved indices). */
+int phn_islands(phn_handle *h, double thres, int mode, int z_periodic, int *labels, phn_island *out,
+                int max_out, int *n_islands);
+
+/* Device pointers of the current fields (precision-typed: double* for
+ * PHN_FP64, float* otherwise; SoA [a][z][y][x], no ghosts) and the stream the
+ * handle launches on, for callers that keep data resident on the device. */
+int phn_device_fields(phn_handle *h, void **phi, void **pi, void **stream);
+int phn_synchronize(phn_handle *h);
+
+/* Launch statistics: kernels launched by this handle since creation, and the
+ * device time of the last phn_evolve / phn_run_loop step kernels (CUDA events
+ * on the handle's stream), for roofline accounting. */
+int phn_stats(const phn_handle *h, long long *kernel_launches, double *last_evolve_ms, int *last_evolve_steps);
+
+/* Page-locks (unlocks) a caller-owned host buffer so that phn_upload /
+ * phn_download move it by DMA at full link bandwidth (cudaHostRegister). */
+int phn_pin_host(void *ptr, size_t bytes);
+int phn_unpin_host(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,108 @@
+"""ctypes binding of libphinum_gpu.so (include/phinum_gpu.h).
+
+The library is the product; this module only declares its C ABI for Python
+callers (tests, bench).  Loading fails loudly when the shared object is
+missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libphinum_gpu.so")
+
+MAX_NC = 4
+OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NOMEM, ERR_UNSUPPORTED, ERR_TRUNCATED = \
+    0, -1, -2, -3, -4, -5, -6, -7
+FP64, FP32, FP32_KAHAN = 0, 1, 2
+ISLAND_REFERENCE, ISLAND_ENERGY = 0, 1
+
+_D, _I = ctypes.c_double, ctypes.c_int
+_PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+
+
+class PhnParams(ctypes.Structure):
+    _fields_ = [("N", _I), ("Nc", _I), ("theory", _I), ("mass_mode", _I), ("lambda_mode", _I),
+                ("precision", _I), ("a", _D), ("dt", _D), ("T0", _D), ("m_sqr", _D), ("kappa", _D),
+                ("h", _D)]
+
+
+class PhnAverages(ctypes.Structure):
+    _fields_ = [("t", _D), ("phi", _D * MAX_NC), ("pi", _D * MAX_NC), ("phi2", _D), ("pi2", _D),
+                ("phipi", _D), ("phi4", _D), ("phi6", _D), ("energy", _D), ("interaction", _D),
+                ("charge", _D), ("min_phi", _D), ("max_phi", _D), ("max_abs_phi", _D), ("min_pos", _D),
+                ("max_pos", _D), ("max_abs_pos", _D), ("gradient", _D), ("nonfinite", _D),
+                ("reserved", _D)]
+
+
+AVG_LEN = ctypes.sizeof(PhnAverages) // 8
+ISLAND_FIELDS = ["index", "size", "volume", "pot_en", "kin_en", "grad_en", "av_phi", "peak_pos",
+                 "peak_value", "seed_pos"]
+
+
+class PhnError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"phn error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+# name: (restype, argtypes)
+_SIGS = {
+    "phn_abi_version": (_I, []),
+    "phn_last_error": (ctypes.c_char_p, []),
+    "phn_device_count": (_I, [_PI]),
+    "phn_create": (_I, [ctypes.POINTER(PhnParams), ctypes.POINTER(ctypes.c_void_p)]),
+    "phn_destroy": (_I, [ctypes.c_void_p]),
+    "phn_upload": (_I, [ctypes.c_void_p, _PD, _PD]),
+    "phn_download": (_I, [ctypes.c_void_p, _PD, _PD]),
+    "phn_reset": (_I, [ctypes.c_void_p]),
+    "phn_evolve": (_I, [ctypes.c_void_p, _I]),
+    "phn_time": (_I, [ctypes.c_void_p, _PD, _PI]),
+    "phn_volume_averages": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnAverages)]),
+    "phn_false_vacuum_decayed": (_I, [ctypes.POINTER(PhnAverages), _I, _PI]),
+    "phn_run_loop": (_I, [ctypes.c_void_p, _I, _D, ctypes.POINTER(PhnAverages), _I, _PI]),
+    "phn_spectrum_bins": (_I, [ctypes.c_void_p, _PI, _PD]),
+    "phn_spectrum": (_I, [ctypes.c_void_p, _PD, _PD, _PD, _PI, _I]),
+    "phn_islands": (_I, [ctypes.c_void_p, _D, _I, _I, _PI, _PD, _I, _PI]),
+    "phn_device_fields": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                               ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
+    "phn_synchronize": (_I, [ctypes.c_void_p]),
+    "phn_stats": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _PD, _PI]),
+    "phn_pin_host": (_I, [ctypes.c_void_p, ctypes.c_size_t]),
+    "phn_unpin_host": (_I, [ctypes.c_void_p]),
+}
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def load(build_if_missing: bool = False):
+    """Loads the library once.  Raises if it is not built (build() builds it)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            from . import build as _b
+            _b.build()
+        else:
+            raise OSError(f"{LIB_PATH} is not built; run phinum_gb300.build.build() "
+                          "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code: int):
+    if code != OK:
+        msg = _lib.phn_last_error().decode() if _lib is not None else ""
+        raise PhnError(code, msg)
+    return code

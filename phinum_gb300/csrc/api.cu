@@ -1,0 +1,434 @@
+// C ABI: handle lifetime, field transfer, the reference clock and the run
+// loop.  The host keeps tau/Last_*_update exactly as dynamics.cpp:28-237 does
+// (FP64, same operation order), so the per-step kick and drift factors handed
+// to the kernels are the reference's own values.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "phn_internal.h"
+
+namespace {
+thread_local char g_err[512] = "";
+}
+
+namespace phn {
+int set_error(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+int cuda_error(cudaError_t e, const char *what) {
+  if (e == cudaErrorMemoryAllocation) return set_error(PHN_ERR_NOMEM, "%s: %s", what, cudaGetErrorString(e));
+  return set_error(PHN_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+}  // namespace phn
+
+using namespace phn;
+
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_error(e_, #call); \
+  } while (0)
+
+static int validate(const phn_params *p) {
+  if (!p) return set_error(PHN_ERR_INVALID, "params is NULL");
+  if (p->N < 2 || p->N > 2048) return set_error(PHN_ERR_INVALID, "N=%d outside [2, 2048]", p->N);
+  if (p->Nc < 1 || p->Nc > PHN_MAX_NC) return set_error(PHN_ERR_UNSUPPORTED, "Nc=%d outside [1, %d]", p->Nc, PHN_MAX_NC);
+  if (p->theory != 0 && p->theory != 1)
+    return set_error(PHN_ERR_UNSUPPORTED, "theory %d: only theories 0 and 1 are provided", p->theory);
+  if (p->precision < PHN_FP64 || p->precision > PHN_FP32_KAHAN)
+    return set_error(PHN_ERR_INVALID, "precision %d", p->precision);
+  if (!(p->a > 0.0) || !isfinite(p->a)) return set_error(PHN_ERR_INVALID, "a must be positive");
+  if (!isfinite(p->dt)) return set_error(PHN_ERR_INVALID, "dt must be finite");
+  if (p->theory == 0 && !(p->kappa != 0.0)) return set_error(PHN_ERR_INVALID, "Kappa must be non-zero");
+  return PHN_OK;
+}
+
+// Coefficients evaluated with the reference's expressions (dynamics.cpp:80-100,
+// fieldanalysis.cpp:445-579); see Consts.
+static Consts make_consts(const phn_params *p) {
+  Consts k;
+  memset(&k, 0, sizeof(k));
+  const int Nc = p->Nc;
+  k.N = p->N;
+  k.Nc = Nc;
+  k.theory = p->theory;
+  k.a2 = p->a * p->a;
+  k.mmM = p->mass_mode * p->m_sqr;
+  k.lm = (double)p->lambda_mode;
+  k.six_nc = 6. * Nc;
+  k.kappa = p->kappa;
+  k.c120 = 120. * Nc * Nc;
+  k.h = p->h;
+  k.mm_half_M = (p->mass_mode) * 0.5 * p->m_sqr;
+  k.c24 = 24.0 * Nc;
+  k.c720 = 720.0 * Nc * Nc * p->kappa * p->kappa;
+  k.inv_a2_f = (float)(1.0 / k.a2);
+  k.mmM_f = (float)k.mmM;
+  k.c4_f = (float)(k.lm / k.six_nc);
+  k.c6_f = p->theory == 0 ? (float)(1.0 / (p->kappa * p->kappa * k.c120)) : 0.f;
+  k.h_f = (float)p->h;
+  k.mmh_f = (float)k.mm_half_M;
+  k.e4_f = (float)(k.lm / k.c24);
+  k.e6_f = p->theory == 0 ? (float)(1.0 / k.c720) : 0.f;
+  return k;
+}
+
+static void free_all(phn_handle *h) {
+  if (!h) return;
+  spectrum_release(h);
+  islands_release(h);
+  cudaFree(h->phi[0]);
+  cudaFree(h->phi[1]);
+  cudaFree(h->pi);
+  cudaFree(h->cphi);
+  cudaFree(h->cpi);
+  cudaFree(h->partials);
+  cudaFree(h->d_avg);
+  cudaFree(h->d_ref);
+  if (h->h_avg) cudaFreeHost(h->h_avg);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+extern "C" {
+
+int phn_abi_version(void) { return PHN_ABI_VERSION; }
+
+const char *phn_last_error(void) { return g_err; }
+
+int phn_device_count(int *count) {
+  if (!count) return set_error(PHN_ERR_INVALID, "count is NULL");
+  *count = 0;
+  cudaError_t e = cudaGetDeviceCount(count);
+  if (e != cudaSuccess) {
+    *count = 0;
+    return cuda_error(e, "cudaGetDeviceCount");
+  }
+  return PHN_OK;
+}
+
+int phn_reset(phn_handle *h) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  h->tau = h->p.T0;
+  h->dtau = h->p.dt * h->p.a;
+  h->last_field = h->tau;
+  h->last_mom = h->tau;
+  h->steps = 0;
+  return PHN_OK;
+}
+
+int phn_create(const phn_params *params, phn_handle **out) {
+  if (!out) return set_error(PHN_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int r = validate(params);
+  if (r) return r;
+  phn_handle *h = new phn_handle();
+  memset((void *)h, 0, sizeof(*h));
+  h->p = *params;
+  h->k = make_consts(params);
+  h->grid = lattice_grid(params->N);
+  h->V = (size_t)params->N * params->N * params->N;
+  h->elem = params->precision == PHN_FP64 ? sizeof(double) : sizeof(float);
+  const size_t bytes = h->V * params->Nc * h->elem;
+  cudaError_t e = cudaGetDevice(&h->device);
+#define CKF(call)                                  \
+  do {                                             \
+    e = (call);                                    \
+    if (e != cudaSuccess) {                        \
+      int rr = cuda_error(e, #call);               \
+      free_all(h);                                 \
+      return rr;                                   \
+    }                                              \
+  } while (0)
+  if (e != cudaSuccess) {
+    int rr = cuda_error(e, "cudaGetDevice");
+    delete h;
+    return rr;
+  }
+  CKF(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CKF(cudaEventCreate(&h->ev0));
+  CKF(cudaEventCreate(&h->ev1));
+  CKF(cudaMalloc(&h->phi[0], bytes));
+  CKF(cudaMalloc(&h->phi[1], bytes));
+  CKF(cudaMalloc(&h->pi, bytes));
+  CKF(cudaMemsetAsync(h->phi[0], 0, bytes, h->stream));
+  CKF(cudaMemsetAsync(h->phi[1], 0, bytes, h->stream));
+  CKF(cudaMemsetAsync(h->pi, 0, bytes, h->stream));
+  if (params->precision == PHN_FP32_KAHAN) {
+    CKF(cudaMalloc(&h->cphi, bytes));
+    CKF(cudaMalloc(&h->cpi, bytes));
+    CKF(cudaMemsetAsync(h->cphi, 0, bytes, h->stream));
+    CKF(cudaMemsetAsync(h->cpi, 0, bytes, h->stream));
+  }
+  CKF(cudaMalloc(&h->partials, (size_t)h->grid.nblocks * REC * sizeof(double)));
+  CKF(cudaMalloc(&h->d_avg, sizeof(phn_averages)));
+  h->h_avg_cap = 64;
+  CKF(cudaHostAlloc((void **)&h->h_avg, h->h_avg_cap * sizeof(phn_averages), cudaHostAllocDefault));
+  CKF(cudaStreamSynchronize(h->stream));
+#undef CKF
+  phn_reset(h);
+  *out = h;
+  return PHN_OK;
+}
+
+int phn_destroy(phn_handle *h) {
+  if (!h) return PHN_OK;
+  cudaStreamSynchronize(h->stream);
+  free_all(h);
+  return PHN_OK;
+}
+
+static int ensure_ref_staging(phn_handle *h) {
+  if (h->d_ref) return PHN_OK;
+  const size_t n = (size_t)h->p.Nc * h->p.N * h->p.N * (h->p.N + 2);
+  CK(cudaMalloc(&h->d_ref, n * sizeof(double)));
+  return PHN_OK;
+}
+
+int phn_upload(phn_handle *h, const double *Phi, const double *Pi) {
+  if (!h || !Phi || !Pi) return set_error(PHN_ERR_INVALID, "NULL argument");
+  int r = ensure_ref_staging(h);
+  if (r) return r;
+  const int N = h->p.N, Nc = h->p.Nc;
+  const size_t n = (size_t)Nc * N * N * (N + 2);
+  // phi
+  CK(cudaMemcpyAsync(h->d_ref, Phi, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (h->p.precision == PHN_FP32_KAHAN)
+    CK(launch_from_ref_kahan(h->d_ref, (float *)h->phi[h->cur], h->cphi, N, Nc, h->stream));
+  else
+    CK(launch_from_ref(h->d_ref, h->phi[h->cur], h->p.precision, N, Nc, h->stream));
+  // pi
+  CK(cudaMemcpyAsync(h->d_ref, Pi, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (h->p.precision == PHN_FP32_KAHAN)
+    CK(launch_from_ref_kahan(h->d_ref, (float *)h->pi, h->cpi, N, Nc, h->stream));
+  else
+    CK(launch_from_ref(h->d_ref, h->pi, h->p.precision, N, Nc, h->stream));
+  h->launches += 2;
+  CK(cudaStreamSynchronize(h->stream));
+  return PHN_OK;
+}
+
+int phn_download(phn_handle *h, double *Phi, double *Pi) {
+  if (!h || (!Phi && !Pi)) return set_error(PHN_ERR_INVALID, "NULL argument");
+  int r = ensure_ref_staging(h);
+  if (r) return r;
+  const int N = h->p.N, Nc = h->p.Nc;
+  const size_t n = (size_t)Nc * N * N * (N + 2);
+  const bool kahan = h->p.precision == PHN_FP32_KAHAN;
+  if (Phi) {
+    if (kahan)
+      CK(launch_to_ref_kahan((const float *)h->phi[h->cur], h->cphi, h->d_ref, N, Nc, h->stream));
+    else
+      CK(launch_to_ref(h->phi[h->cur], h->d_ref, h->p.precision, N, Nc, h->stream));
+    CK(cudaMemcpyAsync(Phi, h->d_ref, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->launches++;
+  }
+  if (Pi) {
+    if (kahan)
+      CK(launch_to_ref_kahan((const float *)h->pi, h->cpi, h->d_ref, N, Nc, h->stream));
+    else
+      CK(launch_to_ref(h->pi, h->d_ref, h->p.precision, N, Nc, h->stream));
+    CK(cudaMemcpyAsync(Pi, h->d_ref, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->launches++;
+  }
+  return PHN_OK;
+}
+
+int phn_time(const phn_handle *h, double *tau, int *total_stepcount) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (tau) *tau = h->tau;
+  if (total_stepcount) *total_stepcount = h->steps;
+  return PHN_OK;
+}
+
+// One evolve(): host clock as dynamics.cpp:200-236, one fused kernel.
+static int step_once(phn_handle *h, int mode) {
+  StepF s;
+  if (mode != MODE_OBS) {
+    h->tau += 0.5 * h->dtau;
+    s.fk = h->tau - h->last_mom;
+    h->last_mom = h->tau;
+    h->tau += 0.5 * h->dtau;
+    s.fd = h->tau - h->last_field;
+    h->last_field = h->tau;
+  } else {
+    s.fk = s.fd = 0.0;
+  }
+  const int nxt = 1 - h->cur;
+  cudaError_t e;
+  switch (h->p.precision) {
+    case PHN_FP64:
+      e = launch_step_f64(h->k, h->grid, mode, (const double *)h->phi[h->cur], (double *)h->phi[nxt],
+                          (double *)h->pi, s, h->partials, h->stream);
+      break;
+    case PHN_FP32:
+      e = launch_step_f32(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt],
+                          (float *)h->pi, s, h->partials, h->stream);
+      break;
+    default:
+      e = launch_step_kahan(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt], h->cphi,
+                            h->cphi, (float *)h->pi, h->cpi, s, h->partials, h->stream);
+      break;
+  }
+  if (e != cudaSuccess) return cuda_error(e, "step kernel launch");
+  h->launches++;
+  if (mode != MODE_OBS) {
+    h->cur = nxt;
+    h->steps++;
+  }
+  return PHN_OK;
+}
+
+int phn_evolve(phn_handle *h, int nsteps) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (nsteps < 0) return set_error(PHN_ERR_INVALID, "nsteps < 0");
+  CK(cudaEventRecord(h->ev0, h->stream));
+  for (int i = 0; i < nsteps; ++i) {
+    int r = step_once(h, MODE_STEP);
+    if (r) return r;
+  }
+  CK(cudaEventRecord(h->ev1, h->stream));
+  CK(cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->last_ms = ms;
+  h->last_steps = nsteps;
+  return PHN_OK;
+}
+
+static int fetch_avg(phn_handle *h, phn_averages *dst_host_slot) {
+  CK(launch_finalize(h->k, h->partials, h->grid.nblocks, h->d_avg, h->stream));
+  h->launches++;
+  CK(cudaMemcpyAsync(dst_host_slot, h->d_avg, sizeof(phn_averages), cudaMemcpyDeviceToHost, h->stream));
+  return PHN_OK;
+}
+
+int phn_volume_averages(phn_handle *h, phn_averages *out) {
+  if (!h || !out) return set_error(PHN_ERR_INVALID, "NULL argument");
+  int r = step_once(h, MODE_OBS);
+  if (r) return r;
+  r = fetch_avg(h, &h->h_avg[0]);
+  if (r) return r;
+  CK(cudaStreamSynchronize(h->stream));
+  *out = h->h_avg[0];
+  out->t = h->tau;
+  if (out->nonfinite > 0) return set_error(PHN_ERR_NONFINITE, "%.0f non-finite field values", out->nonfinite);
+  return PHN_OK;
+}
+
+int phn_false_vacuum_decayed(const phn_averages *avg, int theory, int *decayed) {
+  if (!avg || !decayed) return set_error(PHN_ERR_INVALID, "NULL argument");
+  const double v = avg->interaction;
+  // fieldanalysis.cpp:889-892 (theories 0, 1, 4)
+  *decayed = (theory == 0 || theory == 1 || theory == 4) ? (v < 0 || v != v || v * 0. != 0.) : 0;
+  return PHN_OK;
+}
+
+int phn_run_loop(phn_handle *h, int nsteps, double tso, phn_averages *rows, int max_rows, int *nrows) {
+  if (!h || nsteps < 0 || (max_rows > 0 && !rows)) return set_error(PHN_ERR_INVALID, "bad argument");
+  if (max_rows > h->h_avg_cap) {
+    cudaFreeHost(h->h_avg);
+    h->h_avg = nullptr;
+    h->h_avg_cap = max_rows;
+    CK(cudaHostAlloc((void **)&h->h_avg, (size_t)max_rows * sizeof(phn_averages), cudaHostAllocDefault));
+  }
+  phn_reset(h);
+  double last_so = 0.0;
+  int n = 0, due_total = 0;
+  double *stamps = new double[max_rows > 0 ? max_rows : 1];
+  CK(cudaEventRecord(h->ev0, h->stream));
+  for (int count = 0; count < nsteps; ++count) {
+    // Print_AveragesExtrema cadence (fieldanalysis.cpp:753-780)
+    bool due = false;
+    if (h->steps == 0) {
+      last_so = h->tau;
+      due = true;
+    } else if (!(h->tau < last_so + tso)) {
+      if (h->tau >= last_so + tso) last_so += tso;
+      due = true;
+    }
+    int r;
+    if (due) {
+      due_total++;
+      r = step_once(h, MODE_STEP_OBS);
+      if (!r && n < max_rows) {
+        r = fetch_avg(h, &h->h_avg[n]);
+        stamps[n] = last_so;
+        n++;
+      }
+    } else {
+      r = step_once(h, MODE_STEP);
+    }
+    if (r) {
+      delete[] stamps;
+      return r;
+    }
+  }
+  cudaError_t e = cudaEventRecord(h->ev1, h->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(h->ev1);
+  if (e != cudaSuccess) {
+    delete[] stamps;
+    return cuda_error(e, "run loop");
+  }
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  h->last_steps = nsteps;
+  int nonfinite = 0;
+  for (int i = 0; i < n; ++i) {
+    rows[i] = h->h_avg[i];
+    rows[i].t = stamps[i];
+    if (rows[i].nonfinite > 0) nonfinite = 1;
+  }
+  delete[] stamps;
+  if (nrows) *nrows = due_total;
+  if (due_total > max_rows) return set_error(PHN_ERR_TRUNCATED, "%d rows due, %d written", due_total, max_rows);
+  if (nonfinite) return set_error(PHN_ERR_NONFINITE, "non-finite field values in a row");
+  return PHN_OK;
+}
+
+int phn_device_fields(phn_handle *h, void **phi, void **pi, void **stream) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (phi) *phi = h->phi[h->cur];
+  if (pi) *pi = h->pi;
+  if (stream) *stream = (void *)h->stream;
+  return PHN_OK;
+}
+
+int phn_synchronize(phn_handle *h) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  CK(cudaStreamSynchronize(h->stream));
+  return PHN_OK;
+}
+
+int phn_stats(const phn_handle *h, long long *kernel_launches, double *last_evolve_ms, int *last_evolve_steps) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (kernel_launches) *kernel_launches = h->launches;
+  if (last_evolve_ms) *last_evolve_ms = h->last_ms;
+  if (last_evolve_steps) *last_evolve_steps = h->last_steps;
+  return PHN_OK;
+}
+
+int phn_pin_host(void *ptr, size_t bytes) {
+  if (!ptr || !bytes) return set_error(PHN_ERR_INVALID, "bad argument");
+  CK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return PHN_OK;
+}
+
+int phn_unpin_host(void *ptr) {
+  if (!ptr) return set_error(PHN_ERR_INVALID, "bad argument");
+  CK(cudaHostUnregister(ptr));
+  return PHN_OK;
+}
+
+}  // extern "C"

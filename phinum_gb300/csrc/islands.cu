@@ -1,0 +1,437 @@
+// Island detection as connected-component labelling on the GPU.
+//
+// Replaces is_island + BFS + the seeding scan of Full_Analysis
+// (islands.cpp:72-279, 778-840) for a first analysis (empty island history):
+//   1. mask + init: parent[i] = i for mask sites, -1 elsewhere;
+//   2. merge: every mask site unites with its -x, -y (periodic) and -z (open
+//      as on one rank, islands.cpp:224-236, or periodic) mask neighbours,
+//      linking the larger root under the smaller with atomicMin;
+//   3. compress: parent[i] = root(i).  Links always point to smaller indices,
+//      so each root is the smallest site index of its island;
+//   4. number: islands are numbered by their root in increasing index order,
+//      which is the order in which the reference's linear scan seeds BFS, so
+//      the labels equal the reference's b[] labels;
+//   5. statistics per island (size, energies, <phi>, peak) with FP64 atomics.
+// Every loop terminates: a root search follows strictly decreasing indices,
+// and a union retry strictly decreases the larger root.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "phn_internal.h"
+
+namespace phn {
+
+constexpr int CCL_THREADS = 256;
+
+struct IslState {
+  int *parent;     // [V]
+  int *ids;        // [V] island id of each root
+  int *blk;        // [nblk] roots per block, then exclusive offsets
+  int nblk;
+  // per-island arrays, grown on demand
+  int cap;
+  int *size;
+  double *sums;                 // [cap][5]: pot, kin, grad, phi, (unused)
+  unsigned long long *peak2;    // max phi^2 bits
+  long long *peakpos;           // reference index of the first max site
+  double *peakval;
+  int *seed;                    // root site (interior linear index)
+};
+
+template <typename T>
+__device__ __forceinline__ double val(const T *f, const float *comp, size_t i) {
+  double v = (double)f[i];
+  if (comp) v -= (double)comp[i];
+  return v;
+}
+
+// Per-site energy density: the summand of the reference's Energy
+// (fieldanalysis.cpp:437-471,571-579), Nc = 1.
+template <typename T>
+__device__ double site_rho(const T *phi, const float *cphi, const T *pi, const float *cpi, int N, int x, int y, int z,
+                           const Consts k) {
+  const size_t NN = (size_t)N * N;
+  const size_t i = (size_t)z * NN + (size_t)y * N + x;
+  const double c = val(phi, cphi, i), p = val(pi, cpi, i);
+  const double fx = val(phi, cphi, (size_t)z * NN + (size_t)y * N + (x + 1 == N ? 0 : x + 1));
+  const double fy = val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
+  const double fz = val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
+  const double c2 = c * c;
+  const double grad = ((fx - c) * (fx - c) / k.a2 + (fy - c) * (fy - c) / k.a2) + (fz - c) * (fz - c) / k.a2;
+  double inter = k.mm_half_M * c2;
+  if (k.theory == 1) inter = k.h * c + inter;
+  const double l2 = c2 * c2;
+  if (k.theory == 0)
+    inter += k.lm * (l2 / k.c24) + (l2 * c2 / k.c720);
+  else
+    inter += k.lm * (l2 / k.c24);
+  return 0.5 * (p * p) + 0.5 * grad + inter;
+}
+
+template <typename T>
+__global__ void ccl_init(const T *__restrict__ phi, const float *__restrict__ cphi, const T *__restrict__ pi,
+                         const float *__restrict__ cpi, int N, int mode, double thr, const Consts k,
+                         int *__restrict__ parent) {
+  const size_t V = (size_t)N * N * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    bool m;
+    if (mode == PHN_ISLAND_REFERENCE) {
+      // islands.cpp:76: Phi*Phi*0.5 + Pi*Pi*0.5 > thres*thres*0.5 (thr holds the right side)
+      const double c = val(phi, cphi, i), p = val(pi, cpi, i);
+      m = __dadd_rn(__dmul_rn(__dmul_rn(c, c), 0.5), __dmul_rn(__dmul_rn(p, p), 0.5)) > thr;
+    } else {
+      const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((size_t)N * N));
+      m = site_rho(phi, cphi, pi, cpi, N, x, y, z, k) > thr;
+    }
+    parent[i] = m ? (int)i : -1;
+  }
+}
+
+__device__ __forceinline__ int find_root(const int *parent, int x) {
+  int p = parent[x];
+  while (p != x) {
+    x = p;
+    p = parent[x];
+  }
+  return x;
+}
+
+__device__ void unite(int *parent, int a, int b) {
+  while (true) {
+    a = find_root(parent, a);
+    b = find_root(parent, b);
+    if (a == b) return;
+    if (a < b) {
+      const int t = a;
+      a = b;
+      b = t;
+    }
+    const int old = atomicMin(&parent[a], b);
+    if (old == a) return;
+    a = old;  // a had been linked meanwhile: continue from its new parent
+  }
+}
+
+__global__ void ccl_merge(int *__restrict__ parent, int N, int zper) {
+  const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    if (parent[i] < 0) continue;
+    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
+    const size_t jx = i - x + (x == 0 ? N - 1 : x - 1);
+    const size_t jy = (y == 0) ? i + (size_t)(N - 1) * N : i - N;
+    if (parent[jx] >= 0) unite(parent, (int)i, (int)jx);
+    if (parent[jy] >= 0) unite(parent, (int)i, (int)jy);
+    if (z > 0 || zper) {
+      const size_t jz = (z == 0) ? i + (size_t)(N - 1) * NN : i - NN;
+      if (parent[jz] >= 0) unite(parent, (int)i, (int)jz);
+    }
+  }
+}
+
+// compress and count roots per block of CCL_THREADS sites
+__global__ void ccl_compress(int *__restrict__ parent, size_t V, int *__restrict__ blk) {
+  const size_t i = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
+  bool root = false;
+  if (i < V) {
+    const int p = parent[i];
+    if (p >= 0) {
+      const int r = find_root(parent, (int)i);
+      parent[i] = r;
+      root = (r == (int)i);
+    }
+  }
+  __shared__ int cnt[CCL_THREADS / 32];
+  const unsigned b = __ballot_sync(0xffffffffu, root);
+  if ((threadIdx.x & 31) == 0) cnt[threadIdx.x >> 5] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < CCL_THREADS / 32; ++w) s += cnt[w];
+    blk[blockIdx.x] = s;
+  }
+}
+
+// exclusive scan of the block counts, one block, fixed order
+__global__ void ccl_scan(int *__restrict__ blk, int n, int *__restrict__ total) {
+  __shared__ int part[1024];
+  const int t = threadIdx.x;
+  const int per = (n + 1023) / 1024;
+  const int b0 = t * per, b1 = min(n, b0 + per);
+  int s = 0;
+  for (int b = b0; b < b1; ++b) s += blk[b];
+  part[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    int run = 0;
+    for (int j = 0; j < 1024; ++j) {
+      const int v = part[j];
+      part[j] = run;
+      run += v;
+    }
+    *total = run;
+  }
+  __syncthreads();
+  int run = part[t];
+  for (int b = b0; b < b1; ++b) {
+    const int v = blk[b];
+    blk[b] = run;
+    run += v;
+  }
+}
+
+__global__ void ccl_number(const int *__restrict__ parent, size_t V, const int *__restrict__ blk, int *__restrict__ ids,
+                           int *__restrict__ seed, int cap) {
+  const size_t i = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
+  const bool root = (i < V) && parent[i] == (int)i;
+  __shared__ int cnt[CCL_THREADS / 32];
+  const unsigned b = __ballot_sync(0xffffffffu, root);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) cnt[warp] = __popc(b);
+  __syncthreads();
+  if (root) {
+    int off = blk[blockIdx.x];
+    for (int w = 0; w < warp; ++w) off += cnt[w];
+    off += __popc(b & ((1u << lane) - 1u));
+    ids[i] = off;
+    if (off < cap) seed[off] = (int)i;
+  }
+}
+
+template <typename T>
+__global__ void ccl_stats(const T *__restrict__ phi, const float *__restrict__ cphi, const T *__restrict__ pi,
+                          const float *__restrict__ cpi, const int *__restrict__ parent, const int *__restrict__ ids,
+                          int N, const Consts k, int *__restrict__ size, double *__restrict__ sums,
+                          unsigned long long *__restrict__ peak2) {
+  const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = parent[i];
+    if (r < 0) continue;
+    const int id = ids[r];
+    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
+    const double c = val(phi, cphi, i), p = val(pi, cpi, i);
+    const double fx = val(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
+    const double fy = val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
+    const double fz = val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
+    // BFS accumulators (islands.cpp:131-198), static box, theories 0 and 1
+    const double grad = 0.5 * ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) / k.a2;
+    const double kin = 0.5 * (p * p);
+    const double c2 = c * c, c4 = c2 * c2;
+    double pot;
+    if (k.theory == 0)
+      pot = k.mm_half_M * c2 + k.lm * (c4 / k.c24) + (c4 * c2 / k.c720);
+    else
+      pot = (k.h * c + k.mm_half_M * c2 + k.lm * (c4 / k.c24));
+    atomicAdd(&size[id], 1);
+    atomicAdd(&sums[(size_t)id * 4 + 0], pot);
+    atomicAdd(&sums[(size_t)id * 4 + 1], kin);
+    atomicAdd(&sums[(size_t)id * 4 + 2], grad);
+    atomicAdd(&sums[(size_t)id * 4 + 3], c);
+    // phi^2 >= 0: its IEEE bit pattern orders like the value
+    atomicMax(&peak2[id], (unsigned long long)__double_as_longlong(c2));
+  }
+}
+
+template <typename T>
+__global__ void ccl_peak(const T *__restrict__ phi, const float *__restrict__ cphi, const int *__restrict__ parent,
+                         const int *__restrict__ ids, int N, const unsigned long long *__restrict__ peak2,
+                         long long *__restrict__ peakpos) {
+  const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = parent[i];
+    if (r < 0) continue;
+    const int id = ids[r];
+    const double c = val(phi, cphi, i);
+    if ((unsigned long long)__double_as_longlong(c * c) == peak2[id])
+      atomicMin(&peakpos[id], (long long)(i + NN));  // reference index (Nc = 1)
+  }
+}
+
+template <typename T>
+__global__ void ccl_peakval(const T *__restrict__ phi, const float *__restrict__ cphi, int N, int n,
+                            const long long *__restrict__ peakpos, double *__restrict__ peakval) {
+  const size_t NN = (size_t)N * N;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    peakval[j] = val(phi, cphi, (size_t)peakpos[j] - NN);
+}
+
+// labels in the reference layout: ghost slabs -1, interior island ids
+__global__ void ccl_labels(const int *__restrict__ parent, const int *__restrict__ ids, int N, int *__restrict__ out) {
+  const size_t NN = (size_t)N * N, V = NN * N, total = NN * (N + 2);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    int v = -1;
+    if (i >= NN && i < NN + V) {
+      const int r = parent[i - NN];
+      if (r >= 0) v = ids[r];
+    }
+    out[i] = v;
+  }
+}
+
+__global__ void fill_ll(long long *p, long long v, int n) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) p[j] = v;
+}
+
+static void free_isl_arrays(IslState *s) {
+  cudaFree(s->size);
+  cudaFree(s->sums);
+  cudaFree(s->peak2);
+  cudaFree(s->peakpos);
+  cudaFree(s->peakval);
+  cudaFree(s->seed);
+  s->size = nullptr;
+  s->sums = nullptr;
+  s->peak2 = nullptr;
+  s->peakpos = nullptr;
+  s->peakval = nullptr;
+  s->seed = nullptr;
+  s->cap = 0;
+}
+
+void islands_release(phn_handle *h) {
+  IslState *s = (IslState *)h->isl;
+  if (!s) return;
+  cudaFree(s->parent);
+  cudaFree(s->ids);
+  cudaFree(s->blk);
+  free_isl_arrays(s);
+  delete s;
+  h->isl = nullptr;
+}
+
+static int grid_blocks(size_t n) {
+  size_t b = (n + CCL_THREADS - 1) / CCL_THREADS;
+  if (b > 152 * 32) b = 152 * 32;
+  return (int)(b ? b : 1);
+}
+
+template <typename T>
+static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, int mode, int zper, int *labels,
+                       phn_island *out, int max_out, int *n_islands) {
+  const int N = h->p.N;
+  const size_t V = h->V;
+  cudaStream_t st = h->stream;
+  const float *cphi = h->p.precision == PHN_FP32_KAHAN ? h->cphi : nullptr;
+  const float *cpi = h->p.precision == PHN_FP32_KAHAN ? h->cpi : nullptr;
+  if (!h->isl) {
+    IslState *s = new IslState();
+    memset(s, 0, sizeof(*s));
+    h->isl = s;
+    s->nblk = (int)((V + CCL_THREADS - 1) / CCL_THREADS);
+    cudaError_t e = cudaMalloc(&s->parent, V * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->ids, V * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->blk, ((size_t)s->nblk + 1) * sizeof(int));
+    if (e != cudaSuccess) {
+      islands_release(h);
+      return cuda_error(e, "island buffers");
+    }
+  }
+  IslState *s = (IslState *)h->isl;
+  const double thr = mode == PHN_ISLAND_REFERENCE ? (thres * thres * 0.5) : thres;
+  const int gb = grid_blocks(V);
+  ccl_init<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, h->k, s->parent);
+  ccl_merge<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, zper);
+  ccl_compress<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk);
+  ccl_scan<<<1, 1024, 0, st>>>(s->blk, s->nblk, s->blk + s->nblk);
+  h->launches += 4;
+  int count = 0;
+  cudaError_t e = cudaMemcpyAsync(&count, s->blk + s->nblk, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_error(e, "island count");
+  if (count > s->cap) {
+    free_isl_arrays(s);
+    const int cap = count + count / 4 + 64;
+    e = cudaMalloc(&s->size, cap * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->sums, (size_t)cap * 4 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->peak2, cap * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&s->peakpos, cap * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&s->peakval, cap * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->seed, cap * sizeof(int));
+    if (e != cudaSuccess) {
+      free_isl_arrays(s);
+      return cuda_error(e, "island arrays");
+    }
+    s->cap = cap;
+  }
+  ccl_number<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk, s->ids, s->seed, s->cap);
+  h->launches++;
+  if (count > 0) {
+    cudaMemsetAsync(s->size, 0, count * sizeof(int), st);
+    cudaMemsetAsync(s->sums, 0, (size_t)count * 4 * sizeof(double), st);
+    cudaMemsetAsync(s->peak2, 0, count * sizeof(unsigned long long), st);
+    fill_ll<<<(count + 255) / 256, 256, 0, st>>>(s->peakpos, LLONG_MAX, count);
+    ccl_stats<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, h->k, s->size, s->sums,
+                                             s->peak2);
+    ccl_peak<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
+    ccl_peakval<T><<<(count + 255) / 256, 256, 0, st>>>(phi, cphi, N, count, s->peakpos, s->peakval);
+    h->launches += 4;
+  }
+  if (labels) {
+    const size_t total = (size_t)N * N * (N + 2);
+    int *d_lab = nullptr;
+    e = cudaMallocAsync((void **)&d_lab, total * sizeof(int), st);
+    if (e != cudaSuccess) return cuda_error(e, "label buffer");
+    ccl_labels<<<grid_blocks(total), CCL_THREADS, 0, st>>>(s->parent, s->ids, N, d_lab);
+    h->launches++;
+    e = cudaMemcpyAsync(labels, d_lab, total * sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d_lab, st);
+    if (e != cudaSuccess) return cuda_error(e, "label readback");
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "island kernels");
+  const int n_out = count < max_out ? count : max_out;
+  if (out && n_out > 0) {
+    std::vector<int> size(n_out), seed(n_out);
+    std::vector<double> sums((size_t)n_out * 4), pval(n_out);
+    std::vector<long long> ppos(n_out);
+    e = cudaMemcpyAsync(size.data(), s->size, n_out * sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(seed.data(), s->seed, n_out * sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(sums.data(), s->sums, (size_t)n_out * 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pval.data(), s->peakval, n_out * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(ppos.data(), s->peakpos, n_out * sizeof(long long), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "island readback");
+    const double a = h->p.a, cell = (a * a) * a;
+    const size_t NN = (size_t)N * N;
+    for (int j = 0; j < n_out; ++j) {
+      phn_island &I = out[j];
+      I.index = j;
+      I.size = size[j];
+      I.volume = size[j] * a * a * a;  // cV = NN*a_t*a_t*a_eta (islands.cpp:241)
+      I.pot_en = sums[(size_t)j * 4 + 0] * cell;
+      I.kin_en = sums[(size_t)j * 4 + 1] * cell;
+      I.grad_en = sums[(size_t)j * 4 + 2] * cell;
+      I.av_phi = sums[(size_t)j * 4 + 3] / (double)size[j];
+      I.peak_pos = (double)ppos[j];
+      I.peak_value = pval[j];
+      I.seed_pos = (double)((size_t)seed[j] + NN);
+    }
+  } else {
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "islands");
+  }
+  if (n_islands) *n_islands = count;
+  if (out && count > max_out) return set_error(PHN_ERR_TRUNCATED, "%d islands, %d records written", count, max_out);
+  return PHN_OK;
+}
+
+}  // namespace phn
+
+using namespace phn;
+
+extern "C" int phn_islands(phn_handle *h, double thres, int mode, int z_periodic, int *labels, phn_island *out,
+                           int max_out, int *n_islands) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (h->p.Nc != 1) return set_error(PHN_ERR_UNSUPPORTED, "islands need Nc == 1");
+  if (mode != PHN_ISLAND_REFERENCE && mode != PHN_ISLAND_ENERGY) return set_error(PHN_ERR_INVALID, "mode %d", mode);
+  if (h->V > (size_t)0x7fffffff) return set_error(PHN_ERR_UNSUPPORTED, "lattice too large for 32-bit labels");
+  if (max_out < 0) return set_error(PHN_ERR_INVALID, "max_out < 0");
+  if (h->p.precision == PHN_FP64)
+    return run_islands<double>(h, (const double *)h->phi[h->cur], (const double *)h->pi, thres, mode, z_periodic,
+                               labels, out, max_out, n_islands);
+  return run_islands<float>(h, (const float *)h->phi[h->cur], (const float *)h->pi, thres, mode, z_periodic, labels,
+                            out, max_out, n_islands);
+}

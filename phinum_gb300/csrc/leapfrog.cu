@@ -1,0 +1,531 @@
+// Fused leapfrog step: kick (7-point Laplacian + potential force), drift into
+// the second phi buffer, and optionally the volume averages and extrema of the
+// state the step starts from -- all in one pass over HBM.
+//
+// Replaces updateMomenta + updateFields + Communication::exchange
+// (dynamics.cpp:52-194, comm.cpp:63-78) and, on observation steps,
+// CalculateVolumeAverages + CalculateExtrema (fieldanalysis.cpp:319-699).
+// The periodic halo is in-kernel modular indexing; the MPI reductions become a
+// deterministic two-stage tree (warp shuffles + shared memory per block, then
+// finalize_averages over the block records in a fixed order).
+//
+// Work decomposition: a block is 32 x-sites by 8 y-rows and marches a chunk of
+// z-planes, carrying phi(z-1), phi(z), phi(z+1) in registers, so every plane
+// of phi is fetched from HBM once per chunk; x/y neighbours hit L1/L2.
+#include <math.h>
+
+#include "phn_internal.h"
+
+namespace phn {
+
+// ----------------------------------------------------------- accumulators
+struct Acc {
+  double s[NSUM];
+  double minv, maxv, absv;
+  long long mini, maxi, absi;
+  __device__ void init() {
+#pragma unroll
+    for (int j = 0; j < NSUM; ++j) s[j] = 0.0;
+    // CalculateExtrema's starting values (fieldanalysis.cpp:324-325)
+    minv = 10000000.0;
+    maxv = -10000000.0;
+    absv = 0.0;
+    mini = maxi = absi = LLONG_MAX;
+  }
+  // Strict comparisons as in the reference; equal values keep the smaller
+  // index, which is the first one the reference's linear scan meets.
+  __device__ void take_max(double v, long long i) {
+    if (v > maxv || (v == maxv && i < maxi && v > -10000000.0)) { maxv = v; maxi = i; }
+  }
+  __device__ void take_min(double v, long long i) {
+    if (v < minv || (v == minv && i < mini && v < 10000000.0)) { minv = v; mini = i; }
+  }
+  __device__ void take_abs(double v, long long i) {
+    if (v > absv || (v == absv && i < absi && v > 0.0)) { absv = v; absi = i; }
+  }
+};
+
+__device__ __forceinline__ void combine(Acc &a, const Acc &b) {
+#pragma unroll
+  for (int j = 0; j < NSUM; ++j) a.s[j] += b.s[j];
+  if (b.maxi != LLONG_MAX) a.take_max(b.maxv, b.maxi);
+  if (b.mini != LLONG_MAX) a.take_min(b.minv, b.mini);
+  if (b.absi != LLONG_MAX) a.take_abs(b.absv, b.absi);
+}
+
+__device__ __forceinline__ Acc shfl_down(const Acc &a, int off) {
+  Acc b;
+#pragma unroll
+  for (int j = 0; j < NSUM; ++j) b.s[j] = __shfl_down_sync(0xffffffffu, a.s[j], off);
+  b.minv = __shfl_down_sync(0xffffffffu, a.minv, off);
+  b.maxv = __shfl_down_sync(0xffffffffu, a.maxv, off);
+  b.absv = __shfl_down_sync(0xffffffffu, a.absv, off);
+  b.mini = __shfl_down_sync(0xffffffffu, a.mini, off);
+  b.maxi = __shfl_down_sync(0xffffffffu, a.maxi, off);
+  b.absi = __shfl_down_sync(0xffffffffu, a.absi, off);
+  return b;
+}
+
+__device__ __forceinline__ void store_rec(double *r, const Acc &a) {
+#pragma unroll
+  for (int j = 0; j < NSUM; ++j) r[j] = a.s[j];
+  r[E_MIN_V] = a.minv;
+  r[E_MIN_I] = __longlong_as_double(a.mini);
+  r[E_MAX_V] = a.maxv;
+  r[E_MAX_I] = __longlong_as_double(a.maxi);
+  r[E_ABS_V] = a.absv;
+  r[E_ABS_I] = __longlong_as_double(a.absi);
+}
+
+__device__ __forceinline__ void load_rec(Acc &a, const double *r) {
+#pragma unroll
+  for (int j = 0; j < NSUM; ++j) a.s[j] = r[j];
+  a.minv = r[E_MIN_V];
+  a.mini = __double_as_longlong(r[E_MIN_I]);
+  a.maxv = r[E_MAX_V];
+  a.maxi = __double_as_longlong(r[E_MAX_I]);
+  a.absv = r[E_ABS_V];
+  a.absi = __double_as_longlong(r[E_ABS_I]);
+}
+
+// Fixed-order block reduction; the block's record goes to partials.
+__device__ void block_store(Acc &acc, double *partials) {
+  __shared__ double sh[THREADS / 32][REC];
+  const int tid = threadIdx.x + TX * threadIdx.y;
+  const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    Acc o = shfl_down(acc, off);
+    combine(acc, o);
+  }
+  if (lane == 0) store_rec(sh[warp], acc);
+  __syncthreads();
+  if (warp == 0) {
+    Acc a;
+    a.init();
+    if (lane < THREADS / 32) load_rec(a, sh[lane]);
+#pragma unroll
+    for (int off = 4; off > 0; off >>= 1) {
+      Acc o = shfl_down(a, off);
+      combine(a, o);
+    }
+    if (lane == 0) {
+      const size_t b = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
+      store_rec(partials + b * REC, a);
+    }
+  }
+}
+
+// Per-site observation terms, each computed with the reference's expression
+// (fieldanalysis.cpp:331-355 and 433-616).  c, p: phi and pi of the site;
+// fxp, fyp, fzp: forward neighbours of phi; kidx: reference index of
+// component 0 of the site.
+template <int NC, int THEORY>
+__device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c, const double *p,
+                                        const double *fxp, const double *fyp, const double *fzp,
+                                        long long kidx) {
+  double l = 0.0, inter = 0.0;
+#pragma unroll
+  for (int a = 0; a < NC; ++a) {
+    A.s[S_PHI + a] += c[a];
+    A.s[S_PI + a] += p[a];
+    const double c2 = __dmul_rn(c[a], c[a]);
+    A.s[S_PHI2] += c2;
+    A.s[S_PI2] += __dmul_rn(p[a], p[a]);
+    A.s[S_PHIPI] += __dmul_rn(c[a], p[a]);
+    l = __dadd_rn(l, c2);
+    const double dx = __dadd_rn(fxp[a], -c[a]), dy = __dadd_rn(fyp[a], -c[a]), dz = __dadd_rn(fzp[a], -c[a]);
+    A.s[S_GRAD] += __dadd_rn(__dadd_rn(__dmul_rn(dx, dx) / k.a2, __dmul_rn(dy, dy) / k.a2),
+                             __dmul_rn(dz, dz) / k.a2);
+    double term = __dmul_rn(k.mm_half_M, c2);
+    if (THEORY == 1 && a == 0) term = __dadd_rn(__dmul_rn(k.h, c[a]), term);
+    inter += term;
+    if (!isfinite(c[a]) || !isfinite(p[a])) A.s[S_NONFINITE] += 1.0;
+    A.take_max(c[a], kidx + a);
+    A.take_min(c[a], kidx + a);
+  }
+  const double l2 = __dmul_rn(l, l);
+  A.s[S_PHI4] += l2;
+  A.s[S_PHI6] += __dmul_rn(l2, l);
+  if (THEORY == 0)
+    inter += __dadd_rn(__dmul_rn(k.lm, l2 / k.c24), __dmul_rn(l2, l) / k.c720);
+  else
+    inter += __dmul_rn(k.lm, l2 / k.c24);
+  A.s[S_INTER] += inter;
+  A.take_abs(sqrt(l), kidx);
+}
+
+// ----------------------------------------------------------- FP64 kernel
+// The kick and drift use explicit round-to-nearest intrinsics and IEEE
+// division in the reference's operation order (dynamics.cpp:80-84,96-100,183),
+// so every site value is bit-identical to the reference's FP64 build.
+template <int NC, int THEORY, int MODE>
+__global__ void __launch_bounds__(THREADS) step_f64(const double *__restrict__ phi, double *__restrict__ phi_out,
+                                                    double *__restrict__ pi, const Consts k, const StepF s,
+                                                    const int cz, double *__restrict__ partials) {
+  const int N = k.N;
+  const int x = blockIdx.x * TX + threadIdx.x;
+  const int y = blockIdx.y * TY + threadIdx.y;
+  const int z0 = blockIdx.z * cz;
+  const int z1 = min(z0 + cz, N);
+  const size_t NN = (size_t)N * N, V = NN * N;
+  Acc acc;
+  if (MODE != MODE_STEP) acc.init();
+  if (x < N && y < N && z0 < z1) {
+    const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
+    const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
+    double cm[NC], c[NC], cp[NC];
+    const size_t col = (size_t)y * N + x;
+    const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
+#pragma unroll
+    for (int a = 0; a < NC; ++a) {
+      cm[a] = phi[a * V + zm0 * NN + col];
+      c[a] = phi[a * V + z0 * NN + col];
+    }
+    for (int z = z0; z < z1; ++z) {
+      const int zn = (z + 1 == N) ? 0 : z + 1;
+      const size_t pl = (size_t)z * NN;
+      double fxp[NC], fxm[NC], fyp[NC], fym[NC], p[NC];
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        cp[a] = phi[a * V + zn * NN + col];
+        fxp[a] = phi[a * V + pl + (size_t)y * N + xp];
+        fxm[a] = phi[a * V + pl + (size_t)y * N + xm];
+        fyp[a] = phi[a * V + pl + (size_t)yp * N + x];
+        fym[a] = phi[a * V + pl + (size_t)ym * N + x];
+        p[a] = pi[a * V + pl + col];
+      }
+      if (MODE != MODE_STEP)
+        observe<NC, THEORY>(acc, k, c, p, fxp, fyp, cp, (long long)NC * (long long)(col + (size_t)(z + 1) * NN));
+      if (MODE != MODE_OBS) {
+        double l = 0.0;
+#pragma unroll
+        for (int a = 0; a < NC; ++a) l = __dadd_rn(l, __dmul_rn(c[a], c[a]));
+        double coef = __dadd_rn(k.mmM, __dmul_rn(k.lm, l / k.six_nc));
+        if (THEORY == 0) {
+          const double r = l / k.kappa;
+          coef = __dadd_rn(coef, __dmul_rn(r, r) / k.c120);
+        }
+#pragma unroll
+        for (int a = 0; a < NC; ++a) {
+          const double sum = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(fxp[a], fxm[a]), fyp[a]), fym[a]), cp[a]), cm[a]);
+          const double lap = __dadd_rn(sum, -__dmul_rn(6.0, c[a])) / k.a2;
+          double f = lap;
+          if (THEORY == 1 && a == 0) f = __dadd_rn(f, -k.h);
+          f = __dadd_rn(f, -__dmul_rn(coef, c[a]));
+          const double pn = __dadd_rn(p[a], __dmul_rn(f, s.fk));
+          pi[a * V + pl + col] = pn;
+          phi_out[a * V + pl + col] = __dadd_rn(c[a], __dmul_rn(pn, s.fd));
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        cm[a] = c[a];
+        c[a] = cp[a];
+      }
+    }
+  }
+  if (MODE != MODE_STEP) block_store(acc, partials);
+}
+
+// ----------------------------------------------------------- FP32 kernel
+template <int NC, int THEORY, int MODE>
+__global__ void __launch_bounds__(THREADS) step_f32(const float *__restrict__ phi, float *__restrict__ phi_out,
+                                                    float *__restrict__ pi, const Consts k, const float fk,
+                                                    const float fd, const int cz, double *__restrict__ partials) {
+  const int N = k.N;
+  const int x = blockIdx.x * TX + threadIdx.x;
+  const int y = blockIdx.y * TY + threadIdx.y;
+  const int z0 = blockIdx.z * cz;
+  const int z1 = min(z0 + cz, N);
+  const size_t NN = (size_t)N * N, V = NN * N;
+  Acc acc;
+  if (MODE != MODE_STEP) acc.init();
+  if (x < N && y < N && z0 < z1) {
+    const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
+    const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
+    float cm[NC], c[NC], cp[NC];
+    const size_t col = (size_t)y * N + x;
+    const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
+#pragma unroll
+    for (int a = 0; a < NC; ++a) {
+      cm[a] = __ldg(phi + a * V + zm0 * NN + col);
+      c[a] = __ldg(phi + a * V + z0 * NN + col);
+    }
+    for (int z = z0; z < z1; ++z) {
+      const int zn = (z + 1 == N) ? 0 : z + 1;
+      const size_t pl = (size_t)z * NN;
+      float fxp[NC], fxm[NC], fyp[NC], fym[NC], p[NC];
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        cp[a] = __ldg(phi + a * V + zn * NN + col);
+        fxp[a] = __ldg(phi + a * V + pl + (size_t)y * N + xp);
+        fxm[a] = __ldg(phi + a * V + pl + (size_t)y * N + xm);
+        fyp[a] = __ldg(phi + a * V + pl + (size_t)yp * N + x);
+        fym[a] = __ldg(phi + a * V + pl + (size_t)ym * N + x);
+        p[a] = pi[a * V + pl + col];
+      }
+      if (MODE != MODE_STEP) {
+        double cd[NC], pd[NC], xd[NC], yd[NC], zd[NC];
+#pragma unroll
+        for (int a = 0; a < NC; ++a) {
+          cd[a] = c[a]; pd[a] = p[a]; xd[a] = fxp[a]; yd[a] = fyp[a]; zd[a] = cp[a];
+        }
+        observe<NC, THEORY>(acc, k, cd, pd, xd, yd, zd, (long long)NC * (long long)(col + (size_t)(z + 1) * NN));
+      }
+      if (MODE != MODE_OBS) {
+        float l = 0.f;
+#pragma unroll
+        for (int a = 0; a < NC; ++a) l = fmaf(c[a], c[a], l);
+        float coef = fmaf(l, k.c4_f, k.mmM_f);
+        if (THEORY == 0) coef = fmaf(l * l, k.c6_f, coef);
+#pragma unroll
+        for (int a = 0; a < NC; ++a) {
+          const float lap = (((fxp[a] + fxm[a]) + (fyp[a] + fym[a])) + (cp[a] + cm[a]) - 6.f * c[a]) * k.inv_a2_f;
+          float f = fmaf(-coef, c[a], lap);
+          if (THEORY == 1 && a == 0) f -= k.h_f;
+          const float pn = fmaf(fk, f, p[a]);
+          pi[a * V + pl + col] = pn;
+          phi_out[a * V + pl + col] = fmaf(fd, pn, c[a]);
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        cm[a] = c[a];
+        c[a] = cp[a];
+      }
+    }
+  }
+  if (MODE != MODE_STEP) block_store(acc, partials);
+}
+
+// ------------------------------------------------ compensated FP32 kernel
+// phi, pi in FP32 with FP32 compensation terms (Kahan): the represented
+// value is hi - comp.  Kick and drift add their increments with Kahan's
+// update, so the rounding error of each addition is carried instead of lost.
+// comp arrays are per site (no stencil reads), updated in place.
+template <int NC, int THEORY, int MODE>
+__global__ void __launch_bounds__(THREADS) step_kahan(const float *__restrict__ phi, float *__restrict__ phi_out,
+                                                      float *__restrict__ cphi, float *__restrict__ pi,
+                                                      float *__restrict__ cpi, const Consts k, const float fk,
+                                                      const float fd, const int cz, double *__restrict__ partials) {
+  const int N = k.N;
+  const int x = blockIdx.x * TX + threadIdx.x;
+  const int y = blockIdx.y * TY + threadIdx.y;
+  const int z0 = blockIdx.z * cz;
+  const int z1 = min(z0 + cz, N);
+  const size_t NN = (size_t)N * N, V = NN * N;
+  Acc acc;
+  if (MODE != MODE_STEP) acc.init();
+  if (x < N && y < N && z0 < z1) {
+    const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
+    const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
+    float cm[NC], c[NC], cp[NC];
+    const size_t col = (size_t)y * N + x;
+    const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
+#pragma unroll
+    for (int a = 0; a < NC; ++a) {
+      cm[a] = __ldg(phi + a * V + zm0 * NN + col);
+      c[a] = __ldg(phi + a * V + z0 * NN + col);
+    }
+    for (int z = z0; z < z1; ++z) {
+      const int zn = (z + 1 == N) ? 0 : z + 1;
+      const size_t pl = (size_t)z * NN;
+      float fxp[NC], fxm[NC], fyp[NC], fym[NC], p[NC], ec[NC], ep[NC];
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        cp[a] = __ldg(phi + a * V + zn * NN + col);
+        fxp[a] = __ldg(phi + a * V + pl + (size_t)y * N + xp);
+        fxm[a] = __ldg(phi + a * V + pl + (size_t)y * N + xm);
+        fyp[a] = __ldg(phi + a * V + pl + (size_t)yp * N + x);
+        fym[a] = __ldg(phi + a * V + pl + (size_t)ym * N + x);
+        p[a] = pi[a * V + pl + col];
+        ec[a] = cphi[a * V + pl + col];
+        ep[a] = cpi[a * V + pl + col];
+      }
+      if (MODE != MODE_STEP) {
+        // observables of the represented values hi - comp (neighbours: hi only)
+        double cd[NC], pd[NC], xd[NC], yd[NC], zd[NC];
+#pragma unroll
+        for (int a = 0; a < NC; ++a) {
+          cd[a] = (double)c[a] - (double)ec[a];
+          pd[a] = (double)p[a] - (double)ep[a];
+          xd[a] = fxp[a]; yd[a] = fyp[a]; zd[a] = cp[a];
+        }
+        observe<NC, THEORY>(acc, k, cd, pd, xd, yd, zd, (long long)NC * (long long)(col + (size_t)(z + 1) * NN));
+      }
+      if (MODE != MODE_OBS) {
+        float l = 0.f;
+#pragma unroll
+        for (int a = 0; a < NC; ++a) l = fmaf(c[a], c[a], l);
+        float coef = fmaf(l, k.c4_f, k.mmM_f);
+        if (THEORY == 0) coef = fmaf(l * l, k.c6_f, coef);
+#pragma unroll
+        for (int a = 0; a < NC; ++a) {
+          const float lap = (((fxp[a] + fxm[a]) + (fyp[a] + fym[a])) + (cp[a] + cm[a]) - 6.f * c[a]) * k.inv_a2_f;
+          float f = fmaf(-coef, c[a], lap);
+          if (THEORY == 1 && a == 0) f -= k.h_f;
+          // kick: pi += fk * f  (Kahan)
+          const float yk = __fsub_rn(__fmul_rn(fk, f), ep[a]);
+          const float tk = __fadd_rn(p[a], yk);
+          const float ek = __fsub_rn(__fsub_rn(tk, p[a]), yk);
+          // drift: phi += fd * pi_new  (Kahan); the increment uses the
+          // represented momentum tk - ek
+          const float yd = __fsub_rn(__fmul_rn(fd, __fsub_rn(tk, ek)), ec[a]);
+          const float td = __fadd_rn(c[a], yd);
+          const float ed = __fsub_rn(__fsub_rn(td, c[a]), yd);
+          pi[a * V + pl + col] = tk;
+          cpi[a * V + pl + col] = ek;
+          phi_out[a * V + pl + col] = td;
+          cphi[a * V + pl + col] = ed;
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        cm[a] = c[a];
+        c[a] = cp[a];
+      }
+    }
+  }
+  if (MODE != MODE_STEP) block_store(acc, partials);
+}
+
+// ----------------------------------------------------------- finalize
+constexpr int FIN_THREADS = 128;
+
+// Folds the block records in a fixed order and forms the reference's derived
+// quantities (fieldanalysis.cpp:619-638): Energy, Charge, Interaction and the
+// per-volume moments.
+__global__ void __launch_bounds__(FIN_THREADS) finalize_averages(const double *__restrict__ partials, int nblocks,
+                                                                 const Consts k, phn_averages *__restrict__ out) {
+  __shared__ double sh[FIN_THREADS][REC];
+  const int t = threadIdx.x;
+  Acc a;
+  a.init();
+  for (int b = t; b < nblocks; b += FIN_THREADS) {
+    Acc o;
+    load_rec(o, partials + (size_t)b * REC);
+    combine(a, o);
+  }
+  store_rec(sh[t], a);
+  __syncthreads();
+  for (int w = FIN_THREADS / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      Acc x, y;
+      load_rec(x, sh[t]);
+      load_rec(y, sh[t + w]);
+      combine(x, y);
+      store_rec(sh[t], x);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    Acc r;
+    load_rec(r, sh[0]);
+    const double vol = (double)(k.N * k.N * k.N);
+    phn_averages o;
+    o.t = 0.0;
+    for (int c = 0; c < PHN_MAX_NC; ++c) {
+      o.phi[c] = c < k.Nc ? r.s[S_PHI + c] / vol : 0.0;
+      o.pi[c] = c < k.Nc ? r.s[S_PI + c] / vol : 0.0;
+    }
+    const double pi2 = r.s[S_PI2], grad = r.s[S_GRAD], inter = r.s[S_INTER];
+    const double charge = (0.5 * pi2 - grad / 6. - inter);
+    const double energy = (0.5 * pi2 + 0.5 * grad + inter);
+    o.energy = energy / vol;
+    o.interaction = inter / vol;
+    o.charge = charge / vol;
+    o.phi2 = r.s[S_PHI2] / vol;
+    o.pi2 = pi2 / vol;
+    o.phi4 = r.s[S_PHI4] / vol;
+    o.phi6 = r.s[S_PHI6] / vol;
+    o.phipi = r.s[S_PHIPI] / vol;
+    o.min_phi = r.minv;
+    o.max_phi = r.maxv;
+    o.max_abs_phi = r.absv;
+    o.min_pos = r.mini == LLONG_MAX ? -1.0 : (double)r.mini;
+    o.max_pos = r.maxi == LLONG_MAX ? -1.0 : (double)r.maxi;
+    o.max_abs_pos = r.absi == LLONG_MAX ? -1.0 : (double)r.absi;
+    o.gradient = grad / vol;
+    o.nonfinite = r.s[S_NONFINITE];
+    o.reserved = 0.0;
+    *out = o;
+  }
+}
+
+// ----------------------------------------------------------- launchers
+Grid lattice_grid(int N) {
+  Grid g;
+  g.block = dim3(TX, TY, 1);
+  const int gx = (N + TX - 1) / TX, gy = (N + TY - 1) / TY;
+  int cz;
+  if (N >= 256)
+    cz = 16;
+  else if (N >= 128)
+    cz = 8;
+  else {
+    // small lattices: enough blocks to fill the GPU, planes per block >= 1
+    const long long cols = (long long)gx * gy;
+    const long long want = 152LL * 8;
+    const long long gz = (want + cols - 1) / cols;
+    cz = (int)((N + gz - 1) / gz);
+    if (cz < 1) cz = 1;
+  }
+  const int gz = (N + cz - 1) / cz;
+  g.grid = dim3(gx, gy, gz);
+  g.cz = cz;
+  g.nblocks = gx * gy * gz;
+  return g;
+}
+
+#define PHN_DISPATCH_NC(NCV, ...)                              \
+  switch (NCV) {                                               \
+    case 1: { constexpr int NC_ = 1; __VA_ARGS__; } break;     \
+    case 2: { constexpr int NC_ = 2; __VA_ARGS__; } break;     \
+    case 3: { constexpr int NC_ = 3; __VA_ARGS__; } break;     \
+    case 4: { constexpr int NC_ = 4; __VA_ARGS__; } break;     \
+    default: return cudaErrorInvalidValue;                     \
+  }
+
+#define PHN_DISPATCH_TH(THV, ...)                              \
+  if ((THV) == 0) { constexpr int TH_ = 0; __VA_ARGS__; }      \
+  else { constexpr int TH_ = 1; __VA_ARGS__; }
+
+#define PHN_DISPATCH_MODE(MV, ...)                             \
+  if ((MV) == MODE_STEP) { constexpr int MD_ = MODE_STEP; __VA_ARGS__; }          \
+  else if ((MV) == MODE_STEP_OBS) { constexpr int MD_ = MODE_STEP_OBS; __VA_ARGS__; } \
+  else { constexpr int MD_ = MODE_OBS; __VA_ARGS__; }
+
+cudaError_t launch_step_f64(const Consts &k, const Grid &g, int mode, const double *phi, double *phi_out,
+                            double *pi, StepF s, double *partials, cudaStream_t st) {
+  PHN_DISPATCH_NC(k.Nc, PHN_DISPATCH_TH(k.theory, PHN_DISPATCH_MODE(mode,
+      step_f64<NC_, TH_, MD_><<<g.grid, g.block, 0, st>>>(phi, phi_out, pi, k, s, g.cz, partials))));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_f32(const Consts &k, const Grid &g, int mode, const float *phi, float *phi_out,
+                            float *pi, StepF s, double *partials, cudaStream_t st) {
+  const float fk = (float)s.fk, fd = (float)s.fd;
+  PHN_DISPATCH_NC(k.Nc, PHN_DISPATCH_TH(k.theory, PHN_DISPATCH_MODE(mode,
+      step_f32<NC_, TH_, MD_><<<g.grid, g.block, 0, st>>>(phi, phi_out, pi, k, fk, fd, g.cz, partials))));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_kahan(const Consts &k, const Grid &g, int mode, const float *phi, float *phi_out,
+                              const float *cphi, float *cphi_out, float *pi, float *cpi, StepF s,
+                              double *partials, cudaStream_t st) {
+  (void)cphi;
+  const float fk = (float)s.fk, fd = (float)s.fd;
+  PHN_DISPATCH_NC(k.Nc, PHN_DISPATCH_TH(k.theory, PHN_DISPATCH_MODE(mode,
+      step_kahan<NC_, TH_, MD_><<<g.grid, g.block, 0, st>>>(phi, phi_out, cphi_out, pi, cpi, k, fk, fd, g.cz,
+                                                            partials))));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const Consts &k, const double *partials, int nblocks, phn_averages *out,
+                            cudaStream_t st) {
+  finalize_averages<<<1, FIN_THREADS, 0, st>>>(partials, nblocks, k, out);
+  return cudaGetLastError();
+}
+
+}  // namespace phn

@@ -1,0 +1,136 @@
+// Internal declarations shared by the CUDA translation units of libphinum_gpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/phinum_gpu.h"
+
+namespace phn {
+
+// Block shape of the lattice kernels: 32 x-sites (one warp) by 8 y-rows,
+// each thread marching a chunk of z-planes.
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int THREADS = TX * TY;
+
+// Observation record written per block by the step kernels and folded by
+// finalize_averages.  Sums are FP64.
+enum {
+  S_PHI = 0,   // [PHN_MAX_NC]
+  S_PI = 4,    // [PHN_MAX_NC]
+  S_PHI2 = 8,
+  S_PI2,
+  S_PHIPI,
+  S_PHI4,
+  S_PHI6,
+  S_GRAD,
+  S_INTER,
+  S_NONFINITE,
+  NSUM,        // 16
+  E_MIN_V = NSUM,
+  E_MIN_I,
+  E_MAX_V,
+  E_MAX_I,
+  E_ABS_V,
+  E_ABS_I,
+  REC = 24     // doubles per block record (padded)
+};
+
+// Coefficients of the kick, the volume averages and the energy density,
+// evaluated on the host with the reference's own expressions so that the FP64
+// kernels combine exactly the same IEEE values.
+struct Consts {
+  int N, Nc, theory;
+  double a2;         // sqr(a_t)
+  double mmM;        // Mass_Mode * BareM_sqr_long
+  double lm;         // (double)Lambda_Mode
+  double six_nc;     // 6.*Nc
+  double kappa;      // Kappa
+  double c120;       // 120.*Nc*Nc
+  double h;          // h
+  double mm_half_M;  // (Mass_Mode)*0.5*BareM_sqr_long
+  double c24;        // 24.0*Nc
+  double c720;       // 720.0*Nc*Nc*Kappa*Kappa
+  // FP32 forms of the kick
+  float inv_a2_f, mmM_f, c4_f, c6_f, h_f;
+  // FP32 forms of the energy density
+  float mmh_f, e4_f, e6_f;
+};
+
+// Per-step kick and drift factors: tau - Last_Momenta_update and
+// tau - Last_Field_update (dynamics.cpp:84,183).
+struct StepF {
+  double fk, fd;
+};
+
+enum StepMode { MODE_STEP = 0, MODE_STEP_OBS = 1, MODE_OBS = 2 };
+
+struct Grid {
+  dim3 grid, block;
+  int cz;          // z-planes per block
+  int nblocks;     // grid.x * grid.y * grid.z
+};
+Grid lattice_grid(int N);
+
+// Launchers (leapfrog.cu).  Return cudaGetLastError().
+cudaError_t launch_step_f64(const Consts &k, const Grid &g, int mode, const double *phi, double *phi_out,
+                            double *pi, StepF s, double *partials, cudaStream_t st);
+cudaError_t launch_step_f32(const Consts &k, const Grid &g, int mode, const float *phi, float *phi_out,
+                            float *pi, StepF s, double *partials, cudaStream_t st);
+cudaError_t launch_step_kahan(const Consts &k, const Grid &g, int mode, const float *phi, float *phi_out,
+                              const float *cphi, float *cphi_out, float *pi, float *cpi, StepF s,
+                              double *partials, cudaStream_t st);
+cudaError_t launch_finalize(const Consts &k, const double *partials, int nblocks, phn_averages *out,
+                            cudaStream_t st);
+
+// Layout conversion between the reference layout (host order, ghosts) and
+// the device SoA layout [a][z][y][x] (layout.cu).
+cudaError_t launch_from_ref(const double *ref, void *dst, int prec, int N, int Nc, cudaStream_t st);
+cudaError_t launch_to_ref(const void *src, double *ref, int prec, int N, int Nc, cudaStream_t st);
+cudaError_t launch_to_ref_kahan(const float *hi, const float *comp, double *ref, int N, int Nc,
+                                cudaStream_t st);
+cudaError_t launch_from_ref_kahan(const double *ref, float *hi, float *comp, int N, int Nc, cudaStream_t st);
+
+// Error text for phn_last_error (api.cu).
+int set_error(int code, const char *fmt, ...);
+int cuda_error(cudaError_t e, const char *what);
+
+}  // namespace phn
+
+// The handle behind the opaque phn_handle pointer.
+struct phn_handle {
+  phn_params p;
+  phn::Consts k;
+  phn::Grid grid;
+  int device;
+  cudaStream_t stream;
+  size_t V;            // sites per component
+  size_t elem;         // bytes per field element
+  void *phi[2];        // double-buffered phi
+  void *pi;
+  float *cphi, *cpi;   // compensation terms (PHN_FP32_KAHAN)
+  int cur;             // phi[cur] holds the current field
+  double *partials;    // block records of the fused observation
+  phn_averages *d_avg; // finalize output (device)
+  phn_averages *h_avg; // pinned host mirror, one per row slot
+  int h_avg_cap;
+  double *d_ref;       // reference-layout staging for upload/download
+  // reference clock (dynamics.cpp:8-50)
+  double tau, dtau, last_mom, last_field;
+  int steps;
+  // accounting
+  long long launches;
+  cudaEvent_t ev0, ev1;
+  double last_ms;
+  int last_steps;
+  // spectrum (spectrum.cu)
+  void *spec;
+  // islands (islands.cu)
+  void *isl;
+};
+
+namespace phn {
+void spectrum_release(phn_handle *h);
+void islands_release(phn_handle *h);
+}  // namespace phn

@@ -1,0 +1,164 @@
+"""Python mirror of the reference's hot-path entry points over the C ABI.
+
+One `Lattice` is one reference run: `LocalLattice` fields on the GPU plus the
+reference clock.  Method names follow the reference functions they replace:
+
+    reset()                     dynamics.cpp:28-50
+    evolve(n)                   n x evolve(), dynamics.cpp:196-237
+    volume_averages()           CalculateExtrema + CalculateVolumeAverages,
+                                fieldanalysis.cpp:319-699
+    run_loop(n, TSO)            main.cpp:685-699 with Print_AveragesExtrema's cadence
+    correlation_functions()     Calculate_CorrelationFunctions, momentumspace.cpp:140-278
+    full_analysis(thres)        Full_Analysis seeding, islands.cpp:778-840
+
+Arrays are numpy float64 in the reference layout (Nc*N*N*(N+2), ghost slabs).
+Errors raise PhnError carrying the library's status code.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+@dataclass
+class Params:
+    """Reference run parameters (parameters.cpp:84-201)."""
+    N: int = 64
+    Nc: int = 1
+    theory: int = 0
+    mass_mode: int = 1
+    lambda_mode: int = -1
+    precision: int = L.FP64
+    a: float = 0.25
+    dt: float = 0.08
+    T0: float = 0.0
+    m_sqr: float = 1.0
+    kappa: float = 3.0 ** 0.5
+    h: float = 0.0
+
+    def c(self) -> L.PhnParams:
+        return L.PhnParams(self.N, self.Nc, self.theory, self.mass_mode, self.lambda_mode, self.precision,
+                           self.a, self.dt, self.T0, self.m_sqr, self.kappa, self.h)
+
+    @property
+    def field_len(self) -> int:
+        return self.Nc * self.N * self.N * (self.N + 2)
+
+
+def _pd(a: np.ndarray):
+    return a.ctypes.data_as(L._PD)
+
+
+def _pi(a: np.ndarray):
+    return a.ctypes.data_as(L._PI)
+
+
+def avg_array(a: L.PhnAverages) -> np.ndarray:
+    return np.frombuffer(bytes(a), dtype=np.float64).copy()
+
+
+class Lattice:
+    def __init__(self, p: Params):
+        self.p = p
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        L.check(self.lib.phn_create(ctypes.byref(p.c()), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.phn_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------- fields
+    def upload(self, phi: np.ndarray, pi: np.ndarray):
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        pi = np.ascontiguousarray(pi, dtype=np.float64)
+        assert phi.size == self.p.field_len and pi.size == self.p.field_len
+        L.check(self.lib.phn_upload(self.h, _pd(phi), _pd(pi)))
+
+    def download(self):
+        phi = np.zeros(self.p.field_len)
+        pi = np.zeros(self.p.field_len)
+        L.check(self.lib.phn_download(self.h, _pd(phi), _pd(pi)))
+        return phi, pi
+
+    # -------------------------------------------------------------- clock
+    def reset(self):
+        L.check(self.lib.phn_reset(self.h))
+
+    def evolve(self, n: int):
+        L.check(self.lib.phn_evolve(self.h, int(n)))
+
+    def time(self):
+        t, s = ctypes.c_double(), ctypes.c_int()
+        L.check(self.lib.phn_time(self.h, ctypes.byref(t), ctypes.byref(s)))
+        return t.value, s.value
+
+    # ----------------------------------------------------------- analysis
+    def volume_averages(self, allow_nonfinite: bool = False) -> np.ndarray:
+        a = L.PhnAverages()
+        r = self.lib.phn_volume_averages(self.h, ctypes.byref(a))
+        if not (allow_nonfinite and r == L.ERR_NONFINITE):
+            L.check(r)
+        return avg_array(a)
+
+    def run_loop(self, nsteps: int, tso: float, max_rows: int = 100000) -> np.ndarray:
+        rows = (L.PhnAverages * max_rows)()
+        n = ctypes.c_int()
+        L.check(self.lib.phn_run_loop(self.h, int(nsteps), float(tso), rows, max_rows, ctypes.byref(n)))
+        out = np.frombuffer(bytes(rows), dtype=np.float64).reshape(max_rows, L.AVG_LEN)
+        return out[:n.value].copy()
+
+    def spectrum_bins(self):
+        nb, bs = ctypes.c_int(), ctypes.c_double()
+        L.check(self.lib.phn_spectrum_bins(self.h, ctypes.byref(nb), ctypes.byref(bs)))
+        return nb.value, bs.value
+
+    def correlation_functions(self):
+        nb, _ = self.spectrum_bins()
+        F, K, Q = (np.zeros(nb * self.p.Nc) for _ in range(3))
+        C = np.zeros(nb, dtype=np.int32)
+        L.check(self.lib.phn_spectrum(self.h, _pd(F), _pd(K), _pd(Q), _pi(C), nb))
+        return F, K, Q, C
+
+    def full_analysis(self, thres: float, mode: int = L.ISLAND_REFERENCE, z_periodic: bool = False,
+                      labels: bool = True, max_out: int = 1 << 20):
+        lab = np.zeros(self.p.N * self.p.N * (self.p.N + 2), dtype=np.int32) if labels else None
+        recs = np.zeros((max_out, len(L.ISLAND_FIELDS)))
+        n = ctypes.c_int()
+        r = self.lib.phn_islands(self.h, float(thres), int(mode), int(bool(z_periodic)),
+                                 _pi(lab) if labels else None, _pd(recs), max_out, ctypes.byref(n))
+        L.check(r)
+        return lab, recs[:n.value].copy()
+
+    def stats(self):
+        n, ms, st = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_int()
+        L.check(self.lib.phn_stats(self.h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(st)))
+        return n.value, ms.value, st.value
+
+    def synchronize(self):
+        L.check(self.lib.phn_synchronize(self.h))
+
+
+def device_count() -> int:
+    lib = L.load()
+    n = ctypes.c_int()
+    r = lib.phn_device_count(ctypes.byref(n))
+    return n.value if r == L.OK else 0

@@ -1,3 +1,4 @@
+import ctypes
 import os
 import sys
 
@@ -9,20 +10,25 @@ for p in (ROOT, os.path.join(ROOT, "tests", "golden")):
         sys.path.insert(0, p)
 
 
+def _has_cuda_device() -> bool:
+    try:
+        cuda = ctypes.CDLL("libcuda.so.1")
+    except OSError:
+        return False
+    if cuda.cuInit(0) != 0:
+        return False
+    n = ctypes.c_int(0)
+    return cuda.cuDeviceGetCount(ctypes.byref(n)) == 0 and n.value > 0
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
 def pytest_collection_modifyitems(config, items):
     # Without a GPU, GPU tests are skipped rather than failed when selected.
-    try:
-        import torch  # noqa: F401
-        has_gpu = torch.cuda.is_available()
-    except Exception:
-        has_gpu = False
-    if has_gpu:
-        return
-    skip = pytest.mark.skip(reason="no CUDA device")
-    for item in items:
-        if "gpu" in item.keywords:
-            item.add_marker(skip)
+    if any("gpu" in it.keywords for it in items) and not _has_cuda_device():
+        skip = pytest.mark.skip(reason="no CUDA device")
+        for item in items:
+            if "gpu" in item.keywords:
+                item.add_marker(skip)

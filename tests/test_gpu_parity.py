@@ -1,0 +1,270 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's own
+outputs (tests/golden/, produced by the reference sources) and the oracle.
+
+Tolerances
+  FP64 fields and SO-row extrema: bit-exact (same IEEE operations in the
+      reference's order).
+  FP64 sums (averages, energies): relative 1e-11 -- tree order vs the
+      reference's sequential sums.
+  FP64 spectra: relative 1e-10 of the largest bin (cuFFT vs the oracle FFT);
+      bin counts exact.
+  FP32 fields after 100 steps: absolute 2e-4 (fields are O(1)); averages
+      relative 2e-5.  Compensated FP32: absolute 2e-5.
+  Islands: labels, counts and sizes exact; island sums relative 1e-11.
+"""
+import numpy as np
+import pytest
+
+import fixtures
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ROW_COLS = slice(0, 23)
+SUM_COLS = [1, 5, 9, 10, 11, 12, 13, 14, 15, 16]      # phi0, pi0, phi2 .. charge
+EXACT_COLS = [0, 17, 18, 19, 20, 21, 22]               # t, extrema values and positions
+
+
+def gpu():
+    from phinum_gb300 import lattice as PL
+    return PL
+
+
+def gparams(d, precision):
+    PL = gpu()
+    return PL.Params(precision=precision, a=d["a"], dt=d["dt"], **d["params"])
+
+
+def start(d, precision):
+    PL = gpu()
+    p = gparams(d, precision)
+    lat = PL.Lattice(p)
+    phi_i, pi_i = fixtures.inputs_for(d)
+    lat.upload(O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc))
+    return lat, p
+
+
+def interior(flat, p):
+    return O.from_ref_layout(flat, p.N, p.Nc)
+
+
+CASES = fixtures.names()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_fields_bit_exact(name):
+    d = fixtures.load(name)
+    lat, p = start(d, 0)
+    done = 0
+    for c in fixtures.checkpoints(d):
+        lat.evolve(c - done)
+        done = c
+        phi, pi = lat.download()
+        assert fixtures.digest(interior(phi, p)) == str(d[f"phi_sha_{c}"]), f"phi after {c}"
+        assert fixtures.digest(interior(pi, p)) == str(d[f"pi_sha_{c}"]), f"pi after {c}"
+        a = lat.volume_averages()
+        ref = d[f"avg_{c}"]
+        assert np.array_equal(a[EXACT_COLS[1:]], ref[EXACT_COLS[1:]])
+        np.testing.assert_allclose(a[SUM_COLS], ref[SUM_COLS], rtol=1e-11, atol=1e-14)
+    t, s = lat.time()
+    assert t == d["tau_end"] and s == d["steps_end"]
+    lat.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_run_loop_rows(name):
+    d = fixtures.load(name)
+    lat, p = start(d, 0)
+    rows = lat.run_loop(d["steps"], d["tso"])
+    ref = d["rows"]
+    assert rows.shape[0] == ref.shape[0]
+    assert np.array_equal(rows[:, EXACT_COLS], ref[:, EXACT_COLS])
+    np.testing.assert_allclose(rows[:, SUM_COLS], ref[:, SUM_COLS], rtol=1e-11, atol=1e-14)
+    # the fused rows leave the fields exactly where plain evolve() does
+    phi, pi = lat.download()
+    c = max(fixtures.checkpoints(d))
+    if c == d["steps"]:
+        assert fixtures.digest(interior(phi, p)) == str(d[f"phi_sha_{c}"])
+    lat.close()
+
+
+@pytest.mark.parametrize("precision,atol", [(1, 2e-4), (2, 2e-5)])
+@pytest.mark.parametrize("name", ["t0_n8", "t1_n8", "t0_n12", "t0_n16_nc2"])
+def test_fp32_fields_close(name, precision, atol):
+    d = fixtures.load(name)
+    lat, p = start(d, precision)
+    last = max(fixtures.checkpoints(d))
+    lat.evolve(last)
+    phi, pi = lat.download()
+    np.testing.assert_allclose(interior(phi, p), d[f"phi_{last}"], rtol=0, atol=atol)
+    np.testing.assert_allclose(interior(pi, p), d[f"pi_{last}"], rtol=0, atol=atol)
+    rows = lat.run_loop(0, 1.0)  # nothing due: no rows
+    assert rows.shape[0] == 0
+    lat.close()
+
+
+@pytest.mark.parametrize("precision,rtol", [(1, 2e-5), (2, 2e-6)])
+@pytest.mark.parametrize("name", ["c0_n64", "t1_n32"])
+def test_fp32_rows_close(name, precision, rtol):
+    d = fixtures.load(name)
+    lat, p = start(d, precision)
+    steps = min(d["steps"], 500)
+    rows = lat.run_loop(steps, d["tso"])
+    ref = d["rows"][: rows.shape[0]]
+    assert rows.shape[0] == ref.shape[0]
+    assert np.array_equal(rows[:, 0], ref[:, 0])  # stamps come from the same FP64 clock
+    for col in ("energy", "interaction", "phi2", "pi2", "phi4"):
+        j = O.AVG[col]
+        np.testing.assert_allclose(rows[:, j], ref[:, j], rtol=rtol, atol=rtol * np.abs(ref[:, j]).max())
+    lat.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", CASES)
+def test_spectrum(name, precision):
+    d = fixtures.load(name)
+    lat, p = start(d, precision)
+    lat.evolve(d["steps"]) if precision == 0 else None
+    F, K, Q, C = lat.correlation_functions()
+    assert np.array_equal(C, d["spec_counts"])
+    if precision == 0:
+        for got, key in ((F, "spec_F"), (K, "spec_K"), (Q, "spec_Q")):
+            ref = d[key]
+            np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
+    else:
+        # FP32 spectrum of the initial fields against the oracle's FP64 spectrum
+        phi_i, pi_i = fixtures.inputs_for(d)
+        op = O.Params(a=d["a"], dt=d["dt"], **d["params"])
+        oF, oK, oQ, oC = O.spectrum(op, O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc))
+        assert np.array_equal(C, oC)
+        for got, ref in ((F, oF), (K, oK), (Q, oQ)):
+            np.testing.assert_allclose(got, ref, rtol=1e-4, atol=1e-5 * np.abs(ref).max())
+    lat.close()
+
+
+@pytest.mark.parametrize("name", [n for n in CASES if "nc2" not in n])
+def test_islands_fp64(name):
+    d = fixtures.load(name)
+    lat, p = start(d, 0)
+    lat.evolve(d["steps"])
+    lab, recs = lat.full_analysis(float(d["island_thres"]))
+    li = O.from_ref_layout(lab.astype(np.float64), p.N, 1)[0].astype(np.int32)
+    assert fixtures.label_digest(li) == str(d["island_labels_sha"])
+    st = d["island_stats"]  # index, V, PotEn, KinEn, GradEn, avPhi, peak pos, Peak_value
+    assert recs.shape[0] == st.shape[0]
+    I = {k: i for i, k in enumerate(O.ISLAND_FIELDS)}
+    assert np.array_equal(recs[:, I["index"]], st[:, 0])
+    assert np.array_equal(recs[:, I["volume"]], st[:, 1])
+    for j, k in ((2, "pot_en"), (3, "kin_en"), (4, "grad_en"), (5, "av_phi")):
+        np.testing.assert_allclose(recs[:, I[k]], st[:, j], rtol=1e-11, atol=1e-13)
+    # peak: the reference keeps the first maximum of phi^2 in BFS order, this
+    # implementation the smallest index among maxima -- equal unless tied
+    assert np.array_equal(np.abs(recs[:, I["peak_value"]]), np.abs(st[:, 7]))
+    lat.close()
+
+
+def test_islands_energy_mask_and_z_periodic_match_oracle():
+    d = fixtures.load("t1_n32")
+    lat, p = start(d, 0)
+    phi_i, pi_i = fixtures.inputs_for(d)
+    op = O.Params(a=d["a"], dt=d["dt"], **d["params"])
+    phi, pi = O.to_ref_layout(phi_i), O.to_ref_layout(pi_i)
+    rho_mean = O.averages(op, phi, pi)[O.AVG["energy"]]
+    for mode, thr in ((0, 2.6), (1, 2.0 * rho_mean)):
+        for zper in (0, 1):
+            lab, recs = lat.full_analysis(thr, mode=mode, z_periodic=bool(zper))
+            olab, orecs = O.islands(op, phi, pi, thr, mode=mode, zper=zper)
+            assert np.array_equal(lab, olab), (mode, zper)
+            assert recs.shape[0] == orecs.shape[0]
+            assert np.array_equal(recs[:, 1], orecs[:, 1])  # sizes
+            assert np.array_equal(recs[:, 9], orecs[:, 9])  # seeds
+    lat.close()
+
+
+def test_download_fills_ghost_slabs_like_exchange():
+    d = fixtures.load("t0_n16_nc2")
+    lat, p = start(d, 0)
+    lat.evolve(3)
+    phi, _ = lat.download()
+    slab = p.Nc * p.N * p.N
+    assert np.array_equal(phi[:slab], phi[p.N * slab:(p.N + 1) * slab])
+    assert np.array_equal(phi[(p.N + 1) * slab:], phi[slab:2 * slab])
+    lat.close()
+
+
+def test_results_are_deterministic():
+    d = fixtures.load("c0_n64")
+    outs = []
+    for _ in range(2):
+        lat, p = start(d, 1)
+        rows = lat.run_loop(120, d["tso"])
+        F, K, Q, C = lat.correlation_functions()
+        lab, recs = lat.full_analysis(2.6)
+        outs.append((rows, F, K, Q, lab, recs[:, :2]))
+        lat.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+
+
+def test_errors_are_status_codes():
+    PL = gpu()
+    from phinum_gb300 import _lib as L
+    with pytest.raises(L.PhnError) as e:
+        PL.Lattice(PL.Params(N=8, Nc=9))
+    assert e.value.code == L.ERR_UNSUPPORTED
+    with pytest.raises(L.PhnError) as e:
+        PL.Lattice(PL.Params(N=8, theory=3))
+    assert e.value.code == L.ERR_UNSUPPORTED
+    with pytest.raises(L.PhnError) as e:
+        PL.Lattice(PL.Params(N=8, a=-1.0))
+    assert e.value.code == L.ERR_INVALID
+    lat = PL.Lattice(PL.Params(N=8, Nc=2))
+    with pytest.raises(L.PhnError) as e:
+        lat.full_analysis(1.0)
+    assert e.value.code == L.ERR_UNSUPPORTED
+    lat.close()
+    # a NaN injected on the host is reported, not trapped
+    lat = PL.Lattice(PL.Params(N=8))
+    phi = O.to_ref_layout(np.ones((8, 8, 8)))
+    phi[8 * 8 + 5] = np.nan
+    lat.upload(phi, np.zeros_like(phi))
+    with pytest.raises(L.PhnError) as e:
+        lat.volume_averages()
+    assert e.value.code == L.ERR_NONFINITE
+    a = lat.volume_averages(allow_nonfinite=True)
+    assert a[24] == 1.0
+    lat.close()
+
+
+@pytest.mark.parametrize("N", [128, 256])
+def test_large_lattice_fp32_against_fp64(N):
+    """Full-size properties: FP32 tracks the bit-exact FP64 path, mode counts
+    cover every lattice mode, island partitions agree between precisions'
+    shared inputs and the oracle."""
+    import inputs
+    PL = gpu()
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 11)
+    phi, pi = O.to_ref_layout(phi_i), O.to_ref_layout(pi_i)
+    res = {}
+    for prec in (0, 1, 2):
+        lat = PL.Lattice(PL.Params(N=N, precision=prec))
+        lat.upload(phi, pi)
+        rows = lat.run_loop(100, 1.0)
+        F, K, Q, C = lat.correlation_functions()
+        assert C.sum() == N ** 3
+        res[prec] = (rows, lat.download()[0])
+        lat.close()
+    e64 = res[0][0][:, O.AVG["energy"]]
+    for prec, tol in ((1, 1e-5), (2, 1e-6)):
+        np.testing.assert_allclose(res[prec][0][:, O.AVG["energy"]], e64, rtol=tol)
+        assert np.abs(res[prec][1] - res[0][1]).max() < 100 * tol
+    # islands at full size: GPU labels = oracle BFS labels (FP64 inputs)
+    lat = PL.Lattice(PL.Params(N=N, precision=0))
+    lat.upload(phi, pi)
+    thr = float(np.quantile(np.sqrt(phi_i ** 2 + pi_i ** 2), 0.9))
+    lab, recs = lat.full_analysis(thr)
+    op = O.Params(N=N)
+    olab, orecs = O.islands(op, phi, pi, thr)
+    assert np.array_equal(lab, olab)
+    assert np.array_equal(recs[:, 1], orecs[:, 1])
+    lat.close()
