@@ -104,8 +104,10 @@ int phn_create(const phn_params *params, phn_handle **out);
 int phn_destroy(phn_handle *h);
 
 /* Replaces direct writes/reads of LocalLattice::Phi/Pi (lattice.cpp:77-78):
- * host arrays in the reference layout; upload reads the interior only,
- * download also fills the ghost slabs as Communication::exchange() would. */
+ * host arrays in the reference layout; upload reads the interior only.
+ * download writes Phi including its ghost slabs, as Communication::exchange()
+ * leaves them, and Pi's interior only: the reference never writes Pi's ghost
+ * slabs, so the caller's values there are left untouched. */
 int phn_upload(phn_handle *h, const double *Phi, const double *Pi);
 int phn_download(phn_handle *h, double *Phi, double *Pi);
 

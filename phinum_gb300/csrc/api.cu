@@ -233,11 +233,14 @@ int phn_download(phn_handle *h, double *Phi, double *Pi) {
     h->launches++;
   }
   if (Pi) {
+    // exchange() moves Phi only (comm.cpp:43-61): Pi's ghost slabs are never
+    // written by the reference, so only the interior is returned.
+    const size_t slab = (size_t)Nc * N * N;
     if (kahan)
       CK(launch_to_ref_kahan((const float *)h->pi, h->cpi, h->d_ref, N, Nc, h->stream));
     else
       CK(launch_to_ref(h->pi, h->d_ref, h->p.precision, N, Nc, h->stream));
-    CK(cudaMemcpyAsync(Pi, h->d_ref, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(Pi + slab, h->d_ref + slab, slab * N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->launches++;
   }

@@ -189,6 +189,12 @@ def test_download_fills_ghost_slabs_like_exchange():
     slab = p.Nc * p.N * p.N
     assert np.array_equal(phi[:slab], phi[p.N * slab:(p.N + 1) * slab])
     assert np.array_equal(phi[(p.N + 1) * slab:], phi[slab:2 * slab])
+    # Pi's ghost slabs belong to the caller: exchange() never writes them
+    from phinum_gb300 import _lib as L
+    pi = np.full(p.field_len, 7.5)
+    L.check(lat.lib.phn_download(lat.h, None, pi.ctypes.data_as(L._PD)))
+    assert np.all(pi[:slab] == 7.5) and np.all(pi[-slab:] == 7.5)
+    assert not np.any(pi[slab:-slab] == 7.5)
     lat.close()
 
 
