@@ -160,6 +160,23 @@ int phn_synchronize(phn_handle *h);
  * on the handle's stream), for roofline accounting. */
 int phn_stats(const phn_handle *h, long long *kernel_launches, double *last_evolve_ms, int *last_evolve_steps);
 
+/* Volume averages of caller-owned device fields, allocating nothing.
+ * No counterpart in the reference: it exists for hosts that cannot allocate
+ * device memory where they need the averages -- a framework that owns all
+ * device memory through its own pool, or a stream-ordered loop in which a
+ * cudaMalloc (which may synchronise the device) is not allowed.
+ * d_phi, d_pi: device fields in the layout phn_device_fields describes
+ * (PHN_FP64: double, PHN_FP32: float; PHN_FP32_KAHAN is rejected); stream:
+ * the cudaStream_t to run on (NULL: the legacy default stream); out: host.
+ * The reduction's scratch is one fixed __device__ array of 768 KiB per GPU
+ * (kept until the process exits), which limits N to 1024; larger lattices
+ * get PHN_ERR_INVALID.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race, so serialise them.  Returns after the result is on the host. */
+int phn_volume_averages_noalloc(const phn_params *params, const void *d_phi, const void *d_pi, void *stream,
+                                phn_averages *out);
+
 /* Page-locks (unlocks) a caller-owned host buffer so that phn_upload /
  * phn_download move it by DMA at full link bandwidth (cudaHostRegister). */
 int phn_pin_host(void *ptr, size_t bytes);

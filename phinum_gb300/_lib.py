@@ -71,6 +71,8 @@ _SIGS = {
                                ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
     "phn_synchronize": (_I, [ctypes.c_void_p]),
     "phn_stats": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _PD, _PI]),
+    "phn_volume_averages_noalloc": (_I, [ctypes.POINTER(PhnParams), ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.POINTER(PhnAverages)]),
     "phn_pin_host": (_I, [ctypes.c_void_p, ctypes.c_size_t]),
     "phn_unpin_host": (_I, [ctypes.c_void_p]),
 }

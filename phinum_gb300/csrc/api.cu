@@ -35,7 +35,7 @@ using namespace phn;
     if (e_ != cudaSuccess) return cuda_error(e_, #call); \
   } while (0)
 
-static int validate(const phn_params *p) {
+int phn::validate_params(const phn_params *p) {
   if (!p) return set_error(PHN_ERR_INVALID, "params is NULL");
   if (p->N < 2 || p->N > 2048) return set_error(PHN_ERR_INVALID, "N=%d outside [2, 2048]", p->N);
   if (p->Nc < 1 || p->Nc > PHN_MAX_NC) return set_error(PHN_ERR_UNSUPPORTED, "Nc=%d outside [1, %d]", p->Nc, PHN_MAX_NC);
@@ -51,7 +51,7 @@ static int validate(const phn_params *p) {
 
 // Coefficients evaluated with the reference's expressions (dynamics.cpp:80-100,
 // fieldanalysis.cpp:445-579); see Consts.
-static Consts make_consts(const phn_params *p) {
+Consts phn::make_consts(const phn_params *p) {
   Consts k;
   memset(&k, 0, sizeof(k));
   const int Nc = p->Nc;
@@ -128,7 +128,7 @@ int phn_reset(phn_handle *h) {
 int phn_create(const phn_params *params, phn_handle **out) {
   if (!out) return set_error(PHN_ERR_INVALID, "out is NULL");
   *out = nullptr;
-  int r = validate(params);
+  int r = validate_params(params);
   if (r) return r;
   phn_handle *h = new phn_handle();
   memset((void *)h, 0, sizeof(*h));

@@ -96,6 +96,10 @@ cudaError_t launch_from_ref_kahan(const double *ref, float *hi, float *comp, int
 int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);
 
+// Parameter checks and kernel coefficients of phn_create (api.cu).
+int validate_params(const phn_params *p);
+Consts make_consts(const phn_params *p);
+
 }  // namespace phn
 
 // The handle behind the opaque phn_handle pointer.

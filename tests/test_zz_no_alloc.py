@@ -1,0 +1,62 @@
+"""phn_volume_averages_noalloc: averages of caller-owned device fields with
+no allocation, for hosts that cannot call cudaMalloc where they need the
+averages (a framework that owns all device memory, or a stream-ordered loop
+in which a device-synchronising allocation is not allowed).
+
+It runs the same fused observation kernel as phn_volume_averages, with its
+block records in a fixed __device__ array, so its output must match the
+handle-based entry point: extrema exactly, sums within the tolerances used
+elsewhere (FP64 relative 1e-11; FP32 fields relative 2e-5).  Checked on two
+calls in a row, since every call reuses the same scratch array.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import inputs
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+EXACT = [17, 18, 19, 20, 21, 22]  # min/max/max|phi| values and positions
+SUMS = [1, 5, 9, 10, 11, 12, 13, 14, 15, 16, 23]
+
+
+@pytest.mark.parametrize("precision,rtol", [(0, 1e-11), (1, 2e-5)])
+@pytest.mark.parametrize("N,Nc", [(64, 1), (48, 2)])
+def test_noalloc_matches_handle_averages_twice(precision, rtol, N, Nc):
+    from phinum_gb300 import _lib as L
+    from phinum_gb300 import lattice as PL
+
+    p = PL.Params(N=N, Nc=Nc, precision=precision)
+    phi_i, pi_i = inputs.lattice_fields(N, Nc, 31)
+    with PL.Lattice(p) as lat:
+        lat.upload(O.to_ref_layout(phi_i, Nc), O.to_ref_layout(pi_i, Nc))
+        lat.evolve(9)
+        ref = lat.volume_averages()
+        d_phi, d_pi, st = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        L.check(lat.lib.phn_device_fields(lat.h, ctypes.byref(d_phi), ctypes.byref(d_pi), ctypes.byref(st)))
+        lat.synchronize()
+        for _ in range(2):
+            out = L.PhnAverages()
+            L.check(lat.lib.phn_volume_averages_noalloc(ctypes.byref(p.c()), d_phi, d_pi, st, ctypes.byref(out)))
+            got = np.frombuffer(bytes(out), dtype=np.float64)
+            assert np.array_equal(got[EXACT], ref[EXACT])
+            np.testing.assert_allclose(got[SUMS], ref[SUMS], rtol=rtol, atol=rtol * 1e-3)
+            assert got[24] == 0.0
+
+
+def test_noalloc_rejects_lattices_beyond_its_scratch():
+    from phinum_gb300 import _lib as L
+    from phinum_gb300 import lattice as PL
+
+    lib = L.load()
+    out = L.PhnAverages()
+    p = PL.Params(N=1056, precision=1)
+    r = lib.phn_volume_averages_noalloc(ctypes.byref(p.c()), None, None, None, ctypes.byref(out))
+    assert r == L.ERR_INVALID
+    assert b"N <= 1024" in lib.phn_last_error()
+    p = PL.Params(N=64, precision=2)
+    assert lib.phn_volume_averages_noalloc(ctypes.byref(p.c()), None, None, None, ctypes.byref(out)) == \
+        L.ERR_UNSUPPORTED
