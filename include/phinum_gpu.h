@@ -149,6 +149,14 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
 int phn_islands(phn_handle *h, double thres, int mode, int z_periodic, int *labels, phn_island *out,
                 int max_out, int *n_islands);
 
+/* Kernel path of the FP32 step (the others have one path each):
+ * PHN_PATH_TMA, the TMA-pipelined persistent kernel (default where it
+ * applies: Nc = 1, N in {128,256,384,512,768,1024}), or PHN_PATH_PLAIN, the
+ * register z-marching kernel (every size).  Both compute bit-identical fields. */
+enum { PHN_PATH_AUTO = 0, PHN_PATH_PLAIN = 1, PHN_PATH_TMA = 2 };
+int phn_set_path(phn_handle *h, int path);
+int phn_get_path(const phn_handle *h, int *path);
+
 /* Device pointers of the current fields (precision-typed: double* for
  * PHN_FP64, float* otherwise; SoA [a][z][y][x], no ghosts) and the stream the
  * handle launches on, for callers that keep data resident on the device. */

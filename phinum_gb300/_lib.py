@@ -17,6 +17,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NOMEM, ERR_UNSUPPORTE
     0, -1, -2, -3, -4, -5, -6, -7
 FP64, FP32, FP32_KAHAN = 0, 1, 2
 ISLAND_REFERENCE, ISLAND_ENERGY = 0, 1
+PATH_AUTO, PATH_PLAIN, PATH_TMA = 0, 1, 2
 
 _D, _I = ctypes.c_double, ctypes.c_int
 _PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
@@ -67,6 +68,8 @@ _SIGS = {
     "phn_spectrum_bins": (_I, [ctypes.c_void_p, _PI, _PD]),
     "phn_spectrum": (_I, [ctypes.c_void_p, _PD, _PD, _PD, _PI, _I]),
     "phn_islands": (_I, [ctypes.c_void_p, _D, _I, _I, _PI, _PD, _I, _PI]),
+    "phn_set_path": (_I, [ctypes.c_void_p, _I]),
+    "phn_get_path": (_I, [ctypes.c_void_p, _PI]),
     "phn_device_fields": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
                                ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
     "phn_synchronize": (_I, [ctypes.c_void_p]),

@@ -91,6 +91,7 @@ static void free_all(phn_handle *h) {
   cudaFree(h->partials);
   cudaFree(h->d_avg);
   cudaFree(h->d_ref);
+  cudaFree(h->d_err);
   if (h->h_avg) cudaFreeHost(h->h_avg);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -168,7 +169,14 @@ int phn_create(const phn_params *params, phn_handle **out) {
     CKF(cudaMemsetAsync(h->cphi, 0, bytes, h->stream));
     CKF(cudaMemsetAsync(h->cpi, 0, bytes, h->stream));
   }
-  CKF(cudaMalloc(&h->partials, (size_t)h->grid.nblocks * REC * sizeof(double)));
+  h->tma_grid = tma_supported(*params) ? tma_grid(*params) : 0;
+  h->path = h->tma_grid > 0 ? PHN_PATH_TMA : PHN_PATH_PLAIN;
+  {
+    const int recs = h->grid.nblocks > h->tma_grid ? h->grid.nblocks : h->tma_grid;
+    CKF(cudaMalloc(&h->partials, (size_t)recs * REC * sizeof(double)));
+  }
+  CKF(cudaMalloc(&h->d_err, sizeof(int)));
+  CKF(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
   CKF(cudaMalloc(&h->d_avg, sizeof(phn_averages)));
   h->h_avg_cap = 64;
   CKF(cudaHostAlloc((void **)&h->h_avg, h->h_avg_cap * sizeof(phn_averages), cudaHostAllocDefault));
@@ -273,14 +281,23 @@ static int step_once(phn_handle *h, int mode) {
     case PHN_FP64:
       e = launch_step_f64(h->k, h->grid, mode, (const double *)h->phi[h->cur], (double *)h->phi[nxt],
                           (double *)h->pi, s, h->partials, h->stream);
+      if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
       break;
     case PHN_FP32:
-      e = launch_step_f32(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt],
-                          (float *)h->pi, s, h->partials, h->stream);
+      if (h->path == PHN_PATH_TMA && mode != MODE_OBS) {
+        e = launch_step_f32_tma(h->k, h->tma_grid, mode == MODE_STEP_OBS, (const float *)h->phi[h->cur],
+                                (float *)h->phi[nxt], (float *)h->pi, s, h->partials, h->d_err, h->stream);
+        if (mode == MODE_STEP_OBS) h->obs_records = h->tma_grid;
+      } else {
+        e = launch_step_f32(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt],
+                            (float *)h->pi, s, h->partials, h->stream);
+        if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
+      }
       break;
     default:
       e = launch_step_kahan(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt], h->cphi,
                             h->cphi, (float *)h->pi, h->cpi, s, h->partials, h->stream);
+      if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
       break;
   }
   if (e != cudaSuccess) return cuda_error(e, "step kernel launch");
@@ -288,6 +305,18 @@ static int step_once(phn_handle *h, int mode) {
   if (mode != MODE_OBS) {
     h->cur = nxt;
     h->steps++;
+  }
+  return PHN_OK;
+}
+
+// Reads (and clears) the device error word of the bounded waits.
+static int check_device_error(phn_handle *h) {
+  int word = 0;
+  CK(cudaMemcpyAsync(&word, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (word) {
+    CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    return set_error(PHN_ERR_TIMEOUT, "a bounded device wait gave up (code %d)", word);
   }
   return PHN_OK;
 }
@@ -306,11 +335,11 @@ int phn_evolve(phn_handle *h, int nsteps) {
   CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
   h->last_ms = ms;
   h->last_steps = nsteps;
-  return PHN_OK;
+  return check_device_error(h);
 }
 
 static int fetch_avg(phn_handle *h, phn_averages *dst_host_slot) {
-  CK(launch_finalize(h->k, h->partials, h->grid.nblocks, h->d_avg, h->stream));
+  CK(launch_finalize(h->k, h->partials, h->obs_records, h->d_avg, h->stream));
   h->launches++;
   CK(cudaMemcpyAsync(dst_host_slot, h->d_avg, sizeof(phn_averages), cudaMemcpyDeviceToHost, h->stream));
   return PHN_OK;
@@ -395,8 +424,28 @@ int phn_run_loop(phn_handle *h, int nsteps, double tso, phn_averages *rows, int 
   }
   delete[] stamps;
   if (nrows) *nrows = due_total;
+  {
+    int r = check_device_error(h);
+    if (r) return r;
+  }
   if (due_total > max_rows) return set_error(PHN_ERR_TRUNCATED, "%d rows due, %d written", due_total, max_rows);
   if (nonfinite) return set_error(PHN_ERR_NONFINITE, "non-finite field values in a row");
+  return PHN_OK;
+}
+
+int phn_set_path(phn_handle *h, int path) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (path == PHN_PATH_AUTO) path = h->tma_grid > 0 ? PHN_PATH_TMA : PHN_PATH_PLAIN;
+  if (path != PHN_PATH_PLAIN && path != PHN_PATH_TMA) return set_error(PHN_ERR_INVALID, "path %d", path);
+  if (path == PHN_PATH_TMA && h->tma_grid == 0)
+    return set_error(PHN_ERR_UNSUPPORTED, "TMA step needs FP32, Nc = 1, N in {128,256,384,512,768,1024}");
+  h->path = path;
+  return PHN_OK;
+}
+
+int phn_get_path(const phn_handle *h, int *path) {
+  if (!h || !path) return set_error(PHN_ERR_INVALID, "NULL argument");
+  *path = h->path;
   return PHN_OK;
 }
 

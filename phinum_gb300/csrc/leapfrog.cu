@@ -14,146 +14,10 @@
 // of phi is fetched from HBM once per chunk; x/y neighbours hit L1/L2.
 #include <math.h>
 
+#include "observe.cuh"
 #include "phn_internal.h"
 
 namespace phn {
-
-// ----------------------------------------------------------- accumulators
-struct Acc {
-  double s[NSUM];
-  double minv, maxv, absv;
-  long long mini, maxi, absi;
-  __device__ void init() {
-#pragma unroll
-    for (int j = 0; j < NSUM; ++j) s[j] = 0.0;
-    // CalculateExtrema's starting values (fieldanalysis.cpp:324-325)
-    minv = 10000000.0;
-    maxv = -10000000.0;
-    absv = 0.0;
-    mini = maxi = absi = LLONG_MAX;
-  }
-  // Strict comparisons as in the reference; equal values keep the smaller
-  // index, which is the first one the reference's linear scan meets.
-  __device__ void take_max(double v, long long i) {
-    if (v > maxv || (v == maxv && i < maxi && v > -10000000.0)) { maxv = v; maxi = i; }
-  }
-  __device__ void take_min(double v, long long i) {
-    if (v < minv || (v == minv && i < mini && v < 10000000.0)) { minv = v; mini = i; }
-  }
-  __device__ void take_abs(double v, long long i) {
-    if (v > absv || (v == absv && i < absi && v > 0.0)) { absv = v; absi = i; }
-  }
-};
-
-__device__ __forceinline__ void combine(Acc &a, const Acc &b) {
-#pragma unroll
-  for (int j = 0; j < NSUM; ++j) a.s[j] += b.s[j];
-  if (b.maxi != LLONG_MAX) a.take_max(b.maxv, b.maxi);
-  if (b.mini != LLONG_MAX) a.take_min(b.minv, b.mini);
-  if (b.absi != LLONG_MAX) a.take_abs(b.absv, b.absi);
-}
-
-__device__ __forceinline__ Acc shfl_down(const Acc &a, int off) {
-  Acc b;
-#pragma unroll
-  for (int j = 0; j < NSUM; ++j) b.s[j] = __shfl_down_sync(0xffffffffu, a.s[j], off);
-  b.minv = __shfl_down_sync(0xffffffffu, a.minv, off);
-  b.maxv = __shfl_down_sync(0xffffffffu, a.maxv, off);
-  b.absv = __shfl_down_sync(0xffffffffu, a.absv, off);
-  b.mini = __shfl_down_sync(0xffffffffu, a.mini, off);
-  b.maxi = __shfl_down_sync(0xffffffffu, a.maxi, off);
-  b.absi = __shfl_down_sync(0xffffffffu, a.absi, off);
-  return b;
-}
-
-__device__ __forceinline__ void store_rec(double *r, const Acc &a) {
-#pragma unroll
-  for (int j = 0; j < NSUM; ++j) r[j] = a.s[j];
-  r[E_MIN_V] = a.minv;
-  r[E_MIN_I] = __longlong_as_double(a.mini);
-  r[E_MAX_V] = a.maxv;
-  r[E_MAX_I] = __longlong_as_double(a.maxi);
-  r[E_ABS_V] = a.absv;
-  r[E_ABS_I] = __longlong_as_double(a.absi);
-}
-
-__device__ __forceinline__ void load_rec(Acc &a, const double *r) {
-#pragma unroll
-  for (int j = 0; j < NSUM; ++j) a.s[j] = r[j];
-  a.minv = r[E_MIN_V];
-  a.mini = __double_as_longlong(r[E_MIN_I]);
-  a.maxv = r[E_MAX_V];
-  a.maxi = __double_as_longlong(r[E_MAX_I]);
-  a.absv = r[E_ABS_V];
-  a.absi = __double_as_longlong(r[E_ABS_I]);
-}
-
-// Fixed-order block reduction; the block's record goes to partials.
-__device__ void block_store(Acc &acc, double *partials) {
-  __shared__ double sh[THREADS / 32][REC];
-  const int tid = threadIdx.x + TX * threadIdx.y;
-  const int lane = tid & 31, warp = tid >> 5;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    Acc o = shfl_down(acc, off);
-    combine(acc, o);
-  }
-  if (lane == 0) store_rec(sh[warp], acc);
-  __syncthreads();
-  if (warp == 0) {
-    Acc a;
-    a.init();
-    if (lane < THREADS / 32) load_rec(a, sh[lane]);
-#pragma unroll
-    for (int off = 4; off > 0; off >>= 1) {
-      Acc o = shfl_down(a, off);
-      combine(a, o);
-    }
-    if (lane == 0) {
-      const size_t b = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
-      store_rec(partials + b * REC, a);
-    }
-  }
-}
-
-// Per-site observation terms, each computed with the reference's expression
-// (fieldanalysis.cpp:331-355 and 433-616).  c, p: phi and pi of the site;
-// fxp, fyp, fzp: forward neighbours of phi; kidx: reference index of
-// component 0 of the site.
-template <int NC, int THEORY>
-__device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c, const double *p,
-                                        const double *fxp, const double *fyp, const double *fzp,
-                                        long long kidx) {
-  double l = 0.0, inter = 0.0;
-#pragma unroll
-  for (int a = 0; a < NC; ++a) {
-    A.s[S_PHI + a] += c[a];
-    A.s[S_PI + a] += p[a];
-    const double c2 = __dmul_rn(c[a], c[a]);
-    A.s[S_PHI2] += c2;
-    A.s[S_PI2] += __dmul_rn(p[a], p[a]);
-    A.s[S_PHIPI] += __dmul_rn(c[a], p[a]);
-    l = __dadd_rn(l, c2);
-    const double dx = __dadd_rn(fxp[a], -c[a]), dy = __dadd_rn(fyp[a], -c[a]), dz = __dadd_rn(fzp[a], -c[a]);
-    A.s[S_GRAD] += __dadd_rn(__dadd_rn(__dmul_rn(dx, dx) / k.a2, __dmul_rn(dy, dy) / k.a2),
-                             __dmul_rn(dz, dz) / k.a2);
-    double term = __dmul_rn(k.mm_half_M, c2);
-    if (THEORY == 1 && a == 0) term = __dadd_rn(__dmul_rn(k.h, c[a]), term);
-    inter += term;
-    if (!isfinite(c[a]) || !isfinite(p[a])) A.s[S_NONFINITE] += 1.0;
-    A.take_max(c[a], kidx + a);
-    A.take_min(c[a], kidx + a);
-  }
-  const double l2 = __dmul_rn(l, l);
-  A.s[S_PHI4] += l2;
-  A.s[S_PHI6] += __dmul_rn(l2, l);
-  if (THEORY == 0)
-    inter += __dadd_rn(__dmul_rn(k.lm, l2 / k.c24), __dmul_rn(l2, l) / k.c720);
-  else
-    inter += __dmul_rn(k.lm, l2 / k.c24);
-  A.s[S_INTER] += inter;
-  A.take_abs(sqrt(l), kidx);
-}
 
 // ----------------------------------------------------------- FP64 kernel
 // The kick and drift use explicit round-to-nearest intrinsics and IEEE
@@ -239,8 +103,8 @@ __global__ void __launch_bounds__(THREADS) step_f32(const float *__restrict__ ph
   const int z0 = blockIdx.z * cz;
   const int z1 = min(z0 + cz, N);
   const size_t NN = (size_t)N * N, V = NN * N;
-  Acc acc;
-  if (MODE != MODE_STEP) acc.init();
+  AccF accf;
+  if (MODE != MODE_STEP) accf.init();
   if (x < N && y < N && z0 < z1) {
     const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
     const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
@@ -265,25 +129,23 @@ __global__ void __launch_bounds__(THREADS) step_f32(const float *__restrict__ ph
         fym[a] = __ldg(phi + a * V + pl + (size_t)ym * N + x);
         p[a] = pi[a * V + pl + col];
       }
-      if (MODE != MODE_STEP) {
-        double cd[NC], pd[NC], xd[NC], yd[NC], zd[NC];
-#pragma unroll
-        for (int a = 0; a < NC; ++a) {
-          cd[a] = c[a]; pd[a] = p[a]; xd[a] = fxp[a]; yd[a] = fyp[a]; zd[a] = cp[a];
-        }
-        observe<NC, THEORY>(acc, k, cd, pd, xd, yd, zd, (long long)NC * (long long)(col + (size_t)(z + 1) * NN));
-      }
+      if (MODE != MODE_STEP)
+        observe_f32<NC, THEORY>(accf, k, c, p, fxp, fyp, cp, (long long)NC * (long long)(col + (size_t)(z + 1) * NN));
       if (MODE != MODE_OBS) {
         float l = 0.f;
 #pragma unroll
         for (int a = 0; a < NC; ++a) l = fmaf(c[a], c[a], l);
         float coef = fmaf(l, k.c4_f, k.mmM_f);
-        if (THEORY == 0) coef = fmaf(l * l, k.c6_f, coef);
+        if (THEORY == 0) coef = fmaf(__fmul_rn(l, l), k.c6_f, coef);
 #pragma unroll
         for (int a = 0; a < NC; ++a) {
-          const float lap = (((fxp[a] + fxm[a]) + (fyp[a] + fym[a])) + (cp[a] + cm[a]) - 6.f * c[a]) * k.inv_a2_f;
+          // rounding pinned with explicit intrinsics: the TMA kernel computes the same bits
+          const float lap = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(fxp[a], fxm[a]), __fadd_rn(fyp[a], fym[a])),
+                                                          __fadd_rn(cp[a], cm[a])),
+                                                __fmul_rn(-6.f, c[a])),
+                                      k.inv_a2_f);
           float f = fmaf(-coef, c[a], lap);
-          if (THEORY == 1 && a == 0) f -= k.h_f;
+          if (THEORY == 1 && a == 0) f = __fsub_rn(f, k.h_f);
           const float pn = fmaf(fk, f, p[a]);
           pi[a * V + pl + col] = pn;
           phi_out[a * V + pl + col] = fmaf(fd, pn, c[a]);
@@ -296,7 +158,11 @@ __global__ void __launch_bounds__(THREADS) step_f32(const float *__restrict__ ph
       }
     }
   }
-  if (MODE != MODE_STEP) block_store(acc, partials);
+  if (MODE != MODE_STEP) {
+    Acc acc;
+    accf.to_double(acc);
+    block_store(acc, partials);
+  }
 }
 
 // ------------------------------------------------ compensated FP32 kernel
@@ -315,8 +181,8 @@ __global__ void __launch_bounds__(THREADS) step_kahan(const float *__restrict__ 
   const int z0 = blockIdx.z * cz;
   const int z1 = min(z0 + cz, N);
   const size_t NN = (size_t)N * N, V = NN * N;
-  Acc acc;
-  if (MODE != MODE_STEP) acc.init();
+  AccF accf;
+  if (MODE != MODE_STEP) accf.init();
   if (x < N && y < N && z0 < z1) {
     const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
     const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
@@ -345,26 +211,29 @@ __global__ void __launch_bounds__(THREADS) step_kahan(const float *__restrict__ 
       }
       if (MODE != MODE_STEP) {
         // observables of the represented values hi - comp (neighbours: hi only)
-        double cd[NC], pd[NC], xd[NC], yd[NC], zd[NC];
+        float cr[NC], pr[NC];
 #pragma unroll
         for (int a = 0; a < NC; ++a) {
-          cd[a] = (double)c[a] - (double)ec[a];
-          pd[a] = (double)p[a] - (double)ep[a];
-          xd[a] = fxp[a]; yd[a] = fyp[a]; zd[a] = cp[a];
+          cr[a] = __fsub_rn(c[a], ec[a]);
+          pr[a] = __fsub_rn(p[a], ep[a]);
         }
-        observe<NC, THEORY>(acc, k, cd, pd, xd, yd, zd, (long long)NC * (long long)(col + (size_t)(z + 1) * NN));
+        observe_f32<NC, THEORY>(accf, k, cr, pr, fxp, fyp, cp, (long long)NC * (long long)(col + (size_t)(z + 1) * NN));
       }
       if (MODE != MODE_OBS) {
         float l = 0.f;
 #pragma unroll
         for (int a = 0; a < NC; ++a) l = fmaf(c[a], c[a], l);
         float coef = fmaf(l, k.c4_f, k.mmM_f);
-        if (THEORY == 0) coef = fmaf(l * l, k.c6_f, coef);
+        if (THEORY == 0) coef = fmaf(__fmul_rn(l, l), k.c6_f, coef);
 #pragma unroll
         for (int a = 0; a < NC; ++a) {
-          const float lap = (((fxp[a] + fxm[a]) + (fyp[a] + fym[a])) + (cp[a] + cm[a]) - 6.f * c[a]) * k.inv_a2_f;
+          // rounding pinned with explicit intrinsics: the TMA kernel computes the same bits
+          const float lap = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(fxp[a], fxm[a]), __fadd_rn(fyp[a], fym[a])),
+                                                          __fadd_rn(cp[a], cm[a])),
+                                                __fmul_rn(-6.f, c[a])),
+                                      k.inv_a2_f);
           float f = fmaf(-coef, c[a], lap);
-          if (THEORY == 1 && a == 0) f -= k.h_f;
+          if (THEORY == 1 && a == 0) f = __fsub_rn(f, k.h_f);
           // kick: pi += fk * f  (Kahan)
           const float yk = __fsub_rn(__fmul_rn(fk, f), ep[a]);
           const float tk = __fadd_rn(p[a], yk);
@@ -387,7 +256,11 @@ __global__ void __launch_bounds__(THREADS) step_kahan(const float *__restrict__ 
       }
     }
   }
-  if (MODE != MODE_STEP) block_store(acc, partials);
+  if (MODE != MODE_STEP) {
+    Acc acc;
+    accf.to_double(acc);
+    block_store(acc, partials);
+  }
 }
 
 // ----------------------------------------------------------- finalize

@@ -84,6 +84,12 @@ cudaError_t launch_step_kahan(const Consts &k, const Grid &g, int mode, const fl
 cudaError_t launch_finalize(const Consts &k, const double *partials, int nblocks, phn_averages *out,
                             cudaStream_t st);
 
+// TMA-pipelined FP32 step (leapfrog_tma.cu): Nc = 1, N in {128,256,384,512,768,1024}.
+bool tma_supported(const phn_params &p);
+int tma_grid(const phn_params &p);
+cudaError_t launch_step_f32_tma(const Consts &k, int grid, bool obs, const float *phi, float *phi_out, float *pi,
+                                StepF s, double *partials, int *err, cudaStream_t st);
+
 // Layout conversion between the reference layout (host order, ghosts) and
 // the device SoA layout [a][z][y][x] (layout.cu).
 cudaError_t launch_from_ref(const double *ref, void *dst, int prec, int N, int Nc, cudaStream_t st);
@@ -115,6 +121,10 @@ struct phn_handle {
   void *pi;
   float *cphi, *cpi;   // compensation terms (PHN_FP32_KAHAN)
   int cur;             // phi[cur] holds the current field
+  int path;            // PHN_PATH_* in use for FP32 steps
+  int tma_grid;        // persistent grid of the TMA step kernel (0: unsupported)
+  int obs_records;     // block records written by the last observation launch
+  int *d_err;          // device error word of bounded waits (0: none)
   double *partials;    // block records of the fused observation
   phn_averages *d_avg; // finalize output (device)
   phn_averages *h_avg; // pinned host mirror, one per row slot

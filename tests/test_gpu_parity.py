@@ -274,3 +274,30 @@ def test_large_lattice_fp32_against_fp64(N):
     assert np.array_equal(lab, olab)
     assert np.array_equal(recs[:, 1], orecs[:, 1])
     lat.close()
+
+
+@pytest.mark.parametrize("theory", [0, 1])
+@pytest.mark.parametrize("N", [128, 256, 384])
+def test_tma_path_matches_plain_path_bit_for_bit(N, theory):
+    """The TMA-pipelined FP32 step and the register z-marching step compute
+    identical fields; their fused SO rows agree to FP32-summation rounding,
+    extrema exactly."""
+    import inputs
+    PL = gpu()
+    from phinum_gb300 import _lib as L
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 40 + theory, phi0=(-1) ** theory * 6 ** 0.5)
+    phi, pi = O.to_ref_layout(phi_i), O.to_ref_layout(pi_i)
+    kw = dict(theory=0) if theory == 0 else dict(theory=1, mass_mode=-1, lambda_mode=1, h=0.12247)
+    out = {}
+    for path in (L.PATH_PLAIN, L.PATH_TMA):
+        lat = PL.Lattice(PL.Params(N=N, precision=1, **kw))
+        L.check(lat.lib.phn_set_path(lat.h, path))
+        lat.upload(phi, pi)
+        rows = lat.run_loop(120, 0.5)
+        lat.evolve(7)
+        out[path] = (rows,) + lat.download()
+        lat.close()
+    (r0, f0, p0), (r1, f1, p1) = out[L.PATH_PLAIN], out[L.PATH_TMA]
+    assert np.array_equal(f0, f1) and np.array_equal(p0[N * N:-N * N], p1[N * N:-N * N])
+    assert np.array_equal(r0[:, 17:23], r1[:, 17:23])
+    np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
