@@ -167,7 +167,7 @@ def measure_gpu(args, dist: Dist):
     from phinum_gb300 import lattice as PL
     from phinum_gb300 import _lib as L
 
-    N = N_MAIN
+    N = args.n
     phi, pi = make_fields(N)
     lib = L.load()
     sites = N ** 3
@@ -212,6 +212,11 @@ def measure_gpu(args, dist: Dist):
                        "mean_launch_ms": round(t_launch * 1e3, 4)}
     lat.close()
 
+    if args.no_e2e:
+        out["e2e"] = None
+        out["also"] = {}
+        return out
+
     # ---------------------------------------------------------------- e2e
     lat = PL.Lattice(PL.Params(N=N, precision=L.FP32))
     for a in (phi, pi):
@@ -243,6 +248,9 @@ def measure_gpu(args, dist: Dist):
 
     # ------------------------------------------- the other precisions/sizes
     also = {}
+    if args.no_extra:
+        out["also"] = also
+        return out
     for label, n, prec, k in (("n256_fp32", 256, L.FP32, 400), ("n256_fp64", 256, L.FP64, 40),
                               ("n512_fp64", 512, L.FP64, 10), ("n512_kahan_fp32", 512, L.FP32_KAHAN, 200)):
         if args.quick and n == 512 and prec != L.FP32:
@@ -288,12 +296,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the slow FP64/compensated extra lines")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other sizes/precisions")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--n", type=int, default=N_MAIN, help="lattice edge (profiling runs use smaller cases)")
     args = ap.parse_args()
     rank, local, world = env_rank()
-    config = {"workload": f"phi^6 oscillon (theory 0, Kappa=sqrt(3)), {N_MAIN}^3 periodic lattice, a=0.25, "
+    config = {"workload": f"phi^6 oscillon (theory 0, Kappa=sqrt(3)), {args.n}^3 periodic lattice, a=0.25, "
                           f"dtau=0.02, leapfrog kick-drift with fused volume averages + extrema every "
                           f"{TSO_STEPS} steps (TSO=1.0)",
-              "N": N_MAIN, "sites": N_MAIN ** 3, "tso_steps": TSO_STEPS,
+              "N": args.n, "sites": args.n ** 3, "tso_steps": TSO_STEPS,
               "l2": "inputs larger than L2 (1.5 GB of fields vs 129 MB L2); no flush",
               "parallelism": f"replicas x{args.gpus}"}
 

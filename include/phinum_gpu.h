@@ -157,6 +157,17 @@ enum { PHN_PATH_AUTO = 0, PHN_PATH_PLAIN = 1, PHN_PATH_TMA = 2 };
 int phn_set_path(phn_handle *h, int path);
 int phn_get_path(const phn_handle *h, int *path);
 
+/* Autotuner of the TMA step kernel: times each variant (tile height, stage
+ * count, pi through shared memory or straight from HBM) for `steps` launches
+ * on the live lattice, keeps the fastest for this handle and reports it.  The
+ * lattice state is unchanged; all variants compute bit-identical fields.
+ * A handle on another path has nothing to tune (*variant = -1). */
+int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms);
+/* Number of variants on this handle (0 without the TMA kernel) and an explicit
+ * choice of one (0 .. n-1), e.g. to reproduce a tuned configuration. */
+int phn_num_variants(const phn_handle *h, int *n);
+int phn_set_variant(phn_handle *h, int variant);
+
 /* Device pointers of the current fields (precision-typed: double* for
  * PHN_FP64, float* otherwise; SoA [a][z][y][x], no ghosts) and the stream the
  * handle launches on, for callers that keep data resident on the device. */

@@ -70,6 +70,9 @@ _SIGS = {
     "phn_islands": (_I, [ctypes.c_void_p, _D, _I, _I, _PI, _PD, _I, _PI]),
     "phn_set_path": (_I, [ctypes.c_void_p, _I]),
     "phn_get_path": (_I, [ctypes.c_void_p, _PI]),
+    "phn_autotune": (_I, [ctypes.c_void_p, _I, _PI, _PD]),
+    "phn_num_variants": (_I, [ctypes.c_void_p, _PI]),
+    "phn_set_variant": (_I, [ctypes.c_void_p, _I]),
     "phn_device_fields": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
                                ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
     "phn_synchronize": (_I, [ctypes.c_void_p]),

@@ -169,10 +169,23 @@ int phn_create(const phn_params *params, phn_handle **out) {
     CKF(cudaMemsetAsync(h->cphi, 0, bytes, h->stream));
     CKF(cudaMemsetAsync(h->cpi, 0, bytes, h->stream));
   }
-  h->tma_grid = tma_supported(*params) ? tma_grid(*params) : 0;
+  // default variant: 8-row tiles with pi streamed from HBM from N = 256 up
+  // (fewer y-halo re-reads), 4-row tiles below; phn_autotune can override
+  h->tma_variant = params->N >= 256 ? 1 : 0;
+  h->tma_grid = tma_supported(*params) ? tma_grid(*params, h->tma_variant) : 0;
+  if (h->tma_grid == 0 && tma_supported(*params)) {
+    h->tma_variant = 0;
+    h->tma_grid = tma_grid(*params, 0);
+  }
   h->path = h->tma_grid > 0 ? PHN_PATH_TMA : PHN_PATH_PLAIN;
   {
-    const int recs = h->grid.nblocks > h->tma_grid ? h->grid.nblocks : h->tma_grid;
+    int recs = h->grid.nblocks;
+    if (h->tma_grid > 0)
+      for (int v = 0; v < tma_num_variants(params->N); ++v) {
+        const int g = tma_grid(*params, v);
+        if (g > recs) recs = g;
+      }
+    h->partial_cap = recs;
     CKF(cudaMalloc(&h->partials, (size_t)recs * REC * sizeof(double)));
   }
   CKF(cudaMalloc(&h->d_err, sizeof(int)));
@@ -285,7 +298,7 @@ static int step_once(phn_handle *h, int mode) {
       break;
     case PHN_FP32:
       if (h->path == PHN_PATH_TMA && mode != MODE_OBS) {
-        e = launch_step_f32_tma(h->k, h->tma_grid, mode == MODE_STEP_OBS, (const float *)h->phi[h->cur],
+        e = launch_step_f32_tma(h->k, h->tma_variant, h->tma_grid, mode == MODE_STEP_OBS, (const float *)h->phi[h->cur],
                                 (float *)h->phi[nxt], (float *)h->pi, s, h->partials, h->d_err, h->stream);
         if (mode == MODE_STEP_OBS) h->obs_records = h->tma_grid;
       } else {
@@ -440,6 +453,68 @@ int phn_set_path(phn_handle *h, int path) {
   if (path == PHN_PATH_TMA && h->tma_grid == 0)
     return set_error(PHN_ERR_UNSUPPORTED, "TMA step needs FP32, Nc = 1, N in {128,256,384,512,768,1024}");
   h->path = path;
+  return PHN_OK;
+}
+
+int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms) {
+  if (!h || steps < 1) return set_error(PHN_ERR_INVALID, "bad argument");
+  if (h->tma_grid == 0 || h->path != PHN_PATH_TMA) {
+    if (variant) *variant = -1;
+    if (best_ms) *best_ms = 0.0;
+    return PHN_OK;  // one kernel only: nothing to choose
+  }
+  int r = ensure_ref_staging(h);
+  if (r) return r;
+  // pi is updated in place by a step: keep a copy and put it back after each
+  // trial, so the lattice state is unchanged by tuning (phi[cur] is only read)
+  const size_t bytes = h->V * h->elem;
+  const StepF s = {h->dtau, h->dtau};
+  double best = 1e30;
+  int best_v = h->tma_variant;
+  CK(cudaMemcpyAsync(h->d_ref, h->pi, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  for (int v = 0; v < tma_num_variants(h->p.N); ++v) {
+    const int g = tma_grid(h->p, v);
+    if (g <= 0) continue;
+    for (int i = 0; i < steps + 2; ++i) {
+      if (i == 2) CK(cudaEventRecord(h->ev0, h->stream));
+      CK(launch_step_f32_tma(h->k, v, g, false, (const float *)h->phi[h->cur], (float *)h->phi[1 - h->cur],
+                             (float *)h->pi, s, h->partials, h->d_err, h->stream));
+      h->launches++;
+    }
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaEventSynchronize(h->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    CK(cudaMemcpyAsync(h->pi, h->d_ref, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    if (ms / steps < best) {
+      best = ms / steps;
+      best_v = v;
+    }
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  r = check_device_error(h);
+  if (r) return r;
+  h->tma_variant = best_v;
+  h->tma_grid = tma_grid(h->p, best_v);
+  if (variant) *variant = best_v;
+  if (best_ms) *best_ms = best;
+  return PHN_OK;
+}
+
+int phn_set_variant(phn_handle *h, int variant) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (h->tma_grid == 0) return set_error(PHN_ERR_UNSUPPORTED, "no kernel variants on this handle");
+  if (variant < 0 || variant >= tma_num_variants(h->p.N)) return set_error(PHN_ERR_INVALID, "variant %d", variant);
+  const int g = tma_grid(h->p, variant);
+  if (g <= 0) return set_error(PHN_ERR_UNSUPPORTED, "variant %d does not fit this device", variant);
+  h->tma_variant = variant;
+  h->tma_grid = g;
+  return PHN_OK;
+}
+
+int phn_num_variants(const phn_handle *h, int *n) {
+  if (!h || !n) return set_error(PHN_ERR_INVALID, "NULL argument");
+  *n = h->tma_grid > 0 ? tma_num_variants(h->p.N) : 0;
   return PHN_OK;
 }
 

@@ -1,59 +1,66 @@
 // TMA-pipelined leapfrog step for FP32 fields, one component, N a multiple
 // of 128 (the production path for the large lattices).
 //
-// Same arithmetic as step_f32 (leapfrog.cu) -- the two kernels produce
+// Same arithmetic as step_f32 (leapfrog.cu) -- the kernels produce
 // bit-identical fields -- with a different memory pipeline:
 //   * a persistent grid (blocks = SMs x resident blocks); block b owns the
 //     contiguous range [W*b/G, W*(b+1)/G) of the plane-tiles
-//     w = tile*N + z, tile = 4 full lattice rows, so work is balanced to one
-//     plane-tile and each block marches long runs of z;
+//     w = tile*N + z, a tile being TY full lattice rows, so work is balanced
+//     to one plane-tile and each block marches long runs of z;
 //   * one producer lane issues 1-D bulk copies (cp.async.bulk, the TMA
 //     engine) of each plane-tile into a ring of S shared-memory stages:
-//     phi rows y0-1 .. y0+4 (y halo, periodic wrap as two copies) and the
-//     tile's pi rows, completing on the stage's "full" mbarrier;
-//   * four consumer warps (one per row) read the stage, take x neighbours by
+//     phi rows y0-1 .. y0+TY (y halo, periodic wrap as two copies) and, in
+//     the PI_SMEM variants, the tile's pi rows, completing on the stage's
+//     "full" mbarrier;
+//   * TY consumer warps (one per row) read the stage, take x neighbours by
 //     warp shuffles (a warp holds whole rows, so the periodic x wrap is a
-//     shuffle too), keep phi(z-1), phi(z), phi(z+1) in registers, write
-//     pi' and phi' with 16-byte stores, then release the stage on its
-//     "empty" mbarrier.
-// HBM traffic per site: phi read once (+ the y-halo rows, served by L2),
-// pi read once, pi' and phi' written once: the 16-byte algorithmic minimum.
+//     shuffle too), keep phi(z-1), phi(z), phi(z+1) in registers, stream pi
+//     (from the stage, or straight from HBM one plane ahead), write pi' and
+//     phi' with 16-byte stores, then release the stage on its "empty"
+//     mbarrier.
+// HBM traffic per site: phi once plus the y halo ((TY+2)/TY, partly served by
+// L2), pi once, pi' and phi' once: 16 B algorithmic.
+//
+// Variants (TY, S, PI_SMEM) trade halo re-reads against shared memory per
+// block; phn_autotune times them on the live lattice and keeps the fastest.
 #include "observe.cuh"
 #include "phn_internal.h"
 #include "tma.cuh"
 
 namespace phn {
 
-constexpr int TMA_TY = 4;                       // lattice rows per tile (= consumer warps)
-constexpr int TMA_THREADS = (TMA_TY + 1) * 32;  // + one producer warp
+struct TmaVariant {
+  int ty, stages;
+  bool pi_smem;
+};
+// index = variant id
+constexpr TmaVariant kTmaVariants[] = {{4, 4, true}, {8, 4, false}, {8, 5, false}, {4, 6, false}};
+constexpr int kNumTmaVariants = 4;
 
-template <int K>
+template <int K, int TY, int S, bool PI_SMEM>
 struct TmaShape {
   static constexpr int N = K * 128;
-  static constexpr int PHI_ROWS = TMA_TY + 2;
-  static constexpr int STAGE_FLOATS = (PHI_ROWS + TMA_TY) * N;
+  static constexpr int PHI_ROWS = TY + 2;
+  static constexpr int STAGE_FLOATS = (PHI_ROWS + (PI_SMEM ? TY : 0)) * N;
   static constexpr uint32_t PHI_BYTES = PHI_ROWS * N * 4;
-  static constexpr uint32_t PI_BYTES = TMA_TY * N * 4;
+  static constexpr uint32_t PI_BYTES = TY * N * 4;
+  static constexpr int THREADS = (TY + 1) * 32;
+  static constexpr size_t SMEM = 128 + (size_t)S * STAGE_FLOATS * sizeof(float);
 };
-
-template <int K, int S>
-constexpr size_t tma_smem_bytes() {
-  return 128 + (size_t)S * TmaShape<K>::STAGE_FLOATS * sizeof(float);
-}
 
 __device__ __forceinline__ float get(const float4 &v, int e) {
   return e == 0 ? v.x : (e == 1 ? v.y : (e == 2 ? v.z : v.w));
 }
 
-template <int K, int THEORY, bool OBS, int S>
-__global__ void __launch_bounds__(TMA_THREADS) step_f32_tma(const float *__restrict__ phi, float *__restrict__ phi_out,
-                                                            float *__restrict__ pi, const Consts k, const float fk,
-                                                            const float fd, double *__restrict__ partials,
-                                                            int *__restrict__ err) {
-  using Sh = TmaShape<K>;
+template <int K, int TY, int S, bool PI_SMEM, int THEORY, bool OBS>
+__global__ void __launch_bounds__((TY + 1) * 32) step_f32_tma(const float *__restrict__ phi,
+                                                              float *__restrict__ phi_out, float *__restrict__ pi,
+                                                              const Consts k, const float fk, const float fd,
+                                                              double *__restrict__ partials, int *__restrict__ err) {
+  using Sh = TmaShape<K, TY, S, PI_SMEM>;
   constexpr int N = Sh::N;
   constexpr long long NN = (long long)N * N;
-  constexpr long long W = (long long)(N / TMA_TY) * N;
+  constexpr long long W = (long long)(N / TY) * N;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ int abort_flag;
   uint64_t *bars = (uint64_t *)smem;  // full[S], empty[S]
@@ -64,7 +71,7 @@ __global__ void __launch_bounds__(TMA_THREADS) step_f32_tma(const float *__restr
     abort_flag = 0;
     for (int s = 0; s < S; ++s) {
       mbar_init(smem_u32(&bars[s]), 1);
-      mbar_init(smem_u32(&bars[S + s]), TMA_TY);
+      mbar_init(smem_u32(&bars[S + s]), TY);
     }
     mbar_fence_init();
   }
@@ -73,7 +80,7 @@ __global__ void __launch_bounds__(TMA_THREADS) step_f32_tma(const float *__restr
   AccF accf;
   if (OBS) accf.init();
 
-  if (warp == TMA_TY) {
+  if (warp == TY) {
     // ---------------------------------------------------------- producer
     if (lane == 0) {
       long long L = 0;
@@ -82,10 +89,10 @@ __global__ void __launch_bounds__(TMA_THREADS) step_f32_tma(const float *__restr
         const int t = (int)(w / N), za = (int)(w % N);
         const long long wend = min(w1, (long long)(t + 1) * N);
         const int zb = za + (int)(wend - w);
-        const int y0 = t * TMA_TY;
+        const int y0 = t * TY;
         for (int j = -1; j <= zb - za && ok; ++j) {
           const int z = (za + j + N) % N;
-          const bool center = (j >= 0 && j < zb - za);
+          const bool center = PI_SMEM && (j >= 0 && j < zb - za);
           const int s = (int)(L % S);
           const long long n = L / S;
           if (n > 0) {
@@ -99,12 +106,12 @@ __global__ void __launch_bounds__(TMA_THREADS) step_f32_tma(const float *__restr
           constexpr uint32_t ROWB = N * 4;
           if (y0 == 0) {
             bulk_g2s(dst, plane + (long long)(N - 1) * N, ROWB, full);
-            bulk_g2s(dst + ROWB, plane, ROWB * (TMA_TY + 1), full);
-          } else if (y0 + TMA_TY == N) {
-            bulk_g2s(dst, plane + (long long)(y0 - 1) * N, ROWB * (TMA_TY + 1), full);
-            bulk_g2s(dst + ROWB * (TMA_TY + 1), plane, ROWB, full);
+            bulk_g2s(dst + ROWB, plane, ROWB * (TY + 1), full);
+          } else if (y0 + TY == N) {
+            bulk_g2s(dst, plane + (long long)(y0 - 1) * N, ROWB * (TY + 1), full);
+            bulk_g2s(dst + ROWB * (TY + 1), plane, ROWB, full);
           } else {
-            bulk_g2s(dst, plane + (long long)(y0 - 1) * N, ROWB * (TMA_TY + 2), full);
+            bulk_g2s(dst, plane + (long long)(y0 - 1) * N, ROWB * (TY + 2), full);
           }
           if (center) bulk_g2s(dst + Sh::PHI_BYTES, pi + (long long)z * NN + (long long)y0 * N, Sh::PI_BYTES, full);
           ++L;
@@ -121,14 +128,19 @@ __global__ void __launch_bounds__(TMA_THREADS) step_f32_tma(const float *__restr
   } else {
     // ---------------------------------------------------------- consumers
     long long L = 0;
-    float4 cm[K], c[K], cp[K];
+    float4 cm[K], c[K], cp[K], pnx[K];
     const int r = warp;  // row within the tile
     bool ok = true;
     for (long long w = w0; w < w1 && ok;) {
       const int t = (int)(w / N), za = (int)(w % N);
       const long long wend = min(w1, (long long)(t + 1) * N);
       const int zb = za + (int)(wend - w);
-      const int y = t * TMA_TY + r;
+      const int y = t * TY + r;
+      if (!PI_SMEM) {
+#pragma unroll
+        for (int q = 0; q < K; ++q)
+          pnx[q] = __ldcs((const float4 *)(pi + (long long)za * NN + (long long)y * N + 128 * q + 4 * lane));
+      }
       // plane za-1: its centre row becomes phi(z-1)
       {
         const int s = (int)(L % S);
@@ -154,19 +166,26 @@ __global__ void __launch_bounds__(TMA_THREADS) step_f32_tma(const float *__restr
       for (int z = za; z < zb; ++z) {
         const int sz = (int)((L - 1) % S);
         const int s1 = (int)(L % S);
+        const long long gz = (long long)z * NN + (long long)y * N;
+        float4 pcur[K];
+#pragma unroll
+        for (int q = 0; q < K; ++q) pcur[q] = pnx[q];
+        if (!PI_SMEM && z + 1 < zb) {
+#pragma unroll
+          for (int q = 0; q < K; ++q) pnx[q] = __ldcs((const float4 *)(pi + gz + NN + 128 * q + 4 * lane));
+        }
         ok = mbar_wait(smem_u32(&bars[s1]), (uint32_t)((L / S) & 1), err, 2, &abort_flag);
         if (!ok) break;
         const float *nrow = stages + (size_t)s1 * Sh::STAGE_FLOATS + (r + 1) * N;
 #pragma unroll
         for (int q = 0; q < K; ++q) cp[q] = *(const float4 *)(nrow + 128 * q + 4 * lane);
         const float *st = stages + (size_t)sz * Sh::STAGE_FLOATS;
-        const long long gz = (long long)z * NN + (long long)y * N;
 #pragma unroll
         for (int q = 0; q < K; ++q) {
           const int x0 = 128 * q + 4 * lane;
           const float4 ym = *(const float4 *)(st + r * N + x0);
           const float4 yp = *(const float4 *)(st + (r + 2) * N + x0);
-          const float4 pv = *(const float4 *)(st + (Sh::PHI_ROWS + r) * N + x0);
+          const float4 pv = PI_SMEM ? *(const float4 *)(st + (Sh::PHI_ROWS + r) * N + x0) : pcur[q];
           // x neighbours: within the lane, from lanes -+1, and across chunks at the warp edges
           float left = __shfl_up_sync(0xffffffffu, c[q].w, 1);
           const float lwrap = __shfl_sync(0xffffffffu, c[(q + K - 1) % K].w, 31);
@@ -223,78 +242,110 @@ __global__ void __launch_bounds__(TMA_THREADS) step_f32_tma(const float *__restr
   }
   if (OBS) {
     Acc acc;
-    if (warp < TMA_TY)
+    if (warp < TY)
       accf.to_double(acc);
     else
       acc.init();
-    block_store_n(acc, partials, tid, TMA_THREADS / 32, blockIdx.x);
+    block_store_n(acc, partials, tid, TY + 1, blockIdx.x);
   }
 }
 
-template <int K, int S>
-static cudaError_t launch_k(const Consts &k, int theory, bool obs, int grid, const float *phi, float *phi_out,
-                            float *pi, float fk, float fd, double *partials, int *err, cudaStream_t st) {
-  const size_t smem = tma_smem_bytes<K, S>();
-#define PHN_TMA_LAUNCH(TH, OB)                                                                        \
-  do {                                                                                                \
-    cudaError_t e = cudaFuncSetAttribute(step_f32_tma<K, TH, OB, S>,                                  \
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
-    if (e != cudaSuccess) return e;                                                                   \
-    step_f32_tma<K, TH, OB, S><<<grid, TMA_THREADS, smem, st>>>(phi, phi_out, pi, k, fk, fd, partials, err); \
-  } while (0)
-  if (theory == 0) {
-    if (obs) PHN_TMA_LAUNCH(0, true); else PHN_TMA_LAUNCH(0, false);
-  } else {
-    if (obs) PHN_TMA_LAUNCH(1, true); else PHN_TMA_LAUNCH(1, false);
+// --------------------------------------------------------------- dispatch
+template <int K, int TY, int S, bool PS>
+struct TmaLaunch {
+  using Sh = TmaShape<K, TY, S, PS>;
+  template <int TH, bool OB>
+  static const void *fn() {
+    return (const void *)step_f32_tma<K, TY, S, PS, TH, OB>;
   }
-#undef PHN_TMA_LAUNCH
-  return cudaGetLastError();
-}
+  static cudaError_t prepare() {
+    cudaError_t e;
+    const void *fns[4] = {fn<0, false>(), fn<0, true>(), fn<1, false>(), fn<1, true>()};
+    for (const void *f : fns)
+      if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Sh::SMEM)) != cudaSuccess)
+        return e;
+    return cudaSuccess;
+  }
+  static int occupancy() {
+    int occ = 0;
+    if (prepare() != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn<0, false>(), Sh::THREADS, Sh::SMEM) != cudaSuccess)
+      return 0;
+    return occ;
+  }
+  static cudaError_t launch(const Consts &k, bool obs, int grid, const float *phi, float *phi_out, float *pi,
+                            float fk, float fd, double *partials, int *err, cudaStream_t st) {
+    if (k.theory == 0) {
+      if (obs)
+        step_f32_tma<K, TY, S, PS, 0, true><<<grid, Sh::THREADS, Sh::SMEM, st>>>(phi, phi_out, pi, k, fk, fd, partials, err);
+      else
+        step_f32_tma<K, TY, S, PS, 0, false><<<grid, Sh::THREADS, Sh::SMEM, st>>>(phi, phi_out, pi, k, fk, fd, partials, err);
+    } else {
+      if (obs)
+        step_f32_tma<K, TY, S, PS, 1, true><<<grid, Sh::THREADS, Sh::SMEM, st>>>(phi, phi_out, pi, k, fk, fd, partials, err);
+      else
+        step_f32_tma<K, TY, S, PS, 1, false><<<grid, Sh::THREADS, Sh::SMEM, st>>>(phi, phi_out, pi, k, fk, fd, partials, err);
+    }
+    return cudaGetLastError();
+  }
+};
 
-constexpr int TMA_STAGES = 4;
+// Calls F<K, TY, S, PI_SMEM>::... for the runtime (K, variant).
+#define PHN_TMA_SWITCH(KV, VAR, EXPR_T, FAIL)                                   \
+  switch ((KV) * 16 + (VAR)) {                                                  \
+    case 1 * 16 + 0: { using T = TmaLaunch<1, 4, 4, true>; EXPR_T; }            \
+    case 1 * 16 + 1: { using T = TmaLaunch<1, 8, 4, false>; EXPR_T; }           \
+    case 1 * 16 + 2: { using T = TmaLaunch<1, 8, 5, false>; EXPR_T; }           \
+    case 1 * 16 + 3: { using T = TmaLaunch<1, 4, 6, false>; EXPR_T; }           \
+    case 2 * 16 + 0: { using T = TmaLaunch<2, 4, 4, true>; EXPR_T; }            \
+    case 2 * 16 + 1: { using T = TmaLaunch<2, 8, 4, false>; EXPR_T; }           \
+    case 2 * 16 + 2: { using T = TmaLaunch<2, 8, 5, false>; EXPR_T; }           \
+    case 2 * 16 + 3: { using T = TmaLaunch<2, 4, 6, false>; EXPR_T; }           \
+    case 3 * 16 + 0: { using T = TmaLaunch<3, 4, 4, true>; EXPR_T; }            \
+    case 3 * 16 + 1: { using T = TmaLaunch<3, 8, 4, false>; EXPR_T; }           \
+    case 4 * 16 + 0: { using T = TmaLaunch<4, 4, 4, true>; EXPR_T; }            \
+    case 4 * 16 + 1: { using T = TmaLaunch<4, 8, 4, false>; EXPR_T; }           \
+    case 4 * 16 + 2: { using T = TmaLaunch<4, 8, 5, false>; EXPR_T; }           \
+    case 4 * 16 + 3: { using T = TmaLaunch<4, 4, 6, false>; EXPR_T; }           \
+    case 6 * 16 + 0: { using T = TmaLaunch<6, 4, 4, true>; EXPR_T; }            \
+    case 6 * 16 + 1: { using T = TmaLaunch<6, 8, 3, false>; EXPR_T; }           \
+    case 8 * 16 + 0: { using T = TmaLaunch<8, 4, 3, true>; EXPR_T; }            \
+    case 8 * 16 + 1: { using T = TmaLaunch<8, 8, 3, false>; EXPR_T; }           \
+    default: FAIL;                                                              \
+  }
 
 bool tma_supported(const phn_params &p) {
-  return p.Nc == 1 && p.precision == PHN_FP32 && p.N % 128 == 0 && p.N >= 128 && p.N <= 1024 &&
-         (p.N / 128 == 1 || p.N / 128 == 2 || p.N / 128 == 3 || p.N / 128 == 4 || p.N / 128 == 6 ||
-          p.N / 128 == 8);
+  if (p.Nc != 1 || p.precision != PHN_FP32 || p.N % 128 != 0) return false;
+  const int K = p.N / 128;
+  return K == 1 || K == 2 || K == 3 || K == 4 || K == 6 || K == 8;
 }
 
-// Blocks of the persistent grid: SMs x resident blocks per SM.
-int tma_grid(const phn_params &p) {
-  int dev = 0, sms = 0, occ = 0;
+int tma_num_variants(int N) {
+  const int K = N / 128;
+  return (K == 1 || K == 2 || K == 4) ? kNumTmaVariants : 2;
+}
+
+// Persistent grid for a variant: SMs x resident blocks (0 if it cannot run).
+int tma_grid(const phn_params &p, int variant) {
+  int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int K = p.N / 128;
-  size_t smem = 0;
-  const void *fn = nullptr;
-  switch (K) {
-    case 1: smem = tma_smem_bytes<1, TMA_STAGES>(); fn = (const void *)step_f32_tma<1, 0, false, TMA_STAGES>; break;
-    case 2: smem = tma_smem_bytes<2, TMA_STAGES>(); fn = (const void *)step_f32_tma<2, 0, false, TMA_STAGES>; break;
-    case 3: smem = tma_smem_bytes<3, TMA_STAGES>(); fn = (const void *)step_f32_tma<3, 0, false, TMA_STAGES>; break;
-    case 4: smem = tma_smem_bytes<4, TMA_STAGES>(); fn = (const void *)step_f32_tma<4, 0, false, TMA_STAGES>; break;
-    case 6: smem = tma_smem_bytes<6, TMA_STAGES>(); fn = (const void *)step_f32_tma<6, 0, false, TMA_STAGES>; break;
-    default: smem = tma_smem_bytes<8, TMA_STAGES>(); fn = (const void *)step_f32_tma<8, 0, false, TMA_STAGES>; break;
-  }
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, TMA_THREADS, smem) != cudaSuccess || occ < 1) occ = 1;
-  const long long W = (long long)(p.N / TMA_TY) * p.N;
+  int occ = 0, ty = 0;
+  PHN_TMA_SWITCH(K, variant, occ = T::occupancy(); ty = T::Sh::THREADS / 32 - 1; break, return 0);
+  if (occ < 1) return 0;
+  const long long W = (long long)(p.N / ty) * p.N;
   long long g = (long long)sms * occ;
   if (g > W) g = W;
   return (int)g;
 }
 
-cudaError_t launch_step_f32_tma(const Consts &k, int grid, bool obs, const float *phi, float *phi_out, float *pi,
-                                StepF s, double *partials, int *err, cudaStream_t st) {
+cudaError_t launch_step_f32_tma(const Consts &k, int variant, int grid, bool obs, const float *phi, float *phi_out,
+                                float *pi, StepF s, double *partials, int *err, cudaStream_t st) {
   const float fk = (float)s.fk, fd = (float)s.fd;
-  switch (k.N / 128) {
-    case 1: return launch_k<1, TMA_STAGES>(k, k.theory, obs, grid, phi, phi_out, pi, fk, fd, partials, err, st);
-    case 2: return launch_k<2, TMA_STAGES>(k, k.theory, obs, grid, phi, phi_out, pi, fk, fd, partials, err, st);
-    case 3: return launch_k<3, TMA_STAGES>(k, k.theory, obs, grid, phi, phi_out, pi, fk, fd, partials, err, st);
-    case 4: return launch_k<4, TMA_STAGES>(k, k.theory, obs, grid, phi, phi_out, pi, fk, fd, partials, err, st);
-    case 6: return launch_k<6, TMA_STAGES>(k, k.theory, obs, grid, phi, phi_out, pi, fk, fd, partials, err, st);
-    case 8: return launch_k<8, TMA_STAGES>(k, k.theory, obs, grid, phi, phi_out, pi, fk, fd, partials, err, st);
-    default: return cudaErrorInvalidValue;
-  }
+  PHN_TMA_SWITCH(k.N / 128, variant,
+                 return T::launch(k, obs, grid, phi, phi_out, pi, fk, fd, partials, err, st),
+                 return cudaErrorInvalidValue);
 }
 
 }  // namespace phn

@@ -84,11 +84,13 @@ cudaError_t launch_step_kahan(const Consts &k, const Grid &g, int mode, const fl
 cudaError_t launch_finalize(const Consts &k, const double *partials, int nblocks, phn_averages *out,
                             cudaStream_t st);
 
-// TMA-pipelined FP32 step (leapfrog_tma.cu): Nc = 1, N in {128,256,384,512,768,1024}.
+// TMA-pipelined FP32 step (leapfrog_tma.cu): Nc = 1, N in {128,256,384,512,768,1024};
+// variants are tile heights / stage counts, all bit-identical.
 bool tma_supported(const phn_params &p);
-int tma_grid(const phn_params &p);
-cudaError_t launch_step_f32_tma(const Consts &k, int grid, bool obs, const float *phi, float *phi_out, float *pi,
-                                StepF s, double *partials, int *err, cudaStream_t st);
+int tma_num_variants(int N);
+int tma_grid(const phn_params &p, int variant);
+cudaError_t launch_step_f32_tma(const Consts &k, int variant, int grid, bool obs, const float *phi, float *phi_out,
+                                float *pi, StepF s, double *partials, int *err, cudaStream_t st);
 
 // Layout conversion between the reference layout (host order, ghosts) and
 // the device SoA layout [a][z][y][x] (layout.cu).
@@ -123,6 +125,8 @@ struct phn_handle {
   int cur;             // phi[cur] holds the current field
   int path;            // PHN_PATH_* in use for FP32 steps
   int tma_grid;        // persistent grid of the TMA step kernel (0: unsupported)
+  int tma_variant;     // TMA kernel variant in use (phn_autotune picks it)
+  int partial_cap;     // block records the partials buffer holds
   int obs_records;     // block records written by the last observation launch
   int *d_err;          // device error word of bounded waits (0: none)
   double *partials;    // block records of the fused observation

@@ -288,16 +288,44 @@ def test_tma_path_matches_plain_path_bit_for_bit(N, theory):
     phi_i, pi_i = inputs.lattice_fields(N, 1, 40 + theory, phi0=(-1) ** theory * 6 ** 0.5)
     phi, pi = O.to_ref_layout(phi_i), O.to_ref_layout(pi_i)
     kw = dict(theory=0) if theory == 0 else dict(theory=1, mass_mode=-1, lambda_mode=1, h=0.12247)
+    import ctypes
     out = {}
-    for path in (L.PATH_PLAIN, L.PATH_TMA):
+    lat = PL.Lattice(PL.Params(N=N, precision=1, **kw))
+    nv = ctypes.c_int()
+    L.check(lat.lib.phn_num_variants(lat.h, ctypes.byref(nv)))
+    lat.close()
+    assert nv.value >= 2
+    for path, variant in [(L.PATH_PLAIN, None)] + [(L.PATH_TMA, v) for v in range(nv.value)]:
         lat = PL.Lattice(PL.Params(N=N, precision=1, **kw))
         L.check(lat.lib.phn_set_path(lat.h, path))
+        if variant is not None:
+            L.check(lat.lib.phn_set_variant(lat.h, variant))
         lat.upload(phi, pi)
         rows = lat.run_loop(120, 0.5)
         lat.evolve(7)
-        out[path] = (rows,) + lat.download()
+        out[(path, variant)] = (rows,) + lat.download()
         lat.close()
-    (r0, f0, p0), (r1, f1, p1) = out[L.PATH_PLAIN], out[L.PATH_TMA]
-    assert np.array_equal(f0, f1) and np.array_equal(p0[N * N:-N * N], p1[N * N:-N * N])
-    assert np.array_equal(r0[:, 17:23], r1[:, 17:23])
-    np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
+    r0, f0, p0 = out[(L.PATH_PLAIN, None)]
+    for key, (r1, f1, p1) in out.items():
+        assert np.array_equal(f0, f1) and np.array_equal(p0[N * N:-N * N], p1[N * N:-N * N]), key
+        assert np.array_equal(r0[:, 17:23], r1[:, 17:23]), key
+        np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
+
+
+def test_autotune_keeps_state_and_picks_a_variant():
+    import ctypes
+    import inputs
+    PL = gpu()
+    from phinum_gb300 import _lib as L
+    N = 256
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 5)
+    lat = PL.Lattice(PL.Params(N=N, precision=1))
+    lat.upload(O.to_ref_layout(phi_i), O.to_ref_layout(pi_i))
+    lat.evolve(3)
+    before = lat.download()
+    v, ms = ctypes.c_int(), ctypes.c_double()
+    L.check(lat.lib.phn_autotune(lat.h, 5, ctypes.byref(v), ctypes.byref(ms)))
+    after = lat.download()
+    assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
+    assert v.value >= 0 and ms.value > 0
+    lat.close()
