@@ -29,13 +29,24 @@
 
 namespace phn {
 
-struct TmaVariant {
+// Kernel configurations (tile height TY, stages S, pi through shared memory)
+// and variants = configuration x grid policy.  "aligned" grids use
+// G = (N/TY) * m blocks with m | N, so a block's range of plane-tiles is
+// N/m planes of one tile and the blocks working on vertically adjacent tiles
+// are at the same z at the same time: the y-halo rows one block loads are the
+// rows its neighbours loaded moments earlier, still in L2.
+struct TmaConfig {
   int ty, stages;
   bool pi_smem;
 };
-// index = variant id
-constexpr TmaVariant kTmaVariants[] = {{4, 4, true}, {8, 4, false}, {8, 5, false}, {4, 6, false}};
-constexpr int kNumTmaVariants = 4;
+constexpr TmaConfig kTmaConfigs[] = {{4, 4, true}, {8, 4, false}, {8, 5, false}, {4, 6, false}};
+struct TmaVariantDef {
+  int config;
+  bool aligned;
+};
+constexpr TmaVariantDef kTmaVariants[] = {{0, false}, {1, false}, {2, false}, {3, false},
+                                          {1, true},  {0, true},  {2, true}};
+constexpr int kNumTmaVariants = 7;
 
 template <int K, int TY, int S, bool PI_SMEM>
 struct TmaShape {
@@ -180,6 +191,8 @@ __global__ void __launch_bounds__((TY + 1) * 32) step_f32_tma(const float *__res
 #pragma unroll
         for (int q = 0; q < K; ++q) cp[q] = *(const float4 *)(nrow + 128 * q + 4 * lane);
         const float *st = stages + (size_t)sz * Sh::STAGE_FLOATS;
+        PlaneF plane;
+        if (OBS) plane.clear();
 #pragma unroll
         for (int q = 0; q < K; ++q) {
           const int x0 = 128 * q + 4 * lane;
@@ -201,10 +214,7 @@ __global__ void __launch_bounds__((TY + 1) * 32) step_f32_tma(const float *__res
             const float xp = e == 3 ? right : get(c[q], e + 1);
             const float ymv = get(ym, e), ypv = get(yp, e), zm = get(cm[q], e), zp = get(cp[q], e);
             const float pp = get(pv, e);
-            if (OBS) {
-              const float fxp1[1] = {xp}, fyp1[1] = {ypv}, fzp1[1] = {zp}, c1[1] = {cc}, p1[1] = {pp};
-              observe_f32<1, THEORY>(accf, k, c1, p1, fxp1, fyp1, fzp1, gz + NN + x0 + e);
-            }
+            if (OBS) observe_site<THEORY>(plane, accf, k, cc, pp, xp, ypv, zp, gz + NN + x0 + e);
             const float lap = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(xp, xm), __fadd_rn(ypv, ymv)),
                                                             __fadd_rn(zp, zm)),
                                                   __fmul_rn(-6.f, cc)),
@@ -224,6 +234,7 @@ __global__ void __launch_bounds__((TY + 1) * 32) step_f32_tma(const float *__res
           *(float4 *)(pi + gz + x0) = pn;
           *(float4 *)(phi_out + gz + x0) = fn;
         }
+        if (OBS) flush_plane(accf, plane);
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(&bars[S + sz]));
 #pragma unroll
@@ -291,8 +302,8 @@ struct TmaLaunch {
 };
 
 // Calls F<K, TY, S, PI_SMEM>::... for the runtime (K, variant).
-#define PHN_TMA_SWITCH(KV, VAR, EXPR_T, FAIL)                                   \
-  switch ((KV) * 16 + (VAR)) {                                                  \
+#define PHN_TMA_SWITCH(KV, CFG, EXPR_T, FAIL)                                   \
+  switch ((KV) * 16 + (CFG)) {                                                  \
     case 1 * 16 + 0: { using T = TmaLaunch<1, 4, 4, true>; EXPR_T; }            \
     case 1 * 16 + 1: { using T = TmaLaunch<1, 8, 4, false>; EXPR_T; }           \
     case 1 * 16 + 2: { using T = TmaLaunch<1, 8, 5, false>; EXPR_T; }           \
@@ -320,30 +331,51 @@ bool tma_supported(const phn_params &p) {
   return K == 1 || K == 2 || K == 3 || K == 4 || K == 6 || K == 8;
 }
 
-int tma_num_variants(int N) {
-  const int K = N / 128;
-  return (K == 1 || K == 2 || K == 4) ? kNumTmaVariants : 2;
+static bool config_built(int K, int cfg) { return (K == 1 || K == 2 || K == 4) ? cfg < 4 : cfg < 2; }
+static bool all_configs(int N) { return N / 128 == 1 || N / 128 == 2 || N / 128 == 4; }
+
+int tma_num_variants(int N) { return all_configs(N) ? kNumTmaVariants : 4; }
+
+// Row of kTmaVariants behind a handle-level variant number: sizes with only
+// configurations 0 and 1 built expose variants {0, 1, 4, 5}.
+static int variant_row(int N, int variant) {
+  static const int remap[4] = {0, 1, 4, 5};
+  return all_configs(N) ? variant : remap[variant];
 }
 
-// Persistent grid for a variant: SMs x resident blocks (0 if it cannot run).
+// Persistent grid for a variant: SMs x resident blocks, or the aligned size
+// (0 if the variant cannot run here).
 int tma_grid(const phn_params &p, int variant) {
+  if (variant < 0 || variant >= tma_num_variants(p.N)) return 0;
+  const TmaVariantDef v = kTmaVariants[variant_row(p.N, variant)];
+  const int K = p.N / 128;
+  if (!config_built(K, v.config)) return 0;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int K = p.N / 128;
-  int occ = 0, ty = 0;
-  PHN_TMA_SWITCH(K, variant, occ = T::occupancy(); ty = T::Sh::THREADS / 32 - 1; break, return 0);
+  int occ = 0;
+  PHN_TMA_SWITCH(K, v.config, occ = T::occupancy(); break, return 0);
   if (occ < 1) return 0;
-  const long long W = (long long)(p.N / ty) * p.N;
+  const int ty = kTmaConfigs[v.config].ty;
+  const long long NT = p.N / ty, W = NT * p.N;
   long long g = (long long)sms * occ;
+  if (v.aligned) {
+    long long best = 0;
+    for (long long m = 1; m <= p.N; ++m)
+      if (p.N % m == 0 && NT * m <= g && p.N / m >= 8) best = NT * m;
+    if (best == 0) return 0;
+    g = best;
+  }
   if (g > W) g = W;
   return (int)g;
 }
 
+static int tma_config_of(int N, int variant) { return kTmaVariants[variant_row(N, variant)].config; }
+
 cudaError_t launch_step_f32_tma(const Consts &k, int variant, int grid, bool obs, const float *phi, float *phi_out,
                                 float *pi, StepF s, double *partials, int *err, cudaStream_t st) {
   const float fk = (float)s.fk, fd = (float)s.fd;
-  PHN_TMA_SWITCH(k.N / 128, variant,
+  PHN_TMA_SWITCH(k.N / 128, tma_config_of(k.N, variant),
                  return T::launch(k, obs, grid, phi, phi_out, pi, fk, fd, partials, err, st),
                  return cudaErrorInvalidValue);
 }

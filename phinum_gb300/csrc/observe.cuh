@@ -216,4 +216,49 @@ __device__ __forceinline__ void observe_f32(AccF &A, const Consts &k, const floa
   if ((r > A.absv || (r == A.absv && kidx < A.absi)) && r > 0.f) { A.absv = r; A.absi = kidx; }
 }
 
+// Single-component form for the TMA kernel: per-site terms go into plain FP32
+// partials of the current plane (16 sites per lane), and only those partials
+// enter the compensated running totals -- one Kahan update per plane instead
+// of one per site.  Extrema are tracked per site.
+struct PlaneF {
+  float v[S_NONFINITE + 1];
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int j = 0; j <= S_NONFINITE; ++j) v[j] = 0.f;
+  }
+};
+
+template <int THEORY>
+__device__ __forceinline__ void observe_site(PlaneF &P, AccF &A, const Consts &k, float c, float p, float xp, float yp,
+                                             float zp, long long kidx) {
+  const float c2 = c * c;
+  P.v[S_PHI] += c;
+  P.v[S_PI] += p;
+  P.v[S_PHI2] += c2;
+  P.v[S_PI2] += p * p;
+  P.v[S_PHIPI] += c * p;
+  const float dx = xp - c, dy = yp - c, dz = zp - c;
+  P.v[S_GRAD] += (dx * dx + dy * dy + dz * dz) * k.inv_a2_f;
+  const float l2 = c2 * c2;
+  P.v[S_PHI4] += l2;
+  P.v[S_PHI6] += l2 * c2;
+  float inter = k.mmh_f * c2;
+  if (THEORY == 1) inter = fmaf(k.h_f, c, inter);
+  inter = fmaf(k.e4_f, l2, inter);
+  if (THEORY == 0) inter = fmaf(k.e6_f, l2 * c2, inter);
+  P.v[S_INTER] += inter;
+  if (!isfinite(c) || !isfinite(p)) P.v[S_NONFINITE] += 1.f;
+  if ((c > A.maxv || (c == A.maxv && kidx < A.maxi)) && c > -10000000.f) { A.maxv = c; A.maxi = kidx; }
+  if ((c < A.minv || (c == A.minv && kidx < A.mini)) && c < 10000000.f) { A.minv = c; A.mini = kidx; }
+  const float r = fabsf(c);  // sqrt(phi^2) for one component
+  if ((r > A.absv || (r == A.absv && kidx < A.absi)) && r > 0.f) { A.absv = r; A.absi = kidx; }
+}
+
+__device__ __forceinline__ void flush_plane(AccF &A, PlaneF &P) {
+#pragma unroll
+  for (int j = 0; j < S_NONFINITE; ++j) A.add(j, P.v[j]);
+  A.s[S_NONFINITE] += P.v[S_NONFINITE];
+  P.clear();
+}
+
 }  // namespace phn
