@@ -169,9 +169,10 @@ int phn_create(const phn_params *params, phn_handle **out) {
     CKF(cudaMemsetAsync(h->cphi, 0, bytes, h->stream));
     CKF(cudaMemsetAsync(h->cpi, 0, bytes, h->stream));
   }
-  // default variant: 8-row tiles with pi streamed from HBM from N = 256 up
-  // (fewer y-halo re-reads), 4-row tiles below; phn_autotune can override
-  h->tma_variant = params->N >= 256 ? 1 : 0;
+  // default variant from N = 256 up: 8-row tiles, pi streamed from HBM,
+  // aligned grid (fewer y-halo re-reads, halo rows served by L2); 4-row
+  // tiles below.  phn_autotune can override.
+  h->tma_variant = params->N >= 256 ? tma_default_variant(params->N) : 0;
   h->tma_grid = tma_supported(*params) ? tma_grid(*params, h->tma_variant) : 0;
   if (h->tma_grid == 0 && tma_supported(*params)) {
     h->tma_variant = 0;

@@ -336,6 +336,9 @@ static bool all_configs(int N) { return N / 128 == 1 || N / 128 == 2 || N / 128 
 
 int tma_num_variants(int N) { return all_configs(N) ? kNumTmaVariants : 4; }
 
+// 8-row tiles, pi from HBM, aligned grid (row 4 of kTmaVariants)
+int tma_default_variant(int N) { return all_configs(N) ? 4 : 2; }
+
 // Row of kTmaVariants behind a handle-level variant number: sizes with only
 // configurations 0 and 1 built expose variants {0, 1, 4, 5}.
 static int variant_row(int N, int variant) {

@@ -88,6 +88,7 @@ cudaError_t launch_finalize(const Consts &k, const double *partials, int nblocks
 // variants are tile heights / stage counts, all bit-identical.
 bool tma_supported(const phn_params &p);
 int tma_num_variants(int N);
+int tma_default_variant(int N);
 int tma_grid(const phn_params &p, int variant);
 cudaError_t launch_step_f32_tma(const Consts &k, int variant, int grid, bool obs, const float *phi, float *phi_out,
                                 float *pi, StepF s, double *partials, int *err, cudaStream_t st);
