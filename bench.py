@@ -181,7 +181,11 @@ def measure_gpu(args, dist: Dist):
     # (state unchanged; all variants compute identical fields)
     import ctypes
     tv, tms = ctypes.c_int(), ctypes.c_double()
-    L.check(lib.phn_autotune(lat.h, 10, ctypes.byref(tv), ctypes.byref(tms)))
+    if args.variant is None:
+        L.check(lib.phn_autotune(lat.h, 30, ctypes.byref(tv), ctypes.byref(tms)))
+    else:
+        L.check(lib.phn_set_variant(lat.h, args.variant))
+        tv.value = args.variant
     out["variant"] = tv.value
     lat.run_loop(max(3, args.warmup), 1.0)
     lat.synchronize()
@@ -306,6 +310,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the other sizes/precisions")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--n", type=int, default=N_MAIN, help="lattice edge (profiling runs use smaller cases)")
+    ap.add_argument("--variant", type=int, default=None, help="TMA kernel variant instead of the autotuner's pick")
     args = ap.parse_args()
     rank, local, world = env_rank()
     config = {"workload": f"phi^6 oscillon (theory 0, Kappa=sqrt(3)), {args.n}^3 periodic lattice, a=0.25, "

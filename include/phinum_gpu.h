@@ -58,7 +58,9 @@ enum {
 typedef struct phn_params {
   int N;           /* N_t = N_eta: lattice edge (cubic box) */
   int Nc;          /* field components, 1..PHN_MAX_NC */
-  int theory;      /* 0: phi^4+phi^6 (Kappa), 1: phi^4 + linear h  (parameters.cpp:86-120) */
+  int potential;   /* the reference's `theory`: 0 phi^4+phi^6 (Kappa), 1 phi^4 + linear h
+                      (parameters.cpp:86-120); named apart because the reference
+                      #defines `theory` in the translation unit that includes this */
   int mass_mode;   /* Mass_Mode */
   int lambda_mode; /* Lambda_Mode */
   int precision;   /* PHN_FP64 / PHN_FP32 / PHN_FP32_KAHAN */
@@ -124,7 +126,7 @@ int phn_time(const phn_handle *h, double *tau, int *total_stepcount);
  * on the current state. */
 int phn_volume_averages(phn_handle *h, phn_averages *out);
 /* false_vacuum_decayed() (fieldanalysis.cpp:887-893) on the last averages. */
-int phn_false_vacuum_decayed(const phn_averages *avg, int theory, int *decayed);
+int phn_false_vacuum_decayed(const phn_averages *avg, int potential, int *decayed);
 
 /* The run loop of main.cpp:685-699 with an explicit step count: reset(),
  * then nsteps x { Print_AveragesExtrema() cadence (TSO on the accumulated tau,

@@ -24,7 +24,7 @@ _PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
 
 
 class PhnParams(ctypes.Structure):
-    _fields_ = [("N", _I), ("Nc", _I), ("theory", _I), ("mass_mode", _I), ("lambda_mode", _I),
+    _fields_ = [("N", _I), ("Nc", _I), ("potential", _I), ("mass_mode", _I), ("lambda_mode", _I),
                 ("precision", _I), ("a", _D), ("dt", _D), ("T0", _D), ("m_sqr", _D), ("kappa", _D),
                 ("h", _D)]
 

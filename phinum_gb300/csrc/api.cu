@@ -39,13 +39,13 @@ int phn::validate_params(const phn_params *p) {
   if (!p) return set_error(PHN_ERR_INVALID, "params is NULL");
   if (p->N < 2 || p->N > 2048) return set_error(PHN_ERR_INVALID, "N=%d outside [2, 2048]", p->N);
   if (p->Nc < 1 || p->Nc > PHN_MAX_NC) return set_error(PHN_ERR_UNSUPPORTED, "Nc=%d outside [1, %d]", p->Nc, PHN_MAX_NC);
-  if (p->theory != 0 && p->theory != 1)
-    return set_error(PHN_ERR_UNSUPPORTED, "theory %d: only theories 0 and 1 are provided", p->theory);
+  if (p->potential != 0 && p->potential != 1)
+    return set_error(PHN_ERR_UNSUPPORTED, "theory %d: only theories 0 and 1 are provided", p->potential);
   if (p->precision < PHN_FP64 || p->precision > PHN_FP32_KAHAN)
     return set_error(PHN_ERR_INVALID, "precision %d", p->precision);
   if (!(p->a > 0.0) || !isfinite(p->a)) return set_error(PHN_ERR_INVALID, "a must be positive");
   if (!isfinite(p->dt)) return set_error(PHN_ERR_INVALID, "dt must be finite");
-  if (p->theory == 0 && !(p->kappa != 0.0)) return set_error(PHN_ERR_INVALID, "Kappa must be non-zero");
+  if (p->potential == 0 && !(p->kappa != 0.0)) return set_error(PHN_ERR_INVALID, "Kappa must be non-zero");
   return PHN_OK;
 }
 
@@ -57,7 +57,7 @@ Consts phn::make_consts(const phn_params *p) {
   const int Nc = p->Nc;
   k.N = p->N;
   k.Nc = Nc;
-  k.theory = p->theory;
+  k.theory = p->potential;
   k.a2 = p->a * p->a;
   k.mmM = p->mass_mode * p->m_sqr;
   k.lm = (double)p->lambda_mode;
@@ -71,11 +71,11 @@ Consts phn::make_consts(const phn_params *p) {
   k.inv_a2_f = (float)(1.0 / k.a2);
   k.mmM_f = (float)k.mmM;
   k.c4_f = (float)(k.lm / k.six_nc);
-  k.c6_f = p->theory == 0 ? (float)(1.0 / (p->kappa * p->kappa * k.c120)) : 0.f;
+  k.c6_f = p->potential == 0 ? (float)(1.0 / (p->kappa * p->kappa * k.c120)) : 0.f;
   k.h_f = (float)p->h;
   k.mmh_f = (float)k.mm_half_M;
   k.e4_f = (float)(k.lm / k.c24);
-  k.e6_f = p->theory == 0 ? (float)(1.0 / k.c720) : 0.f;
+  k.e6_f = p->potential == 0 ? (float)(1.0 / k.c720) : 0.f;
   return k;
 }
 
@@ -372,11 +372,11 @@ int phn_volume_averages(phn_handle *h, phn_averages *out) {
   return PHN_OK;
 }
 
-int phn_false_vacuum_decayed(const phn_averages *avg, int theory, int *decayed) {
+int phn_false_vacuum_decayed(const phn_averages *avg, int potential, int *decayed) {
   if (!avg || !decayed) return set_error(PHN_ERR_INVALID, "NULL argument");
   const double v = avg->interaction;
   // fieldanalysis.cpp:889-892 (theories 0, 1, 4)
-  *decayed = (theory == 0 || theory == 1 || theory == 4) ? (v < 0 || v != v || v * 0. != 0.) : 0;
+  *decayed = (potential == 0 || potential == 1 || potential == 4) ? (v < 0 || v != v || v * 0. != 0.) : 0;
   return PHN_OK;
 }
 
@@ -473,6 +473,8 @@ int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms) {
   double best = 1e30;
   int best_v = h->tma_variant;
   CK(cudaMemcpyAsync(h->d_ref, h->pi, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  // two rounds over the variants, each variant keeping its best round
+  for (int round = 0; round < 2; ++round)
   for (int v = 0; v < tma_num_variants(h->p.N); ++v) {
     const int g = tma_grid(h->p, v);
     if (g <= 0) continue;

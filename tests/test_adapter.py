@@ -1,0 +1,21 @@
+"""The reference-side adapter (phinum_gb300/adapter/phinum_dynamics.cpp)
+compiles inside the reference's own translation unit, for both theories.
+Needs the reference tree (present where the build runs); skipped elsewhere."""
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = "/root/reference"
+
+
+@pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "dynamics.cpp")), reason="reference tree not present")
+@pytest.mark.parametrize("theory", [0, 1])
+def test_adapter_compiles_in_reference_tu(theory):
+    cmd = ["g++", "-std=gnu++14", "-fsyntax-only", "-w", f"-DPHN_REF_THEORY={theory}", "-DPHN_REF_PRECISION=0",
+           "-I", os.path.join(ROOT, "oracle", "ref_shim"), "-I", os.path.join(ROOT, "oracle"),
+           "-I", REF, "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "phinum_gb300", "adapter"),
+           os.path.join(ROOT, "tests", "adapter_check.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
