@@ -277,8 +277,66 @@ def measure_gpu(args, dist: Dist):
                        "hbm_gbs_algorithmic": BYTES_PER_SITE[prec] * n ** 3 / t / 1e9,
                        "frac_of_measured_hbm": BYTES_PER_SITE[prec] * n ** 3 / t / 1e9 / peak}
         lat.close()
+    if not args.quick:
+        also["ensemble_c3"] = measure_ensemble(2000, 100)
     out["also"] = also
     return out
+
+
+def measure_ensemble(steps: int, steps_per_lattice: int):
+    """Batched form: 256 realizations, 128 x 32^3 + 96 x 64^3 + 32 x 128^3,
+    phi0 ~ U[0.8, 1.2] and g ~ U[0.05, 0.2] (config units; x sqrt(6) and
+    Kappa = sqrt(0.3/g) in the reference's), FP32, one persistent kernel per
+    step in CUDA-graph chunks, autotuned tile; against one handle per lattice
+    (one launch per lattice per step)."""
+    import ctypes
+    from phinum_gb300 import initial, layout
+    from phinum_gb300 import lattice as PL
+    rng = np.random.default_rng(2026)
+    sizes = [32] * 128 + [64] * 96 + [128] * 32
+    params, fields = [], []
+    for i, N in enumerate(sizes):
+        phi0 = rng.uniform(0.8, 1.2) * 6 ** 0.5
+        g = rng.uniform(0.05, 0.2)
+        params.append(PL.Params(N=N, precision=1, theory=0, kappa=(0.3 / g) ** 0.5))
+        phi, pi = initial.gaussian_fields(N, phi0=phi0, seed=i)
+        fields.append((layout.to_ref_layout(phi), layout.to_ref_layout(pi)))
+    sites = sum(N ** 3 for N in sizes)
+    ens = PL.Ensemble(params)
+    for m, (phi, pi) in enumerate(fields):
+        ens.upload(m, phi, pi)
+    tile, _ = ens.autotune(5)
+    ens.evolve(50)
+    n0, _, _ = ens.stats()
+    ens.evolve(steps)
+    n1, ms, _ = ens.stats()
+    ens_rate = sites * steps / (ms / 1e3)
+    ens.close()
+    lats = []
+    for p, f in zip(params, fields):
+        lat = PL.Lattice(p)
+        lat.upload(*f)
+        lats.append(lat)
+    for lat in lats:
+        lat.evolve(2)
+    lib = lats[0].lib
+    for lat in lats:
+        lat.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps_per_lattice):
+        for lat in lats:
+            lib.phn_evolve(lat.h, 1)
+    for lat in lats:
+        lat.synchronize()
+    pl_s = time.perf_counter() - t0
+    pl_rate = sites * steps_per_lattice / pl_s
+    for lat in lats:
+        lat.close()
+    return {"members": len(sizes), "sites": sites, "steps": steps, "tile": tile,
+            "site_updates_per_s": ens_rate, "ms_per_step": ms / steps, "launches_per_step": (n1 - n0) / steps,
+            "per_lattice_site_updates_per_s": pl_rate, "per_lattice_steps": steps_per_lattice,
+            "speedup_vs_per_lattice": ens_rate / pl_rate,
+            "hbm_gbs_algorithmic": 16 * sites * steps / (ms / 1e3) / 1e9}
 
 
 def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int):

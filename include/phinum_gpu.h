@@ -181,6 +181,35 @@ int phn_synchronize(phn_handle *h);
  * on the handle's stream), for roofline accounting. */
 int phn_stats(const phn_handle *h, long long *kernel_launches, double *last_evolve_ms, int *last_evolve_steps);
 
+/* ---- Batched ensemble ---------------------------------------------------
+ * Many independent lattices (the reference run once per realization, one
+ * `main` per seed) evolved together: one persistent kernel per step walks a
+ * work list of (member, tile) items, and the step loop runs as a captured CUDA
+ * graph.  Members: FP32, Nc = 1, N a multiple of 32, any potential/couplings;
+ * they share a, dt and T0 (one clock).  A member's fields are bit-identical to
+ * those of a single-lattice handle with the same inputs. */
+typedef struct phn_ensemble phn_ensemble;
+int phn_ensemble_create(const phn_params *members, int n, phn_ensemble **out);
+int phn_ensemble_destroy(phn_ensemble *e);
+/* per member, reference layout as phn_upload / phn_download */
+int phn_ensemble_upload(phn_ensemble *e, int member, const double *Phi, const double *Pi);
+int phn_ensemble_download(phn_ensemble *e, int member, double *Phi, double *Pi);
+/* reset() / n x evolve() for every member (dynamics.cpp:28-237) */
+int phn_ensemble_reset(phn_ensemble *e);
+int phn_ensemble_evolve(phn_ensemble *e, int nsteps);
+int phn_ensemble_time(const phn_ensemble *e, double *tau, int *total_stepcount);
+/* CalculateVolumeAverages + CalculateExtrema of every member: out[n] */
+int phn_ensemble_averages(phn_ensemble *e, phn_averages *out);
+/* phn_islands on one member */
+int phn_ensemble_islands(phn_ensemble *e, int member, double thres, int mode, int z_periodic, int *labels,
+                         phn_island *out, int max_out, int *n_islands);
+/* Autotuner of the work-list tile (rows x planes per item): times every
+ * candidate on the live ensemble (state unchanged) and keeps the fastest. */
+int phn_ensemble_autotune(phn_ensemble *e, int steps, int *tile, double *best_ms);
+int phn_ensemble_set_tile(phn_ensemble *e, int tile);
+int phn_ensemble_stats(const phn_ensemble *e, long long *kernel_launches, double *last_evolve_ms,
+                       int *last_evolve_steps);
+
 /* Volume averages of caller-owned device fields, allocating nothing.
  * No counterpart in the reference: it exists for hosts that cannot allocate
  * device memory where they need the averages -- a framework that owns all

@@ -79,6 +79,18 @@ _SIGS = {
     "phn_stats": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _PD, _PI]),
     "phn_volume_averages_noalloc": (_I, [ctypes.POINTER(PhnParams), ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.POINTER(PhnAverages)]),
+    "phn_ensemble_create": (_I, [ctypes.POINTER(PhnParams), _I, ctypes.POINTER(ctypes.c_void_p)]),
+    "phn_ensemble_destroy": (_I, [ctypes.c_void_p]),
+    "phn_ensemble_upload": (_I, [ctypes.c_void_p, _I, _PD, _PD]),
+    "phn_ensemble_download": (_I, [ctypes.c_void_p, _I, _PD, _PD]),
+    "phn_ensemble_reset": (_I, [ctypes.c_void_p]),
+    "phn_ensemble_evolve": (_I, [ctypes.c_void_p, _I]),
+    "phn_ensemble_time": (_I, [ctypes.c_void_p, _PD, _PI]),
+    "phn_ensemble_averages": (_I, [ctypes.c_void_p, ctypes.c_void_p]),
+    "phn_ensemble_islands": (_I, [ctypes.c_void_p, _I, _D, _I, _I, _PI, _PD, _I, _PI]),
+    "phn_ensemble_autotune": (_I, [ctypes.c_void_p, _I, _PI, _PD]),
+    "phn_ensemble_set_tile": (_I, [ctypes.c_void_p, _I]),
+    "phn_ensemble_stats": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _PD, _PI]),
     "phn_pin_host": (_I, [ctypes.c_void_p, ctypes.c_size_t]),
     "phn_unpin_host": (_I, [ctypes.c_void_p]),
 }

@@ -23,6 +23,7 @@
 //
 // Variants (TY, S, PI_SMEM) trade halo re-reads against shared memory per
 // block; phn_autotune times them on the live lattice and keeps the fastest.
+#include "kick.cuh"
 #include "observe.cuh"
 #include "phn_internal.h"
 #include "tma.cuh"
@@ -215,17 +216,8 @@ __global__ void __launch_bounds__((TY + 1) * 32) step_f32_tma(const float *__res
             const float ymv = get(ym, e), ypv = get(yp, e), zm = get(cm[q], e), zp = get(cp[q], e);
             const float pp = get(pv, e);
             if (OBS) observe_site<THEORY>(plane, accf, k, cc, pp, xp, ypv, zp, gz + NN + x0 + e);
-            const float lap = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(xp, xm), __fadd_rn(ypv, ymv)),
-                                                            __fadd_rn(zp, zm)),
-                                                  __fmul_rn(-6.f, cc)),
-                                        k.inv_a2_f);
-            const float l = __fmul_rn(cc, cc);
-            float coef = fmaf(l, k.c4_f, k.mmM_f);
-            if (THEORY == 0) coef = fmaf(__fmul_rn(l, l), k.c6_f, coef);
-            float f = fmaf(-coef, cc, lap);
-            if (THEORY == 1) f = __fsub_rn(f, k.h_f);
-            const float pnv = fmaf(fk, f, pp);
-            const float fnv = fmaf(fd, pnv, cc);
+            float pnv, fnv;
+            kick_drift_f32<THEORY>(k, fk, fd, cc, xm, xp, ymv, ypv, zm, zp, pp, pnv, fnv);
             if (e == 0) { pn.x = pnv; fn.x = fnv; }
             if (e == 1) { pn.y = pnv; fn.y = fnv; }
             if (e == 2) { pn.z = pnv; fn.z = fnv; }

@@ -261,4 +261,67 @@ __device__ __forceinline__ void flush_plane(AccF &A, PlaneF &P) {
   P.clear();
 }
 
+constexpr int FIN_THREADS = 128;
+
+// Folds block records [b0, b1) in a fixed order with one block of FIN_THREADS
+// threads and forms the reference's derived quantities
+// (fieldanalysis.cpp:619-638): Energy, Charge, Interaction and the per-volume
+// moments of a lattice of k.N^3 sites.
+__device__ __forceinline__ void fold_records(const double *__restrict__ partials, int b0, int b1, const Consts &k,
+                             phn_averages *__restrict__ out) {
+  __shared__ double sh[FIN_THREADS][REC];
+  const int t = threadIdx.x;
+  Acc a;
+  a.init();
+  for (int b = b0 + t; b < b1; b += FIN_THREADS) {
+    Acc o;
+    load_rec(o, partials + (size_t)b * REC);
+    combine(a, o);
+  }
+  store_rec(sh[t], a);
+  __syncthreads();
+  for (int w = FIN_THREADS / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      Acc x, y;
+      load_rec(x, sh[t]);
+      load_rec(y, sh[t + w]);
+      combine(x, y);
+      store_rec(sh[t], x);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    Acc r;
+    load_rec(r, sh[0]);
+    const double vol = (double)k.N * (double)k.N * (double)k.N;
+    phn_averages o;
+    o.t = 0.0;
+    for (int c = 0; c < PHN_MAX_NC; ++c) {
+      o.phi[c] = c < k.Nc ? r.s[S_PHI + c] / vol : 0.0;
+      o.pi[c] = c < k.Nc ? r.s[S_PI + c] / vol : 0.0;
+    }
+    const double pi2 = r.s[S_PI2], grad = r.s[S_GRAD], inter = r.s[S_INTER];
+    const double charge = (0.5 * pi2 - grad / 6. - inter);
+    const double energy = (0.5 * pi2 + 0.5 * grad + inter);
+    o.energy = energy / vol;
+    o.interaction = inter / vol;
+    o.charge = charge / vol;
+    o.phi2 = r.s[S_PHI2] / vol;
+    o.pi2 = pi2 / vol;
+    o.phi4 = r.s[S_PHI4] / vol;
+    o.phi6 = r.s[S_PHI6] / vol;
+    o.phipi = r.s[S_PHIPI] / vol;
+    o.min_phi = r.minv;
+    o.max_phi = r.maxv;
+    o.max_abs_phi = r.absv;
+    o.min_pos = r.mini == LLONG_MAX ? -1.0 : (double)r.mini;
+    o.max_pos = r.maxi == LLONG_MAX ? -1.0 : (double)r.maxi;
+    o.max_abs_pos = r.absi == LLONG_MAX ? -1.0 : (double)r.absi;
+    o.gradient = grad / vol;
+    o.nonfinite = r.s[S_NONFINITE];
+    o.reserved = 0.0;
+    *out = o;
+  }
+}
+
 }  // namespace phn

@@ -157,6 +157,79 @@ class Lattice:
         L.check(self.lib.phn_synchronize(self.h))
 
 
+class Ensemble:
+    """Many lattices evolved together (phn_ensemble_*): one persistent kernel
+    per step over all members, step loop in a CUDA graph."""
+
+    def __init__(self, members: list):
+        self.members = members
+        self.lib = L.load()
+        arr = (L.PhnParams * len(members))(*[m.c() for m in members])
+        h = ctypes.c_void_p()
+        L.check(self.lib.phn_ensemble_create(arr, len(members), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.phn_ensemble_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, m: int, phi: np.ndarray, pi: np.ndarray):
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        pi = np.ascontiguousarray(pi, dtype=np.float64)
+        L.check(self.lib.phn_ensemble_upload(self.h, m, _pd(phi), _pd(pi)))
+
+    def download(self, m: int):
+        n = self.members[m].field_len
+        phi, pi = np.zeros(n), np.zeros(n)
+        L.check(self.lib.phn_ensemble_download(self.h, m, _pd(phi), _pd(pi)))
+        return phi, pi
+
+    def reset(self):
+        L.check(self.lib.phn_ensemble_reset(self.h))
+
+    def evolve(self, n: int):
+        L.check(self.lib.phn_ensemble_evolve(self.h, int(n)))
+
+    def averages(self) -> np.ndarray:
+        out = (L.PhnAverages * len(self.members))()
+        L.check(self.lib.phn_ensemble_averages(self.h, out))
+        return np.frombuffer(bytes(out), dtype=np.float64).reshape(len(self.members), L.AVG_LEN).copy()
+
+    def islands(self, m: int, thres: float, mode: int = L.ISLAND_REFERENCE, z_periodic: bool = False,
+                max_out: int = 0):
+        n = ctypes.c_int()
+        recs = np.zeros((max(max_out, 1), len(L.ISLAND_FIELDS)))
+        L.check(self.lib.phn_ensemble_islands(self.h, m, float(thres), int(mode), int(bool(z_periodic)), None,
+                                              _pd(recs) if max_out else None, max_out, ctypes.byref(n)))
+        return n.value, recs[:min(n.value, max_out)].copy()
+
+    def autotune(self, steps: int = 5):
+        t, ms = ctypes.c_int(), ctypes.c_double()
+        L.check(self.lib.phn_ensemble_autotune(self.h, steps, ctypes.byref(t), ctypes.byref(ms)))
+        return t.value, ms.value
+
+    def set_tile(self, t: int):
+        L.check(self.lib.phn_ensemble_set_tile(self.h, t))
+
+    def stats(self):
+        n, ms, st = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_int()
+        L.check(self.lib.phn_ensemble_stats(self.h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(st)))
+        return n.value, ms.value, st.value
+
+
 def device_count() -> int:
     lib = L.load()
     n = ctypes.c_int()
