@@ -339,6 +339,58 @@ def measure_ensemble(steps: int, steps_per_lattice: int):
             "hbm_gbs_algorithmic": 16 * sites * steps / (ms / 1e3) / 1e9}
 
 
+def precision_form(N: int, steps: int, check_step: int = 500, tso_steps: int = 50):
+    """Precision form (config C2): the same seeded 512^3 phi^6 run in FP64
+    (the GPU oracle: bit-identical to the reference's FP64 arithmetic), plain
+    FP32 and compensated FP32.  Reports, against FP64: the relative L2 error
+    of phi after `check_step` steps, the per-bin relative error of the field
+    spectrum F(|p|) at that step, and the relative energy drift
+    |E(t) - E(0)| / |E(0)| over `steps` steps (E from the fused SO rows every
+    `tso_steps` steps, FP64 sums)."""
+    from phinum_gb300 import _lib as L
+    from phinum_gb300 import lattice as PL
+    phi, pi = make_fields(N)
+    res = {}
+    ref_phi = ref_F = None
+    for name, prec in (("fp64", L.FP64), ("kahan_fp32", L.FP32_KAHAN), ("fp32", L.FP32)):
+        lat = PL.Lattice(PL.Params(N=N, precision=prec))
+        lat.upload(phi, pi)
+        t0 = time.perf_counter()
+        energies = []
+        done = 0
+        e_check = None
+        while done < steps:
+            energies.append(lat.volume_averages()[14])  # SO row before the next evolve()
+            lat.evolve(tso_steps)
+            done += tso_steps
+            if done == check_step:
+                fphi, _ = lat.download()
+                F, K, Q, C = lat.correlation_functions()
+                e_check = (fphi, F)
+        energies.append(lat.volume_averages()[14])
+        wall = time.perf_counter() - t0
+        lat.close()
+        E = np.asarray(energies)
+        r = {"energy0": float(E[0]), "energy_end": float(E[-1]),
+             "drift_end": float(abs(E[-1] - E[0]) / abs(E[0])),
+             "drift_max": float(np.max(np.abs(E - E[0])) / abs(E[0])), "wall_s": wall}
+        if name == "fp64":
+            ref_phi, ref_F = e_check
+        else:
+            fphi, F = e_check
+            r["l2_phi_rel_at_check"] = float(np.linalg.norm(fphi - ref_phi) / np.linalg.norm(ref_phi))
+            nz = ref_F > 0
+            rel = np.abs(F[nz] - ref_F[nz]) / ref_F[nz]
+            r["spectrum_rel_err_max"] = float(rel.max())
+            r["spectrum_rel_err_median"] = float(np.median(rel))
+        res[name] = r
+    res["kahan_drift_over_fp64_drift"] = res["kahan_fp32"]["drift_end"] / max(res["fp64"]["drift_end"], 1e-300)
+    res["fp32_drift_over_fp64_drift"] = res["fp32"]["drift_end"] / max(res["fp64"]["drift_end"], 1e-300)
+    return {"form": "precision", "N": N, "steps": steps, "check_step": check_step, "tso_steps": tso_steps,
+            "workload": f"phi^6 (theory 0, Kappa=sqrt(3)), {N}^3, a=0.25, dtau=0.02, seeded Gaussian fields",
+            "results": res}
+
+
 def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int):
     """The oracle's reference loop (FP64) on all host threads, bounded."""
     from oracle import oracle as O
@@ -369,6 +421,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--n", type=int, default=N_MAIN, help="lattice edge (profiling runs use smaller cases)")
     ap.add_argument("--variant", type=int, default=None, help="TMA kernel variant instead of the autotuner's pick")
+    ap.add_argument("--form", default=None, choices=["precision", "adjoint"],
+                    help="report one of the north-star forms instead of the benchmark line")
     args = ap.parse_args()
     rank, local, world = env_rank()
     config = {"workload": f"phi^6 oscillon (theory 0, Kappa=sqrt(3)), {args.n}^3 periodic lattice, a=0.25, "
@@ -377,6 +431,13 @@ def main():
               "N": args.n, "sites": args.n ** 3, "tso_steps": TSO_STEPS,
               "l2": "inputs larger than L2 (1.5 GB of fields vs 129 MB L2); no flush",
               "parallelism": f"replicas x{args.gpus}"}
+
+    if args.form == "precision":
+        print(json.dumps(precision_form(args.n, max(args.steps, 500))))
+        return
+    if args.form == "adjoint":
+        print(json.dumps(adjoint_form(args.n, args.steps)))
+        return
 
     if args.impl == "reference":
         if rank != 0:
