@@ -391,6 +391,73 @@ def precision_form(N: int, steps: int, check_step: int = 500, tso_steps: int = 5
             "results": res}
 
 
+def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: float = 1e-3):
+    """Adjoint form (config C4): phi^6, N^3, FP32, `steps` steps, checkpoints
+    every `every`; J = sum rho sigmoid((rho - 2<rho>)/0.1) of the final state.
+    Gradients w.r.t. the initial phi field, its homogeneous part phi0 and the
+    phi^6 coupling, checked against the FP64 adjoint and against central
+    finite differences of the FP64 forward (step h_fd) on `ndir` random unit
+    directions; cost = (forward with checkpoints + backward) / plain forward."""
+    from phinum_gb300 import lattice as PL
+    phi, pi = make_fields(N)
+    sl = slice(N * N, -N * N)
+    kappa = 3 ** 0.5
+    # plain forward solve: the production step kernel, same steps
+    lat = PL.Lattice(PL.Params(N=N, precision=1, kappa=kappa))
+    lat.upload(phi, pi)
+    lat.evolve(steps)
+    _, fwd_plain_ms, _ = lat.stats()
+    lat.close()
+    out = {"form": "adjoint", "N": N, "steps": steps, "every": every, "width": 0.1}
+    res = {}
+    for name, prec in (("fp32", 1), ("fp64", 0)):
+        with PL.Adjoint(PL.Params(N=N, precision=prec, kappa=kappa), steps, every) as adj:
+            adj.forward(phi, pi)
+            dphi, dpi, g = adj.backward()
+            J, fms, bms = adj.info()
+        res[name] = {"J": J, "dphi": dphi, "g": g, "forward_ms": fms, "backward_ms": bms}
+    d32, d64 = res["fp32"]["dphi"][sl], res["fp64"]["dphi"][sl]
+    out["J_fp32"], out["J_fp64"] = res["fp32"]["J"], res["fp64"]["J"]
+    out["cost_ratio"] = (res["fp32"]["forward_ms"] + res["fp32"]["backward_ms"]) / fwd_plain_ms
+    out["forward_plain_ms"] = fwd_plain_ms
+    out["adjoint_forward_ms"] = res["fp32"]["forward_ms"]
+    out["adjoint_backward_ms"] = res["fp32"]["backward_ms"]
+    out["fp32_vs_fp64_field_rel_l2"] = float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64))
+    g32, g64 = res["fp32"]["g"], res["fp64"]["g"]
+    out["fp32_vs_fp64_dphi0_rel"] = float(abs(g32[0] - g64[0]) / abs(g64[0]))
+    out["fp32_vs_fp64_dc6_rel"] = float(abs(g32[1] - g64[1]) / abs(g64[1]))
+    # central finite differences of the FP64 forward
+    rng = np.random.default_rng(99)
+    errs64, errs32 = [], []
+    with PL.Adjoint(PL.Params(N=N, precision=0, kappa=kappa), steps, every) as adj:
+        for _ in range(ndir):
+            v = np.zeros_like(phi)
+            v[sl] = rng.standard_normal(N ** 3)
+            v /= np.linalg.norm(v[sl])
+            fd = (adj.forward(phi + h_fd * v, pi) - adj.forward(phi - h_fd * v, pi)) / (2 * h_fd)
+            errs64.append(abs(float(np.dot(d64, v[sl])) - fd) / abs(fd))
+            errs32.append(abs(float(np.dot(d32, v[sl])) - fd) / abs(fd))
+        one = np.ones_like(phi)
+        fd_phi0 = (adj.forward(phi + h_fd * one, pi) - adj.forward(phi - h_fd * one, pi)) / (2 * h_fd)
+    c6 = 1.0 / (720 * kappa ** 2)
+    Jc = []
+    for d in (+1, -1):
+        c = c6 * (1 + d * h_fd)
+        with PL.Adjoint(PL.Params(N=N, precision=0, kappa=(1.0 / (720 * c)) ** 0.5), steps, every) as adj:
+            Jc.append(adj.forward(phi, pi))
+    fd_c6 = (Jc[0] - Jc[1]) / (2 * h_fd * c6)
+    out["fd_directions"] = ndir
+    out["fd_step"] = h_fd
+    out["fp64_adjoint_vs_fd_rel_max"] = float(max(errs64))
+    out["fp32_adjoint_vs_fd_rel_max"] = float(max(errs32))
+    out["fp32_adjoint_vs_fd_rel_median"] = float(np.median(errs32))
+    out["dphi0"] = {"fp32": float(g32[0]), "fp64": float(g64[0]), "fd": fd_phi0}
+    out["dc6"] = {"fp32": float(g32[1]), "fp64": float(g64[1]), "fd": fd_c6}
+    # the configuration's units: phi_ref = sqrt(6) phi, c6 = g / 216
+    out["config_units"] = {"dJ_dphi0": float(g32[0]) * 6 ** 0.5, "dJ_dg": float(g32[1]) / 216.0}
+    return out
+
+
 def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int):
     """The oracle's reference loop (FP64) on all host threads, bounded."""
     from oracle import oracle as O

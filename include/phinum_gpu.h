@@ -210,6 +210,27 @@ int phn_ensemble_set_tile(phn_ensemble *e, int tile);
 int phn_ensemble_stats(const phn_ensemble *e, long long *kernel_launches, double *last_evolve_ms,
                        int *last_evolve_steps);
 
+/* ---- Adjoint ---------------------------------------------------------------
+ * No counterpart in the reference (it has no derivatives).  Objective on the
+ * final state: J = sum_x rho(x) sigmoid((rho(x) - 2 <rho>) / width), rho the
+ * energy density (the summand of the reference's Energy).  Forward: the same
+ * step kernels as phn_evolve, checkpoints every `every` steps.  Backward: the
+ * discrete adjoint of the implemented leapfrog, reverse time stepping that
+ * restarts from each checkpoint (finite-precision reversal drifts).
+ * Nc = 1, FP32 or FP64 (the FP64 run is the reference gradient). */
+typedef struct phn_adjoint phn_adjoint;
+int phn_adjoint_create(const phn_params *params, int nsteps, int every, double width, phn_adjoint **out);
+int phn_adjoint_destroy(phn_adjoint *a);
+/* reset() + nsteps x evolve() from (Phi0, Pi0) (reference layout); *J = J. */
+int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, double *J);
+/* After a forward: dJ/dPhi0 and dJ/dPi0 in the reference layout (either may be
+ * NULL; Pi0's ghost slabs untouched) and grads[3] = { dJ/d(homogeneous shift
+ * of Phi0), dJ/dc6 with c6 = 1/(720 Kappa^2) the phi^6 coefficient of V
+ * (theory 0), dJ/dh (theory 1) }. */
+int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *grads);
+/* J of the last forward and device times (ms) of the last forward and backward. */
+int phn_adjoint_info(const phn_adjoint *a, double *J, double *forward_ms, double *backward_ms);
+
 /* Volume averages of caller-owned device fields, allocating nothing.
  * No counterpart in the reference: it exists for hosts that cannot allocate
  * device memory where they need the averages -- a framework that owns all

@@ -7,4 +7,4 @@ sources, the build step, the C++ adapter for the reference host
 """
 from . import _lib  # noqa: F401
 from ._lib import FP32, FP32_KAHAN, FP64, ISLAND_ENERGY, ISLAND_REFERENCE, PhnError  # noqa: F401
-from .lattice import Ensemble, Lattice, Params, device_count  # noqa: F401
+from .lattice import Adjoint, Ensemble, Lattice, Params, device_count  # noqa: F401

@@ -91,6 +91,11 @@ _SIGS = {
     "phn_ensemble_autotune": (_I, [ctypes.c_void_p, _I, _PI, _PD]),
     "phn_ensemble_set_tile": (_I, [ctypes.c_void_p, _I]),
     "phn_ensemble_stats": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _PD, _PI]),
+    "phn_adjoint_create": (_I, [ctypes.POINTER(PhnParams), _I, _I, _D, ctypes.POINTER(ctypes.c_void_p)]),
+    "phn_adjoint_destroy": (_I, [ctypes.c_void_p]),
+    "phn_adjoint_forward": (_I, [ctypes.c_void_p, _PD, _PD, _PD]),
+    "phn_adjoint_backward": (_I, [ctypes.c_void_p, _PD, _PD, _PD]),
+    "phn_adjoint_info": (_I, [ctypes.c_void_p, _PD, _PD, _PD]),
     "phn_pin_host": (_I, [ctypes.c_void_p, ctypes.c_size_t]),
     "phn_unpin_host": (_I, [ctypes.c_void_p]),
 }

@@ -1,0 +1,532 @@
+// Hand-written adjoint of the leapfrog (no reference counterpart: the
+// reference has no derivatives).  Differentiates
+//     J = sum_x rho(x) * sigmoid((rho(x) - 2 <rho>) / w)
+// of the final state, rho(x) the energy density (the summand of the
+// reference's Energy, fieldanalysis.cpp:437-579), with respect to the initial
+// phi field, its homogeneous part, the initial pi field and the potential's
+// couplings.
+//
+// Forward (phn_adjoint_forward): the production step kernels through an
+// internal handle (bit-identical to phn_evolve), with a checkpoint of (phi, pi)
+// every `every` steps.
+//
+// Reverse (phn_adjoint_backward): the discrete adjoint of the implemented
+// update  pi' = pi + fk F(phi),  phi' = phi + fd pi',  F = Lap(phi) - V'(phi):
+//     mu      = lam_pi + fd lam_phi                  (adjoint of pi')
+//     lam_phi = lam_phi + fk (Lap(mu) - V''(phi) mu)
+//     lam_pi  = mu
+// with (phi, pi) of the earlier time reconstructed by running the step
+// backwards, phi = phi' - fd pi',  pi = pi' - fk F(phi).  Reversal is exact in
+// exact arithmetic but drifts in finite precision, so each segment of `every`
+// steps starts from its stored checkpoint (checkpoint-and-recompute).  One
+// fused kernel per reverse step reads phi', pi', lam_phi, lam_pi and writes
+// the four earlier fields: 32 bytes per site in FP32.  Coupling gradients
+// accumulate per block across steps in fixed slots (deterministic).
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "phn_internal.h"
+
+namespace phn {
+
+constexpr int ADJ_TX = 32, ADJ_TY = 8, ADJ_THREADS = ADJ_TX * ADJ_TY;
+constexpr int ADJ_NG = 4;  // coupling-gradient slots: c6 (phi^6 coefficient), h, M^2 term, spare
+
+template <typename T>
+struct AdjOps;
+template <>
+struct AdjOps<float> {
+  __device__ static float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+};
+template <>
+struct AdjOps<double> {
+  __device__ static double fma_(double a, double b, double c) { return fma(a, b, c); }
+};
+
+// Potential pieces for one component (Nc = 1), in T arithmetic.
+//   V'(phi)  = (mmM + lm phi^2/6 [+ phi^4 / (120 Kappa^2)]) phi [+ h]
+//   V''(phi) =  mmM + lm phi^2/2 [+ 5 phi^4 / (120 Kappa^2)]
+template <typename T>
+__device__ __forceinline__ T force(const Consts &k, T lap_sum, T c) {
+  // F = Lap(phi) - V'(phi): same expression as the forward kernels
+  const T inv_a2 = (T)1 / (T)k.a2;
+  const T l = c * c;
+  T coef = (T)k.mmM + l * ((T)k.lm / (T)k.six_nc);
+  if (k.theory == 0) coef += (l * l) * ((T)1 / ((T)k.kappa * (T)k.kappa * (T)k.c120));
+  T f = (lap_sum - (T)6 * c) * inv_a2 - coef * c;
+  if (k.theory == 1) f -= (T)k.h;
+  return f;
+}
+
+template <typename T>
+__device__ __forceinline__ T vpp(const Consts &k, T c) {
+  const T l = c * c;
+  T v = (T)k.mmM + (T)3 * l * ((T)k.lm / (T)k.six_nc);
+  if (k.theory == 0) v += (T)5 * (l * l) * ((T)1 / ((T)k.kappa * (T)k.kappa * (T)k.c120));
+  return v;
+}
+
+// One reverse step.  phi1, pi1: state after the step; lphi, lpi: adjoints at
+// that time.  Writes phi0, pi0 (state before) and lphi0, lpi0 (adjoints
+// before).  Gradient slots: gs[block][j] += this step's coupling terms.
+template <typename T>
+__global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict__ phi1, const T *__restrict__ pi1,
+                                                            const T *__restrict__ lphi, const T *__restrict__ lpi,
+                                                            T *__restrict__ phi0, T *__restrict__ pi0,
+                                                            T *__restrict__ lphi0, T *__restrict__ lpi0,
+                                                            const Consts k, const T fk, const T fd, const int cz,
+                                                            double *__restrict__ gs) {
+  const int N = k.N;
+  const int x = blockIdx.x * ADJ_TX + threadIdx.x, y = blockIdx.y * ADJ_TY + threadIdx.y;
+  const int z0 = blockIdx.z * cz, z1 = min(z0 + cz, N);
+  const size_t NN = (size_t)N * N;
+  double g_c6 = 0.0, g_h = 0.0;
+  if (x < N && y < N && z0 < z1) {
+    const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
+    const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
+    const size_t col = (size_t)y * N + x;
+    // reconstructed phi and mu at a site
+    auto rphi = [&](size_t i) { return AdjOps<T>::fma_(-fd, pi1[i], phi1[i]); };
+    auto rmu = [&](size_t i) { return AdjOps<T>::fma_(fd, lphi[i], lpi[i]); };
+    const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
+    T pm = rphi((size_t)zm0 * NN + col), pc = rphi((size_t)z0 * NN + col);
+    T mm = rmu((size_t)zm0 * NN + col), mc = rmu((size_t)z0 * NN + col);
+    const T inv_a2 = (T)1 / (T)k.a2;
+    const T c6 = k.theory == 0 ? (T)1 / ((T)720 * (T)k.kappa * (T)k.kappa) : (T)0;
+    for (int z = z0; z < z1; ++z) {
+      const int zn = (z + 1 == N) ? 0 : z + 1;
+      const size_t pl = (size_t)z * NN, i = pl + col;
+      const T pn = rphi((size_t)zn * NN + col), mn = rmu((size_t)zn * NN + col);
+      const size_t ixp = pl + (size_t)y * N + xp, ixm = pl + (size_t)y * N + xm;
+      const size_t iyp = pl + (size_t)yp * N + x, iym = pl + (size_t)ym * N + x;
+      // state before the step
+      const T sum_phi = ((rphi(ixp) + rphi(ixm)) + (rphi(iyp) + rphi(iym))) + (pn + pm);
+      const T f = force<T>(k, sum_phi, pc);
+      const T pi_before = AdjOps<T>::fma_(-fk, f, pi1[i]);
+      // adjoint
+      const T sum_mu = ((rmu(ixp) + rmu(ixm)) + (rmu(iyp) + rmu(iym))) + (mn + mm);
+      const T lap_mu = (sum_mu - (T)6 * mc) * inv_a2;
+      const T lphi_before = AdjOps<T>::fma_(fk, lap_mu - vpp<T>(k, pc) * mc, lphi[i]);
+      phi0[i] = pc;
+      pi0[i] = pi_before;
+      lphi0[i] = lphi_before;
+      lpi0[i] = mc;
+      // dF/dc6 = -6 phi^5 ; dF/dh = -1   (kick pi' = pi + fk F)
+      const double p5 = (double)pc * (double)pc * (double)pc * (double)pc * (double)pc;
+      g_c6 += (double)fk * (double)mc * (-6.0 * p5);
+      g_h += -(double)fk * (double)mc;
+      pm = pc;
+      pc = pn;
+      mm = mc;
+      mc = mn;
+    }
+    (void)c6;
+  }
+  // block sums (fixed order) into this block's gradient slot
+  __shared__ double sh[2][ADJ_THREADS];
+  const int tid = threadIdx.x + ADJ_TX * threadIdx.y;
+  sh[0][tid] = g_c6;
+  sh[1][tid] = g_h;
+  __syncthreads();
+  for (int w = ADJ_THREADS / 2; w > 0; w >>= 1) {
+    if (tid < w) {
+      sh[0][tid] += sh[0][tid + w];
+      sh[1][tid] += sh[1][tid + w];
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const size_t b = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
+    gs[b * ADJ_NG + 0] += sh[0][0];
+    gs[b * ADJ_NG + 1] += sh[1][0];
+  }
+}
+
+// ---------------------------------------------------------------- objective
+__device__ __forceinline__ double sigmoid(double u) { return 1.0 / (1.0 + exp(-u)); }
+
+// rho(x), FP64, from T fields (the reference's per-site Energy summand).
+template <typename T>
+__global__ void obj_rho(const T *__restrict__ phi, const T *__restrict__ pi, const Consts k,
+                        double *__restrict__ rho) {
+  const int N = k.N;
+  const size_t NN = (size_t)N * N, V = NN * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
+    const double c = phi[i], p = pi[i];
+    const double fx = phi[i - x + (x + 1 == N ? 0 : x + 1)];
+    const double fy = phi[(size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x];
+    const double fz = phi[(size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x];
+    const double c2 = c * c, c4 = c2 * c2;
+    const double grad = ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) / k.a2;
+    double v = k.mm_half_M * c2 + k.lm * (c4 / k.c24);
+    if (k.theory == 0) v += c4 * c2 / k.c720;
+    if (k.theory == 1) v += k.h * c;
+    rho[i] = 0.5 * p * p + 0.5 * grad + v;
+  }
+}
+
+// Block sums of a per-site expression into out[block] (one value per block).
+enum { SUM_RHO = 0, SUM_J = 1, SUM_S = 2, SUM_GPHI6 = 3, SUM_GPHI = 4 };
+__global__ void obj_sum(const double *__restrict__ rho, const double *__restrict__ gseed, size_t V, int what,
+                        double mean, double w, const void *__restrict__ phi, int phi_is_double,
+                        double *__restrict__ out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    const double r = rho[i];
+    if (what == SUM_RHO) {
+      s += r;
+    } else if (what == SUM_J || what == SUM_S) {
+      const double u = (r - 2.0 * mean) / w, sg = sigmoid(u);
+      s += what == SUM_J ? r * sg : r * sg * (1.0 - sg);
+    } else {
+      const double c = phi_is_double ? ((const double *)phi)[i] : (double)((const float *)phi)[i];
+      const double c2 = c * c;
+      s += what == SUM_GPHI6 ? gseed[i] * c2 * c2 * c2 : gseed[i] * c;
+    }
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+
+// g(x) = dJ/drho(x)
+__global__ void obj_seed(const double *__restrict__ rho, size_t V, double mean, double S, double w,
+                         double *__restrict__ g) {
+  const double corr = -2.0 * S / (w * (double)V);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    const double r = rho[i], sg = sigmoid((r - 2.0 * mean) / w);
+    g[i] = sg + r * sg * (1.0 - sg) / w + corr;
+  }
+}
+
+// lam_pi = g pi ; lam_phi = g (-sum_d (phi(x+d)-phi(x))/a^2 + V'(phi)) + sum_d g(x-d) (phi(x)-phi(x-d))/a^2
+template <typename T>
+__global__ void obj_adjoint_init(const T *__restrict__ phi, const T *__restrict__ pi, const double *__restrict__ g,
+                                 const Consts k, T *__restrict__ lphi, T *__restrict__ lpi) {
+  const int N = k.N;
+  const size_t NN = (size_t)N * N, V = NN * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
+    const size_t ixp = i - x + (x + 1 == N ? 0 : x + 1), ixm = i - x + (x == 0 ? N - 1 : x - 1);
+    const size_t iyp = (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x;
+    const size_t iym = (size_t)z * NN + (size_t)(y == 0 ? N - 1 : y - 1) * N + x;
+    const size_t izp = (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x;
+    const size_t izm = (size_t)(z == 0 ? N - 1 : z - 1) * NN + (size_t)y * N + x;
+    const double c = phi[i];
+    const double fwd = ((double)phi[ixp] - c) + ((double)phi[iyp] - c) + ((double)phi[izp] - c);
+    const double bwd = g[ixm] * (c - (double)phi[ixm]) + g[iym] * (c - (double)phi[iym]) +
+                       g[izm] * (c - (double)phi[izm]);
+    const double c2 = c * c;
+    double vp = 2.0 * k.mm_half_M * c + k.lm * c2 * c / 6.0 * (24.0 / k.c24);
+    if (k.theory == 0) vp += 6.0 * c2 * c2 * c / k.c720;
+    if (k.theory == 1) vp += k.h;
+    lphi[i] = (T)(g[i] * (-fwd / k.a2 + vp) + bwd / k.a2);
+    lpi[i] = (T)(g[i] * (double)pi[i]);
+  }
+}
+
+__global__ void gs_zero(double *gs, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) gs[i] = 0.0;
+}
+
+}  // namespace phn
+
+using namespace phn;
+
+struct phn_adjoint {
+  phn_params p;
+  Consts k;
+  int nsteps, every, nseg;
+  double w;
+  size_t V, elem;
+  phn_handle *fwd;
+  void *ckpt;              // (nseg + 1) x {phi, pi}
+  void *rphi[2], *rpi[2], *lphi[2], *lpi[2];
+  double *rho, *g, *sums;  // per-site FP64 scratch, block sums
+  double *gs;              // gradient slots [blocks][ADJ_NG]
+  int sum_blocks;
+  std::vector<double> fk, fd;  // clock factors of each forward step
+  bool forward_done;
+  double J, mean, S;
+  cudaEvent_t ev0, ev1;
+  double fwd_ms, bwd_ms;
+};
+
+static void adj_free(phn_adjoint *a) {
+  if (!a) return;
+  if (a->fwd) phn_destroy(a->fwd);
+  cudaFree(a->ckpt);
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(a->rphi[i]);
+    cudaFree(a->rpi[i]);
+    cudaFree(a->lphi[i]);
+    cudaFree(a->lpi[i]);
+  }
+  cudaFree(a->rho);
+  cudaFree(a->g);
+  cudaFree(a->sums);
+  cudaFree(a->gs);
+  if (a->ev0) cudaEventDestroy(a->ev0);
+  if (a->ev1) cudaEventDestroy(a->ev1);
+  delete a;
+}
+
+#define CKA(call)                                        \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_error(e_, #call); \
+  } while (0)
+
+static double host_sum(phn_adjoint *a, cudaStream_t st) {
+  std::vector<double> h(a->sum_blocks);
+  cudaMemcpyAsync(h.data(), a->sums, a->sum_blocks * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  double s = 0.0;
+  for (double v : h) s += v;  // fixed order
+  return s;
+}
+
+// J and its seed on the current forward state (phi, pi device pointers).
+template <typename T>
+static int objective(phn_adjoint *a, const T *phi, const T *pi, bool seed, cudaStream_t st) {
+  const int nb = a->sum_blocks;
+  obj_rho<T><<<nb, 256, 0, st>>>(phi, pi, a->k, a->rho);
+  obj_sum<<<nb, 256, 0, st>>>(a->rho, nullptr, a->V, SUM_RHO, 0.0, a->w, nullptr, 0, a->sums);
+  CKA(cudaGetLastError());
+  a->mean = host_sum(a, st) / (double)a->V;
+  obj_sum<<<nb, 256, 0, st>>>(a->rho, nullptr, a->V, SUM_J, a->mean, a->w, nullptr, 0, a->sums);
+  CKA(cudaGetLastError());
+  a->J = host_sum(a, st);
+  if (!seed) return PHN_OK;
+  obj_sum<<<nb, 256, 0, st>>>(a->rho, nullptr, a->V, SUM_S, a->mean, a->w, nullptr, 0, a->sums);
+  CKA(cudaGetLastError());
+  a->S = host_sum(a, st);
+  obj_seed<<<nb, 256, 0, st>>>(a->rho, a->V, a->mean, a->S, a->w, a->g);
+  CKA(cudaGetLastError());
+  return PHN_OK;
+}
+
+extern "C" {
+
+int phn_adjoint_create(const phn_params *params, int nsteps, int every, double width, phn_adjoint **out) {
+  if (!out || nsteps < 1 || every < 1 || nsteps % every != 0 || !(width > 0.0))
+    return set_error(PHN_ERR_INVALID, "nsteps must be a positive multiple of every; width > 0");
+  *out = nullptr;
+  int r = validate_params(params);
+  if (r) return r;
+  if (params->Nc != 1 || params->precision == PHN_FP32_KAHAN)
+    return set_error(PHN_ERR_UNSUPPORTED, "adjoint: Nc = 1, FP32 or FP64");
+  phn_adjoint *a = new phn_adjoint();
+  a->p = *params;
+  a->k = make_consts(params);
+  a->nsteps = nsteps;
+  a->every = every;
+  a->nseg = nsteps / every;
+  a->w = width;
+  a->V = (size_t)params->N * params->N * params->N;
+  a->elem = params->precision == PHN_FP64 ? 8 : 4;
+  r = phn_create(params, &a->fwd);
+  if (r) {
+    adj_free(a);
+    return r;
+  }
+  const size_t fb = a->V * a->elem;
+  cudaError_t e = cudaMalloc(&a->ckpt, (size_t)(a->nseg + 1) * 2 * fb);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    e = cudaMalloc(&a->rphi[i], fb);
+    if (e == cudaSuccess) e = cudaMalloc(&a->rpi[i], fb);
+    if (e == cudaSuccess) e = cudaMalloc(&a->lphi[i], fb);
+    if (e == cudaSuccess) e = cudaMalloc(&a->lpi[i], fb);
+  }
+  a->sum_blocks = 152 * 4;
+  if (e == cudaSuccess) e = cudaMalloc(&a->rho, a->V * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&a->g, a->V * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&a->sums, a->sum_blocks * sizeof(double));
+  const Grid gr = lattice_grid(params->N);
+  if (e == cudaSuccess) e = cudaMalloc(&a->gs, (size_t)gr.nblocks * ADJ_NG * sizeof(double));
+  if (e == cudaSuccess) e = cudaEventCreate(&a->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&a->ev1);
+  if (e != cudaSuccess) {
+    r = cuda_error(e, "adjoint buffers");
+    adj_free(a);
+    return r;
+  }
+  *out = a;
+  return PHN_OK;
+}
+
+int phn_adjoint_destroy(phn_adjoint *a) {
+  adj_free(a);
+  return PHN_OK;
+}
+
+int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, double *J) {
+  if (!a || !Phi0 || !Pi0) return set_error(PHN_ERR_INVALID, "NULL argument");
+  phn_handle *h = a->fwd;
+  int r = phn_upload(h, Phi0, Pi0);
+  if (r) return r;
+  r = phn_reset(h);
+  if (r) return r;
+  void *phi = nullptr, *pi = nullptr, *stv = nullptr;
+  const size_t fb = a->V * a->elem;
+  char *ck = (char *)a->ckpt;
+  a->fk.clear();
+  a->fd.clear();
+  phn_device_fields(h, &phi, &pi, &stv);
+  cudaStream_t st = (cudaStream_t)stv;
+  CKA(cudaEventRecord(a->ev0, st));
+  CKA(cudaMemcpyAsync(ck, phi, fb, cudaMemcpyDeviceToDevice, st));
+  CKA(cudaMemcpyAsync(ck + fb, pi, fb, cudaMemcpyDeviceToDevice, st));
+  for (int s = 0; s < a->nseg; ++s) {
+    // the factors the next `every` steps will use: the clock arithmetic of
+    // dynamics.cpp:200-213, as the handle runs it
+    double tau = h->tau, lm = h->last_mom, lf = h->last_field;
+    for (int i = 0; i < a->every; ++i) {
+      tau += 0.5 * h->dtau;
+      a->fk.push_back(tau - lm);
+      lm = tau;
+      tau += 0.5 * h->dtau;
+      a->fd.push_back(tau - lf);
+      lf = tau;
+    }
+    r = phn_evolve(h, a->every);
+    if (r) return r;
+    phn_device_fields(h, &phi, &pi, &stv);
+    CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb, phi, fb, cudaMemcpyDeviceToDevice, st));
+    CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb + fb, pi, fb, cudaMemcpyDeviceToDevice, st));
+  }
+  if (a->elem == 8)
+    r = objective<double>(a, (const double *)phi, (const double *)pi, true, st);
+  else
+    r = objective<float>(a, (const float *)phi, (const float *)pi, true, st);
+  if (r) return r;
+  CKA(cudaEventRecord(a->ev1, st));
+  CKA(cudaEventSynchronize(a->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a->ev0, a->ev1);
+  a->fwd_ms = ms;
+  a->forward_done = true;
+  if (J) *J = a->J;
+  return PHN_OK;
+}
+
+// grads[0] = dJ/d(homogeneous phi shift) = sum_x dJ/dphi_0(x)
+// grads[1] = dJ/dc6, c6 the phi^6 coefficient of V (theory 0: 1/(720 Kappa^2))
+// grads[2] = dJ/dh (theory 1)
+int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *grads) {
+  if (!a) return set_error(PHN_ERR_INVALID, "NULL argument");
+  if (!a->forward_done) return set_error(PHN_ERR_INVALID, "phn_adjoint_forward first");
+  phn_handle *h = a->fwd;
+  void *phi = nullptr, *pi = nullptr, *stv = nullptr;
+  phn_device_fields(h, &phi, &pi, &stv);
+  cudaStream_t st = (cudaStream_t)stv;
+  const size_t fb = a->V * a->elem;
+  const Grid gr = lattice_grid(a->p.N);
+  const bool dbl = a->elem == 8;
+  const int nb = a->sum_blocks;
+  CKA(cudaEventRecord(a->ev0, st));
+  gs_zero<<<64, 256, 0, st>>>(a->gs, (size_t)gr.nblocks * ADJ_NG);
+  // adjoint of the objective at the final state
+  if (dbl)
+    obj_adjoint_init<double><<<nb, 256, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
+                                                 (double *)a->lphi[0], (double *)a->lpi[0]);
+  else
+    obj_adjoint_init<float><<<nb, 256, 0, st>>>((const float *)phi, (const float *)pi, a->g, a->k,
+                                                (float *)a->lphi[0], (float *)a->lpi[0]);
+  CKA(cudaGetLastError());
+  // direct dependence of rho on the couplings
+  obj_sum<<<nb, 256, 0, st>>>(a->rho, a->g, a->V, SUM_GPHI6, 0.0, a->w, phi, dbl, a->sums);
+  const double direct_c6 = host_sum(a, st);
+  obj_sum<<<nb, 256, 0, st>>>(a->rho, a->g, a->V, SUM_GPHI, 0.0, a->w, phi, dbl, a->sums);
+  const double direct_h = host_sum(a, st);
+  CKA(cudaEventRecord(a->ev0, st));  // backward timing starts after the seed
+  int cur = 0;  // lphi[cur], lpi[cur] hold the adjoint
+  char *ck = (char *)a->ckpt;
+  int sbuf = 0;
+  for (int s = a->nseg - 1; s >= 0; --s) {
+    // re-anchor: the segment's end state is its checkpoint
+    const void *phi1 = ck + (size_t)(s + 1) * 2 * fb;
+    const void *pi1 = ck + (size_t)(s + 1) * 2 * fb + fb;
+    for (int i = a->every - 1; i >= 0; --i) {
+      const int n = s * a->every + i;
+      void *phi0 = a->rphi[sbuf], *pi0 = a->rpi[sbuf];
+      if (dbl)
+        adjoint_step<double><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
+            (const double *)phi1, (const double *)pi1, (const double *)a->lphi[cur], (const double *)a->lpi[cur],
+            (double *)phi0, (double *)pi0, (double *)a->lphi[1 - cur], (double *)a->lpi[1 - cur], a->k, a->fk[n],
+            a->fd[n], gr.cz, a->gs);
+      else
+        adjoint_step<float><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
+            (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
+            (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
+            (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
+      CKA(cudaGetLastError());
+      h->launches++;
+      cur = 1 - cur;
+      phi1 = phi0;
+      pi1 = pi0;
+      sbuf = 1 - sbuf;
+    }
+  }
+  CKA(cudaEventRecord(a->ev1, st));
+  CKA(cudaEventSynchronize(a->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a->ev0, a->ev1);
+  a->bwd_ms = ms;
+  // gradient slots, fixed order
+  std::vector<double> gsh((size_t)gr.nblocks * ADJ_NG);
+  CKA(cudaMemcpy(gsh.data(), a->gs, gsh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  double g_c6 = 0.0, g_h = 0.0;
+  for (int b = 0; b < gr.nblocks; ++b) {
+    g_c6 += gsh[(size_t)b * ADJ_NG + 0];
+    g_h += gsh[(size_t)b * ADJ_NG + 1];
+  }
+  // fields: lam_phi(0), lam_pi(0) in the reference layout
+  const int N = a->p.N;
+  double *ref = nullptr;
+  CKA(cudaMalloc(&ref, (size_t)N * N * (N + 2) * sizeof(double)));
+  const size_t slab = (size_t)N * N, nref = slab * (N + 2);
+  double sum_lphi = 0.0;
+  std::vector<double> tmp;
+  if (dPhi0 || grads) {
+    CKA(launch_to_ref(a->lphi[cur], ref, a->p.precision, N, 1, st));
+    double *dst = dPhi0;
+    if (!dst) {
+      tmp.resize(nref);
+      dst = tmp.data();
+    }
+    CKA(cudaMemcpyAsync(dst, ref, nref * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CKA(cudaStreamSynchronize(st));
+    for (size_t i = slab; i < slab * (N + 1); ++i) sum_lphi += dst[i];
+  }
+  if (dPi0) {
+    CKA(launch_to_ref(a->lpi[cur], ref, a->p.precision, N, 1, st));
+    CKA(cudaMemcpyAsync(dPi0 + slab, ref + slab, slab * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CKA(cudaStreamSynchronize(st));
+  }
+  cudaFree(ref);
+  if (grads) {
+    grads[0] = sum_lphi;
+    grads[1] = g_c6 + direct_c6;
+    grads[2] = g_h + direct_h;
+  }
+  return PHN_OK;
+}
+
+int phn_adjoint_info(const phn_adjoint *a, double *J, double *forward_ms, double *backward_ms) {
+  if (!a) return set_error(PHN_ERR_INVALID, "NULL argument");
+  if (J) *J = a->J;
+  if (forward_ms) *forward_ms = a->fwd_ms;
+  if (backward_ms) *backward_ms = a->bwd_ms;
+  return PHN_OK;
+}
+
+}  // extern "C"

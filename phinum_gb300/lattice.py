@@ -235,3 +235,52 @@ def device_count() -> int:
     n = ctypes.c_int()
     r = lib.phn_device_count(ctypes.byref(n))
     return n.value if r == L.OK else 0
+
+
+class Adjoint:
+    """Forward/backward pair of the hand-written adjoint (phn_adjoint_*)."""
+
+    def __init__(self, p: Params, nsteps: int, every: int = 50, width: float = 0.1):
+        self.p = p
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        L.check(self.lib.phn_adjoint_create(ctypes.byref(p.c()), int(nsteps), int(every), float(width),
+                                            ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.phn_adjoint_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, phi: np.ndarray, pi: np.ndarray) -> float:
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        pi = np.ascontiguousarray(pi, dtype=np.float64)
+        J = ctypes.c_double()
+        L.check(self.lib.phn_adjoint_forward(self.h, _pd(phi), _pd(pi), ctypes.byref(J)))
+        return J.value
+
+    def backward(self):
+        """Returns (dJ/dPhi0, dJ/dPi0, [dJ/dshift, dJ/dc6, dJ/dh]) in the reference layout."""
+        n = self.p.field_len
+        dphi, dpi = np.zeros(n), np.zeros(n)
+        g = np.zeros(3)
+        L.check(self.lib.phn_adjoint_backward(self.h, _pd(dphi), _pd(dpi), _pd(g)))
+        return dphi, dpi, g
+
+    def info(self):
+        J, f, b = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        L.check(self.lib.phn_adjoint_info(self.h, ctypes.byref(J), ctypes.byref(f), ctypes.byref(b)))
+        return J.value, f.value, b.value

@@ -1,0 +1,103 @@
+"""Hand-written adjoint (phn_adjoint_*): gradients against central finite
+differences of the forward objective (FP64), and FP32 gradients against the
+FP64 adjoint.
+
+Tolerances: FP64 adjoint vs FD, relative 1e-6 per direction (FD step 1e-5,
+O(h^2) truncation); FP32 vs FP64 adjoint, relative L2 error of the field
+gradient 2e-3 on short runs."""
+import numpy as np
+import pytest
+
+import inputs
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SQ6 = 6 ** 0.5
+
+
+def setup(N, seed, theory=0):
+    from phinum_gb300 import lattice as PL
+    phi0 = SQ6 if theory == 0 else -SQ6
+    phi, pi = inputs.lattice_fields(N, 1, seed, phi0=phi0)
+    kw = dict(theory=0, kappa=3 ** 0.5) if theory == 0 else dict(theory=1, mass_mode=-1, lambda_mode=1, h=0.3)
+    return kw, O.to_ref_layout(phi), O.to_ref_layout(pi)
+
+
+def direction(N, seed):
+    rng = np.random.default_rng(seed)
+    v = O.to_ref_layout(rng.standard_normal((N, N, N)))
+    return v / np.linalg.norm(v[N * N:-N * N])
+
+
+@pytest.mark.parametrize("theory", [0, 1])
+def test_fp64_adjoint_matches_finite_differences(theory):
+    from phinum_gb300 import lattice as PL
+    N, steps, every = 16, 40, 10
+    kw, phi, pi = setup(N, 7 + theory, theory)
+    p = PL.Params(N=N, precision=0, **kw)
+    with PL.Adjoint(p, steps, every) as adj:
+        J0 = adj.forward(phi, pi)
+        dphi, dpi, g = adj.backward()
+        eps = 1e-5
+        sl = slice(N * N, -N * N)
+        for k in range(3):
+            v = direction(N, 100 + k)
+            fd = (adj.forward(phi + eps * v, pi) - adj.forward(phi - eps * v, pi)) / (2 * eps)
+            ad = float(np.dot(dphi[sl], v[sl]))
+            assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(J0)), (k, ad, fd)
+            fdp = (adj.forward(phi, pi + eps * v) - adj.forward(phi, pi - eps * v)) / (2 * eps)
+            adp = float(np.dot(dpi[sl], v[sl]))
+            assert abs(adp - fdp) <= 1e-6 * max(abs(fdp), 1e-3 * abs(J0)), (k, adp, fdp)
+        # homogeneous shift of the initial phi
+        one = np.ones_like(phi)
+        fd = (adj.forward(phi + eps * one, pi) - adj.forward(phi - eps * one, pi)) / (2 * eps)
+        assert abs(g[0] - fd) <= 1e-6 * abs(fd), (g[0], fd)
+    # coupling: c6 = 1/(720 Kappa^2) (theory 0) or h (theory 1), by re-running with it perturbed
+    def J_at(delta):
+        if theory == 0:
+            c6 = 1.0 / (720 * kw["kappa"] ** 2) + delta
+            q = PL.Params(N=N, precision=0, **dict(kw, kappa=(1.0 / (720 * c6)) ** 0.5))
+        else:
+            q = PL.Params(N=N, precision=0, **dict(kw, h=kw["h"] + delta))
+        with PL.Adjoint(q, steps, every) as a2:
+            return a2.forward(phi, pi)
+    epsc = 1e-6 if theory == 0 else 1e-5
+    fd = (J_at(epsc) - J_at(-epsc)) / (2 * epsc)
+    ad = g[1] if theory == 0 else g[2]
+    assert abs(ad - fd) <= 2e-6 * abs(fd), (ad, fd)
+
+
+def test_fp32_adjoint_close_to_fp64_adjoint():
+    from phinum_gb300 import lattice as PL
+    N, steps, every = 32, 100, 50
+    kw, phi, pi = setup(N, 21)
+    out = {}
+    for prec in (0, 1):
+        with PL.Adjoint(PL.Params(N=N, precision=prec, **kw), steps, every) as adj:
+            J = adj.forward(phi, pi)
+            out[prec] = (J,) + adj.backward()
+    sl = slice(N * N, -N * N)
+    J64, d64, p64, g64 = out[0]
+    J32, d32, p32, g32 = out[1]
+    assert abs(J32 - J64) <= 1e-4 * abs(J64)
+    assert np.linalg.norm(d32[sl] - d64[sl]) <= 2e-3 * np.linalg.norm(d64[sl])
+    assert np.linalg.norm(p32[sl] - p64[sl]) <= 2e-3 * np.linalg.norm(p64[sl])
+    assert abs(g32[0] - g64[0]) <= 2e-3 * abs(g64[0])
+    assert abs(g32[1] - g64[1]) <= 2e-3 * abs(g64[1])
+
+
+def test_backward_is_deterministic_and_forward_matches_evolve():
+    from phinum_gb300 import lattice as PL
+    N, steps, every = 32, 60, 20
+    kw, phi, pi = setup(N, 5)
+    p = PL.Params(N=N, precision=1, **kw)
+    with PL.Adjoint(p, steps, every) as adj:
+        adj.forward(phi, pi)
+        a = adj.backward()
+        adj.forward(phi, pi)
+        b = adj.backward()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    with pytest.raises(Exception):
+        PL.Adjoint(p, 61, 20)
