@@ -48,17 +48,31 @@ struct AdjOps<double> {
 // Potential pieces for one component (Nc = 1), in T arithmetic.
 //   V'(phi)  = (mmM + lm phi^2/6 [+ phi^4 / (120 Kappa^2)]) phi [+ h]
 //   V''(phi) =  mmM + lm phi^2/2 [+ 5 phi^4 / (120 Kappa^2)]
+// F = Lap(phi) - V'(phi), the Laplacian given as the sum of the six
+// neighbour differences (phi_nb - phi), as in the FP32 forward kernels.
 template <typename T>
-__device__ __forceinline__ T force(const Consts &k, T lap_sum, T c) {
-  // F = Lap(phi) - V'(phi): same expression as the forward kernels
+__device__ __forceinline__ T force(const Consts &k, T diff_sum, T c) {
   const T inv_a2 = (T)1 / (T)k.a2;
   const T l = c * c;
   T coef = (T)k.mmM + l * ((T)k.lm / (T)k.six_nc);
   if (k.theory == 0) coef += (l * l) * ((T)1 / ((T)k.kappa * (T)k.kappa * (T)k.c120));
-  T f = (lap_sum - (T)6 * c) * inv_a2 - coef * c;
+  T f = diff_sum * inv_a2 - coef * c;
   if (k.theory == 1) f -= (T)k.h;
   return f;
 }
+
+// Per-thread compensated sum (Kahan) in T; FP64 only once per thread.
+template <typename T>
+struct KSum {
+  T s = 0, c = 0;
+  __device__ __forceinline__ void add(T v) {
+    const T y = v - c;
+    const T t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
 
 template <typename T>
 __device__ __forceinline__ T vpp(const Consts &k, T c) {
@@ -82,7 +96,7 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
   const int x = blockIdx.x * ADJ_TX + threadIdx.x, y = blockIdx.y * ADJ_TY + threadIdx.y;
   const int z0 = blockIdx.z * cz, z1 = min(z0 + cz, N);
   const size_t NN = (size_t)N * N;
-  double g_c6 = 0.0, g_h = 0.0;
+  KSum<T> k_c6, k_h;
   if (x < N && y < N && z0 < z1) {
     const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
     const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
@@ -94,7 +108,6 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
     T pm = rphi((size_t)zm0 * NN + col), pc = rphi((size_t)z0 * NN + col);
     T mm = rmu((size_t)zm0 * NN + col), mc = rmu((size_t)z0 * NN + col);
     const T inv_a2 = (T)1 / (T)k.a2;
-    const T c6 = k.theory == 0 ? (T)1 / ((T)720 * (T)k.kappa * (T)k.kappa) : (T)0;
     for (int z = z0; z < z1; ++z) {
       const int zn = (z + 1 == N) ? 0 : z + 1;
       const size_t pl = (size_t)z * NN, i = pl + col;
@@ -102,33 +115,34 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
       const size_t ixp = pl + (size_t)y * N + xp, ixm = pl + (size_t)y * N + xm;
       const size_t iyp = pl + (size_t)yp * N + x, iym = pl + (size_t)ym * N + x;
       // state before the step
-      const T sum_phi = ((rphi(ixp) + rphi(ixm)) + (rphi(iyp) + rphi(iym))) + (pn + pm);
-      const T f = force<T>(k, sum_phi, pc);
+      const T dphi = (((rphi(ixp) - pc) + (rphi(ixm) - pc)) + ((rphi(iyp) - pc) + (rphi(iym) - pc))) +
+                     ((pn - pc) + (pm - pc));
+      const T f = force<T>(k, dphi, pc);
       const T pi_before = AdjOps<T>::fma_(-fk, f, pi1[i]);
       // adjoint
-      const T sum_mu = ((rmu(ixp) + rmu(ixm)) + (rmu(iyp) + rmu(iym))) + (mn + mm);
-      const T lap_mu = (sum_mu - (T)6 * mc) * inv_a2;
+      const T dmu = (((rmu(ixp) - mc) + (rmu(ixm) - mc)) + ((rmu(iyp) - mc) + (rmu(iym) - mc))) +
+                    ((mn - mc) + (mm - mc));
+      const T lap_mu = dmu * inv_a2;
       const T lphi_before = AdjOps<T>::fma_(fk, lap_mu - vpp<T>(k, pc) * mc, lphi[i]);
       phi0[i] = pc;
       pi0[i] = pi_before;
       lphi0[i] = lphi_before;
       lpi0[i] = mc;
       // dF/dc6 = -6 phi^5 ; dF/dh = -1   (kick pi' = pi + fk F)
-      const double p5 = (double)pc * (double)pc * (double)pc * (double)pc * (double)pc;
-      g_c6 += (double)fk * (double)mc * (-6.0 * p5);
-      g_h += -(double)fk * (double)mc;
+      const T p2 = pc * pc;
+      k_c6.add(fk * mc * ((T)-6 * (p2 * p2 * pc)));
+      k_h.add(-fk * mc);
       pm = pc;
       pc = pn;
       mm = mc;
       mc = mn;
     }
-    (void)c6;
   }
   // block sums (fixed order) into this block's gradient slot
   __shared__ double sh[2][ADJ_THREADS];
   const int tid = threadIdx.x + ADJ_TX * threadIdx.y;
-  sh[0][tid] = g_c6;
-  sh[1][tid] = g_h;
+  sh[0][tid] = k_c6.value();
+  sh[1][tid] = k_h.value();
   __syncthreads();
   for (int w = ADJ_THREADS / 2; w > 0; w >>= 1) {
     if (tid < w) {
@@ -484,7 +498,7 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   // gradient slots, fixed order
   std::vector<double> gsh((size_t)gr.nblocks * ADJ_NG);
   CKA(cudaMemcpy(gsh.data(), a->gs, gsh.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  double g_c6 = 0.0, g_h = 0.0;
+  KSum<T> k_c6, k_h;
   for (int b = 0; b < gr.nblocks; ++b) {
     g_c6 += gsh[(size_t)b * ADJ_NG + 0];
     g_h += gsh[(size_t)b * ADJ_NG + 1];

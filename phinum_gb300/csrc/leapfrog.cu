@@ -14,6 +14,7 @@
 // of phi is fetched from HBM once per chunk; x/y neighbours hit L1/L2.
 #include <math.h>
 
+#include "kick.cuh"
 #include "observe.cuh"
 #include "phn_internal.h"
 
@@ -139,11 +140,8 @@ __global__ void __launch_bounds__(THREADS) step_f32(const float *__restrict__ ph
         if (THEORY == 0) coef = fmaf(__fmul_rn(l, l), k.c6_f, coef);
 #pragma unroll
         for (int a = 0; a < NC; ++a) {
-          // rounding pinned with explicit intrinsics: the TMA kernel computes the same bits
-          const float lap = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(fxp[a], fxm[a]), __fadd_rn(fyp[a], fym[a])),
-                                                          __fadd_rn(cp[a], cm[a])),
-                                                __fmul_rn(-6.f, c[a])),
-                                      k.inv_a2_f);
+          // the shared neighbour-difference Laplacian: the TMA kernel computes the same bits
+          const float lap = lap_diff_f32(c[a], fxm[a], fxp[a], fym[a], fyp[a], cm[a], cp[a], k.inv_a2_f);
           float f = fmaf(-coef, c[a], lap);
           if (THEORY == 1 && a == 0) f = __fsub_rn(f, k.h_f);
           const float pn = fmaf(fk, f, p[a]);
@@ -227,11 +225,8 @@ __global__ void __launch_bounds__(THREADS) step_kahan(const float *__restrict__ 
         if (THEORY == 0) coef = fmaf(__fmul_rn(l, l), k.c6_f, coef);
 #pragma unroll
         for (int a = 0; a < NC; ++a) {
-          // rounding pinned with explicit intrinsics: the TMA kernel computes the same bits
-          const float lap = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(fxp[a], fxm[a]), __fadd_rn(fyp[a], fym[a])),
-                                                          __fadd_rn(cp[a], cm[a])),
-                                                __fmul_rn(-6.f, c[a])),
-                                      k.inv_a2_f);
+          // the shared neighbour-difference Laplacian: the TMA kernel computes the same bits
+          const float lap = lap_diff_f32(c[a], fxm[a], fxp[a], fym[a], fyp[a], cm[a], cp[a], k.inv_a2_f);
           float f = fmaf(-coef, c[a], lap);
           if (THEORY == 1 && a == 0) f = __fsub_rn(f, k.h_f);
           // kick: pi += fk * f  (Kahan)

@@ -62,7 +62,7 @@ def test_fp64_adjoint_matches_finite_differences(theory):
             q = PL.Params(N=N, precision=0, **dict(kw, h=kw["h"] + delta))
         with PL.Adjoint(q, steps, every) as a2:
             return a2.forward(phi, pi)
-    epsc = 1e-6 if theory == 0 else 1e-5
+    epsc = 1e-8 if theory == 0 else 1e-6
     fd = (J_at(epsc) - J_at(-epsc)) / (2 * epsc)
     ad = g[1] if theory == 0 else g[2]
     assert abs(ad - fd) <= 2e-6 * abs(fd), (ad, fd)
