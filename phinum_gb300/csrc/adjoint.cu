@@ -498,7 +498,7 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   // gradient slots, fixed order
   std::vector<double> gsh((size_t)gr.nblocks * ADJ_NG);
   CKA(cudaMemcpy(gsh.data(), a->gs, gsh.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  KSum<T> k_c6, k_h;
+  double g_c6 = 0.0, g_h = 0.0;
   for (int b = 0; b < gr.nblocks; ++b) {
     g_c6 += gsh[(size_t)b * ADJ_NG + 0];
     g_h += gsh[(size_t)b * ADJ_NG + 1];
