@@ -85,6 +85,12 @@ __device__ __forceinline__ T vpp(const Consts &k, T c) {
 // One reverse step.  phi1, pi1: state after the step; lphi, lpi: adjoints at
 // that time.  Writes phi0, pi0 (state before) and lphi0, lpi0 (adjoints
 // before).  Gradient slots: gs[block][j] += this step's coupling terms.
+//
+// A block is 32 x 8 sites marching `cz` planes.  The reconstructed field
+// phi = phi' - fd pi' and the adjoint mu = lam_pi + fd lam_phi of each site are
+// formed once, kept in registers along z and put in a shared-memory tile of
+// the current plane (with its one-site x/y halo, formed by the edge threads)
+// for the stencils.
 template <typename T>
 __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict__ phi1, const T *__restrict__ pi1,
                                                             const T *__restrict__ lphi, const T *__restrict__ lpi,
@@ -92,38 +98,71 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
                                                             T *__restrict__ lphi0, T *__restrict__ lpi0,
                                                             const Consts k, const T fk, const T fd, const int cz,
                                                             double *__restrict__ gs) {
+  __shared__ T sp[ADJ_TY + 2][ADJ_TX + 2], sm[ADJ_TY + 2][ADJ_TX + 2];
   const int N = k.N;
-  const int x = blockIdx.x * ADJ_TX + threadIdx.x, y = blockIdx.y * ADJ_TY + threadIdx.y;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x = blockIdx.x * ADJ_TX + tx, y = blockIdx.y * ADJ_TY + ty;
   const int z0 = blockIdx.z * cz, z1 = min(z0 + cz, N);
   const size_t NN = (size_t)N * N;
+  const bool act = x < N && y < N;
+  // clamp inactive threads onto a valid site so that they can still fill halos
+  const int xs = act ? x : N - 1, ys = act ? y : N - 1;
+  const int xp = (xs + 1 == N) ? 0 : xs + 1, xm = (xs == 0) ? N - 1 : xs - 1;
+  const int yp = (ys + 1 == N) ? 0 : ys + 1, ym = (ys == 0) ? N - 1 : ys - 1;
+  const size_t col = (size_t)ys * N + xs;
+  auto rphi = [&](size_t i) { return AdjOps<T>::fma_(-fd, pi1[i], phi1[i]); };
+  auto rmu = [&](size_t i) { return AdjOps<T>::fma_(fd, lphi[i], lpi[i]); };
+  const T inv_a2 = (T)1 / (T)k.a2;
   KSum<T> k_c6, k_h;
-  if (x < N && y < N && z0 < z1) {
-    const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
-    const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
-    const size_t col = (size_t)y * N + x;
-    // reconstructed phi and mu at a site
-    auto rphi = [&](size_t i) { return AdjOps<T>::fma_(-fd, pi1[i], phi1[i]); };
-    auto rmu = [&](size_t i) { return AdjOps<T>::fma_(fd, lphi[i], lpi[i]); };
-    const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
-    T pm = rphi((size_t)zm0 * NN + col), pc = rphi((size_t)z0 * NN + col);
-    T mm = rmu((size_t)zm0 * NN + col), mc = rmu((size_t)z0 * NN + col);
-    const T inv_a2 = (T)1 / (T)k.a2;
-    for (int z = z0; z < z1; ++z) {
-      const int zn = (z + 1 == N) ? 0 : z + 1;
-      const size_t pl = (size_t)z * NN, i = pl + col;
-      const T pn = rphi((size_t)zn * NN + col), mn = rmu((size_t)zn * NN + col);
-      const size_t ixp = pl + (size_t)y * N + xp, ixm = pl + (size_t)y * N + xm;
-      const size_t iyp = pl + (size_t)yp * N + x, iym = pl + (size_t)ym * N + x;
-      // state before the step
-      const T dphi = (((rphi(ixp) - pc) + (rphi(ixm) - pc)) + ((rphi(iyp) - pc) + (rphi(iym) - pc))) +
+  const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
+  T pm = rphi((size_t)zm0 * NN + col), mm = rmu((size_t)zm0 * NN + col);
+  size_t ic = (size_t)z0 * NN + col;
+  T pc = rphi(ic), mc = rmu(ic), pic = pi1[ic], lphic = lphi[ic];
+  // edge threads own the halo sites of their row / column
+  const bool hx0 = tx == 0, hx1 = (tx == ADJ_TX - 1) || (x == N - 1);
+  const bool hy0 = ty == 0, hy1 = (ty == ADJ_TY - 1) || (y == N - 1);
+  for (int z = z0; z < z1; ++z) {
+    const size_t pl = (size_t)z * NN;
+    if (act) {  // only sites of the lattice write the tile (no slot has two writers)
+      sp[ty + 1][tx + 1] = pc;
+      sm[ty + 1][tx + 1] = mc;
+      if (hx0) {
+        const size_t j = pl + (size_t)ys * N + xm;
+        sp[ty + 1][0] = rphi(j);
+        sm[ty + 1][0] = rmu(j);
+      }
+      if (hx1) {
+        const size_t j = pl + (size_t)ys * N + xp;
+        sp[ty + 1][tx + 2] = rphi(j);
+        sm[ty + 1][tx + 2] = rmu(j);
+      }
+      if (hy0) {
+        const size_t j = pl + (size_t)ym * N + xs;
+        sp[0][tx + 1] = rphi(j);
+        sm[0][tx + 1] = rmu(j);
+      }
+      if (hy1) {
+        const size_t j = pl + (size_t)yp * N + xs;
+        sp[ty + 2][tx + 1] = rphi(j);
+        sm[ty + 2][tx + 1] = rmu(j);
+      }
+    }
+    // next plane of this column (also phi(z+1), mu(z+1) of the stencils)
+    const int zn = (z + 1 == N) ? 0 : z + 1;
+    const size_t in = (size_t)zn * NN + col;
+    const T pn = rphi(in), mn = rmu(in), pin = pi1[in], lphin = lphi[in];
+    __syncthreads();
+    if (act) {
+      const size_t i = pl + col;
+      const T dphi = (((sp[ty + 1][tx + 2] - pc) + (sp[ty + 1][tx] - pc)) +
+                      ((sp[ty + 2][tx + 1] - pc) + (sp[ty][tx + 1] - pc))) +
                      ((pn - pc) + (pm - pc));
       const T f = force<T>(k, dphi, pc);
-      const T pi_before = AdjOps<T>::fma_(-fk, f, pi1[i]);
-      // adjoint
-      const T dmu = (((rmu(ixp) - mc) + (rmu(ixm) - mc)) + ((rmu(iyp) - mc) + (rmu(iym) - mc))) +
+      const T pi_before = AdjOps<T>::fma_(-fk, f, pic);
+      const T dmu = (((sm[ty + 1][tx + 2] - mc) + (sm[ty + 1][tx] - mc)) +
+                     ((sm[ty + 2][tx + 1] - mc) + (sm[ty][tx + 1] - mc))) +
                     ((mn - mc) + (mm - mc));
-      const T lap_mu = dmu * inv_a2;
-      const T lphi_before = AdjOps<T>::fma_(fk, lap_mu - vpp<T>(k, pc) * mc, lphi[i]);
+      const T lphi_before = AdjOps<T>::fma_(fk, dmu * inv_a2 - vpp<T>(k, pc) * mc, lphic);
       phi0[i] = pc;
       pi0[i] = pi_before;
       lphi0[i] = lphi_before;
@@ -132,15 +171,18 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
       const T p2 = pc * pc;
       k_c6.add(fk * mc * ((T)-6 * (p2 * p2 * pc)));
       k_h.add(-fk * mc);
-      pm = pc;
-      pc = pn;
-      mm = mc;
-      mc = mn;
     }
+    __syncthreads();
+    pm = pc;
+    pc = pn;
+    mm = mc;
+    mc = mn;
+    pic = pin;
+    lphic = lphin;
   }
   // block sums (fixed order) into this block's gradient slot
   __shared__ double sh[2][ADJ_THREADS];
-  const int tid = threadIdx.x + ADJ_TX * threadIdx.y;
+  const int tid = tx + ADJ_TX * ty;
   sh[0][tid] = k_c6.value();
   sh[1][tid] = k_h.value();
   __syncthreads();
@@ -156,6 +198,35 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
     gs[b * ADJ_NG + 0] += sh[0][0];
     gs[b * ADJ_NG + 1] += sh[1][0];
   }
+}
+
+// Grid of the reverse kernel: planes per block chosen so that the blocks
+// fill whole waves of the resident capacity (larger chunks preferred).
+template <typename T>
+static Grid adjoint_grid(int N) {
+  Grid g;
+  g.block = dim3(ADJ_TX, ADJ_TY, 1);
+  const int gx = (N + ADJ_TX - 1) / ADJ_TX, gy = (N + ADJ_TY - 1) / ADJ_TY;
+  int dev = 0, sms = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step<T>, ADJ_THREADS, 0);
+  const double resident = (double)sms * (occ > 0 ? occ : 1);
+  int best_cz = 1;
+  double best_eff = -1.0;
+  for (int cz = 32; cz >= 1; cz /= 2) {
+    const int gz = (N + cz - 1) / cz;
+    const double waves = (double)gx * gy * gz / resident;
+    const double eff = waves / ceil(waves);
+    if (eff > best_eff + 0.02) {
+      best_eff = eff;
+      best_cz = cz;
+    }
+  }
+  g.cz = best_cz;
+  g.grid = dim3(gx, gy, (N + best_cz - 1) / best_cz);
+  g.nblocks = gx * gy * g.grid.z;
+  return g;
 }
 
 // ---------------------------------------------------------------- objective
@@ -364,7 +435,7 @@ int phn_adjoint_create(const phn_params *params, int nsteps, int every, double w
   if (e == cudaSuccess) e = cudaMalloc(&a->rho, a->V * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&a->g, a->V * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&a->sums, a->sum_blocks * sizeof(double));
-  const Grid gr = lattice_grid(params->N);
+  const Grid gr = params->precision == PHN_FP64 ? adjoint_grid<double>(params->N) : adjoint_grid<float>(params->N);
   if (e == cudaSuccess) e = cudaMalloc(&a->gs, (size_t)gr.nblocks * ADJ_NG * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreate(&a->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&a->ev1);
@@ -411,7 +482,7 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
       a->fd.push_back(tau - lf);
       lf = tau;
     }
-    r = phn_evolve(h, a->every);
+    r = evolve_async(h, a->every);
     if (r) return r;
     phn_device_fields(h, &phi, &pi, &stv);
     CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb, phi, fb, cudaMemcpyDeviceToDevice, st));
@@ -443,8 +514,8 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   phn_device_fields(h, &phi, &pi, &stv);
   cudaStream_t st = (cudaStream_t)stv;
   const size_t fb = a->V * a->elem;
-  const Grid gr = lattice_grid(a->p.N);
   const bool dbl = a->elem == 8;
+  const Grid gr = dbl ? adjoint_grid<double>(a->p.N) : adjoint_grid<float>(a->p.N);
   const int nb = a->sum_blocks;
   CKA(cudaEventRecord(a->ev0, st));
   gs_zero<<<64, 256, 0, st>>>(a->gs, (size_t)gr.nblocks * ADJ_NG);

@@ -335,6 +335,15 @@ static int check_device_error(phn_handle *h) {
   return PHN_OK;
 }
 
+// nsteps plain steps queued on the handle's stream, no synchronisation.
+int phn::evolve_async(phn_handle *h, int nsteps) {
+  for (int i = 0; i < nsteps; ++i) {
+    int r = step_once(h, MODE_STEP);
+    if (r) return r;
+  }
+  return PHN_OK;
+}
+
 int phn_evolve(phn_handle *h, int nsteps) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
   if (nsteps < 0) return set_error(PHN_ERR_INVALID, "nsteps < 0");

@@ -152,4 +152,5 @@ struct phn_handle {
 namespace phn {
 void spectrum_release(phn_handle *h);
 void islands_release(phn_handle *h);
+int evolve_async(phn_handle *h, int nsteps);  // api.cu: steps queued, no sync
 }  // namespace phn
