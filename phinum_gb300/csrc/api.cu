@@ -335,6 +335,8 @@ static int check_device_error(phn_handle *h) {
   return PHN_OK;
 }
 
+}  // extern "C"
+
 // nsteps plain steps queued on the handle's stream, no synchronisation.
 int phn::evolve_async(phn_handle *h, int nsteps) {
   for (int i = 0; i < nsteps; ++i) {
@@ -343,6 +345,8 @@ int phn::evolve_async(phn_handle *h, int nsteps) {
   }
   return PHN_OK;
 }
+
+extern "C" {
 
 int phn_evolve(phn_handle *h, int nsteps) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
