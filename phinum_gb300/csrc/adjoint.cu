@@ -23,6 +23,7 @@
 // the four earlier fields: 32 bytes per site in FP32.  Coupling gradients
 // accumulate per block across steps in fixed slots (deterministic).
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <vector>
@@ -200,8 +201,10 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
   }
 }
 
-// Grid of the reverse kernel: planes per block chosen so that the blocks
-// fill whole waves of the resident capacity (larger chunks preferred).
+// Grid of the reverse kernel.  Cost model: whole waves of the resident
+// capacity times the planes a block handles plus its fixed overhead (the two
+// z-halo planes and the gradient reduction, about six planes' worth).
+// PHN_ADJ_CZ overrides the planes per block (tuning).
 template <typename T>
 static Grid adjoint_grid(int N) {
   Grid g;
@@ -211,18 +214,19 @@ static Grid adjoint_grid(int N) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step<T>, ADJ_THREADS, 0);
-  const double resident = (double)sms * (occ > 0 ? occ : 1);
-  int best_cz = 1;
-  double best_eff = -1.0;
-  for (int cz = 32; cz >= 1; cz /= 2) {
-    const int gz = (N + cz - 1) / cz;
-    const double waves = (double)gx * gy * gz / resident;
-    const double eff = waves / ceil(waves);
-    if (eff > best_eff + 0.02) {
-      best_eff = eff;
+  const long long resident = (long long)sms * (occ > 0 ? occ : 1);
+  int best_cz = 8;
+  double best_cost = 1e300;
+  for (int cz = 1; cz <= 64 && cz <= N; cz *= 2) {
+    const long long blocks = (long long)gx * gy * ((N + cz - 1) / cz);
+    const double cost = (double)((blocks + resident - 1) / resident) * (cz + 6.0);
+    if (cost < best_cost) {
+      best_cost = cost;
       best_cz = cz;
     }
   }
+  const char *env = getenv("PHN_ADJ_CZ");
+  if (env && atoi(env) > 0) best_cz = atoi(env);
   g.cz = best_cz;
   g.grid = dim3(gx, gy, (N + best_cz - 1) / best_cz);
   g.nblocks = gx * gy * g.grid.z;
