@@ -83,15 +83,36 @@ __device__ __forceinline__ T vpp(const Consts &k, T c) {
   return v;
 }
 
-// One reverse step.  phi1, pi1: state after the step; lphi, lpi: adjoints at
-// that time.  Writes phi0, pi0 (state before) and lphi0, lpi0 (adjoints
-// before).  Gradient slots: gs[block][j] += this step's coupling terms.
-//
-// A block is 32 x 8 sites marching `cz` planes.  The reconstructed field
-// phi = phi' - fd pi' and the adjoint mu = lam_pi + fd lam_phi of each site are
-// formed once, kept in registers along z and put in a shared-memory tile of
-// the current plane (with its one-site x/y halo, formed by the edge threads)
-// for the stencils.
+// Block-level sum of the two per-thread gradient partials into this
+// block's slot (fixed order: warp shuffles, then the warps in order).
+__device__ __forceinline__ void grad_slot_add(double g0, double g1, double *gs, int tid, int nwarps) {
+  __shared__ double sh[2][32];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    g0 += __shfl_down_sync(0xffffffffu, g0, off);
+    g1 += __shfl_down_sync(0xffffffffu, g1, off);
+  }
+  if ((tid & 31) == 0) {
+    sh[0][tid >> 5] = g0;
+    sh[1][tid >> 5] = g1;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double s0 = 0.0, s1 = 0.0;
+    for (int w = 0; w < nwarps; ++w) {
+      s0 += sh[0][w];
+      s1 += sh[1][w];
+    }
+    const size_t b = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
+    gs[b * ADJ_NG + 0] += s0;
+    gs[b * ADJ_NG + 1] += s1;
+  }
+}
+
+// One reverse step, one site per thread (any N; the FP64 path).
+// phi1, pi1: state after the step; lphi, lpi: adjoints at that time.  Writes
+// phi0, pi0 (state before) and lphi0, lpi0 (adjoints before).  Gradient slots:
+// gs[block][j] += this step's coupling terms.
 template <typename T>
 __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict__ phi1, const T *__restrict__ pi1,
                                                             const T *__restrict__ lphi, const T *__restrict__ lpi,
@@ -99,71 +120,33 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
                                                             T *__restrict__ lphi0, T *__restrict__ lpi0,
                                                             const Consts k, const T fk, const T fd, const int cz,
                                                             double *__restrict__ gs) {
-  __shared__ T sp[ADJ_TY + 2][ADJ_TX + 2], sm[ADJ_TY + 2][ADJ_TX + 2];
   const int N = k.N;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int x = blockIdx.x * ADJ_TX + tx, y = blockIdx.y * ADJ_TY + ty;
+  const int x = blockIdx.x * ADJ_TX + threadIdx.x, y = blockIdx.y * ADJ_TY + threadIdx.y;
   const int z0 = blockIdx.z * cz, z1 = min(z0 + cz, N);
   const size_t NN = (size_t)N * N;
-  const bool act = x < N && y < N;
-  // clamp inactive threads onto a valid site so that they can still fill halos
-  const int xs = act ? x : N - 1, ys = act ? y : N - 1;
-  const int xp = (xs + 1 == N) ? 0 : xs + 1, xm = (xs == 0) ? N - 1 : xs - 1;
-  const int yp = (ys + 1 == N) ? 0 : ys + 1, ym = (ys == 0) ? N - 1 : ys - 1;
-  const size_t col = (size_t)ys * N + xs;
-  auto rphi = [&](size_t i) { return AdjOps<T>::fma_(-fd, pi1[i], phi1[i]); };
-  auto rmu = [&](size_t i) { return AdjOps<T>::fma_(fd, lphi[i], lpi[i]); };
-  const T inv_a2 = (T)1 / (T)k.a2;
   KSum<T> k_c6, k_h;
-  const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
-  T pm = rphi((size_t)zm0 * NN + col), mm = rmu((size_t)zm0 * NN + col);
-  size_t ic = (size_t)z0 * NN + col;
-  T pc = rphi(ic), mc = rmu(ic), pic = pi1[ic], lphic = lphi[ic];
-  // edge threads own the halo sites of their row / column
-  const bool hx0 = tx == 0, hx1 = (tx == ADJ_TX - 1) || (x == N - 1);
-  const bool hy0 = ty == 0, hy1 = (ty == ADJ_TY - 1) || (y == N - 1);
-  for (int z = z0; z < z1; ++z) {
-    const size_t pl = (size_t)z * NN;
-    if (act) {  // only sites of the lattice write the tile (no slot has two writers)
-      sp[ty + 1][tx + 1] = pc;
-      sm[ty + 1][tx + 1] = mc;
-      if (hx0) {
-        const size_t j = pl + (size_t)ys * N + xm;
-        sp[ty + 1][0] = rphi(j);
-        sm[ty + 1][0] = rmu(j);
-      }
-      if (hx1) {
-        const size_t j = pl + (size_t)ys * N + xp;
-        sp[ty + 1][tx + 2] = rphi(j);
-        sm[ty + 1][tx + 2] = rmu(j);
-      }
-      if (hy0) {
-        const size_t j = pl + (size_t)ym * N + xs;
-        sp[0][tx + 1] = rphi(j);
-        sm[0][tx + 1] = rmu(j);
-      }
-      if (hy1) {
-        const size_t j = pl + (size_t)yp * N + xs;
-        sp[ty + 2][tx + 1] = rphi(j);
-        sm[ty + 2][tx + 1] = rmu(j);
-      }
-    }
-    // next plane of this column (also phi(z+1), mu(z+1) of the stencils)
-    const int zn = (z + 1 == N) ? 0 : z + 1;
-    const size_t in = (size_t)zn * NN + col;
-    const T pn = rphi(in), mn = rmu(in), pin = pi1[in], lphin = lphi[in];
-    __syncthreads();
-    if (act) {
-      const size_t i = pl + col;
-      const T dphi = (((sp[ty + 1][tx + 2] - pc) + (sp[ty + 1][tx] - pc)) +
-                      ((sp[ty + 2][tx + 1] - pc) + (sp[ty][tx + 1] - pc))) +
+  if (x < N && y < N && z0 < z1) {
+    const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
+    const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
+    const size_t col = (size_t)y * N + x;
+    auto rphi = [&](size_t i) { return AdjOps<T>::fma_(-fd, pi1[i], phi1[i]); };
+    auto rmu = [&](size_t i) { return AdjOps<T>::fma_(fd, lphi[i], lpi[i]); };
+    const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
+    T pm = rphi((size_t)zm0 * NN + col), pc = rphi((size_t)z0 * NN + col);
+    T mm = rmu((size_t)zm0 * NN + col), mc = rmu((size_t)z0 * NN + col);
+    const T inv_a2 = (T)1 / (T)k.a2;
+    for (int z = z0; z < z1; ++z) {
+      const int zn = (z + 1 == N) ? 0 : z + 1;
+      const size_t pl = (size_t)z * NN, i = pl + col;
+      const T pn = rphi((size_t)zn * NN + col), mn = rmu((size_t)zn * NN + col);
+      const size_t ixp = pl + (size_t)y * N + xp, ixm = pl + (size_t)y * N + xm;
+      const size_t iyp = pl + (size_t)yp * N + x, iym = pl + (size_t)ym * N + x;
+      const T dphi = (((rphi(ixp) - pc) + (rphi(ixm) - pc)) + ((rphi(iyp) - pc) + (rphi(iym) - pc))) +
                      ((pn - pc) + (pm - pc));
-      const T f = force<T>(k, dphi, pc);
-      const T pi_before = AdjOps<T>::fma_(-fk, f, pic);
-      const T dmu = (((sm[ty + 1][tx + 2] - mc) + (sm[ty + 1][tx] - mc)) +
-                     ((sm[ty + 2][tx + 1] - mc) + (sm[ty][tx + 1] - mc))) +
+      const T pi_before = AdjOps<T>::fma_(-fk, force<T>(k, dphi, pc), pi1[i]);
+      const T dmu = (((rmu(ixp) - mc) + (rmu(ixm) - mc)) + ((rmu(iyp) - mc) + (rmu(iym) - mc))) +
                     ((mn - mc) + (mm - mc));
-      const T lphi_before = AdjOps<T>::fma_(fk, dmu * inv_a2 - vpp<T>(k, pc) * mc, lphic);
+      const T lphi_before = AdjOps<T>::fma_(fk, dmu * inv_a2 - vpp<T>(k, pc) * mc, lphi[i]);
       phi0[i] = pc;
       pi0[i] = pi_before;
       lphi0[i] = lphi_before;
@@ -172,54 +155,119 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
       const T p2 = pc * pc;
       k_c6.add(fk * mc * ((T)-6 * (p2 * p2 * pc)));
       k_h.add(-fk * mc);
+      pm = pc;
+      pc = pn;
+      mm = mc;
+      mc = mn;
     }
-    __syncthreads();
-    pm = pc;
-    pc = pn;
-    mm = mc;
-    mc = mn;
-    pic = pin;
-    lphic = lphin;
   }
-  // block sums (fixed order) into this block's gradient slot
-  __shared__ double sh[2][ADJ_THREADS];
-  const int tid = tx + ADJ_TX * ty;
-  sh[0][tid] = k_c6.value();
-  sh[1][tid] = k_h.value();
-  __syncthreads();
-  for (int w = ADJ_THREADS / 2; w > 0; w >>= 1) {
-    if (tid < w) {
-      sh[0][tid] += sh[0][tid + w];
-      sh[1][tid] += sh[1][tid + w];
-    }
-    __syncthreads();
-  }
-  if (tid == 0) {
-    const size_t b = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
-    gs[b * ADJ_NG + 0] += sh[0][0];
-    gs[b * ADJ_NG + 1] += sh[1][0];
-  }
+  grad_slot_add(k_c6.value(), k_h.value(), gs, threadIdx.x + ADJ_TX * threadIdx.y, ADJ_THREADS / 32);
 }
 
-// Grid of the reverse kernel.  Cost model: whole waves of the resident
-// capacity times the planes a block handles plus its fixed overhead (the two
-// z-halo planes and the gradient reduction, about six planes' worth).
+// The same reverse step for FP32, four consecutive x-sites per thread
+// (N a multiple of 4): 16-byte loads and stores, x neighbours inside the
+// thread plus one scalar per side, y rows and z planes as float4.
+__device__ __forceinline__ float4 f4fma(float a, float4 b, float4 c) {
+  return make_float4(fmaf(a, b.x, c.x), fmaf(a, b.y, c.y), fmaf(a, b.z, c.z), fmaf(a, b.w, c.w));
+}
+__device__ __forceinline__ float f4get(const float4 &v, int e) {
+  return e == 0 ? v.x : (e == 1 ? v.y : (e == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ void f4set(float4 &v, int e, float x) {
+  if (e == 0) v.x = x;
+  else if (e == 1) v.y = x;
+  else if (e == 2) v.z = x;
+  else v.w = x;
+}
+
+__global__ void __launch_bounds__(ADJ_THREADS) adjoint_step_x4(const float *__restrict__ phi1,
+                                                               const float *__restrict__ pi1,
+                                                               const float *__restrict__ lphi,
+                                                               const float *__restrict__ lpi, float *__restrict__ phi0,
+                                                               float *__restrict__ pi0, float *__restrict__ lphi0,
+                                                               float *__restrict__ lpi0, const Consts k, const float fk,
+                                                               const float fd, const int cz, double *__restrict__ gs) {
+  const int N = k.N;
+  const int x0 = (blockIdx.x * ADJ_TX + threadIdx.x) * 4, y = blockIdx.y * ADJ_TY + threadIdx.y;
+  const int z0 = blockIdx.z * cz, z1 = min(z0 + cz, N);
+  const size_t NN = (size_t)N * N;
+  KSum<float> k_c6, k_h;
+  if (x0 < N && y < N && z0 < z1) {
+    const int xl = (x0 == 0) ? N - 1 : x0 - 1, xr = (x0 + 4 == N) ? 0 : x0 + 4;
+    const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
+    const size_t col = (size_t)y * N + x0;
+    auto ld4 = [&](const float *f, size_t i) { return *(const float4 *)(f + i); };
+    auto rphi4 = [&](size_t i) { return f4fma(-fd, ld4(pi1, i), ld4(phi1, i)); };
+    auto rmu4 = [&](size_t i) { return f4fma(fd, ld4(lphi, i), ld4(lpi, i)); };
+    auto rphi1 = [&](size_t i) { return fmaf(-fd, pi1[i], phi1[i]); };
+    auto rmu1 = [&](size_t i) { return fmaf(fd, lphi[i], lpi[i]); };
+    const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
+    float4 pm = rphi4((size_t)zm0 * NN + col), mm = rmu4((size_t)zm0 * NN + col);
+    size_t ic = (size_t)z0 * NN + col;
+    float4 pc = rphi4(ic), mc = rmu4(ic), pic = ld4(pi1, ic), lphic = ld4(lphi, ic);
+    const float inv_a2 = 1.f / (float)k.a2;
+    for (int z = z0; z < z1; ++z) {
+      const int zn = (z + 1 == N) ? 0 : z + 1;
+      const size_t pl = (size_t)z * NN, i = pl + col, in = (size_t)zn * NN + col;
+      const float4 pn = rphi4(in), mn = rmu4(in), pin = ld4(pi1, in), lphin = ld4(lphi, in);
+      const size_t iyp = pl + (size_t)yp * N + x0, iym = pl + (size_t)ym * N + x0;
+      const float4 pyp = rphi4(iyp), pym = rphi4(iym), myp = rmu4(iyp), mym = rmu4(iym);
+      const size_t ixl = pl + (size_t)y * N + xl, ixr = pl + (size_t)y * N + xr;
+      const float pxl = rphi1(ixl), pxr = rphi1(ixr), mxl = rmu1(ixl), mxr = rmu1(ixr);
+      float4 o_phi, o_pi, o_lphi;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float c = f4get(pc, e), m = f4get(mc, e);
+        const float cxm = e == 0 ? pxl : f4get(pc, e - 1), cxp = e == 3 ? pxr : f4get(pc, e + 1);
+        const float mxm = e == 0 ? mxl : f4get(mc, e - 1), mxp = e == 3 ? mxr : f4get(mc, e + 1);
+        const float dphi = (((cxp - c) + (cxm - c)) + ((f4get(pyp, e) - c) + (f4get(pym, e) - c))) +
+                           ((f4get(pn, e) - c) + (f4get(pm, e) - c));
+        const float dmu = (((mxp - m) + (mxm - m)) + ((f4get(myp, e) - m) + (f4get(mym, e) - m))) +
+                          ((f4get(mn, e) - m) + (f4get(mm, e) - m));
+        f4set(o_phi, e, c);
+        f4set(o_pi, e, fmaf(-fk, force<float>(k, dphi, c), f4get(pic, e)));
+        f4set(o_lphi, e, fmaf(fk, dmu * inv_a2 - vpp<float>(k, c) * m, f4get(lphic, e)));
+        const float c2 = c * c;
+        k_c6.add(fk * m * (-6.f * (c2 * c2 * c)));
+        k_h.add(-fk * m);
+      }
+      *(float4 *)(phi0 + i) = o_phi;
+      *(float4 *)(pi0 + i) = o_pi;
+      *(float4 *)(lphi0 + i) = o_lphi;
+      *(float4 *)(lpi0 + i) = mc;
+      pm = pc;
+      pc = pn;
+      mm = mc;
+      mc = mn;
+      pic = pin;
+      lphic = lphin;
+    }
+  }
+  grad_slot_add(k_c6.value(), k_h.value(), gs, threadIdx.x + ADJ_TX * threadIdx.y, ADJ_THREADS / 32);
+}
+
+// Grid of the reverse kernel (x4: a block covers 128 x-sites).  Cost model:
+// whole waves of the resident capacity times the planes a block handles
+// plus its fixed overhead (two z-halo planes, the gradient reduction).
 // PHN_ADJ_CZ overrides the planes per block (tuning).
-template <typename T>
-static Grid adjoint_grid(int N) {
+static Grid adjoint_grid(int N, bool x4) {
   Grid g;
   g.block = dim3(ADJ_TX, ADJ_TY, 1);
-  const int gx = (N + ADJ_TX - 1) / ADJ_TX, gy = (N + ADJ_TY - 1) / ADJ_TY;
+  const int xs = x4 ? 4 * ADJ_TX : ADJ_TX;
+  const int gx = (N + xs - 1) / xs, gy = (N + ADJ_TY - 1) / ADJ_TY;
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step<T>, ADJ_THREADS, 0);
+  if (x4)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step_x4, ADJ_THREADS, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step<double>, ADJ_THREADS, 0);
   const long long resident = (long long)sms * (occ > 0 ? occ : 1);
   int best_cz = 8;
   double best_cost = 1e300;
   for (int cz = 1; cz <= 64 && cz <= N; cz *= 2) {
     const long long blocks = (long long)gx * gy * ((N + cz - 1) / cz);
-    const double cost = (double)((blocks + resident - 1) / resident) * (cz + 6.0);
+    const double cost = (double)((blocks + resident - 1) / resident) * (cz + 2.0);
     if (cost < best_cost) {
       best_cost = cost;
       best_cz = cz;
@@ -439,7 +487,7 @@ int phn_adjoint_create(const phn_params *params, int nsteps, int every, double w
   if (e == cudaSuccess) e = cudaMalloc(&a->rho, a->V * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&a->g, a->V * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&a->sums, a->sum_blocks * sizeof(double));
-  const Grid gr = params->precision == PHN_FP64 ? adjoint_grid<double>(params->N) : adjoint_grid<float>(params->N);
+  const Grid gr = adjoint_grid(params->N, params->precision != PHN_FP64 && params->N % 4 == 0);
   if (e == cudaSuccess) e = cudaMalloc(&a->gs, (size_t)gr.nblocks * ADJ_NG * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreate(&a->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&a->ev1);
@@ -519,7 +567,8 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   cudaStream_t st = (cudaStream_t)stv;
   const size_t fb = a->V * a->elem;
   const bool dbl = a->elem == 8;
-  const Grid gr = dbl ? adjoint_grid<double>(a->p.N) : adjoint_grid<float>(a->p.N);
+  const bool x4 = !dbl && a->p.N % 4 == 0;
+  const Grid gr = adjoint_grid(a->p.N, x4);
   const int nb = a->sum_blocks;
   CKA(cudaEventRecord(a->ev0, st));
   gs_zero<<<64, 256, 0, st>>>(a->gs, (size_t)gr.nblocks * ADJ_NG);
@@ -552,6 +601,11 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
             (const double *)phi1, (const double *)pi1, (const double *)a->lphi[cur], (const double *)a->lpi[cur],
             (double *)phi0, (double *)pi0, (double *)a->lphi[1 - cur], (double *)a->lpi[1 - cur], a->k, a->fk[n],
             a->fd[n], gr.cz, a->gs);
+      else if (x4)
+        adjoint_step_x4<<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
+            (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
+            (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
+            (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
       else
         adjoint_step<float><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
             (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
