@@ -395,6 +395,9 @@ struct phn_adjoint {
   double J, mean, S;
   cudaEvent_t ev0, ev1;
   double fwd_ms, bwd_ms;
+  cudaGraphExec_t sweep;  // the captured reverse sweep
+  bool graph_ok;
+  int final_cur;          // buffer parity of the adjoint after the sweep
 };
 
 static void adj_free(phn_adjoint *a) {
@@ -413,6 +416,7 @@ static void adj_free(phn_adjoint *a) {
   cudaFree(a->gs);
   if (a->ev0) cudaEventDestroy(a->ev0);
   if (a->ev1) cudaEventDestroy(a->ev1);
+  if (a->graph_ok) cudaGraphExecDestroy(a->sweep);
   delete a;
 }
 
@@ -586,10 +590,15 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   obj_sum<<<nb, 256, 0, st>>>(a->rho, a->g, a->V, SUM_GPHI, 0.0, a->w, phi, dbl, a->sums);
   const double direct_h = host_sum(a, st);
   CKA(cudaEventRecord(a->ev0, st));  // backward timing starts after the seed
+  // The sweep's launches depend only on the handle's buffers and the clock
+  // factors (identical for every forward from reset()): they are captured
+  // once as a CUDA graph and replayed.
+  const bool capture = !a->graph_ok;
+  if (capture) CKA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   int cur = 0;  // lphi[cur], lpi[cur] hold the adjoint
   char *ck = (char *)a->ckpt;
   int sbuf = 0;
-  for (int s = a->nseg - 1; s >= 0; --s) {
+  for (int s = a->nseg - 1; s >= 0 && (capture || !a->graph_ok); --s) {
     // re-anchor: the segment's end state is its checkpoint
     const void *phi1 = ck + (size_t)(s + 1) * 2 * fb;
     const void *pi1 = ck + (size_t)(s + 1) * 2 * fb + fb;
@@ -612,13 +621,24 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
             (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
             (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
       CKA(cudaGetLastError());
-      h->launches++;
       cur = 1 - cur;
       phi1 = phi0;
       pi1 = pi0;
       sbuf = 1 - sbuf;
     }
   }
+  if (capture) {
+    cudaGraph_t g;
+    CKA(cudaStreamEndCapture(st, &g));
+    const cudaError_t ie = cudaGraphInstantiate(&a->sweep, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return cuda_error(ie, "cudaGraphInstantiate (reverse sweep)");
+    a->graph_ok = true;
+    a->final_cur = cur;
+  }
+  CKA(cudaGraphLaunch(a->sweep, st));
+  h->launches += a->nsteps;
+  cur = a->final_cur;
   CKA(cudaEventRecord(a->ev1, st));
   CKA(cudaEventSynchronize(a->ev1));
   float ms = 0.f;
