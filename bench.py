@@ -443,13 +443,16 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
         one = np.ones_like(phi)
         fd_phi0 = (adj.forward(phi + h_s * one, pi) - adj.forward(phi - h_s * one, pi)) / (2 * h_s)
     c6 = 1.0 / (720 * kappa ** 2)
-    Jc = []
-    h_c = 1e-6
-    for d in (+1, -1):
-        c = c6 * (1 + d * h_c)
-        with PL.Adjoint(PL.Params(N=N, precision=0, kappa=(1.0 / (720 * c)) ** 0.5), steps, every) as adj:
-            Jc.append(adj.forward(phi, pi))
-    fd_c6 = (Jc[0] - Jc[1]) / (2 * h_c * c6)
+    fd_c6_by_step = {}
+    for h_c in (1e-4, 1e-5, 1e-6, 1e-7):
+        Jc = []
+        for d in (+1, -1):
+            c = c6 * (1 + d * h_c)
+            with PL.Adjoint(PL.Params(N=N, precision=0, kappa=(1.0 / (720 * c)) ** 0.5), steps, every) as adj:
+                Jc.append(adj.forward(phi, pi))
+        fd_c6_by_step[str(h_c)] = (Jc[0] - Jc[1]) / (2 * h_c * c6)
+    fd_c6 = fd_c6_by_step["1e-06"]
+    out["dc6_fd_by_relative_step"] = fd_c6_by_step
     out["fd_directions"] = ndir
     out["fd_step"] = h_fd
     out["fp64_adjoint_vs_fd_rel_max"] = float(max(errs64))
