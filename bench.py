@@ -391,7 +391,8 @@ def precision_form(N: int, steps: int, check_step: int = 500, tso_steps: int = 5
             "results": res}
 
 
-def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: float = 1e-3):
+def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: float = 1e-3,
+                 c6_steps=(1e-4, 1e-5, 1e-6, 1e-7)):
     """Adjoint form (config C4): phi^6, N^3, FP32, `steps` steps, checkpoints
     every `every`; J = sum rho sigmoid((rho - 2<rho>)/0.1) of the final state.
     Gradients w.r.t. the initial phi field, its homogeneous part phi0 and the
@@ -402,22 +403,36 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     phi, pi = make_fields(N)
     sl = slice(N * N, -N * N)
     kappa = 3 ** 0.5
-    # plain forward solve: the production step kernel, same steps
+    # plain forward solve: the production step kernel, same steps; one warm-up
+    # solve, then the median of `reps` timed solves (device events)
+    reps = 5
     lat = PL.Lattice(PL.Params(N=N, precision=1, kappa=kappa))
-    lat.upload(phi, pi)
-    lat.evolve(steps)
-    _, fwd_plain_ms, _ = lat.stats()
+    plain = []
+    for r in range(reps + 1):
+        lat.upload(phi, pi)
+        lat.evolve(steps)
+        if r:
+            plain.append(lat.stats()[1])
     lat.close()
+    fwd_plain_ms = float(np.median(plain))
     out = {"form": "adjoint", "N": N, "steps": steps, "every": every, "width": 0.1}
     res = {}
     for name, prec in (("fp32", 1), ("fp64", 0)):
         with PL.Adjoint(PL.Params(N=N, precision=prec, kappa=kappa), steps, every) as adj:
-            adj.forward(phi, pi)
-            dphi, dpi, g = adj.backward()
-            J, fms, bms = adj.info()
-        res[name] = {"J": J, "dphi": dphi, "g": g, "forward_ms": fms, "backward_ms": bms}
+            fl, bl = [], []
+            for r in range(reps + 1 if name == "fp32" else 1):
+                adj.forward(phi, pi)
+                dphi, dpi, g = adj.backward()
+                J, fms, bms = adj.info()
+                fl.append(fms)
+                bl.append(bms)
+            if len(fl) > 1:  # drop the warm-up pair
+                fl, bl = fl[1:], bl[1:]
+        res[name] = {"J": J, "dphi": dphi, "g": g, "forward_ms": float(np.median(fl)),
+                     "backward_ms": float(np.median(bl))}
     d32, d64 = res["fp32"]["dphi"][sl], res["fp64"]["dphi"][sl]
     out["J_fp32"], out["J_fp64"] = res["fp32"]["J"], res["fp64"]["J"]
+    out["timing"] = f"device events; median of {reps} solves after one warm-up solve"
     out["cost_ratio"] = (res["fp32"]["forward_ms"] + res["fp32"]["backward_ms"]) / fwd_plain_ms
     out["forward_plain_ms"] = fwd_plain_ms
     out["adjoint_forward_ms"] = res["fp32"]["forward_ms"]
@@ -444,14 +459,16 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
         fd_phi0 = (adj.forward(phi + h_s * one, pi) - adj.forward(phi - h_s * one, pi)) / (2 * h_s)
     c6 = 1.0 / (720 * kappa ** 2)
     fd_c6_by_step = {}
-    for h_c in (1e-4, 1e-5, 1e-6, 1e-7):
+    for h_c in c6_steps:
         Jc = []
         for d in (+1, -1):
             c = c6 * (1 + d * h_c)
             with PL.Adjoint(PL.Params(N=N, precision=0, kappa=(1.0 / (720 * c)) ** 0.5), steps, every) as adj:
                 Jc.append(adj.forward(phi, pi))
         fd_c6_by_step[str(h_c)] = (Jc[0] - Jc[1]) / (2 * h_c * c6)
-    fd_c6 = fd_c6_by_step["1e-06"]
+    # the central difference in c6 converges once the step is small
+    # (1e-4 and 1e-5 sit in the curvature of the sigmoid objective)
+    fd_c6 = fd_c6_by_step[str(c6_steps[-1])]
     out["dc6_fd_by_relative_step"] = fd_c6_by_step
     out["fd_directions"] = ndir
     out["fd_step"] = h_fd
@@ -510,7 +527,8 @@ def main():
         print(json.dumps(precision_form(args.n, max(args.steps, 500))))
         return
     if args.form == "adjoint":
-        print(json.dumps(adjoint_form(args.n, args.steps)))
+        kw = dict(ndir=2, c6_steps=(1e-7,)) if args.quick else {}
+        print(json.dumps(adjoint_form(args.n, args.steps, **kw)))
         return
 
     if args.impl == "reference":
