@@ -392,9 +392,12 @@ def precision_form(N: int, steps: int, check_step: int = 500, tso_steps: int = 5
 
 
 def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: float = 1e-3,
-                 c6_steps=(1e-4, 1e-5, 1e-6, 1e-7)):
+                 c6_steps=(1e-4, 1e-5, 1e-6, 1e-7), width_cfg: float = 0.1):
     """Adjoint form (config C4): phi^6, N^3, FP32, `steps` steps, checkpoints
-    every `every`; J = sum rho sigmoid((rho - 2<rho>)/0.1) of the final state.
+    every `every`; J = sum rho sigmoid((rho - 2<rho>)/0.1) of the final state,
+    in the configuration's units.  The kernels work in the reference's units
+    (Phi = sqrt(6) phi, so rho_ref = 6 rho): the same objective is
+    J_ref = sum rho_ref sigmoid((rho_ref - 2<rho_ref>)/0.6) = 6 J.
     Gradients w.r.t. the initial phi field, its homogeneous part phi0 and the
     phi^6 coupling, checked against the FP64 adjoint and against central
     finite differences of the FP64 forward (step h_fd) on `ndir` random unit
@@ -403,40 +406,45 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     phi, pi = make_fields(N)
     sl = slice(N * N, -N * N)
     kappa = 3 ** 0.5
-    # plain forward solve: the production step kernel, same steps; one warm-up
-    # solve, then the median of `reps` timed solves (device events)
-    reps = 5
-    lat = PL.Lattice(PL.Params(N=N, precision=1, kappa=kappa))
-    plain = []
-    for r in range(reps + 1):
-        lat.upload(phi, pi)
-        lat.evolve(steps)
-        if r:
-            plain.append(lat.stats()[1])
-    lat.close()
-    fwd_plain_ms = float(np.median(plain))
-    out = {"form": "adjoint", "N": N, "steps": steps, "every": every, "width": 0.1}
+    # plain forward solves (the production step kernels, same steps) and the
+    # adjoint pair, FP32 and FP64: one warm-up solve, then the median of
+    # `reps` timed solves (device events)
+    width = 6 * width_cfg  # the configuration's width in the reference's energy units
+    out = {"form": "adjoint", "N": N, "steps": steps, "every": every, "width_config_units": width_cfg,
+           "width_reference_units": width}
     res = {}
-    for name, prec in (("fp32", 1), ("fp64", 0)):
-        with PL.Adjoint(PL.Params(N=N, precision=prec, kappa=kappa), steps, every) as adj:
+    for name, prec, reps in (("fp32", 1, 5), ("fp64", 0, 2)):
+        lat = PL.Lattice(PL.Params(N=N, precision=prec, kappa=kappa))
+        plain = []
+        for r in range(reps + 1):
+            lat.upload(phi, pi)
+            lat.evolve(steps)
+            if r:
+                plain.append(lat.stats()[1])
+        lat.close()
+        with PL.Adjoint(PL.Params(N=N, precision=prec, kappa=kappa), steps, every, width) as adj:
             fl, bl = [], []
-            for r in range(reps + 1 if name == "fp32" else 1):
+            for r in range(reps + 1):
                 adj.forward(phi, pi)
                 dphi, dpi, g = adj.backward()
                 J, fms, bms = adj.info()
-                fl.append(fms)
-                bl.append(bms)
-            if len(fl) > 1:  # drop the warm-up pair
-                fl, bl = fl[1:], bl[1:]
-        res[name] = {"J": J, "dphi": dphi, "g": g, "forward_ms": float(np.median(fl)),
-                     "backward_ms": float(np.median(bl))}
+                if r:
+                    fl.append(fms)
+                    bl.append(bms)
+        res[name] = {"J": J, "dphi": dphi, "g": g, "plain_ms": float(np.median(plain)),
+                     "forward_ms": float(np.median(fl)), "backward_ms": float(np.median(bl))}
     d32, d64 = res["fp32"]["dphi"][sl], res["fp64"]["dphi"][sl]
     out["J_fp32"], out["J_fp64"] = res["fp32"]["J"], res["fp64"]["J"]
-    out["timing"] = f"device events; median of {reps} solves after one warm-up solve"
-    out["cost_ratio"] = (res["fp32"]["forward_ms"] + res["fp32"]["backward_ms"]) / fwd_plain_ms
-    out["forward_plain_ms"] = fwd_plain_ms
-    out["adjoint_forward_ms"] = res["fp32"]["forward_ms"]
-    out["adjoint_backward_ms"] = res["fp32"]["backward_ms"]
+    out["timing"] = ("device events; median of 5 (FP32) / 2 (FP64) solves after one warm-up solve; "
+                     "adjoint = forward with checkpoints and J + backward (seed and reverse sweep)")
+    r32, r64 = res["fp32"], res["fp64"]
+    out["cost_ratio"] = (r32["forward_ms"] + r32["backward_ms"]) / r32["plain_ms"]
+    out["forward_plain_ms"] = r32["plain_ms"]
+    out["adjoint_forward_ms"] = r32["forward_ms"]
+    out["adjoint_backward_ms"] = r32["backward_ms"]
+    out["fp64"] = {"cost_ratio": (r64["forward_ms"] + r64["backward_ms"]) / r64["plain_ms"],
+                   "forward_plain_ms": r64["plain_ms"], "adjoint_forward_ms": r64["forward_ms"],
+                   "adjoint_backward_ms": r64["backward_ms"]}
     out["fp32_vs_fp64_field_rel_l2"] = float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64))
     g32, g64 = res["fp32"]["g"], res["fp64"]["g"]
     out["fp32_vs_fp64_dphi0_rel"] = float(abs(g32[0] - g64[0]) / abs(g64[0]))
@@ -444,7 +452,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     # central finite differences of the FP64 forward
     rng = np.random.default_rng(99)
     errs64, errs32 = [], []
-    with PL.Adjoint(PL.Params(N=N, precision=0, kappa=kappa), steps, every) as adj:
+    with PL.Adjoint(PL.Params(N=N, precision=0, kappa=kappa), steps, every, width) as adj:
         for _ in range(ndir):
             v = np.zeros_like(phi)
             v[sl] = rng.standard_normal(N ** 3)
@@ -463,7 +471,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
         Jc = []
         for d in (+1, -1):
             c = c6 * (1 + d * h_c)
-            with PL.Adjoint(PL.Params(N=N, precision=0, kappa=(1.0 / (720 * c)) ** 0.5), steps, every) as adj:
+            with PL.Adjoint(PL.Params(N=N, precision=0, kappa=(1.0 / (720 * c)) ** 0.5), steps, every, width) as adj:
                 Jc.append(adj.forward(phi, pi))
         fd_c6_by_step[str(h_c)] = (Jc[0] - Jc[1]) / (2 * h_c * c6)
     # the central difference in c6 converges once the step is small
@@ -477,8 +485,9 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     out["fp32_adjoint_vs_fd_rel_median"] = float(np.median(errs32))
     out["dphi0"] = {"fp32": float(g32[0]), "fp64": float(g64[0]), "fd": fd_phi0}
     out["dc6"] = {"fp32": float(g32[1]), "fp64": float(g64[1]), "fd": fd_c6}
-    # the configuration's units: phi_ref = sqrt(6) phi, c6 = g / 216
-    out["config_units"] = {"dJ_dphi0": float(g32[0]) * 6 ** 0.5, "dJ_dg": float(g32[1]) / 216.0}
+    # the configuration's units: J = J_ref / 6, phi_ref = sqrt(6) phi, c6 = g / 216
+    out["config_units"] = {"J": out["J_fp32"] / 6, "dJ_dphi0": float(g32[0]) * 6 ** 0.5 / 6,
+                           "dJ_dg": float(g32[1]) / 216.0 / 6}
     return out
 
 

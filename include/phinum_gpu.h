@@ -213,7 +213,9 @@ int phn_ensemble_stats(const phn_ensemble *e, long long *kernel_launches, double
 /* ---- Adjoint ---------------------------------------------------------------
  * No counterpart in the reference (it has no derivatives).  Objective on the
  * final state: J = sum_x rho(x) sigmoid((rho(x) - 2 <rho>) / width), rho the
- * energy density (the summand of the reference's Energy).  Forward: the same
+ * energy density (the summand of the reference's Energy), so width is in the
+ * reference's energy units (Phi = sqrt(6) phi makes them 6x the units of the
+ * phi^2/2 - phi^4/4 + g phi^6/6 form: its width 0.1 is 0.6 here).  Forward: the same
  * step kernels as phn_evolve, checkpoints every `every` steps.  Backward: the
  * discrete adjoint of the implemented leapfrog, reverse time stepping that
  * restarts from each checkpoint (finite-precision reversal drifts).

@@ -282,14 +282,57 @@ static Grid adjoint_grid(int N, bool x4) {
 }
 
 // ---------------------------------------------------------------- objective
+// J = sum_x rho(x) s(x), s = sigmoid((rho(x) - 2 <rho>) / w), and its seed
+// g = dJ/drho, in three passes with FP64 per-site terms.  Each pass leaves one
+// sum per block in part[]; the next pass folds those on the device in a fixed
+// order (the same in every block), so nothing returns to the host until J is
+// read back and the result is identical run to run.
+constexpr int OBJ_THREADS = 256;
+
 __device__ __forceinline__ double sigmoid(double u) { return 1.0 / (1.0 + exp(-u)); }
 
-// rho(x), FP64, from T fields (the reference's per-site Energy summand).
+// Fixed-order block sum of one value per thread; the result is valid in
+// thread 0.  Every thread of the block calls it.
+__device__ double obj_block_sum(double v) {
+  __shared__ double sh[OBJ_THREADS / 32];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < OBJ_THREADS / 32; ++w) s += sh[w];
+  __syncthreads();
+  return s;
+}
+
+// Sum of part[0..n): lane l adds part[l], part[l+32], ... in sequence, then a
+// butterfly; the same bits in every block.  Every thread of the block calls it.
+__device__ double obj_fold(const double *part, int n) {
+  __shared__ double r;
+  if (threadIdx.x < 32) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) s += part[i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (threadIdx.x == 0) r = s;
+  }
+  __syncthreads();
+  const double v = r;
+  __syncthreads();
+  return v;
+}
+
+// Pass 1: rho(x) from T fields (the summand of the reference's Energy:
+// pi^2/2 + forward-difference gradient energy + V) and block sums of rho.
 template <typename T>
-__global__ void obj_rho(const T *__restrict__ phi, const T *__restrict__ pi, const Consts k,
-                        double *__restrict__ rho) {
+__global__ void __launch_bounds__(OBJ_THREADS) obj_rho(const T *__restrict__ phi, const T *__restrict__ pi,
+                                                       const Consts k, double *__restrict__ rho,
+                                                       double *__restrict__ part) {
   const int N = k.N;
   const size_t NN = (size_t)N * N, V = NN * N;
+  const double ia2 = 1.0 / k.a2, i24 = 1.0 / k.c24, i720 = 1.0 / k.c720;
+  double acc = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
     const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
     const double c = phi[i], p = pi[i];
@@ -297,59 +340,74 @@ __global__ void obj_rho(const T *__restrict__ phi, const T *__restrict__ pi, con
     const double fy = phi[(size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x];
     const double fz = phi[(size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x];
     const double c2 = c * c, c4 = c2 * c2;
-    const double grad = ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) / k.a2;
-    double v = k.mm_half_M * c2 + k.lm * (c4 / k.c24);
-    if (k.theory == 0) v += c4 * c2 / k.c720;
+    const double grad = ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) * ia2;
+    double v = k.mm_half_M * c2 + k.lm * (c4 * i24);
+    if (k.theory == 0) v += c4 * c2 * i720;
     if (k.theory == 1) v += k.h * c;
-    rho[i] = 0.5 * p * p + 0.5 * grad + v;
+    const double r = 0.5 * p * p + 0.5 * grad + v;
+    rho[i] = r;
+    acc += r;
+  }
+  const double s = obj_block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// Pass 2: <rho> from pass 1; s(x) into sg; block sums of rho s (J) and of
+// rho s (1 - s) (S, the seed's coupling through the mean).
+__global__ void __launch_bounds__(OBJ_THREADS) obj_sigmoid(const double *__restrict__ rho, size_t V, double w,
+                                                           double *__restrict__ sg, double *__restrict__ part,
+                                                           int nb) {
+  const double mean = obj_fold(part, nb) / (double)V;
+  const double iw = 1.0 / w;
+  double aj = 0.0, as = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    const double r = rho[i], s = sigmoid((r - 2.0 * mean) * iw);
+    sg[i] = s;
+    aj += r * s;
+    as += r * s * (1.0 - s);
+  }
+  const double sj = obj_block_sum(aj), ss = obj_block_sum(as);
+  if (threadIdx.x == 0) {
+    part[nb + blockIdx.x] = sj;
+    part[2 * nb + blockIdx.x] = ss;
   }
 }
 
-// Block sums of a per-site expression into out[block] (one value per block).
-enum { SUM_RHO = 0, SUM_J = 1, SUM_S = 2, SUM_GPHI6 = 3, SUM_GPHI = 4 };
-__global__ void obj_sum(const double *__restrict__ rho, const double *__restrict__ gseed, size_t V, int what,
-                        double mean, double w, const void *__restrict__ phi, int phi_is_double,
-                        double *__restrict__ out) {
-  __shared__ double sh[256];
-  double s = 0.0;
+// Pass 3: g(x) = dJ/drho(x) = s + rho s (1 - s) / w - 2 S / (w V), written
+// over s; block 0 stores <rho>, J, S in res[0..2].
+__global__ void __launch_bounds__(OBJ_THREADS) obj_seed(const double *__restrict__ rho, size_t V, double w,
+                                                        double *__restrict__ g, const double *__restrict__ part,
+                                                        int nb, double *__restrict__ res) {
+  const double S = obj_fold(part + 2 * nb, nb);
+  const double iw = 1.0 / w, corr = -2.0 * S * iw / (double)V;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    const double r = rho[i];
-    if (what == SUM_RHO) {
-      s += r;
-    } else if (what == SUM_J || what == SUM_S) {
-      const double u = (r - 2.0 * mean) / w, sg = sigmoid(u);
-      s += what == SUM_J ? r * sg : r * sg * (1.0 - sg);
-    } else {
-      const double c = phi_is_double ? ((const double *)phi)[i] : (double)((const float *)phi)[i];
-      const double c2 = c * c;
-      s += what == SUM_GPHI6 ? gseed[i] * c2 * c2 * c2 : gseed[i] * c;
+    const double r = rho[i], s = g[i];
+    g[i] = s + r * s * (1.0 - s) * iw + corr;
+  }
+  if (blockIdx.x == 0) {
+    const double sr = obj_fold(part, nb), sj = obj_fold(part + nb, nb);
+    if (threadIdx.x == 0) {
+      res[0] = sr / (double)V;
+      res[1] = sj;
+      res[2] = S;
     }
   }
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
 }
 
-// g(x) = dJ/drho(x)
-__global__ void obj_seed(const double *__restrict__ rho, size_t V, double mean, double S, double w,
-                         double *__restrict__ g) {
-  const double corr = -2.0 * S / (w * (double)V);
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    const double r = rho[i], sg = sigmoid((r - 2.0 * mean) / w);
-    g[i] = sg + r * sg * (1.0 - sg) / w + corr;
-  }
-}
-
-// lam_pi = g pi ; lam_phi = g (-sum_d (phi(x+d)-phi(x))/a^2 + V'(phi)) + sum_d g(x-d) (phi(x)-phi(x-d))/a^2
+// Adjoint of J at the final state (lam = dJ/d(phi, pi)):
+//   lam_pi = g pi
+//   lam_phi = g (-sum_d (phi(x+d) - phi(x)) / a^2 + V'(phi)) + sum_d g(x-d) (phi(x) - phi(x-d)) / a^2
+// and, in the same pass, block sums of the direct coupling terms
+// dJ/dc6 = sum g phi^6 and dJ/dh = sum g phi into part[0..nb), part[nb..2nb).
 template <typename T>
-__global__ void obj_adjoint_init(const T *__restrict__ phi, const T *__restrict__ pi, const double *__restrict__ g,
-                                 const Consts k, T *__restrict__ lphi, T *__restrict__ lpi) {
+__global__ void __launch_bounds__(OBJ_THREADS) obj_adjoint_init(const T *__restrict__ phi, const T *__restrict__ pi,
+                                                                const double *__restrict__ g, const Consts k,
+                                                                T *__restrict__ lphi, T *__restrict__ lpi,
+                                                                double *__restrict__ part, int nb) {
   const int N = k.N;
   const size_t NN = (size_t)N * N, V = NN * N;
+  const double ia2 = 1.0 / k.a2, i720 = 1.0 / k.c720, l6 = k.lm * (24.0 / k.c24) / 6.0;
+  double a6 = 0.0, ah = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
     const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
     const size_t ixp = i - x + (x + 1 == N ? 0 : x + 1), ixm = i - x + (x == 0 ? N - 1 : x - 1);
@@ -357,16 +415,23 @@ __global__ void obj_adjoint_init(const T *__restrict__ phi, const T *__restrict_
     const size_t iym = (size_t)z * NN + (size_t)(y == 0 ? N - 1 : y - 1) * N + x;
     const size_t izp = (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x;
     const size_t izm = (size_t)(z == 0 ? N - 1 : z - 1) * NN + (size_t)y * N + x;
-    const double c = phi[i];
+    const double c = phi[i], gi = g[i];
     const double fwd = ((double)phi[ixp] - c) + ((double)phi[iyp] - c) + ((double)phi[izp] - c);
     const double bwd = g[ixm] * (c - (double)phi[ixm]) + g[iym] * (c - (double)phi[iym]) +
                        g[izm] * (c - (double)phi[izm]);
     const double c2 = c * c;
-    double vp = 2.0 * k.mm_half_M * c + k.lm * c2 * c / 6.0 * (24.0 / k.c24);
-    if (k.theory == 0) vp += 6.0 * c2 * c2 * c / k.c720;
+    double vp = 2.0 * k.mm_half_M * c + l6 * c2 * c;
+    if (k.theory == 0) vp += 6.0 * c2 * c2 * c * i720;
     if (k.theory == 1) vp += k.h;
-    lphi[i] = (T)(g[i] * (-fwd / k.a2 + vp) + bwd / k.a2);
-    lpi[i] = (T)(g[i] * (double)pi[i]);
+    lphi[i] = (T)(gi * (-fwd * ia2 + vp) + bwd * ia2);
+    lpi[i] = (T)(gi * (double)pi[i]);
+    a6 += gi * (c2 * c2 * c2);
+    ah += gi * c;
+  }
+  const double s6 = obj_block_sum(a6), sh = obj_block_sum(ah);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s6;
+    part[nb + blockIdx.x] = sh;
   }
 }
 
@@ -387,7 +452,9 @@ struct phn_adjoint {
   phn_handle *fwd;
   void *ckpt;              // (nseg + 1) x {phi, pi}
   void *rphi[2], *rpi[2], *lphi[2], *lpi[2];
-  double *rho, *g, *sums;  // per-site FP64 scratch, block sums
+  double *rho, *g;         // per-site FP64 scratch: rho, then s / the seed g
+  double *sums;            // block sums [3][sum_blocks] + 4 results (<rho>, J, S)
+  double *h_res;           // pinned host copy of the results
   double *gs;              // gradient slots [blocks][ADJ_NG]
   int sum_blocks;
   std::vector<double> fk, fd;  // clock factors of each forward step
@@ -413,6 +480,7 @@ static void adj_free(phn_adjoint *a) {
   cudaFree(a->rho);
   cudaFree(a->g);
   cudaFree(a->sums);
+  if (a->h_res) cudaFreeHost(a->h_res);
   cudaFree(a->gs);
   if (a->ev0) cudaEventDestroy(a->ev0);
   if (a->ev1) cudaEventDestroy(a->ev1);
@@ -426,32 +494,17 @@ static void adj_free(phn_adjoint *a) {
     if (e_ != cudaSuccess) return cuda_error(e_, #call); \
   } while (0)
 
-static double host_sum(phn_adjoint *a, cudaStream_t st) {
-  std::vector<double> h(a->sum_blocks);
-  cudaMemcpyAsync(h.data(), a->sums, a->sum_blocks * sizeof(double), cudaMemcpyDeviceToHost, st);
-  cudaStreamSynchronize(st);
-  double s = 0.0;
-  for (double v : h) s += v;  // fixed order
-  return s;
-}
-
-// J and its seed on the current forward state (phi, pi device pointers).
+// J and its seed g on the current forward state (phi, pi device pointers);
+// <rho>, J, S are copied to the pinned h_res (read after the stream syncs).
 template <typename T>
-static int objective(phn_adjoint *a, const T *phi, const T *pi, bool seed, cudaStream_t st) {
+static int objective(phn_adjoint *a, const T *phi, const T *pi, cudaStream_t st) {
   const int nb = a->sum_blocks;
-  obj_rho<T><<<nb, 256, 0, st>>>(phi, pi, a->k, a->rho);
-  obj_sum<<<nb, 256, 0, st>>>(a->rho, nullptr, a->V, SUM_RHO, 0.0, a->w, nullptr, 0, a->sums);
+  double *res = a->sums + 3 * nb;
+  obj_rho<T><<<nb, OBJ_THREADS, 0, st>>>(phi, pi, a->k, a->rho, a->sums);
+  obj_sigmoid<<<nb, OBJ_THREADS, 0, st>>>(a->rho, a->V, a->w, a->g, a->sums, nb);
+  obj_seed<<<nb, OBJ_THREADS, 0, st>>>(a->rho, a->V, a->w, a->g, a->sums, nb, res);
   CKA(cudaGetLastError());
-  a->mean = host_sum(a, st) / (double)a->V;
-  obj_sum<<<nb, 256, 0, st>>>(a->rho, nullptr, a->V, SUM_J, a->mean, a->w, nullptr, 0, a->sums);
-  CKA(cudaGetLastError());
-  a->J = host_sum(a, st);
-  if (!seed) return PHN_OK;
-  obj_sum<<<nb, 256, 0, st>>>(a->rho, nullptr, a->V, SUM_S, a->mean, a->w, nullptr, 0, a->sums);
-  CKA(cudaGetLastError());
-  a->S = host_sum(a, st);
-  obj_seed<<<nb, 256, 0, st>>>(a->rho, a->V, a->mean, a->S, a->w, a->g);
-  CKA(cudaGetLastError());
+  CKA(cudaMemcpyAsync(a->h_res, res, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
   return PHN_OK;
 }
 
@@ -490,7 +543,8 @@ int phn_adjoint_create(const phn_params *params, int nsteps, int every, double w
   a->sum_blocks = 152 * 4;
   if (e == cudaSuccess) e = cudaMalloc(&a->rho, a->V * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&a->g, a->V * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&a->sums, a->sum_blocks * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&a->sums, (3 * (size_t)a->sum_blocks + 4) * sizeof(double));
+  if (e == cudaSuccess) e = cudaHostAlloc((void **)&a->h_res, 4 * sizeof(double), cudaHostAllocDefault);
   const Grid gr = adjoint_grid(params->N, params->precision != PHN_FP64 && params->N % 4 == 0);
   if (e == cudaSuccess) e = cudaMalloc(&a->gs, (size_t)gr.nblocks * ADJ_NG * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreate(&a->ev0);
@@ -545,15 +599,18 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
     CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb + fb, pi, fb, cudaMemcpyDeviceToDevice, st));
   }
   if (a->elem == 8)
-    r = objective<double>(a, (const double *)phi, (const double *)pi, true, st);
+    r = objective<double>(a, (const double *)phi, (const double *)pi, st);
   else
-    r = objective<float>(a, (const float *)phi, (const float *)pi, true, st);
+    r = objective<float>(a, (const float *)phi, (const float *)pi, st);
   if (r) return r;
   CKA(cudaEventRecord(a->ev1, st));
   CKA(cudaEventSynchronize(a->ev1));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, a->ev0, a->ev1);
   a->fwd_ms = ms;
+  a->mean = a->h_res[0];
+  a->J = a->h_res[1];
+  a->S = a->h_res[2];
   a->forward_done = true;
   if (J) *J = a->J;
   return PHN_OK;
@@ -574,90 +631,92 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   const bool x4 = !dbl && a->p.N % 4 == 0;
   const Grid gr = adjoint_grid(a->p.N, x4);
   const int nb = a->sum_blocks;
-  CKA(cudaEventRecord(a->ev0, st));
-  gs_zero<<<64, 256, 0, st>>>(a->gs, (size_t)gr.nblocks * ADJ_NG);
-  // adjoint of the objective at the final state
-  if (dbl)
-    obj_adjoint_init<double><<<nb, 256, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
-                                                 (double *)a->lphi[0], (double *)a->lpi[0]);
-  else
-    obj_adjoint_init<float><<<nb, 256, 0, st>>>((const float *)phi, (const float *)pi, a->g, a->k,
-                                                (float *)a->lphi[0], (float *)a->lpi[0]);
-  CKA(cudaGetLastError());
-  // direct dependence of rho on the couplings
-  obj_sum<<<nb, 256, 0, st>>>(a->rho, a->g, a->V, SUM_GPHI6, 0.0, a->w, phi, dbl, a->sums);
-  const double direct_c6 = host_sum(a, st);
-  obj_sum<<<nb, 256, 0, st>>>(a->rho, a->g, a->V, SUM_GPHI, 0.0, a->w, phi, dbl, a->sums);
-  const double direct_h = host_sum(a, st);
   // The sweep's launches depend only on the handle's buffers and the clock
   // factors (identical for every forward from reset()): they are captured
-  // once as a CUDA graph and replayed.
-  const bool capture = !a->graph_ok;
-  if (capture) CKA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  int cur = 0;  // lphi[cur], lpi[cur] hold the adjoint
-  char *ck = (char *)a->ckpt;
-  int sbuf = 0;
-  for (int s = a->nseg - 1; s >= 0 && (capture || !a->graph_ok); --s) {
-    // re-anchor: the segment's end state is its checkpoint
-    const void *phi1 = ck + (size_t)(s + 1) * 2 * fb;
-    const void *pi1 = ck + (size_t)(s + 1) * 2 * fb + fb;
-    for (int i = a->every - 1; i >= 0; --i) {
-      const int n = s * a->every + i;
-      void *phi0 = a->rphi[sbuf], *pi0 = a->rpi[sbuf];
-      if (dbl)
-        adjoint_step<double><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
-            (const double *)phi1, (const double *)pi1, (const double *)a->lphi[cur], (const double *)a->lpi[cur],
-            (double *)phi0, (double *)pi0, (double *)a->lphi[1 - cur], (double *)a->lpi[1 - cur], a->k, a->fk[n],
-            a->fd[n], gr.cz, a->gs);
-      else if (x4)
-        adjoint_step_x4<<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
-            (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
-            (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
-            (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
-      else
-        adjoint_step<float><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
-            (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
-            (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
-            (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
-      CKA(cudaGetLastError());
-      cur = 1 - cur;
-      phi1 = phi0;
-      pi1 = pi0;
-      sbuf = 1 - sbuf;
+  // once as a CUDA graph, before the timed region, and replayed.
+  if (!a->graph_ok) {
+    CKA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int cur = 0;  // lphi[cur], lpi[cur] hold the adjoint
+    char *ck = (char *)a->ckpt;
+    int sbuf = 0;
+    cudaError_t le = cudaSuccess;
+    for (int s = a->nseg - 1; s >= 0 && le == cudaSuccess; --s) {
+      // re-anchor: the segment's end state is its checkpoint
+      const void *phi1 = ck + (size_t)(s + 1) * 2 * fb;
+      const void *pi1 = ck + (size_t)(s + 1) * 2 * fb + fb;
+      for (int i = a->every - 1; i >= 0 && le == cudaSuccess; --i) {
+        const int n = s * a->every + i;
+        void *phi0 = a->rphi[sbuf], *pi0 = a->rpi[sbuf];
+        if (dbl)
+          adjoint_step<double><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
+              (const double *)phi1, (const double *)pi1, (const double *)a->lphi[cur], (const double *)a->lpi[cur],
+              (double *)phi0, (double *)pi0, (double *)a->lphi[1 - cur], (double *)a->lpi[1 - cur], a->k,
+              a->fk[n], a->fd[n], gr.cz, a->gs);
+        else if (x4)
+          adjoint_step_x4<<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
+              (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
+              (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
+              (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
+        else
+          adjoint_step<float><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
+              (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
+              (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
+              (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
+        le = cudaGetLastError();
+        cur = 1 - cur;
+        phi1 = phi0;
+        pi1 = pi0;
+        sbuf = 1 - sbuf;
+      }
     }
-  }
-  if (capture) {
-    cudaGraph_t g;
-    CKA(cudaStreamEndCapture(st, &g));
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return cuda_error(le != cudaSuccess ? le : ce, "reverse sweep capture");
+    }
     const cudaError_t ie = cudaGraphInstantiate(&a->sweep, g, 0);
     cudaGraphDestroy(g);
     if (ie != cudaSuccess) return cuda_error(ie, "cudaGraphInstantiate (reverse sweep)");
     a->graph_ok = true;
     a->final_cur = cur;
   }
-  // backward timing: the reverse sweep only (after the seed, without the
-  // one-time capture and instantiation of its graph)
+  // timed: the seed at the final state and the reverse sweep
   CKA(cudaEventRecord(a->ev0, st));
+  gs_zero<<<64, 256, 0, st>>>(a->gs, (size_t)gr.nblocks * ADJ_NG);
+  // adjoint of the objective, with the direct dependence of rho on the couplings
+  if (dbl)
+    obj_adjoint_init<double><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
+                                                         (double *)a->lphi[0], (double *)a->lpi[0], a->sums, nb);
+  else
+    obj_adjoint_init<float><<<nb, OBJ_THREADS, 0, st>>>((const float *)phi, (const float *)pi, a->g, a->k,
+                                                        (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
+  CKA(cudaGetLastError());
   CKA(cudaGraphLaunch(a->sweep, st));
-  h->launches += a->nsteps;
-  cur = a->final_cur;
+  h->launches += a->nsteps + 2;
+  const int cur = a->final_cur;
   CKA(cudaEventRecord(a->ev1, st));
   CKA(cudaEventSynchronize(a->ev1));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, a->ev0, a->ev1);
   a->bwd_ms = ms;
-  // gradient slots, fixed order
-  std::vector<double> gsh((size_t)gr.nblocks * ADJ_NG);
+  // gradient slots and direct coupling terms, fixed order
+  std::vector<double> gsh((size_t)gr.nblocks * ADJ_NG), dsh(2 * (size_t)nb);
   CKA(cudaMemcpy(gsh.data(), a->gs, gsh.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  double g_c6 = 0.0, g_h = 0.0;
+  CKA(cudaMemcpy(dsh.data(), a->sums, dsh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  double g_c6 = 0.0, g_h = 0.0, direct_c6 = 0.0, direct_h = 0.0;
   for (int b = 0; b < gr.nblocks; ++b) {
     g_c6 += gsh[(size_t)b * ADJ_NG + 0];
     g_h += gsh[(size_t)b * ADJ_NG + 1];
   }
-  // fields: lam_phi(0), lam_pi(0) in the reference layout
+  for (int b = 0; b < nb; ++b) {
+    direct_c6 += dsh[b];
+    direct_h += dsh[nb + b];
+  }
+  // fields: lam_phi(0), lam_pi(0) in the reference layout, through the
+  // handle's upload/download staging buffer
   const int N = a->p.N;
-  double *ref = nullptr;
-  CKA(cudaMalloc(&ref, (size_t)N * N * (N + 2) * sizeof(double)));
+  double *ref = h->d_ref;
   const size_t slab = (size_t)N * N, nref = slab * (N + 2);
   double sum_lphi = 0.0;
   std::vector<double> tmp;
@@ -677,7 +736,6 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
     CKA(cudaMemcpyAsync(dPi0 + slab, ref + slab, slab * N * sizeof(double), cudaMemcpyDeviceToHost, st));
     CKA(cudaStreamSynchronize(st));
   }
-  cudaFree(ref);
   if (grads) {
     grads[0] = sum_lphi;
     grads[1] = g_c6 + direct_c6;

@@ -238,9 +238,13 @@ def device_count() -> int:
 
 
 class Adjoint:
-    """Forward/backward pair of the hand-written adjoint (phn_adjoint_*)."""
+    """Forward/backward pair of the hand-written adjoint (phn_adjoint_*).
 
-    def __init__(self, p: Params, nsteps: int, every: int = 50, width: float = 0.1):
+    `width` is the sigmoid width of the objective in the reference's energy
+    units; the default 0.6 is width 0.1 in the units of the
+    phi^2/2 - phi^4/4 + g phi^6/6 form (Phi = sqrt(6) phi, energies 6x)."""
+
+    def __init__(self, p: Params, nsteps: int, every: int = 50, width: float = 0.6):
         self.p = p
         self.lib = L.load()
         h = ctypes.c_void_p()
