@@ -142,6 +142,12 @@ int phn_spectrum_bins(const phn_handle *h, int *nbins, double *binsize);
  * momentumspace.cpp:140-278) on the current state: TotalCorrF/K/Q[bin*Nc+a]
  * and TotalBCounts[bin].  Arrays hold nbins*Nc (F, K, Q) and nbins (counts). */
 int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, int nbins);
+/* The configuration's radial spectrum (no reference counterpart): the modes,
+ * weights and sums of phn_spectrum, binned uniformly in the lattice momentum
+ * |p| on [0, p_max], p_max = 2 sqrt(3) / a (pTmax of momentumspace.cpp:43):
+ * bin = (int)(|p| / (p_max / nbins)), the top edge in the last bin.
+ * 1 <= nbins <= 1024; F, K, Q hold nbins*Nc, counts nbins. */
+int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double *Q, int *counts);
 
 /* Full_Analysis() seeding from an empty history (islands.cpp:72-279,778-840):
  * mask (mode), 6-connectivity, x and y periodic, z open as on one rank unless

@@ -129,8 +129,7 @@ def _load(fast: bool = False):
     key = "fast" if fast else "exact"
     if key not in _libs:
         path = lib_path(fast)
-        if not os.path.exists(path):
-            build()
+        build()  # rebuilds only when the C source is newer than the library
         lib = ctypes.CDLL(path)
         lib.orc_evolve.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock), _PD, _PD, _I, _I]
         lib.orc_reset.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock)]
@@ -141,6 +140,8 @@ def _load(fast: bool = False):
         lib.orc_spectrum_bins.argtypes = [ctypes.POINTER(_CParams), _PI, _PD]
         lib.orc_spectrum.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _PD, _PD, _PD, _PI]
         lib.orc_spectrum.restype = _I
+        lib.orc_spectrum_uniform.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _I, _PD, _PD, _PD, _PI]
+        lib.orc_spectrum_uniform.restype = _I
         lib.orc_spectrum_columns.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _PD, _PI, _I, _PD]
         lib.orc_islands.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _D, _I, _I, _PI, _PD, _I]
         lib.orc_islands.restype = _I
@@ -212,6 +213,15 @@ def spectrum(p: Params, phi: np.ndarray, pi: np.ndarray):
                              _ptr(C, _PI))
     if r < 0:
         raise RuntimeError("bin array too small")
+    return F, K, Q, C
+
+
+def spectrum_uniform(p: Params, phi: np.ndarray, pi: np.ndarray, nbins: int = 64):
+    """Config-mode spectrum: nbins uniform |p| bins on [0, p_max]."""
+    F, K, Q = (np.zeros(nbins * p.Nc) for _ in range(3))
+    C = np.zeros(nbins, dtype=np.int32)
+    _load().orc_spectrum_uniform(ctypes.byref(_cp(p)), _ptr(phi), _ptr(pi), int(nbins), _ptr(F), _ptr(K), _ptr(Q),
+                                 _ptr(C, _PI))
     return F, K, Q, C
 
 

@@ -406,6 +406,49 @@ int orc_spectrum(const orc_params *p, const double *Phi, const double *Pi, doubl
   return bad ? -1 : nb;
 }
 
+/* Config-mode spectrum (the configuration's radial |k| bins; no reference
+ * counterpart): the modes, weights and sums of orc_spectrum, binned
+ * uniformly in the lattice momentum |p| on [0, p_max], p_max = pTmax of
+ * momentumspace.cpp:43 (the largest |p|): bin = (int)(|p| / (p_max / nbins)),
+ * the top edge folded into the last bin.  Returns nbins. */
+int orc_spectrum_uniform(const orc_params *p, const double *Phi, const double *Pi, int nbins, double *F, double *K,
+                         double *Q, int *counts) {
+  const int N = p->N, Nc = p->Nc;
+  const double pmax = sqrt(3.0 * (4.0 / sqr(p->a)));
+  const double width = pmax / nbins;
+  const long NN = (long)N * N, V = NN * N;
+  for (int k = 0; k < nbins * Nc; k++) { F[k] = 0.; K[k] = 0.; Q[k] = 0.; }
+  for (int k = 0; k < nbins; k++) counts[k] = 0;
+  double *fr = (double *)malloc(sizeof(double) * V), *fi = (double *)malloc(sizeof(double) * V);
+  double *gr = (double *)malloc(sizeof(double) * V), *gi = (double *)malloc(sizeof(double) * V);
+  for (int a = 0; a < Nc; a++) {
+    forward_fft(p, Phi, a, fr, fi);
+    forward_fft(p, Pi, a, gr, gi);
+    for (int pz = 0; pz < N; pz++) {
+      double nu = lattice_p(pz, N, p->a);
+      for (int px = 0; px < N; px++) {
+        double ppx = lattice_p(px, N, p->a);
+        for (int py = 0; py < N / 2 + 1; py++) {
+          double ppy = lattice_p(py, N, p->a);
+          double psqr = sqr(ppx) + sqr(ppy) + sqr(nu);
+          int bin = (int)(sqrt(psqr) / width);
+          if (bin >= nbins) bin = nbins - 1;
+          long m = px + (long)N * py + NN * pz;
+          double f = sqr(fr[m]) + sqr(fi[m]), k = sqr(gr[m]) + sqr(gi[m]);
+          double q = fr[m] * gr[m] + fi[m] * gi[m];
+          int w = (py != 0 && py != N / 2) ? 2 : 1;
+          F[bin * Nc + a] += w * f;
+          K[bin * Nc + a] += w * k;
+          Q[bin * Nc + a] += w * q;
+          if (a == 0) counts[bin] += w;
+        }
+      }
+    }
+  }
+  free(fr); free(fi); free(gr); free(gi);
+  return nbins;
+}
+
 /* Print_fp (momentumspace.cpp:280-384) per-bin columns, for bins with a
  * non-zero count and F: p, count, omega, F/(L^3 count), K/(L^3 count),
  * sqrt(FK)/(L^3 count), F p^3 /(2 pi^2 L^3 count).  cols[k*7 + ...]; rows of

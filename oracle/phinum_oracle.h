@@ -62,6 +62,8 @@ int orc_run_loop(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int
 void orc_spectrum_bins(const orc_params *p, int *nbins, double *binsize);
 int orc_spectrum(const orc_params *p, const double *Phi, const double *Pi, double *F, double *K, double *Q,
                  int *counts);
+int orc_spectrum_uniform(const orc_params *p, const double *Phi, const double *Pi, int nbins, double *F, double *K,
+                         double *Q, int *counts);
 void orc_spectrum_columns(const orc_params *p, const double *F, const double *K, const double *Q,
                           const int *counts, int nb, double *cols);
 double orc_site_energy(const orc_params *p, const double *Phi, const double *Pi, long K, int x, int y, int z);

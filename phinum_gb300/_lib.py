@@ -67,6 +67,7 @@ _SIGS = {
     "phn_run_loop": (_I, [ctypes.c_void_p, _I, _D, ctypes.POINTER(PhnAverages), _I, _PI]),
     "phn_spectrum_bins": (_I, [ctypes.c_void_p, _PI, _PD]),
     "phn_spectrum": (_I, [ctypes.c_void_p, _PD, _PD, _PD, _PI, _I]),
+    "phn_spectrum_uniform": (_I, [ctypes.c_void_p, _I, _PD, _PD, _PD, _PI]),
     "phn_islands": (_I, [ctypes.c_void_p, _D, _I, _I, _PI, _PD, _I, _PI]),
     "phn_set_path": (_I, [ctypes.c_void_p, _I]),
     "phn_get_path": (_I, [ctypes.c_void_p, _PI]),

@@ -13,6 +13,10 @@
 // and bin membership are identical; the sums differ from FFTW's only by
 // rounding.
 //
+// A second bin rule serves the configuration's radial spectrum (no reference
+// counterpart): the same modes, weights and sums, binned uniformly in |p| on
+// [0, p_max] with p_max the largest lattice momentum.
+//
 // Accumulation is deterministic: per-warp shared-memory histograms (one lane
 // per distinct bin adds a fixed-shape butterfly sum of the warp's values),
 // folded per block in warp order, then over blocks in block order.
@@ -43,7 +47,14 @@ struct SpecState {
   double binsize;
   std::vector<int> h_counts;
   bool counts_ok;
+  // uniform-bin (configuration) mode, allocated on first use
+  int u_nbins;
+  double *u_partials, *u_bins;
+  int *u_counts;
 };
+
+constexpr int SPEC_MAX_UNIFORM_BINS = 1024;  // per-warp histograms in shared memory
+enum { RULE_REFERENCE = 0, RULE_UNIFORM = 1 };
 
 // Lattice momentum of index n along an axis (momentumspace.cpp:222-244).
 static double lattice_p(int n, int N, double a) {
@@ -57,11 +68,15 @@ __device__ __forceinline__ double dotre(float2 a, float2 b) { return (double)a.x
 __device__ __forceinline__ double dotre(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
 
 // COUNT: only the mode counts (InitBCounts), no field reads.
+// rule RULE_REFERENCE: bin = int(|p| / binsize + 0.5) (momentumspace.cpp:228);
+// rule RULE_UNIFORM: bin = int(|p| / binsize), binsize = p_max / nbins, the
+// top edge folded into the last bin.
 template <typename C, bool COUNT>
 __global__ void __launch_bounds__(SPEC_THREADS) bin_kernel(const C *__restrict__ fphi, const C *__restrict__ fpi,
                                                           const double *__restrict__ ptab, int N, double binsize,
-                                                          int nbins, double scale, double *__restrict__ partials,
-                                                          int *__restrict__ counts, int *__restrict__ flag) {
+                                                          int nbins, int rule, double scale,
+                                                          double *__restrict__ partials, int *__restrict__ counts,
+                                                          int *__restrict__ flag) {
   extern __shared__ double hist[];  // [SPEC_WARPS][3][nbins]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < SPEC_WARPS * 3 * nbins; i += SPEC_THREADS) hist[i] = 0.0;
@@ -83,7 +98,13 @@ __global__ void __launch_bounds__(SPEC_THREADS) bin_kernel(const C *__restrict__
       const int pz = (int)(t / M);
       const double ppx = ptab[px], ppy = ptab[py], nu = ptab[pz];
       const double psqr = __dadd_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)), __dmul_rn(nu, nu));
-      const int bin = (int)(__dadd_rn(sqrt(psqr) / binsize, 0.5));
+      int bin;
+      if (rule == RULE_REFERENCE) {
+        bin = (int)(__dadd_rn(sqrt(psqr) / binsize, 0.5));
+      } else {
+        bin = (int)(sqrt(psqr) / binsize);
+        if (bin >= nbins) bin = nbins - 1;
+      }
       const int w = (py != 0 && py != h) ? 2 : 1;
       if (bin >= nbins) {
         atomicOr(flag, 1);
@@ -154,6 +175,9 @@ void spectrum_release(phn_handle *h) {
   cudaFree(s->bins);
   cudaFree(s->counts);
   cudaFree(s->flag);
+  cudaFree(s->u_partials);
+  cudaFree(s->u_bins);
+  cudaFree(s->u_counts);
   delete s;
   h->spec = nullptr;
 }
@@ -197,16 +221,17 @@ static int spec_init(phn_handle *h) {
   s->plan_ok = true;
   if (cufftSetStream(s->plan, h->stream) != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cufftSetStream failed");
   const size_t smem = (size_t)SPEC_WARPS * 3 * s->nbins * sizeof(double);
-  if (smem > 48 * 1024) {
-    CKS(cudaFuncSetAttribute(bin_kernel<float2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CKS(cudaFuncSetAttribute(bin_kernel<double2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CKS(cudaFuncSetAttribute(bin_kernel<float2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  }
+  // the largest histogram either rule uses
+  const size_t smem_max = (size_t)SPEC_WARPS * 3 * (s->nbins > SPEC_MAX_UNIFORM_BINS ? s->nbins : SPEC_MAX_UNIFORM_BINS) *
+                          sizeof(double);
+  CKS(cudaFuncSetAttribute(bin_kernel<float2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+  CKS(cudaFuncSetAttribute(bin_kernel<double2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+  CKS(cudaFuncSetAttribute(bin_kernel<float2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
   // mode counts (InitBCounts, momentumspace.cpp:89-138): field independent
   CKS(cudaMemsetAsync(s->counts, 0, s->nbins * sizeof(int), h->stream));
   CKS(cudaMemsetAsync(s->flag, 0, sizeof(int), h->stream));
   bin_kernel<float2, true><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-      nullptr, nullptr, s->ptab, N, s->binsize, s->nbins, 0.0, nullptr, s->counts, s->flag);
+      nullptr, nullptr, s->ptab, N, s->binsize, s->nbins, RULE_REFERENCE, 0.0, nullptr, s->counts, s->flag);
   CKS(cudaGetLastError());
   h->launches++;
   s->h_counts.resize(s->nbins);
@@ -269,12 +294,12 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
     if (fr != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cuFFT exec failed (%d)", (int)fr);
     if (dbl)
       bin_kernel<double2, false><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-          (const double2 *)s->fphi, (const double2 *)s->fpi, s->ptab, N, s->binsize, s->nbins, scale, s->partials,
-          nullptr, s->flag);
+          (const double2 *)s->fphi, (const double2 *)s->fpi, s->ptab, N, s->binsize, s->nbins, RULE_REFERENCE, scale,
+          s->partials, nullptr, s->flag);
     else
       bin_kernel<float2, false><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-          (const float2 *)s->fphi, (const float2 *)s->fpi, s->ptab, N, s->binsize, s->nbins, scale, s->partials,
-          nullptr, s->flag);
+          (const float2 *)s->fphi, (const float2 *)s->fpi, s->ptab, N, s->binsize, s->nbins, RULE_REFERENCE, scale,
+          s->partials, nullptr, s->flag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "bin_kernel");
     fold_blocks<<<(3 * s->nbins + 255) / 256, 256, 0, h->stream>>>(s->partials, s->nblocks, s->nbins, s->bins);
@@ -292,6 +317,91 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
   }
   if (counts)
     for (int b = 0; b < s->nbins; ++b) counts[b] = s->h_counts[b];
+  return PHN_OK;
+}
+
+int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double *Q, int *counts) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (nbins < 1 || nbins > SPEC_MAX_UNIFORM_BINS)
+    return set_error(PHN_ERR_INVALID, "nbins=%d outside [1, %d]", nbins, SPEC_MAX_UNIFORM_BINS);
+  int r = spec_init(h);
+  if (r) {
+    spectrum_release(h);
+    return r;
+  }
+  SpecState *s = (SpecState *)h->spec;
+  const int N = h->p.N, Nc = h->p.Nc;
+  const bool dbl = h->p.precision == PHN_FP64;
+  cudaError_t e;
+  if (s->u_nbins != nbins) {
+    cudaFree(s->u_partials);
+    cudaFree(s->u_bins);
+    cudaFree(s->u_counts);
+    s->u_partials = s->u_bins = nullptr;
+    s->u_counts = nullptr;
+    s->u_nbins = 0;
+    e = cudaMalloc(&s->u_partials, (size_t)s->nblocks * 3 * nbins * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->u_bins, (size_t)3 * nbins * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->u_counts, (size_t)nbins * sizeof(int));
+    if (e != cudaSuccess) return cuda_error(e, "uniform spectrum buffers");
+    s->u_nbins = nbins;
+  }
+  // p_max = pTmax of momentumspace.cpp:43, the largest lattice |p|
+  const double pmax = sqrt(3.0 * (4.0 / (h->p.a * h->p.a)));
+  const double width = pmax / nbins;
+  const double f3 = (h->p.a * h->p.a) * h->p.a;
+  const double scale = f3 * f3;
+  const size_t smem = (size_t)SPEC_WARPS * 3 * nbins * sizeof(double);
+  std::vector<int> hc(nbins);
+  e = cudaMemsetAsync(s->u_counts, 0, nbins * sizeof(int), h->stream);
+  if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
+  bin_kernel<float2, true><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
+      nullptr, nullptr, s->ptab, N, width, nbins, RULE_UNIFORM, 0.0, nullptr, s->u_counts, s->flag);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "bin_kernel (counts)");
+  h->launches++;
+  e = cudaMemcpyAsync(hc.data(), s->u_counts, nbins * sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+  if (e != cudaSuccess) return cuda_error(e, "counts readback");
+  std::vector<double> hb((size_t)3 * nbins);
+  for (int a = 0; a < Nc; ++a) {
+    cufftResult fr;
+    if (dbl) {
+      double *phi = (double *)h->phi[h->cur] + (size_t)a * h->V, *pi = (double *)h->pi + (size_t)a * h->V;
+      fr = cufftExecD2Z(s->plan, phi, (cufftDoubleComplex *)s->fphi);
+      if (fr == CUFFT_SUCCESS) fr = cufftExecD2Z(s->plan, pi, (cufftDoubleComplex *)s->fpi);
+    } else {
+      float *phi = (float *)h->phi[h->cur] + (size_t)a * h->V, *pi = (float *)h->pi + (size_t)a * h->V;
+      fr = cufftExecR2C(s->plan, phi, (cufftComplex *)s->fphi);
+      if (fr == CUFFT_SUCCESS) fr = cufftExecR2C(s->plan, pi, (cufftComplex *)s->fpi);
+    }
+    if (fr != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cuFFT exec failed (%d)", (int)fr);
+    if (dbl)
+      bin_kernel<double2, false><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
+          (const double2 *)s->fphi, (const double2 *)s->fpi, s->ptab, N, width, nbins, RULE_UNIFORM, scale,
+          s->u_partials, nullptr, s->flag);
+    else
+      bin_kernel<float2, false><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
+          (const float2 *)s->fphi, (const float2 *)s->fpi, s->ptab, N, width, nbins, RULE_UNIFORM, scale,
+          s->u_partials, nullptr, s->flag);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "bin_kernel");
+    fold_blocks<<<(3 * nbins + 255) / 256, 256, 0, h->stream>>>(s->u_partials, s->nblocks, nbins, s->u_bins);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "fold_blocks");
+    h->launches += 2;
+    e = cudaMemcpyAsync(hb.data(), s->u_bins, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_error(e, "spectrum readback");
+    for (int b = 0; b < nbins; ++b) {
+      if (F) F[b * Nc + a] = hb[b];
+      if (K) K[b * Nc + a] = hb[nbins + b];
+      if (Q) Q[b * Nc + a] = hb[2 * nbins + b];
+    }
+  }
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_error(e, "spectrum readback");
+  if (counts)
+    for (int b = 0; b < nbins; ++b) counts[b] = hc[b];
   return PHN_OK;
 }
 

@@ -138,6 +138,13 @@ class Lattice:
         L.check(self.lib.phn_spectrum(self.h, _pd(F), _pd(K), _pd(Q), _pi(C), nb))
         return F, K, Q, C
 
+    def spectrum_uniform(self, nbins: int = 64):
+        """The configuration's radial spectrum: nbins uniform |p| bins on [0, p_max]."""
+        F, K, Q = (np.zeros(nbins * self.p.Nc) for _ in range(3))
+        C = np.zeros(nbins, dtype=np.int32)
+        L.check(self.lib.phn_spectrum_uniform(self.h, int(nbins), _pd(F), _pd(K), _pd(Q), _pi(C)))
+        return F, K, Q, C
+
     def full_analysis(self, thres: float, mode: int = L.ISLAND_REFERENCE, z_periodic: bool = False,
                       labels: bool = True, max_out: int = 1 << 20):
         lab = np.zeros(self.p.N * self.p.N * (self.p.N + 2), dtype=np.int32) if labels else None
