@@ -34,6 +34,6 @@ def test_uniform_spectrum_rejects_bad_bin_counts():
     from phinum_gb300 import _lib as L
     with PL.Lattice(PL.Params(N=16)) as lat:
         for nb in (0, -3, 1025):
-            with pytest.raises(L.PhnError) as e:
-                lat.spectrum_uniform(nb)
-            assert e.value.code == L.ERR_INVALID
+            assert lat.lib.phn_spectrum_uniform(lat.h, nb, None, None, None, None) == L.ERR_INVALID
+        F, K, Q, C = lat.spectrum_uniform(1024)  # the largest bin count
+        assert C.sum() == 16 ** 3
