@@ -135,10 +135,16 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile():
-    """DRAM bytes per launch of the plain FP32 step kernel at 512^3, from the
-    committed ncu summary (profiles/leapfrog_f32_512.md, line 'traffic_bytes_per_launch: X')."""
-    path = os.path.join(ROOT, "profiles", "leapfrog_f32_512.md")
+PROFILE_OF_PATH = {2: "leapfrog_f32_512.md", 3: "leapfrog_f32_x4_512.md"}  # PHN_PATH_TMA, PHN_PATH_X4
+
+
+def traffic_from_profile(path_kind: int):
+    """DRAM bytes per launch of the FP32 step kernel of the given path at
+    512^3, from its committed ncu summary (line 'traffic_bytes_per_launch: X');
+    None when that kernel has no summary."""
+    if path_kind not in PROFILE_OF_PATH:
+        return None
+    path = os.path.join(ROOT, "profiles", PROFILE_OF_PATH[path_kind])
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -177,16 +183,20 @@ def measure_gpu(args, dist: Dist):
     # ---------------------------------------------------------------- value
     lat = PL.Lattice(PL.Params(N=N, precision=L.FP32))
     lat.upload(phi, pi)
-    # the project's autotuner picks the TMA kernel variant for this lattice
-    # (state unchanged; all variants compute identical fields)
+    # the project's autotuner picks the FP32 step kernel for this lattice: the
+    # plain kernel or a variant of the TMA or x4 kernels (state unchanged; all
+    # compute identical fields)
     import ctypes
-    tv, tms = ctypes.c_int(), ctypes.c_double()
+    tv, tms, pk = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
     if args.variant is None:
         L.check(lib.phn_autotune(lat.h, 30, ctypes.byref(tv), ctypes.byref(tms)))
     else:
         L.check(lib.phn_set_variant(lat.h, args.variant))
         tv.value = args.variant
+    L.check(lib.phn_get_path(lat.h, ctypes.byref(pk)))
     out["variant"] = tv.value
+    kernel_name = {L.PATH_PLAIN: "phn::step_f32", L.PATH_TMA: f"phn::step_f32_tma (variant {tv.value})",
+                   L.PATH_X4: f"phn::step_f32_x4 (variant {tv.value})"}[pk.value]
     lat.run_loop(max(3, args.warmup), 1.0)
     lat.synchronize()
     n0, _, _ = lat.stats()
@@ -217,8 +227,9 @@ def measure_gpu(args, dist: Dist):
     achieved = BYTES_PER_SITE[1] * sites / t_launch / 1e9
     peak, kind = peaks()
     out["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                       "frac": round(achieved / peak, 4), "traffic": traffic_from_profile(),
-                       "kernel": f"phn::step_f32_tma (variant {out['variant']})", "peak_kind": f"{kind} hbm_gbs",
+                       "frac": round(achieved / peak, 4),
+                       "traffic": traffic_from_profile(pk.value) if N == 512 else None,
+                       "kernel": kernel_name, "peak_kind": f"{kind} hbm_gbs",
                        "algorithmic_bytes_per_launch": BYTES_PER_SITE[1] * sites,
                        "mean_launch_ms": round(t_launch * 1e3, 4)}
     lat.close()
@@ -230,6 +241,8 @@ def measure_gpu(args, dist: Dist):
 
     # ---------------------------------------------------------------- e2e
     lat = PL.Lattice(PL.Params(N=N, precision=L.FP32))
+    # the kernel the autotuner chose above
+    L.check(lib.phn_set_path(lat.h, L.PATH_PLAIN) if tv.value < 0 else lib.phn_set_variant(lat.h, tv.value))
     for a in (phi, pi):
         L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
     hphi, hpi = np.empty_like(phi), np.empty_like(pi)

@@ -159,20 +159,27 @@ int phn_islands(phn_handle *h, double thres, int mode, int z_periodic, int *labe
 
 /* Kernel path of the FP32 step (the others have one path each):
  * PHN_PATH_TMA, the TMA-pipelined persistent kernel (default where it
- * applies: Nc = 1, N in {128,256,384,512,768,1024}), or PHN_PATH_PLAIN, the
- * register z-marching kernel (every size).  Both compute bit-identical fields. */
-enum { PHN_PATH_AUTO = 0, PHN_PATH_PLAIN = 1, PHN_PATH_TMA = 2 };
+ * applies: Nc = 1, N in {128,256,384,512,768,1024}); PHN_PATH_X4, the
+ * register kernel with four x-sites per thread (Nc = 1, N a multiple of 32);
+ * or PHN_PATH_PLAIN, the register z-marching kernel (every size).  All compute
+ * bit-identical fields.  PHN_PATH_AUTO restores the default. */
+enum { PHN_PATH_AUTO = 0, PHN_PATH_PLAIN = 1, PHN_PATH_TMA = 2, PHN_PATH_X4 = 3 };
 int phn_set_path(phn_handle *h, int path);
 int phn_get_path(const phn_handle *h, int *path);
 
-/* Autotuner of the TMA step kernel: times each variant (tile height, stage
- * count, pi through shared memory or straight from HBM) for `steps` launches
- * on the live lattice, keeps the fastest for this handle and reports it.  The
- * lattice state is unchanged; all variants compute bit-identical fields.
- * A handle on another path has nothing to tune (*variant = -1). */
+/* Autotuner of the FP32 step: times the plain kernel and every variant of the
+ * TMA kernel (tile height, stage count, pi through shared memory or straight
+ * from HBM, grid policy) and of the x4 kernel (block shape, planes per item,
+ * grid policy) that applies to this lattice, `steps` launches each on the
+ * live lattice, and keeps the fastest for this handle.  *variant is its index
+ * (as phn_set_variant takes it) or -1 for the plain kernel.  The lattice state
+ * is unchanged; all kernels compute bit-identical fields.  Other precisions
+ * have one kernel: nothing to tune (*variant = -1). */
 int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms);
-/* Number of variants on this handle (0 without the TMA kernel) and an explicit
- * choice of one (0 .. n-1), e.g. to reproduce a tuned configuration. */
+/* Number of variants on this handle -- the TMA kernel's first, then the x4
+ * kernel's; 0 when neither applies -- and an explicit choice of one
+ * (0 .. n-1, which also selects its path), e.g. to reproduce a tuned
+ * configuration. */
 int phn_num_variants(const phn_handle *h, int *n);
 int phn_set_variant(phn_handle *h, int variant);
 

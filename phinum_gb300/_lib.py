@@ -17,7 +17,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NOMEM, ERR_UNSUPPORTE
     0, -1, -2, -3, -4, -5, -6, -7
 FP64, FP32, FP32_KAHAN = 0, 1, 2
 ISLAND_REFERENCE, ISLAND_ENERGY = 0, 1
-PATH_AUTO, PATH_PLAIN, PATH_TMA = 0, 1, 2
+PATH_AUTO, PATH_PLAIN, PATH_TMA, PATH_X4 = 0, 1, 2, 3
 
 _D, _I = ctypes.c_double, ctypes.c_int
 _PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)

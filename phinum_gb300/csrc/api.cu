@@ -179,11 +179,19 @@ int phn_create(const phn_params *params, phn_handle **out) {
     h->tma_grid = tma_grid(*params, 0);
   }
   h->path = h->tma_grid > 0 ? PHN_PATH_TMA : PHN_PATH_PLAIN;
+  h->x4_variant = 0;
+  h->x4_grid = x4_supported(*params) ? x4_grid(*params, 0) : 0;
+  h->x4_obs_grid = h->x4_grid > 0 ? x4_grid(*params, x4_obs_variant(0)) : 0;
   {
     int recs = h->grid.nblocks;
     if (h->tma_grid > 0)
       for (int v = 0; v < tma_num_variants(params->N); ++v) {
         const int g = tma_grid(*params, v);
+        if (g > recs) recs = g;
+      }
+    if (h->x4_grid > 0)
+      for (int v = 0; v < x4_num_variants(); ++v) {
+        const int g = x4_grid(*params, v);
         if (g > recs) recs = g;
       }
     h->partial_cap = recs;
@@ -298,7 +306,13 @@ static int step_once(phn_handle *h, int mode) {
       if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
       break;
     case PHN_FP32:
-      if (h->path == PHN_PATH_TMA && mode != MODE_OBS) {
+      if (h->path == PHN_PATH_X4) {
+        const bool obs = mode != MODE_STEP;
+        e = launch_step_f32_x4(h->k, obs ? x4_obs_variant(h->x4_variant) : h->x4_variant,
+                               obs ? h->x4_obs_grid : h->x4_grid, mode, (const float *)h->phi[h->cur],
+                               (float *)h->phi[nxt], (float *)h->pi, s, h->partials, h->stream);
+        if (obs) h->obs_records = h->x4_obs_grid;
+      } else if (h->path == PHN_PATH_TMA && mode != MODE_OBS) {
         e = launch_step_f32_tma(h->k, h->tma_variant, h->tma_grid, mode == MODE_STEP_OBS, (const float *)h->phi[h->cur],
                                 (float *)h->phi[nxt], (float *)h->pi, s, h->partials, h->d_err, h->stream);
         if (mode == MODE_STEP_OBS) h->obs_records = h->tma_grid;
@@ -463,16 +477,54 @@ int phn_run_loop(phn_handle *h, int nsteps, double tso, phn_averages *rows, int 
 int phn_set_path(phn_handle *h, int path) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
   if (path == PHN_PATH_AUTO) path = h->tma_grid > 0 ? PHN_PATH_TMA : PHN_PATH_PLAIN;
-  if (path != PHN_PATH_PLAIN && path != PHN_PATH_TMA) return set_error(PHN_ERR_INVALID, "path %d", path);
+  if (path != PHN_PATH_PLAIN && path != PHN_PATH_TMA && path != PHN_PATH_X4)
+    return set_error(PHN_ERR_INVALID, "path %d", path);
   if (path == PHN_PATH_TMA && h->tma_grid == 0)
     return set_error(PHN_ERR_UNSUPPORTED, "TMA step needs FP32, Nc = 1, N in {128,256,384,512,768,1024}");
+  if (path == PHN_PATH_X4 && h->x4_grid == 0)
+    return set_error(PHN_ERR_UNSUPPORTED, "x4 step needs FP32, Nc = 1, N a multiple of 32");
   h->path = path;
   return PHN_OK;
 }
 
+// Variants of the FP32 step on this handle: the TMA kernel's, then the x4
+// kernel's.
+static int n_tma_variants(const phn_handle *h) { return h->tma_grid > 0 ? tma_num_variants(h->p.N) : 0; }
+static int n_x4_variants(const phn_handle *h) { return h->x4_grid > 0 ? x4_num_variants() : 0; }
+
+// Selects combined variant v (-1: the plain kernel); returns its grid, 0 if it
+// does not apply to this lattice or device.
+static int select_variant(phn_handle *h, int v) {
+  if (v < 0) {
+    h->path = PHN_PATH_PLAIN;
+    return h->grid.nblocks;
+  }
+  const int nt = n_tma_variants(h);
+  if (v < nt) {
+    const int g = tma_grid(h->p, v);
+    if (g > 0) {
+      h->path = PHN_PATH_TMA;
+      h->tma_variant = v;
+      h->tma_grid = g;
+    }
+    return g;
+  }
+  const int g = x4_grid(h->p, v - nt);
+  const int go = g > 0 ? x4_grid(h->p, x4_obs_variant(v - nt)) : 0;
+  if (g > 0 && go > 0) {
+    h->path = PHN_PATH_X4;
+    h->x4_variant = v - nt;
+    h->x4_grid = g;
+    h->x4_obs_grid = go;
+    return g;
+  }
+  return 0;
+}
+
 int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms) {
   if (!h || steps < 1) return set_error(PHN_ERR_INVALID, "bad argument");
-  if (h->tma_grid == 0 || h->path != PHN_PATH_TMA) {
+  const int nt = n_tma_variants(h), nv = nt + n_x4_variants(h);
+  if (h->p.precision != PHN_FP32 || nv == 0) {
     if (variant) *variant = -1;
     if (best_ms) *best_ms = 0.0;
     return PHN_OK;  // one kernel only: nothing to choose
@@ -483,35 +535,53 @@ int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms) {
   // trial, so the lattice state is unchanged by tuning (phi[cur] is only read)
   const size_t bytes = h->V * h->elem;
   const StepF s = {h->dtau, h->dtau};
+  const int path0 = h->path, tv0 = h->tma_variant, xv0 = h->x4_variant;
+  const int tg0 = h->tma_grid, xg0 = h->x4_grid, xo0 = h->x4_obs_grid;
   double best = 1e30;
-  int best_v = h->tma_variant;
+  int best_v = -2;
   CK(cudaMemcpyAsync(h->d_ref, h->pi, bytes, cudaMemcpyDeviceToDevice, h->stream));
-  // two rounds over the variants, each variant keeping its best round
+  // two rounds over the candidates (plain kernel = -1), each keeping its best round
   for (int round = 0; round < 2; ++round)
-  for (int v = 0; v < tma_num_variants(h->p.N); ++v) {
-    const int g = tma_grid(h->p, v);
-    if (g <= 0) continue;
-    for (int i = 0; i < steps + 2; ++i) {
-      if (i == 2) CK(cudaEventRecord(h->ev0, h->stream));
-      CK(launch_step_f32_tma(h->k, v, g, false, (const float *)h->phi[h->cur], (float *)h->phi[1 - h->cur],
-                             (float *)h->pi, s, h->partials, h->d_err, h->stream));
-      h->launches++;
+    for (int v = -1; v < nv; ++v) {
+      if (select_variant(h, v) <= 0) continue;
+      for (int i = 0; i < steps + 2; ++i) {
+        if (i == 2) CK(cudaEventRecord(h->ev0, h->stream));
+        cudaError_t e;
+        if (h->path == PHN_PATH_TMA)
+          e = launch_step_f32_tma(h->k, h->tma_variant, h->tma_grid, false, (const float *)h->phi[h->cur],
+                                  (float *)h->phi[1 - h->cur], (float *)h->pi, s, h->partials, h->d_err, h->stream);
+        else if (h->path == PHN_PATH_X4)
+          e = launch_step_f32_x4(h->k, h->x4_variant, h->x4_grid, MODE_STEP, (const float *)h->phi[h->cur],
+                                 (float *)h->phi[1 - h->cur], (float *)h->pi, s, h->partials, h->stream);
+        else
+          e = launch_step_f32(h->k, h->grid, MODE_STEP, (const float *)h->phi[h->cur], (float *)h->phi[1 - h->cur],
+                              (float *)h->pi, s, h->partials, h->stream);
+        if (e != cudaSuccess) return cuda_error(e, "step kernel launch (autotune)");
+        h->launches++;
+      }
+      CK(cudaEventRecord(h->ev1, h->stream));
+      CK(cudaEventSynchronize(h->ev1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+      CK(cudaMemcpyAsync(h->pi, h->d_ref, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      if (ms / steps < best) {
+        best = ms / steps;
+        best_v = v;
+      }
     }
-    CK(cudaEventRecord(h->ev1, h->stream));
-    CK(cudaEventSynchronize(h->ev1));
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-    CK(cudaMemcpyAsync(h->pi, h->d_ref, bytes, cudaMemcpyDeviceToDevice, h->stream));
-    if (ms / steps < best) {
-      best = ms / steps;
-      best_v = v;
-    }
-  }
   CK(cudaStreamSynchronize(h->stream));
   r = check_device_error(h);
   if (r) return r;
-  h->tma_variant = best_v;
-  h->tma_grid = tma_grid(h->p, best_v);
+  if (best_v == -2) {  // nothing ran: keep the previous choice
+    h->path = path0;
+    h->tma_variant = tv0;
+    h->x4_variant = xv0;
+    h->tma_grid = tg0;
+    h->x4_grid = xg0;
+    h->x4_obs_grid = xo0;
+    return set_error(PHN_ERR_UNSUPPORTED, "no step kernel fits this device");
+  }
+  select_variant(h, best_v);
   if (variant) *variant = best_v;
   if (best_ms) *best_ms = best;
   return PHN_OK;
@@ -519,18 +589,20 @@ int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms) {
 
 int phn_set_variant(phn_handle *h, int variant) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
-  if (h->tma_grid == 0) return set_error(PHN_ERR_UNSUPPORTED, "no kernel variants on this handle");
-  if (variant < 0 || variant >= tma_num_variants(h->p.N)) return set_error(PHN_ERR_INVALID, "variant %d", variant);
-  const int g = tma_grid(h->p, variant);
-  if (g <= 0) return set_error(PHN_ERR_UNSUPPORTED, "variant %d does not fit this device", variant);
-  h->tma_variant = variant;
-  h->tma_grid = g;
+  const int nv = n_tma_variants(h) + n_x4_variants(h);
+  if (nv == 0) return set_error(PHN_ERR_UNSUPPORTED, "no kernel variants on this handle");
+  if (variant < 0 || variant >= nv) return set_error(PHN_ERR_INVALID, "variant %d", variant);
+  const int path0 = h->path;
+  if (select_variant(h, variant) <= 0) {
+    h->path = path0;
+    return set_error(PHN_ERR_UNSUPPORTED, "variant %d does not fit this lattice or device", variant);
+  }
   return PHN_OK;
 }
 
 int phn_num_variants(const phn_handle *h, int *n) {
   if (!h || !n) return set_error(PHN_ERR_INVALID, "NULL argument");
-  *n = h->tma_grid > 0 ? tma_num_variants(h->p.N) : 0;
+  *n = n_tma_variants(h) + n_x4_variants(h);
   return PHN_OK;
 }
 

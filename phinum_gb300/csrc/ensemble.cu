@@ -7,7 +7,8 @@
 // potential and couplings.  Fields live back to back in one FP32 buffer.
 //
 // Work list: items = (member, 32-wide x tile, TY-row y tile, CZ-plane z
-// chunk), member-major.  A persistent grid (SMs x resident blocks) walks the
+// chunk), member-major; or, for the x4 tiles, (member, chunk of 128 W
+// consecutive plane sites, CZ-plane z chunk) with four x-sites per thread.  A persistent grid (SMs x resident blocks) walks the
 // list round-robin; every item is the same size (32 x TY x CZ sites), so the
 // load is balanced whatever the mix of lattice sizes.  The per-site arithmetic
 // is kick_drift_f32 (kick.cuh), the same bits as the single-lattice kernels,
@@ -37,11 +38,15 @@ struct EnsItem {
   int member, x0, y0, z0, nz;
 };
 
+// ty: rows per block (scalar tiles) or warps per block (x4 tiles).
 struct EnsTile {
   int ty, cz;
+  bool x4;
 };
-constexpr EnsTile kEnsTiles[] = {{8, 16}, {4, 16}, {8, 8}, {4, 32}, {8, 32}, {4, 8}};
-constexpr int kNumEnsTiles = 6;
+constexpr EnsTile kEnsTiles[] = {{8, 16, false}, {4, 16, false}, {8, 8, false}, {4, 32, false},
+                                 {8, 32, false}, {4, 8, false},  {8, 16, true},  {4, 16, true},
+                                 {8, 32, true},  {4, 32, true},  {2, 32, true}};
+constexpr int kNumEnsTiles = 11;
 constexpr int kGraphSteps = 50;
 
 template <int TY, int MODE>
@@ -109,6 +114,92 @@ __global__ void __launch_bounds__(32 * TY) ens_step(const EnsMember *__restrict_
   }
 }
 
+// Four consecutive x-sites per thread (16-byte loads and stores); a warp
+// covers 128 consecutive sites of a plane -- several rows when N < 128 -- and
+// a block W warps.  An item's chunk starts at plane site q0 = y0 * N + x0.
+// x neighbours inside the thread's four sites come from registers, the two
+// outside ones from scalar loads (the same cache lines as the neighbouring
+// lanes' vectors); y rows and z planes are float4.  kick_drift_f32 gets the
+// same values as in the scalar kernels, so the fields are bit-identical.
+template <int W, int MODE>
+__global__ void __launch_bounds__(32 * W) ens_step_x4(const EnsMember *__restrict__ members,
+                                                      const EnsItem *__restrict__ items, int nitems,
+                                                      const float *__restrict__ phi, float *__restrict__ phi_out,
+                                                      float *__restrict__ pi, const double *__restrict__ factors,
+                                                      int slot, double *__restrict__ partials) {
+  const float fk = MODE == MODE_OBS ? 0.f : (float)factors[2 * slot];
+  const float fd = MODE == MODE_OBS ? 0.f : (float)factors[2 * slot + 1];
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const EnsItem I = items[it];
+    const int N = members[I.member].N;
+    const int theory = members[I.member].theory;
+    const long long off = members[I.member].off;
+    const Consts k = members[I.member].k;
+    const float *f = phi + off;
+    float *fo = phi_out + off;
+    float *pp = pi + off;
+    const int NN = N * N;
+    const int q = I.y0 * N + I.x0 + 4 * tid;  // this thread's first site in the plane
+    const int y = q / N, x = q - y * N;
+    const int qxl = (x == 0) ? q + N - 1 : q - 1;
+    const int qxr = (x + 4 == N) ? q + 4 - N : q + 4;
+    const int qyp = (y + 1 == N) ? q - (N - 1) * N : q + N;
+    const int qym = (y == 0) ? q + (N - 1) * N : q - N;
+    const int z0 = I.z0, z1 = I.z0 + I.nz;
+    AccF accf;
+    if (MODE != MODE_STEP) accf.init();
+    float4 cm = __ldg((const float4 *)(f + (size_t)((z0 == 0) ? N - 1 : z0 - 1) * NN + q));
+    float4 c = __ldg((const float4 *)(f + (size_t)z0 * NN + q));
+    for (int z = z0; z < z1; ++z) {
+      const int zn = (z + 1 == N) ? 0 : z + 1;
+      const float *pl = f + (size_t)z * NN;
+      const size_t i = (size_t)z * NN + q;
+      const float4 cp = __ldg((const float4 *)(f + (size_t)zn * NN + q));
+      const float4 yp = __ldg((const float4 *)(pl + qyp));
+      const float4 ym = __ldg((const float4 *)(pl + qym));
+      const float xm = __ldg(pl + qxl), xp = __ldg(pl + qxr);
+      const float4 p = *(const float4 *)(pp + i);
+      if (MODE != MODE_STEP) {
+        const float cv[4] = {c.x, c.y, c.z, c.w}, pv[4] = {p.x, p.y, p.z, p.w};
+        const float xv[4] = {c.y, c.z, c.w, xp}, yv[4] = {yp.x, yp.y, yp.z, yp.w};
+        const float zv[4] = {cp.x, cp.y, cp.z, cp.w};
+        const long long kidx = (long long)q + (long long)(z + 1) * NN;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (theory == 0)
+            observe_f32<1, 0>(accf, k, cv + e, pv + e, xv + e, yv + e, zv + e, kidx + e);
+          else
+            observe_f32<1, 1>(accf, k, cv + e, pv + e, xv + e, yv + e, zv + e, kidx + e);
+        }
+      }
+      if (MODE != MODE_OBS) {
+        float4 pn, fn;
+        if (theory == 0) {
+          kick_drift_f32<0>(k, fk, fd, c.x, xm, c.y, ym.x, yp.x, cm.x, cp.x, p.x, pn.x, fn.x);
+          kick_drift_f32<0>(k, fk, fd, c.y, c.x, c.z, ym.y, yp.y, cm.y, cp.y, p.y, pn.y, fn.y);
+          kick_drift_f32<0>(k, fk, fd, c.z, c.y, c.w, ym.z, yp.z, cm.z, cp.z, p.z, pn.z, fn.z);
+          kick_drift_f32<0>(k, fk, fd, c.w, c.z, xp, ym.w, yp.w, cm.w, cp.w, p.w, pn.w, fn.w);
+        } else {
+          kick_drift_f32<1>(k, fk, fd, c.x, xm, c.y, ym.x, yp.x, cm.x, cp.x, p.x, pn.x, fn.x);
+          kick_drift_f32<1>(k, fk, fd, c.y, c.x, c.z, ym.y, yp.y, cm.y, cp.y, p.y, pn.y, fn.y);
+          kick_drift_f32<1>(k, fk, fd, c.z, c.y, c.w, ym.z, yp.z, cm.z, cp.z, p.z, pn.z, fn.z);
+          kick_drift_f32<1>(k, fk, fd, c.w, c.z, xp, ym.w, yp.w, cm.w, cp.w, p.w, pn.w, fn.w);
+        }
+        *(float4 *)(pp + i) = pn;
+        *(float4 *)(fo + i) = fn;
+      }
+      cm = c;
+      c = cp;
+    }
+    if (MODE != MODE_STEP) {
+      Acc acc;
+      accf.to_double(acc);
+      block_store_n(acc, partials, tid, W, (size_t)it);
+    }
+  }
+}
+
 // One block per member folds that member's item records, in item order.
 __global__ void __launch_bounds__(FIN_THREADS) ens_fold(const double *__restrict__ partials,
                                                         const int *__restrict__ item_begin,
@@ -126,9 +217,36 @@ static cudaError_t ens_launch_t(int grid, const EnsMember *members, const EnsIte
   return cudaGetLastError();
 }
 
-static cudaError_t ens_launch(int ty, int mode, int grid, const EnsMember *members, const EnsItem *items, int nitems,
-                              const float *phi, float *phi_out, float *pi, const double *factors, int slot,
-                              double *partials, cudaStream_t st) {
+template <int W, int MODE>
+static cudaError_t ens_launch_x4_t(int grid, const EnsMember *members, const EnsItem *items, int nitems,
+                                   const float *phi, float *phi_out, float *pi, const double *factors, int slot,
+                                   double *partials, cudaStream_t st) {
+  ens_step_x4<W, MODE><<<grid, dim3(32, W), 0, st>>>(members, items, nitems, phi, phi_out, pi, factors, slot,
+                                                     partials);
+  return cudaGetLastError();
+}
+
+static cudaError_t ens_launch(const EnsTile &T, int mode, int grid, const EnsMember *members, const EnsItem *items,
+                              int nitems, const float *phi, float *phi_out, float *pi, const double *factors,
+                              int slot, double *partials, cudaStream_t st) {
+  const int ty = T.ty;
+  if (T.x4) {
+#define PHN_ENS4(WV, MD) return ens_launch_x4_t<WV, MD>(grid, members, items, nitems, phi, phi_out, pi, factors, slot, partials, st)
+    if (ty == 8) {
+      if (mode == MODE_STEP) PHN_ENS4(8, MODE_STEP);
+      if (mode == MODE_STEP_OBS) PHN_ENS4(8, MODE_STEP_OBS);
+      PHN_ENS4(8, MODE_OBS);
+    }
+    if (ty == 4) {
+      if (mode == MODE_STEP) PHN_ENS4(4, MODE_STEP);
+      if (mode == MODE_STEP_OBS) PHN_ENS4(4, MODE_STEP_OBS);
+      PHN_ENS4(4, MODE_OBS);
+    }
+    if (mode == MODE_STEP) PHN_ENS4(2, MODE_STEP);
+    if (mode == MODE_STEP_OBS) PHN_ENS4(2, MODE_STEP_OBS);
+    PHN_ENS4(2, MODE_OBS);
+#undef PHN_ENS4
+  }
 #define PHN_ENS(TYV, MD) return ens_launch_t<TYV, MD>(grid, members, items, nitems, phi, phi_out, pi, factors, slot, partials, st)
   if (ty == 8) {
     if (mode == MODE_STEP) PHN_ENS(8, MODE_STEP);
@@ -141,12 +259,17 @@ static cudaError_t ens_launch(int ty, int mode, int grid, const EnsMember *membe
 #undef PHN_ENS
 }
 
-static int ens_grid(int ty) {
+static int ens_grid(const EnsTile &T) {
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const void *fn = ty == 8 ? (const void *)ens_step<8, MODE_STEP> : (const void *)ens_step<4, MODE_STEP>;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 32 * ty, 0) != cudaSuccess || occ < 1) occ = 1;
+  const void *fn;
+  if (T.x4)
+    fn = T.ty == 8 ? (const void *)ens_step_x4<8, MODE_STEP>
+                   : (T.ty == 4 ? (const void *)ens_step_x4<4, MODE_STEP> : (const void *)ens_step_x4<2, MODE_STEP>);
+  else
+    fn = T.ty == 8 ? (const void *)ens_step<8, MODE_STEP> : (const void *)ens_step<4, MODE_STEP>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 32 * T.ty, 0) != cudaSuccess || occ < 1) occ = 1;
   return sms * occ;
 }
 
@@ -236,6 +359,17 @@ static int ens_set_tile(phn_ensemble *e, int t) {
     begin[m] = (int)items.size();
     const int N = e->p[m].N;
     const int cz = T.cz < N ? T.cz : N;
+    if (T.x4) {
+      // chunks of 128 W plane sites; N a multiple of 32 makes N^2 a multiple
+      // of 1024, so chunks tile every plane exactly
+      const int chunk = 128 * T.ty, NN = N * N;
+      for (int z0 = 0; z0 < N; z0 += cz)
+        for (int q0 = 0; q0 < NN; q0 += chunk) {
+          EnsItem I = {m, q0 % N, q0 / N, z0, (z0 + cz <= N) ? cz : N - z0};
+          items.push_back(I);
+        }
+      continue;
+    }
     for (int z0 = 0; z0 < N; z0 += cz)
       for (int y0 = 0; y0 < N; y0 += T.ty)
         for (int x0 = 0; x0 < N; x0 += 32) {
@@ -257,13 +391,13 @@ static int ens_set_tile(phn_ensemble *e, int t) {
     e->partial_cap = e->nitems;
   }
   e->tile = t;
-  e->grid = ens_grid(T.ty);
+  e->grid = ens_grid(T);
   ens_free_graphs(e);
   return PHN_OK;
 }
 
 static int ens_launch_step(phn_ensemble *e, int mode, int slot, int cur) {
-  CKE(ens_launch(kEnsTiles[e->tile].ty, mode, e->grid, e->d_members, e->d_items, e->nitems, e->phi[cur],
+  CKE(ens_launch(kEnsTiles[e->tile], mode, e->grid, e->d_members, e->d_items, e->nitems, e->phi[cur],
                  e->phi[1 - cur], e->pi, e->d_factors, slot, e->partials, e->stream));
   e->launches++;
   return PHN_OK;

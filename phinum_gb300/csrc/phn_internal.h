@@ -93,6 +93,16 @@ int tma_grid(const phn_params &p, int variant);
 cudaError_t launch_step_f32_tma(const Consts &k, int variant, int grid, bool obs, const float *phi, float *phi_out,
                                 float *pi, StepF s, double *partials, int *err, cudaStream_t st);
 
+// Register FP32 step with four x-sites per thread (leapfrog_x4.cu): Nc = 1,
+// N a multiple of 32; variants are block shapes and grid policies, all
+// bit-identical to the other FP32 kernels.  mode: MODE_STEP/STEP_OBS/OBS.
+bool x4_supported(const phn_params &p);
+int x4_num_variants();
+int x4_obs_variant(int variant);  // the persistent variant observation steps use
+int x4_grid(const phn_params &p, int variant);
+cudaError_t launch_step_f32_x4(const Consts &k, int variant, int grid, int mode, const float *phi, float *phi_out,
+                               float *pi, StepF s, double *partials, cudaStream_t st);
+
 // Layout conversion between the reference layout (host order, ghosts) and
 // the device SoA layout [a][z][y][x] (layout.cu).
 cudaError_t launch_from_ref(const double *ref, void *dst, int prec, int N, int Nc, cudaStream_t st);
@@ -127,6 +137,9 @@ struct phn_handle {
   int path;            // PHN_PATH_* in use for FP32 steps
   int tma_grid;        // persistent grid of the TMA step kernel (0: unsupported)
   int tma_variant;     // TMA kernel variant in use (phn_autotune picks it)
+  int x4_grid;         // grid of the x4 step kernel (0: unsupported)
+  int x4_variant;      // x4 kernel variant in use
+  int x4_obs_grid;     // grid of its observation-step variant
   int partial_cap;     // block records the partials buffer holds
   int obs_records;     // block records written by the last observation launch
   int *d_err;          // device error word of bounded waits (0: none)

@@ -31,7 +31,7 @@ def members():
     return ms, fields
 
 
-@pytest.mark.parametrize("tile", [0, 1, 3])
+@pytest.mark.parametrize("tile", [0, 1, 3, 6, 9, 10])  # scalar tiles, then x4 tiles with 8, 4, 2 warps
 def test_members_match_single_lattice_runs(tile):
     from phinum_gb300 import lattice as PL
     ms, fields = members()

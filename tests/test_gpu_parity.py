@@ -327,5 +327,48 @@ def test_autotune_keeps_state_and_picks_a_variant():
     L.check(lat.lib.phn_autotune(lat.h, 5, ctypes.byref(v), ctypes.byref(ms)))
     after = lat.download()
     assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
-    assert v.value >= 0 and ms.value > 0
+    assert v.value >= -1 and ms.value > 0  # -1: the plain kernel was fastest
     lat.close()
+
+
+@pytest.mark.parametrize("theory", [0, 1])
+@pytest.mark.parametrize("N", [32, 64, 96])
+def test_x4_path_matches_plain_path_bit_for_bit(N, theory):
+    """The four-sites-per-thread FP32 step (every variant) against the register
+    z-marching step at sizes without the TMA kernel: identical fields, SO rows
+    to FP32-summation rounding, extrema exact."""
+    import ctypes
+    import inputs
+    PL = gpu()
+    from phinum_gb300 import _lib as L
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 60 + theory, phi0=(-1) ** theory * 6 ** 0.5)
+    phi, pi = O.to_ref_layout(phi_i), O.to_ref_layout(pi_i)
+    kw = dict(theory=0) if theory == 0 else dict(theory=1, mass_mode=-1, lambda_mode=1, h=0.12247)
+    lat = PL.Lattice(PL.Params(N=N, precision=1, **kw))
+    nv = ctypes.c_int()
+    L.check(lat.lib.phn_num_variants(lat.h, ctypes.byref(nv)))
+    lat.close()
+    assert nv.value >= 2
+    out = {}
+    for variant in [None] + list(range(nv.value)):
+        lat = PL.Lattice(PL.Params(N=N, precision=1, **kw))
+        if variant is None:
+            L.check(lat.lib.phn_set_path(lat.h, L.PATH_PLAIN))
+        else:
+            L.check(lat.lib.phn_set_variant(lat.h, variant))
+            path = ctypes.c_int()
+            L.check(lat.lib.phn_get_path(lat.h, ctypes.byref(path)))
+            assert path.value == L.PATH_X4
+        lat.upload(phi, pi)
+        rows = lat.run_loop(120, 0.5)
+        lat.evolve(7)
+        avg = lat.volume_averages()
+        out[variant] = (rows, avg) + lat.download()
+        lat.close()
+    r0, a0, f0, p0 = out[None]
+    for key, (r1, a1, f1, p1) in out.items():
+        assert np.array_equal(f0, f1) and np.array_equal(p0[N * N:-N * N], p1[N * N:-N * N]), key
+        assert np.array_equal(r0[:, 17:23], r1[:, 17:23]), key
+        assert np.array_equal(a0[17:23], a1[17:23]), key
+        np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
+        np.testing.assert_allclose(a0[9:17], a1[9:17], rtol=1e-6, atol=1e-9)
