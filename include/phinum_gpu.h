@@ -149,6 +149,28 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
  * 1 <= nbins <= 1024; F, K, Q hold nbins*Nc, counts nbins. */
 int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double *Q, int *counts);
 
+/* SetInitialConditions() (initialconditions.cpp:45-723) for `initialize 3`,
+ * static box, no charge, on the device: drand48's stream from srand48(seed)
+ * (the reference seeds with time(NULL)*(ID+1), initialconditions.cpp:16),
+ * consumed in the reference's mode order -- two phases and one polar
+ * Box-Muller acceptance per mode and component -- then ensureRealResult and
+ * fftPtoX (clusterfft.cpp:55-182) with cuFFT.  Writes phi and pi of the
+ * handle (the clock is not reset).  The stream and its assignment to modes
+ * are exact; amplitudes agree with the C library's log/sin/cos to rounding.
+ * N even.  Parameters are the reference's globals of the same names. */
+typedef struct phn_ic_params {
+  long seed;            /* the srand48 argument */
+  int justnoise;        /* justnoise */
+  double QS, scale2;    /* QS, scale2 (0: no cutoff) */
+  double amplitude;     /* Amplitude */
+  double noise;         /* Noise */
+  double phi0[2];       /* phi0_0, phi0_1 (homogeneous values of components 0, 1) */
+  double pi0[2];        /* pi0_0, pi0_1 */
+  double m2_long;       /* M2_long (= M_sqr without tadpole renormalisation, renormalization.cpp:17) */
+  double m2_trans;      /* M2_trans (components a >= 1) */
+} phn_ic_params;
+int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic);
+
 /* Full_Analysis() seeding from an empty history (islands.cpp:72-279,778-840):
  * mask (mode), 6-connectivity, x and y periodic, z open as on one rank unless
  * z_periodic.  labels (optional, reference layout, -1 outside islands) and up

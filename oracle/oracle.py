@@ -60,6 +60,17 @@ class _CClock(ctypes.Structure):
                 ("steps", _I), ("pad_", _I)]
 
 
+class _CIc(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_long), ("justnoise", _I), ("pad_", _I), ("QS", _D), ("scale2", _D),
+                ("amplitude", _D), ("noise", _D), ("phi0", _D * 2), ("pi0", _D * 2), ("m2_long", _D),
+                ("m2_trans", _D)]
+
+
+# SetInitialConditions parameters (initialize 3): the reference globals' names
+IC_DEFAULTS = dict(seed=1, justnoise=0, QS=1.0, scale2=1.0, amplitude=0.0, noise=0.5, phi0=(0.0, 0.0),
+                   pi0=(0.0, 0.0))
+
+
 def _cp(p: Params) -> _CParams:
     return _CParams(p.N, p.Nc, p.theory, p.mass_mode, p.lambda_mode, 0, p.a, p.dt, p.T0,
                     p.m_sqr, p.kappa, p.h)
@@ -142,6 +153,8 @@ def _load(fast: bool = False):
         lib.orc_spectrum.restype = _I
         lib.orc_spectrum_uniform.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _I, _PD, _PD, _PD, _PI]
         lib.orc_spectrum_uniform.restype = _I
+        lib.orc_initial_conditions.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CIc), _PD, _PD]
+        lib.orc_initial_conditions.restype = _I
         lib.orc_spectrum_columns.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _PD, _PI, _I, _PD]
         lib.orc_islands.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _D, _I, _I, _PI, _PD, _I]
         lib.orc_islands.restype = _I
@@ -225,6 +238,17 @@ def spectrum_uniform(p: Params, phi: np.ndarray, pi: np.ndarray, nbins: int = 64
     return F, K, Q, C
 
 
+def initial_conditions(p: Params, **kw):
+    """SetInitialConditions (initialize 3) with srand48(seed): Phi, Pi in the
+    reference layout (Pi's ghost slabs zero).  M2_long = M2_trans = M_sqr."""
+    q = dict(IC_DEFAULTS, **kw)
+    c = _CIc(int(q["seed"]), int(q["justnoise"]), 0, q["QS"], q["scale2"], q["amplitude"], q["noise"],
+             (_D * 2)(*q["phi0"]), (_D * 2)(*q["pi0"]), p.m_sqr, p.m_sqr)
+    phi, pi = np.zeros(field_len(p)), np.zeros(field_len(p))
+    _load().orc_initial_conditions(ctypes.byref(_cp(p)), ctypes.byref(c), _ptr(phi), _ptr(pi))
+    return phi, pi
+
+
 def spectrum_columns(p: Params, F, K, Q, C) -> np.ndarray:
     nb = C.size
     cols = np.zeros((nb, 7))
@@ -291,11 +315,23 @@ class Reference:
         lib.ref_spectrum.argtypes = [_PD, _PD, _PD, _PI]
         lib.ref_islands.argtypes = [_D, _PI, _PD, _I]
         lib.ref_islands.restype = _I
+        lib.ref_initial_conditions.argtypes = [ctypes.c_long, _I, _D, _D, _D, _D, _D, _D, _D, _D]
+        lib.ref_initial_conditions.restype = _I
         self.lib = lib
         r = lib.ref_init(p.N, p.Nc, p.a, p.dt, p.T0, p.mass_mode, p.m_sqr, p.lambda_mode, 1.0,
                          p.kappa, p.h)
         if r != 0:
             raise RuntimeError(f"ref_init failed ({r}); one Reference per process")
+
+    def initial_conditions(self, **kw):
+        """The reference's SetInitialConditions with srand48(seed); returns Phi, Pi."""
+        q = dict(IC_DEFAULTS, **kw)
+        r = self.lib.ref_initial_conditions(int(q["seed"]), int(q["justnoise"]), q["QS"], q["scale2"],
+                                            q["amplitude"], q["noise"], q["phi0"][0], q["phi0"][1],
+                                            q["pi0"][0], q["pi0"][1])
+        if r != 0:
+            raise RuntimeError("ref_initial_conditions failed")
+        return self.get_fields()
 
     def set_fields(self, phi, pi):
         self.lib.ref_set_fields(_ptr(np.ascontiguousarray(phi, np.float64)),

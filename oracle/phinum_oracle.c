@@ -19,6 +19,9 @@
  *                        Calculate_CorrelationFunctions, fftXtoP_direct
  *                                                     momentumspace.cpp:32-278,
  *                                                     clusterfft.cpp:185-225
+ *   orc_initial_conditions  SetInitialConditions (initialize 3), ensureRealResult,
+ *                        fftPtoX            initialconditions.cpp:14-723,
+ *                                           clusterfft.cpp:10-16,55-182
  *   orc_islands          is_island()/BFS()/Full_Analysis() scan
  *                                                     islands.cpp:72-279,778-840
  * for theories 0 (phi^4 + phi^6) and 1 (phi^4 + linear h), static box, one
@@ -35,6 +38,7 @@
  * Nc*N*N*(N+2) doubles, index Nc*(x + N*y + N*N*z) + a, z-slabs 0 and N+1
  * are ghosts that mirror slabs N and 1.
  */
+#define _DEFAULT_SOURCE /* srand48 / drand48 under -std=c99 */
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -447,6 +451,157 @@ int orc_spectrum_uniform(const orc_params *p, const double *Phi, const double *P
   }
   free(fr); free(fi); free(gr); free(gi);
   return nbins;
+}
+
+/* ------------------------------------------------------ initial conditions */
+/* randGen::Gauss (initialconditions.cpp:27-41): polar Box-Muller on drand48,
+ * the second value cached for the next call. */
+static int ic_on = 0;
+static double ic_gauss2 = 0.0;
+static double ic_gauss(void) {
+  if (ic_on == 1) { ic_on = 0; return ic_gauss2; }
+  double x, y, r, c, s, g1;
+  int accept = 0;
+  while (accept == 0) {
+    x = 2.0 * drand48() - 1.0; y = 2.0 * drand48() - 1.0;
+    r = sqrt(sqr(x) + sqr(y));
+    if (r < 1.0) accept = 1;
+  }
+  c = x / r; s = y / r;
+  g1 = c * sqrt(-2.0 * log(sqr(r)));
+  ic_gauss2 = (s / c) * g1;
+  ic_on = 1;
+  return g1;
+}
+
+/* sgn of clusterfft.cpp:10-16 (sgn(0) = -1). */
+static int ic_sgn(double x) { return x > 0 ? 1 : -1; }
+
+/* ensureRealResult (clusterfft.cpp:55-139) for one rank: F[py + px M + pz N M]. */
+static void ic_ensure_real(int N, double *re, double *im) {
+  const int M = N / 2 + 1;
+  for (int pz = 0; pz < N; pz++)
+    for (int px = 0; px < N; px++)
+      for (int py = 0; py < M; py++) {
+        const int mpz = mod(N - pz, N), mpx = mod(N - px, N), mpy = mod(N - py, N);
+        if (mpy != py) continue;
+        const long i = py + (long)px * M + (long)pz * N * M;
+        if (px == mpx && pz == mpz) {
+          const double v = hypot(re[i], im[i]) * ic_sgn(re[i]);
+          re[i] = v; im[i] = 0.0;
+        } else {
+          const long j = mpy + (long)mpx * M + (long)mpz * N * M;
+          re[j] = re[i]; im[j] = -im[i];
+        }
+      }
+}
+
+/* fftPtoX (clusterfft.cpp:148-182): the half spectrum [pz][px][py] is
+ * completed by Hermitian symmetry and transformed with exp(+2 pi i ...);
+ * out[x + N y + N^2 z] = X(z, x, y) / L^3.  The inverse transform is the
+ * conjugate of the forward transform of the conjugate. */
+static void ic_fft_ptox(const orc_params *p, const double *hre, const double *him, double *out) {
+  const int N = p->N, M = N / 2 + 1;
+  const long NN = (long)N * N, V = NN * N;
+  double *re = (double *)malloc(sizeof(double) * V), *im = (double *)malloc(sizeof(double) * V);
+  double *wr = (double *)malloc(sizeof(double) * N), *wi = (double *)malloc(sizeof(double) * N);
+  /* full[py + N px + N^2 pz] */
+  for (int pz = 0; pz < N; pz++)
+    for (int px = 0; px < N; px++)
+      for (int py = 0; py < N; py++) {
+        double vr, vi;
+        if (py < M) {
+          const long i = py + (long)px * M + (long)pz * N * M;
+          vr = hre[i]; vi = him[i];
+        } else {
+          const long i = (N - py) + (long)mod(N - px, N) * M + (long)mod(N - pz, N) * N * M;
+          vr = hre[i]; vi = -him[i];
+        }
+        re[py + N * px + NN * pz] = vr;
+        im[py + N * px + NN * pz] = -vi; /* conjugate in */
+      }
+  for (long r = 0; r < NN; r++) dft_line(re + r * N, im + r * N, N, 1, wr, wi);
+  for (int z = 0; z < N; z++)
+    for (int y = 0; y < N; y++) dft_line(re + y + NN * z, im + y + NN * z, N, N, wr, wi);
+  for (long r = 0; r < NN; r++) dft_line(re + r, im + r, N, NN, wr, wi);
+  const double Norm = sqr(p->a * N) * N * p->a;
+  /* conjugate out: the real part is unchanged; re[y + N x + N^2 z] = X(z, x, y) */
+  for (int z = 0; z < N; z++)
+    for (int y = 0; y < N; y++)
+      for (int x = 0; x < N; x++) out[x + N * y + NN * z] = re[y + N * x + NN * z] / Norm;
+  free(re); free(im); free(wr); free(wi);
+}
+
+/* SetInitialConditions (initialconditions.cpp:45-723), initialize 3,
+ * expansion 0, withcharge 0, one rank.  Phi/Pi in the reference layout;
+ * Phi's ghost slabs exchanged, Pi's left as they were.  Returns 0. */
+int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, double *Pi) {
+  const int N = p->N, Nc = p->Nc, M = N / 2 + 1;
+  const long NM = (long)N * N * M, NN = (long)N * N;
+  const double a = p->a;
+  double *Are = (double *)calloc((size_t)Nc * NM, sizeof(double)), *Aim = (double *)calloc((size_t)Nc * NM, sizeof(double));
+  double *Ere = (double *)calloc((size_t)Nc * NM, sizeof(double)), *Eim = (double *)calloc((size_t)Nc * NM, sizeof(double));
+  double *X = (double *)malloc(sizeof(double) * NN * N);
+  srand48(ic->seed);
+  ic_on = 0;
+  for (int pz = 0; pz < N; pz++) {
+    double nu;
+    if (pz == 0) nu = 0;
+    else if (pz < N / 2 + 1) nu = 2.0 / (a) * sin((pz) * acos(-1.) / N);
+    else nu = -2.0 / (a) * sin((pz) * acos(-1.) / N);
+    for (int px = 0; px < N; px++) {
+      double ppx;
+      if (px < N / 2 + 1) ppx = 2.0 / (a) * sin(px * acos(-1.) / N);
+      else ppx = -2.0 / (a) * sin(px * acos(-1.) / N);
+      for (int py = 0; py < M; py++) {
+        const double ppy = 2.0 / (a) * sin(py * acos(-1.) / N);
+        const double pt = sqrt(sqr(ppx) + sqr(ppy));
+        const double psqr = sqr(pt) + sqr(nu);
+        const long posMom = py + (long)px * M + (long)pz * N * M;
+        for (int c = 0; c < Nc; c++) {
+          const double phase1 = 2.0 * acos(-1.) * drand48(), phase2 = 2.0 * acos(-1.) * drand48();
+          const double gauss1 = fabs(ic_gauss()), gauss2 = fabs(ic_gauss());
+          const double pchisqr = sqr(pt) + sqr(nu);
+          double occ;
+          if (ic->justnoise == 0) {
+            if (pchisqr < ic->QS * ic->QS) occ = ic->amplitude + ic->noise;
+            else if (ic->scale2 == 0) occ = ic->noise;
+            else occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
+          } else {
+            if (ic->scale2 == 0) occ = ic->noise;
+            else occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
+          }
+          const double omega = c == 0 ? sqrt(psqr + ic->m2_long) : sqrt(psqr + ic->m2_trans);
+          const double s1 = sqrt(occ) * gauss1, s2 = sqrt(occ) * gauss2;
+          const long o = (long)c * NM + posMom;
+          if (fabs(omega) < 1e-8) {
+            Are[o] = Aim[o] = Ere[o] = Eim[o] = 0.0;
+          } else {
+            const double so = sqrt(omega);
+            Are[o] = s1 * cos(phase1) / so; Aim[o] = s1 * sin(phase1) / so;
+            Ere[o] = s2 * cos(phase2) * so; Eim[o] = s2 * sin(phase2) * so;
+          }
+        }
+      }
+    }
+  }
+  const double NormFactor = sqrt(sqr(N * a) * N * a);
+  for (int c = 0; c < Nc; c++) {
+    ic_ensure_real(N, Are + (long)c * NM, Aim + (long)c * NM);
+    ic_ensure_real(N, Ere + (long)c * NM, Eim + (long)c * NM);
+  }
+  for (int f = 0; f < 2; f++)
+    for (int c = 0; c < Nc; c++) {
+      ic_fft_ptox(p, (f == 0 ? Are : Ere) + (long)c * NM, (f == 0 ? Aim : Eim) + (long)c * NM, X);
+      const double off = c < 2 ? (f == 0 ? ic->phi0[c] : ic->pi0[c]) : 0.0;
+      double *dst = f == 0 ? Phi : Pi;
+      for (int z = 0; z < N; z++)
+        for (int y = 0; y < N; y++)
+          for (int x = 0; x < N; x++) dst[c + pos3(p, x, y, z + 1)] = X[x + N * y + NN * z] * NormFactor + off;
+    }
+  orc_exchange(p, Phi); /* Communication::exchange moves Phi only (comm.cpp:63-78) */
+  free(Are); free(Aim); free(Ere); free(Eim); free(X);
+  return 0;
 }
 
 /* Print_fp (momentumspace.cpp:280-384) per-bin columns, for bins with a

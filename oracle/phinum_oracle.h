@@ -51,6 +51,17 @@ typedef struct orc_island {
   double index, size, volume, pot_en, kin_en, grad_en, av_phi, peak_pos, peak_value, seed_pos;
 } orc_island;
 
+/* Parameters of SetInitialConditions for `initialize 3` (the reference's
+ * globals of the same names, parameters.cpp; M2_long/M2_trans as
+ * renormalization.cpp:17-18 sets them). */
+typedef struct orc_ic {
+  long seed;  /* srand48 argument */
+  int justnoise, pad_;
+  double QS, scale2, amplitude, noise;
+  double phi0[2], pi0[2];
+  double m2_long, m2_trans;
+} orc_ic;
+
 int orc_version(void);
 int orc_max_threads(void);
 void orc_reset(const orc_params *p, orc_clock *c);
@@ -60,6 +71,7 @@ void orc_averages(const orc_params *p, const orc_clock *c, const double *Phi, co
 int orc_run_loop(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int nsteps, double tso,
                  orc_row *rows, int max_rows, int nthreads);
 void orc_spectrum_bins(const orc_params *p, int *nbins, double *binsize);
+int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, double *Pi);
 int orc_spectrum(const orc_params *p, const double *Phi, const double *Pi, double *F, double *K, double *Q,
                  int *counts);
 int orc_spectrum_uniform(const orc_params *p, const double *Phi, const double *Pi, int nbins, double *F, double *K,

@@ -51,6 +51,16 @@ using namespace std;
 #include "islands.cpp"
 #include "renormalization.cpp"
 
+/* SetInitialConditions seeds with srand48(time(NULL)*(ID+1))
+ * (initialconditions.cpp:16).  While its source is included, `time` names a
+ * function returning a seed the harness chooses, so the stream is
+ * reproducible; the file itself is compiled unchanged. */
+static long g_ref_seed = 0;
+static time_t phn_ref_seed_clock(time_t *) { return (time_t)g_ref_seed; }
+#define time(x) phn_ref_seed_clock(x)
+#include "initialconditions.cpp"
+#undef time
+
 /* ---- extern "C" surface for the golden-vector generator -------------------- */
 namespace {
 bool g_ready = false;
@@ -229,6 +239,26 @@ int ref_islands(double thres, int *labels, double *stats, int max_islands) {
     s[7] = (double)B.Peak_value.back();
   }
   return count;
+}
+
+/* SetInitialConditions() (initialize 3) with srand48(seed); the fields land
+ * in LocalLattice::Phi/Pi (read them with ref_get_fields). */
+int ref_initial_conditions(long seed, int justnoise_, double qs, double scale2_, double amplitude, double noise,
+                           double phi00, double phi01, double pi00, double pi01) {
+  if (!g_ready) return -1;
+  g_ref_seed = seed;
+  justnoise = justnoise_;
+  QS = (pseudo_double)qs;
+  scale2 = (pseudo_double)scale2_;
+  Amplitude = (pseudo_double)amplitude;
+  Noise = (pseudo_double)noise;
+  phi0_0 = (pseudo_double)phi00;
+  phi0_1 = (pseudo_double)phi01;
+  pi0_0 = (pseudo_double)pi00;
+  pi0_1 = (pseudo_double)pi01;
+  randGen::on = 0;
+  SetInitialConditions();
+  return 0;
 }
 
 } /* extern "C" */

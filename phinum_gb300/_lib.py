@@ -29,6 +29,11 @@ class PhnParams(ctypes.Structure):
                 ("h", _D)]
 
 
+class PhnIcParams(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_long), ("justnoise", _I), ("QS", _D), ("scale2", _D), ("amplitude", _D),
+                ("noise", _D), ("phi0", _D * 2), ("pi0", _D * 2), ("m2_long", _D), ("m2_trans", _D)]
+
+
 class PhnAverages(ctypes.Structure):
     _fields_ = [("t", _D), ("phi", _D * MAX_NC), ("pi", _D * MAX_NC), ("phi2", _D), ("pi2", _D),
                 ("phipi", _D), ("phi4", _D), ("phi6", _D), ("energy", _D), ("interaction", _D),
@@ -68,6 +73,7 @@ _SIGS = {
     "phn_spectrum_bins": (_I, [ctypes.c_void_p, _PI, _PD]),
     "phn_spectrum": (_I, [ctypes.c_void_p, _PD, _PD, _PD, _PI, _I]),
     "phn_spectrum_uniform": (_I, [ctypes.c_void_p, _I, _PD, _PD, _PD, _PI]),
+    "phn_initial_conditions": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams)]),
     "phn_islands": (_I, [ctypes.c_void_p, _D, _I, _I, _PI, _PD, _I, _PI]),
     "phn_set_path": (_I, [ctypes.c_void_p, _I]),
     "phn_get_path": (_I, [ctypes.c_void_p, _PI]),

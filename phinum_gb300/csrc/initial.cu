@@ -1,0 +1,446 @@
+// Initial conditions on the GPU: SetInitialConditions for `initialize 3`,
+// static box, no charge (initialconditions.cpp:45-723, clusterfft.cpp:55-182),
+// with the reference's own random stream.
+//
+// The reference draws from drand48 (seeded by srand48, initialconditions.cpp:
+// 14-22) in mode order (pz, px, py <= N/2, component): per mode two phases
+// (two draws), then two Gaussians from one polar Box-Muller acceptance
+// (Gauss(), :27-41: pairs of draws until the point falls inside the unit
+// disc; the second Gaussian of the pair is cached for the next call).  Every
+// mode consumes 2 + 2k draws, so every mode starts on an even draw and the
+// stream splits into pairs: one phase pair, then trial pairs up to the first
+// accepted one.  Which pair belongs to which mode is a two-state automaton
+// over the acceptance flags ("next pair is a phase pair" / "a trial pair");
+// it is evaluated with a parallel prefix over chunks of pairs.
+//
+//   ic_pairs    drand48 by jump-ahead (X <- A^k X + C_k mod 2^48): each thread
+//               one chunk of pairs; stores the pairs (exact doubles X / 2^48),
+//               and the chunk's automaton transition for both entry states
+//   ic_scan_*   prefix over chunks: per block in shared memory, then over
+//               blocks on one thread, then the entry state and first mode of
+//               every chunk
+//   ic_assign   each chunk re-walks its pairs and records, per mode, the phase
+//               pair and the accepted pair
+//   ic_modes    amplitudes in FP64 with the reference's expressions and order
+//               (occupation, Omega, F1, F2, A = F1/sqrt(Omega), E = F2 sqrt(Omega))
+//   ic_reality  ensureRealResult (clusterfft.cpp:55-139) on the py = 0 and
+//               py = N/2 planes: the mode visited first sets its partner
+//   cuFFT Z2D   fftPtoX (clusterfft.cpp:148-182): the complex array is
+//               [pz][px][py], so lattice y is the halved axis
+//   ic_store    X / L^3 * sqrt(L^3) + phi0 into the handle's [z][y][x] fields
+//               (a shared-memory transpose of x and y)
+//
+// The stream, the acceptance decisions and the mode assignment are exact;
+// the amplitudes use CUDA's log/sin/cos, which may differ from the C
+// library's in the last bit, and cuFFT rounds differently from FFTW.
+#include <cufft.h>
+#include <math.h>
+
+#include "phn_internal.h"
+
+namespace phn {
+
+constexpr unsigned long long LCG_A = 0x5DEECE66DULL, LCG_C = 0xBULL, LCG_MASK = (1ULL << 48) - 1;
+constexpr int IC_CHUNK = 64;     // pairs per thread in ic_pairs / ic_assign
+constexpr int IC_THREADS = 256;  // chunks per scan block
+
+struct Lcg {  // X -> a X + c (mod 2^48)
+  unsigned long long a, c;
+};
+
+__host__ __device__ inline Lcg lcg_then(Lcg f, Lcg g) {  // f first, then g
+  Lcg h;
+  h.a = (g.a * f.a) & LCG_MASK;
+  h.c = (g.a * f.c + g.c) & LCG_MASK;
+  return h;
+}
+
+// k steps of the drand48 recurrence
+__host__ __device__ inline Lcg lcg_pow(unsigned long long k) {
+  Lcg r = {1, 0}, b = {LCG_A, LCG_C};
+  while (k) {
+    if (k & 1) r = lcg_then(r, b);
+    b = lcg_then(b, b);
+    k >>= 1;
+  }
+  return r;
+}
+
+// Automaton over pairs: state 0 = the next pair is a mode's phase pair,
+// state 1 = the next pair is a Box-Muller trial.  A transition records, for
+// each entry state, the exit state and the number of modes completed.
+struct Trans {
+  unsigned char e[2];
+  unsigned int n[2];
+};
+
+__device__ __forceinline__ Trans trans_id() {
+  Trans t;
+  t.e[0] = 0;
+  t.e[1] = 1;
+  t.n[0] = t.n[1] = 0;
+  return t;
+}
+
+__device__ __forceinline__ Trans trans_then(const Trans &f, const Trans &g) {  // f first
+  Trans h;
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    h.e[s] = g.e[f.e[s]];
+    h.n[s] = f.n[s] + g.n[f.e[s]];
+  }
+  return h;
+}
+
+// The reference's acceptance test (initialconditions.cpp:33-35) in IEEE
+// operations without contraction: x = 2u - 1, y = 2v - 1, sqrt(x^2 + y^2) < 1.
+__device__ __forceinline__ bool accepted(double u, double v) {
+  const double x = __dsub_rn(__dmul_rn(2.0, u), 1.0), y = __dsub_rn(__dmul_rn(2.0, v), 1.0);
+  const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)));
+  return r < 1.0;
+}
+
+// Stream pairs [chunk * IC_CHUNK, ...) of the drand48 stream that starts in
+// state x0 (srand48); draw k is X_{k+1} / 2^48.
+__global__ void ic_pairs(unsigned long long x0, long long npairs, double2 *__restrict__ uv, Trans *__restrict__ trans,
+                         long long nchunks) {
+  const long long chunk = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (chunk >= nchunks) return;
+  const long long p0 = chunk * IC_CHUNK;
+  const Lcg jump = lcg_pow(2ULL * (unsigned long long)p0);
+  unsigned long long x = (jump.a * x0 + jump.c) & LCG_MASK;
+  Trans t = trans_id();
+  const long long p1 = min(p0 + IC_CHUNK, npairs);
+  for (long long p = p0; p < p1; ++p) {
+    x = (LCG_A * x + LCG_C) & LCG_MASK;
+    const double u = (double)x * 0x1p-48;
+    x = (LCG_A * x + LCG_C) & LCG_MASK;
+    const double v = (double)x * 0x1p-48;
+    uv[p] = make_double2(u, v);
+    const bool acc = accepted(u, v);
+    // one pair: state 0 -> 1; state 1 -> 0 with a mode completed if accepted
+    Trans step;
+    step.e[0] = 1;
+    step.n[0] = 0;
+    step.e[1] = acc ? 0 : 1;
+    step.n[1] = acc ? 1 : 0;
+    t = trans_then(t, step);
+  }
+  trans[chunk] = t;
+}
+
+// Exclusive prefix of the chunk transitions inside each block (shared-memory
+// Hillis-Steele scan) and the block's total.
+__global__ void ic_scan_blocks(const Trans *__restrict__ trans, long long nchunks, Trans *__restrict__ excl,
+                               Trans *__restrict__ block_total) {
+  __shared__ Trans sh[2][IC_THREADS];
+  const long long i = blockIdx.x * (long long)IC_THREADS + threadIdx.x;
+  Trans mine = i < nchunks ? trans[i] : trans_id();
+  int cur = 0;
+  sh[cur][threadIdx.x] = mine;
+  __syncthreads();
+  for (int off = 1; off < IC_THREADS; off <<= 1) {
+    Trans v = sh[cur][threadIdx.x];
+    if (threadIdx.x >= off) v = trans_then(sh[cur][threadIdx.x - off], v);
+    sh[1 - cur][threadIdx.x] = v;
+    cur = 1 - cur;
+    __syncthreads();
+  }
+  // sh[cur] holds inclusive prefixes
+  if (i < nchunks) excl[i] = threadIdx.x == 0 ? trans_id() : sh[cur][threadIdx.x - 1];
+  if (threadIdx.x == IC_THREADS - 1) block_total[blockIdx.x] = sh[cur][threadIdx.x];
+}
+
+// Entry state and modes completed before each block, from the start state 0.
+__global__ void ic_scan_top(const Trans *__restrict__ block_total, long long nblocks, unsigned char *__restrict__ bstate,
+                            unsigned long long *__restrict__ bmodes) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  unsigned char s = 0;
+  unsigned long long n = 0;
+  for (long long b = 0; b < nblocks; ++b) {
+    bstate[b] = s;
+    bmodes[b] = n;
+    const Trans &t = block_total[b];
+    n += t.n[s];
+    s = t.e[s];
+  }
+  bstate[nblocks] = s;
+  bmodes[nblocks] = n;
+}
+
+// Each chunk re-walks its pairs from its entry state and records, for every
+// mode it touches, the phase pair and the accepted pair.
+__global__ void ic_assign(const double2 *__restrict__ uv, long long npairs, long long nchunks,
+                          const Trans *__restrict__ excl, const unsigned char *__restrict__ bstate,
+                          const unsigned long long *__restrict__ bmodes, long long nmodes,
+                          long long *__restrict__ phase_pair, long long *__restrict__ acc_pair) {
+  const long long chunk = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (chunk >= nchunks) return;
+  const long long b = chunk / IC_THREADS;
+  const Trans &pre = excl[chunk];
+  const unsigned char sb = bstate[b];
+  int s = pre.e[sb];
+  unsigned long long m = bmodes[b] + pre.n[sb];
+  const long long p0 = chunk * IC_CHUNK, p1 = min(p0 + IC_CHUNK, npairs);
+  for (long long p = p0; p < p1 && (long long)m < nmodes; ++p) {
+    if (s == 0) {
+      phase_pair[m] = p;
+      s = 1;
+    } else {
+      const double2 w = uv[p];
+      if (accepted(w.x, w.y)) {
+        acc_pair[m] = p;
+        ++m;
+        s = 0;
+      }
+    }
+  }
+}
+
+struct IcConsts {
+  int N, Nc, justnoise;
+  double a, QS, scale2, amplitude, noise, m2_long, m2_trans;
+};
+
+// Per-axis lattice momentum as initialconditions.cpp:88-113 writes it.
+__device__ __forceinline__ double ic_p(int n, int N, double a) {
+  const double s = sin(n * acos(-1.) / N);
+  return n < N / 2 + 1 ? 2.0 / a * s : -2.0 / a * s;
+}
+
+// One (mode, component): initialconditions.cpp:339-569 (initialize 3,
+// expansion 0, withcharge 0).  A and E are [a][pz][px][py] complex arrays.
+__global__ void ic_modes(const IcConsts k, const double2 *__restrict__ uv, const long long *__restrict__ phase_pair,
+                         const long long *__restrict__ acc_pair, long long nmodes, double2 *__restrict__ A,
+                         double2 *__restrict__ E) {
+  const long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (m >= nmodes) return;
+  const int N = k.N, M = N / 2 + 1;
+  const int a = (int)(m % k.Nc);
+  const long long pos = m / k.Nc;  // py + px M + pz N M: the mode loop order
+  const int py = (int)(pos % M), px = (int)((pos / M) % N), pz = (int)(pos / ((long long)M * N));
+  const double nu = pz == 0 ? 0.0 : ic_p(pz, N, k.a);
+  const double ppx = ic_p(px, N, k.a);
+  const double ppy = 2.0 / k.a * sin(py * acos(-1.) / N);
+  const double pt = __dsqrt_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)));
+  const double psqr = __dadd_rn(__dmul_rn(pt, pt), __dmul_rn(nu, nu));
+  // phases and Gaussians (initialconditions.cpp:27-41, 344-349)
+  const double2 ph = uv[phase_pair[m]], g = uv[acc_pair[m]];
+  const double two_pi = __dmul_rn(2.0, acos(-1.));
+  const double phase1 = __dmul_rn(two_pi, ph.x), phase2 = __dmul_rn(two_pi, ph.y);
+  const double x = __dsub_rn(__dmul_rn(2.0, g.x), 1.0), y = __dsub_rn(__dmul_rn(2.0, g.y), 1.0);
+  const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)));
+  const double c = __ddiv_rn(x, r), s = __ddiv_rn(y, r);
+  const double g1 = __dmul_rn(c, __dsqrt_rn(__dmul_rn(-2.0, log(__dmul_rn(r, r)))));
+  const double g2 = __dmul_rn(__ddiv_rn(s, c), g1);
+  const double gauss1 = fabs(g1), gauss2 = fabs(g2);
+  // occupation (initialconditions.cpp:442-497) and Omega (:499-505)
+  const double pchisqr = psqr;
+  double occ;
+  const double root = __dsqrt_rn(pchisqr);
+  const double plateau = k.scale2 == 0 ? k.noise : (root < k.scale2 ? k.noise : 0.0);
+  if (k.justnoise == 0)
+    occ = pchisqr < __dmul_rn(k.QS, k.QS) ? __dadd_rn(k.amplitude, k.noise) : plateau;
+  else
+    occ = plateau;
+  const double omega = __dsqrt_rn(__dadd_rn(psqr, a == 0 ? k.m2_long : k.m2_trans));
+  // F = sqrt(occ) g (cos th, sin th); A = F1 / sqrt(Omega), E = F2 sqrt(Omega)
+  const double amp1 = __dmul_rn(__dsqrt_rn(occ), gauss1), amp2 = __dmul_rn(__dsqrt_rn(occ), gauss2);
+  double2 fa = make_double2(0.0, 0.0), fe = make_double2(0.0, 0.0);
+  if (!(fabs(omega) < 1e-8)) {
+    const double so = __dsqrt_rn(omega);
+    fa = make_double2(__ddiv_rn(__dmul_rn(amp1, cos(phase1)), so), __ddiv_rn(__dmul_rn(amp1, sin(phase1)), so));
+    fe = make_double2(__dmul_rn(__dmul_rn(amp2, cos(phase2)), so), __dmul_rn(__dmul_rn(amp2, sin(phase2)), so));
+  }
+  const size_t o = (size_t)a * N * N * M + ((size_t)pz * N + px) * M + py;
+  A[o] = fa;
+  E[o] = fe;
+}
+
+// ensureRealResult on the py = 0 and py = N/2 planes (clusterfft.cpp:55-139):
+// the mode visited first in (pz, px) order sets its partner to its
+// conjugate; a self-conjugate mode becomes |F| sgn(Re F) (sgn(0) = -1,
+// clusterfft.cpp:10-16).
+__global__ void ic_reality(double2 *__restrict__ F, int N, int Nc) {
+  const int M = N / 2 + 1;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long per = 2LL * N * N;
+  if (t >= per * Nc) return;
+  const int a = (int)(t / per);
+  const long long r = t % per;
+  const int py = (r / ((long long)N * N)) == 0 ? 0 : N / 2;
+  const int pz = (int)((r / N) % N), px = (int)(r % N);
+  const int mpz = (N - pz) % N, mpx = (N - px) % N;
+  double2 *base = F + (size_t)a * N * N * M;
+  const size_t i = ((size_t)pz * N + px) * M + py;
+  if (pz == mpz && px == mpx) {
+    const double2 v = base[i];
+    const double mag = hypot(v.x, v.y);
+    base[i] = make_double2(v.x > 0 ? mag : -mag, 0.0);
+  } else if (pz < mpz || (pz == mpz && px < mpx)) {
+    const double2 v = base[i];
+    base[((size_t)mpz * N + mpx) * M + py] = make_double2(v.x, -v.y);
+  }
+}
+
+// out[z][y][x] = X[z][x][y] * scale + offset: 32 x 32 tiles through shared memory.
+template <typename T>
+__global__ void ic_store(const double *__restrict__ X, T *__restrict__ out, int N, double scale, double offset) {
+  __shared__ double tile[32][33];
+  const int z = blockIdx.z;
+  const int x0 = blockIdx.y * 32, y0 = blockIdx.x * 32;
+  const size_t plane = (size_t)z * N * N;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int x = x0 + j, y = y0 + threadIdx.x;
+    if (x < N && y < N) tile[j][threadIdx.x] = X[plane + (size_t)x * N + y];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int y = y0 + j, x = x0 + threadIdx.x;
+    if (x < N && y < N) out[plane + (size_t)y * N + x] = (T)(tile[threadIdx.x][j] * scale + offset);
+  }
+}
+
+}  // namespace phn
+
+using namespace phn;
+
+extern "C" {
+
+int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
+  if (!h || !ic) return set_error(PHN_ERR_INVALID, "NULL argument");
+  const int N = h->p.N, Nc = h->p.Nc;
+  if (N % 2 != 0) return set_error(PHN_ERR_UNSUPPORTED, "initial conditions need an even N");
+  const int M = N / 2 + 1;
+  const long long nmodes = (long long)N * N * M * Nc;
+  // pairs: one phase pair per mode plus 4/pi trials on average; 2.5 per mode
+  // leaves a margin of thousands of standard deviations
+  const long long npairs = nmodes * 5 / 2 + 65536;
+  const long long nchunks = (npairs + IC_CHUNK - 1) / IC_CHUNK;
+  const long long nsblocks = (nchunks + IC_THREADS - 1) / IC_THREADS;
+  const size_t nspec = (size_t)N * N * M;
+  cudaStream_t st = h->stream;
+  double2 *uv = nullptr, *A = nullptr, *E = nullptr;
+  Trans *trans = nullptr, *excl = nullptr, *btot = nullptr;
+  unsigned char *bstate = nullptr;
+  unsigned long long *bmodes = nullptr;
+  long long *phase_pair = nullptr, *acc_pair = nullptr;
+  double *X = nullptr;
+  unsigned long long done = 0;
+  cufftHandle plan = 0;
+  bool plan_ok = false;
+  int r = PHN_OK;
+  cudaError_t e = cudaSuccess;
+#define ICK(call)                          \
+  do {                                     \
+    e = (call);                            \
+    if (e != cudaSuccess) {                \
+      r = cuda_error(e, #call);            \
+      goto cleanup;                        \
+    }                                      \
+  } while (0)
+  {
+    ICK(cudaMalloc(&uv, npairs * sizeof(double2)));
+    ICK(cudaMalloc(&trans, nchunks * sizeof(Trans)));
+    ICK(cudaMalloc(&excl, nchunks * sizeof(Trans)));
+    ICK(cudaMalloc(&btot, nsblocks * sizeof(Trans)));
+    ICK(cudaMalloc(&bstate, (nsblocks + 1) * sizeof(unsigned char)));
+    ICK(cudaMalloc(&bmodes, (nsblocks + 1) * sizeof(unsigned long long)));
+    ICK(cudaMalloc(&phase_pair, nmodes * sizeof(long long)));
+    ICK(cudaMalloc(&acc_pair, nmodes * sizeof(long long)));
+    ICK(cudaMalloc(&A, (size_t)Nc * nspec * sizeof(double2)));
+    ICK(cudaMalloc(&E, (size_t)Nc * nspec * sizeof(double2)));
+    ICK(cudaMalloc(&X, (size_t)N * N * N * sizeof(double)));
+    // srand48(seed): X0 = (seed mod 2^32) 2^16 + 0x330E
+    const unsigned long long x0 = (((unsigned long long)ic->seed & 0xFFFFFFFFULL) << 16) | 0x330EULL;
+    const int tb = 128;
+    ic_pairs<<<(unsigned)((nchunks + tb - 1) / tb), tb, 0, st>>>(x0, npairs, uv, trans, nchunks);
+    ICK(cudaGetLastError());
+    ic_scan_blocks<<<(unsigned)nsblocks, IC_THREADS, 0, st>>>(trans, nchunks, excl, btot);
+    ICK(cudaGetLastError());
+    ic_scan_top<<<1, 1, 0, st>>>(btot, nsblocks, bstate, bmodes);
+    ICK(cudaGetLastError());
+    ICK(cudaMemcpyAsync(&done, bmodes + nsblocks, sizeof(done), cudaMemcpyDeviceToHost, st));
+    ICK(cudaStreamSynchronize(st));
+    if ((long long)done < nmodes) {
+      r = set_error(PHN_ERR_INVALID, "random stream too short (%llu of %lld modes)", done, nmodes);
+      goto cleanup;
+    }
+    ic_assign<<<(unsigned)((nchunks + tb - 1) / tb), tb, 0, st>>>(uv, npairs, nchunks, excl, bstate, bmodes, nmodes,
+                                                                  phase_pair, acc_pair);
+    ICK(cudaGetLastError());
+    IcConsts k;
+    k.N = N;
+    k.Nc = Nc;
+    k.justnoise = ic->justnoise;
+    k.a = h->p.a;
+    k.QS = ic->QS;
+    k.scale2 = ic->scale2;
+    k.amplitude = ic->amplitude;
+    k.noise = ic->noise;
+    k.m2_long = ic->m2_long;
+    k.m2_trans = ic->m2_trans;
+    ic_modes<<<(unsigned)((nmodes + 255) / 256), 256, 0, st>>>(k, uv, phase_pair, acc_pair, nmodes, A, E);
+    ICK(cudaGetLastError());
+    const long long nre = 2LL * N * N * Nc;
+    ic_reality<<<(unsigned)((nre + 255) / 256), 256, 0, st>>>(A, N, Nc);
+    ic_reality<<<(unsigned)((nre + 255) / 256), 256, 0, st>>>(E, N, Nc);
+    ICK(cudaGetLastError());
+    h->launches += 8;
+    if (cufftPlan3d(&plan, N, N, N, CUFFT_Z2D) != CUFFT_SUCCESS) {
+      r = set_error(PHN_ERR_CUDA, "cufftPlan3d (Z2D %d^3) failed", N);
+      goto cleanup;
+    }
+    plan_ok = true;
+    if (cufftSetStream(plan, st) != CUFFT_SUCCESS) {
+      r = set_error(PHN_ERR_CUDA, "cufftSetStream failed");
+      goto cleanup;
+    }
+    // fftPtoX divides by L^3 (clusterfft.cpp:150,179), the caller multiplies
+    // by sqrt(L^3) (initialconditions.cpp:638)
+    const double L = h->p.a * N;
+    const double norm = (L * L) * (N * h->p.a);
+    const double scale = sqrt(norm) / norm;
+    const double phi0[2] = {ic->phi0[0], ic->phi0[1]}, pi0[2] = {ic->pi0[0], ic->pi0[1]};
+    const dim3 sg((N + 31) / 32, (N + 31) / 32, N), sb(32, 8);
+    for (int f = 0; f < 2; ++f)
+      for (int a = 0; a < Nc; ++a) {
+        double2 *src = (f == 0 ? A : E) + (size_t)a * nspec;
+        if (cufftExecZ2D(plan, (cufftDoubleComplex *)src, X) != CUFFT_SUCCESS) {
+          r = set_error(PHN_ERR_CUDA, "cufftExecZ2D failed");
+          goto cleanup;
+        }
+        const double off = a < 2 ? (f == 0 ? phi0[a] : pi0[a]) : 0.0;
+        void *dst = f == 0 ? h->phi[h->cur] : h->pi;
+        if (h->p.precision == PHN_FP64) {
+          ic_store<double><<<sg, sb, 0, st>>>(X, (double *)dst + (size_t)a * h->V, N, scale, off);
+        } else {
+          ic_store<float><<<sg, sb, 0, st>>>(X, (float *)dst + (size_t)a * h->V, N, scale, off);
+        }
+        ICK(cudaGetLastError());
+        h->launches++;
+      }
+    if (h->p.precision == PHN_FP32_KAHAN) {
+      ICK(cudaMemsetAsync(h->cphi, 0, h->V * h->p.Nc * sizeof(float), st));
+      ICK(cudaMemsetAsync(h->cpi, 0, h->V * h->p.Nc * sizeof(float), st));
+    }
+    ICK(cudaStreamSynchronize(st));
+  }
+cleanup:
+#undef ICK
+  if (plan_ok) cufftDestroy(plan);
+  cudaFree(uv);
+  cudaFree(trans);
+  cudaFree(excl);
+  cudaFree(btot);
+  cudaFree(bstate);
+  cudaFree(bmodes);
+  cudaFree(phase_pair);
+  cudaFree(acc_pair);
+  cudaFree(A);
+  cudaFree(E);
+  cudaFree(X);
+  return r;
+}
+
+}  // extern "C"

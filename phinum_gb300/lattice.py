@@ -99,6 +99,18 @@ class Lattice:
         L.check(self.lib.phn_download(self.h, _pd(phi), _pd(pi)))
         return phi, pi
 
+    def initial_conditions(self, seed: int = 1, justnoise: int = 0, QS: float = 1.0, scale2: float = 1.0,
+                           amplitude: float = 0.0, noise: float = 0.5, phi0=(0.0, 0.0), pi0=(0.0, 0.0),
+                           m2_long: float | None = None, m2_trans: float | None = None):
+        """SetInitialConditions (initialize 3) on the device with the
+        reference's drand48 stream from srand48(seed); M2_long and M2_trans
+        default to M_sqr (renormalization.cpp:17-18)."""
+        m2l = self.p.m_sqr if m2_long is None else m2_long
+        m2t = self.p.m_sqr if m2_trans is None else m2_trans
+        ic = L.PhnIcParams(int(seed), int(justnoise), QS, scale2, amplitude, noise, (ctypes.c_double * 2)(*phi0),
+                           (ctypes.c_double * 2)(*pi0), m2l, m2t)
+        L.check(self.lib.phn_initial_conditions(self.h, ctypes.byref(ic)))
+
     # -------------------------------------------------------------- clock
     def reset(self):
         L.check(self.lib.phn_reset(self.h))

@@ -3,6 +3,10 @@ sources (oracle/_ref, built by oracle/build_ref.sh from the reference tree).
 
     sh oracle/build_ref.sh && python tests/golden/make_golden.py
 
+The initial-condition fixtures (tests/golden/ic/) hold the reference's own
+SetInitialConditions output (initialize 3) for chosen srand48 seeds: the
+harness redirects its time(NULL) seed (oracle/ref_driver.cpp).
+
 Every case runs in a fresh process because the reference keeps its lattice in
 globals.  Inputs come from tests/golden/inputs.py (bit-reproducible on any
 platform), so the fixtures store seeds for the large cases and full arrays only
@@ -44,6 +48,28 @@ CASES = {
     "t1_n32": (dict(N=32, Nc=1, **TDW), 5, -SQRT6, 500, 1.0, False, (1, 100, 500)),
     "c0_n64": (dict(N=64, Nc=1, **PHI6), 6, SQRT6, 2000, 1.0, False, (1, 500, 2000)),
 }
+
+
+# SetInitialConditions cases: name -> (lattice params, initial-condition params)
+IC_CASES = {
+    "n8_phi6": (dict(N=8, Nc=1, **PHI6), dict(seed=7, noise=3.0, scale2=6.2832, phi0=(SQRT6, 0.0))),
+    "n12_nc2": (dict(N=12, Nc=2, **PHI6), dict(seed=123, noise=0.5, QS=6.0, scale2=10.0, amplitude=1.5,
+                                                 phi0=(1.0, -0.5), pi0=(0.2, 0.1))),
+    "n16_tdw": (dict(N=16, Nc=1, **TDW), dict(seed=20260, noise=3.0, scale2=6.2832, phi0=(-SQRT6, 0.0))),
+    "n16_noise": (dict(N=16, Nc=1, **PHI6), dict(seed=-5, justnoise=1, scale2=0.0, noise=1.0)),
+}
+
+
+def run_ic_case(name: str) -> None:
+    from oracle import oracle as O
+    pd, ic = IC_CASES[name]
+    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    R = O.Reference(p)
+    phi, pi = R.initial_conditions(**ic)
+    os.makedirs(os.path.join(HERE, "ic"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "ic", f"{name}.npz"), params=json.dumps(pd), ic=json.dumps(ic),
+                        phi=phi, pi=pi)
+    print(f"ic/{name}: |phi|max={np.abs(phi).max():.4g} |pi|max={np.abs(pi).max():.4g}")
 
 
 def digest(a: np.ndarray) -> str:
@@ -106,10 +132,19 @@ def main() -> None:
     if len(sys.argv) > 2 and sys.argv[1] == "--case":
         run_case(sys.argv[2])
         return
+    if len(sys.argv) > 2 and sys.argv[1] == "--ic-case":
+        run_ic_case(sys.argv[2])
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "--ic":
+        for name in IC_CASES:
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--ic-case", name], check=True)
+        return
     if not O.ref_available(0) or not O.ref_available(1):
         sys.exit("reference pin not built: run oracle/build_ref.sh first")
     for name in CASES:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--case", name], check=True)
+    for name in IC_CASES:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--ic-case", name], check=True)
 
 
 if __name__ == "__main__":
