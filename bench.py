@@ -521,6 +521,45 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     return out
 
 
+def initial_form(N: int, n_cpu: int = 128, n_check: int = 64):
+    """Initial conditions (SetInitialConditions, initialize 3, the
+    configuration's spectrum: Noise 3 below |p| = 2 pi, phi0 = sqrt(6)) on the
+    GPU: wall time of one phn_initial_conditions call (drand48 stream, mode
+    assignment, amplitudes, two cuFFT Z2D, stores; cuFFT plan included),
+    median of 3 after a warm-up call.  Agreement with the oracle at n_check^3
+    and the oracle's single-thread time at n_cpu^3 (the reference generates on
+    one thread per rank)."""
+    from oracle import oracle as O
+    from phinum_gb300 import lattice as PL
+    ic = dict(seed=2026, noise=3.0, scale2=2 * np.pi, phi0=(6 ** 0.5, 0.0))
+    out = {"form": "initial", "N": N, "ic": {k: v for k, v in ic.items()}}
+    for name, prec in (("fp64", 0), ("fp32", 1)):
+        lat = PL.Lattice(PL.Params(N=N, precision=prec))
+        lat.initial_conditions(**ic)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            lat.initial_conditions(**ic)
+            ts.append(time.perf_counter() - t0)
+        lat.close()
+        t = float(np.median(ts))
+        out[name] = {"ms": t * 1e3, "sites_per_s": N ** 3 / t}
+    lat = PL.Lattice(PL.Params(N=n_check))
+    lat.initial_conditions(**ic)
+    phi, pi = lat.download()
+    lat.close()
+    ophi, opi = O.initial_conditions(O.Params(N=n_check), **ic)
+    sl = slice(n_check ** 2, -n_check ** 2)
+    out["check"] = {"N": n_check, "phi_max_dev_rel": float(np.abs(phi - ophi).max() / np.abs(ophi).max()),
+                    "pi_max_dev_rel": float(np.abs(pi[sl] - opi[sl]).max() / np.abs(opi[sl]).max())}
+    t0 = time.perf_counter()
+    O.initial_conditions(O.Params(N=n_cpu), **ic)
+    t = time.perf_counter() - t0
+    out["cpu_oracle"] = {"N": n_cpu, "s": t, "sites_per_s": n_cpu ** 3 / t, "cores": 1}
+    out["speedup_fp64_vs_cpu_sites_per_s"] = out["fp64"]["sites_per_s"] / out["cpu_oracle"]["sites_per_s"]
+    return out
+
+
 def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int):
     """The oracle's reference loop (FP64) on all host threads, bounded."""
     from oracle import oracle as O
@@ -551,7 +590,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--n", type=int, default=N_MAIN, help="lattice edge (profiling runs use smaller cases)")
     ap.add_argument("--variant", type=int, default=None, help="TMA kernel variant instead of the autotuner's pick")
-    ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble"],
+    ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble", "initial"],
                     help="report one of the north-star forms instead of the benchmark line")
     args = ap.parse_args()
     rank, local, world = env_rank()
@@ -568,6 +607,9 @@ def main():
     if args.form == "adjoint":
         kw = dict(check=False) if args.quick else {}
         print(json.dumps(adjoint_form(args.n, args.steps, **kw)))
+        return
+    if args.form == "initial":
+        print(json.dumps(initial_form(args.n)))
         return
     if args.form == "ensemble":
         out = measure_ensemble(max(args.steps, 100), 100)
