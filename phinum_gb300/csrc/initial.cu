@@ -30,9 +30,10 @@
 //   ic_store    X / L^3 * sqrt(L^3) + phi0 into the handle's [z][y][x] fields
 //               (a shared-memory transpose of x and y)
 //
-// The stream, the acceptance decisions and the mode assignment are exact;
-// the amplitudes use CUDA's log/sin/cos, which may differ from the C
-// library's in the last bit, and cuFFT rounds differently from FFTW.
+// The stream, the acceptance decisions and the mode assignment are exact, and
+// the per-axis momenta are the C library's values (computed on the host); the
+// Box-Muller log and the phases' cos/sin are CUDA's, which may differ from the
+// C library's in the last bit, and cuFFT rounds differently from FFTW.
 #include <cufft.h>
 #include <math.h>
 
@@ -202,15 +203,17 @@ struct IcConsts {
   double a, QS, scale2, amplitude, noise, m2_long, m2_trans;
 };
 
-// Per-axis lattice momentum as initialconditions.cpp:88-113 writes it.
-__device__ __forceinline__ double ic_p(int n, int N, double a) {
-  const double s = sin(n * acos(-1.) / N);
-  return n < N / 2 + 1 ? 2.0 / a * s : -2.0 / a * s;
+// Per-axis lattice momentum as initialconditions.cpp:88-113 writes it,
+// evaluated on the host with the C library's sin (the reference's values).
+static double ic_p_host(int n, int N, double a) {
+  if (n < N / 2 + 1) return 2.0 / (a) * sin(n * acos(-1.) / N);
+  return -2.0 / (a) * sin(n * acos(-1.) / N);
 }
 
 // One (mode, component): initialconditions.cpp:339-569 (initialize 3,
 // expansion 0, withcharge 0).  A and E are [a][pz][px][py] complex arrays.
-__global__ void ic_modes(const IcConsts k, const double2 *__restrict__ uv, const long long *__restrict__ phase_pair,
+__global__ void ic_modes(const IcConsts k, const double *__restrict__ ptab, const double2 *__restrict__ uv,
+                         const long long *__restrict__ phase_pair,
                          const long long *__restrict__ acc_pair, long long nmodes, double2 *__restrict__ A,
                          double2 *__restrict__ E) {
   const long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -219,9 +222,9 @@ __global__ void ic_modes(const IcConsts k, const double2 *__restrict__ uv, const
   const int a = (int)(m % k.Nc);
   const long long pos = m / k.Nc;  // py + px M + pz N M: the mode loop order
   const int py = (int)(pos % M), px = (int)((pos / M) % N), pz = (int)(pos / ((long long)M * N));
-  const double nu = pz == 0 ? 0.0 : ic_p(pz, N, k.a);
-  const double ppx = ic_p(px, N, k.a);
-  const double ppy = 2.0 / k.a * sin(py * acos(-1.) / N);
+  const double nu = pz == 0 ? 0.0 : ptab[pz];
+  const double ppx = ptab[px];
+  const double ppy = ptab[py];  // py <= N/2: the positive branch
   const double pt = __dsqrt_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)));
   const double psqr = __dadd_rn(__dmul_rn(pt, pt), __dmul_rn(nu, nu));
   // phases and Gaussians (initialconditions.cpp:27-41, 344-349)
@@ -325,7 +328,7 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
   unsigned char *bstate = nullptr;
   unsigned long long *bmodes = nullptr;
   long long *phase_pair = nullptr, *acc_pair = nullptr;
-  double *X = nullptr;
+  double *X = nullptr, *ptab = nullptr;
   unsigned long long done = 0;
   cufftHandle plan = 0;
   bool plan_ok = false;
@@ -351,6 +354,16 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
     ICK(cudaMalloc(&A, (size_t)Nc * nspec * sizeof(double2)));
     ICK(cudaMalloc(&E, (size_t)Nc * nspec * sizeof(double2)));
     ICK(cudaMalloc(&X, (size_t)N * N * N * sizeof(double)));
+    ICK(cudaMalloc(&ptab, N * sizeof(double)));
+    {
+      double tab[4096];
+      if (N > 4096) {
+        r = set_error(PHN_ERR_UNSUPPORTED, "N > 4096");
+        goto cleanup;
+      }
+      for (int n = 0; n < N; ++n) tab[n] = ic_p_host(n, N, h->p.a);
+      ICK(cudaMemcpy(ptab, tab, N * sizeof(double), cudaMemcpyHostToDevice));
+    }
     // srand48(seed): X0 = (seed mod 2^32) 2^16 + 0x330E
     const unsigned long long x0 = (((unsigned long long)ic->seed & 0xFFFFFFFFULL) << 16) | 0x330EULL;
     const int tb = 128;
@@ -380,7 +393,7 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
     k.noise = ic->noise;
     k.m2_long = ic->m2_long;
     k.m2_trans = ic->m2_trans;
-    ic_modes<<<(unsigned)((nmodes + 255) / 256), 256, 0, st>>>(k, uv, phase_pair, acc_pair, nmodes, A, E);
+    ic_modes<<<(unsigned)((nmodes + 255) / 256), 256, 0, st>>>(k, ptab, uv, phase_pair, acc_pair, nmodes, A, E);
     ICK(cudaGetLastError());
     const long long nre = 2LL * N * N * Nc;
     ic_reality<<<(unsigned)((nre + 255) / 256), 256, 0, st>>>(A, N, Nc);
@@ -440,6 +453,7 @@ cleanup:
   cudaFree(A);
   cudaFree(E);
   cudaFree(X);
+  cudaFree(ptab);
   return r;
 }
 
