@@ -179,6 +179,64 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic);
 int phn_islands(phn_handle *h, double thres, int mode, int z_periodic, int *labels, phn_island *out,
                 int max_out, int *n_islands);
 
+/* After phn_islands: the island (numbered as phn_islands numbers them) that
+ * holds each queried site, reference-layout indices; -1 outside the mask. */
+int phn_islands_lookup(phn_handle *h, const long long *pos, int n, int *island);
+
+/* ---- Island tracking over a run -------------------------------------------
+ * Full_Analysis() with its history (islands.cpp:651-840): island_analysis::
+ * found_islands is held by a tracker.  Each update sorts the tracked islands
+ * by their last volume (std::sort with the reference's ordering), retires
+ * those whose centre left the mask (Old_islands), re-seeds the others from
+ * their centres in that order -- an island whose centre lies in an island
+ * already claimed this update is merged away -- appends one history entry
+ * (at most 5 kept: the first two and the last three, islands.cpp:264-276),
+ * sets status 1 for an expanding bubble (is_bubble, reported once per
+ * update as print_bubble_history does) or 2 for an oscillon (is_oscillon),
+ * and adds the unclaimed islands as new ones in the reference's scan order,
+ * numbered number_of_islands + rank * 1000000. */
+#define PHN_TRACK_HISTORY 5
+typedef struct phn_track_island {
+  double index, status, disp, length; /* island::index, status, disp; history entries held */
+  double at_time[PHN_TRACK_HISTORY], center[PHN_TRACK_HISTORY], volume[PHN_TRACK_HISTORY];
+  double pot_en[PHN_TRACK_HISTORY], kin_en[PHN_TRACK_HISTORY], grad_en[PHN_TRACK_HISTORY];
+  double av_phi[PHN_TRACK_HISTORY], peak_value[PHN_TRACK_HISTORY];
+} phn_track_island;
+enum {
+  PHN_TRACK_ALIVE = 0,   /* found_islands after the last update, in its order */
+  PHN_TRACK_RETIRED = 1, /* islands Old_islands removed in the last update (their history as written) */
+  PHN_TRACK_BUBBLES = 2  /* islands print_bubble_history reported in the last update */
+};
+typedef struct phn_tracker phn_tracker;
+int phn_tracker_create(int rank, phn_tracker **out);
+int phn_tracker_destroy(phn_tracker *t);
+int phn_tracker_reset(phn_tracker *t);
+/* Full_Analysis on the handle's current state (Nc = 1): phn_islands with
+ * (thres, mode, z_periodic), centre lookups, the bookkeeping below; labels
+ * (optional, reference layout) receive island_analysis::b, the position of
+ * each site's island in found_islands, -1 elsewhere. */
+int phn_tracker_update(phn_tracker *t, phn_handle *h, double thres, int mode, int z_periodic, int *labels);
+/* The bookkeeping alone, for callers that label islands themselves: comps[c]
+ * are this update's islands in seed order, center_island[i] the island that
+ * holds alive island i's centre (-1: outside the mask), in the current
+ * found_islands order (phn_tracker_centers).  owner (optional, ncomp
+ * entries) receives each island's position in found_islands afterwards. */
+int phn_tracker_update_records(phn_tracker *t, double tau, const phn_island *comps, int ncomp,
+                               const int *center_island, int *owner);
+/* Centres (reference-layout index of the last entry) of the alive islands. */
+int phn_tracker_centers(const phn_tracker *t, long long *pos, int max, int *n);
+int phn_tracker_count(const phn_tracker *t, int set, int *n);
+int phn_tracker_get(const phn_tracker *t, int set, int i, phn_track_island *out);
+/* Oscillon_specific_observables (islands.cpp:745-775): over alive islands
+ * with disp set and is_oscillon, out[0] = r_osc (their energy / (L^3
+ * avg_energy), L = N a), out[1] = n_osc (count / L^3), out[2] = avgM_osc
+ * (mean energy). */
+int phn_tracker_oscillons(const phn_tracker *t, int N, double a, double avg_energy, double out[3]);
+/* add_stat_new (statistics.cpp:43-67): adds the alive disp islands to the
+ * 200 x 200 histograms of (|peak|, radius) and (|peak|, radius /
+ * sqrt(log(peak^2 / thres^2))), row-major int counts. */
+int phn_tracker_add_stat(const phn_tracker *t, double thres, double QS, int *hist_r, int *hist_r0);
+
 /* Kernel path of the FP32 step (the others have one path each):
  * PHN_PATH_TMA, the TMA-pipelined persistent kernel (default where it
  * applies: Nc = 1, N in {128,256,384,512,768,1024}); PHN_PATH_X4, the

@@ -315,6 +315,10 @@ class Reference:
         lib.ref_spectrum.argtypes = [_PD, _PD, _PD, _PI]
         lib.ref_islands.argtypes = [_D, _PI, _PD, _I]
         lib.ref_islands.restype = _I
+        lib.ref_track_step.argtypes = [_D, _PI]
+        lib.ref_track_step.restype = _I
+        lib.ref_track_island.argtypes = [_I, _PD]
+        lib.ref_track_island.restype = _I
         lib.ref_initial_conditions.argtypes = [ctypes.c_long, _I, _D, _D, _D, _D, _D, _D, _D, _D]
         lib.ref_initial_conditions.restype = _I
         self.lib = lib
@@ -332,6 +336,19 @@ class Reference:
         if r != 0:
             raise RuntimeError("ref_initial_conditions failed")
         return self.get_fields()
+
+    def track_reset(self):
+        self.lib.ref_track_reset()
+
+    def track_step(self, thres: float):
+        """Full_Analysis() on the current fields; returns the tracked islands
+        as an (n, 44) array: index, status, disp, L, then 5 x (at_time, centre,
+        V, PotEn, KinEn, GradEn, avPhi, Peak_value), unused entries zero."""
+        n = self.lib.ref_track_step(float(thres), None)
+        out = np.zeros((n, 44))
+        for i in range(n):
+            self.lib.ref_track_island(i, _ptr(out[i]))
+        return out
 
     def set_fields(self, phi, pi):
         self.lib.ref_set_fields(_ptr(np.ascontiguousarray(phi, np.float64)),

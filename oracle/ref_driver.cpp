@@ -241,6 +241,53 @@ int ref_islands(double thres, int *labels, double *stats, int max_islands) {
   return count;
 }
 
+/* Island tracking over a run: ref_track_reset() empties the history, then
+ * each ref_track_step(thres) runs the reference's Full_Analysis() on the
+ * current fields (islands.cpp:778-840: sort, Old_islands, re-seeding from
+ * the old centres, new islands) and returns the number of tracked islands;
+ * ref_track_island(i, out) reports island i as
+ *   out[0..3]   index, status, disp, history length L (<= 5)
+ *   out[4 + 8 j .. 11 + 8 j], j < L: at_time, centre pos, V, PotEn, KinEn,
+ *               GradEn, avPhi, Peak_value of history entry j. */
+void ref_track_reset() {
+  island_analysis::fin();
+  island_analysis::init();
+}
+
+int ref_track_step(double thres, int *labels) {
+  using namespace island_analysis;
+  island_analysis::thres = (pseudo_double)thres;
+  Full_Analysis();
+  if (labels) {
+    const size_t n = field_len();
+    for (size_t k = 0; k < n; ++k) labels[k] = b[k];
+  }
+  return (int)found_islands.size();
+}
+
+int ref_track_island(int i, double *out) {
+  using namespace island_analysis;
+  if (i < 0 || i >= (int)found_islands.size()) return -1;
+  island &B = found_islands[(size_t)i];
+  const int L = (int)B.V.size();
+  out[0] = B.index;
+  out[1] = B.status;
+  out[2] = B.disp ? 1.0 : 0.0;
+  out[3] = L;
+  for (int j = 0; j < L && j < 5; ++j) {
+    double *e = out + 4 + 8 * j;
+    e[0] = B.at_time[(size_t)j];
+    e[1] = B.center[(size_t)j].pos;
+    e[2] = B.V[(size_t)j];
+    e[3] = B.PotEn[(size_t)j];
+    e[4] = B.KinEn[(size_t)j];
+    e[5] = B.GradEn[(size_t)j];
+    e[6] = B.avPhi[(size_t)j];
+    e[7] = B.Peak_value[(size_t)j];
+  }
+  return L;
+}
+
 /* SetInitialConditions() (initialize 3) with srand48(seed); the fields land
  * in LocalLattice::Phi/Pi (read them with ref_get_fields). */
 int ref_initial_conditions(long seed, int justnoise_, double qs, double scale2_, double amplitude, double noise,

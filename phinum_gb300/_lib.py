@@ -18,6 +18,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NOMEM, ERR_UNSUPPORTE
 FP64, FP32, FP32_KAHAN = 0, 1, 2
 ISLAND_REFERENCE, ISLAND_ENERGY = 0, 1
 PATH_AUTO, PATH_PLAIN, PATH_TMA, PATH_X4 = 0, 1, 2, 3
+TRACK_ALIVE, TRACK_RETIRED, TRACK_BUBBLES = 0, 1, 2
 
 _D, _I = ctypes.c_double, ctypes.c_int
 _PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
@@ -32,6 +33,11 @@ class PhnParams(ctypes.Structure):
 class PhnIcParams(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_long), ("justnoise", _I), ("QS", _D), ("scale2", _D), ("amplitude", _D),
                 ("noise", _D), ("phi0", _D * 2), ("pi0", _D * 2), ("m2_long", _D), ("m2_trans", _D)]
+
+
+class PhnTrackIsland(ctypes.Structure):
+    _fields_ = [("index", _D), ("status", _D), ("disp", _D), ("length", _D)] + [
+        (f, _D * 5) for f in ("at_time", "center", "volume", "pot_en", "kin_en", "grad_en", "av_phi", "peak_value")]
 
 
 class PhnAverages(ctypes.Structure):
@@ -74,6 +80,17 @@ _SIGS = {
     "phn_spectrum": (_I, [ctypes.c_void_p, _PD, _PD, _PD, _PI, _I]),
     "phn_spectrum_uniform": (_I, [ctypes.c_void_p, _I, _PD, _PD, _PD, _PI]),
     "phn_initial_conditions": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams)]),
+    "phn_islands_lookup": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _I, _PI]),
+    "phn_tracker_create": (_I, [_I, ctypes.POINTER(ctypes.c_void_p)]),
+    "phn_tracker_destroy": (_I, [ctypes.c_void_p]),
+    "phn_tracker_reset": (_I, [ctypes.c_void_p]),
+    "phn_tracker_update": (_I, [ctypes.c_void_p, ctypes.c_void_p, _D, _I, _I, _PI]),
+    "phn_tracker_update_records": (_I, [ctypes.c_void_p, _D, ctypes.c_void_p, _I, _PI, _PI]),
+    "phn_tracker_centers": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _I, _PI]),
+    "phn_tracker_count": (_I, [ctypes.c_void_p, _I, _PI]),
+    "phn_tracker_get": (_I, [ctypes.c_void_p, _I, _I, ctypes.POINTER(PhnTrackIsland)]),
+    "phn_tracker_oscillons": (_I, [ctypes.c_void_p, _I, _D, _D, _PD]),
+    "phn_tracker_add_stat": (_I, [ctypes.c_void_p, _D, _D, _PI, _PI]),
     "phn_islands": (_I, [ctypes.c_void_p, _D, _I, _I, _PI, _PD, _I, _PI]),
     "phn_set_path": (_I, [ctypes.c_void_p, _I]),
     "phn_get_path": (_I, [ctypes.c_void_p, _PI]),

@@ -269,6 +269,36 @@ __global__ void ccl_labels(const int *__restrict__ parent, const int *__restrict
   }
 }
 
+// Island of each queried site (reference-layout index; -1 outside the mask or
+// the interior).
+__global__ void ccl_lookup(const int *__restrict__ parent, const int *__restrict__ ids, int N,
+                           const long long *__restrict__ pos, int n, int *__restrict__ out) {
+  const size_t NN = (size_t)N * N, V = NN * N;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const long long k = pos[j];
+    int v = -1;
+    if (k >= (long long)NN && k < (long long)(NN + V)) {
+      const int r = parent[k - NN];
+      if (r >= 0) v = ids[r];
+    }
+    out[j] = v;
+  }
+}
+
+// Labels in the reference layout through a map from island number to label.
+__global__ void ccl_labels_mapped(const int *__restrict__ parent, const int *__restrict__ ids,
+                                  const int *__restrict__ map, int N, int *__restrict__ out) {
+  const size_t NN = (size_t)N * N, V = NN * N, total = NN * (N + 2);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    int v = -1;
+    if (i >= NN && i < NN + V) {
+      const int r = parent[i - NN];
+      if (r >= 0) v = map[ids[r]];
+    }
+    out[i] = v;
+  }
+}
+
 __global__ void fill_ll(long long *p, long long v, int n) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) p[j] = v;
 }
@@ -421,6 +451,53 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
 }  // namespace phn
 
 using namespace phn;
+
+// Labels of the last phn_islands call mapped through map[island] (n entries),
+// into host memory (reference layout).
+int phn::islands_labels_mapped(phn_handle *h, const int *map, int n, int *labels) {
+  IslState *s = (IslState *)h->isl;
+  if (!s) return set_error(PHN_ERR_INVALID, "no island labelling on this handle yet");
+  cudaStream_t st = h->stream;
+  const int N = h->p.N;
+  const size_t total = (size_t)N * N * (N + 2);
+  int *d_map = nullptr, *d_lab = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&d_map, (size_t)(n > 0 ? n : 1) * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_lab, total * sizeof(int), st);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpyAsync(d_map, map, n * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    ccl_labels_mapped<<<grid_blocks(total), CCL_THREADS, 0, st>>>(s->parent, s->ids, d_map, N, d_lab);
+    h->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(labels, d_lab, total * sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d_map, st);
+  cudaFreeAsync(d_lab, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? PHN_OK : cuda_error(e, "mapped labels");
+}
+
+extern "C" int phn_islands_lookup(phn_handle *h, const long long *pos, int n, int *island) {
+  if (!h || (n > 0 && (!pos || !island)) || n < 0) return set_error(PHN_ERR_INVALID, "bad argument");
+  IslState *s = (IslState *)h->isl;
+  if (!s) return set_error(PHN_ERR_INVALID, "phn_islands first");
+  if (n == 0) return PHN_OK;
+  cudaStream_t st = h->stream;
+  long long *d_pos = nullptr;
+  int *d_out = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&d_pos, n * sizeof(long long), st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_out, n * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_pos, pos, n * sizeof(long long), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    ccl_lookup<<<(n + 255) / 256, 256, 0, st>>>(s->parent, s->ids, h->p.N, d_pos, n, d_out);
+    h->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(island, d_out, n * sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d_pos, st);
+  cudaFreeAsync(d_out, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? PHN_OK : cuda_error(e, "island lookup");
+}
 
 extern "C" int phn_islands(phn_handle *h, double thres, int mode, int z_periodic, int *labels, phn_island *out,
                            int max_out, int *n_islands) {

@@ -165,5 +165,6 @@ struct phn_handle {
 namespace phn {
 void spectrum_release(phn_handle *h);
 void islands_release(phn_handle *h);
+int islands_labels_mapped(phn_handle *h, const int *map, int n, int *labels);  // islands.cu
 int evolve_async(phn_handle *h, int nsteps);  // api.cu: steps queued, no sync
 }  // namespace phn

@@ -176,6 +176,73 @@ class Lattice:
         L.check(self.lib.phn_synchronize(self.h))
 
 
+class Tracker:
+    """Island tracking over a run (phn_tracker_*): Full_Analysis with its
+    history.  islands(set) returns an (n, 44) array per island: index,
+    status, disp, history length, then 5 x (at_time, centre, volume, PotEn,
+    KinEn, GradEn, avPhi, Peak_value)."""
+
+    def __init__(self, rank: int = 0):
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        L.check(self.lib.phn_tracker_create(int(rank), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.phn_tracker_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def update(self, lat: "Lattice", thres: float, mode: int = L.ISLAND_REFERENCE, z_periodic: bool = False,
+               labels: bool = False):
+        lab = np.zeros(lat.p.N * lat.p.N * (lat.p.N + 2), dtype=np.int32) if labels else None
+        L.check(self.lib.phn_tracker_update(self.h, lat.h, float(thres), int(mode), int(bool(z_periodic)),
+                                            _pi(lab) if labels else None))
+        return lab
+
+    def update_records(self, tau: float, comps: np.ndarray, center_island: np.ndarray):
+        """The bookkeeping alone: comps as phn_islands records (n, 10),
+        center_island aligned with centers(); returns each island's owner."""
+        comps = np.ascontiguousarray(comps, dtype=np.float64)
+        ci = np.ascontiguousarray(center_island, dtype=np.int32)
+        owner = np.zeros(max(1, comps.shape[0]), dtype=np.int32)
+        L.check(self.lib.phn_tracker_update_records(self.h, float(tau), comps.ctypes.data_as(ctypes.c_void_p),
+                                                    comps.shape[0], _pi(ci), _pi(owner)))
+        return owner[:comps.shape[0]]
+
+    def centers(self) -> np.ndarray:
+        n = ctypes.c_int()
+        L.check(self.lib.phn_tracker_count(self.h, L.TRACK_ALIVE, ctypes.byref(n)))
+        out = np.zeros(max(1, n.value), dtype=np.int64)
+        L.check(self.lib.phn_tracker_centers(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                             n.value, ctypes.byref(n)))
+        return out[:n.value]
+
+    def islands(self, which: int = L.TRACK_ALIVE) -> np.ndarray:
+        n = ctypes.c_int()
+        L.check(self.lib.phn_tracker_count(self.h, int(which), ctypes.byref(n)))
+        out = np.zeros((n.value, 44))
+        rec = L.PhnTrackIsland()
+        for i in range(n.value):
+            L.check(self.lib.phn_tracker_get(self.h, int(which), i, ctypes.byref(rec)))
+            a = np.frombuffer(bytes(rec), dtype=np.float64)
+            out[i, :4] = a[:4]
+            out[i, 4:] = a[4:].reshape(8, 5).T.ravel()
+        return out
+
+
 class Ensemble:
     """Many lattices evolved together (phn_ensemble_*): one persistent kernel
     per step over all members, step loop in a CUDA graph."""

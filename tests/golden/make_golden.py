@@ -60,6 +60,55 @@ IC_CASES = {
 }
 
 
+# Island tracking (Full_Analysis over a run): N, input seed, mask quantile,
+# steps, steps between analyses
+TRACK_CASES = {"n24_phi6": (dict(N=24, Nc=1, **PHI6), 3, 0.95, 2500, 50)}
+
+
+def run_track_case(name: str) -> None:
+    """The reference's Full_Analysis() every `every` steps from t = 0 (as
+    main.cpp:68-83 calls it).  Per call: the tracked islands' integer data
+    (index, status, disp, history length, centres, sizes), the labels' digest,
+    per-column sums of the float data, and the full float data for the first
+    two and the last ten calls."""
+    from oracle import oracle as O
+    import inputs
+    pd, seed, q, steps, every = TRACK_CASES[name]
+    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    phi_i, pi_i = inputs.lattice_fields(p.N, 1, seed, phi0=SQRT6)
+    thr = float(np.quantile(np.sqrt(phi_i ** 2 + pi_i ** 2), q))
+    R = O.Reference(p)
+    R.set_fields(O.to_ref_layout(phi_i), O.to_ref_layout(pi_i))
+    R.reset()
+    R.track_reset()
+    ncalls = steps // every + 1
+    ints, offs, sums, lab_sha, full = [], [0], [], [], {}
+    cell = p.a ** 3
+    labels = np.zeros(p.N * p.N * (p.N + 2), dtype=np.int32)
+    for c in range(ncalls):
+        n = R.lib.ref_track_step(thr, labels.ctypes.data_as(O._PI))
+        T = np.zeros((n, 44))
+        for i in range(n):
+            R.lib.ref_track_island(i, T[i].ctypes.data_as(O._PD))
+        H = T[:, 4:].reshape(n, 5, 8)
+        iv = np.zeros((n, 14), dtype=np.int64)
+        iv[:, :4] = T[:, :4].astype(np.int64)
+        iv[:, 4:9] = H[:, :, 1].astype(np.int64)
+        iv[:, 9:14] = np.rint(H[:, :, 2] / cell).astype(np.int64)
+        ints.append(iv)
+        offs.append(offs[-1] + n)
+        sums.append(H[:, :, [0, 3, 4, 5, 6, 7]].sum(axis=(0, 1)))
+        lab_sha.append(hashlib.sha256(labels.astype("<i4").tobytes()).hexdigest())
+        if c < 2 or c >= ncalls - 10:
+            full[f"floats_{c}"] = H[:, :, [0, 3, 4, 5, 6, 7]]
+        if c + 1 < ncalls:
+            R.evolve(every)
+    np.savez_compressed(os.path.join(HERE, "track", f"{name}.npz"), params=json.dumps(pd), seed=seed, thres=thr,
+                        every=every, ncalls=ncalls, ints=np.concatenate(ints), offs=np.array(offs),
+                        sums=np.array(sums), labels_sha=np.array(lab_sha), **full)
+    print(f"track/{name}: calls={ncalls} islands per call max={max(np.diff(offs))} total={offs[-1]}")
+
+
 def run_ic_case(name: str) -> None:
     from oracle import oracle as O
     pd, ic = IC_CASES[name]
@@ -135,6 +184,14 @@ def main() -> None:
     if len(sys.argv) > 2 and sys.argv[1] == "--ic-case":
         run_ic_case(sys.argv[2])
         return
+    if len(sys.argv) > 2 and sys.argv[1] == "--track-case":
+        os.makedirs(os.path.join(HERE, "track"), exist_ok=True)
+        run_track_case(sys.argv[2])
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "--track":
+        for name in TRACK_CASES:
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--track-case", name], check=True)
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "--ic":
         for name in IC_CASES:
             subprocess.run([sys.executable, os.path.abspath(__file__), "--ic-case", name], check=True)
@@ -145,6 +202,8 @@ def main() -> None:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--case", name], check=True)
     for name in IC_CASES:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--ic-case", name], check=True)
+    for name in TRACK_CASES:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--track-case", name], check=True)
 
 
 if __name__ == "__main__":
