@@ -15,7 +15,8 @@
 //   Print_fp           momentumspace.cpp:280-384   phn_gpu::Print_fp()
 //     (Calculate_CorrelationFunctions :140)
 //   Full_Analysis      islands.cpp:778-840         phn_gpu::Full_Analysis_first()
-//     (first call of a run: empty island history)
+//     (first call of a run: empty island history), or phn_gpu::Full_Analysis()
+//     for every call with the history (islands.cpp:651-840)
 //
 // The device holds the authoritative fields between calls; phn_gpu::to_host()
 // brings them back into LocalLattice::Phi/Pi for any host code that reads
@@ -257,6 +258,75 @@ inline void Full_Analysis_first() {
     number_of_islands++;
     found_islands.push_back(B);
   }
+}
+
+// Full_Analysis() with its history (islands.cpp:651-840) on the device
+// fields: the tracker does the labelling and the bookkeeping; its islands are
+// then mirrored into island_analysis::found_islands, so the reference's own
+// consumers (add_stat_new, Oscillon_specific_observables, is_bubble,
+// is_oscillon) read them unchanged, and the reference's own writers record
+// what this update retired (Old_islands: non_critical_islands.txt,
+// islands.txt) and which expanding bubbles it saw (print_bubble_history).
+static phn_tracker *tracker = nullptr;
+
+static island to_island(const phn_track_island &r) {
+  island B;
+  const int L = (int)r.length;
+  for (int j = 0; j < L; ++j) {
+    point P;
+    P.pos = (int)r.center[j];
+    P.id = ID;
+    B.center.push_back(P);
+    B.at_time.push_back(r.at_time[j]);
+    B.V.push_back(r.volume[j]);
+    B.PotEn.push_back(r.pot_en[j]);
+    B.KinEn.push_back(r.kin_en[j]);
+    B.GradEn.push_back(r.grad_en[j]);
+    B.avPhi.push_back(r.av_phi[j]);
+    B.Peak_value.push_back(r.peak_value[j]);
+    B.addr.push_back(-1);
+    B.addl.push_back(-1);
+  }
+  B.index = (int)r.index;
+  B.status = (int)r.status;
+  B.disp = r.disp != 0.0;
+  return B;
+}
+
+static void mirror_set(int set, std::vector<island> &dst) {
+  int n = 0;
+  check(phn_tracker_count(tracker, set, &n), "phn_tracker_count");
+  dst.clear();
+  phn_track_island r;
+  for (int i = 0; i < n; ++i) {
+    check(phn_tracker_get(tracker, set, i, &r), "phn_tracker_get");
+    dst.push_back(to_island(r));
+  }
+}
+
+inline void Full_Analysis() {
+  using namespace island_analysis;
+  if (!tracker) check(phn_tracker_create(ID, &tracker), "phn_tracker_create");
+  check(phn_tracker_update(tracker, handle, thres, PHN_ISLAND_REFERENCE, 0, b), "phn_tracker_update");
+  // retired islands through the reference's Old_islands: their centres are
+  // outside the mask, so the host copy of the fields is set to 0 there first
+  mirror_set(PHN_TRACK_RETIRED, found_islands);
+  if (!found_islands.empty()) {
+    for (island &B : found_islands)
+      for (int a = 0; a < Nc; ++a) {
+        LocalLattice::Phi[B.center.back().pos + a] = 0;
+        LocalLattice::Pi[B.center.back().pos + a] = 0;
+      }
+    Old_islands();
+  }
+  // bubbles reported this update, printed from their own records
+  std::vector<island> bubbles;
+  mirror_set(PHN_TRACK_BUBBLES, bubbles);
+  for (island &B : bubbles) {
+    found_islands.assign(1, B);
+    print_bubble_history(0);
+  }
+  mirror_set(PHN_TRACK_ALIVE, found_islands);
 }
 
 }  // namespace phn_gpu

@@ -56,6 +56,7 @@ int main(int argc, char **argv) {
       phn_gpu::Print_AveragesExtrema();
       if (false_vacuum_decayed()) break;
       phn_gpu::Print_fp();
+      if (numeric::total_stepcount % 5 == 0) phn_gpu::Full_Analysis();  // main.cpp:81-84
     }
     phn_gpu::to_host();
     phn_gpu::fin();
