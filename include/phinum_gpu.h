@@ -179,6 +179,24 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic);
 int phn_islands(phn_handle *h, double thres, int mode, int z_periodic, int *labels, phn_island *out,
                 int max_out, int *n_islands);
 
+/* SaveConfig(Name) (fieldanalysis.cpp:252-283): writes <dir>/field-<name>-<rank>.out,
+ * one line "%.17e %.17e\n" of Phi and Pi per interior site in the reference
+ * layout's order ("%.9e %.9e\n" of the float values for PHN_FP32 handles, as
+ * the reference's single-precision build writes), and for rank 0
+ * <dir>/moment-<name>.out with tau as an ostream prints it.  The bytes are the
+ * reference's; lines are formatted on nthreads host threads (0: all cores).
+ * dir NULL or "" means the working directory, as the reference uses. */
+int phn_save_config(phn_handle *h, const char *dir, int name, int rank, int nthreads);
+/* ExtractConfig(Name) (fieldanalysis.cpp:285-312): reads those files into the
+ * handle; *t0 (optional) receives the time stamp, which the reference
+ * assigns to T0. */
+int phn_load_config(phn_handle *h, const char *dir, int name, int rank, double *t0, int nthreads);
+/* The file formatting and parsing alone, on host arrays in the reference
+ * layout (interior slabs; no device involved). */
+int phn_write_config_file(const char *path, const double *Phi, const double *Pi, int N, int Nc, int precision,
+                          int nthreads);
+int phn_read_config_file(const char *path, double *Phi, double *Pi, int N, int Nc, int nthreads);
+
 /* After phn_islands: the island (numbered as phn_islands numbers them) that
  * holds each queried site, reference-layout indices; -1 outside the mask. */
 int phn_islands_lookup(phn_handle *h, const long long *pos, int n, int *island);

@@ -315,6 +315,7 @@ class Reference:
         lib.ref_spectrum.argtypes = [_PD, _PD, _PD, _PI]
         lib.ref_islands.argtypes = [_D, _PI, _PD, _I]
         lib.ref_islands.restype = _I
+        lib.ref_save_config.argtypes = [_I]
         lib.ref_track_step.argtypes = [_D, _PI]
         lib.ref_track_step.restype = _I
         lib.ref_track_island.argtypes = [_I, _PD]
@@ -336,6 +337,10 @@ class Reference:
         if r != 0:
             raise RuntimeError("ref_initial_conditions failed")
         return self.get_fields()
+
+    def save_config(self, name: int):
+        """The reference's SaveConfig: files in the working directory."""
+        self.lib.ref_save_config(int(name))
 
     def track_reset(self):
         self.lib.ref_track_reset()

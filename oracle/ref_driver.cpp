@@ -288,6 +288,10 @@ int ref_track_island(int i, double *out) {
   return L;
 }
 
+/* SaveConfig(Name) (fieldanalysis.cpp:252-283): writes ./field-<name>-0.out
+ * and ./moment-<name>.out in the working directory. */
+void ref_save_config(int name) { SaveConfig(name); }
+
 /* SetInitialConditions() (initialize 3) with srand48(seed); the fields land
  * in LocalLattice::Phi/Pi (read them with ref_get_fields). */
 int ref_initial_conditions(long seed, int justnoise_, double qs, double scale2_, double amplitude, double noise,

@@ -81,6 +81,10 @@ _SIGS = {
     "phn_spectrum_uniform": (_I, [ctypes.c_void_p, _I, _PD, _PD, _PD, _PI]),
     "phn_initial_conditions": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams)]),
     "phn_islands_lookup": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _I, _PI]),
+    "phn_save_config": (_I, [ctypes.c_void_p, ctypes.c_char_p, _I, _I, _I]),
+    "phn_load_config": (_I, [ctypes.c_void_p, ctypes.c_char_p, _I, _I, _PD, _I]),
+    "phn_write_config_file": (_I, [ctypes.c_char_p, _PD, _PD, _I, _I, _I, _I]),
+    "phn_read_config_file": (_I, [ctypes.c_char_p, _PD, _PD, _I, _I, _I]),
     "phn_tracker_create": (_I, [_I, ctypes.POINTER(ctypes.c_void_p)]),
     "phn_tracker_destroy": (_I, [ctypes.c_void_p]),
     "phn_tracker_reset": (_I, [ctypes.c_void_p]),

@@ -111,6 +111,17 @@ class Lattice:
                            (ctypes.c_double * 2)(*pi0), m2l, m2t)
         L.check(self.lib.phn_initial_conditions(self.h, ctypes.byref(ic)))
 
+    def save_config(self, name: int, directory: str = ".", rank: int = 0, nthreads: int = 0):
+        """SaveConfig: field-<name>-<rank>.out (and moment-<name>.out) in the reference's format."""
+        L.check(self.lib.phn_save_config(self.h, directory.encode(), int(name), int(rank), int(nthreads)))
+
+    def load_config(self, name: int, directory: str = ".", rank: int = 0, nthreads: int = 0) -> float:
+        """ExtractConfig: reads the files back; returns the time stamp (the reference's T0)."""
+        t0 = ctypes.c_double()
+        L.check(self.lib.phn_load_config(self.h, directory.encode(), int(name), int(rank), ctypes.byref(t0),
+                                         int(nthreads)))
+        return t0.value
+
     # -------------------------------------------------------------- clock
     def reset(self):
         L.check(self.lib.phn_reset(self.h))

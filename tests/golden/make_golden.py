@@ -109,6 +109,41 @@ def run_track_case(name: str) -> None:
     print(f"track/{name}: calls={ncalls} islands per call max={max(np.diff(offs))} total={offs[-1]}")
 
 
+# Checkpoint files (SaveConfig): lattice params, input seed, precision build
+CONFIG_CASES = {"n8_f64": (dict(N=8, Nc=1, **PHI6), 11, "f64"), "n8_nc2_f64": (dict(N=8, Nc=2, **PHI6), 12, "f64"),
+                "n8_f32": (dict(N=8, Nc=1, **PHI6), 13, "f32")}
+
+
+def run_config_case(name: str) -> None:
+    """The reference's SaveConfig(3) on seeded fields, run in a scratch
+    directory: SHA-256 of field-3-0.out and the text of moment-3.out."""
+    import tempfile
+    from oracle import oracle as O
+    import inputs
+    pd, seed, prec = CONFIG_CASES[name]
+    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, seed, phi0=SQRT6)
+    R = O.Reference(p, prec)
+    R.set_fields(O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc))
+    R.reset()
+    R.evolve(3)
+    phi, pi = R.get_fields()
+    with tempfile.TemporaryDirectory() as tmp:
+        cwd = os.getcwd()
+        os.chdir(tmp)
+        try:
+            R.save_config(3)
+            raw = open("field-3-0.out", "rb").read()
+            moment = open("moment-3.out").read()
+        finally:
+            os.chdir(cwd)
+    out = os.path.join(HERE, "config")
+    os.makedirs(out, exist_ok=True)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), params=json.dumps(pd), prec=prec, phi=phi, pi=pi,
+                        sha=hashlib.sha256(raw).hexdigest(), nbytes=len(raw), moment=moment)
+    print(f"config/{name}: {len(raw)} bytes, moment {moment.strip()}")
+
+
 def run_ic_case(name: str) -> None:
     from oracle import oracle as O
     pd, ic = IC_CASES[name]
@@ -192,6 +227,13 @@ def main() -> None:
         for name in TRACK_CASES:
             subprocess.run([sys.executable, os.path.abspath(__file__), "--track-case", name], check=True)
         return
+    if len(sys.argv) > 2 and sys.argv[1] == "--config-case":
+        run_config_case(sys.argv[2])
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "--config":
+        for name in CONFIG_CASES:
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--config-case", name], check=True)
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "--ic":
         for name in IC_CASES:
             subprocess.run([sys.executable, os.path.abspath(__file__), "--ic-case", name], check=True)
@@ -204,6 +246,8 @@ def main() -> None:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--ic-case", name], check=True)
     for name in TRACK_CASES:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--track-case", name], check=True)
+    for name in CONFIG_CASES:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--config-case", name], check=True)
 
 
 if __name__ == "__main__":
