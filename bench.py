@@ -560,6 +560,39 @@ def initial_form(N: int, n_cpu: int = 128, n_check: int = 64):
     return out
 
 
+def io_form(N: int, directory: str):
+    """Checkpoint files (SaveConfig / ExtractConfig format): phn_save_config
+    and phn_load_config on an N^3 FP64 lattice with all host threads and with
+    one (the reference's single fprintf loop), wall time each; the two
+    outputs are compared byte for byte."""
+    import hashlib
+    from phinum_gb300 import lattice as PL
+    phi, pi = make_fields(N)
+    out = {"form": "io", "N": N, "lines": N ** 3}
+    os.makedirs(directory, exist_ok=True)
+    with PL.Lattice(PL.Params(N=N, precision=0)) as lat:
+        lat.upload(phi, pi)
+        for name, nt in (("all_threads", 0), ("one_thread", 1)):
+            d = os.path.join(directory, name)
+            os.makedirs(d, exist_ok=True)
+            t0 = time.perf_counter()
+            lat.save_config(1, d, nthreads=nt)
+            ts = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            lat.load_config(1, d, nthreads=nt)
+            tl = time.perf_counter() - t0
+            path = os.path.join(d, "field-1-0.out")
+            with open(path, "rb") as f:
+                sha = hashlib.sha256(f.read()).hexdigest()
+            out[name] = {"threads": nt if nt else os.cpu_count(), "save_s": ts, "load_s": tl,
+                         "bytes": os.path.getsize(path), "sha256": sha}
+            os.remove(path)
+    out["identical_bytes"] = out["all_threads"]["sha256"] == out["one_thread"]["sha256"]
+    out["save_speedup"] = out["one_thread"]["save_s"] / out["all_threads"]["save_s"]
+    out["load_speedup"] = out["one_thread"]["load_s"] / out["all_threads"]["load_s"]
+    return out
+
+
 def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int):
     """The oracle's reference loop (FP64) on all host threads, bounded."""
     from oracle import oracle as O
@@ -590,7 +623,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--n", type=int, default=N_MAIN, help="lattice edge (profiling runs use smaller cases)")
     ap.add_argument("--variant", type=int, default=None, help="TMA kernel variant instead of the autotuner's pick")
-    ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble", "initial"],
+    ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble", "initial", "io"],
                     help="report one of the north-star forms instead of the benchmark line")
     args = ap.parse_args()
     rank, local, world = env_rank()
@@ -607,6 +640,15 @@ def main():
     if args.form == "adjoint":
         kw = dict(check=False) if args.quick else {}
         print(json.dumps(adjoint_form(args.n, args.steps, **kw)))
+        return
+    if args.form == "io":
+        import shutil
+        import tempfile
+        scratch = tempfile.mkdtemp(prefix="phn_io_")
+        try:
+            print(json.dumps(io_form(args.n, scratch)))
+        finally:
+            shutil.rmtree(scratch, ignore_errors=True)
         return
     if args.form == "initial":
         print(json.dumps(initial_form(args.n)))
