@@ -179,6 +179,15 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic);
 int phn_islands(phn_handle *h, double thres, int mode, int z_periodic, int *labels, phn_island *out,
                 int max_out, int *n_islands);
 
+/* apply_filter(r_filter, which_filter) (filter.cpp:53-133): every component
+ * of phi and pi is multiplied in momentum space by a window of |p|: a top hat
+ * (W_tophat), a Gaussian (W_gaussian), a tabulated window (W_import_bounce:
+ * table[min(int(|p| / dp), ntable - 1)], the reference reads it from
+ * bounce.txt) or a sharp cut at 2 pi / r (W_ktophat).  Compensated FP32
+ * handles restart their compensation at zero. */
+enum { PHN_FILTER_TOPHAT = 0, PHN_FILTER_GAUSSIAN = 1, PHN_FILTER_TABLE = 2, PHN_FILTER_KTOPHAT = 3 };
+int phn_apply_filter(phn_handle *h, double r_filter, int which, const double *table, int ntable, double dp);
+
 /* SaveConfig(Name) (fieldanalysis.cpp:252-283): writes <dir>/field-<name>-<rank>.out,
  * one line "%.17e %.17e\n" of Phi and Pi per interior site in the reference
  * layout's order ("%.9e %.9e\n" of the float values for PHN_FP32 handles, as

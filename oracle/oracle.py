@@ -155,6 +155,8 @@ def _load(fast: bool = False):
         lib.orc_spectrum_uniform.restype = _I
         lib.orc_initial_conditions.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CIc), _PD, _PD]
         lib.orc_initial_conditions.restype = _I
+        lib.orc_apply_filter.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _D, _I, _PD, _I, _D]
+        lib.orc_apply_filter.restype = _I
         lib.orc_spectrum_columns.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _PD, _PI, _I, _PD]
         lib.orc_islands.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _D, _I, _I, _PI, _PD, _I]
         lib.orc_islands.restype = _I
@@ -249,6 +251,15 @@ def initial_conditions(p: Params, **kw):
     return phi, pi
 
 
+def apply_filter(p: Params, phi: np.ndarray, pi: np.ndarray, r: float, which: int, table=None, dp: float = 0.0):
+    """apply_filter on copies of Phi, Pi (reference layout); returns them."""
+    phi, pi = np.array(phi, dtype=np.float64), np.array(pi, dtype=np.float64)
+    t = np.ascontiguousarray(table if table is not None else np.zeros(1), dtype=np.float64)
+    _load().orc_apply_filter(ctypes.byref(_cp(p)), _ptr(phi), _ptr(pi), float(r), int(which), _ptr(t), t.size,
+                             float(dp))
+    return phi, pi
+
+
 def spectrum_columns(p: Params, F, K, Q, C) -> np.ndarray:
     nb = C.size
     cols = np.zeros((nb, 7))
@@ -316,6 +327,8 @@ class Reference:
         lib.ref_islands.argtypes = [_D, _PI, _PD, _I]
         lib.ref_islands.restype = _I
         lib.ref_save_config.argtypes = [_I]
+        lib.ref_apply_filter.argtypes = [_D, _I, _PD, _I, _D]
+        lib.ref_apply_filter.restype = _I
         lib.ref_track_step.argtypes = [_D, _PI]
         lib.ref_track_step.restype = _I
         lib.ref_track_island.argtypes = [_I, _PD]
@@ -336,6 +349,13 @@ class Reference:
                                             q["pi0"][0], q["pi0"][1])
         if r != 0:
             raise RuntimeError("ref_initial_conditions failed")
+        return self.get_fields()
+
+    def apply_filter(self, r: float, which: int, table=None, dp: float = 0.0):
+        """The reference's apply_filter on its current fields; returns Phi, Pi."""
+        t = np.ascontiguousarray(table if table is not None else np.zeros(1), dtype=np.float64)
+        if self.lib.ref_apply_filter(float(r), int(which), _ptr(t), t.size, float(dp)) != 0:
+            raise RuntimeError("ref_apply_filter failed")
         return self.get_fields()
 
     def save_config(self, name: int):

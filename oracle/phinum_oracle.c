@@ -22,6 +22,7 @@
  *   orc_initial_conditions  SetInitialConditions (initialize 3), ensureRealResult,
  *                        fftPtoX            initialconditions.cpp:14-723,
  *                                           clusterfft.cpp:10-16,55-182
+ *   orc_apply_filter     apply_filter      filter.cpp:11-133
  *   orc_islands          is_island()/BFS()/Full_Analysis() scan
  *                                                     islands.cpp:72-279,778-840
  * for theories 0 (phi^4 + phi^6) and 1 (phi^4 + linear h), static box, one
@@ -601,6 +602,76 @@ int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, d
     }
   orc_exchange(p, Phi); /* Communication::exchange moves Phi only (comm.cpp:63-78) */
   free(Are); free(Aim); free(Ere); free(Eim); free(X);
+  return 0;
+}
+
+/* ------------------------------------------------------- momentum filter */
+/* Window functions of filter.cpp:11-51. */
+static double flt_w(int which, double r, double p, const double *table, int ntable, double dp) {
+  if (which == 0) {
+    if (p * r == 0) return 1;
+    return 3. * (sin(p * r) / (p * p * p * r * r * r) - cos(p * r) / (p * p * r * r));
+  }
+  if (which == 1) return exp(-p * p * r * r / 2.);
+  if (which == 2) {
+    if (p > (ntable - 1) * dp) return table[ntable - 1];
+    return table[(int)(p / dp)];
+  }
+  {
+    const double P = 2. * acos(-1.) / r;
+    return p < P ? 1 : 0;
+  }
+}
+
+/* |p| of a stored mode (px, py <= N/2, pz) as apply_filter computes it
+ * (filter.cpp:76-99). */
+static double flt_pabs(int px, int py, int pz, int N, double a) {
+  double nu, ppx, ppy;
+  if (pz == 0) nu = 0;
+  else if (pz < N / 2 + 1) nu = 2.0 / (a) * sin((pz) * acos(-1.) / N);
+  else nu = -2.0 / (a) * sin((pz) * acos(-1.) / N);
+  if (px < N / 2 + 1) ppx = 2.0 / (a) * sin(px * acos(-1.) / N);
+  else ppx = -2.0 / (a) * sin(px * acos(-1.) / N);
+  ppy = 2.0 / (a) * sin(py * acos(-1.) / N);
+  return sqrt(sqr(ppx) + sqr(ppy) + sqr(nu));
+}
+
+/* apply_filter(r_filter, which) (filter.cpp:53-133), one rank: each
+ * component of Phi and Pi goes to momentum space (fftXtoP_direct, x a^3),
+ * every mode is multiplied by W(r, |p|) -- a mode with py > N/2, which the
+ * reference holds as its conjugate, takes the conjugate's |p| -- and back
+ * (fftPtoX_direct, / L^3) into the interior.  which: 0 top hat, 1 Gaussian,
+ * 2 tabulated (table[ntable], spacing dp), 3 sharp cut at 2 pi / r. */
+int orc_apply_filter(const orc_params *p, double *Phi, double *Pi, double r, int which, const double *table,
+                     int ntable, double dp) {
+  const int N = p->N, Nc = p->Nc;
+  const long NN = (long)N * N, V = NN * N;
+  double *re = (double *)malloc(sizeof(double) * V), *im = (double *)malloc(sizeof(double) * V);
+  double *wr = (double *)malloc(sizeof(double) * N), *wi = (double *)malloc(sizeof(double) * N);
+  const double Norm = sqr(p->a * N) * N * p->a;
+  for (int f = 0; f < 2; f++)
+    for (int c = 0; c < Nc; c++) {
+      double *fld = f == 0 ? Phi : Pi;
+      forward_fft(p, fld, c, re, im); /* re/im[kx + N ky + N^2 kz], x a^3 */
+      for (int kz = 0; kz < N; kz++)
+        for (int ky = 0; ky < N; ky++)
+          for (int kx = 0; kx < N; kx++) {
+            int px = kx, py = ky, pz = kz;
+            if (ky > N / 2) { px = mod(N - kx, N); py = N - ky; pz = mod(N - kz, N); }
+            const double w = flt_w(which, r, flt_pabs(px, py, pz, N, p->a), table, ntable, dp);
+            const long i = kx + (long)N * ky + NN * kz;
+            re[i] *= w;
+            im[i] = -(im[i] * w); /* conjugate in: the inverse is conj(DFT(conj)) */
+          }
+      for (long q = 0; q < NN; q++) dft_line(re + q * N, im + q * N, N, 1, wr, wi);
+      for (int z = 0; z < N; z++)
+        for (int x = 0; x < N; x++) dft_line(re + x + NN * z, im + x + NN * z, N, N, wr, wi);
+      for (long q = 0; q < NN; q++) dft_line(re + q, im + q, N, NN, wr, wi);
+      for (int z = 0; z < N; z++)
+        for (int y = 0; y < N; y++)
+          for (int x = 0; x < N; x++) fld[c + pos3(p, x, y, z + 1)] = re[x + N * y + NN * z] / Norm;
+    }
+  free(re); free(im); free(wr); free(wi);
   return 0;
 }
 

@@ -72,6 +72,8 @@ int orc_run_loop(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int
                  orc_row *rows, int max_rows, int nthreads);
 void orc_spectrum_bins(const orc_params *p, int *nbins, double *binsize);
 int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, double *Pi);
+int orc_apply_filter(const orc_params *p, double *Phi, double *Pi, double r, int which, const double *table,
+                     int ntable, double dp);
 int orc_spectrum(const orc_params *p, const double *Phi, const double *Pi, double *F, double *K, double *Q,
                  int *counts);
 int orc_spectrum_uniform(const orc_params *p, const double *Phi, const double *Pi, int nbins, double *F, double *K,

@@ -60,6 +60,7 @@ static time_t phn_ref_seed_clock(time_t *) { return (time_t)g_ref_seed; }
 #define time(x) phn_ref_seed_clock(x)
 #include "initialconditions.cpp"
 #undef time
+#include "filter.cpp"
 
 /* ---- extern "C" surface for the golden-vector generator -------------------- */
 namespace {
@@ -286,6 +287,19 @@ int ref_track_island(int i, double *out) {
     e[7] = B.Peak_value[(size_t)j];
   }
   return L;
+}
+
+/* apply_filter(r, which) (filter.cpp:53-133) on the current fields; for
+ * which = 2 the table W_import[0..n) and dp_import are set first (the
+ * reference reads them from bounce.txt, filter.cpp:32-44). */
+int ref_apply_filter(double r, int which, const double *table, int n, double dp) {
+  if (which == 2) {
+    if (!table || n < 1 || n > 25000) return -1;
+    for (int i = 0; i < 25000; ++i) ImportFilter::W_import[i] = (pseudo_double)table[i < n ? i : n - 1];
+    ImportFilter::dp_import = (pseudo_double)dp;
+  }
+  apply_filter((pseudo_double)r, which);
+  return 0;
 }
 
 /* SaveConfig(Name) (fieldanalysis.cpp:252-283): writes ./field-<name>-0.out

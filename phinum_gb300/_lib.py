@@ -19,6 +19,7 @@ FP64, FP32, FP32_KAHAN = 0, 1, 2
 ISLAND_REFERENCE, ISLAND_ENERGY = 0, 1
 PATH_AUTO, PATH_PLAIN, PATH_TMA, PATH_X4 = 0, 1, 2, 3
 TRACK_ALIVE, TRACK_RETIRED, TRACK_BUBBLES = 0, 1, 2
+FILTER_TOPHAT, FILTER_GAUSSIAN, FILTER_TABLE, FILTER_KTOPHAT = 0, 1, 2, 3
 
 _D, _I = ctypes.c_double, ctypes.c_int
 _PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
@@ -82,6 +83,7 @@ _SIGS = {
     "phn_initial_conditions": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams)]),
     "phn_islands_lookup": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _I, _PI]),
     "phn_save_config": (_I, [ctypes.c_void_p, ctypes.c_char_p, _I, _I, _I]),
+    "phn_apply_filter": (_I, [ctypes.c_void_p, _D, _I, _PD, _I, _D]),
     "phn_load_config": (_I, [ctypes.c_void_p, ctypes.c_char_p, _I, _I, _PD, _I]),
     "phn_write_config_file": (_I, [ctypes.c_char_p, _PD, _PD, _I, _I, _I, _I]),
     "phn_read_config_file": (_I, [ctypes.c_char_p, _PD, _PD, _I, _I, _I]),

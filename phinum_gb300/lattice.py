@@ -111,6 +111,11 @@ class Lattice:
                            (ctypes.c_double * 2)(*pi0), m2l, m2t)
         L.check(self.lib.phn_initial_conditions(self.h, ctypes.byref(ic)))
 
+    def apply_filter(self, r_filter: float, which: int, table=None, dp: float = 0.0):
+        """apply_filter (filter.cpp:53-133): 0 top hat, 1 Gaussian, 2 table, 3 sharp cut."""
+        t = np.ascontiguousarray(table if table is not None else np.zeros(1), dtype=np.float64)
+        L.check(self.lib.phn_apply_filter(self.h, float(r_filter), int(which), _pd(t), t.size, float(dp)))
+
     def save_config(self, name: int, directory: str = ".", rank: int = 0, nthreads: int = 0):
         """SaveConfig: field-<name>-<rank>.out (and moment-<name>.out) in the reference's format."""
         L.check(self.lib.phn_save_config(self.h, directory.encode(), int(name), int(rank), int(nthreads)))

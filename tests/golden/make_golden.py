@@ -144,6 +144,35 @@ def run_config_case(name: str) -> None:
     print(f"config/{name}: {len(raw)} bytes, moment {moment.strip()}")
 
 
+# Momentum-space filter: lattice params, input seed, r_filter, which
+FILTER_CASES = {"n8_tophat": (dict(N=8, Nc=1, **PHI6), 21, 0.6, 0), "n8_gauss": (dict(N=8, Nc=1, **PHI6), 22, 0.6, 1),
+                "n12_table": (dict(N=12, Nc=1, **PHI6), 23, 0.6, 2),
+                "n12_nc2_ktophat": (dict(N=12, Nc=2, **PHI6), 24, 0.6, 3),
+                "n16_tophat": (dict(N=16, Nc=1, **TDW), 25, 0.9, 0)}
+FILTER_TABLE_DP = 0.01
+
+
+def filter_table() -> np.ndarray:
+    """The tabulated window of the which = 2 case (25000 entries, spacing 0.01)."""
+    return np.exp(-np.arange(25000) * 0.001) * (1.0 + 0.1 * np.cos(np.arange(25000) * 0.01))
+
+
+def run_filter_case(name: str) -> None:
+    """The reference's apply_filter on seeded fields."""
+    from oracle import oracle as O
+    import inputs
+    pd, seed, r, which = FILTER_CASES[name]
+    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, seed, phi0=SQRT6)
+    R = O.Reference(p)
+    R.set_fields(O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc))
+    phi, pi = R.apply_filter(r, which, filter_table(), FILTER_TABLE_DP)
+    os.makedirs(os.path.join(HERE, "filter"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "filter", f"{name}.npz"), params=json.dumps(pd), seed=seed, r=r,
+                        which=which, dp=FILTER_TABLE_DP, phi=phi, pi=pi)
+    print(f"filter/{name}")
+
+
 def run_ic_case(name: str) -> None:
     from oracle import oracle as O
     pd, ic = IC_CASES[name]
@@ -227,6 +256,13 @@ def main() -> None:
         for name in TRACK_CASES:
             subprocess.run([sys.executable, os.path.abspath(__file__), "--track-case", name], check=True)
         return
+    if len(sys.argv) > 2 and sys.argv[1] == "--filter-case":
+        run_filter_case(sys.argv[2])
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "--filter":
+        for name in FILTER_CASES:
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--filter-case", name], check=True)
+        return
     if len(sys.argv) > 2 and sys.argv[1] == "--config-case":
         run_config_case(sys.argv[2])
         return
@@ -248,6 +284,8 @@ def main() -> None:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--track-case", name], check=True)
     for name in CONFIG_CASES:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--config-case", name], check=True)
+    for name in FILTER_CASES:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--filter-case", name], check=True)
 
 
 if __name__ == "__main__":
