@@ -6,8 +6,13 @@
 // the x axis where the reference's transposed transform halves y; a mode
 // whose y index is above N/2 is held by the reference as its conjugate, so
 // its |p| is taken from that conjugate's indices, exactly as the reference's
-// loop (filter.cpp:76-99) evaluates it.  Per-axis momenta come from the host
-// C library (the reference's values); the windows' exp/sin/cos are CUDA's.
+// loop (filter.cpp:76-99) evaluates it.  On the planes y = 0 and y = N/2 the
+// reference stores both p and -p, each with its own window value (their |p|
+// can differ in the last bit); the inverse transform then sees the average
+// of the two for the real field, so those modes get (W(p) + W(-p)) / 2, which
+// is W itself unless a discontinuous window separates them.  Per-axis momenta
+// come from the host C library (the reference's values); the windows'
+// exp/sin/cos are CUDA's.
 #include <cufft.h>
 #include <math.h>
 
@@ -37,6 +42,12 @@ __device__ __forceinline__ double flt_window(const FltArgs &f, double p, const d
   return p < P ? 1 : 0;
 }
 
+// |p| of the reference's stored mode (px, py <= N/2, pz): filter.cpp:76-99.
+__device__ __forceinline__ double flt_pabs(const double *ptab, int px, int py, int pz) {
+  const double ppx = ptab[px], ppy = ptab[py], nu = pz == 0 ? 0.0 : ptab[pz];
+  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)), __dmul_rn(nu, nu)));
+}
+
 // C: float2 or double2 half spectrum [kz][ky][kx <= N/2].
 template <typename C>
 __global__ void flt_modes(C *__restrict__ F, const double *__restrict__ ptab, const double *__restrict__ table,
@@ -46,15 +57,16 @@ __global__ void flt_modes(C *__restrict__ F, const double *__restrict__ ptab, co
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const int kx = (int)(i % M), ky = (int)((i / M) % N), kz = (int)(i / ((long long)M * N));
-    int px = kx, py = ky, pz = kz;
-    if (ky > N / 2) {  // the reference holds the conjugate mode
-      px = (N - kx) % N;
-      py = N - ky;
-      pz = (N - kz) % N;
+    double w;
+    if (ky == 0 || 2 * ky == N) {  // both p and -p are stored by the reference
+      const double w1 = flt_window(f, flt_pabs(ptab, kx, ky, kz), table);
+      const double w2 = flt_window(f, flt_pabs(ptab, (N - kx) % N, ky, (N - kz) % N), table);
+      w = 0.5 * (w1 + w2);
+    } else if (ky > N / 2) {  // the reference holds the conjugate mode
+      w = flt_window(f, flt_pabs(ptab, (N - kx) % N, N - ky, (N - kz) % N), table);
+    } else {
+      w = flt_window(f, flt_pabs(ptab, kx, ky, kz), table);
     }
-    const double ppx = ptab[px], ppy = ptab[py], nu = pz == 0 ? 0.0 : ptab[pz];
-    const double pabs = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)), __dmul_rn(nu, nu)));
-    const double w = flt_window(f, pabs, table);
     C v = F[i];
     v.x = (decltype(v.x))(((double)(decltype(v.x))(f.factor * (double)v.x)) * w);
     v.y = (decltype(v.y))(((double)(decltype(v.y))(f.factor * (double)v.y)) * w);
