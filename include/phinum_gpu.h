@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PHN_ABI_VERSION 1
+#define PHN_ABI_VERSION 2
 #define PHN_MAX_NC 4
 
 enum {
@@ -58,9 +58,11 @@ enum {
 typedef struct phn_params {
   int N;           /* N_t = N_eta: lattice edge (cubic box) */
   int Nc;          /* field components, 1..PHN_MAX_NC */
-  int potential;   /* the reference's `theory`: 0 phi^4+phi^6 (Kappa), 1 phi^4 + linear h
-                      (parameters.cpp:86-120); named apart because the reference
-                      #defines `theory` in the translation unit that includes this */
+  int potential;   /* the reference's `theory` (parameters.cpp:86-170): 0 phi^4 + phi^6 (Kappa),
+                      1 phi^4 + linear h, 2 cosine, 3 cosine + monodromy mass,
+                      4 cubic (g), 5 power-law monodromy (p_mono); 2-5 with Nc = 1.
+                      Named apart because the reference #defines `theory` in the
+                      translation unit that includes this */
   int mass_mode;   /* Mass_Mode */
   int lambda_mode; /* Lambda_Mode */
   int precision;   /* PHN_FP64 / PHN_FP32 / PHN_FP32_KAHAN */
@@ -70,6 +72,9 @@ typedef struct phn_params {
   double m_sqr;    /* M_sqr (bare masses without tadpole renormalisation) */
   double kappa;    /* Kappa, theory 0 */
   double h;        /* h, theory 1 */
+  double g;        /* g, theory 4 */
+  double p_mono;   /* p_mono, theory 5 */
+  double m_mono_sqr; /* M_mono_sqr, theory 3 */
 } phn_params;
 
 /* One SO row: the outputs of CalculateVolumeAverages + CalculateExtrema

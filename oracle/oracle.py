@@ -47,12 +47,15 @@ class Params:
     m_sqr: float = 1.0
     kappa: float = 3.0 ** 0.5
     h: float = 0.0
+    g: float = 2.0            # theory 4
+    p_mono: float = -0.5      # theory 5
+    m_mono_sqr: float = 1.0   # theory 3
 
 
 class _CParams(ctypes.Structure):
     _fields_ = [("N", _I), ("Nc", _I), ("theory", _I), ("mass_mode", _I), ("lambda_mode", _I),
                 ("pad_", _I), ("a", _D), ("dt", _D), ("T0", _D), ("m_sqr", _D), ("kappa", _D),
-                ("h", _D)]
+                ("h", _D), ("g", _D), ("p_mono", _D), ("m_mono_sqr", _D)]
 
 
 class _CClock(ctypes.Structure):
@@ -73,7 +76,7 @@ IC_DEFAULTS = dict(seed=1, justnoise=0, QS=1.0, scale2=1.0, amplitude=0.0, noise
 
 def _cp(p: Params) -> _CParams:
     return _CParams(p.N, p.Nc, p.theory, p.mass_mode, p.lambda_mode, 0, p.a, p.dt, p.T0,
-                    p.m_sqr, p.kappa, p.h)
+                    p.m_sqr, p.kappa, p.h, p.g, p.p_mono, p.m_mono_sqr)
 
 
 def _ptr(a: np.ndarray, kind=_PD):
@@ -336,6 +339,8 @@ class Reference:
         lib.ref_initial_conditions.argtypes = [ctypes.c_long, _I, _D, _D, _D, _D, _D, _D, _D, _D]
         lib.ref_initial_conditions.restype = _I
         self.lib = lib
+        lib.ref_set_extra.argtypes = [_D, _D, _D]
+        lib.ref_set_extra(p.g, p.p_mono, p.m_mono_sqr)
         r = lib.ref_init(p.N, p.Nc, p.a, p.dt, p.T0, p.mass_mode, p.m_sqr, p.lambda_mode, 1.0,
                          p.kappa, p.h)
         if r != 0:

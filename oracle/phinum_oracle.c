@@ -25,7 +25,8 @@
  *   orc_apply_filter     apply_filter      filter.cpp:11-133
  *   orc_islands          is_island()/BFS()/Full_Analysis() scan
  *                                                     islands.cpp:72-279,778-840
- * for theories 0 (phi^4 + phi^6) and 1 (phi^4 + linear h), static box, one
+ * for theories 0 (phi^4 + phi^6), 1 (phi^4 + linear h), 2 (cosine), 3
+ * (cosine + monodromy mass), 4 (cubic) and 5 (power-law monodromy), static box, one
  * rank (z-slab count 1), Nc components interleaved innermost.
  *
  * Parity pin: the FP64 results are bit-identical to the reference's own
@@ -85,7 +86,8 @@ void orc_exchange(const orc_params *p, double *f) {
   memcpy(f, f + (long)p->N * slab, (size_t)slab * sizeof(double));
 }
 
-/* updateMomenta(): dynamics.cpp:52-175 for theory 0 (:82-87) and 1 (:96-101),
+/* updateMomenta(): dynamics.cpp:52-175 for theories 0 (:82-87), 1 (:96-101),
+ * 2 (:109-114), 3 (:123-129), 4 (:137-143) and 5 (:151-157), static box,
  * slabs z in [z0, z1). */
 static void update_momenta_slabs(const orc_params *p, const double *Phi, double *Pi,
                                  double factor, int z0, int z1) {
@@ -110,6 +112,17 @@ static void update_momenta_slabs(const orc_params *p, const double *Phi, double 
             Pi[Kooo] += (LapPhi - ((double)p->mass_mode * mass +
                                    (double)p->lambda_mode * (locPhiSqr / (6. * Nc)) +
                                    (sqr(locPhiSqr / p->kappa) / (120. * Nc * Nc))) * Phi[Kooo]) * factor;
+          } else if (p->theory == 2) {
+            Pi[Kooo] += (LapPhi - mass * sqrt(mass) * (Phi[Kooo] / sqrt(locPhiSqr)) *
+                                      sin(sqrt(locPhiSqr) / sqrt(mass))) * factor;
+          } else if (p->theory == 3) {
+            Pi[Kooo] += (LapPhi - p->m_mono_sqr * Phi[Kooo] - mass * sqrt(mass) * (Phi[Kooo] / sqrt(locPhiSqr)) *
+                                      sin(sqrt(locPhiSqr) / sqrt(mass))) * factor;
+          } else if (p->theory == 4) {
+            Pi[Kooo] += (LapPhi - ((double)p->mass_mode * mass - p->g * Phi[Kooo] / 2. +
+                                   (double)p->lambda_mode * (locPhiSqr / (6. * Nc))) * Phi[Kooo]) * factor;
+          } else if (p->theory == 5) {
+            Pi[Kooo] += (LapPhi - mass * Phi[Kooo] * pow((1. + locPhiSqr / mass), (p->p_mono - 1))) * factor;
           } else {
             if (a == 0)
               Pi[Kooo] += (LapPhi - p->h - ((double)p->mass_mode * mass +
@@ -179,7 +192,29 @@ static void extrema(const orc_params *p, const double *Phi, orc_row *o) {
   o->max_abs_pos = (double)maxAbspos;
 }
 
-/* CalculateVolumeAverages(): fieldanalysis.cpp:399-699, theories 0 and 1,
+/* The per-site (all components) interaction terms of CalculateVolumeAverages
+ * (fieldanalysis.cpp:565-617; per component :456-508), static box; locPhi is the sum of the
+ * components (:434-443). */
+static double site_interaction(const orc_params *p, double locPhiSqr, double locPhi) {
+  const int Nc = p->Nc;
+  const double mass = p->m_sqr;
+  switch (p->theory) {
+    case 0:
+      return (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)) +
+             (sqr(locPhiSqr) * locPhiSqr / (720.0 * Nc * Nc * p->kappa * p->kappa));
+    case 1:
+      return (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc));
+    case 2:
+    case 3:
+      return sqr(mass) * (1. - cos(sqrt(locPhiSqr / mass)));
+    case 4:
+      return (((-p->g * locPhi * locPhiSqr) / (6.0)) + (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)));
+    default:
+      return sqr(mass) * 0.5 / p->p_mono * (pow((1. + locPhiSqr / mass), p->p_mono) - 1.);
+  }
+}
+
+/* CalculateVolumeAverages(): fieldanalysis.cpp:399-699, theories 0 to 5,
  * static box, no charge / energy-density extras.  Also returns the gradient
  * term GradPhiSqr/vol, which the reference keeps local. */
 static void volume_averages(const orc_params *p, const double *Phi, const double *Pi, orc_row *o) {
@@ -208,9 +243,11 @@ static void volume_averages(const orc_params *p, const double *Phi, const double
           locPhi += Phi[Kooo];
           GradPhiSqr += (sqr(Phi[Kuoo] - Phi[Kooo]) / sqr(p->a) + sqr(Phi[Kouo] - Phi[Kooo]) / sqr(p->a) +
                          sqr(Phi[Koou] - Phi[Kooo]) / sqr(p->a));
-          if (p->theory == 0) {
+          if (p->theory == 0 || p->theory == 4) {
             Interaction += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
-          } else {
+          } else if (p->theory == 3) {
+            Interaction += 0.5 * p->m_mono_sqr * sqr(Phi[Kooo]);
+          } else if (p->theory == 1) {
             if (a == 0)
               Interaction += (p->h * Phi[Kooo] + (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]));
             else
@@ -218,14 +255,9 @@ static void volume_averages(const orc_params *p, const double *Phi, const double
           }
           Kooo++; Kuoo++; Kouo++; Koou++;
         }
-        (void)locPhi;
         phi4 += sqr(locPhiSqr);
         phi6 += sqr(locPhiSqr) * locPhiSqr;
-        if (p->theory == 0)
-          Interaction += (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)) +
-                         (sqr(locPhiSqr) * locPhiSqr / (720.0 * Nc * Nc * p->kappa * p->kappa));
-        else
-          Interaction += (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc));
+        Interaction += site_interaction(p, locPhiSqr, locPhi);
       }
   for (int a = 0; a < Nc; a++) { phi[a] /= (vol); pi[a] /= (vol); }
   Charge = (0.5 * pi2 - GradPhiSqr / 6. - Interaction);
@@ -716,25 +748,24 @@ double orc_site_energy(const orc_params *p, const double *Phi, const double *Pi,
   const double mass = p->m_sqr;
   long Kooo = Kooo0;
   long Kuoo = pos3(p, mod(x + 1, N), y, z), Kouo = pos3(p, x, mod(y + 1, N), z), Koou = pos3(p, x, y, z + 1);
-  double kin = 0., grad = 0., inter = 0., locPhiSqr = 0.;
+  double kin = 0., grad = 0., inter = 0., locPhiSqr = 0., locPhi = 0.;
   for (int a = 0; a < Nc; a++) {
     kin += sqr(Pi[Kooo]);
     locPhiSqr += sqr(Phi[Kooo]);
+    locPhi += Phi[Kooo];
     grad += (sqr(Phi[Kuoo] - Phi[Kooo]) / sqr(p->a) + sqr(Phi[Kouo] - Phi[Kooo]) / sqr(p->a) +
              sqr(Phi[Koou] - Phi[Kooo]) / sqr(p->a));
-    if (p->theory == 0)
+    if (p->theory == 0 || p->theory == 4)
       inter += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
-    else if (a == 0)
+    else if (p->theory == 3)
+      inter += 0.5 * p->m_mono_sqr * sqr(Phi[Kooo]);
+    else if (p->theory == 1 && a == 0)
       inter += (p->h * Phi[Kooo] + (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]));
-    else
+    else if (p->theory == 1)
       inter += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
     Kooo++; Kuoo++; Kouo++; Koou++;
   }
-  if (p->theory == 0)
-    inter += (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)) +
-             (sqr(locPhiSqr) * locPhiSqr / (720.0 * Nc * Nc * p->kappa * p->kappa));
-  else
-    inter += (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc));
+  inter += site_interaction(p, locPhiSqr, locPhi);
   return 0.5 * kin + 0.5 * grad + inter;
 }
 
@@ -788,9 +819,18 @@ static void bfs(const orc_params *p, const double *Phi, const double *Pi, const 
       cPotEn += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]) +
                 (double)(p->lambda_mode) * (sqr(sqr(Phi[Kooo])) / (24.0 * Nc)) +
                 (sqr(sqr(Phi[Kooo])) * sqr(Phi[Kooo]) / (720.0 * Nc * Nc * p->kappa * p->kappa));
-    else
+    else if (p->theory == 1)
       cPotEn += (p->h * Phi[Kooo] + (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]) +
                  (double)(p->lambda_mode) * (sqr(sqr(Phi[Kooo])) / (24.0 * Nc)));
+    else if (p->theory == 2) /* islands.cpp:160-167 */
+      cPotEn += sqr(mass) * (1. - cos(sqrt(sqr(Phi[Kooo]) / mass)));
+    else if (p->theory == 3) /* :169-177 */
+      cPotEn += 0.5 * p->m_mono_sqr * sqr(Phi[Kooo]) + sqr(mass) * (1. - cos(sqrt(sqr(Phi[Kooo]) / mass)));
+    else if (p->theory == 4) /* :179-187 */
+      cPotEn += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]) - p->g * sqr(Phi[Kooo]) * Phi[Kooo] / 6. +
+                (double)(p->lambda_mode) * (sqr(sqr(Phi[Kooo])) / (24.0 * Nc));
+    else /* :189-196 */
+      cPotEn += sqr(mass) * 0.5 / p->p_mono * (pow((1. + Phi[Kooo] * Phi[Kooo] / mass), p->p_mono) - 1.);
     cavPhi += Phi[Kooo];
     if (mask[Kuoo] && b[Kuoo] == -1) { b[Kuoo] = flag; queue[tail++] = Kuoo; }
     if (mask[Kdoo] && b[Kdoo] == -1) { b[Kdoo] = flag; queue[tail++] = Kdoo; }

@@ -25,6 +25,9 @@ typedef struct orc_params {
   double m_sqr;    /* M_sqr (= BareM_sqr_long/_trans without tadpole renormalisation) */
   double kappa;    /* Kappa (theory 0) */
   double h;        /* h (theory 1) */
+  double g;        /* g (theory 4) */
+  double p_mono;   /* p_mono (theory 5) */
+  double m_mono_sqr; /* M_mono_sqr (theory 3) */
 } orc_params;
 
 /* numeric:: and LocalLattice:: time keeping (dynamics.cpp:8-50). */

@@ -76,6 +76,13 @@ enum { REF_MAX_NC = 4, REF_AVG_LEN = 1 + 2 * REF_MAX_NC + 14 + 3 };
 int ref_precision() { return doubleprecision; }
 int ref_theory() { return theory; }
 
+/* Couplings of theories 3-5 (M_mono_sqr, g, p_mono); call before ref_init. */
+void ref_set_extra(double gcub, double pmono, double mmono) {
+  g = (pseudo_double)gcub;
+  p_mono = (pseudo_double)pmono;
+  M_mono_sqr = (pseudo_double)mmono;
+}
+
 int ref_init(int N, int nc, double a, double dt, double t0, int mass_mode, double m_sqr,
              int lambda_mode, double lambda, double kappa, double hlin) {
   if (g_ready) return -1;

@@ -75,6 +75,12 @@ int Lambda_Mode = -1;
 pseudo_double Lambda = 1.;
 pseudo_double Kappa = 2.;
 pseudo_double h = 0.;
+/* theories 2-5 (parameters.cpp:122-170) */
+pseudo_double F_SSB = 1.;
+pseudo_double alpha = 0.;
+pseudo_double M_mono_sqr = 1.;
+pseudo_double g = 2.;
+pseudo_double p_mono = -0.5;
 
 int renorm_tadpole = 0;
 int max_renSteps = 2000;

@@ -25,10 +25,13 @@ _D, _I = ctypes.c_double, ctypes.c_int
 _PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
 
 
+ABI_VERSION = 2  # PHN_ABI_VERSION of include/phinum_gpu.h
+
+
 class PhnParams(ctypes.Structure):
     _fields_ = [("N", _I), ("Nc", _I), ("potential", _I), ("mass_mode", _I), ("lambda_mode", _I),
                 ("precision", _I), ("a", _D), ("dt", _D), ("T0", _D), ("m_sqr", _D), ("kappa", _D),
-                ("h", _D)]
+                ("h", _D), ("g", _D), ("p_mono", _D), ("m_mono_sqr", _D)]
 
 
 class PhnIcParams(ctypes.Structure):
@@ -152,6 +155,8 @@ def load(build_if_missing: bool = False):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.phn_abi_version() != ABI_VERSION:  # the structures above follow one layout
+        raise OSError(f"{LIB_PATH} has ABI {lib.phn_abi_version()}, this binding {ABI_VERSION}: rebuild")
     _lib = lib
     return lib
 

@@ -65,17 +65,31 @@ inline void init() {
   std::memset(&p, 0, sizeof(p));
   p.N = N_t;
   p.Nc = Nc;
+  // the couplings each theory defines (parameters.cpp:86-170)
 #if (theory == 0)
   p.potential = 0;
   p.kappa = Kappa;
+  p.mass_mode = Mass_Mode;
+  p.lambda_mode = Lambda_Mode;
 #elif (theory == 1)
   p.potential = 1;
   p.h = ::h;  // the reference's linear coupling (parameters.cpp:117)
-#else
-#error "phinum_gpu provides theories 0 and 1"
-#endif
   p.mass_mode = Mass_Mode;
   p.lambda_mode = Lambda_Mode;
+#elif (theory == 2)
+  p.potential = 2;
+#elif (theory == 3)
+  p.potential = 3;
+  p.m_mono_sqr = LocalLattice::BareM_mono_sqr_long;
+#elif (theory == 4)
+  p.potential = 4;
+  p.g = ::g;
+  p.mass_mode = Mass_Mode;
+  p.lambda_mode = Lambda_Mode;
+#elif (theory == 5)
+  p.potential = 5;
+  p.p_mono = ::p_mono;
+#endif
   p.m_sqr = LocalLattice::BareM_sqr_long;
   p.a = a_t;
   p.dt = dtBaseTrans;

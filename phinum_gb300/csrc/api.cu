@@ -39,8 +39,11 @@ int phn::validate_params(const phn_params *p) {
   if (!p) return set_error(PHN_ERR_INVALID, "params is NULL");
   if (p->N < 2 || p->N > 2048) return set_error(PHN_ERR_INVALID, "N=%d outside [2, 2048]", p->N);
   if (p->Nc < 1 || p->Nc > PHN_MAX_NC) return set_error(PHN_ERR_UNSUPPORTED, "Nc=%d outside [1, %d]", p->Nc, PHN_MAX_NC);
-  if (p->potential != 0 && p->potential != 1)
-    return set_error(PHN_ERR_UNSUPPORTED, "theory %d: only theories 0 and 1 are provided", p->potential);
+  if (p->potential < 0 || p->potential > 5) return set_error(PHN_ERR_INVALID, "theory %d", p->potential);
+  if (p->potential >= 2 && p->Nc != 1)
+    return set_error(PHN_ERR_UNSUPPORTED, "theory %d is provided for Nc = 1", p->potential);
+  if (p->potential >= 2 && !(p->m_sqr > 0.0)) return set_error(PHN_ERR_INVALID, "theory %d needs M_sqr > 0", p->potential);
+  if (p->potential == 5 && !(p->p_mono != 0.0)) return set_error(PHN_ERR_INVALID, "p_mono must be non-zero");
   if (p->precision < PHN_FP64 || p->precision > PHN_FP32_KAHAN)
     return set_error(PHN_ERR_INVALID, "precision %d", p->precision);
   if (!(p->a > 0.0) || !isfinite(p->a)) return set_error(PHN_ERR_INVALID, "a must be positive");
@@ -76,6 +79,27 @@ Consts phn::make_consts(const phn_params *p) {
   k.mmh_f = (float)k.mm_half_M;
   k.e4_f = (float)(k.lm / k.c24);
   k.e6_f = p->potential == 0 ? (float)(1.0 / k.c720) : 0.f;
+  // theories 2-5 (dynamics.cpp:109-157, fieldanalysis.cpp:482-617)
+  k.msq = p->m_sqr;
+  k.sqrt_m = sqrt(p->m_sqr);
+  k.m3 = p->m_sqr * sqrt(p->m_sqr);
+  k.msq2 = p->m_sqr * p->m_sqr;
+  k.mmono = p->m_mono_sqr;
+  k.g = p->g;
+  k.p_mono = p->p_mono;
+  k.t5c = p->potential == 5 ? k.msq2 * 0.5 / p->p_mono : 0.0;
+  k.m3_f = (float)k.m3;
+  k.inv_sqrtm_f = p->m_sqr > 0 ? (float)(1.0 / k.sqrt_m) : 0.f;
+  k.inv_m_f = p->m_sqr > 0 ? (float)(1.0 / p->m_sqr) : 0.f;
+  k.mmono_f = (float)p->m_mono_sqr;
+  k.ghalf_f = (float)(p->g / 2.);
+  k.msq_f = (float)p->m_sqr;
+  k.pm1_f = (float)(p->p_mono - 1);
+  k.p_f = (float)p->p_mono;
+  k.msq2_f = (float)k.msq2;
+  k.mono_half_f = (float)(0.5 * p->m_mono_sqr);
+  k.g6_f = (float)(p->g / 6.0);
+  k.t5c_f = (float)k.t5c;
   return k;
 }
 

@@ -47,6 +47,27 @@ __device__ __forceinline__ double val(const T *f, const float *comp, size_t i) {
   return v;
 }
 
+// Potential of one single-component site, theories 0-5: the BFS PotEn
+// summand (islands.cpp:137-196), which is also the Interaction summand of
+// CalculateVolumeAverages (fieldanalysis.cpp:456-617) for Nc = 1.
+__device__ __forceinline__ double site_potential(const Consts &k, double c, double c2) {
+  const double l2 = c2 * c2;
+  switch (k.theory) {
+    case 0:
+      return k.mm_half_M * c2 + k.lm * (l2 / k.c24) + (l2 * c2 / k.c720);
+    case 1:
+      return k.h * c + k.mm_half_M * c2 + k.lm * (l2 / k.c24);
+    case 2:
+      return k.msq2 * (1. - cos(sqrt(c2 / k.msq)));
+    case 3:
+      return 0.5 * k.mmono * c2 + k.msq2 * (1. - cos(sqrt(c2 / k.msq)));
+    case 4:
+      return k.mm_half_M * c2 - k.g * c2 * c / 6. + k.lm * (l2 / k.c24);
+    default:
+      return k.t5c * (pow(1. + c2 / k.msq, k.p_mono) - 1.);
+  }
+}
+
 // Per-site energy density: the summand of the reference's Energy
 // (fieldanalysis.cpp:437-471,571-579), Nc = 1.
 template <typename T>
@@ -60,14 +81,7 @@ __device__ double site_rho(const T *phi, const float *cphi, const T *pi, const f
   const double fz = val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
   const double c2 = c * c;
   const double grad = ((fx - c) * (fx - c) / k.a2 + (fy - c) * (fy - c) / k.a2) + (fz - c) * (fz - c) / k.a2;
-  double inter = k.mm_half_M * c2;
-  if (k.theory == 1) inter = k.h * c + inter;
-  const double l2 = c2 * c2;
-  if (k.theory == 0)
-    inter += k.lm * (l2 / k.c24) + (l2 * c2 / k.c720);
-  else
-    inter += k.lm * (l2 / k.c24);
-  return 0.5 * (p * p) + 0.5 * grad + inter;
+  return 0.5 * (p * p) + 0.5 * grad + site_potential(k, c, c2);
 }
 
 template <typename T>
@@ -214,15 +228,11 @@ __global__ void ccl_stats(const T *__restrict__ phi, const float *__restrict__ c
     const double fx = val(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
     const double fy = val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
     const double fz = val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
-    // BFS accumulators (islands.cpp:131-198), static box, theories 0 and 1
+    // BFS accumulators (islands.cpp:131-198), static box
     const double grad = 0.5 * ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) / k.a2;
     const double kin = 0.5 * (p * p);
-    const double c2 = c * c, c4 = c2 * c2;
-    double pot;
-    if (k.theory == 0)
-      pot = k.mm_half_M * c2 + k.lm * (c4 / k.c24) + (c4 * c2 / k.c720);
-    else
-      pot = (k.h * c + k.mm_half_M * c2 + k.lm * (c4 / k.c24));
+    const double c2 = c * c;
+    const double pot = site_potential(k, c, c2);
     atomicAdd(&size[id], 1);
     atomicAdd(&sums[(size_t)id * 4 + 0], pot);
     atomicAdd(&sums[(size_t)id * 4 + 1], kin);

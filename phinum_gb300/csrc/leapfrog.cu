@@ -21,6 +21,24 @@
 namespace phn {
 
 // ----------------------------------------------------------- FP64 kernel
+// Force of theories 2-5 (Nc = 1) in the reference's order (dynamics.cpp:
+// 109-157, static box); sin and pow are CUDA's, so these agree with the
+// reference to rounding, not bitwise.
+template <int THEORY>
+__device__ __forceinline__ double force_f64_ext(const Consts &k, double lap, double c, double l) {
+  if (THEORY == 2 || THEORY == 3) {
+    const double s = __dsqrt_rn(l);
+    const double t = __dmul_rn(__dmul_rn(k.m3, c / s), sin(s / k.sqrt_m));
+    if (THEORY == 2) return __dadd_rn(lap, -t);
+    return __dadd_rn(__dadd_rn(lap, -__dmul_rn(k.mmono, c)), -t);
+  }
+  if (THEORY == 4) {
+    const double coef = __dadd_rn(__dadd_rn(k.mmM, -(__dmul_rn(k.g, c) / 2.)), __dmul_rn(k.lm, l / k.six_nc));
+    return __dadd_rn(lap, -__dmul_rn(coef, c));
+  }
+  return __dadd_rn(lap, -__dmul_rn(__dmul_rn(k.msq, c), pow(__dadd_rn(1., l / k.msq), k.p_mono - 1)));
+}
+
 // The kick and drift use explicit round-to-nearest intrinsics and IEEE
 // division in the reference's operation order (dynamics.cpp:80-84,96-100,183),
 // so every site value is bit-identical to the reference's FP64 build.
@@ -76,8 +94,12 @@ __global__ void __launch_bounds__(THREADS) step_f64(const double *__restrict__ p
           const double sum = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(fxp[a], fxm[a]), fyp[a]), fym[a]), cp[a]), cm[a]);
           const double lap = __dadd_rn(sum, -__dmul_rn(6.0, c[a])) / k.a2;
           double f = lap;
-          if (THEORY == 1 && a == 0) f = __dadd_rn(f, -k.h);
-          f = __dadd_rn(f, -__dmul_rn(coef, c[a]));
+          if (THEORY <= 1) {
+            if (THEORY == 1 && a == 0) f = __dadd_rn(f, -k.h);
+            f = __dadd_rn(f, -__dmul_rn(coef, c[a]));
+          } else {
+            f = force_f64_ext<THEORY>(k, lap, c[a], l);
+          }
           const double pn = __dadd_rn(p[a], __dmul_rn(f, s.fk));
           pi[a * V + pl + col] = pn;
           phi_out[a * V + pl + col] = __dadd_rn(c[a], __dmul_rn(pn, s.fd));
@@ -142,8 +164,13 @@ __global__ void __launch_bounds__(THREADS) step_f32(const float *__restrict__ ph
         for (int a = 0; a < NC; ++a) {
           // the shared neighbour-difference Laplacian: the TMA kernel computes the same bits
           const float lap = lap_diff_f32(c[a], fxm[a], fxp[a], fym[a], fyp[a], cm[a], cp[a], k.inv_a2_f);
-          float f = fmaf(-coef, c[a], lap);
-          if (THEORY == 1 && a == 0) f = __fsub_rn(f, k.h_f);
+          float f;
+          if (NC == 1) {
+            f = force_f32<THEORY>(k, lap, c[a], l);
+          } else {
+            f = fmaf(-coef, c[a], lap);
+            if (THEORY == 1 && a == 0) f = __fsub_rn(f, k.h_f);
+          }
           const float pn = fmaf(fk, f, p[a]);
           pi[a * V + pl + col] = pn;
           phi_out[a * V + pl + col] = fmaf(fd, pn, c[a]);
@@ -227,8 +254,13 @@ __global__ void __launch_bounds__(THREADS) step_kahan(const float *__restrict__ 
         for (int a = 0; a < NC; ++a) {
           // the shared neighbour-difference Laplacian: the TMA kernel computes the same bits
           const float lap = lap_diff_f32(c[a], fxm[a], fxp[a], fym[a], fyp[a], cm[a], cp[a], k.inv_a2_f);
-          float f = fmaf(-coef, c[a], lap);
-          if (THEORY == 1 && a == 0) f = __fsub_rn(f, k.h_f);
+          float f;
+          if (NC == 1) {
+            f = force_f32<THEORY>(k, lap, c[a], l);
+          } else {
+            f = fmaf(-coef, c[a], lap);
+            if (THEORY == 1 && a == 0) f = __fsub_rn(f, k.h_f);
+          }
           // kick: pi += fk * f  (Kahan)
           const float yk = __fsub_rn(__fmul_rn(fk, f), ep[a]);
           const float tk = __fadd_rn(p[a], yk);
@@ -302,6 +334,19 @@ Grid lattice_grid(int N) {
   if ((THV) == 0) { constexpr int TH_ = 0; __VA_ARGS__; }      \
   else { constexpr int TH_ = 1; __VA_ARGS__; }
 
+// Theories 0 and 1 for every component count; theories 2-5 with Nc = 1.
+#define PHN_DISPATCH_NC_TH(NCV, THV, ...)                                          \
+  if ((THV) <= 1) {                                                                \
+    PHN_DISPATCH_NC(NCV, PHN_DISPATCH_TH(THV, __VA_ARGS__));                       \
+  } else {                                                                         \
+    if ((NCV) != 1) return cudaErrorInvalidValue;                                  \
+    constexpr int NC_ = 1;                                                         \
+    if ((THV) == 2) { constexpr int TH_ = 2; __VA_ARGS__; }                        \
+    else if ((THV) == 3) { constexpr int TH_ = 3; __VA_ARGS__; }                   \
+    else if ((THV) == 4) { constexpr int TH_ = 4; __VA_ARGS__; }                   \
+    else { constexpr int TH_ = 5; __VA_ARGS__; }                                   \
+  }
+
 #define PHN_DISPATCH_MODE(MV, ...)                             \
   if ((MV) == MODE_STEP) { constexpr int MD_ = MODE_STEP; __VA_ARGS__; }          \
   else if ((MV) == MODE_STEP_OBS) { constexpr int MD_ = MODE_STEP_OBS; __VA_ARGS__; } \
@@ -309,16 +354,16 @@ Grid lattice_grid(int N) {
 
 cudaError_t launch_step_f64(const Consts &k, const Grid &g, int mode, const double *phi, double *phi_out,
                             double *pi, StepF s, double *partials, cudaStream_t st) {
-  PHN_DISPATCH_NC(k.Nc, PHN_DISPATCH_TH(k.theory, PHN_DISPATCH_MODE(mode,
-      step_f64<NC_, TH_, MD_><<<g.grid, g.block, 0, st>>>(phi, phi_out, pi, k, s, g.cz, partials))));
+  PHN_DISPATCH_NC_TH(k.Nc, k.theory, PHN_DISPATCH_MODE(mode,
+      step_f64<NC_, TH_, MD_><<<g.grid, g.block, 0, st>>>(phi, phi_out, pi, k, s, g.cz, partials)));
   return cudaGetLastError();
 }
 
 cudaError_t launch_step_f32(const Consts &k, const Grid &g, int mode, const float *phi, float *phi_out,
                             float *pi, StepF s, double *partials, cudaStream_t st) {
   const float fk = (float)s.fk, fd = (float)s.fd;
-  PHN_DISPATCH_NC(k.Nc, PHN_DISPATCH_TH(k.theory, PHN_DISPATCH_MODE(mode,
-      step_f32<NC_, TH_, MD_><<<g.grid, g.block, 0, st>>>(phi, phi_out, pi, k, fk, fd, g.cz, partials))));
+  PHN_DISPATCH_NC_TH(k.Nc, k.theory, PHN_DISPATCH_MODE(mode,
+      step_f32<NC_, TH_, MD_><<<g.grid, g.block, 0, st>>>(phi, phi_out, pi, k, fk, fd, g.cz, partials)));
   return cudaGetLastError();
 }
 
@@ -327,9 +372,9 @@ cudaError_t launch_step_kahan(const Consts &k, const Grid &g, int mode, const fl
                               double *partials, cudaStream_t st) {
   (void)cphi;
   const float fk = (float)s.fk, fd = (float)s.fd;
-  PHN_DISPATCH_NC(k.Nc, PHN_DISPATCH_TH(k.theory, PHN_DISPATCH_MODE(mode,
+  PHN_DISPATCH_NC_TH(k.Nc, k.theory, PHN_DISPATCH_MODE(mode,
       step_kahan<NC_, TH_, MD_><<<g.grid, g.block, 0, st>>>(phi, phi_out, cphi_out, pi, cpi, k, fk, fd, g.cz,
-                                                            partials))));
+                                                            partials)));
   return cudaGetLastError();
 }
 

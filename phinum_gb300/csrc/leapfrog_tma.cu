@@ -318,7 +318,7 @@ struct TmaLaunch {
   }
 
 bool tma_supported(const phn_params &p) {
-  if (p.Nc != 1 || p.precision != PHN_FP32 || p.N % 128 != 0) return false;
+  if (p.Nc != 1 || p.precision != PHN_FP32 || p.N % 128 != 0 || p.potential > 1) return false;
   const int K = p.N / 128;
   return K == 1 || K == 2 || K == 3 || K == 4 || K == 6 || K == 8;
 }

@@ -131,7 +131,10 @@ __device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c
     const double dx = __dadd_rn(fxp[a], -c[a]), dy = __dadd_rn(fyp[a], -c[a]), dz = __dadd_rn(fzp[a], -c[a]);
     A.s[S_GRAD] += __dadd_rn(__dadd_rn(__dmul_rn(dx, dx) / k.a2, __dmul_rn(dy, dy) / k.a2),
                              __dmul_rn(dz, dz) / k.a2);
-    double term = __dmul_rn(k.mm_half_M, c2);
+    // per-component terms (fieldanalysis.cpp:456-508)
+    double term = 0.0;
+    if (THEORY == 0 || THEORY == 1 || THEORY == 4) term = __dmul_rn(k.mm_half_M, c2);
+    if (THEORY == 3) term = __dmul_rn(__dmul_rn(0.5, k.mmono), c2);
     if (THEORY == 1 && a == 0) term = __dadd_rn(__dmul_rn(k.h, c[a]), term);
     inter += term;
     if (!isfinite(c[a]) || !isfinite(p[a])) A.s[S_NONFINITE] += 1.0;
@@ -141,10 +144,18 @@ __device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c
   const double l2 = __dmul_rn(l, l);
   A.s[S_PHI4] += l2;
   A.s[S_PHI6] += __dmul_rn(l2, l);
-  if (THEORY == 0)
+  // per-site terms (fieldanalysis.cpp:565-617); theories 2-5 have Nc = 1
+  if (THEORY == 0) {
     inter += __dadd_rn(__dmul_rn(k.lm, l2 / k.c24), __dmul_rn(l2, l) / k.c720);
-  else
+  } else if (THEORY == 1) {
     inter += __dmul_rn(k.lm, l2 / k.c24);
+  } else if (THEORY == 2 || THEORY == 3) {
+    inter += __dmul_rn(k.msq2, __dsub_rn(1., cos(__dsqrt_rn(l / k.msq))));
+  } else if (THEORY == 4) {
+    inter += __dadd_rn(__dmul_rn(__dmul_rn(-k.g, c[0]), l) / 6.0, __dmul_rn(k.lm, l2 / k.c24));
+  } else {
+    inter += __dmul_rn(k.t5c, __dsub_rn(pow(__dadd_rn(1., l / k.msq), k.p_mono), 1.));
+  }
   A.s[S_INTER] += inter;
   A.take_abs(sqrt(l), kidx);
 }
@@ -197,7 +208,9 @@ __device__ __forceinline__ void observe_f32(AccF &A, const Consts &k, const floa
     l += c2;
     const float dx = fxp[a] - c[a], dy = fyp[a] - c[a], dz = fzp[a] - c[a];
     A.add(S_GRAD, (dx * dx + dy * dy + dz * dz) * k.inv_a2_f);
-    float term = k.mmh_f * c2;
+    float term = 0.f;
+    if (THEORY == 0 || THEORY == 1 || THEORY == 4) term = k.mmh_f * c2;
+    if (THEORY == 3) term = k.mono_half_f * c2;
     if (THEORY == 1 && a == 0) term = fmaf(k.h_f, c[a], term);
     inter += term;
     if (!isfinite(c[a]) || !isfinite(p[a])) A.s[S_NONFINITE] += 1.f;
@@ -209,8 +222,11 @@ __device__ __forceinline__ void observe_f32(AccF &A, const Consts &k, const floa
   const float l2 = l * l;
   A.add(S_PHI4, l2);
   A.add(S_PHI6, l2 * l);
-  inter = fmaf(k.e4_f, l2, inter);
+  if (THEORY == 0 || THEORY == 1 || THEORY == 4) inter = fmaf(k.e4_f, l2, inter);
   if (THEORY == 0) inter = fmaf(k.e6_f, l2 * l, inter);
+  if (THEORY == 2 || THEORY == 3) inter = fmaf(k.msq2_f, 1.f - cosf(sqrtf(l * k.inv_m_f)), inter);
+  if (THEORY == 4) inter = fmaf(-k.g6_f * c[0], l, inter);
+  if (THEORY == 5) inter = fmaf(k.t5c_f, powf(fmaf(l, k.inv_m_f, 1.f), k.p_f) - 1.f, inter);
   A.add(S_INTER, inter);
   const float r = sqrtf(l);
   if ((r > A.absv || (r == A.absv && kidx < A.absi)) && r > 0.f) { A.absv = r; A.absi = kidx; }

@@ -56,6 +56,13 @@ struct Consts {
   float inv_a2_f, mmM_f, c4_f, c6_f, h_f;
   // FP32 forms of the energy density
   float mmh_f, e4_f, e6_f;
+  // theories 2-5 (Nc = 1): M = BareM_sqr, as the reference writes the terms
+  double msq, sqrt_m, m3;  // M, sqrt(M), M sqrt(M)
+  double msq2;             // sqr(M)
+  double mmono, g, p_mono; // BareM_mono_sqr, g, p_mono
+  double t5c;              // sqr(M) * 0.5 / p_mono
+  float m3_f, inv_sqrtm_f, inv_m_f, mmono_f, ghalf_f, msq_f, pm1_f, p_f;
+  float msq2_f, mono_half_f, g6_f, t5c_f;
 };
 
 // Per-step kick and drift factors: tau - Last_Momenta_update and

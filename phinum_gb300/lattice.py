@@ -39,10 +39,14 @@ class Params:
     m_sqr: float = 1.0
     kappa: float = 3.0 ** 0.5
     h: float = 0.0
+    g: float = 2.0            # theory 4
+    p_mono: float = -0.5      # theory 5
+    m_mono_sqr: float = 1.0   # theory 3
 
     def c(self) -> L.PhnParams:
         return L.PhnParams(self.N, self.Nc, self.theory, self.mass_mode, self.lambda_mode, self.precision,
-                           self.a, self.dt, self.T0, self.m_sqr, self.kappa, self.h)
+                           self.a, self.dt, self.T0, self.m_sqr, self.kappa, self.h, self.g, self.p_mono,
+                           self.m_mono_sqr)
 
     @property
     def field_len(self) -> int:

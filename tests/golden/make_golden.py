@@ -38,6 +38,11 @@ SQRT6 = 6.0 ** 0.5
 #                 Mmode=-1, M=1, Lmode=1, h = sqrt(6) eps
 PHI6 = dict(theory=0, mass_mode=1, lambda_mode=-1, m_sqr=1.0, kappa=3.0 ** 0.5, h=0.0)
 TDW = dict(theory=1, mass_mode=-1, lambda_mode=1, m_sqr=1.0, kappa=1.0, h=SQRT6 * 0.05)
+# theories 2-5 with the couplings parameters.cpp:122-170 sets
+COS = dict(theory=2, mass_mode=1, lambda_mode=1, m_sqr=0.49, kappa=1.0, h=0.0)
+MONO = dict(theory=3, mass_mode=1, lambda_mode=1, m_sqr=9.0, kappa=1.0, h=0.0, m_mono_sqr=1.0)
+CUBIC = dict(theory=4, mass_mode=1, lambda_mode=1, m_sqr=1.0, kappa=1.0, h=0.0, g=2.0)
+POWER = dict(theory=5, mass_mode=1, lambda_mode=1, m_sqr=1.0, kappa=1.0, h=0.0, p_mono=-0.5)
 
 CASES = {
     # name: (params, seed, phi0, steps, tso, full arrays?, checkpoints)
@@ -47,6 +52,11 @@ CASES = {
     "t0_n16_nc2": (dict(N=16, Nc=2, **PHI6), 4, SQRT6, 50, 0.25, True, (1, 50)),
     "t1_n32": (dict(N=32, Nc=1, **TDW), 5, -SQRT6, 500, 1.0, False, (1, 100, 500)),
     "c0_n64": (dict(N=64, Nc=1, **PHI6), 6, SQRT6, 2000, 1.0, False, (1, 500, 2000)),
+    "t2_n8": (dict(N=8, Nc=1, **COS), 7, 1.5, 100, 0.25, True, (1, 10, 100)),
+    "t3_n8": (dict(N=8, Nc=1, **MONO), 8, 2.0, 100, 0.25, True, (1, 10, 100)),
+    "t4_n8": (dict(N=8, Nc=1, **CUBIC), 9, 1.0, 100, 0.25, True, (1, 10, 100)),
+    "t4_n16": (dict(N=16, Nc=1, **CUBIC), 10, 1.0, 300, 0.5, False, (1, 100, 300)),
+    "t5_n8": (dict(N=8, Nc=1, **POWER), 11, 2.0, 100, 0.25, True, (1, 10, 100)),
 }
 
 

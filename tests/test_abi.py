@@ -45,5 +45,8 @@ def test_library_exports_every_declared_symbol(lib):
 def test_binding_covers_header(lib):
     from phinum_gb300 import _lib
     assert set(_lib.exported_symbols()) <= set(declared())
-    assert lib.phn_abi_version() == 1
+    import re
+    hdr = open(os.path.join(ROOT, "include", "phinum_gpu.h")).read()
+    version = int(re.search(r"#define PHN_ABI_VERSION (\d+)", hdr).group(1))
+    assert lib.phn_abi_version() == version == _lib.ABI_VERSION
 

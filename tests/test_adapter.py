@@ -11,7 +11,7 @@ REF = "/root/reference"
 
 
 @pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "dynamics.cpp")), reason="reference tree not present")
-@pytest.mark.parametrize("theory", [0, 1])
+@pytest.mark.parametrize("theory", [0, 1, 2, 3, 4, 5])
 def test_adapter_compiles_in_reference_tu(theory):
     cmd = ["g++", "-std=gnu++14", "-fsyntax-only", "-w", f"-DPHN_REF_THEORY={theory}", "-DPHN_REF_PRECISION=0",
            "-I", os.path.join(ROOT, "oracle", "ref_shim"), "-I", os.path.join(ROOT, "oracle"),

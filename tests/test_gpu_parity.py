@@ -3,7 +3,10 @@ outputs (tests/golden/, produced by the reference sources) and the oracle.
 
 Tolerances
   FP64 fields and SO-row extrema: bit-exact (same IEEE operations in the
-      reference's order).
+      reference's order) for theories 0, 1 and 4; theories 2, 3 and 5 call
+      sin/cos/pow, whose CUDA results may differ from the C library's in the
+      last bit: fields and extrema within 1e-12 of the largest value after
+      100 steps, extrema positions exact.
   FP64 sums (averages, energies): relative 1e-11 -- tree order vs the
       reference's sequential sums.
   FP64 spectra: relative 1e-10 of the largest bin (cuFFT vs the oracle FFT);
@@ -23,6 +26,11 @@ pytestmark = pytest.mark.gpu
 ROW_COLS = slice(0, 23)
 SUM_COLS = [1, 5, 9, 10, 11, 12, 13, 14, 15, 16]      # phi0, pi0, phi2 .. charge
 EXACT_COLS = [0, 17, 18, 19, 20, 21, 22]               # t, extrema values and positions
+TRANSCENDENTAL = {2, 3, 5}                             # theories whose force calls sin / pow
+
+
+def fp64_exact(d) -> bool:
+    return d["params"]["theory"] not in TRANSCENDENTAL
 
 
 def gpu():
@@ -60,11 +68,17 @@ def test_fp64_fields_bit_exact(name):
         lat.evolve(c - done)
         done = c
         phi, pi = lat.download()
-        assert fixtures.digest(interior(phi, p)) == str(d[f"phi_sha_{c}"]), f"phi after {c}"
-        assert fixtures.digest(interior(pi, p)) == str(d[f"pi_sha_{c}"]), f"pi after {c}"
         a = lat.volume_averages()
         ref = d[f"avg_{c}"]
-        assert np.array_equal(a[EXACT_COLS[1:]], ref[EXACT_COLS[1:]])
+        if fp64_exact(d):
+            assert fixtures.digest(interior(phi, p)) == str(d[f"phi_sha_{c}"]), f"phi after {c}"
+            assert fixtures.digest(interior(pi, p)) == str(d[f"pi_sha_{c}"]), f"pi after {c}"
+            assert np.array_equal(a[EXACT_COLS[1:]], ref[EXACT_COLS[1:]])
+        else:
+            for got, want in ((interior(phi, p), d[f"phi_{c}"]), (interior(pi, p), d[f"pi_{c}"])):
+                assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max(), f"after {c}"
+            assert np.array_equal(a[[20, 21, 22]], ref[[20, 21, 22]])
+            np.testing.assert_allclose(a[[17, 18, 19]], ref[[17, 18, 19]], rtol=1e-12)
         np.testing.assert_allclose(a[SUM_COLS], ref[SUM_COLS], rtol=1e-11, atol=1e-14)
     t, s = lat.time()
     assert t == d["tau_end"] and s == d["steps_end"]
@@ -78,18 +92,22 @@ def test_fp64_run_loop_rows(name):
     rows = lat.run_loop(d["steps"], d["tso"])
     ref = d["rows"]
     assert rows.shape[0] == ref.shape[0]
-    assert np.array_equal(rows[:, EXACT_COLS], ref[:, EXACT_COLS])
+    if fp64_exact(d):
+        assert np.array_equal(rows[:, EXACT_COLS], ref[:, EXACT_COLS])
+    else:
+        assert np.array_equal(rows[:, [0, 20, 21, 22]], ref[:, [0, 20, 21, 22]])
+        np.testing.assert_allclose(rows[:, [17, 18, 19]], ref[:, [17, 18, 19]], rtol=1e-12)
     np.testing.assert_allclose(rows[:, SUM_COLS], ref[:, SUM_COLS], rtol=1e-11, atol=1e-14)
     # the fused rows leave the fields exactly where plain evolve() does
     phi, pi = lat.download()
     c = max(fixtures.checkpoints(d))
-    if c == d["steps"]:
+    if c == d["steps"] and fp64_exact(d):
         assert fixtures.digest(interior(phi, p)) == str(d[f"phi_sha_{c}"])
     lat.close()
 
 
 @pytest.mark.parametrize("precision,atol", [(1, 2e-4), (2, 2e-5)])
-@pytest.mark.parametrize("name", ["t0_n8", "t1_n8", "t0_n12", "t0_n16_nc2"])
+@pytest.mark.parametrize("name", ["t0_n8", "t1_n8", "t0_n12", "t0_n16_nc2", "t2_n8", "t3_n8", "t4_n8", "t5_n8"])
 def test_fp32_fields_close(name, precision, atol):
     d = fixtures.load(name)
     lat, p = start(d, precision)

@@ -98,9 +98,10 @@ def test_spectrum_counts_cover_every_mode():
         assert nb == {8: 7, 12: 9, 32: 20, 64: 37}[N]
 
 
-@pytest.mark.skipif(not (O.ref_available(0) and O.ref_available(1)),
+@pytest.mark.skipif(not all(O.ref_available(t) for t in range(6)),
                     reason="reference pin not built here (oracle/build_ref.sh)")
-@pytest.mark.parametrize("theory,N,Nc", [(0, 6, 1), (1, 10, 1), (0, 8, 3)])
+@pytest.mark.parametrize("theory,N,Nc", [(0, 6, 1), (1, 10, 1), (0, 8, 3), (2, 6, 1), (3, 6, 1), (4, 8, 1),
+                                         (5, 6, 1)])
 def test_oracle_matches_reference_live(theory, N, Nc, tmp_path):
     """Runs the reference pin in a child process on fresh random inputs."""
     import subprocess
@@ -111,8 +112,10 @@ def test_oracle_matches_reference_live(theory, N, Nc, tmp_path):
         import sys, numpy as np
         sys.path.insert(0, {os.getcwd()!r}); sys.path.insert(0, {os.path.dirname(O.HERE)!r})
         from oracle import oracle as O
-        kw = dict(theory=0, mass_mode=1, lambda_mode=-1, kappa=3**0.5) if {theory} == 0 else \\
-             dict(theory=1, mass_mode=-1, lambda_mode=1, h=0.3)
+        kw = {{0: dict(theory=0, mass_mode=1, lambda_mode=-1, kappa=3**0.5),
+              1: dict(theory=1, mass_mode=-1, lambda_mode=1, h=0.3),
+              2: dict(theory=2, m_sqr=0.49), 3: dict(theory=3, m_sqr=9.0, m_mono_sqr=1.0),
+              4: dict(theory=4, mass_mode=1, lambda_mode=1, g=2.0), 5: dict(theory=5, p_mono=-0.5)}}[{theory}]
         p = O.Params(N={N}, Nc={Nc}, **kw)
         rng = np.random.default_rng({N})
         phi = O.to_ref_layout(2.0 + 0.5 * rng.standard_normal(({Nc}, {N}, {N}, {N})), {Nc})
