@@ -177,7 +177,10 @@ def test_islands_fp64(name):
         np.testing.assert_allclose(recs[:, I[k]], st[:, j], rtol=1e-11, atol=1e-13)
     # peak: the reference keeps the first maximum of phi^2 in BFS order, this
     # implementation the smallest index among maxima -- equal unless tied
-    assert np.array_equal(np.abs(recs[:, I["peak_value"]]), np.abs(st[:, 7]))
+    if fp64_exact(d):
+        assert np.array_equal(np.abs(recs[:, I["peak_value"]]), np.abs(st[:, 7]))
+    else:
+        np.testing.assert_allclose(np.abs(recs[:, I["peak_value"]]), np.abs(st[:, 7]), rtol=1e-12)
     lat.close()
 
 
