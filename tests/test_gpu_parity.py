@@ -240,8 +240,11 @@ def test_errors_are_status_codes():
         PL.Lattice(PL.Params(N=8, Nc=9))
     assert e.value.code == L.ERR_UNSUPPORTED
     with pytest.raises(L.PhnError) as e:
-        PL.Lattice(PL.Params(N=8, theory=3))
+        PL.Lattice(PL.Params(N=8, Nc=2, theory=3))  # theories 2-5: Nc = 1
     assert e.value.code == L.ERR_UNSUPPORTED
+    with pytest.raises(L.PhnError) as e:
+        PL.Lattice(PL.Params(N=8, theory=6))
+    assert e.value.code == L.ERR_INVALID
     with pytest.raises(L.PhnError) as e:
         PL.Lattice(PL.Params(N=8, a=-1.0))
     assert e.value.code == L.ERR_INVALID
