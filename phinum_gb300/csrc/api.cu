@@ -62,6 +62,11 @@ Consts phn::make_consts(const phn_params *p) {
   k.Nc = Nc;
   k.theory = p->potential;
   k.a2 = p->a * p->a;
+  {
+    int ex = 0;
+    k.a2_pow2 = frexp(k.a2, &ex) == 0.5;
+    k.inv_a2 = 1.0 / k.a2;
+  }
   k.mmM = p->mass_mode * p->m_sqr;
   k.lm = (double)p->lambda_mode;
   k.six_nc = 6. * Nc;

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(THREADS) step_f64(const double *__restrict__ p
 #pragma unroll
         for (int a = 0; a < NC; ++a) {
           const double sum = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(fxp[a], fxm[a]), fyp[a]), fym[a]), cp[a]), cm[a]);
-          const double lap = __dadd_rn(sum, -__dmul_rn(6.0, c[a])) / k.a2;
+          const double lap = div_a2(k, __dadd_rn(sum, -__dmul_rn(6.0, c[a])));
           double f = lap;
           if (THEORY <= 1) {
             if (THEORY == 1 && a == 0) f = __dadd_rn(f, -k.h);

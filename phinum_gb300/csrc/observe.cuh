@@ -129,8 +129,8 @@ __device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c
     A.s[S_PHIPI] += __dmul_rn(c[a], p[a]);
     l = __dadd_rn(l, c2);
     const double dx = __dadd_rn(fxp[a], -c[a]), dy = __dadd_rn(fyp[a], -c[a]), dz = __dadd_rn(fzp[a], -c[a]);
-    A.s[S_GRAD] += __dadd_rn(__dadd_rn(__dmul_rn(dx, dx) / k.a2, __dmul_rn(dy, dy) / k.a2),
-                             __dmul_rn(dz, dz) / k.a2);
+    A.s[S_GRAD] += __dadd_rn(__dadd_rn(div_a2(k, __dmul_rn(dx, dx)), div_a2(k, __dmul_rn(dy, dy))),
+                             div_a2(k, __dmul_rn(dz, dz)));
     // per-component terms (fieldanalysis.cpp:456-508)
     double term = 0.0;
     if (THEORY == 0 || THEORY == 1 || THEORY == 4) term = __dmul_rn(k.mm_half_M, c2);

@@ -42,7 +42,9 @@ enum {
 // kernels combine exactly the same IEEE values.
 struct Consts {
   int N, Nc, theory;
+  int a2_pow2;       // sqr(a_t) is a power of two: x / a2 == x * inv_a2 exactly
   double a2;         // sqr(a_t)
+  double inv_a2;     // 1 / sqr(a_t)
   double mmM;        // Mass_Mode * BareM_sqr_long
   double lm;         // (double)Lambda_Mode
   double six_nc;     // 6.*Nc
@@ -64,6 +66,13 @@ struct Consts {
   float m3_f, inv_sqrtm_f, inv_m_f, mmono_f, ghalf_f, msq_f, pm1_f, p_f;
   float msq2_f, mono_half_f, g6_f, t5c_f;
 };
+
+// x / sqr(a_t) in IEEE arithmetic.  When sqr(a_t) is a power of two the
+// quotient is an exact scaling and the product by its reciprocal rounds the
+// same real number the same way (bit-identical, cheaper on the FP64 pipes).
+__device__ __forceinline__ double div_a2(const Consts &k, double x) {
+  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : x / k.a2;
+}
 
 // Per-step kick and drift factors: tau - Last_Momenta_update and
 // tau - Last_Field_update (dynamics.cpp:84,183).
