@@ -288,11 +288,12 @@ def measure_gpu(args, dist: Dist):
         ph, pp = (phi, pi) if n == N else make_fields(n)
         lat = PL.Lattice(PL.Params(N=n, precision=prec))
         lat.upload(ph, pp)
+        kernel = tune(lib, lat)
         lat.evolve(3)
         lat.evolve(k)
         _, ms_k, _ = lat.stats()
         t = ms_k / 1e3 / k
-        also[label] = {"site_updates_per_s": n ** 3 / t, "ms_per_step": t * 1e3,
+        also[label] = {"site_updates_per_s": n ** 3 / t, "ms_per_step": t * 1e3, "kernel": kernel,
                        "hbm_gbs_algorithmic": BYTES_PER_SITE[prec] * n ** 3 / t / 1e9,
                        "frac_of_measured_hbm": BYTES_PER_SITE[prec] * n ** 3 / t / 1e9 / peak}
         lat.close()
@@ -300,6 +301,17 @@ def measure_gpu(args, dist: Dist):
         also["ensemble_c3"] = measure_ensemble(2000, 100)
     out["also"] = also
     return out
+
+
+def tune(lib, lat, steps: int = 20) -> str:
+    """The project's autotuner on a live lattice (state unchanged; every
+    kernel of a precision computes the same bits); returns the kernel's name."""
+    import ctypes
+    from phinum_gb300 import _lib as L
+    v, ms, pk = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+    L.check(lib.phn_autotune(lat.h, steps, ctypes.byref(v), ctypes.byref(ms)))
+    L.check(lib.phn_get_path(lat.h, ctypes.byref(pk)))
+    return {L.PATH_PLAIN: "plain", L.PATH_TMA: f"tma variant {v.value}", L.PATH_X4: f"x4 variant {v.value}"}[pk.value]
 
 
 def measure_ensemble(steps: int, steps_per_lattice: int):
@@ -385,6 +397,7 @@ def precision_form(N: int, steps: int, check_step: int = 500, tso_steps: int = 5
     for name, prec in (("fp64", L.FP64), ("kahan_fp32", L.FP32_KAHAN), ("fp32", L.FP32)):
         lat = PL.Lattice(PL.Params(N=N, precision=prec))
         lat.upload(phi, pi)
+        kernel = tune(L.load(), lat)
         t0 = time.perf_counter()
         energies = []
         done = 0
@@ -403,7 +416,7 @@ def precision_form(N: int, steps: int, check_step: int = 500, tso_steps: int = 5
         E = np.asarray(energies)
         r = {"energy0": float(E[0]), "energy_end": float(E[-1]),
              "drift_end": float(abs(E[-1] - E[0]) / abs(E[0])),
-             "drift_max": float(np.max(np.abs(E - E[0])) / abs(E[0])), "wall_s": wall}
+             "drift_max": float(np.max(np.abs(E - E[0])) / abs(E[0])), "wall_s": wall, "kernel": kernel}
         if name == "fp64":
             ref_phi, ref_F = e_check
         else:

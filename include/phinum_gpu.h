@@ -279,14 +279,15 @@ enum { PHN_PATH_AUTO = 0, PHN_PATH_PLAIN = 1, PHN_PATH_TMA = 2, PHN_PATH_X4 = 3 
 int phn_set_path(phn_handle *h, int path);
 int phn_get_path(const phn_handle *h, int *path);
 
-/* Autotuner of the FP32 step: times the plain kernel and every variant of the
- * TMA kernel (tile height, stage count, pi through shared memory or straight
- * from HBM, grid policy) and of the x4 kernel (block shape, planes per item,
- * grid policy) that applies to this lattice, `steps` launches each on the
- * live lattice, and keeps the fastest for this handle.  *variant is its index
- * (as phn_set_variant takes it) or -1 for the plain kernel.  The lattice state
- * is unchanged; all kernels compute bit-identical fields.  Other precisions
- * have one kernel: nothing to tune (*variant = -1). */
+/* Autotuner of the FP32 and compensated FP32 steps: times the plain kernel
+ * and every variant of the TMA kernel (FP32 only: tile height, stage count,
+ * pi through shared memory or straight from HBM, grid policy) and of the x4
+ * kernel (block shape, planes per item, grid policy) that applies to this
+ * lattice, `steps` launches each on the live lattice, and keeps the fastest
+ * for this handle.  *variant is its index (as phn_set_variant takes it) or -1
+ * for the plain kernel.  The lattice state is unchanged; all kernels of a
+ * precision compute bit-identical fields.  FP64 has one kernel: nothing to
+ * tune (*variant = -1). */
 int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms);
 /* Number of variants on this handle -- the TMA kernel's first, then the x4
  * kernel's; 0 when neither applies -- and an explicit choice of one

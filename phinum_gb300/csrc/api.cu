@@ -339,7 +339,7 @@ static int step_once(phn_handle *h, int mode) {
         const bool obs = mode != MODE_STEP;
         e = launch_step_f32_x4(h->k, obs ? x4_obs_variant(h->x4_variant) : h->x4_variant,
                                obs ? h->x4_obs_grid : h->x4_grid, mode, (const float *)h->phi[h->cur],
-                               (float *)h->phi[nxt], (float *)h->pi, s, h->partials, h->stream);
+                               (float *)h->phi[nxt], (float *)h->pi, nullptr, nullptr, s, h->partials, h->stream);
         if (obs) h->obs_records = h->x4_obs_grid;
       } else if (h->path == PHN_PATH_TMA && mode != MODE_OBS) {
         e = launch_step_f32_tma(h->k, h->tma_variant, h->tma_grid, mode == MODE_STEP_OBS, (const float *)h->phi[h->cur],
@@ -352,9 +352,17 @@ static int step_once(phn_handle *h, int mode) {
       }
       break;
     default:
-      e = launch_step_kahan(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt], h->cphi,
-                            h->cphi, (float *)h->pi, h->cpi, s, h->partials, h->stream);
-      if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
+      if (h->path == PHN_PATH_X4) {
+        const bool obs = mode != MODE_STEP;
+        e = launch_step_f32_x4(h->k, obs ? x4_obs_variant(h->x4_variant) : h->x4_variant,
+                               obs ? h->x4_obs_grid : h->x4_grid, mode, (const float *)h->phi[h->cur],
+                               (float *)h->phi[nxt], (float *)h->pi, h->cphi, h->cpi, s, h->partials, h->stream);
+        if (obs) h->obs_records = h->x4_obs_grid;
+      } else {
+        e = launch_step_kahan(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt], h->cphi,
+                              h->cphi, (float *)h->pi, h->cpi, s, h->partials, h->stream);
+        if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
+      }
       break;
   }
   if (e != cudaSuccess) return cuda_error(e, "step kernel launch");
@@ -553,22 +561,30 @@ static int select_variant(phn_handle *h, int v) {
 int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms) {
   if (!h || steps < 1) return set_error(PHN_ERR_INVALID, "bad argument");
   const int nt = n_tma_variants(h), nv = nt + n_x4_variants(h);
-  if (h->p.precision != PHN_FP32 || nv == 0) {
+  if (h->p.precision == PHN_FP64 || nv == 0) {
     if (variant) *variant = -1;
     if (best_ms) *best_ms = 0.0;
     return PHN_OK;  // one kernel only: nothing to choose
   }
   int r = ensure_ref_staging(h);
   if (r) return r;
-  // pi is updated in place by a step: keep a copy and put it back after each
-  // trial, so the lattice state is unchanged by tuning (phi[cur] is only read)
+  // pi (and, compensated, both compensation words) are updated in place by a
+  // step: keep copies and put them back after each trial, so the lattice
+  // state is unchanged by tuning (phi[cur] is only read)
   const size_t bytes = h->V * h->elem;
+  const bool kahan = h->p.precision == PHN_FP32_KAHAN;
   const StepF s = {h->dtau, h->dtau};
   const int path0 = h->path, tv0 = h->tma_variant, xv0 = h->x4_variant;
   const int tg0 = h->tma_grid, xg0 = h->x4_grid, xo0 = h->x4_obs_grid;
   double best = 1e30;
   int best_v = -2;
+  float *save_c = nullptr;
+  if (kahan) CK(cudaMallocAsync((void **)&save_c, 2 * bytes, h->stream));
   CK(cudaMemcpyAsync(h->d_ref, h->pi, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  if (kahan) {
+    CK(cudaMemcpyAsync(save_c, h->cphi, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync((char *)save_c + bytes, h->cpi, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  }
   // two rounds over the candidates (plain kernel = -1), each keeping its best round
   for (int round = 0; round < 2; ++round)
     for (int v = -1; v < nv; ++v) {
@@ -581,7 +597,11 @@ int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms) {
                                   (float *)h->phi[1 - h->cur], (float *)h->pi, s, h->partials, h->d_err, h->stream);
         else if (h->path == PHN_PATH_X4)
           e = launch_step_f32_x4(h->k, h->x4_variant, h->x4_grid, MODE_STEP, (const float *)h->phi[h->cur],
-                                 (float *)h->phi[1 - h->cur], (float *)h->pi, s, h->partials, h->stream);
+                                 (float *)h->phi[1 - h->cur], (float *)h->pi, kahan ? h->cphi : nullptr,
+                                 kahan ? h->cpi : nullptr, s, h->partials, h->stream);
+        else if (kahan)
+          e = launch_step_kahan(h->k, h->grid, MODE_STEP, (const float *)h->phi[h->cur], (float *)h->phi[1 - h->cur],
+                                h->cphi, h->cphi, (float *)h->pi, h->cpi, s, h->partials, h->stream);
         else
           e = launch_step_f32(h->k, h->grid, MODE_STEP, (const float *)h->phi[h->cur], (float *)h->phi[1 - h->cur],
                               (float *)h->pi, s, h->partials, h->stream);
@@ -593,11 +613,16 @@ int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms) {
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
       CK(cudaMemcpyAsync(h->pi, h->d_ref, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      if (kahan) {
+        CK(cudaMemcpyAsync(h->cphi, save_c, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->cpi, (char *)save_c + bytes, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      }
       if (ms / steps < best) {
         best = ms / steps;
         best_v = v;
       }
     }
+  if (save_c) CK(cudaFreeAsync(save_c, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   r = check_device_error(h);
   if (r) return r;

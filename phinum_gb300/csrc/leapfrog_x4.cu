@@ -14,6 +14,11 @@
 // them with a persistent grid or launches one block per item.  Observation
 // steps always use a persistent variant (few block records to fold) and
 // per-plane FP32 partials with one compensated update per plane.
+//
+// KAHAN: the compensated FP32 step (PHN_FP32_KAHAN) -- phi and pi carry
+// per-site compensation words (read and written as float4, never read by the
+// stencil) and the kick and drift use the Kahan update of step_kahan
+// (leapfrog.cu) operation for operation, so both kernels give the same bits.
 #include "kick.cuh"
 #include "observe.cuh"
 #include "phn_internal.h"
@@ -28,9 +33,21 @@ constexpr X4Variant kX4Variants[] = {{8, 32, true}, {8, 16, true}, {4, 32, true}
                                      {8, 16, false}, {8, 8, false}, {4, 16, false}};
 constexpr int kNumX4Variants = 6;
 
-template <int W, int MODE, int THEORY>
+// The compensated kick and drift of one site (step_kahan's arithmetic).
+__device__ __forceinline__ void kahan_site(float fk, float fd, float f, float c, float ec, float p, float ep,
+                                           float &tk, float &ek, float &td, float &ed) {
+  const float yk = __fsub_rn(__fmul_rn(fk, f), ep);
+  tk = __fadd_rn(p, yk);
+  ek = __fsub_rn(__fsub_rn(tk, p), yk);
+  const float yd = __fsub_rn(__fmul_rn(fd, __fsub_rn(tk, ek)), ec);
+  td = __fadd_rn(c, yd);
+  ed = __fsub_rn(__fsub_rn(td, c), yd);
+}
+
+template <int W, int MODE, int THEORY, bool KAHAN>
 __global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const float *__restrict__ phi,
-                                                      float *__restrict__ phi_out, float *__restrict__ pi, StepF s,
+                                                      float *__restrict__ phi_out, float *__restrict__ pi,
+                                                      float *__restrict__ cphi, float *__restrict__ cpi, StepF s,
                                                       int cz, int nitems, double *__restrict__ partials) {
   const float fk = MODE == MODE_OBS ? 0.f : (float)s.fk;
   const float fd = MODE == MODE_OBS ? 0.f : (float)s.fd;
@@ -59,24 +76,58 @@ __global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const floa
       const float4 ym = __ldg((const float4 *)(pl + qym));
       const float xm = __ldg(pl + qxl), xp = __ldg(pl + qxr);
       const float4 p = *(const float4 *)(pi + i);
+      float4 ec = make_float4(0.f, 0.f, 0.f, 0.f), ep = ec;
+      if (KAHAN) {
+        ec = *(const float4 *)(cphi + i);
+        ep = *(const float4 *)(cpi + i);
+      }
       if (MODE != MODE_STEP) {
+        // observables of the represented values hi - comp (neighbours: hi only)
         const long long kidx = (long long)q + (long long)(z + 1) * NN;
         PlaneF P;
         P.clear();
-        observe_site<THEORY>(P, accf, k, c.x, p.x, c.y, yp.x, cp.x, kidx);
-        observe_site<THEORY>(P, accf, k, c.y, p.y, c.z, yp.y, cp.y, kidx + 1);
-        observe_site<THEORY>(P, accf, k, c.z, p.z, c.w, yp.z, cp.z, kidx + 2);
-        observe_site<THEORY>(P, accf, k, c.w, p.w, xp, yp.w, cp.w, kidx + 3);
+        if (KAHAN) {
+          observe_site<THEORY>(P, accf, k, __fsub_rn(c.x, ec.x), __fsub_rn(p.x, ep.x), c.y, yp.x, cp.x, kidx);
+          observe_site<THEORY>(P, accf, k, __fsub_rn(c.y, ec.y), __fsub_rn(p.y, ep.y), c.z, yp.y, cp.y, kidx + 1);
+          observe_site<THEORY>(P, accf, k, __fsub_rn(c.z, ec.z), __fsub_rn(p.z, ep.z), c.w, yp.z, cp.z, kidx + 2);
+          observe_site<THEORY>(P, accf, k, __fsub_rn(c.w, ec.w), __fsub_rn(p.w, ep.w), xp, yp.w, cp.w, kidx + 3);
+        } else {
+          observe_site<THEORY>(P, accf, k, c.x, p.x, c.y, yp.x, cp.x, kidx);
+          observe_site<THEORY>(P, accf, k, c.y, p.y, c.z, yp.y, cp.y, kidx + 1);
+          observe_site<THEORY>(P, accf, k, c.z, p.z, c.w, yp.z, cp.z, kidx + 2);
+          observe_site<THEORY>(P, accf, k, c.w, p.w, xp, yp.w, cp.w, kidx + 3);
+        }
         flush_plane(accf, P);
       }
       if (MODE != MODE_OBS) {
-        float4 pn, fn;
-        kick_drift_f32<THEORY>(k, fk, fd, c.x, xm, c.y, ym.x, yp.x, cm.x, cp.x, p.x, pn.x, fn.x);
-        kick_drift_f32<THEORY>(k, fk, fd, c.y, c.x, c.z, ym.y, yp.y, cm.y, cp.y, p.y, pn.y, fn.y);
-        kick_drift_f32<THEORY>(k, fk, fd, c.z, c.y, c.w, ym.z, yp.z, cm.z, cp.z, p.z, pn.z, fn.z);
-        kick_drift_f32<THEORY>(k, fk, fd, c.w, c.z, xp, ym.w, yp.w, cm.w, cp.w, p.w, pn.w, fn.w);
-        *(float4 *)(pi + i) = pn;
-        *(float4 *)(phi_out + i) = fn;
+        if (KAHAN) {
+          const float inv = k.inv_a2_f;
+          float4 tk, ek, td, ed;
+          kahan_site(fk, fd, force_f32<THEORY>(k, lap_diff_f32(c.x, xm, c.y, ym.x, yp.x, cm.x, cp.x, inv), c.x,
+                                               __fmul_rn(c.x, c.x)),
+                     c.x, ec.x, p.x, ep.x, tk.x, ek.x, td.x, ed.x);
+          kahan_site(fk, fd, force_f32<THEORY>(k, lap_diff_f32(c.y, c.x, c.z, ym.y, yp.y, cm.y, cp.y, inv), c.y,
+                                               __fmul_rn(c.y, c.y)),
+                     c.y, ec.y, p.y, ep.y, tk.y, ek.y, td.y, ed.y);
+          kahan_site(fk, fd, force_f32<THEORY>(k, lap_diff_f32(c.z, c.y, c.w, ym.z, yp.z, cm.z, cp.z, inv), c.z,
+                                               __fmul_rn(c.z, c.z)),
+                     c.z, ec.z, p.z, ep.z, tk.z, ek.z, td.z, ed.z);
+          kahan_site(fk, fd, force_f32<THEORY>(k, lap_diff_f32(c.w, c.z, xp, ym.w, yp.w, cm.w, cp.w, inv), c.w,
+                                               __fmul_rn(c.w, c.w)),
+                     c.w, ec.w, p.w, ep.w, tk.w, ek.w, td.w, ed.w);
+          *(float4 *)(pi + i) = tk;
+          *(float4 *)(cpi + i) = ek;
+          *(float4 *)(phi_out + i) = td;
+          *(float4 *)(cphi + i) = ed;
+        } else {
+          float4 pn, fn;
+          kick_drift_f32<THEORY>(k, fk, fd, c.x, xm, c.y, ym.x, yp.x, cm.x, cp.x, p.x, pn.x, fn.x);
+          kick_drift_f32<THEORY>(k, fk, fd, c.y, c.x, c.z, ym.y, yp.y, cm.y, cp.y, p.y, pn.y, fn.y);
+          kick_drift_f32<THEORY>(k, fk, fd, c.z, c.y, c.w, ym.z, yp.z, cm.z, cp.z, p.z, pn.z, fn.z);
+          kick_drift_f32<THEORY>(k, fk, fd, c.w, c.z, xp, ym.w, yp.w, cm.w, cp.w, p.w, pn.w, fn.w);
+          *(float4 *)(pi + i) = pn;
+          *(float4 *)(phi_out + i) = fn;
+        }
       }
       cm = c;
       c = cp;
@@ -91,7 +142,8 @@ __global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const floa
 }
 
 bool x4_supported(const phn_params &p) {
-  return p.precision == PHN_FP32 && p.Nc == 1 && p.N % 32 == 0 && p.N >= 32 && (p.potential == 0 || p.potential == 1);
+  return (p.precision == PHN_FP32 || p.precision == PHN_FP32_KAHAN) && p.Nc == 1 && p.N % 32 == 0 && p.N >= 32 &&
+         (p.potential == 0 || p.potential == 1);
 }
 
 int x4_num_variants() { return kNumX4Variants; }
@@ -109,8 +161,8 @@ static int x4_items(int N, const X4Variant &v) {
 }
 
 template <int W>
-static const void *x4_fn() {
-  return (const void *)step_f32_x4<W, MODE_STEP, 0>;
+static const void *x4_fn(bool kahan) {
+  return kahan ? (const void *)step_f32_x4<W, MODE_STEP, 0, true> : (const void *)step_f32_x4<W, MODE_STEP, 0, false>;
 }
 
 int x4_grid(const phn_params &p, int variant) {
@@ -122,7 +174,8 @@ int x4_grid(const phn_params &p, int variant) {
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const void *fn = v.w == 8 ? x4_fn<8>() : x4_fn<4>();
+  const bool kahan = p.precision == PHN_FP32_KAHAN;
+  const void *fn = v.w == 8 ? x4_fn<8>(kahan) : x4_fn<4>(kahan);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 32 * v.w, 0) != cudaSuccess || occ < 1) occ = 1;
   const int g = sms * occ;
   return g < items ? g : items;
@@ -130,20 +183,32 @@ int x4_grid(const phn_params &p, int variant) {
 
 template <int W, int MODE>
 static cudaError_t x4_launch_t(const Consts &k, int theory, int grid, int cz, int nitems, const float *phi,
-                               float *phi_out, float *pi, StepF s, double *partials, cudaStream_t st) {
-  if (theory == 0)
-    step_f32_x4<W, MODE, 0><<<grid, dim3(32, W), 0, st>>>(k, phi, phi_out, pi, s, cz, nitems, partials);
-  else
-    step_f32_x4<W, MODE, 1><<<grid, dim3(32, W), 0, st>>>(k, phi, phi_out, pi, s, cz, nitems, partials);
+                               float *phi_out, float *pi, float *cphi, float *cpi, StepF s, double *partials,
+                               cudaStream_t st) {
+  const dim3 b(32, W);
+  if (cphi) {
+    if (theory == 0)
+      step_f32_x4<W, MODE, 0, true><<<grid, b, 0, st>>>(k, phi, phi_out, pi, cphi, cpi, s, cz, nitems, partials);
+    else
+      step_f32_x4<W, MODE, 1, true><<<grid, b, 0, st>>>(k, phi, phi_out, pi, cphi, cpi, s, cz, nitems, partials);
+  } else {
+    if (theory == 0)
+      step_f32_x4<W, MODE, 0, false><<<grid, b, 0, st>>>(k, phi, phi_out, pi, nullptr, nullptr, s, cz, nitems,
+                                                          partials);
+    else
+      step_f32_x4<W, MODE, 1, false><<<grid, b, 0, st>>>(k, phi, phi_out, pi, nullptr, nullptr, s, cz, nitems,
+                                                          partials);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_step_f32_x4(const Consts &k, int variant, int grid, int mode, const float *phi, float *phi_out,
-                               float *pi, StepF s, double *partials, cudaStream_t st) {
+                               float *pi, float *cphi, float *cpi, StepF s, double *partials, cudaStream_t st) {
   const X4Variant &v = kX4Variants[variant];
   const int cz = v.cz < k.N ? v.cz : k.N;
   const int nitems = x4_items(k.N, v);
-#define PHN_X4(WV, MD) return x4_launch_t<WV, MD>(k, k.theory, grid, cz, nitems, phi, phi_out, pi, s, partials, st)
+#define PHN_X4(WV, MD) \
+  return x4_launch_t<WV, MD>(k, k.theory, grid, cz, nitems, phi, phi_out, pi, cphi, cpi, s, partials, st)
   if (v.w == 8) {
     if (mode == MODE_STEP) PHN_X4(8, MODE_STEP);
     if (mode == MODE_STEP_OBS) PHN_X4(8, MODE_STEP_OBS);

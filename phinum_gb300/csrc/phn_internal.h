@@ -110,14 +110,15 @@ cudaError_t launch_step_f32_tma(const Consts &k, int variant, int grid, bool obs
                                 float *pi, StepF s, double *partials, int *err, cudaStream_t st);
 
 // Register FP32 step with four x-sites per thread (leapfrog_x4.cu): Nc = 1,
-// N a multiple of 32; variants are block shapes and grid policies, all
-// bit-identical to the other FP32 kernels.  mode: MODE_STEP/STEP_OBS/OBS.
+// N a multiple of 32, FP32 or compensated FP32 (cphi, cpi non-null);
+// variants are block shapes and grid policies, all bit-identical to the
+// other kernels of the same precision.  mode: MODE_STEP/STEP_OBS/OBS.
 bool x4_supported(const phn_params &p);
 int x4_num_variants();
 int x4_obs_variant(int variant);  // the persistent variant observation steps use
 int x4_grid(const phn_params &p, int variant);
 cudaError_t launch_step_f32_x4(const Consts &k, int variant, int grid, int mode, const float *phi, float *phi_out,
-                               float *pi, StepF s, double *partials, cudaStream_t st);
+                               float *pi, float *cphi, float *cpi, StepF s, double *partials, cudaStream_t st);
 
 // Layout conversion between the reference layout (host order, ghosts) and
 // the device SoA layout [a][z][y][x] (layout.cu).

@@ -396,3 +396,49 @@ def test_x4_path_matches_plain_path_bit_for_bit(N, theory):
         assert np.array_equal(a0[17:23], a1[17:23]), key
         np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
         np.testing.assert_allclose(a0[9:17], a1[9:17], rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.parametrize("N", [64, 128])
+def test_compensated_x4_matches_plain_compensated_bit_for_bit(N):
+    """The compensated FP32 step in the x4 kernel (every variant) against
+    step_kahan: identical fields and compensation words (the download returns
+    hi - comp), SO rows to FP32-summation rounding, extrema exact; tuning
+    leaves the state unchanged."""
+    import ctypes
+    import inputs
+    PL = gpu()
+    from phinum_gb300 import _lib as L
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 70, phi0=6 ** 0.5)
+    phi, pi = O.to_ref_layout(phi_i), O.to_ref_layout(pi_i)
+    lat = PL.Lattice(PL.Params(N=N, precision=2))
+    nv = ctypes.c_int()
+    L.check(lat.lib.phn_num_variants(lat.h, ctypes.byref(nv)))
+    lat.close()
+    assert nv.value >= 2
+    out = {}
+    for variant in [None] + list(range(nv.value)):
+        lat = PL.Lattice(PL.Params(N=N, precision=2))
+        if variant is None:
+            L.check(lat.lib.phn_set_path(lat.h, L.PATH_PLAIN))
+        else:
+            L.check(lat.lib.phn_set_variant(lat.h, variant))
+        lat.upload(phi, pi)
+        rows = lat.run_loop(120, 0.5)
+        lat.evolve(7)
+        out[variant] = (rows,) + lat.download()
+        lat.close()
+    r0, f0, p0 = out[None]
+    for key, (r1, f1, p1) in out.items():
+        assert np.array_equal(f0, f1) and np.array_equal(p0[N * N:-N * N], p1[N * N:-N * N]), key
+        assert np.array_equal(r0[:, 17:23], r1[:, 17:23]), key
+        np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
+    lat = PL.Lattice(PL.Params(N=N, precision=2))
+    lat.upload(phi, pi)
+    lat.evolve(3)
+    before = lat.download()
+    v, ms = ctypes.c_int(), ctypes.c_double()
+    L.check(lat.lib.phn_autotune(lat.h, 3, ctypes.byref(v), ctypes.byref(ms)))
+    after = lat.download()
+    assert np.array_equal(before[0], after[0]) and np.array_equal(before[1][N * N:-N * N], after[1][N * N:-N * N])
+    assert v.value >= -1
+    lat.close()
