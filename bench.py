@@ -612,7 +612,7 @@ def io_form(N: int, directory: str):
     return out
 
 
-def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int):
+def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int, warmup: int = 1):
     """The oracle's reference loop (FP64) on all host threads, bounded."""
     from oracle import oracle as O
     O.build()
@@ -620,7 +620,7 @@ def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int):
     phi, pi = make_fields(N)
     nt = O.max_threads(True)
     clock = O.Clock(p, fast=True)
-    O.evolve(p, phi, pi, 1, clock, nthreads=nt, fast=True)  # warm-up, page-in
+    O.evolve(p, phi, pi, max(1, warmup), clock, nthreads=nt, fast=True)  # warm-up, page-in
     t0 = time.perf_counter()
     steps = 0
     while steps < steps_cap and time.perf_counter() - t0 < max_seconds:
@@ -640,7 +640,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extra", action="store_true", help="skip the other sizes/precisions")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
-    ap.add_argument("--n", type=int, default=N_MAIN, help="lattice edge (profiling runs use smaller cases)")
+    ap.add_argument("--n", "--lattice-edge", dest="n", type=int, default=N_MAIN,
+                    help="lattice edge (profiling runs use smaller cases); under torchrun spell it --lattice-edge")
     ap.add_argument("--variant", type=int, default=None, help="TMA kernel variant instead of the autotuner's pick")
     ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble", "initial", "io"],
                     help="report one of the north-star forms instead of the benchmark line")
@@ -682,12 +683,13 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        rate, nt, steps, dt = cpu_reference_rate(N_MAIN, 45.0, max(1, args.steps))
+        warm = max(3, args.warmup)
+        rate, nt, steps, dt = cpu_reference_rate(args.n, 45.0, max(1, args.steps), warm)
         line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": args.gpus,
-                "steps": steps, "warmup": 1, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
+                "steps": steps, "warmup": warm, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": rate, "unit": METRIC, "cores": nt, "kind": "port",
-                                 "sample": f"{steps} steps of the {N_MAIN}^3 lattice, FP64, {nt} OpenMP threads "
+                                 "sample": f"{steps} steps of the {args.n}^3 lattice, FP64, {nt} OpenMP threads "
                                            f"over z-slabs, -O3 -ffast-math (reference flags)"},
                 "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -706,9 +708,9 @@ def main():
             "gpu_launches": res["gpu_launches"], "also": res["also"],
             "so_rows": res["rows"], "energy_drift_rel": res["energy_drift"]}
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, nt, steps, dt = cpu_reference_rate(N_MAIN, 15.0, 200)
+        rate, nt, steps, dt = cpu_reference_rate(args.n, 15.0, 200, 3)
         line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": nt, "kind": "port",
-                                "sample": f"{steps} steps of the {N_MAIN}^3 lattice ({dt:.1f} s), FP64, {nt} "
+                                "sample": f"{steps} steps of the {args.n}^3 lattice ({dt:.1f} s), FP64, {nt} "
                                           f"OpenMP threads over z-slabs, -O3 -ffast-math (reference flags)"}
     if rank == 0:
         print(json.dumps(line))
