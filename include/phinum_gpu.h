@@ -296,6 +296,13 @@ int phn_autotune(phn_handle *h, int steps, int *variant, double *best_ms);
 int phn_num_variants(const phn_handle *h, int *n);
 int phn_set_variant(phn_handle *h, int variant);
 
+/* Self-test of the failure path: a kernel waits on a device barrier that
+ * nothing completes, with a budget of `polls` polls (1 .. the step kernels'
+ * budget), gives up, records the code in the handle's error word and returns.
+ * Returns PHN_ERR_TIMEOUT, as a step whose pipeline stalled would; the handle
+ * stays usable.  No copy is issued and nothing faults. */
+int phn_wait_selftest(phn_handle *h, long long polls);
+
 /* Device pointers of the current fields (precision-typed: double* for
  * PHN_FP64, float* otherwise; SoA [a][z][y][x], no ghosts) and the stream the
  * handle launches on, for callers that keep data resident on the device. */

@@ -55,9 +55,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 // if it does not within the poll budget (then `code` goes to *err and the
 // block-wide *abort flag is raised) or if another thread of the block raised
 // *abort meanwhile.  err and abort may be null.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code, int *abort) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code, int *abort,
+                                          long long polls = kWaitPolls) {
   volatile int *ab = abort;
-  for (long long i = 0; i < kWaitPolls; ++i) {
+  for (long long i = 0; i < polls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if (ab && *ab) return false;
     if (i > 32) __nanosleep(64);
