@@ -29,4 +29,9 @@ for t in 2 3 4 5; do
   build libphinum_ref_t${t}_f64.so -DPHN_REF_THEORY=$t -DPHN_REF_PRECISION=0 &
 done
 wait
+# the expanding box (expansion 1), every theory
+for t in 0 1 2 3 4 5; do
+  build libphinum_ref_t${t}_f64_exp.so -DPHN_REF_THEORY=$t -DPHN_REF_PRECISION=0 -DPHN_REF_EXPANSION=1 &
+done
+wait
 ls -1 "$OUT"

@@ -50,17 +50,20 @@ class Params:
     g: float = 2.0            # theory 4
     p_mono: float = -0.5      # theory 5
     m_mono_sqr: float = 1.0   # theory 3
+    expansion: int = 0        # 1: radiation-era expanding box
+    H0: float = 0.0171156     # H_0 (parameters.cpp:177)
 
 
 class _CParams(ctypes.Structure):
     _fields_ = [("N", _I), ("Nc", _I), ("theory", _I), ("mass_mode", _I), ("lambda_mode", _I),
-                ("pad_", _I), ("a", _D), ("dt", _D), ("T0", _D), ("m_sqr", _D), ("kappa", _D),
-                ("h", _D), ("g", _D), ("p_mono", _D), ("m_mono_sqr", _D)]
+                ("expansion", _I), ("a", _D), ("dt", _D), ("T0", _D), ("m_sqr", _D), ("kappa", _D),
+                ("h", _D), ("g", _D), ("p_mono", _D), ("m_mono_sqr", _D), ("H0", _D)]
 
 
 class _CClock(ctypes.Structure):
     _fields_ = [("tau", _D), ("dtau", _D), ("last_mom", _D), ("last_field", _D),
-                ("steps", _I), ("pad_", _I)]
+                ("steps", _I), ("pad_", _I), ("tau_c", _D), ("sf", _D), ("last_mom_c", _D),
+                ("last_field_c", _D)]
 
 
 class _CIc(ctypes.Structure):
@@ -75,8 +78,8 @@ IC_DEFAULTS = dict(seed=1, justnoise=0, QS=1.0, scale2=1.0, amplitude=0.0, noise
 
 
 def _cp(p: Params) -> _CParams:
-    return _CParams(p.N, p.Nc, p.theory, p.mass_mode, p.lambda_mode, 0, p.a, p.dt, p.T0,
-                    p.m_sqr, p.kappa, p.h, p.g, p.p_mono, p.m_mono_sqr)
+    return _CParams(p.N, p.Nc, p.theory, p.mass_mode, p.lambda_mode, int(p.expansion), p.a, p.dt, p.T0,
+                    p.m_sqr, p.kappa, p.h, p.g, p.p_mono, p.m_mono_sqr, p.H0)
 
 
 def _ptr(a: np.ndarray, kind=_PD):
@@ -161,10 +164,12 @@ def _load(fast: bool = False):
         lib.orc_apply_filter.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _D, _I, _PD, _I, _D]
         lib.orc_apply_filter.restype = _I
         lib.orc_spectrum_columns.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _PD, _PI, _I, _PD]
-        lib.orc_islands.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, _D, _I, _I, _PI, _PD, _I]
-        lib.orc_islands.restype = _I
-        lib.orc_site_energy.argtypes = [ctypes.POINTER(_CParams), _PD, _PD, ctypes.c_long, _I, _I, _I]
-        lib.orc_site_energy.restype = _D
+        lib.orc_islands_at.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock), _PD, _PD, _D, _I, _I,
+                                       _PI, _PD, _I]
+        lib.orc_islands_at.restype = _I
+        lib.orc_site_energy_at.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock), _PD, _PD,
+                                           ctypes.c_long, _I, _I, _I]
+        lib.orc_site_energy_at.restype = _D
         lib.orc_max_threads.restype = _I
         _libs[key] = lib
     return _libs[key]
@@ -184,6 +189,16 @@ class Clock:
     @property
     def steps(self) -> int:
         return self._c.steps
+
+    @property
+    def tau_c(self) -> float:
+        """Conformal time (tau for the static box)."""
+        return self._c.tau_c
+
+    @property
+    def sf(self) -> float:
+        """Scale factor (1 for the static box)."""
+        return self._c.sf
 
 
 def max_threads(fast: bool = True) -> int:
@@ -271,27 +286,31 @@ def spectrum_columns(p: Params, F, K, Q, C) -> np.ndarray:
     return cols
 
 
-def site_energy(p: Params, phi: np.ndarray, pi: np.ndarray) -> np.ndarray:
-    """rho(x) for every interior site, [z][y][x] (slow; small lattices only)."""
+def site_energy(p: Params, phi: np.ndarray, pi: np.ndarray, clock: Clock | None = None) -> np.ndarray:
+    """rho(x) for every interior site, [z][y][x] (slow; small lattices only).
+    The expanding box reads the scale factor from clock."""
     N = p.N
     out = np.zeros((N, N, N))
     lib = _load()
     cp = ctypes.byref(_cp(p))
+    ck = ctypes.byref(clock._c) if clock else None
     for z in range(N):
         for y in range(N):
             for x in range(N):
                 K = p.Nc * (x + N * y + N * N * (z + 1))
-                out[z, y, x] = lib.orc_site_energy(cp, _ptr(phi), _ptr(pi), K, x, y, z + 1)
+                out[z, y, x] = lib.orc_site_energy_at(cp, ck, _ptr(phi), _ptr(pi), K, x, y, z + 1)
     return out
 
 
 def islands(p: Params, phi: np.ndarray, pi: np.ndarray, thres: float, mode: int = 0, zper: int = 0,
-            max_islands: int = 1 << 20):
-    """Returns (labels in reference layout, island records [n][10])."""
+            max_islands: int = 1 << 20, clock: Clock | None = None):
+    """Returns (labels in reference layout, island records [n][10]).  The
+    expanding box reads the scale factor from clock."""
     labels = np.zeros(field_len(p), dtype=np.int32)
     recs = np.zeros((max_islands, len(ISLAND_FIELDS)))
-    n = _load().orc_islands(ctypes.byref(_cp(p)), _ptr(phi), _ptr(pi), float(thres), int(mode),
-                            int(zper), _ptr(labels, _PI), _ptr(recs), max_islands)
+    n = _load().orc_islands_at(ctypes.byref(_cp(p)), ctypes.byref(clock._c) if clock else None, _ptr(phi),
+                               _ptr(pi), float(thres), int(mode), int(zper), _ptr(labels, _PI), _ptr(recs),
+                               max_islands)
     if n < 0:
         raise MemoryError("oracle islands: allocation failed")
     return labels, recs[:min(n, max_islands)]
@@ -301,12 +320,12 @@ def islands(p: Params, phi: np.ndarray, pi: np.ndarray, thres: float, mode: int 
 REF_DIR = os.path.join(HERE, "_ref")
 
 
-def ref_path(theory: int = 0, precision: str = "f64") -> str:
-    return os.path.join(REF_DIR, f"libphinum_ref_t{theory}_{precision}.so")
+def ref_path(theory: int = 0, precision: str = "f64", expansion: int = 0) -> str:
+    return os.path.join(REF_DIR, f"libphinum_ref_t{theory}_{precision}{'_exp' if expansion else ''}.so")
 
 
-def ref_available(theory: int = 0, precision: str = "f64") -> bool:
-    return os.path.exists(ref_path(theory, precision))
+def ref_available(theory: int = 0, precision: str = "f64", expansion: int = 0) -> bool:
+    return os.path.exists(ref_path(theory, precision, expansion))
 
 
 class Reference:
@@ -315,7 +334,7 @@ class Reference:
 
     def __init__(self, p: Params, precision: str = "f64"):
         self.p = p
-        lib = ctypes.CDLL(ref_path(p.theory, precision))
+        lib = ctypes.CDLL(ref_path(p.theory, precision, p.expansion))
         lib.ref_init.argtypes = [_I, _I, _D, _D, _D, _I, _D, _I, _D, _D, _D]
         lib.ref_init.restype = _I
         lib.ref_set_fields.argtypes = [_PD, _PD]
@@ -341,6 +360,9 @@ class Reference:
         self.lib = lib
         lib.ref_set_extra.argtypes = [_D, _D, _D]
         lib.ref_set_extra(p.g, p.p_mono, p.m_mono_sqr)
+        lib.ref_set_h0.argtypes = [_D]
+        lib.ref_set_h0(p.H0)
+        lib.ref_expansion_state.argtypes = [_PD, _PD]
         r = lib.ref_init(p.N, p.Nc, p.a, p.dt, p.T0, p.mass_mode, p.m_sqr, p.lambda_mode, 1.0,
                          p.kappa, p.h)
         if r != 0:
@@ -400,6 +422,12 @@ class Reference:
         t, s = _D(), _I()
         self.lib.ref_time(ctypes.byref(t), ctypes.byref(s))
         return t.value, s.value
+
+    def expansion_state(self):
+        """(conformal time, scale factor); (tau, 1) for the static box."""
+        tc, sf = _D(), _D()
+        self.lib.ref_expansion_state(ctypes.byref(tc), ctypes.byref(sf))
+        return tc.value, sf.value
 
     def averages(self) -> np.ndarray:
         out = np.zeros(AVG_LEN)

@@ -70,13 +70,34 @@ int orc_max_threads(void) {
 }
 
 /* ------------------------------------------------------------ time keeping */
-/* reset(): dynamics.cpp:28-50 (static box). */
+/* Conformal time and scale factor of the radiation-era box at cosmic time
+ * tau (dynamics.cpp:39-40, :204-205). */
+static void conformal(const orc_params *p, orc_clock *c) {
+  c->tau_c = (sqrt(1. + 2. * p->H0 * c->tau) - 1.) / p->H0;
+  c->sf = sqrt(1. + 2. * p->H0 * c->tau);
+}
+
+/* The scale factor a clock carries: 1 for the static box or no clock. */
+static double clock_sf(const orc_params *p, const orc_clock *c) {
+  return (p->expansion && c) ? c->sf : 1.0;
+}
+
+/* reset(): dynamics.cpp:28-50. */
 void orc_reset(const orc_params *p, orc_clock *c) {
   c->tau = p->T0;
   c->dtau = p->dt * p->a;
   c->last_mom = c->tau;
   c->last_field = c->tau;
   c->steps = 0;
+  c->pad_ = 0;
+  if (p->expansion) {
+    conformal(p, c);
+  } else {
+    c->tau_c = c->tau;
+    c->sf = 1.0;
+  }
+  c->last_mom_c = c->tau_c;
+  c->last_field_c = c->tau_c;
 }
 
 /* Communication::exchange() with one rank: comm.cpp:63-78. */
@@ -86,11 +107,39 @@ void orc_exchange(const orc_params *p, double *f) {
   memcpy(f, f + (long)p->N * slab, (size_t)slab * sizeof(double));
 }
 
+/* updateMomenta() of the expanding box (dynamics.cpp:88-93, :102-107,
+ * :116-121, :130-135, :144-149, :158-163) at one site and component.  The
+ * couplings carry powers of the scale factor sf in the reference's order of
+ * operations; theories 3-5 read the a == 0 branch (they run with Nc = 1). */
+static double kick_expanded(const orc_params *p, double LapPhi, double phi, double locPhiSqr, int a, double sf) {
+  const int Nc = p->Nc;
+  const double mass = p->m_sqr;
+  switch (p->theory) {
+    case 0:
+      return LapPhi - ((double)p->mass_mode * mass * sf * sf + (double)p->lambda_mode * (locPhiSqr / (6. * Nc)) +
+                       (sqr(locPhiSqr / p->kappa / sf) / (120. * Nc * Nc))) * phi;
+    case 1:
+      if (a == 0)
+        return LapPhi - p->h * sf * sf * sf -
+               ((double)p->mass_mode * mass * sf * sf + (double)p->lambda_mode * (locPhiSqr / (6. * Nc))) * phi;
+      return LapPhi - ((double)p->mass_mode * mass * sf * sf + (double)p->lambda_mode * (locPhiSqr / (6. * Nc))) * phi;
+    case 2:
+      return LapPhi - mass * sqrt(mass) * sf * sf * sf * (phi / sqrt(locPhiSqr)) * sin(sqrt(locPhiSqr) / sf / sqrt(mass));
+    case 3: /* the expanded monodromy force is sin(phi / (sf sqrt(M))), without the phi/|phi| factor */
+      return LapPhi - p->m_mono_sqr * sf * sf * phi - mass * sqrt(mass) * sf * sf * sf * sin(phi / (sf * sqrt(mass)));
+    case 4:
+      return LapPhi - ((double)p->mass_mode * mass * sf * sf - p->g * sf * phi / 2. +
+                       (double)p->lambda_mode * (locPhiSqr / (6. * Nc))) * phi;
+    default:
+      return LapPhi - mass * sf * sf * phi * pow((1. + locPhiSqr / mass / sf / sf), (p->p_mono - 1));
+  }
+}
+
 /* updateMomenta(): dynamics.cpp:52-175 for theories 0 (:82-87), 1 (:96-101),
- * 2 (:109-114), 3 (:123-129), 4 (:137-143) and 5 (:151-157), static box,
- * slabs z in [z0, z1). */
+ * 2 (:109-114), 3 (:123-129), 4 (:137-143) and 5 (:151-157), slabs z in
+ * [z0, z1).  sf > 0 selects the expanding box's forms (kick_expanded). */
 static void update_momenta_slabs(const orc_params *p, const double *Phi, double *Pi,
-                                 double factor, int z0, int z1) {
+                                 double factor, int z0, int z1, double sf) {
   const int N = p->N, Nc = p->Nc;
   const double mass = p->m_sqr; /* BareM_sqr_long == BareM_sqr_trans == M_sqr (renormalization.cpp:8-9) */
   for (int z = z0; z < z1; z++) {
@@ -108,7 +157,9 @@ static void update_momenta_slabs(const orc_params *p, const double *Phi, double 
         for (int a = 0; a < Nc; a++) {
           double LapPhi = (Phi[Kuoo] + Phi[Kdoo] + Phi[Kouo] + Phi[Kodo] + Phi[Koou] + Phi[Kood] -
                            6. * Phi[Kooo]) / sqr(p->a);
-          if (p->theory == 0) {
+          if (sf > 0) {
+            Pi[Kooo] += kick_expanded(p, LapPhi, Phi[Kooo], locPhiSqr, a, sf) * factor;
+          } else if (p->theory == 0) {
             Pi[Kooo] += (LapPhi - ((double)p->mass_mode * mass +
                                    (double)p->lambda_mode * (locPhiSqr / (6. * Nc)) +
                                    (sqr(locPhiSqr / p->kappa) / (120. * Nc * Nc))) * Phi[Kooo]) * factor;
@@ -144,21 +195,32 @@ void orc_evolve(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int 
   const int N = p->N;
   const long begin = pos3(p, 0, 0, 1), end = (long)p->Nc * N * N * (N + 1);
   if (nthreads < 1) nthreads = 1;
+  const int ex = p->expansion;
   for (int s = 0; s < nsteps; s++) {
     c->tau += 0.5 * c->dtau;
-    const double fk = c->tau - c->last_mom;
+    if (ex) conformal(p, c);
+    /* the expanding box steps in conformal time (dynamics.cpp:88-93, :186-187) */
+    const double fk = ex ? c->tau_c - c->last_mom_c : c->tau - c->last_mom;
+    const double sf = ex ? c->sf : 0.0;
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads) schedule(static)
 #endif
-    for (int z = 1; z < N + 1; z++) update_momenta_slabs(p, Phi, Pi, fk, z, z + 1);
+    for (int z = 1; z < N + 1; z++) update_momenta_slabs(p, Phi, Pi, fk, z, z + 1, sf);
     c->last_mom = c->tau;
+    c->last_mom_c = ex ? c->tau_c : c->tau;
     c->tau += 0.5 * c->dtau;
-    const double fd = c->tau - c->last_field;
+    if (ex) conformal(p, c);
+    const double fd = ex ? c->tau_c - c->last_field_c : c->tau - c->last_field;
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads) schedule(static)
 #endif
-    for (long K = begin; K < end; K++) Phi[K] += Pi[K] * fd; /* updateFields, dynamics.cpp:182-183 */
+    for (long K = begin; K < end; K++) Phi[K] += Pi[K] * fd; /* updateFields, dynamics.cpp:180-187 */
     c->last_field = c->tau;
+    c->last_field_c = ex ? c->tau_c : c->tau;
+    if (!ex) {
+      c->tau_c = c->tau;
+      c->sf = 1.0;
+    }
     orc_exchange(p, Phi);
     c->steps++;
   }
@@ -195,9 +257,24 @@ static void extrema(const orc_params *p, const double *Phi, orc_row *o) {
 /* The per-site (all components) interaction terms of CalculateVolumeAverages
  * (fieldanalysis.cpp:565-617; per component :456-508), static box; locPhi is the sum of the
  * components (:434-443). */
-static double site_interaction(const orc_params *p, double locPhiSqr, double locPhi) {
+static double site_interaction(const orc_params *p, double locPhiSqr, double locPhi, double sf) {
   const int Nc = p->Nc;
   const double mass = p->m_sqr;
+  if (p->expansion) /* fieldanalysis.cpp:573-615 */
+    switch (p->theory) {
+      case 0:
+        return ((double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)) +
+                (sqr(locPhiSqr) * locPhiSqr / (720.0 * Nc * Nc * p->kappa * p->kappa * sf * sf)));
+      case 1:
+        return (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc));
+      case 2:
+      case 3:
+        return sqr(sf * sf * mass) * (1. - cos(sqrt(locPhiSqr) / (sf * sqrt(mass))));
+      case 4:
+        return (((-p->g * sf * locPhi * locPhiSqr) / (6.0)) + (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)));
+      default:
+        return sqr(sf * sf * mass) * 0.5 / p->p_mono * (pow((1. + locPhiSqr / mass / sf / sf), p->p_mono) - 1.);
+    }
   switch (p->theory) {
     case 0:
       return (double)(p->lambda_mode) * (sqr(locPhiSqr) / (24.0 * Nc)) +
@@ -214,13 +291,40 @@ static double site_interaction(const orc_params *p, double locPhiSqr, double loc
   }
 }
 
+/* The per-component mass / linear terms of CalculateVolumeAverages
+ * (fieldanalysis.cpp:454-508): static box, or expanding box with scale
+ * factor sf. */
+static double component_interaction(const orc_params *p, double phi, int a, double sf) {
+  const double mass = p->m_sqr;
+  if (p->expansion) {
+    if (p->theory == 0 || p->theory == 4)
+      return (double)(p->mass_mode) * 0.5 * mass * sf * sf * sqr(phi);
+    if (p->theory == 3)
+      return (0.5 * p->m_mono_sqr * (sqr(sf)) * sqr(phi));
+    if (p->theory == 1 && a == 0)
+      return (p->h * phi * sf * sf * sf + (double)(p->mass_mode) * 0.5 * mass * sf * sf * sqr(phi));
+    if (p->theory == 1)
+      return (double)(p->mass_mode) * 0.5 * mass * sf * sf * sqr(phi);
+    return 0.0;
+  }
+  if (p->theory == 0 || p->theory == 4)
+    return (double)(p->mass_mode) * 0.5 * mass * sqr(phi);
+  if (p->theory == 3)
+    return 0.5 * p->m_mono_sqr * sqr(phi);
+  if (p->theory == 1 && a == 0)
+    return (p->h * phi + (double)(p->mass_mode) * 0.5 * mass * sqr(phi));
+  if (p->theory == 1)
+    return (double)(p->mass_mode) * 0.5 * mass * sqr(phi);
+  return 0.0;
+}
+
 /* CalculateVolumeAverages(): fieldanalysis.cpp:399-699, theories 0 to 5,
- * static box, no charge / energy-density extras.  Also returns the gradient
- * term GradPhiSqr/vol, which the reference keeps local. */
-static void volume_averages(const orc_params *p, const double *Phi, const double *Pi, orc_row *o) {
+ * static or expanding box (scale factor sf), no charge / energy-density
+ * extras.  Also returns the gradient term GradPhiSqr/vol, which the
+ * reference keeps local. */
+static void volume_averages(const orc_params *p, const double *Phi, const double *Pi, orc_row *o, double sf) {
   const int N = p->N, Nc = p->Nc;
   const int vol = N * N * N;
-  const double mass = p->m_sqr;
   double phi[ORC_MAX_NC], pi[ORC_MAX_NC];
   for (int a = 0; a < Nc; a++) { phi[a] = 0.0; pi[a] = 0.0; }
   double phi2 = 0., pi2 = 0., phi4 = 0., phi6 = 0., phipi = 0.;
@@ -243,25 +347,21 @@ static void volume_averages(const orc_params *p, const double *Phi, const double
           locPhi += Phi[Kooo];
           GradPhiSqr += (sqr(Phi[Kuoo] - Phi[Kooo]) / sqr(p->a) + sqr(Phi[Kouo] - Phi[Kooo]) / sqr(p->a) +
                          sqr(Phi[Koou] - Phi[Kooo]) / sqr(p->a));
-          if (p->theory == 0 || p->theory == 4) {
-            Interaction += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
-          } else if (p->theory == 3) {
-            Interaction += 0.5 * p->m_mono_sqr * sqr(Phi[Kooo]);
-          } else if (p->theory == 1) {
-            if (a == 0)
-              Interaction += (p->h * Phi[Kooo] + (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]));
-            else
-              Interaction += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
-          }
+          if (p->theory == 0 || p->theory == 1 || p->theory == 3 || p->theory == 4)
+            Interaction += component_interaction(p, Phi[Kooo], a, sf);
           Kooo++; Kuoo++; Kouo++; Koou++;
         }
         phi4 += sqr(locPhiSqr);
         phi6 += sqr(locPhiSqr) * locPhiSqr;
-        Interaction += site_interaction(p, locPhiSqr, locPhi);
+        Interaction += site_interaction(p, locPhiSqr, locPhi, sf);
       }
   for (int a = 0; a < Nc; a++) { phi[a] /= (vol); pi[a] /= (vol); }
   Charge = (0.5 * pi2 - GradPhiSqr / 6. - Interaction);
   Energy = (0.5 * pi2 + 0.5 * GradPhiSqr + Interaction);
+  if (p->expansion) { /* fieldanalysis.cpp:626-629 */
+    Energy += (0.5 * phi2 * sqr(p->H0 / sf) - phipi * p->H0 / sf);
+    Charge += (0.5 * phi2 * sqr(p->H0 / sf) - phipi * p->H0 / sf);
+  }
   Energy /= (vol);
   Interaction /= (vol);
   Charge /= (vol);
@@ -283,7 +383,9 @@ void orc_averages(const orc_params *p, const orc_clock *c, const double *Phi, co
   memset(o, 0, sizeof(*o));
   o->t = c ? c->tau : 0.0;
   extrema(p, Phi, o);
-  volume_averages(p, Phi, Pi, o);
+  const double sf = clock_sf(p, c);
+  volume_averages(p, Phi, Pi, o, sf);
+  o->reserved[1] = sf; /* the SO row's scale factor (fieldanalysis.cpp:789-791); 1 for the static box */
 }
 
 /* main.cpp:685-699 with an explicit step count; Print_AveragesExtrema()'s
@@ -566,8 +668,11 @@ static void ic_fft_ptox(const orc_params *p, const double *hre, const double *hi
 }
 
 /* SetInitialConditions (initialconditions.cpp:45-723), initialize 3,
- * expansion 0, withcharge 0, one rank.  Phi/Pi in the reference layout;
- * Phi's ghost slabs exchanged, Pi's left as they were.  Returns 0. */
+ * withcharge 0, one rank.  The expanding box (:459-465, :504-510, :581-583,
+ * :656-658) seeds a scale-invariant spectrum below QS, frequencies with the
+ * initial scale factor squared, E = H0 A and Pi_0 += phi0_0 H0.  Phi/Pi in
+ * the reference layout; Phi's ghost slabs exchanged, Pi's left as they
+ * were.  Returns 0. */
 int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, double *Pi) {
   const int N = p->N, Nc = p->Nc, M = N / 2 + 1;
   const long NM = (long)N * N * M, NN = (long)N * N;
@@ -596,15 +701,17 @@ int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, d
           const double gauss1 = fabs(ic_gauss()), gauss2 = fabs(ic_gauss());
           const double pchisqr = sqr(pt) + sqr(nu);
           double occ;
-          if (ic->justnoise == 0) {
-            if (pchisqr < ic->QS * ic->QS) occ = ic->amplitude + ic->noise;
-            else if (ic->scale2 == 0) occ = ic->noise;
-            else occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
+          if (ic->justnoise == 0 && p->expansion && psqr > 0. && psqr < (ic->QS * ic->QS)) {
+            const double omegap = sqrt(psqr + (1. + 2. * p->H0 * p->T0) * ic->m2_long);
+            occ = 2. * acos(-1.) * acos(-1.) * 2.1e-9 * ic->phi0[0] * ic->phi0[0] / psqr / sqrt(psqr) * omegap;
+          } else if (ic->justnoise == 0 && !p->expansion && pchisqr < ic->QS * ic->QS) {
+            occ = ic->amplitude + ic->noise;
           } else {
             if (ic->scale2 == 0) occ = ic->noise;
             else occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
           }
-          const double omega = c == 0 ? sqrt(psqr + ic->m2_long) : sqrt(psqr + ic->m2_trans);
+          const double m2 = c == 0 ? ic->m2_long : ic->m2_trans;
+          const double omega = p->expansion ? sqrt(psqr + (1. + 2. * p->H0 * p->T0) * m2) : sqrt(psqr + m2);
           const double s1 = sqrt(occ) * gauss1, s2 = sqrt(occ) * gauss2;
           const long o = (long)c * NM + posMom;
           if (fabs(omega) < 1e-8) {
@@ -612,7 +719,11 @@ int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, d
           } else {
             const double so = sqrt(omega);
             Are[o] = s1 * cos(phase1) / so; Aim[o] = s1 * sin(phase1) / so;
-            Ere[o] = s2 * cos(phase2) * so; Eim[o] = s2 * sin(phase2) * so;
+            if (p->expansion) {
+              Ere[o] = Are[o] * p->H0; Eim[o] = Aim[o] * p->H0;
+            } else {
+              Ere[o] = s2 * cos(phase2) * so; Eim[o] = s2 * sin(phase2) * so;
+            }
           }
         }
       }
@@ -627,10 +738,14 @@ int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, d
     for (int c = 0; c < Nc; c++) {
       ic_fft_ptox(p, (f == 0 ? Are : Ere) + (long)c * NM, (f == 0 ? Aim : Eim) + (long)c * NM, X);
       const double off = c < 2 ? (f == 0 ? ic->phi0[c] : ic->pi0[c]) : 0.0;
+      const int hubble = p->expansion && f == 1 && c == 0; /* + phi0_0 H0 (:657) */
       double *dst = f == 0 ? Phi : Pi;
       for (int z = 0; z < N; z++)
         for (int y = 0; y < N; y++)
-          for (int x = 0; x < N; x++) dst[c + pos3(p, x, y, z + 1)] = X[x + N * y + NN * z] * NormFactor + off;
+          for (int x = 0; x < N; x++) {
+            const double v = X[x + N * y + NN * z] * NormFactor + off;
+            dst[c + pos3(p, x, y, z + 1)] = hubble ? v + ic->phi0[0] * p->H0 : v;
+          }
     }
   orc_exchange(p, Phi); /* Communication::exchange moves Phi only (comm.cpp:63-78) */
   free(Are); free(Aim); free(Ere); free(Eim); free(X);
@@ -742,37 +857,41 @@ void orc_spectrum_columns(const orc_params *p, const double *F, const double *K,
 /* ------------------------------------------------------------------ islands */
 /* Per-site energy density, the summand of the reference's Energy
  * (fieldanalysis.cpp:437-471,571-579): 1/2 sum_a pi_a^2 + 1/2 sum_a grad_a
- * + V.  Its lattice mean is the reference's Energy. */
-double orc_site_energy(const orc_params *p, const double *Phi, const double *Pi, long Kooo0, int x, int y, int z) {
+ * + V, plus the expanding box's sum_a (phi_a^2 (H0/sf)^2 / 2 - phi_a pi_a
+ * H0/sf) (:626-629).  Its lattice mean is the reference's Energy. */
+double orc_site_energy_at(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, long Kooo0,
+                          int x, int y, int z) {
   const int N = p->N, Nc = p->Nc;
-  const double mass = p->m_sqr;
+  const double sf = clock_sf(p, c);
   long Kooo = Kooo0;
   long Kuoo = pos3(p, mod(x + 1, N), y, z), Kouo = pos3(p, x, mod(y + 1, N), z), Koou = pos3(p, x, y, z + 1);
-  double kin = 0., grad = 0., inter = 0., locPhiSqr = 0., locPhi = 0.;
+  double kin = 0., grad = 0., inter = 0., locPhiSqr = 0., locPhi = 0., phi2 = 0., phipi = 0.;
   for (int a = 0; a < Nc; a++) {
     kin += sqr(Pi[Kooo]);
     locPhiSqr += sqr(Phi[Kooo]);
     locPhi += Phi[Kooo];
+    phi2 += sqr(Phi[Kooo]);
+    phipi += Phi[Kooo] * Pi[Kooo];
     grad += (sqr(Phi[Kuoo] - Phi[Kooo]) / sqr(p->a) + sqr(Phi[Kouo] - Phi[Kooo]) / sqr(p->a) +
              sqr(Phi[Koou] - Phi[Kooo]) / sqr(p->a));
-    if (p->theory == 0 || p->theory == 4)
-      inter += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
-    else if (p->theory == 3)
-      inter += 0.5 * p->m_mono_sqr * sqr(Phi[Kooo]);
-    else if (p->theory == 1 && a == 0)
-      inter += (p->h * Phi[Kooo] + (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]));
-    else if (p->theory == 1)
-      inter += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]);
+    inter += component_interaction(p, Phi[Kooo], a, sf);
     Kooo++; Kuoo++; Kouo++; Koou++;
   }
-  inter += site_interaction(p, locPhiSqr, locPhi);
-  return 0.5 * kin + 0.5 * grad + inter;
+  inter += site_interaction(p, locPhiSqr, locPhi, sf);
+  double e = 0.5 * kin + 0.5 * grad + inter;
+  if (p->expansion) e += (0.5 * phi2 * sqr(p->H0 / sf) - phipi * p->H0 / sf);
+  return e;
+}
+
+double orc_site_energy(const orc_params *p, const double *Phi, const double *Pi, long K, int x, int y, int z) {
+  return orc_site_energy_at(p, NULL, Phi, Pi, K, x, y, z);
 }
 
 /* Mask: mode 0 is is_island() (islands.cpp:76): the first component at the
  * site satisfies Phi^2/2 + Pi^2/2 > thres^2/2; mode 1 is the energy-density
  * mask rho(x) > thres. */
-static unsigned char *make_mask(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode) {
+static unsigned char *make_mask(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi,
+                                double thres, int mode) {
   const int N = p->N;
   const long n = field_len(p);
   unsigned char *m = (unsigned char *)calloc((size_t)n, 1);
@@ -783,15 +902,49 @@ static unsigned char *make_mask(const orc_params *p, const double *Phi, const do
         if (mode == 0)
           m[K] = (Phi[K] * Phi[K] * 0.5 + Pi[K] * Pi[K] * 0.5 > thres * thres * 0.5);
         else
-          m[K] = orc_site_energy(p, Phi, Pi, K, x, y, z) > thres;
+          m[K] = orc_site_energy_at(p, c, Phi, Pi, K, x, y, z) > thres;
       }
   return m;
 }
 
-/* One BFS (islands.cpp:90-279, theory 0/1, static box) from seed P with label
- * `flag`.  z is open (1..N) as on one rank (:224-236) unless zper. */
+/* The expanding box's island energy terms (islands.cpp:136-196): the
+ * kinetic term with its H0/sf parts, and the potential added in the
+ * reference's separate steps. */
+static void bfs_expanded(const orc_params *p, double phi, double pi, double sf, double *cKinEn, double *cPotEn) {
+  const int Nc = p->Nc;
+  const double mass = p->m_sqr, H0 = p->H0;
+  *cKinEn += (0.5 * sqr(pi) + 0.5 * sqr(H0 / sf) * sqr(phi) - phi * pi * H0 / sf);
+  switch (p->theory) {
+    case 0:
+      *cPotEn += (double)(p->mass_mode) * 0.5 * mass * sf * sf * sqr(phi);
+      *cPotEn += (double)(p->lambda_mode) * (sqr(sqr(phi)) / (24.0 * Nc)) +
+                 (sqr(sqr(phi)) * sqr(phi) / (720.0 * Nc * Nc * p->kappa * p->kappa * sf * sf));
+      break;
+    case 1:
+      *cPotEn += (double)(p->mass_mode) * 0.5 * mass * sf * sf * sqr(phi);
+      *cPotEn += (p->h * phi * sf * sf * sf + (double)(p->lambda_mode) * (sqr(sqr(phi)) / (24.0 * Nc)));
+      break;
+    case 2:
+      *cPotEn += sqr(sf * sf * mass) * (1. - cos(phi / (sf * sqrt(mass))));
+      break;
+    case 3:
+      *cPotEn += (0.5 * p->m_mono_sqr * (sqr(sf)) * sqr(phi));
+      *cPotEn += sqr(sf * sf * mass) * (1. - cos(phi / (sf * sqrt(mass))));
+      break;
+    case 4:
+      *cPotEn += (double)(p->mass_mode) * 0.5 * mass * sf * sf * sqr(phi);
+      *cPotEn += (((-p->g * sf * sqr(phi) * phi) / (6.0)) + (double)(p->lambda_mode) * (sqr(sqr(phi)) / (24.0 * Nc)));
+      break;
+    default:
+      *cPotEn += sqr(sf * sf * mass) * 0.5 / p->p_mono * (pow((1. + phi * phi / mass / sf / sf), p->p_mono) - 1.);
+  }
+}
+
+/* One BFS (islands.cpp:90-279) from seed P with label `flag`; sf > 0 selects
+ * the expanding box's energies.  z is open (1..N) as on one rank (:224-236)
+ * unless zper. */
 static void bfs(const orc_params *p, const double *Phi, const double *Pi, const unsigned char *mask, int *b,
-                long *queue, long P, int flag, int zper, orc_island *B) {
+                long *queue, long P, int flag, int zper, orc_island *B, double sf) {
   const int N = p->N, Nc = p->Nc;
   const double mass = p->m_sqr;
   int NN = 0;
@@ -814,8 +967,13 @@ static void bfs(const orc_params *p, const double *Phi, const double *Pi, const 
     long Kood = pos3(p, x, y, z - 1);
     NN++;
     cGradEn += 0.5 * (sqr(Phi[Kuoo] - Phi[Kooo]) + sqr(Phi[Kouo] - Phi[Kooo]) + sqr(Phi[Koou] - Phi[Kooo])) / sqr(p->a);
-    cKinEn += 0.5 * sqr(Pi[Kooo]);
-    if (p->theory == 0)
+    if (sf > 0)
+      bfs_expanded(p, Phi[Kooo], Pi[Kooo], sf, &cKinEn, &cPotEn);
+    else
+      cKinEn += 0.5 * sqr(Pi[Kooo]);
+    if (sf > 0)
+      ; /* potential added by bfs_expanded */
+    else if (p->theory == 0)
       cPotEn += (double)(p->mass_mode) * 0.5 * mass * sqr(Phi[Kooo]) +
                 (double)(p->lambda_mode) * (sqr(sqr(Phi[Kooo])) / (24.0 * Nc)) +
                 (sqr(sqr(Phi[Kooo])) * sqr(Phi[Kooo]) / (720.0 * Nc * Nc * p->kappa * p->kappa));
@@ -866,11 +1024,12 @@ static void bfs(const orc_params *p, const double *Phi, const double *Pi, const 
  * Island i gets label i, so labels follow each island's smallest site index.
  * labels (may be NULL) uses the reference layout; islands[] receives at most
  * max_islands records.  Returns the island count, or -1 on allocation failure. */
-int orc_islands(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode, int zper,
-                int *labels, orc_island *islands, int max_islands) {
+int orc_islands_at(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, double thres,
+                   int mode, int zper, int *labels, orc_island *islands, int max_islands) {
   const int N = p->N, Nc = p->Nc;
   const long n = field_len(p);
-  unsigned char *mask = make_mask(p, Phi, Pi, thres, mode);
+  const double sf = p->expansion ? clock_sf(p, c) : 0.0;
+  unsigned char *mask = make_mask(p, c, Phi, Pi, thres, mode);
   int *b = labels ? labels : (int *)malloc(sizeof(int) * (size_t)n);
   long *queue = (long *)malloc(sizeof(long) * (size_t)n);
   if (!mask || !b || !queue) return -1;
@@ -880,11 +1039,16 @@ int orc_islands(const orc_params *p, const double *Phi, const double *Pi, double
   for (long K = pos3(p, 0, 0, 1); K < (long)Nc * N * N * (N + 1); K++)
     if (mask[K] && b[K] == -1) {
       orc_island *B = count < max_islands ? &islands[count] : &scratch;
-      bfs(p, Phi, Pi, mask, b, queue, K, count, zper, B);
+      bfs(p, Phi, Pi, mask, b, queue, K, count, zper, B, sf);
       count++;
     }
   free(mask);
   free(queue);
   if (!labels) free(b);
   return count;
+}
+
+int orc_islands(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode, int zper,
+                int *labels, orc_island *islands, int max_islands) {
+  return orc_islands_at(p, NULL, Phi, Pi, thres, mode, zper, labels, islands, max_islands);
 }

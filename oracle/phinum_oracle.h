@@ -15,10 +15,10 @@ extern "C" {
 typedef struct orc_params {
   int N;           /* N_t = N_eta: cubic lattice edge */
   int Nc;          /* field components */
-  int theory;      /* 0: phi^4 + phi^6 (Kappa), 1: phi^4 + linear h */
+  int theory;      /* 0: phi^4 + phi^6 (Kappa), 1: phi^4 + linear h, 2-5 (parameters.cpp:122-170) */
   int mass_mode;   /* Mass_Mode */
   int lambda_mode; /* Lambda_Mode */
-  int pad_;
+  int expansion;   /* 0 static box, 1 expanding box (radiation era, H_0) */
   double a;        /* a_t = a_eta */
   double dt;       /* dtBaseTrans: dtau = dt * a */
   double T0;
@@ -28,12 +28,16 @@ typedef struct orc_params {
   double g;        /* g (theory 4) */
   double p_mono;   /* p_mono (theory 5) */
   double m_mono_sqr; /* M_mono_sqr (theory 3) */
+  double H0;       /* H_0 (expansion 1, parameters.cpp:177) */
 } orc_params;
 
 /* numeric:: and LocalLattice:: time keeping (dynamics.cpp:8-50). */
 typedef struct orc_clock {
   double tau, dtau, last_mom, last_field;
   int steps, pad_;
+  /* expanding box (dynamics.cpp:8-50): conformal time, scale factor and the
+   * conformal update stamps; tau and 1 for the static box */
+  double tau_c, sf, last_mom_c, last_field_c;
 } orc_clock;
 
 /* One SO row: CalculateVolumeAverages + CalculateExtrema outputs
@@ -84,6 +88,10 @@ int orc_spectrum_uniform(const orc_params *p, const double *Phi, const double *P
 void orc_spectrum_columns(const orc_params *p, const double *F, const double *K, const double *Q,
                           const int *counts, int nb, double *cols);
 double orc_site_energy(const orc_params *p, const double *Phi, const double *Pi, long K, int x, int y, int z);
+int orc_islands_at(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, double thres,
+                   int mode, int zper, int *labels, orc_island *islands, int max_islands);
+double orc_site_energy_at(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, long K,
+                          int x, int y, int z);
 int orc_islands(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode, int zper,
                 int *labels, orc_island *islands, int max_islands);
 

@@ -76,6 +76,21 @@ enum { REF_MAX_NC = 4, REF_AVG_LEN = 1 + 2 * REF_MAX_NC + 14 + 3 };
 int ref_precision() { return doubleprecision; }
 int ref_theory() { return theory; }
 
+/* H_0 of the expanding box (parameters.cpp:177); call before ref_init. */
+void ref_set_h0(double h0) { H_0 = (pseudo_double)h0; }
+
+/* Conformal time and scale factor (lattice.cpp:14-17); the static box gives
+ * tau and 1. */
+void ref_expansion_state(double *tau_c, double *a) {
+#if (expansion == 1)
+  *tau_c = (double)LocalLattice::tau_conformal;
+  *a = (double)LocalLattice::scale_factor;
+#else
+  *tau_c = (double)LocalLattice::tau;
+  *a = 1.0;
+#endif
+}
+
 /* Couplings of theories 3-5 (M_mono_sqr, g, p_mono); call before ref_init. */
 void ref_set_extra(double gcub, double pmono, double mmono) {
   g = (pseudo_double)gcub;
@@ -173,7 +188,11 @@ static void record(double t, double *out) {
   out[i++] = (double)maxAbspos;
   out[i++] = 0.0;
   out[i++] = 0.0;
-  out[i++] = 0.0;
+#if (expansion == 1)
+  out[i++] = (double)scale_factor;  /* the SO row's scale-factor column (fieldanalysis.cpp:789-791) */
+#else
+  out[i++] = 1.0;
+#endif
 }
 
 int ref_avg_len() { return REF_AVG_LEN; }

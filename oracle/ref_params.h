@@ -54,7 +54,10 @@
 #define withBins 1
 #define LAMBDA_MODE 1
 #define withcharge 0
-#define expansion 0
+#ifndef PHN_REF_EXPANSION
+#define PHN_REF_EXPANSION 0
+#endif
+#define expansion PHN_REF_EXPANSION
 #define finebin 0
 #define withEnergyPS 0
 #define islanddetect 1
@@ -75,6 +78,8 @@ int Lambda_Mode = -1;
 pseudo_double Lambda = 1.;
 pseudo_double Kappa = 2.;
 pseudo_double h = 0.;
+/* expanding box (parameters.cpp:177): H_0 */
+pseudo_double H_0 = 0.0171156;
 /* theories 2-5 (parameters.cpp:122-170) */
 pseudo_double F_SSB = 1.;
 pseudo_double alpha = 0.;

@@ -2,6 +2,7 @@
 sources (oracle/_ref, built by oracle/build_ref.sh from the reference tree).
 
     sh oracle/build_ref.sh && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --cases e0_n12 n12_exp   # chosen cases only
 
 The initial-condition fixtures (tests/golden/ic/) hold the reference's own
 SetInitialConditions output (initialize 3) for chosen srand48 seeds: the
@@ -43,6 +44,7 @@ COS = dict(theory=2, mass_mode=1, lambda_mode=1, m_sqr=0.49, kappa=1.0, h=0.0)
 MONO = dict(theory=3, mass_mode=1, lambda_mode=1, m_sqr=9.0, kappa=1.0, h=0.0, m_mono_sqr=1.0)
 CUBIC = dict(theory=4, mass_mode=1, lambda_mode=1, m_sqr=1.0, kappa=1.0, h=0.0, g=2.0)
 POWER = dict(theory=5, mass_mode=1, lambda_mode=1, m_sqr=1.0, kappa=1.0, h=0.0, p_mono=-0.5)
+EXP = dict(expansion=1, H0=0.0171156)
 
 CASES = {
     # name: (params, seed, phi0, steps, tso, full arrays?, checkpoints)
@@ -57,6 +59,14 @@ CASES = {
     "t4_n8": (dict(N=8, Nc=1, **CUBIC), 9, 1.0, 100, 0.25, True, (1, 10, 100)),
     "t4_n16": (dict(N=16, Nc=1, **CUBIC), 10, 1.0, 300, 0.5, False, (1, 100, 300)),
     "t5_n8": (dict(N=8, Nc=1, **POWER), 11, 2.0, 100, 0.25, True, (1, 10, 100)),
+    # the radiation-era expanding box (expansion 1) at the reference's H_0
+    "e0_n12": (dict(N=12, Nc=1, **PHI6, **EXP), 31, SQRT6, 300, 0.5, True, (1, 100, 300)),
+    "e0_n8_nc2": (dict(N=8, Nc=2, **PHI6, **EXP), 32, SQRT6, 100, 0.25, True, (1, 100)),
+    "e1_n8": (dict(N=8, Nc=1, **TDW, **EXP), 33, -SQRT6, 200, 0.25, True, (1, 200)),
+    "e2_n8": (dict(N=8, Nc=1, **COS, **EXP), 34, 1.5, 100, 0.25, True, (1, 100)),
+    "e3_n8": (dict(N=8, Nc=1, **MONO, **EXP), 35, 2.0, 100, 0.25, True, (1, 100)),
+    "e4_n16": (dict(N=16, Nc=1, **CUBIC, **EXP, T0=2.0), 36, 1.0, 400, 0.5, False, (1, 100, 400)),
+    "e5_n8": (dict(N=8, Nc=1, **POWER, **EXP), 37, 2.0, 100, 0.25, True, (1, 100)),
 }
 
 
@@ -67,6 +77,10 @@ IC_CASES = {
                                                  phi0=(1.0, -0.5), pi0=(0.2, 0.1))),
     "n16_tdw": (dict(N=16, Nc=1, **TDW), dict(seed=20260, noise=3.0, scale2=6.2832, phi0=(-SQRT6, 0.0))),
     "n16_noise": (dict(N=16, Nc=1, **PHI6), dict(seed=-5, justnoise=1, scale2=0.0, noise=1.0)),
+    "n12_exp": (dict(N=12, Nc=1, **PHI6, **EXP), dict(seed=41, noise=0.3, QS=3.0, scale2=5.0, phi0=(1.5, 0.0),
+                                                      pi0=(0.1, 0.0))),
+    "n16_exp_nc2": (dict(N=16, Nc=2, **PHI6, **EXP, T0=3.0),
+                    dict(seed=42, noise=0.5, QS=4.0, scale2=6.0, phi0=(2.0, -0.5), pi0=(0.0, 0.3))),
 }
 
 
@@ -186,7 +200,7 @@ def run_filter_case(name: str) -> None:
 def run_ic_case(name: str) -> None:
     from oracle import oracle as O
     pd, ic = IC_CASES[name]
-    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    p = O.Params(**{"a": 0.25, "dt": 0.08, "T0": 0.0, **pd})
     R = O.Reference(p)
     phi, pi = R.initial_conditions(**ic)
     os.makedirs(os.path.join(HERE, "ic"), exist_ok=True)
@@ -209,7 +223,7 @@ def run_case(name: str) -> None:
     from oracle import oracle as O
     import inputs
     pd, seed, phi0, steps, tso, full, checkpoints = CASES[name]
-    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    p = O.Params(**{"a": 0.25, "dt": 0.08, "T0": 0.0, **pd})
     phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, seed, phi0=phi0)
     R = O.Reference(p)
     out = {"params": json.dumps(pd), "seed": seed, "phi0": phi0, "steps": steps, "tso": tso,
@@ -286,6 +300,12 @@ def main() -> None:
         return
     if not O.ref_available(0) or not O.ref_available(1):
         sys.exit("reference pin not built: run oracle/build_ref.sh first")
+    only = sys.argv[2:] if len(sys.argv) > 2 and sys.argv[1] == "--cases" else None
+    if only:
+        for name in only:
+            flag = "--ic-case" if name in IC_CASES else "--case"
+            subprocess.run([sys.executable, os.path.abspath(__file__), flag, name], check=True)
+        return
     for name in CASES:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--case", name], check=True)
     for name in IC_CASES:

@@ -33,7 +33,7 @@ def test_fixtures_present():
 @pytest.mark.parametrize("name", IC_FIXTURES)
 def test_oracle_initial_conditions_match_reference(name):
     d = load(name)
-    p = O.Params(a=0.25, dt=0.08, T0=0.0, **d["params"])
+    p = O.Params(**{"a": 0.25, "dt": 0.08, "T0": 0.0, **d["params"]})
     phi, pi = O.initial_conditions(p, **d["ic"])
     sl = slice(p.Nc * p.N * p.N, -p.Nc * p.N * p.N)
     assert np.abs(phi - d["phi"]).max() <= 1e-13 * np.abs(d["phi"]).max()

@@ -15,6 +15,7 @@ from oracle import oracle as O
 
 CASES = fixtures.names()
 ROW_COLS = slice(0, 23)  # t .. max_abs_pos: everything the reference computes
+SF_COL = 25               # the expanding box's scale factor
 
 
 def params(d):
@@ -40,6 +41,8 @@ def test_oracle_matches_reference_fixture(name):
     rows, clk = O.run_loop(p, phi, pi, d["steps"], d["tso"], nthreads=nthreads)
     assert rows.shape[0] == d["rows"].shape[0]
     assert np.array_equal(rows[:, ROW_COLS], d["rows"][:, ROW_COLS])
+    if p.expansion:
+        assert np.array_equal(rows[:, SF_COL], d["rows"][:, SF_COL]) and rows[-1, SF_COL] > 1.0
 
     # fields at each checkpoint: bit-exact
     phi, pi = O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc)
@@ -53,6 +56,8 @@ def test_oracle_matches_reference_fixture(name):
         assert fixtures.digest(pi_c) == str(d[f"pi_sha_{c}"]), f"pi after {c} steps"
         avg = O.averages(p, phi, pi, clock)
         assert np.array_equal(avg[ROW_COLS], d[f"avg_{c}"][ROW_COLS])
+        if p.expansion:
+            assert avg[SF_COL] == d[f"avg_{c}"][SF_COL]
     assert clock.tau == d["tau_end"] and clock.steps == d["steps_end"]
 
     # spectrum of the final state
@@ -65,7 +70,7 @@ def test_oracle_matches_reference_fixture(name):
 
     # islands of the final state: labels and per-island statistics bit-exact
     if p.Nc == 1:
-        labels, recs = O.islands(p, phi, pi, float(d["island_thres"]))
+        labels, recs = O.islands(p, phi, pi, float(d["island_thres"]), clock=clock)
         lab = O.from_ref_layout(labels.astype(np.float64), p.N, 1)[0].astype(np.int32)
         assert fixtures.label_digest(lab) == str(d["island_labels_sha"])
         st = d["island_stats"]
@@ -98,11 +103,13 @@ def test_spectrum_counts_cover_every_mode():
         assert nb == {8: 7, 12: 9, 32: 20, 64: 37}[N]
 
 
-@pytest.mark.skipif(not all(O.ref_available(t) for t in range(6)),
+@pytest.mark.skipif(not all(O.ref_available(t, "f64", e) for t in range(6) for e in (0, 1)),
                     reason="reference pin not built here (oracle/build_ref.sh)")
-@pytest.mark.parametrize("theory,N,Nc", [(0, 6, 1), (1, 10, 1), (0, 8, 3), (2, 6, 1), (3, 6, 1), (4, 8, 1),
-                                         (5, 6, 1)])
-def test_oracle_matches_reference_live(theory, N, Nc, tmp_path):
+@pytest.mark.parametrize("theory,N,Nc,expansion", [(0, 6, 1, 0), (1, 10, 1, 0), (0, 8, 3, 0), (2, 6, 1, 0),
+                                                   (3, 6, 1, 0), (4, 8, 1, 0), (5, 6, 1, 0), (0, 6, 2, 1),
+                                                   (1, 8, 1, 1), (2, 6, 1, 1), (3, 6, 1, 1), (4, 6, 1, 1),
+                                                   (5, 6, 1, 1)])
+def test_oracle_matches_reference_live(theory, N, Nc, expansion, tmp_path):
     """Runs the reference pin in a child process on fresh random inputs."""
     import subprocess
     import sys
@@ -116,7 +123,7 @@ def test_oracle_matches_reference_live(theory, N, Nc, tmp_path):
               1: dict(theory=1, mass_mode=-1, lambda_mode=1, h=0.3),
               2: dict(theory=2, m_sqr=0.49), 3: dict(theory=3, m_sqr=9.0, m_mono_sqr=1.0),
               4: dict(theory=4, mass_mode=1, lambda_mode=1, g=2.0), 5: dict(theory=5, p_mono=-0.5)}}[{theory}]
-        p = O.Params(N={N}, Nc={Nc}, **kw)
+        p = O.Params(N={N}, Nc={Nc}, expansion={expansion}, H0=0.05, T0=0.5 * {expansion}, **kw)
         rng = np.random.default_rng({N})
         phi = O.to_ref_layout(2.0 + 0.5 * rng.standard_normal(({Nc}, {N}, {N}, {N})), {Nc})
         pi = O.to_ref_layout(0.5 * rng.standard_normal(({Nc}, {N}, {N}, {N})), {Nc})
@@ -126,10 +133,16 @@ def test_oracle_matches_reference_live(theory, N, Nc, tmp_path):
         rows, clk = O.run_loop(p, phi, pi, 37, 0.1)
         assert np.array_equal(rr[:, :23], rows[:, :23])
         assert np.array_equal(rf[0], phi) and np.array_equal(rf[1], pi)
+        assert R.expansion_state() == (clk.tau_c, clk.sf)
+        if {expansion}:
+            assert np.array_equal(rr[:, 25], rows[:, 25])
         if {Nc} == 1:
             thr = float(np.quantile(np.sqrt(phi**2 + pi**2), 0.9))
-            l1, s1 = R.islands(thr); l2, s2 = O.islands(p, phi, pi, thr)
+            l1, s1 = R.islands(thr); l2, s2 = O.islands(p, phi, pi, thr, clock=clk)
             assert np.array_equal(l1, l2)
+            cols = [O.ISL[k] for k in ("index", "volume", "pot_en", "kin_en", "grad_en", "av_phi", "peak_pos",
+                                       "peak_value")]
+            assert np.array_equal(s1, s2[:, cols])
         print("ok")
     """)
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
