@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PHN_ABI_VERSION 2
+#define PHN_ABI_VERSION 3
 #define PHN_MAX_NC 4
 
 enum {
@@ -75,6 +75,12 @@ typedef struct phn_params {
   double g;        /* g, theory 4 */
   double p_mono;   /* p_mono, theory 5 */
   double m_mono_sqr; /* M_mono_sqr, theory 3 */
+  int expanding;   /* the reference's `expansion` switch: 0 static box, 1 radiation-era
+                      expanding box, a = sqrt(1 + 2 H_0 tau), kick and drift in conformal
+                      time (dynamics.cpp:36-50, :88-163, :185-212).  Named apart because
+                      the reference #defines `expansion` */
+  int reserved_;   /* zero */
+  double H0;       /* H_0 (parameters.cpp:177), expansion 1 */
 } phn_params;
 
 /* One SO row: the outputs of CalculateVolumeAverages + CalculateExtrema
@@ -88,7 +94,8 @@ typedef struct phn_averages {
   double min_pos, max_pos, max_abs_pos;   /* minpos, maxpos, maxAbspos */
   double gradient;                        /* GradPhiSqr / vol */
   double nonfinite;                       /* number of non-finite phi/pi values seen */
-  double reserved;
+  double scale_factor;                    /* LocalLattice::scale_factor, the expanding box's SO
+                                             time column (fieldanalysis.cpp:789-791); 1 when static */
 } phn_averages;
 
 /* One island (struct island, islands.cpp:13-28).  Islands are numbered by
@@ -126,6 +133,9 @@ int phn_reset(phn_handle *h);
 int phn_evolve(phn_handle *h, int nsteps);
 /* LocalLattice::tau and numeric::total_stepcount. */
 int phn_time(const phn_handle *h, double *tau, int *total_stepcount);
+/* LocalLattice::tau_conformal and scale_factor (lattice.cpp:14-17) of the
+ * expanding box; tau and 1 for the static box. */
+int phn_conformal_time(const phn_handle *h, double *tau_conformal, double *scale_factor);
 
 /* CalculateExtrema() + CalculateVolumeAverages() (fieldanalysis.cpp:319-699)
  * on the current state. */
@@ -379,7 +389,9 @@ int phn_adjoint_info(const phn_adjoint *a, double *J, double *forward_ms, double
  * get PHN_ERR_INVALID.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress); make that first call before any
  * stream capture.  All calls share the array: calls that overlap on the GPU
- * race, so serialise them.  Returns after the result is on the host. */
+ * race, so serialise them.  Returns after the result is on the host.  The
+ * expanding box's averages are those at tau = T0 (scale factor
+ * sqrt(1 + 2 H_0 T0)). */
 int phn_volume_averages_noalloc(const phn_params *params, const void *d_phi, const void *d_pi, void *stream,
                                 phn_averages *out);
 

@@ -25,13 +25,14 @@ _D, _I = ctypes.c_double, ctypes.c_int
 _PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
 
 
-ABI_VERSION = 2  # PHN_ABI_VERSION of include/phinum_gpu.h
+ABI_VERSION = 3  # PHN_ABI_VERSION of include/phinum_gpu.h
 
 
 class PhnParams(ctypes.Structure):
     _fields_ = [("N", _I), ("Nc", _I), ("potential", _I), ("mass_mode", _I), ("lambda_mode", _I),
                 ("precision", _I), ("a", _D), ("dt", _D), ("T0", _D), ("m_sqr", _D), ("kappa", _D),
-                ("h", _D), ("g", _D), ("p_mono", _D), ("m_mono_sqr", _D)]
+                ("h", _D), ("g", _D), ("p_mono", _D), ("m_mono_sqr", _D), ("expanding", _I),
+                ("reserved_", _I), ("H0", _D)]
 
 
 class PhnIcParams(ctypes.Structure):
@@ -49,7 +50,7 @@ class PhnAverages(ctypes.Structure):
                 ("phipi", _D), ("phi4", _D), ("phi6", _D), ("energy", _D), ("interaction", _D),
                 ("charge", _D), ("min_phi", _D), ("max_phi", _D), ("max_abs_phi", _D), ("min_pos", _D),
                 ("max_pos", _D), ("max_abs_pos", _D), ("gradient", _D), ("nonfinite", _D),
-                ("reserved", _D)]
+                ("scale_factor", _D)]
 
 
 AVG_LEN = ctypes.sizeof(PhnAverages) // 8
@@ -77,6 +78,7 @@ _SIGS = {
     "phn_reset": (_I, [ctypes.c_void_p]),
     "phn_evolve": (_I, [ctypes.c_void_p, _I]),
     "phn_time": (_I, [ctypes.c_void_p, _PD, _PI]),
+    "phn_conformal_time": (_I, [ctypes.c_void_p, _PD, _PD]),
     "phn_volume_averages": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnAverages)]),
     "phn_false_vacuum_decayed": (_I, [ctypes.POINTER(PhnAverages), _I, _PI]),
     "phn_run_loop": (_I, [ctypes.c_void_p, _I, _D, ctypes.POINTER(PhnAverages), _I, _PI]),

@@ -20,9 +20,10 @@
 //
 // The device holds the authoritative fields between calls; phn_gpu::to_host()
 // brings them back into LocalLattice::Phi/Pi for any host code that reads
-// them directly (SaveConfig, visualisation).  Theories 0 and 1, static box
-// (expansion 0), FP64 by default (bit-identical to the CPU build) or FP32 with
-// PHN_PRECISION=1 in the environment.
+// them directly (SaveConfig, visualisation).  Theories 0-5, static or
+// expanding box (expansion 0 or 1), FP64 by default (bit-identical to the CPU
+// build for theories 0, 1 and 4) or FP32 with PHN_PRECISION=1 in the
+// environment.
 #ifndef PHINUM_DYNAMICS_ADAPTER_CPP
 #define PHINUM_DYNAMICS_ADAPTER_CPP
 
@@ -56,6 +57,14 @@ static void mirror_clock() {
   numeric::Last_Momenta_update = tau;
   numeric::total_stepcount = steps;
   numeric::normal_stepcount = steps;
+#if (expansion == 1)
+  double tau_c = 0.0, sf = 1.0;
+  check(phn_conformal_time(handle, &tau_c, &sf), "phn_conformal_time");
+  LocalLattice::tau_conformal = tau_c;
+  LocalLattice::scale_factor = sf;
+  numeric::Last_Field_update_conformal = tau_c;
+  numeric::Last_Momenta_update_conformal = tau_c;
+#endif
 }
 
 // After LocalLattice::init, fix_tadpole and SetInitialConditions: creates the
@@ -94,6 +103,10 @@ inline void init() {
   p.a = a_t;
   p.dt = dtBaseTrans;
   p.T0 = T0;
+#if (expansion == 1)
+  p.expanding = 1;  // radiation-era box (dynamics.cpp:36-50)
+  p.H0 = H_0;
+#endif
   const char *prec = std::getenv("PHN_PRECISION");
   p.precision = prec ? std::atoi(prec) : PHN_FP64;
   if (handle) phn_destroy(handle);
@@ -168,12 +181,22 @@ inline void Print_AveragesExtrema() {
       SpatialObs.open(fname, fstream::app);
     }
     numeric::LastSOoutput = tau;
+#if (expansion == 1)
+    numeric::LastSOoutput_conformal = (sqrt(1. + 2. * H_0 * tau) - 1.) / H_0;
+#endif
   } else if (tau >= numeric::LastSOoutput + TSO) {
     numeric::LastSOoutput += TSO;
+#if (expansion == 1)
+    numeric::LastSOoutput_conformal = (sqrt(1. + 2. * H_0 * numeric::LastSOoutput) - 1.) / H_0;
+#endif
   }
   CalculateVolumeAverages();
   if (ID == 0) {
+#if (expansion == 1)
+    SpatialObs << scale_factor << ' ';  // the expanding box's time column (fieldanalysis.cpp:789-791)
+#else
     SpatialObs << numeric::LastSOoutput << ' ';
+#endif
     for (int i = 0; i < Nc; i++) SpatialObs << avgphi[i] << ' ' << avgpi[i] << ' ';
     SpatialObs << avgphi2 << ' ' << avgpi2 << ' ' << avgphipi << ' ' << avgphi4 << ' ' << avgphi6 << ' ';
     SpatialObs << avgEnergy << ' ' << avgInteraction << ' ' << avgCharge << ' ';
@@ -207,10 +230,17 @@ inline void Calculate_CorrelationFunctions() {
 inline void Print_fp() {
   using namespace LocalLattice;
   if (numeric::total_stepcount > 0 && tau < numeric::LastMOoutput + TMO) return;
-  if (numeric::total_stepcount == 0)
+  if (numeric::total_stepcount == 0) {
     numeric::LastMOoutput = tau;
-  else if (tau >= numeric::LastMOoutput + TMO)
+#if (expansion == 1)
+    numeric::LastMOoutput_conformal = (sqrt(1. + 2. * H_0 * tau) - 1.) / H_0;
+#endif
+  } else if (tau >= numeric::LastMOoutput + TMO) {
     numeric::LastMOoutput += TMO;
+#if (expansion == 1)
+    numeric::LastMOoutput_conformal = (sqrt(1. + 2. * H_0 * numeric::LastMOoutput) - 1.) / H_0;
+#endif
+  }
   Calculate_CorrelationFunctions();
   if (ID == 0) {
     using namespace MomentumSpace;

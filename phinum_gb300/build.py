@@ -53,8 +53,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
-    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
-                    "--expt-relaxed-constexpr"]
+    # host code: no FP contraction, so the FP64 clock (tau, conformal time,
+    # scale factor) rounds as the reference's does on every host (aarch64 GCC
+    # would otherwise fuse 1 + 2 H0 tau into one FMA)
+    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                    "-I", os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]
     if verbose:
         flags += ["-Xptxas", "-v"]
 

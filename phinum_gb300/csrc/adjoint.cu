@@ -516,8 +516,8 @@ int phn_adjoint_create(const phn_params *params, int nsteps, int every, double w
   *out = nullptr;
   int r = validate_params(params);
   if (r) return r;
-  if (params->Nc != 1 || params->precision == PHN_FP32_KAHAN || params->potential > 1)
-    return set_error(PHN_ERR_UNSUPPORTED, "adjoint: theories 0 and 1, Nc = 1, FP32 or FP64");
+  if (params->Nc != 1 || params->precision == PHN_FP32_KAHAN || params->potential > 1 || params->expanding)
+    return set_error(PHN_ERR_UNSUPPORTED, "adjoint: theories 0 and 1, Nc = 1, FP32 or FP64, static box");
   phn_adjoint *a = new phn_adjoint();
   a->p = *params;
   a->k = make_consts(params);

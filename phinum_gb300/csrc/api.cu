@@ -49,6 +49,11 @@ int phn::validate_params(const phn_params *p) {
   if (!(p->a > 0.0) || !isfinite(p->a)) return set_error(PHN_ERR_INVALID, "a must be positive");
   if (!isfinite(p->dt)) return set_error(PHN_ERR_INVALID, "dt must be finite");
   if (p->potential == 0 && !(p->kappa != 0.0)) return set_error(PHN_ERR_INVALID, "Kappa must be non-zero");
+  if (p->expanding != 0 && p->expanding != 1) return set_error(PHN_ERR_INVALID, "expansion %d", p->expanding);
+  if (p->expanding && !(p->H0 > 0.0 && isfinite(p->H0)))
+    return set_error(PHN_ERR_INVALID, "the expanding box needs H_0 > 0");
+  if (p->expanding && !(1. + 2. * p->H0 * p->T0 > 0.0))
+    return set_error(PHN_ERR_INVALID, "1 + 2 H_0 T0 must be positive");
   return PHN_OK;
 }
 
@@ -105,6 +110,49 @@ Consts phn::make_consts(const phn_params *p) {
   k.mono_half_f = (float)(0.5 * p->m_mono_sqr);
   k.g6_f = (float)(p->g / 6.0);
   k.t5c_f = (float)k.t5c;
+  k.expansion = p->expanding;
+  k.H0 = p->H0;
+  k.sf = 1.0;
+  k.sf_sqrtm = k.sqrt_m;
+  k.msq_sf2 = k.msq;
+  return k;
+}
+
+// The couplings the expanding box multiplies by powers of the scale factor
+// (dynamics.cpp:88-163, fieldanalysis.cpp:461-615, islands.cpp:136-196),
+// each in the reference's left-to-right order.
+Consts phn::at_scale_factor(const Consts &k0, double sf) {
+  Consts k = k0;
+  k.sf = sf;
+  k.mmM = k0.mmM * sf * sf;          // Mass_Mode * BareM_sqr*scale_factor*scale_factor
+  k.h = k0.h * sf * sf * sf;         // h*scale_factor*scale_factor*scale_factor
+  k.m3 = k0.m3 * sf * sf * sf;       // BareM_sqr*sqrt(BareM_sqr)*scale_factor^3
+  k.mmono = k0.mmono * sf * sf;      // BareM_mono_sqr * scale_factor*scale_factor
+  k.g = k0.g * sf;                   // g*scale_factor
+  k.sf_sqrtm = sf * k0.sqrt_m;       // scale_factor*sqrt(BareM_sqr)
+  k.msq_sf2 = k0.msq * sf * sf;      // BareM_sqr * scale_factor * scale_factor
+  // energy terms
+  k.mm_half_M = k0.mm_half_M * sf * sf;
+  k.c720 = k0.c720 * sf * sf;
+  const double m2 = sf * sf * k0.msq;  // sqr(scale_factor*scale_factor*BareM_sqr)
+  k.msq2 = m2 * m2;
+  k.t5c = k0.theory == 5 ? k.msq2 * 0.5 / k0.p_mono : 0.0;
+  // FP32 forms
+  k.mmM_f = (float)k.mmM;
+  k.c6_f = k0.theory == 0 ? (float)(1.0 / (k0.kappa * k0.kappa * k0.c120 * sf * sf)) : 0.f;
+  k.h_f = (float)k.h;
+  k.mmh_f = (float)k.mm_half_M;
+  k.e6_f = k0.theory == 0 ? (float)(1.0 / k.c720) : 0.f;
+  k.m3_f = (float)k.m3;
+  k.inv_sqrtm_f = k0.msq > 0 ? (float)(1.0 / k.sf_sqrtm) : 0.f;
+  k.inv_m_f = k0.msq > 0 ? (float)(1.0 / k.msq_sf2) : 0.f;
+  k.mmono_f = (float)k.mmono;
+  k.ghalf_f = (float)(k.g / 2.);
+  k.msq_f = (float)k.msq_sf2;
+  k.msq2_f = (float)k.msq2;
+  k.mono_half_f = (float)(0.5 * k.mmono);
+  k.g6_f = (float)(k.g / 6.0);
+  k.t5c_f = (float)k.t5c;
   return k;
 }
 
@@ -145,12 +193,27 @@ int phn_device_count(int *count) {
   return PHN_OK;
 }
 
+// tau_conformal and scale_factor at cosmic time tau (dynamics.cpp:39-40, :204-205).
+static void conformal(phn_handle *h) {
+  const double H0 = h->p.H0;
+  h->tau_c = (sqrt(1. + 2. * H0 * h->tau) - 1.) / H0;
+  h->sf = sqrt(1. + 2. * H0 * h->tau);
+}
+
 int phn_reset(phn_handle *h) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
   h->tau = h->p.T0;
   h->dtau = h->p.dt * h->p.a;
   h->last_field = h->tau;
   h->last_mom = h->tau;
+  if (h->p.expanding) {
+    conformal(h);
+  } else {
+    h->tau_c = h->tau;
+    h->sf = 1.0;
+  }
+  h->last_mom_c = h->tau_c;
+  h->last_field_c = h->tau_c;
   h->steps = 0;
   return PHN_OK;
 }
@@ -313,40 +376,81 @@ int phn_time(const phn_handle *h, double *tau, int *total_stepcount) {
   return PHN_OK;
 }
 
-// One evolve(): host clock as dynamics.cpp:200-236, one fused kernel.
+int phn_conformal_time(const phn_handle *h, double *tau_conformal, double *scale_factor) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (tau_conformal) *tau_conformal = h->tau_c;
+  if (scale_factor) *scale_factor = h->sf;
+  return PHN_OK;
+}
+
+static int step_once(phn_handle *h, int mode);
+
+// One evolve() of the expanding box (dynamics.cpp:196-213): the kick at
+// tau + dtau/2 with that time's scale factor, both factors in conformal time.
+// An observation reads the state before the step with the scale factor it
+// has, so an observed step is an observation launch and a step launch.
+static int step_expanding(phn_handle *h, int mode) {
+  if (mode == MODE_STEP_OBS) {
+    int r = step_once(h, MODE_OBS);
+    return r ? r : step_once(h, MODE_STEP);
+  }
+  return step_once(h, mode);
+}
+
+// One evolve(): host clock as dynamics.cpp:196-237, one fused kernel.
 static int step_once(phn_handle *h, int mode) {
+  if (h->p.expanding && mode == MODE_STEP_OBS) return step_expanding(h, mode);
   StepF s;
+  Consts kx;  // the expanding box's couplings at this launch's scale factor
+  const bool ex = h->p.expanding != 0;
   if (mode != MODE_OBS) {
     h->tau += 0.5 * h->dtau;
-    s.fk = h->tau - h->last_mom;
+    if (ex) {
+      conformal(h);
+      s.fk = h->tau_c - h->last_mom_c;
+      kx = at_scale_factor(h->k, h->sf);
+    } else {
+      s.fk = h->tau - h->last_mom;
+    }
     h->last_mom = h->tau;
+    h->last_mom_c = ex ? h->tau_c : h->tau;
     h->tau += 0.5 * h->dtau;
-    s.fd = h->tau - h->last_field;
+    if (ex) {
+      conformal(h);
+      s.fd = h->tau_c - h->last_field_c;
+    } else {
+      s.fd = h->tau - h->last_field;
+      h->tau_c = h->tau;
+    }
     h->last_field = h->tau;
+    h->last_field_c = h->tau_c;
   } else {
     s.fk = s.fd = 0.0;
+    if (ex) kx = at_scale_factor(h->k, h->sf);
+    h->obs_sf = h->sf;
   }
+  const Consts &k = ex ? kx : h->k;
   const int nxt = 1 - h->cur;
   cudaError_t e;
   switch (h->p.precision) {
     case PHN_FP64:
-      e = launch_step_f64(h->k, h->grid, mode, (const double *)h->phi[h->cur], (double *)h->phi[nxt],
+      e = launch_step_f64(k, h->grid, mode, (const double *)h->phi[h->cur], (double *)h->phi[nxt],
                           (double *)h->pi, s, h->partials, h->stream);
       if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
       break;
     case PHN_FP32:
       if (h->path == PHN_PATH_X4) {
         const bool obs = mode != MODE_STEP;
-        e = launch_step_f32_x4(h->k, obs ? x4_obs_variant(h->x4_variant) : h->x4_variant,
+        e = launch_step_f32_x4(k, obs ? x4_obs_variant(h->x4_variant) : h->x4_variant,
                                obs ? h->x4_obs_grid : h->x4_grid, mode, (const float *)h->phi[h->cur],
                                (float *)h->phi[nxt], (float *)h->pi, nullptr, nullptr, s, h->partials, h->stream);
         if (obs) h->obs_records = h->x4_obs_grid;
       } else if (h->path == PHN_PATH_TMA && mode != MODE_OBS) {
-        e = launch_step_f32_tma(h->k, h->tma_variant, h->tma_grid, mode == MODE_STEP_OBS, (const float *)h->phi[h->cur],
+        e = launch_step_f32_tma(k, h->tma_variant, h->tma_grid, mode == MODE_STEP_OBS, (const float *)h->phi[h->cur],
                                 (float *)h->phi[nxt], (float *)h->pi, s, h->partials, h->d_err, h->stream);
         if (mode == MODE_STEP_OBS) h->obs_records = h->tma_grid;
       } else {
-        e = launch_step_f32(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt],
+        e = launch_step_f32(k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt],
                             (float *)h->pi, s, h->partials, h->stream);
         if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
       }
@@ -354,12 +458,12 @@ static int step_once(phn_handle *h, int mode) {
     default:
       if (h->path == PHN_PATH_X4) {
         const bool obs = mode != MODE_STEP;
-        e = launch_step_f32_x4(h->k, obs ? x4_obs_variant(h->x4_variant) : h->x4_variant,
+        e = launch_step_f32_x4(k, obs ? x4_obs_variant(h->x4_variant) : h->x4_variant,
                                obs ? h->x4_obs_grid : h->x4_grid, mode, (const float *)h->phi[h->cur],
                                (float *)h->phi[nxt], (float *)h->pi, h->cphi, h->cpi, s, h->partials, h->stream);
         if (obs) h->obs_records = h->x4_obs_grid;
       } else {
-        e = launch_step_kahan(h->k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt], h->cphi,
+        e = launch_step_kahan(k, h->grid, mode, (const float *)h->phi[h->cur], (float *)h->phi[nxt], h->cphi,
                               h->cphi, (float *)h->pi, h->cpi, s, h->partials, h->stream);
         if (mode != MODE_STEP) h->obs_records = h->grid.nblocks;
       }
@@ -417,7 +521,8 @@ int phn_evolve(phn_handle *h, int nsteps) {
 }
 
 static int fetch_avg(phn_handle *h, phn_averages *dst_host_slot) {
-  CK(launch_finalize(h->k, h->partials, h->obs_records, h->d_avg, h->stream));
+  CK(launch_finalize(h->p.expanding ? at_scale_factor(h->k, h->obs_sf) : h->k, h->partials, h->obs_records,
+                     h->d_avg, h->stream));
   h->launches++;
   CK(cudaMemcpyAsync(dst_host_slot, h->d_avg, sizeof(phn_averages), cudaMemcpyDeviceToHost, h->stream));
   return PHN_OK;

@@ -444,8 +444,9 @@ int phn_ensemble_create(const phn_params *members, int n, phn_ensemble **out) {
     int r = validate_params(&members[m]);
     if (r) return r;
     const phn_params &q = members[m];
-    if (q.precision != PHN_FP32 || q.Nc != 1 || q.N % 32 != 0 || q.potential > 1)
-      return set_error(PHN_ERR_UNSUPPORTED, "member %d: ensembles take FP32, Nc = 1, N a multiple of 32, theory 0 or 1", m);
+    if (q.precision != PHN_FP32 || q.Nc != 1 || q.N % 32 != 0 || q.potential > 1 || q.expanding)
+      return set_error(PHN_ERR_UNSUPPORTED,
+                       "member %d: ensembles take FP32, Nc = 1, N a multiple of 32, theory 0 or 1, static box", m);
     if (q.a != members[0].a || q.dt != members[0].dt || q.T0 != members[0].T0)
       return set_error(PHN_ERR_INVALID, "member %d: members share a, dt and T0 (one clock)", m);
   }

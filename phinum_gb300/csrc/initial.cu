@@ -1,6 +1,10 @@
 // Initial conditions on the GPU: SetInitialConditions for `initialize 3`,
-// static box, no charge (initialconditions.cpp:45-723, clusterfft.cpp:55-182),
-// with the reference's own random stream.
+// static or expanding box, no charge (initialconditions.cpp:45-723,
+// clusterfft.cpp:55-182), with the reference's own random stream.  The
+// expanding box (:459-465, :504-510, :581-583, :656-658) seeds the
+// scale-invariant occupation 2 pi^2 2.1e-9 phi0_0^2 omega_p / p^3 below QS,
+// uses Omega^2 = p^2 + (1 + 2 H_0 T0) M^2, E = H_0 A, and adds phi0_0 H_0 to
+// the first momentum component.
 //
 // The reference draws from drand48 (seeded by srand48, initialconditions.cpp:
 // 14-22) in mode order (pz, px, py <= N/2, component): per mode two phases
@@ -199,8 +203,11 @@ __global__ void ic_assign(const double2 *__restrict__ uv, long long npairs, long
 }
 
 struct IcConsts {
-  int N, Nc, justnoise;
+  int N, Nc, justnoise, expansion;
   double a, QS, scale2, amplitude, noise, m2_long, m2_trans;
+  double H0;
+  double a0sq;      // 1. + 2.*H_0*T0: the initial scale factor squared
+  double spectrum;  // 2.*acos(-1.)*acos(-1.)*2.1e-9*phi0_0*phi0_0
 };
 
 // Per-axis lattice momentum as initialconditions.cpp:88-113 writes it,
@@ -211,7 +218,7 @@ static double ic_p_host(int n, int N, double a) {
 }
 
 // One (mode, component): initialconditions.cpp:339-569 (initialize 3,
-// expansion 0, withcharge 0).  A and E are [a][pz][px][py] complex arrays.
+// withcharge 0).  A and E are [a][pz][px][py] complex arrays.
 __global__ void ic_modes(const IcConsts k, const double *__restrict__ ptab, const double2 *__restrict__ uv,
                          const long long *__restrict__ phase_pair,
                          const long long *__restrict__ acc_pair, long long nmodes, double2 *__restrict__ A,
@@ -242,18 +249,33 @@ __global__ void ic_modes(const IcConsts k, const double *__restrict__ ptab, cons
   double occ;
   const double root = __dsqrt_rn(pchisqr);
   const double plateau = k.scale2 == 0 ? k.noise : (root < k.scale2 ? k.noise : 0.0);
-  if (k.justnoise == 0)
-    occ = pchisqr < __dmul_rn(k.QS, k.QS) ? __dadd_rn(k.amplitude, k.noise) : plateau;
-  else
-    occ = plateau;
-  const double omega = __dsqrt_rn(__dadd_rn(psqr, a == 0 ? k.m2_long : k.m2_trans));
+  const double m2 = a == 0 ? k.m2_long : k.m2_trans;
+  double omega;
+  if (k.expansion) {  // initialconditions.cpp:459-465, :504-510
+    if (k.justnoise == 0 && psqr > 0. && psqr < __dmul_rn(k.QS, k.QS)) {
+      const double omegap = __dsqrt_rn(__dadd_rn(psqr, __dmul_rn(k.a0sq, k.m2_long)));
+      occ = __dmul_rn(__ddiv_rn(__ddiv_rn(k.spectrum, psqr), __dsqrt_rn(psqr)), omegap);
+    } else {
+      occ = plateau;
+    }
+    omega = __dsqrt_rn(__dadd_rn(psqr, __dmul_rn(k.a0sq, m2)));
+  } else {
+    if (k.justnoise == 0)
+      occ = pchisqr < __dmul_rn(k.QS, k.QS) ? __dadd_rn(k.amplitude, k.noise) : plateau;
+    else
+      occ = plateau;
+    omega = __dsqrt_rn(__dadd_rn(psqr, m2));
+  }
   // F = sqrt(occ) g (cos th, sin th); A = F1 / sqrt(Omega), E = F2 sqrt(Omega)
   const double amp1 = __dmul_rn(__dsqrt_rn(occ), gauss1), amp2 = __dmul_rn(__dsqrt_rn(occ), gauss2);
   double2 fa = make_double2(0.0, 0.0), fe = make_double2(0.0, 0.0);
   if (!(fabs(omega) < 1e-8)) {
     const double so = __dsqrt_rn(omega);
     fa = make_double2(__ddiv_rn(__dmul_rn(amp1, cos(phase1)), so), __ddiv_rn(__dmul_rn(amp1, sin(phase1)), so));
-    fe = make_double2(__dmul_rn(__dmul_rn(amp2, cos(phase2)), so), __dmul_rn(__dmul_rn(amp2, sin(phase2)), so));
+    if (k.expansion)  // EFieldP = AFieldP * H_0 (:581-583)
+      fe = make_double2(__dmul_rn(fa.x, k.H0), __dmul_rn(fa.y, k.H0));
+    else
+      fe = make_double2(__dmul_rn(__dmul_rn(amp2, cos(phase2)), so), __dmul_rn(__dmul_rn(amp2, sin(phase2)), so));
   }
   const size_t o = (size_t)a * N * N * M + ((size_t)pz * N + px) * M + py;
   A[o] = fa;
@@ -286,9 +308,11 @@ __global__ void ic_reality(double2 *__restrict__ F, int N, int Nc) {
   }
 }
 
-// out[z][y][x] = X[z][x][y] * scale + offset: 32 x 32 tiles through shared memory.
+// out[z][y][x] = (X[z][x][y] * scale + offset) + offset2: 32 x 32 tiles
+// through shared memory.
 template <typename T>
-__global__ void ic_store(const double *__restrict__ X, T *__restrict__ out, int N, double scale, double offset) {
+__global__ void ic_store(const double *__restrict__ X, T *__restrict__ out, int N, double scale, double offset,
+                         double offset2) {
   __shared__ double tile[32][33];
   const int z = blockIdx.z;
   const int x0 = blockIdx.y * 32, y0 = blockIdx.x * 32;
@@ -300,7 +324,7 @@ __global__ void ic_store(const double *__restrict__ X, T *__restrict__ out, int 
   __syncthreads();
   for (int j = threadIdx.y; j < 32; j += blockDim.y) {
     const int y = y0 + j, x = x0 + threadIdx.x;
-    if (x < N && y < N) out[plane + (size_t)y * N + x] = (T)(tile[threadIdx.x][j] * scale + offset);
+    if (x < N && y < N) out[plane + (size_t)y * N + x] = (T)((tile[threadIdx.x][j] * scale + offset) + offset2);
   }
 }
 
@@ -393,6 +417,10 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
     k.noise = ic->noise;
     k.m2_long = ic->m2_long;
     k.m2_trans = ic->m2_trans;
+    k.expansion = h->p.expanding;
+    k.H0 = h->p.H0;
+    k.a0sq = 1. + 2. * h->p.H0 * h->p.T0;
+    k.spectrum = 2. * acos(-1.) * acos(-1.) * 2.1e-9 * ic->phi0[0] * ic->phi0[0];
     ic_modes<<<(unsigned)((nmodes + 255) / 256), 256, 0, st>>>(k, ptab, uv, phase_pair, acc_pair, nmodes, A, E);
     ICK(cudaGetLastError());
     const long long nre = 2LL * N * N * Nc;
@@ -424,11 +452,13 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
           goto cleanup;
         }
         const double off = a < 2 ? (f == 0 ? phi0[a] : pi0[a]) : 0.0;
+        // the expanding box's Pi_0 += phi0_0 H_0 (initialconditions.cpp:657)
+        const double off2 = (h->p.expanding && f == 1 && a == 0) ? phi0[0] * h->p.H0 : 0.0;
         void *dst = f == 0 ? h->phi[h->cur] : h->pi;
         if (h->p.precision == PHN_FP64) {
-          ic_store<double><<<sg, sb, 0, st>>>(X, (double *)dst + (size_t)a * h->V, N, scale, off);
+          ic_store<double><<<sg, sb, 0, st>>>(X, (double *)dst + (size_t)a * h->V, N, scale, off, off2);
         } else {
-          ic_store<float><<<sg, sb, 0, st>>>(X, (float *)dst + (size_t)a * h->V, N, scale, off);
+          ic_store<float><<<sg, sb, 0, st>>>(X, (float *)dst + (size_t)a * h->V, N, scale, off, off2);
         }
         ICK(cudaGetLastError());
         h->launches++;

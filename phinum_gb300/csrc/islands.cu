@@ -49,23 +49,34 @@ __device__ __forceinline__ double val(const T *f, const float *comp, size_t i) {
 
 // Potential of one single-component site, theories 0-5: the BFS PotEn
 // summand (islands.cpp:137-196), which is also the Interaction summand of
-// CalculateVolumeAverages (fieldanalysis.cpp:456-617) for Nc = 1.
+// CalculateVolumeAverages (fieldanalysis.cpp:456-617) for Nc = 1.  The
+// expanding box's couplings come folded with the scale factor
+// (at_scale_factor); the cosine and power arguments carry it per site.
 __device__ __forceinline__ double site_potential(const Consts &k, double c, double c2) {
   const double l2 = c2 * c2;
+  const double cos_arg = k.expansion ? sqrt(c2) / k.sf_sqrtm : sqrt(c2 / k.msq);
   switch (k.theory) {
     case 0:
       return k.mm_half_M * c2 + k.lm * (l2 / k.c24) + (l2 * c2 / k.c720);
     case 1:
       return k.h * c + k.mm_half_M * c2 + k.lm * (l2 / k.c24);
     case 2:
-      return k.msq2 * (1. - cos(sqrt(c2 / k.msq)));
+      return k.msq2 * (1. - cos(cos_arg));
     case 3:
-      return 0.5 * k.mmono * c2 + k.msq2 * (1. - cos(sqrt(c2 / k.msq)));
+      return 0.5 * k.mmono * c2 + k.msq2 * (1. - cos(cos_arg));
     case 4:
       return k.mm_half_M * c2 - k.g * c2 * c / 6. + k.lm * (l2 / k.c24);
     default:
-      return k.t5c * (pow(1. + c2 / k.msq, k.p_mono) - 1.);
+      return k.t5c * (pow(1. + (k.expansion ? c2 / k.msq_sf2 : c2 / k.msq), k.p_mono) - 1.);
   }
+}
+
+// Kinetic summand, with the expanding box's H0/sf terms (islands.cpp:133-138,
+// fieldanalysis.cpp:626-629).
+__device__ __forceinline__ double site_kinetic(const Consts &k, double c, double p) {
+  if (!k.expansion) return 0.5 * (p * p);
+  const double hub = k.H0 / k.sf;
+  return (0.5 * (p * p) + 0.5 * (hub * hub) * (c * c) - c * p * k.H0 / k.sf);
 }
 
 // Per-site energy density: the summand of the reference's Energy
@@ -81,7 +92,7 @@ __device__ double site_rho(const T *phi, const float *cphi, const T *pi, const f
   const double fz = val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
   const double c2 = c * c;
   const double grad = ((fx - c) * (fx - c) / k.a2 + (fy - c) * (fy - c) / k.a2) + (fz - c) * (fz - c) / k.a2;
-  return 0.5 * (p * p) + 0.5 * grad + site_potential(k, c, c2);
+  return site_kinetic(k, c, p) + 0.5 * grad + site_potential(k, c, c2);
 }
 
 template <typename T>
@@ -228,9 +239,9 @@ __global__ void ccl_stats(const T *__restrict__ phi, const float *__restrict__ c
     const double fx = val(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
     const double fy = val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
     const double fz = val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
-    // BFS accumulators (islands.cpp:131-198), static box
+    // BFS accumulators (islands.cpp:131-198)
     const double grad = 0.5 * ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) / k.a2;
-    const double kin = 0.5 * (p * p);
+    const double kin = site_kinetic(k, c, p);
     const double c2 = c * c;
     const double pot = site_potential(k, c, c2);
     atomicAdd(&size[id], 1);
@@ -370,7 +381,8 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
   IslState *s = (IslState *)h->isl;
   const double thr = mode == PHN_ISLAND_REFERENCE ? (thres * thres * 0.5) : thres;
   const int gb = grid_blocks(V);
-  ccl_init<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, h->k, s->parent);
+  const Consts k = consts_now(h);
+  ccl_init<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, k, s->parent);
   ccl_merge<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, zper);
   ccl_compress<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk);
   ccl_scan<<<1, 1024, 0, st>>>(s->blk, s->nblk, s->blk + s->nblk);
@@ -401,7 +413,7 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
     cudaMemsetAsync(s->sums, 0, (size_t)count * 4 * sizeof(double), st);
     cudaMemsetAsync(s->peak2, 0, count * sizeof(unsigned long long), st);
     fill_ll<<<(count + 255) / 256, 256, 0, st>>>(s->peakpos, LLONG_MAX, count);
-    ccl_stats<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, h->k, s->size, s->sums,
+    ccl_stats<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, k, s->size, s->sums,
                                              s->peak2);
     ccl_peak<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
     ccl_peakval<T><<<(count + 255) / 256, 256, 0, st>>>(phi, cphi, N, count, s->peakpos, s->peakval);

@@ -22,13 +22,19 @@ namespace phn {
 
 // ----------------------------------------------------------- FP64 kernel
 // Force of theories 2-5 (Nc = 1) in the reference's order (dynamics.cpp:
-// 109-157, static box); sin and pow are CUDA's, so these agree with the
-// reference to rounding, not bitwise.
+// 109-157; the expanding box's forms :116-163 with the couplings of
+// at_scale_factor and the per-site divisions by sf); sin and pow are CUDA's,
+// so theories 2, 3 and 5 agree with the reference to rounding, not bitwise.
 template <int THEORY>
 __device__ __forceinline__ double force_f64_ext(const Consts &k, double lap, double c, double l) {
+  if (THEORY == 3 && k.expansion) {  // sin(phi / (sf sqrt(M))), no phi/|phi| factor
+    const double t = __dmul_rn(k.m3, sin(c / k.sf_sqrtm));
+    return __dadd_rn(__dadd_rn(lap, -__dmul_rn(k.mmono, c)), -t);
+  }
   if (THEORY == 2 || THEORY == 3) {
     const double s = __dsqrt_rn(l);
-    const double t = __dmul_rn(__dmul_rn(k.m3, c / s), sin(s / k.sqrt_m));
+    const double arg = k.expansion ? (s / k.sf) / k.sqrt_m : s / k.sqrt_m;
+    const double t = __dmul_rn(__dmul_rn(k.m3, c / s), sin(arg));
     if (THEORY == 2) return __dadd_rn(lap, -t);
     return __dadd_rn(__dadd_rn(lap, -__dmul_rn(k.mmono, c)), -t);
   }
@@ -36,6 +42,9 @@ __device__ __forceinline__ double force_f64_ext(const Consts &k, double lap, dou
     const double coef = __dadd_rn(__dadd_rn(k.mmM, -(__dmul_rn(k.g, c) / 2.)), __dmul_rn(k.lm, l / k.six_nc));
     return __dadd_rn(lap, -__dmul_rn(coef, c));
   }
+  if (k.expansion)
+    return __dadd_rn(lap, -__dmul_rn(__dmul_rn(k.msq_sf2, c),
+                                     pow(__dadd_rn(1., ((l / k.msq) / k.sf) / k.sf), k.p_mono - 1)));
   return __dadd_rn(lap, -__dmul_rn(__dmul_rn(k.msq, c), pow(__dadd_rn(1., l / k.msq), k.p_mono - 1)));
 }
 
@@ -86,7 +95,8 @@ __global__ void __launch_bounds__(THREADS) step_f64(const double *__restrict__ p
         for (int a = 0; a < NC; ++a) l = __dadd_rn(l, __dmul_rn(c[a], c[a]));
         double coef = __dadd_rn(k.mmM, __dmul_rn(k.lm, l / k.six_nc));
         if (THEORY == 0) {
-          const double r = l / k.kappa;
+          double r = l / k.kappa;
+          if (k.expansion) r = r / k.sf;  // sqr(locPhiSqr / Kappa / scale_factor) (dynamics.cpp:90)
           coef = __dadd_rn(coef, __dmul_rn(r, r) / k.c120);
         }
 #pragma unroll

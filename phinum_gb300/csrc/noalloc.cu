@@ -75,7 +75,9 @@ extern "C" int phn_volume_averages_noalloc(const phn_params *params, const void 
   r = scratch_address(&scratch);
   if (r) return r;
   cudaStream_t st = (cudaStream_t)stream;
-  const Consts k = make_consts(params);
+  // the expanding box's averages at tau = T0: scale factor sqrt(1 + 2 H_0 T0)
+  const Consts k0 = make_consts(params);
+  const Consts k = params->expanding ? at_scale_factor(k0, sqrt(1. + 2. * params->H0 * params->T0)) : k0;
   Grid g;
   g.block = dim3(TX, TY, 1);
   g.grid = dim3(gx, gy, 1);

@@ -150,11 +150,13 @@ __device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c
   } else if (THEORY == 1) {
     inter += __dmul_rn(k.lm, l2 / k.c24);
   } else if (THEORY == 2 || THEORY == 3) {
-    inter += __dmul_rn(k.msq2, __dsub_rn(1., cos(__dsqrt_rn(l / k.msq))));
+    const double arg = k.expansion ? __dsqrt_rn(l) / k.sf_sqrtm : __dsqrt_rn(l / k.msq);
+    inter += __dmul_rn(k.msq2, __dsub_rn(1., cos(arg)));
   } else if (THEORY == 4) {
     inter += __dadd_rn(__dmul_rn(__dmul_rn(-k.g, c[0]), l) / 6.0, __dmul_rn(k.lm, l2 / k.c24));
   } else {
-    inter += __dmul_rn(k.t5c, __dsub_rn(pow(__dadd_rn(1., l / k.msq), k.p_mono), 1.));
+    const double u = k.expansion ? (l / k.msq) / k.sf / k.sf : l / k.msq;
+    inter += __dmul_rn(k.t5c, __dsub_rn(pow(__dadd_rn(1., u), k.p_mono), 1.));
   }
   A.s[S_INTER] += inter;
   A.take_abs(sqrt(l), kidx);
@@ -317,8 +319,13 @@ __device__ __forceinline__ void fold_records(const double *__restrict__ partials
       o.pi[c] = c < k.Nc ? r.s[S_PI + c] / vol : 0.0;
     }
     const double pi2 = r.s[S_PI2], grad = r.s[S_GRAD], inter = r.s[S_INTER];
-    const double charge = (0.5 * pi2 - grad / 6. - inter);
-    const double energy = (0.5 * pi2 + 0.5 * grad + inter);
+    double charge = (0.5 * pi2 - grad / 6. - inter);
+    double energy = (0.5 * pi2 + 0.5 * grad + inter);
+    if (k.expansion) {  // fieldanalysis.cpp:626-629, on the sums
+      const double hub = (0.5 * r.s[S_PHI2] * ((k.H0 / k.sf) * (k.H0 / k.sf)) - r.s[S_PHIPI] * k.H0 / k.sf);
+      energy += hub;
+      charge += hub;
+    }
     o.energy = energy / vol;
     o.interaction = inter / vol;
     o.charge = charge / vol;
@@ -335,7 +342,7 @@ __device__ __forceinline__ void fold_records(const double *__restrict__ partials
     o.max_abs_pos = r.absi == LLONG_MAX ? -1.0 : (double)r.absi;
     o.gradient = grad / vol;
     o.nonfinite = r.s[S_NONFINITE];
-    o.reserved = 0.0;
+    o.scale_factor = k.sf;
     *out = o;
   }
 }

@@ -65,7 +65,23 @@ struct Consts {
   double t5c;              // sqr(M) * 0.5 / p_mono
   float m3_f, inv_sqrtm_f, inv_m_f, mmono_f, ghalf_f, msq_f, pm1_f, p_f;
   float msq2_f, mono_half_f, g6_f, t5c_f;
+  // the expanding box (dynamics.cpp:88-163, fieldanalysis.cpp:461-629): a
+  // launch's Consts are those of make_consts folded with one scale factor by
+  // at_scale_factor; the fields below let the FP64 kernels keep the per-site
+  // divisions by sf that the reference writes
+  int expansion;
+  double H0;
+  double sf;        // scale factor (1 when static)
+  double sf_sqrtm;  // sf * sqrt(M)
+  double msq_sf2;   // (M sf) sf
 };
+
+// Consts of the expanding box at scale factor sf: every coupling that the
+// reference multiplies by powers of sf as a whole (Mass_Mode M sf sf, h sf^3,
+// M sqrt(M) sf^3, M_mono sf sf, g sf, and the energy terms) is evaluated once
+// here in the reference's left-to-right order, so the FP64 kick that uses them
+// stays bit-identical; the FP32 constants are folded the same way.
+Consts at_scale_factor(const Consts &k0, double sf);
 
 // x / sqr(a_t) in IEEE arithmetic.  When sqr(a_t) is a power of two the
 // quotient is an exact scaling and the product by its reciprocal rounds the
@@ -159,14 +175,17 @@ struct phn_handle {
   int x4_obs_grid;     // grid of its observation-step variant
   int partial_cap;     // block records the partials buffer holds
   int obs_records;     // block records written by the last observation launch
+  double obs_sf;       // scale factor of the state the last observation read
   int *d_err;          // device error word of bounded waits (0: none)
   double *partials;    // block records of the fused observation
   phn_averages *d_avg; // finalize output (device)
   phn_averages *h_avg; // pinned host mirror, one per row slot
   int h_avg_cap;
   double *d_ref;       // reference-layout staging for upload/download
-  // reference clock (dynamics.cpp:8-50)
+  // reference clock (dynamics.cpp:8-50); the expanding box's conformal time,
+  // scale factor and conformal update stamps (tau_c = tau, sf = 1 when static)
   double tau, dtau, last_mom, last_field;
+  double tau_c, sf, last_mom_c, last_field_c;
   int steps;
   // accounting
   long long launches;
@@ -180,6 +199,9 @@ struct phn_handle {
 };
 
 namespace phn {
+// The Consts of the handle's current state: folded with its scale factor for
+// the expanding box.
+inline Consts consts_now(const phn_handle *h) { return h->p.expanding ? at_scale_factor(h->k, h->sf) : h->k; }
 void spectrum_release(phn_handle *h);
 void islands_release(phn_handle *h);
 int islands_labels_mapped(phn_handle *h, const int *map, int n, int *labels);  // islands.cu

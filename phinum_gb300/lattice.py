@@ -42,11 +42,13 @@ class Params:
     g: float = 2.0            # theory 4
     p_mono: float = -0.5      # theory 5
     m_mono_sqr: float = 1.0   # theory 3
+    expansion: int = 0        # 1: radiation-era expanding box
+    H0: float = 0.0171156     # H_0 (parameters.cpp:177)
 
     def c(self) -> L.PhnParams:
         return L.PhnParams(self.N, self.Nc, self.theory, self.mass_mode, self.lambda_mode, self.precision,
                            self.a, self.dt, self.T0, self.m_sqr, self.kappa, self.h, self.g, self.p_mono,
-                           self.m_mono_sqr)
+                           self.m_mono_sqr, int(self.expansion), 0, self.H0)
 
     @property
     def field_len(self) -> int:
@@ -142,6 +144,12 @@ class Lattice:
         t, s = ctypes.c_double(), ctypes.c_int()
         L.check(self.lib.phn_time(self.h, ctypes.byref(t), ctypes.byref(s)))
         return t.value, s.value
+
+    def conformal_time(self):
+        """(conformal time, scale factor); (tau, 1) for the static box."""
+        tc, sf = ctypes.c_double(), ctypes.c_double()
+        L.check(self.lib.phn_conformal_time(self.h, ctypes.byref(tc), ctypes.byref(sf)))
+        return tc.value, sf.value
 
     # ----------------------------------------------------------- analysis
     def volume_averages(self, allow_nonfinite: bool = False) -> np.ndarray:

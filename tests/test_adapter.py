@@ -1,5 +1,6 @@
 """The reference-side adapter (phinum_gb300/adapter/phinum_dynamics.cpp)
-compiles inside the reference's own translation unit, for both theories.
+compiles inside the reference's own translation unit, for every theory, in
+the static and the expanding box.
 Needs the reference tree (present where the build runs); skipped elsewhere."""
 import os
 import subprocess
@@ -11,9 +12,11 @@ REF = "/root/reference"
 
 
 @pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "dynamics.cpp")), reason="reference tree not present")
+@pytest.mark.parametrize("expansion", [0, 1])
 @pytest.mark.parametrize("theory", [0, 1, 2, 3, 4, 5])
-def test_adapter_compiles_in_reference_tu(theory):
+def test_adapter_compiles_in_reference_tu(theory, expansion):
     cmd = ["g++", "-std=gnu++14", "-fsyntax-only", "-w", f"-DPHN_REF_THEORY={theory}", "-DPHN_REF_PRECISION=0",
+           f"-DPHN_REF_EXPANSION={expansion}",
            "-I", os.path.join(ROOT, "oracle", "ref_shim"), "-I", os.path.join(ROOT, "oracle"),
            "-I", REF, "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "phinum_gb300", "adapter"),
            os.path.join(ROOT, "tests", "adapter_check.cpp")]
