@@ -248,7 +248,7 @@ def measure_gpu(args, dist: Dist):
     hphi, hpi = np.empty_like(phi), np.empty_like(pi)
     for a in (hphi, hpi):
         L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
-    e2e_iters = 5
+    e2e_iters = 9
 
     def e2e_iter():
         lat.upload(phi, pi)

@@ -313,6 +313,15 @@ int phn_set_variant(phn_handle *h, int variant);
  * stays usable.  No copy is issued and nothing faults. */
 int phn_wait_selftest(phn_handle *h, long long polls);
 
+/* Self-test of the FP64 kernels' division by a constant (a reciprocal
+ * multiply with two residual corrections): n operands a drawn on the device
+ * from `seed` -- half with random significands and exponents in
+ * [2^-1000, 2^1000], half placed at ±1-2 ulps around b times a midpoint
+ * between two doubles, plus zeros, subnormals, infinities and NaN -- each
+ * divided by b both ways; *mismatches counts results whose bits differ from
+ * IEEE a / b (NaN payloads aside).  n <= 2^34. */
+int phn_divide_selftest(phn_handle *h, double b, long long n, unsigned long long seed, long long *mismatches);
+
 /* Device pointers of the current fields (precision-typed: double* for
  * PHN_FP64, float* otherwise; SoA [a][z][y][x], no ghosts) and the stream the
  * handle launches on, for callers that keep data resident on the device. */

@@ -90,6 +90,8 @@ _SIGS = {
     "phn_save_config": (_I, [ctypes.c_void_p, ctypes.c_char_p, _I, _I, _I]),
     "phn_apply_filter": (_I, [ctypes.c_void_p, _D, _I, _PD, _I, _D]),
     "phn_wait_selftest": (_I, [ctypes.c_void_p, ctypes.c_longlong]),
+    "phn_divide_selftest": (_I, [ctypes.c_void_p, _D, ctypes.c_longlong, ctypes.c_ulonglong,
+                                 ctypes.POINTER(ctypes.c_longlong)]),
     "phn_load_config": (_I, [ctypes.c_void_p, ctypes.c_char_p, _I, _I, _PD, _I]),
     "phn_write_config_file": (_I, [ctypes.c_char_p, _PD, _PD, _I, _I, _I, _I]),
     "phn_read_config_file": (_I, [ctypes.c_char_p, _PD, _PD, _I, _I, _I]),

@@ -57,6 +57,27 @@ int phn::validate_params(const phn_params *p) {
   return PHN_OK;
 }
 
+// RN(1/b) of every constant divisor the FP64 kernels divide by (div_by), and
+// whether all of them lie in [2^-100, 2^100], where the residual steps cannot
+// underflow or overflow for the operands div_by accepts.
+static void set_reciprocals(Consts &k) {
+  const double divisors[] = {k.six_nc, k.kappa, k.c120, k.c24, k.c720, k.a2, k.sqrt_m, k.msq, k.sf, k.sf_sqrtm};
+  double *recips[] = {&k.r_six_nc, &k.r_kappa, &k.r_c120, &k.r_c24, &k.r_c720, &k.r_a2, &k.r_sqrtm, &k.r_msq,
+                      &k.r_sf, &k.r_sf_sqrtm};
+  k.fastdiv = 1;
+  for (int i = 0; i < 10; ++i) {
+    const double b = divisors[i];
+    const double m = fabs(b);
+    // unused divisors (zero couplings of other theories) get no reciprocal
+    if (b == 0.0) {
+      *recips[i] = 0.0;
+      continue;
+    }
+    *recips[i] = 1.0 / b;
+    if (!(m >= 0x1p-100 && m <= 0x1p100)) k.fastdiv = 0;
+  }
+}
+
 // Coefficients evaluated with the reference's expressions (dynamics.cpp:80-100,
 // fieldanalysis.cpp:445-579); see Consts.
 Consts phn::make_consts(const phn_params *p) {
@@ -115,6 +136,7 @@ Consts phn::make_consts(const phn_params *p) {
   k.sf = 1.0;
   k.sf_sqrtm = k.sqrt_m;
   k.msq_sf2 = k.msq;
+  set_reciprocals(k);
   return k;
 }
 
@@ -153,6 +175,7 @@ Consts phn::at_scale_factor(const Consts &k0, double sf) {
   k.mono_half_f = (float)(0.5 * k.mmono);
   k.g6_f = (float)(k.g / 6.0);
   k.t5c_f = (float)k.t5c;
+  set_reciprocals(k);
   return k;
 }
 

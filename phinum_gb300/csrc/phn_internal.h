@@ -74,6 +74,10 @@ struct Consts {
   double sf;        // scale factor (1 when static)
   double sf_sqrtm;  // sf * sqrt(M)
   double msq_sf2;   // (M sf) sf
+  // reciprocals RN(1/b) of the FP64 kernels' constant divisors (div_by);
+  // fastdiv = 0 when a divisor lies outside [2^-100, 2^100]
+  int fastdiv;
+  double r_six_nc, r_kappa, r_c120, r_c24, r_c720, r_a2, r_sqrtm, r_msq, r_sf, r_sf_sqrtm;
 };
 
 // Consts of the expanding box at scale factor sf: every coupling that the
@@ -83,11 +87,33 @@ struct Consts {
 // stays bit-identical; the FP32 constants are folded the same way.
 Consts at_scale_factor(const Consts &k0, double sf);
 
+// a / b, correctly rounded, for a divisor b fixed per launch with rb =
+// RN(1/b) from the host: q = RN(a rb), then two residual corrections
+// q <- RN(q + RN(a - b q) rb).  The first makes q a faithful quotient; from a
+// faithful q and rb = RN(1/b) the second returns RN(a/b) (Markstein's
+// theorem: P. Markstein, IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al.,
+// Handbook of Floating-Point Arithmetic, ch. "Markstein's theorems"), and the
+// fma residual of a faithful quotient is exact.  The theorem needs no
+// underflow or overflow in the residuals: operands outside
+// 2^-900 <= |a| < 2^900 (zeros, subnormals, infinities, NaN; an integer test
+// of the exponent) and handles whose divisors leave [2^-100, 2^100] (fastdiv
+// = 0) take IEEE division.  Five FP64 operations instead of a full division:
+// the FP64 kernels are bound by GB300's FP64 rate.
+__device__ __forceinline__ double div_by(const Consts &k, double a, double b, double rb) {
+  const unsigned hi = (unsigned)__double2hiint(a) & 0x7fffffffu;
+  if (k.fastdiv && hi >= 0x07b00000u && hi < 0x78300000u) {
+    double q = __dmul_rn(a, rb);
+    q = __fma_rn(__fma_rn(-b, q, a), rb, q);
+    return __fma_rn(__fma_rn(-b, q, a), rb, q);
+  }
+  return a / b;
+}
+
 // x / sqr(a_t) in IEEE arithmetic.  When sqr(a_t) is a power of two the
 // quotient is an exact scaling and the product by its reciprocal rounds the
 // same real number the same way (bit-identical, cheaper on the FP64 pipes).
 __device__ __forceinline__ double div_a2(const Consts &k, double x) {
-  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : x / k.a2;
+  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : div_by(k, x, k.a2, k.r_a2);
 }
 
 // Per-step kick and drift factors: tau - Last_Momenta_update and

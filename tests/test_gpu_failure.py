@@ -29,3 +29,4 @@ def test_bounded_wait_times_out_and_context_stays_usable():
         lat.evolve(10)
         b = lat.download()
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1][N * N:-N * N], b[1][N * N:-N * N])
+
