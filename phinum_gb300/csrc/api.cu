@@ -65,7 +65,8 @@ static void set_reciprocals(Consts &k) {
   double *recips[] = {&k.r_six_nc, &k.r_kappa, &k.r_c120, &k.r_c24, &k.r_c720, &k.r_a2, &k.r_sqrtm, &k.r_msq,
                       &k.r_sf, &k.r_sf_sqrtm};
   k.fastdiv = 1;
-  for (int i = 0; i < 10; ++i) {
+  k.div1 = 0;
+  for (int i = 0; i < 10; ++i) {  // indices as enum DivIndex
     const double b = divisors[i];
     const double m = fabs(b);
     // unused divisors (zero couplings of other theories) get no reciprocal
@@ -75,6 +76,8 @@ static void set_reciprocals(Consts &k) {
     }
     *recips[i] = 1.0 / b;
     if (!(m >= 0x1p-100 && m <= 0x1p100)) k.fastdiv = 0;
+    // b * RN(1/b) - 1, exact in one fma: the reciprocal's relative error
+    if (fabs(fma(b, *recips[i], -1.0)) <= 0x1p-54) k.div1 |= 1 << i;
   }
 }
 
@@ -95,6 +98,7 @@ Consts phn::make_consts(const phn_params *p) {
   }
   k.mmM = p->mass_mode * p->m_sqr;
   k.lm = (double)p->lambda_mode;
+  k.lm_sign = p->lambda_mode == 1 ? 1 : (p->lambda_mode == -1 ? -1 : 0);
   k.six_nc = 6. * Nc;
   k.kappa = p->kappa;
   k.c120 = 120. * Nc * Nc;

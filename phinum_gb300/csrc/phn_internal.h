@@ -75,10 +75,15 @@ struct Consts {
   double sf_sqrtm;  // sf * sqrt(M)
   double msq_sf2;   // (M sf) sf
   // reciprocals RN(1/b) of the FP64 kernels' constant divisors (div_by);
-  // fastdiv = 0 when a divisor lies outside [2^-100, 2^100]
-  int fastdiv;
+  // fastdiv = 0 when a divisor lies outside [2^-100, 2^100]; bit DIV_x of
+  // div1 is set when RN(1/b) is within 2^-54 relative of 1/b, so that
+  // RN(a RN(1/b)) is already a faithful quotient and one correction suffices
+  int fastdiv, div1;
   double r_six_nc, r_kappa, r_c120, r_c24, r_c720, r_a2, r_sqrtm, r_msq, r_sf, r_sf_sqrtm;
+  int lm_sign;  // Lambda_Mode = +1 / -1: lm * x is x / -x (exact); 0 otherwise
 };
+
+enum DivIndex { DIV_SIX_NC, DIV_KAPPA, DIV_C120, DIV_C24, DIV_C720, DIV_A2, DIV_SQRTM, DIV_MSQ, DIV_SF, DIV_SF_SQRTM };
 
 // Consts of the expanding box at scale factor sf: every coupling that the
 // reference multiplies by powers of sf as a whole (Mass_Mode M sf sf, h sf^3,
@@ -88,32 +93,40 @@ struct Consts {
 Consts at_scale_factor(const Consts &k0, double sf);
 
 // a / b, correctly rounded, for a divisor b fixed per launch with rb =
-// RN(1/b) from the host: q = RN(a rb), then two residual corrections
-// q <- RN(q + RN(a - b q) rb).  The first makes q a faithful quotient; from a
-// faithful q and rb = RN(1/b) the second returns RN(a/b) (Markstein's
-// theorem: P. Markstein, IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al.,
-// Handbook of Floating-Point Arithmetic, ch. "Markstein's theorems"), and the
-// fma residual of a faithful quotient is exact.  The theorem needs no
-// underflow or overflow in the residuals: operands outside
-// 2^-900 <= |a| < 2^900 (zeros, subnormals, infinities, NaN; an integer test
-// of the exponent) and handles whose divisors leave [2^-100, 2^100] (fastdiv
-// = 0) take IEEE division.  Five FP64 operations instead of a full division:
-// the FP64 kernels are bound by GB300's FP64 rate.
-__device__ __forceinline__ double div_by(const Consts &k, double a, double b, double rb) {
+// RN(1/b) from the host: q = RN(a rb), then residual corrections
+// q <- RN(q + RN(a - b q) rb).  From a faithful q (within one ulp of a/b) and
+// rb = RN(1/b), one correction returns RN(a/b) (Markstein's theorem: P.
+// Markstein, IBM J. Res. Dev. 34(1), 1990; M. Cornea-Hasegan, R. Golliver,
+// P. Markstein, ARITH-14, 1999), and the fma residual of a faithful quotient
+// is exact.  RN(a rb) itself is faithful when |b rb - 1| <= 2^-54: a rb then
+// lies within half an ulp of a/b (bit `idx` of div1, decided on the host);
+// otherwise a first correction makes q faithful and a second one rounds it.
+// The theorem needs no underflow or overflow in the residuals: operands
+// outside 2^-900 <= |a| < 2^900 (zeros, subnormals, infinities, NaN; an
+// integer test of the exponent) and handles whose divisors leave
+// [2^-100, 2^100] (fastdiv = 0) take IEEE division.  Three or five FP64
+// operations instead of a full division: the FP64 kernels are bound by
+// GB300's FP64 rate.
+__device__ __forceinline__ double div_by(const Consts &k, double a, double b, double rb, int idx) {
   const unsigned hi = (unsigned)__double2hiint(a) & 0x7fffffffu;
   if (k.fastdiv && hi >= 0x07b00000u && hi < 0x78300000u) {
     double q = __dmul_rn(a, rb);
-    q = __fma_rn(__fma_rn(-b, q, a), rb, q);
+    if (!((k.div1 >> idx) & 1)) q = __fma_rn(__fma_rn(-b, q, a), rb, q);
     return __fma_rn(__fma_rn(-b, q, a), rb, q);
   }
   return a / b;
+}
+
+// Lambda_Mode * x in IEEE arithmetic: a sign flip for Lambda_Mode = +-1.
+__device__ __forceinline__ double times_lm(const Consts &k, double x) {
+  return k.lm_sign > 0 ? x : (k.lm_sign < 0 ? -x : __dmul_rn(k.lm, x));
 }
 
 // x / sqr(a_t) in IEEE arithmetic.  When sqr(a_t) is a power of two the
 // quotient is an exact scaling and the product by its reciprocal rounds the
 // same real number the same way (bit-identical, cheaper on the FP64 pipes).
 __device__ __forceinline__ double div_a2(const Consts &k, double x) {
-  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : div_by(k, x, k.a2, k.r_a2);
+  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : div_by(k, x, k.a2, k.r_a2, DIV_A2);
 }
 
 // Per-step kick and drift factors: tau - Last_Momenta_update and
