@@ -65,8 +65,7 @@ static void set_reciprocals(Consts &k) {
   double *recips[] = {&k.r_six_nc, &k.r_kappa, &k.r_c120, &k.r_c24, &k.r_c720, &k.r_a2, &k.r_sqrtm, &k.r_msq,
                       &k.r_sf, &k.r_sf_sqrtm};
   k.fastdiv = 1;
-  k.div1 = 0;
-  for (int i = 0; i < 10; ++i) {  // indices as enum DivIndex
+  for (int i = 0; i < 10; ++i) {
     const double b = divisors[i];
     const double m = fabs(b);
     // unused divisors (zero couplings of other theories) get no reciprocal
@@ -76,9 +75,13 @@ static void set_reciprocals(Consts &k) {
     }
     *recips[i] = 1.0 / b;
     if (!(m >= 0x1p-100 && m <= 0x1p100)) k.fastdiv = 0;
-    // b * RN(1/b) - 1, exact in one fma: the reciprocal's relative error
-    if (fabs(fma(b, *recips[i], -1.0)) <= 0x1p-54) k.div1 |= 1 << i;
   }
+  // the kernels divide by 6 Nc, 24 Nc and 120 Nc^2 with one correction
+  // (div_by<true>): their reciprocals must be within 2^-54 (b * RN(1/b) - 1
+  // is exact in one fma); true for Nc <= 4, checked all the same
+  const double near[] = {k.six_nc, k.c24, k.c120};
+  for (double b : near)
+    if (!(fabs(fma(b, 1.0 / b, -1.0)) <= 0x1p-54)) k.fastdiv = 0;
 }
 
 // Coefficients evaluated with the reference's expressions (dynamics.cpp:80-100,
@@ -98,7 +101,6 @@ Consts phn::make_consts(const phn_params *p) {
   }
   k.mmM = p->mass_mode * p->m_sqr;
   k.lm = (double)p->lambda_mode;
-  k.lm_sign = p->lambda_mode == 1 ? 1 : (p->lambda_mode == -1 ? -1 : 0);
   k.six_nc = 6. * Nc;
   k.kappa = p->kappa;
   k.c120 = 120. * Nc * Nc;

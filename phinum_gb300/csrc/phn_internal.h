@@ -74,16 +74,12 @@ struct Consts {
   double sf;        // scale factor (1 when static)
   double sf_sqrtm;  // sf * sqrt(M)
   double msq_sf2;   // (M sf) sf
-  // reciprocals RN(1/b) of the FP64 kernels' constant divisors (div_by);
-  // fastdiv = 0 when a divisor lies outside [2^-100, 2^100]; bit DIV_x of
-  // div1 is set when RN(1/b) is within 2^-54 relative of 1/b, so that
-  // RN(a RN(1/b)) is already a faithful quotient and one correction suffices
-  int fastdiv, div1;
+  // reciprocals RN(1/b) of the FP64 kernels' constant divisors (div_by,
+  // div_by_near); fastdiv = 0 when a divisor lies outside [2^-100, 2^100] or
+  // one of 6 Nc, 24 Nc, 120 Nc^2 has a reciprocal further than 2^-54 from 1/b
+  int fastdiv;
   double r_six_nc, r_kappa, r_c120, r_c24, r_c720, r_a2, r_sqrtm, r_msq, r_sf, r_sf_sqrtm;
-  int lm_sign;  // Lambda_Mode = +1 / -1: lm * x is x / -x (exact); 0 otherwise
 };
-
-enum DivIndex { DIV_SIX_NC, DIV_KAPPA, DIV_C120, DIV_C24, DIV_C720, DIV_A2, DIV_SQRTM, DIV_MSQ, DIV_SF, DIV_SF_SQRTM };
 
 // Consts of the expanding box at scale factor sf: every coupling that the
 // reference multiplies by powers of sf as a whole (Mass_Mode M sf sf, h sf^3,
@@ -98,35 +94,31 @@ Consts at_scale_factor(const Consts &k0, double sf);
 // rb = RN(1/b), one correction returns RN(a/b) (Markstein's theorem: P.
 // Markstein, IBM J. Res. Dev. 34(1), 1990; M. Cornea-Hasegan, R. Golliver,
 // P. Markstein, ARITH-14, 1999), and the fma residual of a faithful quotient
-// is exact.  RN(a rb) itself is faithful when |b rb - 1| <= 2^-54: a rb then
-// lies within half an ulp of a/b (bit `idx` of div1, decided on the host);
-// otherwise a first correction makes q faithful and a second one rounds it.
-// The theorem needs no underflow or overflow in the residuals: operands
-// outside 2^-900 <= |a| < 2^900 (zeros, subnormals, infinities, NaN; an
-// integer test of the exponent) and handles whose divisors leave
-// [2^-100, 2^100] (fastdiv = 0) take IEEE division.  Three or five FP64
-// operations instead of a full division: the FP64 kernels are bound by
-// GB300's FP64 rate.
-__device__ __forceinline__ double div_by(const Consts &k, double a, double b, double rb, int idx) {
+// is exact.  RN(a rb) itself is faithful when |b rb - 1| <= 2^-54 (a rb then
+// lies within half an ulp of a/b): NEAR = true, one correction, for the
+// divisors 6 Nc, 24 Nc and 120 Nc^2 (checked on the host); otherwise a first
+// correction makes q faithful and a second one rounds it.  The theorem needs
+// no underflow or overflow in the residuals: operands outside
+// 2^-900 <= |a| < 2^900 (zeros, subnormals, infinities, NaN; an integer test
+// of the exponent) and handles whose divisors leave [2^-100, 2^100]
+// (fastdiv = 0) take IEEE division.  Three or five FP64 operations instead of
+// a full division: the FP64 kernels are bound by GB300's FP64 rate.
+template <bool NEAR = false>
+__device__ __forceinline__ double div_by(const Consts &k, double a, double b, double rb) {
   const unsigned hi = (unsigned)__double2hiint(a) & 0x7fffffffu;
   if (k.fastdiv && hi >= 0x07b00000u && hi < 0x78300000u) {
     double q = __dmul_rn(a, rb);
-    if (!((k.div1 >> idx) & 1)) q = __fma_rn(__fma_rn(-b, q, a), rb, q);
+    if (!NEAR) q = __fma_rn(__fma_rn(-b, q, a), rb, q);
     return __fma_rn(__fma_rn(-b, q, a), rb, q);
   }
   return a / b;
-}
-
-// Lambda_Mode * x in IEEE arithmetic: a sign flip for Lambda_Mode = +-1.
-__device__ __forceinline__ double times_lm(const Consts &k, double x) {
-  return k.lm_sign > 0 ? x : (k.lm_sign < 0 ? -x : __dmul_rn(k.lm, x));
 }
 
 // x / sqr(a_t) in IEEE arithmetic.  When sqr(a_t) is a power of two the
 // quotient is an exact scaling and the product by its reciprocal rounds the
 // same real number the same way (bit-identical, cheaper on the FP64 pipes).
 __device__ __forceinline__ double div_a2(const Consts &k, double x) {
-  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : div_by(k, x, k.a2, k.r_a2, DIV_A2);
+  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : div_by(k, x, k.a2, k.r_a2);
 }
 
 // Per-step kick and drift factors: tau - Last_Momenta_update and
