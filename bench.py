@@ -24,6 +24,11 @@ cpu_baseline / --impl reference
           number of steps of the same lattice.
 Multi-GPU: replicas only -- every rank evolves its own lattice; no collective
 on the data path.
+
+--form precision|adjoint|ensemble|initial|io|analysis prints one JSON object
+for the compensated-FP32 run, the adjoint, the ensemble, the initial
+conditions, the checkpoint files or the spectrum/island passes instead of the
+benchmark line.
 """
 from __future__ import annotations
 
@@ -589,6 +594,64 @@ def initial_form(N: int, n_cpu: int = 128, n_check: int = 64):
     return out
 
 
+def analysis_form(N: int, reps: int = 5, steps: int = 200):
+    """The analysis passes of the hot path on the bench's 512^3 phi^6 lattice
+    after `steps` FP32 steps, wall time per call (the calls return host
+    results, so each ends synchronised), median of `reps` after a warm-up:
+    the reference spectrum (2 x cuFFT R2C + binning into the reference's bins,
+    Calculate_CorrelationFunctions), the configuration's 64 uniform bins,
+    Full_Analysis's labelling with the reference mask (thres = 2.57583
+    sqrt(<phi^2>), main.cpp:70) and with the configuration's mask
+    (rho > 2 <rho>, z periodic), island statistics to the host, labels kept on
+    the device.  FP32 and FP64 fields."""
+    from phinum_gb300 import _lib as L
+    from phinum_gb300 import lattice as PL
+    phi, pi = make_fields(N)
+    out = {"form": "analysis", "N": N, "steps_before": steps}
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            r = fn()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)) * 1e3, r
+
+    for name, prec in (("fp32", L.FP32), ("fp64", L.FP64)):
+        lat = PL.Lattice(PL.Params(N=N, precision=prec))
+        lat.upload(phi, pi)
+        lat.evolve(steps)
+        avg = lat.volume_averages()
+        thr = 2.57583 * float(np.sqrt(avg[O_AVG_PHI2]))
+        lat.correlation_functions()  # warm-up: cuFFT plan, key tables
+        lat.spectrum_uniform(64)
+        ms_spec, spec = timed(lat.correlation_functions)
+        ms_uni, _ = timed(lambda: lat.spectrum_uniform(64))
+        rho_thr = 2.0 * avg[O_AVG_ENERGY]
+        # warm-up calls size the record buffers to the island counts
+        n_isl = lat.full_analysis(thr, labels=False, max_out=1 << 23)[1].shape[0]
+        n_rho = lat.full_analysis(rho_thr, mode=L.ISLAND_ENERGY, z_periodic=True, labels=False,
+                                  max_out=1 << 23)[1].shape[0]
+        ms_isl, isl = timed(lambda: lat.full_analysis(thr, labels=False, max_out=n_isl))
+        ms_rho, rho = timed(lambda: lat.full_analysis(rho_thr, mode=L.ISLAND_ENERGY, z_periodic=True, labels=False,
+                                                      max_out=n_rho))
+        elem = 8 if prec == L.FP32 else 16  # complex bytes
+        half = N * N * (N // 2 + 1) * elem
+        out[name] = {"spectrum_ms": ms_spec, "spectrum_bins": int(spec[3].size),
+                     "spectrum_uniform64_ms": ms_uni,
+                     "spectrum_halfspectra_bytes": 2 * half,
+                     "islands_reference_mask_ms": ms_isl, "islands_reference_mask_count": int(isl[1].shape[0]),
+                     "islands_reference_mask_sites": int(isl[1][:, 1].sum()),
+                     "islands_energy_mask_ms": ms_rho, "islands_energy_mask_count": int(rho[1].shape[0]),
+                     "islands_energy_mask_sites": int(rho[1][:, 1].sum()),
+                     "threshold": thr}
+        lat.close()
+    return out
+
+
+O_AVG_PHI2, O_AVG_ENERGY = 9, 14  # phn_averages columns: avgphi2, avgEnergy
+
+
 def io_form(N: int, directory: str):
     """Checkpoint files (SaveConfig / ExtractConfig format): phn_save_config
     and phn_load_config on an N^3 FP64 lattice with all host threads and with
@@ -653,7 +716,7 @@ def main():
     ap.add_argument("--n", "--lattice-edge", dest="n", type=int, default=N_MAIN,
                     help="lattice edge (profiling runs use smaller cases); under torchrun spell it --lattice-edge")
     ap.add_argument("--variant", type=int, default=None, help="TMA kernel variant instead of the autotuner's pick")
-    ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble", "initial", "io"],
+    ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble", "initial", "io", "analysis"],
                     help="report one of the north-star forms instead of the benchmark line")
     args = ap.parse_args()
     rank, local, world = env_rank()
@@ -682,6 +745,9 @@ def main():
         return
     if args.form == "initial":
         print(json.dumps(initial_form(args.n)))
+        return
+    if args.form == "analysis":
+        print(json.dumps(analysis_form(args.n)))
         return
     if args.form == "ensemble":
         out = measure_ensemble(max(args.steps, 100), 100)

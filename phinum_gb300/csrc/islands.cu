@@ -19,6 +19,8 @@
 
 #include <vector>
 
+#include <type_traits>
+
 #include "phn_internal.h"
 
 namespace phn {
@@ -52,22 +54,44 @@ __device__ __forceinline__ double val(const T *f, const float *comp, size_t i) {
 // CalculateVolumeAverages (fieldanalysis.cpp:456-617) for Nc = 1.  The
 // expanding box's couplings come folded with the scale factor
 // (at_scale_factor); the cosine and power arguments carry it per site.
+// (FP64; the constant divisors as products by their reciprocals: these sums
+// are compared to the reference's within rounding, not bitwise.)
 __device__ __forceinline__ double site_potential(const Consts &k, double c, double c2) {
   const double l2 = c2 * c2;
-  const double cos_arg = k.expansion ? sqrt(c2) / k.sf_sqrtm : sqrt(c2 / k.msq);
+  const double cos_arg = k.expansion ? sqrt(c2) * k.r_sf_sqrtm : sqrt(c2 * k.r_msq);
   switch (k.theory) {
     case 0:
-      return k.mm_half_M * c2 + k.lm * (l2 / k.c24) + (l2 * c2 / k.c720);
+      return k.mm_half_M * c2 + k.lm * (l2 * k.r_c24) + (l2 * c2 * k.r_c720);
     case 1:
-      return k.h * c + k.mm_half_M * c2 + k.lm * (l2 / k.c24);
+      return k.h * c + k.mm_half_M * c2 + k.lm * (l2 * k.r_c24);
     case 2:
       return k.msq2 * (1. - cos(cos_arg));
     case 3:
       return 0.5 * k.mmono * c2 + k.msq2 * (1. - cos(cos_arg));
     case 4:
-      return k.mm_half_M * c2 - k.g * c2 * c / 6. + k.lm * (l2 / k.c24);
+      return k.mm_half_M * c2 - k.g * c2 * c * (1.0 / 6.0) + k.lm * (l2 * k.r_c24);
     default:
-      return k.t5c * (pow(1. + (k.expansion ? c2 / k.msq_sf2 : c2 / k.msq), k.p_mono) - 1.);
+      return k.t5c * (pow(1. + (k.expansion ? c2 / k.msq_sf2 : c2 * k.r_msq), k.p_mono) - 1.);
+  }
+}
+
+// The same in FP32, from the FP32 forms of the couplings (those of the FP32
+// observation): island statistics of FP32 fields.
+__device__ __forceinline__ float site_potential(const Consts &k, float c, float c2) {
+  const float l2 = c2 * c2;
+  switch (k.theory) {
+    case 0:
+      return fmaf(k.e6_f, l2 * c2, fmaf(k.e4_f, l2, k.mmh_f * c2));
+    case 1:
+      return fmaf(k.h_f, c, fmaf(k.e4_f, l2, k.mmh_f * c2));
+    case 2:
+      return k.msq2_f * (1.f - cosf(sqrtf(c2 * k.inv_m_f)));
+    case 3:
+      return fmaf(k.mono_half_f, c2, k.msq2_f * (1.f - cosf(sqrtf(c2 * k.inv_m_f))));
+    case 4:
+      return fmaf(-k.g6_f * c, c2, fmaf(k.e4_f, l2, k.mmh_f * c2));
+    default:
+      return k.t5c_f * (powf(fmaf(c2, k.inv_m_f, 1.f), k.p_f) - 1.f);
   }
 }
 
@@ -79,20 +103,28 @@ __device__ __forceinline__ double site_kinetic(const Consts &k, double c, double
   return (0.5 * (p * p) + 0.5 * (hub * hub) * (c * c) - c * p * k.H0 / k.sf);
 }
 
+__device__ __forceinline__ float site_kinetic(const Consts &k, float c, float p) {
+  if (!k.expansion) return 0.5f * (p * p);
+  const float hub = (float)(k.H0 / k.sf);
+  return fmaf(0.5f * (hub * hub) * c, c, fmaf(0.5f * p, p, -c * p * hub));
+}
+
 // Per-site energy density: the summand of the reference's Energy
-// (fieldanalysis.cpp:437-471,571-579), Nc = 1.
-template <typename T>
-__device__ double site_rho(const T *phi, const float *cphi, const T *pi, const float *cpi, int N, int x, int y, int z,
-                           const Consts k) {
+// (fieldanalysis.cpp:437-471,571-579), Nc = 1, in arithmetic A: FP64 for FP64
+// fields, FP32 for FP32 fields (their values carry FP32 rounding already; a
+// site within that of the threshold is on either side).
+template <typename A, typename T>
+__device__ A site_rho(const T *phi, const float *cphi, const T *pi, const float *cpi, int N, int x, int y, int z,
+                      const Consts k) {
   const size_t NN = (size_t)N * N;
   const size_t i = (size_t)z * NN + (size_t)y * N + x;
-  const double c = val(phi, cphi, i), p = val(pi, cpi, i);
-  const double fx = val(phi, cphi, (size_t)z * NN + (size_t)y * N + (x + 1 == N ? 0 : x + 1));
-  const double fy = val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
-  const double fz = val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
-  const double c2 = c * c;
-  const double grad = ((fx - c) * (fx - c) / k.a2 + (fy - c) * (fy - c) / k.a2) + (fz - c) * (fz - c) / k.a2;
-  return site_kinetic(k, c, p) + 0.5 * grad + site_potential(k, c, c2);
+  const A c = (A)val(phi, cphi, i), p = (A)val(pi, cpi, i);
+  const A fx = (A)val(phi, cphi, (size_t)z * NN + (size_t)y * N + (x + 1 == N ? 0 : x + 1));
+  const A fy = (A)val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
+  const A fz = (A)val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
+  const A c2 = c * c;
+  const A grad = (((fx - c) * (fx - c) + (fy - c) * (fy - c)) + (fz - c) * (fz - c)) * (A)k.inv_a2;
+  return site_kinetic(k, c, p) + (A)0.5 * grad + site_potential(k, c, c2);
 }
 
 template <typename T>
@@ -108,7 +140,8 @@ __global__ void ccl_init(const T *__restrict__ phi, const float *__restrict__ cp
       m = __dadd_rn(__dmul_rn(__dmul_rn(c, c), 0.5), __dmul_rn(__dmul_rn(p, p), 0.5)) > thr;
     } else {
       const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((size_t)N * N));
-      m = site_rho(phi, cphi, pi, cpi, N, x, y, z, k) > thr;
+      using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+      m = site_rho<A>(phi, cphi, pi, cpi, N, x, y, z, k) > (A)thr;
     }
     parent[i] = m ? (int)i : -1;
   }
@@ -224,33 +257,132 @@ __global__ void ccl_number(const int *__restrict__ parent, size_t V, const int *
   }
 }
 
+// Per-island sums.  Block b owns the STATS_SITES consecutive sites
+// [b STATS_SITES, (b+1) STATS_SITES) (whole x rows); a warp takes 32
+// consecutive sites at a time.  Sites of one island along a row form runs,
+// which a segmented inclusive scan over the lanes reduces (size, PotEn, KinEn,
+// GradEn and phi sums, max phi^2); each run's last lane merges its sums into
+// the block's shared-memory table keyed by island id, and the block adds each
+// table entry to the global sums once.  An island that spans the lattice (a
+// percolating mask) so costs one global atomic per block, not one per site:
+// same-address atomics from every warp were what bounded this pass.  A run
+// that finds the table full adds to the global sums directly.
+constexpr int STATS_SITES = 8192;
+constexpr int STATS_SLOTS = 1024;  // power of two
+
+struct StatsSlot {
+  double pot, kin, grad, phi;
+  unsigned long long peak2;
+  int size, id;
+};
+
+template <typename A>
+__device__ __forceinline__ void stats_global(int id, int n, A pot, A kin, A grad, A cs, unsigned long long pk,
+                                             int *size, double *sums, unsigned long long *peak2) {
+  atomicAdd(&size[id], n);
+  atomicAdd(&sums[(size_t)id * 4 + 0], (double)pot);
+  atomicAdd(&sums[(size_t)id * 4 + 1], (double)kin);
+  atomicAdd(&sums[(size_t)id * 4 + 2], (double)grad);
+  atomicAdd(&sums[(size_t)id * 4 + 3], (double)cs);
+  atomicMax(&peak2[id], pk);
+}
+
 template <typename T>
-__global__ void ccl_stats(const T *__restrict__ phi, const float *__restrict__ cphi, const T *__restrict__ pi,
-                          const float *__restrict__ cpi, const int *__restrict__ parent, const int *__restrict__ ids,
-                          int N, const Consts k, int *__restrict__ size, double *__restrict__ sums,
-                          unsigned long long *__restrict__ peak2) {
+__global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ phi, const float *__restrict__ cphi,
+                                                        const T *__restrict__ pi, const float *__restrict__ cpi,
+                                                        const int *__restrict__ parent, const int *__restrict__ ids,
+                                                        int N, const Consts k, int *__restrict__ size,
+                                                        double *__restrict__ sums,
+                                                        unsigned long long *__restrict__ peak2) {
+  __shared__ StatsSlot table[STATS_SLOTS];
+  for (int j = threadIdx.x; j < STATS_SLOTS; j += CCL_THREADS) {
+    table[j].pot = table[j].kin = table[j].grad = table[j].phi = 0.0;
+    table[j].peak2 = 0;
+    table[j].size = 0;
+    table[j].id = -1;
+  }
+  __syncthreads();
   const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    const int r = parent[i];
-    if (r < 0) continue;
-    const int id = ids[r];
-    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
-    const double c = val(phi, cphi, i), p = val(pi, cpi, i);
-    const double fx = val(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
-    const double fy = val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
-    const double fz = val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
-    // BFS accumulators (islands.cpp:131-198)
-    const double grad = 0.5 * ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) / k.a2;
-    const double kin = site_kinetic(k, c, p);
-    const double c2 = c * c;
-    const double pot = site_potential(k, c, c2);
-    atomicAdd(&size[id], 1);
-    atomicAdd(&sums[(size_t)id * 4 + 0], pot);
-    atomicAdd(&sums[(size_t)id * 4 + 1], kin);
-    atomicAdd(&sums[(size_t)id * 4 + 2], grad);
-    atomicAdd(&sums[(size_t)id * 4 + 3], c);
-    // phi^2 >= 0: its IEEE bit pattern orders like the value
-    atomicMax(&peak2[id], (unsigned long long)__double_as_longlong(c2));
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t s0 = (size_t)blockIdx.x * STATS_SITES;
+  const size_t s1 = s0 + STATS_SITES < V ? s0 + STATS_SITES : V;
+  // FP32 fields: per-site terms and the in-warp scan in FP32 (GB300's FP64
+  // rate would otherwise bound the pass); FP64 fields: FP64.  The global
+  // per-island sums are FP64 either way.
+  using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+  // chunk loop: uniform per warp, so every lane takes part in the collectives
+  for (size_t base = s0 + (size_t)warp * 32; base < s1; base += (size_t)(CCL_THREADS / 32) * 32) {
+    const size_t i = base + lane;
+    int id = -1, n = 0;
+    A pot = 0, kin = 0, grad = 0, cs = 0;
+    unsigned long long pk = 0;
+    const int r = i < s1 ? parent[i] : -1;
+    if (r >= 0) {
+      id = ids[r];
+      const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
+      const double cd = val(phi, cphi, i);
+      const A c = (A)cd, p = (A)val(pi, cpi, i);
+      const A fx = (A)val(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
+      const A fy = (A)val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
+      const A fz = (A)val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
+      // BFS accumulators (islands.cpp:131-198)
+      grad = (A)0.5 * ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) * (A)k.inv_a2;
+      kin = site_kinetic(k, c, p);
+      pot = site_potential(k, c, c * c);
+      cs = c;
+      n = 1;
+      // phi^2 >= 0: its bits order like the value; the FP64 square, so that
+      // ccl_peak finds the same maximum
+      pk = (unsigned long long)__double_as_longlong(cd * cd);
+    }
+    const int prev = __shfl_up_sync(full, id, 1);
+    const unsigned heads = __ballot_sync(full, lane == 0 || prev != id);
+    const int start = 31 - __clz(heads & (full >> (31 - lane)));  // first lane of my run
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const A up = __shfl_up_sync(full, pot, off), uk = __shfl_up_sync(full, kin, off);
+      const A ug = __shfl_up_sync(full, grad, off), uc = __shfl_up_sync(full, cs, off);
+      const int un = __shfl_up_sync(full, n, off);
+      const unsigned long long upk = __shfl_up_sync(full, pk, off);
+      if (lane - off >= start) {
+        pot += up;
+        kin += uk;
+        grad += ug;
+        cs += uc;
+        n += un;
+        pk = upk > pk ? upk : pk;
+      }
+    }
+    const int next = __shfl_down_sync(full, id, 1);
+    if ((lane == 31 || next != id) && id >= 0) {
+      // open addressing on the island id, linear probing
+      unsigned h = ((unsigned)id * 2654435761u) & (STATS_SLOTS - 1);
+      int slot = -1;
+      for (int probe = 0; probe < STATS_SLOTS; ++probe) {
+        const int old = atomicCAS(&table[h].id, -1, id);
+        if (old == -1 || old == id) {
+          slot = (int)h;
+          break;
+        }
+        h = (h + 1) & (STATS_SLOTS - 1);
+      }
+      if (slot >= 0) {
+        atomicAdd(&table[slot].size, n);
+        atomicAdd(&table[slot].pot, (double)pot);
+        atomicAdd(&table[slot].kin, (double)kin);
+        atomicAdd(&table[slot].grad, (double)grad);
+        atomicAdd(&table[slot].phi, (double)cs);
+        atomicMax(&table[slot].peak2, pk);
+      } else {
+        stats_global(id, n, pot, kin, grad, cs, pk, size, sums, peak2);
+      }
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < STATS_SLOTS; j += CCL_THREADS) {
+    const StatsSlot &t = table[j];
+    if (t.id >= 0) stats_global(t.id, t.size, t.pot, t.kin, t.grad, t.phi, t.peak2, size, sums, peak2);
   }
 }
 
@@ -413,8 +545,8 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
     cudaMemsetAsync(s->sums, 0, (size_t)count * 4 * sizeof(double), st);
     cudaMemsetAsync(s->peak2, 0, count * sizeof(unsigned long long), st);
     fill_ll<<<(count + 255) / 256, 256, 0, st>>>(s->peakpos, LLONG_MAX, count);
-    ccl_stats<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, k, s->size, s->sums,
-                                             s->peak2);
+    ccl_stats<T><<<(unsigned)((V + STATS_SITES - 1) / STATS_SITES), CCL_THREADS, 0, st>>>(
+        phi, cphi, pi, cpi, s->parent, s->ids, N, k, s->size, s->sums, s->peak2);
     ccl_peak<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
     ccl_peakval<T><<<(count + 255) / 256, 256, 0, st>>>(phi, cphi, N, count, s->peakpos, s->peakval);
     h->launches += 4;

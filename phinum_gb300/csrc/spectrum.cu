@@ -17,9 +17,16 @@
 // counterpart): the same modes, weights and sums, binned uniformly in |p| on
 // [0, p_max] with p_max the largest lattice momentum.
 //
-// Accumulation is deterministic: per-warp shared-memory histograms (one lane
-// per distinct bin adds a fixed-shape butterfly sum of the warp's values),
-// folded per block in warp order, then over blocks in block order.
+// Each mode's bin and weight are evaluated once per handle and rule into a
+// 16-bit key table (bin_keys, which also counts the modes per bin), so the
+// per-call pass (bin_sums) is a stream over the two half-spectra and the keys
+// without FP64 square roots or divisions.  A warp takes 32 consecutive modes;
+// a segmented inclusive scan over its lanes (segments = runs of equal bins)
+// leaves each run's sum in the run's last lane, which adds it to the warp's
+// shared-memory histogram: five shuffle steps per 32 modes however many bins
+// they touch.  Accumulation is deterministic: fixed scan shape, runs that
+// share a bin within a warp added in lane order, warp histograms folded per
+// block in warp order, then over blocks in block order.
 #include <cufft.h>
 #include <math.h>
 #include <stdlib.h>
@@ -43,6 +50,7 @@ struct SpecState {
   double *bins;            // [3][nbins] final, per component
   int *counts;             // [nbins] (device)
   int *flag;               // bin overflow flag (device)
+  unsigned short *keys;    // [N][N/2+1][N] bin | weight bit per mode (reference rule)
   int nblocks, nbins;
   double binsize;
   std::vector<int> h_counts;
@@ -51,7 +59,12 @@ struct SpecState {
   int u_nbins;
   double *u_partials, *u_bins;
   int *u_counts;
+  unsigned short *u_keys;
+  std::vector<int> u_h_counts;
 };
+
+constexpr unsigned KEY_WEIGHT2 = 0x8000u;  // the mode is counted twice (py not 0 or N/2)
+constexpr unsigned KEY_BIN = 0x7fffu;
 
 constexpr int SPEC_MAX_UNIFORM_BINS = 1024;  // per-warp histograms in shared memory
 enum { RULE_REFERENCE = 0, RULE_UNIFORM = 1 };
@@ -62,91 +75,134 @@ static double lattice_p(int n, int N, double a) {
   return -2.0 / (a) * sin(n * acos(-1.) / N);
 }
 
-__device__ __forceinline__ double mag2(float2 v) { return (double)v.x * v.x + (double)v.y * v.y; }
-__device__ __forceinline__ double mag2(double2 v) { return v.x * v.x + v.y * v.y; }
-__device__ __forceinline__ double dotre(float2 a, float2 b) { return (double)a.x * b.x + (double)a.y * b.y; }
-__device__ __forceinline__ double dotre(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ float mag2v(float2 v) { return fmaf(v.x, v.x, v.y * v.y); }
+__device__ __forceinline__ double mag2v(double2 v) { return v.x * v.x + v.y * v.y; }
+__device__ __forceinline__ float dotv(float2 a, float2 b) { return fmaf(a.x, b.x, a.y * b.y); }
+__device__ __forceinline__ double dotv(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
 
-// COUNT: only the mode counts (InitBCounts), no field reads.
+// Key of every mode of the reference's mode set, i = px + N (py + M pz) with
+// px in [0,N), py in [0,N/2], pz in [0,N): the bin (bits 0-14) and the
+// weight-2 bit, plus the per-bin mode counts (InitBCounts, momentumspace.cpp:
+// 89-138; per-block shared-memory counts, then one global add per bin).
 // rule RULE_REFERENCE: bin = int(|p| / binsize + 0.5) (momentumspace.cpp:228);
 // rule RULE_UNIFORM: bin = int(|p| / binsize), binsize = p_max / nbins, the
-// top edge folded into the last bin.
-template <typename C, bool COUNT>
-__global__ void __launch_bounds__(SPEC_THREADS) bin_kernel(const C *__restrict__ fphi, const C *__restrict__ fpi,
-                                                          const double *__restrict__ ptab, int N, double binsize,
-                                                          int nbins, int rule, double scale,
-                                                          double *__restrict__ partials, int *__restrict__ counts,
-                                                          int *__restrict__ flag) {
+// top edge folded into the last bin.  |p| in FP64 as the reference writes it.
+__global__ void __launch_bounds__(SPEC_THREADS) bin_keys(const double *__restrict__ ptab, int N, double binsize,
+                                                        int nbins, int rule, unsigned short *__restrict__ keys,
+                                                        int *__restrict__ counts, int *__restrict__ flag) {
+  extern __shared__ int cnt[];  // [nbins]
+  for (int b = threadIdx.x; b < nbins; b += SPEC_THREADS) cnt[b] = 0;
+  __syncthreads();
+  const int h = N / 2, M = N / 2 + 1;
+  const long long total = (long long)N * M * N;
+  for (long long i = blockIdx.x * (long long)SPEC_THREADS + threadIdx.x; i < total;
+       i += (long long)gridDim.x * SPEC_THREADS) {
+    const int px = (int)(i % N);
+    const long long t = i / N;
+    const int py = (int)(t % M);
+    const int pz = (int)(t / M);
+    const double ppx = ptab[px], ppy = ptab[py], nu = ptab[pz];
+    const double psqr = __dadd_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)), __dmul_rn(nu, nu));
+    int bin;
+    if (rule == RULE_REFERENCE) {
+      bin = (int)(__dadd_rn(sqrt(psqr) / binsize, 0.5));
+    } else {
+      bin = (int)(sqrt(psqr) / binsize);
+      if (bin >= nbins) bin = nbins - 1;
+    }
+    const bool two = py != 0 && py != h;
+    if (bin >= nbins || bin > (int)KEY_BIN) {
+      atomicOr(flag, 1);
+      keys[i] = (unsigned short)KEY_BIN;
+    } else {
+      keys[i] = (unsigned short)(bin | (two ? KEY_WEIGHT2 : 0u));
+      atomicAdd(&cnt[bin], two ? 2 : 1);
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += SPEC_THREADS)
+    if (cnt[b]) atomicAdd(&counts[b], cnt[b]);
+}
+
+// Per-call sums: F += w |Phi_p|^2, K += w |Pi_p|^2, Q += w Re(Phi_p Pi_p*)
+// (momentumspace.cpp:222-240) for every mode, binned by its key; the
+// reference's a^3 a^3 factor is applied in fold_blocks.  A mode with
+// px <= N/2 is read directly from cuFFT's [pz][py][px/2+1] half-spectrum, one
+// with px > N/2 from its conjugate partner (N-px, -py, -pz).  V: the scan's
+// arithmetic, float for FP32 spectra, double for FP64.
+template <typename C, typename V>
+__global__ void __launch_bounds__(SPEC_THREADS) bin_sums(const C *__restrict__ fphi, const C *__restrict__ fpi,
+                                                        const unsigned short *__restrict__ keys, int N, int nbins,
+                                                        double *__restrict__ partials) {
   extern __shared__ double hist[];  // [SPEC_WARPS][3][nbins]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < SPEC_WARPS * 3 * nbins; i += SPEC_THREADS) hist[i] = 0.0;
   __syncthreads();
   double *hF = hist + (size_t)warp * 3 * nbins, *hK = hF + nbins, *hQ = hK + nbins;
+  const unsigned full = 0xffffffffu;
   const int h = N / 2, M = N / 2 + 1;
   const long long total = (long long)N * M * N;
-  const long long stride = (long long)gridDim.x * SPEC_THREADS;
-  // uniform trip count across the warp so that warp collectives stay converged
-  const long long iters = (total + stride - 1) / stride;
-  for (long long it = 0; it < iters; ++it) {
-    const long long i = it * stride + (long long)blockIdx.x * SPEC_THREADS + threadIdx.x;
-    int key = -1;
-    double f = 0.0, k = 0.0, q = 0.0;
+  const long long nchunks = (total + 31) / 32;
+  const long long nw = (long long)gridDim.x * SPEC_WARPS;
+  // chunk loop: uniform per warp, so every lane takes part in the collectives
+  for (long long c = (long long)blockIdx.x * SPEC_WARPS + warp; c < nchunks; c += nw) {
+    const long long i = c * 32 + lane;
+    int bin = -1;  // lanes past the end: a segment that is never written
+    V f = 0, k = 0, q = 0;
     if (i < total) {
+      const unsigned key = keys[i];
+      bin = (int)(key & KEY_BIN);
       const int px = (int)(i % N);
       const long long t = i / N;
       const int py = (int)(t % M);
       const int pz = (int)(t / M);
-      const double ppx = ptab[px], ppy = ptab[py], nu = ptab[pz];
-      const double psqr = __dadd_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)), __dmul_rn(nu, nu));
-      int bin;
-      if (rule == RULE_REFERENCE) {
-        bin = (int)(__dadd_rn(sqrt(psqr) / binsize, 0.5));
-      } else {
-        bin = (int)(sqrt(psqr) / binsize);
-        if (bin >= nbins) bin = nbins - 1;
-      }
-      const int w = (py != 0 && py != h) ? 2 : 1;
-      if (bin >= nbins) {
-        atomicOr(flag, 1);
-      } else if (COUNT) {
-        atomicAdd(&counts[bin], w);
-      } else {
-        long long m;
-        if (px <= h)
-          m = ((long long)pz * N + py) * M + px;
-        else
-          m = ((long long)((N - pz) % N) * N + (N - py) % N) * M + (N - px);
-        const C a = fphi[m], b = fpi[m];
-        key = bin;
-        f = w * mag2(a) * scale;
-        k = w * mag2(b) * scale;
-        q = w * dotre(a, b) * scale;
+      const long long m = px <= h ? ((long long)pz * N + py) * M + px
+                                  : ((long long)((N - pz) % N) * N + (N - py) % N) * M + (N - px);
+      const C a = fphi[m], b = fpi[m];
+      f = mag2v(a);
+      k = mag2v(b);
+      q = dotv(a, b);
+      if (key & KEY_WEIGHT2) {  // exact doubling
+        f += f;
+        k += k;
+        q += q;
       }
     }
-    if (COUNT) continue;
-    unsigned todo = __ballot_sync(0xffffffffu, key >= 0);
-    while (todo) {
-      const int src = __ffs(todo) - 1;
-      const int b = __shfl_sync(0xffffffffu, key, src);
-      const bool mine = (key == b);
-      const unsigned grp = __ballot_sync(0xffffffffu, mine);
-      double vf = mine ? f : 0.0, vk = mine ? k : 0.0, vq = mine ? q : 0.0;
+    // segmented inclusive scan: a segment is a run of lanes with one bin
+    const int prev = __shfl_up_sync(full, bin, 1);
+    const unsigned heads = __ballot_sync(full, lane == 0 || prev != bin);
+    const int start = 31 - __clz(heads & (full >> (31 - lane)));  // first lane of my segment
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        vf += __shfl_xor_sync(0xffffffffu, vf, off);
-        vk += __shfl_xor_sync(0xffffffffu, vk, off);
-        vq += __shfl_xor_sync(0xffffffffu, vq, off);
+    for (int off = 1; off < 32; off <<= 1) {
+      const V uf = __shfl_up_sync(full, f, off), uk = __shfl_up_sync(full, k, off), uq = __shfl_up_sync(full, q, off);
+      if (lane - off >= start) {
+        f += uf;
+        k += uk;
+        q += uq;
       }
-      if (lane == src) {
-        hF[b] += vf;
-        hK[b] += vk;
-        hQ[b] += vq;
-      }
-      todo &= ~grp;
-      __syncwarp();
     }
+    // the last lane of each segment holds the segment's sum
+    const int next = __shfl_down_sync(full, bin, 1);
+    const bool tail = (lane == 31 || next != bin) && bin >= 0;
+    const unsigned same = __match_any_sync(full, tail ? bin : -2 - lane);
+    if (!__any_sync(full, tail && __popc(same) > 1)) {
+      if (tail) {  // distinct bins: one store each
+        hF[bin] += (double)f;
+        hK[bin] += (double)k;
+        hQ[bin] += (double)q;
+      }
+    } else {  // runs sharing a bin (the mirror turn at px = N/2, a row change): in lane order
+      for (unsigned tails = __ballot_sync(full, tail); tails; tails &= tails - 1) {
+        if (lane == __ffs(tails) - 1) {
+          hF[bin] += (double)f;
+          hK[bin] += (double)k;
+          hQ[bin] += (double)q;
+        }
+        __syncwarp();
+      }
+    }
+    __syncwarp();
   }
-  if (COUNT) return;
   __syncthreads();
   // fold the warp histograms in warp order; one record per block
   for (int j = threadIdx.x; j < 3 * nbins; j += SPEC_THREADS) {
@@ -156,11 +212,12 @@ __global__ void __launch_bounds__(SPEC_THREADS) bin_kernel(const C *__restrict__
   }
 }
 
-__global__ void fold_blocks(const double *__restrict__ partials, int nblocks, int nbins, double *__restrict__ out) {
+__global__ void fold_blocks(const double *__restrict__ partials, int nblocks, int nbins, double scale,
+                            double *__restrict__ out) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 3 * nbins; j += gridDim.x * blockDim.x) {
     double s = 0.0;
     for (int b = 0; b < nblocks; ++b) s += partials[(size_t)b * 3 * nbins + j];
-    out[j] = s;
+    out[j] = s * scale;
   }
 }
 
@@ -175,9 +232,11 @@ void spectrum_release(phn_handle *h) {
   cudaFree(s->bins);
   cudaFree(s->counts);
   cudaFree(s->flag);
+  cudaFree(s->keys);
   cudaFree(s->u_partials);
   cudaFree(s->u_bins);
   cudaFree(s->u_counts);
+  cudaFree(s->u_keys);
   delete s;
   h->spec = nullptr;
 }
@@ -188,6 +247,30 @@ static void bin_geometry(const phn_params &p, int *nbins, double *binsize) {
   const double pTmax = sqrt(3.0 * (4.0 / (p.a * p.a)));
   *binsize = pTmin;
   *nbins = (int)(pTmax / pTmin + 0.5) + 2;
+}
+
+static size_t n_modes(int N) { return (size_t)N * (N / 2 + 1) * N; }
+
+// Key table and mode counts of one rule (bin_keys), counts copied to host.
+static int build_keys(phn_handle *h, unsigned short *keys, int *counts, int nbins, double binsize, int rule,
+                      std::vector<int> &h_counts) {
+  SpecState *s = (SpecState *)h->spec;
+  cudaError_t e = cudaMemsetAsync(counts, 0, nbins * sizeof(int), h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->flag, 0, sizeof(int), h->stream);
+  if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
+  bin_keys<<<s->nblocks, SPEC_THREADS, nbins * sizeof(int), h->stream>>>(s->ptab, h->p.N, binsize, nbins, rule, keys,
+                                                                          counts, s->flag);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "bin_keys");
+  h->launches++;
+  h_counts.resize(nbins);
+  int flag = 0;
+  e = cudaMemcpyAsync(h_counts.data(), counts, nbins * sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_error(e, "mode counts");
+  if (flag) return set_error(PHN_ERR_INVALID, "bin array too small (momentumspace.cpp:128)");
+  return PHN_OK;
 }
 
 static int spec_init(phn_handle *h) {
@@ -213,6 +296,7 @@ static int spec_init(phn_handle *h) {
   CKS(cudaMalloc(&s->bins, (size_t)3 * s->nbins * sizeof(double)));
   CKS(cudaMalloc(&s->counts, (size_t)s->nbins * sizeof(int)));
   CKS(cudaMalloc(&s->flag, sizeof(int)));
+  CKS(cudaMalloc(&s->keys, n_modes(N) * sizeof(unsigned short)));
   std::vector<double> tab(N);
   for (int n = 0; n < N; ++n) tab[n] = lattice_p(n, N, h->p.a);
   CKS(cudaMemcpy(s->ptab, tab.data(), N * sizeof(double), cudaMemcpyHostToDevice));
@@ -220,27 +304,52 @@ static int spec_init(phn_handle *h) {
     return set_error(PHN_ERR_CUDA, "cufftPlan3d(%d^3) failed", N);
   s->plan_ok = true;
   if (cufftSetStream(s->plan, h->stream) != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cufftSetStream failed");
-  const size_t smem = (size_t)SPEC_WARPS * 3 * s->nbins * sizeof(double);
   // the largest histogram either rule uses
-  const size_t smem_max = (size_t)SPEC_WARPS * 3 * (s->nbins > SPEC_MAX_UNIFORM_BINS ? s->nbins : SPEC_MAX_UNIFORM_BINS) *
-                          sizeof(double);
-  CKS(cudaFuncSetAttribute(bin_kernel<float2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
-  CKS(cudaFuncSetAttribute(bin_kernel<double2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
-  CKS(cudaFuncSetAttribute(bin_kernel<float2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
-  // mode counts (InitBCounts, momentumspace.cpp:89-138): field independent
-  CKS(cudaMemsetAsync(s->counts, 0, s->nbins * sizeof(int), h->stream));
-  CKS(cudaMemsetAsync(s->flag, 0, sizeof(int), h->stream));
-  bin_kernel<float2, true><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-      nullptr, nullptr, s->ptab, N, s->binsize, s->nbins, RULE_REFERENCE, 0.0, nullptr, s->counts, s->flag);
-  CKS(cudaGetLastError());
-  h->launches++;
-  s->h_counts.resize(s->nbins);
-  int flag = 0;
-  CKS(cudaMemcpyAsync(s->h_counts.data(), s->counts, s->nbins * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-  CKS(cudaMemcpyAsync(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-  CKS(cudaStreamSynchronize(h->stream));
-  if (flag) return set_error(PHN_ERR_INVALID, "bin array too small (momentumspace.cpp:128)");
+  const int maxb = s->nbins > SPEC_MAX_UNIFORM_BINS ? s->nbins : SPEC_MAX_UNIFORM_BINS;
+  const size_t smem_max = (size_t)SPEC_WARPS * 3 * maxb * sizeof(double);
+  CKS(cudaFuncSetAttribute(bin_sums<float2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+  CKS(cudaFuncSetAttribute(bin_sums<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+  CKS(cudaFuncSetAttribute(bin_keys, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(maxb * sizeof(int))));
 #undef CKS
+  // keys and mode counts of the reference rule (InitBCounts): field independent
+  return build_keys(h, s->keys, s->counts, s->nbins, s->binsize, RULE_REFERENCE, s->h_counts);
+}
+
+// One component: R2C of phi and pi, the binned sums, the three bin arrays
+// into hb ([3][nbins], scaled by a^3 a^3).
+static int spectrum_component(phn_handle *h, int a, const unsigned short *keys, int nbins, double *partials,
+                              double *bins, double scale, std::vector<double> &hb) {
+  SpecState *s = (SpecState *)h->spec;
+  const int N = h->p.N;
+  const bool dbl = h->p.precision == PHN_FP64;
+  cufftResult fr;
+  if (dbl) {
+    double *phi = (double *)h->phi[h->cur] + (size_t)a * h->V, *pi = (double *)h->pi + (size_t)a * h->V;
+    fr = cufftExecD2Z(s->plan, phi, (cufftDoubleComplex *)s->fphi);
+    if (fr == CUFFT_SUCCESS) fr = cufftExecD2Z(s->plan, pi, (cufftDoubleComplex *)s->fpi);
+  } else {
+    float *phi = (float *)h->phi[h->cur] + (size_t)a * h->V, *pi = (float *)h->pi + (size_t)a * h->V;
+    fr = cufftExecR2C(s->plan, phi, (cufftComplex *)s->fphi);
+    if (fr == CUFFT_SUCCESS) fr = cufftExecR2C(s->plan, pi, (cufftComplex *)s->fpi);
+  }
+  if (fr != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cuFFT exec failed (%d)", (int)fr);
+  const size_t smem = (size_t)SPEC_WARPS * 3 * nbins * sizeof(double);
+  if (dbl)
+    bin_sums<double2, double><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
+        (const double2 *)s->fphi, (const double2 *)s->fpi, keys, N, nbins, partials);
+  else
+    bin_sums<float2, float><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
+        (const float2 *)s->fphi, (const float2 *)s->fpi, keys, N, nbins, partials);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "bin_sums");
+  fold_blocks<<<(3 * nbins + 255) / 256, 256, 0, h->stream>>>(partials, s->nblocks, nbins, scale, bins);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "fold_blocks");
+  h->launches += 2;
+  hb.resize((size_t)3 * nbins);
+  e = cudaMemcpyAsync(hb.data(), bins, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_error(e, "spectrum readback");
   return PHN_OK;
 }
 
@@ -269,46 +378,17 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
   }
   SpecState *s = (SpecState *)h->spec;
   if (nbins < s->nbins) return set_error(PHN_ERR_TRUNCATED, "nbins=%d < %d", nbins, s->nbins);
-  const int N = h->p.N, Nc = h->p.Nc;
-  const bool dbl = h->p.precision == PHN_FP64;
+  const int Nc = h->p.Nc;
   const double f3 = (h->p.a * h->p.a) * h->p.a;  // fftXtoP_direct's a^3 (clusterfft.cpp:187,222)
-  const double scale = f3 * f3;
-  const size_t smem = (size_t)SPEC_WARPS * 3 * s->nbins * sizeof(double);
-  std::vector<double> hb((size_t)3 * s->nbins);
+  std::vector<double> hb;
   for (int k = 0; k < s->nbins * Nc; ++k) {
     if (F) F[k] = 0.0;
     if (K) K[k] = 0.0;
     if (Q) Q[k] = 0.0;
   }
   for (int a = 0; a < Nc; ++a) {
-    cufftResult fr;
-    if (dbl) {
-      double *phi = (double *)h->phi[h->cur] + (size_t)a * h->V, *pi = (double *)h->pi + (size_t)a * h->V;
-      fr = cufftExecD2Z(s->plan, phi, (cufftDoubleComplex *)s->fphi);
-      if (fr == CUFFT_SUCCESS) fr = cufftExecD2Z(s->plan, pi, (cufftDoubleComplex *)s->fpi);
-    } else {
-      float *phi = (float *)h->phi[h->cur] + (size_t)a * h->V, *pi = (float *)h->pi + (size_t)a * h->V;
-      fr = cufftExecR2C(s->plan, phi, (cufftComplex *)s->fphi);
-      if (fr == CUFFT_SUCCESS) fr = cufftExecR2C(s->plan, pi, (cufftComplex *)s->fpi);
-    }
-    if (fr != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cuFFT exec failed (%d)", (int)fr);
-    if (dbl)
-      bin_kernel<double2, false><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-          (const double2 *)s->fphi, (const double2 *)s->fpi, s->ptab, N, s->binsize, s->nbins, RULE_REFERENCE, scale,
-          s->partials, nullptr, s->flag);
-    else
-      bin_kernel<float2, false><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-          (const float2 *)s->fphi, (const float2 *)s->fpi, s->ptab, N, s->binsize, s->nbins, RULE_REFERENCE, scale,
-          s->partials, nullptr, s->flag);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_error(e, "bin_kernel");
-    fold_blocks<<<(3 * s->nbins + 255) / 256, 256, 0, h->stream>>>(s->partials, s->nblocks, s->nbins, s->bins);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_error(e, "fold_blocks");
-    h->launches += 2;
-    e = cudaMemcpyAsync(hb.data(), s->bins, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    if (e != cudaSuccess) return cuda_error(e, "spectrum readback");
+    r = spectrum_component(h, a, s->keys, s->nbins, s->partials, s->bins, f3 * f3, hb);
+    if (r) return r;
     for (int b = 0; b < s->nbins; ++b) {
       if (F) F[b * Nc + a] = hb[b];
       if (K) K[b * Nc + a] = hb[s->nbins + b];
@@ -331,77 +411,39 @@ int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double 
   }
   SpecState *s = (SpecState *)h->spec;
   const int N = h->p.N, Nc = h->p.Nc;
-  const bool dbl = h->p.precision == PHN_FP64;
-  cudaError_t e;
+  // p_max = pTmax of momentumspace.cpp:43, the largest lattice |p|
+  const double pmax = sqrt(3.0 * (4.0 / (h->p.a * h->p.a)));
   if (s->u_nbins != nbins) {
     cudaFree(s->u_partials);
     cudaFree(s->u_bins);
     cudaFree(s->u_counts);
+    cudaFree(s->u_keys);
     s->u_partials = s->u_bins = nullptr;
     s->u_counts = nullptr;
+    s->u_keys = nullptr;
     s->u_nbins = 0;
-    e = cudaMalloc(&s->u_partials, (size_t)s->nblocks * 3 * nbins * sizeof(double));
+    cudaError_t e = cudaMalloc(&s->u_partials, (size_t)s->nblocks * 3 * nbins * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&s->u_bins, (size_t)3 * nbins * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&s->u_counts, (size_t)nbins * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->u_keys, n_modes(N) * sizeof(unsigned short));
     if (e != cudaSuccess) return cuda_error(e, "uniform spectrum buffers");
+    r = build_keys(h, s->u_keys, s->u_counts, nbins, pmax / nbins, RULE_UNIFORM, s->u_h_counts);
+    if (r) return r;
     s->u_nbins = nbins;
   }
-  // p_max = pTmax of momentumspace.cpp:43, the largest lattice |p|
-  const double pmax = sqrt(3.0 * (4.0 / (h->p.a * h->p.a)));
-  const double width = pmax / nbins;
   const double f3 = (h->p.a * h->p.a) * h->p.a;
-  const double scale = f3 * f3;
-  const size_t smem = (size_t)SPEC_WARPS * 3 * nbins * sizeof(double);
-  std::vector<int> hc(nbins);
-  e = cudaMemsetAsync(s->u_counts, 0, nbins * sizeof(int), h->stream);
-  if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
-  bin_kernel<float2, true><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-      nullptr, nullptr, s->ptab, N, width, nbins, RULE_UNIFORM, 0.0, nullptr, s->u_counts, s->flag);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_error(e, "bin_kernel (counts)");
-  h->launches++;
-  e = cudaMemcpyAsync(hc.data(), s->u_counts, nbins * sizeof(int), cudaMemcpyDeviceToHost, h->stream);
-  if (e != cudaSuccess) return cuda_error(e, "counts readback");
-  std::vector<double> hb((size_t)3 * nbins);
+  std::vector<double> hb;
   for (int a = 0; a < Nc; ++a) {
-    cufftResult fr;
-    if (dbl) {
-      double *phi = (double *)h->phi[h->cur] + (size_t)a * h->V, *pi = (double *)h->pi + (size_t)a * h->V;
-      fr = cufftExecD2Z(s->plan, phi, (cufftDoubleComplex *)s->fphi);
-      if (fr == CUFFT_SUCCESS) fr = cufftExecD2Z(s->plan, pi, (cufftDoubleComplex *)s->fpi);
-    } else {
-      float *phi = (float *)h->phi[h->cur] + (size_t)a * h->V, *pi = (float *)h->pi + (size_t)a * h->V;
-      fr = cufftExecR2C(s->plan, phi, (cufftComplex *)s->fphi);
-      if (fr == CUFFT_SUCCESS) fr = cufftExecR2C(s->plan, pi, (cufftComplex *)s->fpi);
-    }
-    if (fr != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cuFFT exec failed (%d)", (int)fr);
-    if (dbl)
-      bin_kernel<double2, false><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-          (const double2 *)s->fphi, (const double2 *)s->fpi, s->ptab, N, width, nbins, RULE_UNIFORM, scale,
-          s->u_partials, nullptr, s->flag);
-    else
-      bin_kernel<float2, false><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-          (const float2 *)s->fphi, (const float2 *)s->fpi, s->ptab, N, width, nbins, RULE_UNIFORM, scale,
-          s->u_partials, nullptr, s->flag);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_error(e, "bin_kernel");
-    fold_blocks<<<(3 * nbins + 255) / 256, 256, 0, h->stream>>>(s->u_partials, s->nblocks, nbins, s->u_bins);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_error(e, "fold_blocks");
-    h->launches += 2;
-    e = cudaMemcpyAsync(hb.data(), s->u_bins, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    if (e != cudaSuccess) return cuda_error(e, "spectrum readback");
+    r = spectrum_component(h, a, s->u_keys, nbins, s->u_partials, s->u_bins, f3 * f3, hb);
+    if (r) return r;
     for (int b = 0; b < nbins; ++b) {
       if (F) F[b * Nc + a] = hb[b];
       if (K) K[b * Nc + a] = hb[nbins + b];
       if (Q) Q[b * Nc + a] = hb[2 * nbins + b];
     }
   }
-  e = cudaStreamSynchronize(h->stream);
-  if (e != cudaSuccess) return cuda_error(e, "spectrum readback");
   if (counts)
-    for (int b = 0; b < nbins; ++b) counts[b] = hc[b];
+    for (int b = 0; b < nbins; ++b) counts[b] = s->u_h_counts[b];
   return PHN_OK;
 }
 

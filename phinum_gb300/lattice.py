@@ -193,7 +193,7 @@ class Lattice:
         r = self.lib.phn_islands(self.h, float(thres), int(mode), int(bool(z_periodic)),
                                  _pi(lab) if labels else None, _pd(recs), max_out, ctypes.byref(n))
         L.check(r)
-        return lab, recs[:n.value].copy()
+        return lab, recs if n.value == max_out else recs[:n.value].copy()
 
     def stats(self):
         n, ms, st = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_int()
