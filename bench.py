@@ -312,6 +312,7 @@ def measure_gpu(args, dist: Dist):
     e2e_burst(3)
     if not args.quick:
         also["ensemble_c3"] = measure_ensemble(2000, 100)
+        also["analysis"] = analysis_form(N, precisions=("fp32",))["fp32"]
     e2e_burst(3)
     e2e_close()
     out["also"] = also
@@ -594,7 +595,7 @@ def initial_form(N: int, n_cpu: int = 128, n_check: int = 64):
     return out
 
 
-def analysis_form(N: int, reps: int = 5, steps: int = 200):
+def analysis_form(N: int, reps: int = 5, steps: int = 200, precisions=("fp32", "fp64")):
     """The analysis passes of the hot path on the bench's 512^3 phi^6 lattice
     after `steps` FP32 steps, wall time per call (the calls return host
     results, so each ends synchronised), median of `reps` after a warm-up:
@@ -618,6 +619,8 @@ def analysis_form(N: int, reps: int = 5, steps: int = 200):
         return float(np.median(ts)) * 1e3, r
 
     for name, prec in (("fp32", L.FP32), ("fp64", L.FP64)):
+        if name not in precisions:
+            continue
         lat = PL.Lattice(PL.Params(N=N, precision=prec))
         lat.upload(phi, pi)
         lat.evolve(steps)
