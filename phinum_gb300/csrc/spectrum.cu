@@ -32,6 +32,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <type_traits>
 #include <vector>
 
 #include "phn_internal.h"
@@ -130,84 +131,120 @@ __global__ void __launch_bounds__(SPEC_THREADS) bin_keys(const double *__restric
 // px <= N/2 is read directly from cuFFT's [pz][py][px/2+1] half-spectrum, one
 // with px > N/2 from its conjugate partner (N-px, -py, -pz).  V: the scan's
 // arithmetic, float for FP32 spectra, double for FP64.
+// Histogram cell of the warp histograms: FP64 for FP64 spectra; for FP32
+// spectra a compensated FP32 pair (Kahan: value = s - c), so that the FP32
+// pass issues no FP64 instruction (GB300's FP64 rate bound it) and still
+// keeps ~2^-48 of the sum.
+struct CompF {
+  float s, c;
+};
+__device__ __forceinline__ void hist_add(double &h, double v) { h += v; }
+__device__ __forceinline__ void hist_add(CompF &h, float v) {
+  const float y = __fsub_rn(v, h.c);
+  const float t = __fadd_rn(h.s, y);
+  h.c = __fsub_rn(__fsub_rn(t, h.s), y);
+  h.s = t;
+}
+__device__ __forceinline__ double hist_value(double h) { return h; }
+__device__ __forceinline__ double hist_value(CompF h) { return (double)h.s - (double)h.c; }
+__device__ __forceinline__ void hist_zero(double &h) { h = 0.0; }
+__device__ __forceinline__ void hist_zero(CompF &h) { h.s = h.c = 0.f; }
+
 template <typename C, typename V>
 __global__ void __launch_bounds__(SPEC_THREADS) bin_sums(const C *__restrict__ fphi, const C *__restrict__ fpi,
                                                         const unsigned short *__restrict__ keys, int N, int nbins,
                                                         double *__restrict__ partials) {
-  extern __shared__ double hist[];  // [SPEC_WARPS][3][nbins]
+  using H = typename std::conditional<sizeof(V) == 4, CompF, double>::type;
+  extern __shared__ double hist_mem[];
+  H *hist = (H *)hist_mem;  // [SPEC_WARPS][3][nbins]: 8 bytes per cell either way
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < SPEC_WARPS * 3 * nbins; i += SPEC_THREADS) hist[i] = 0.0;
+  for (int i = threadIdx.x; i < SPEC_WARPS * 3 * nbins; i += SPEC_THREADS) hist_zero(hist[i]);
   __syncthreads();
-  double *hF = hist + (size_t)warp * 3 * nbins, *hK = hF + nbins, *hQ = hK + nbins;
+  H *hF = hist + (size_t)warp * 3 * nbins, *hK = hF + nbins, *hQ = hK + nbins;
   const unsigned full = 0xffffffffu;
   const int h = N / 2, M = N / 2 + 1;
-  const long long total = (long long)N * M * N;
-  const long long nchunks = (total + 31) / 32;
-  const long long nw = (long long)gridDim.x * SPEC_WARPS;
-  // chunk loop: uniform per warp, so every lane takes part in the collectives
-  for (long long c = (long long)blockIdx.x * SPEC_WARPS + warp; c < nchunks; c += nw) {
-    const long long i = c * 32 + lane;
-    int bin = -1;  // lanes past the end: a segment that is never written
-    V f = 0, k = 0, q = 0;
-    if (i < total) {
-      const unsigned key = keys[i];
-      bin = (int)(key & KEY_BIN);
-      const int px = (int)(i % N);
-      const long long t = i / N;
-      const int py = (int)(t % M);
-      const int pz = (int)(t / M);
-      const long long m = px <= h ? ((long long)pz * N + py) * M + px
-                                  : ((long long)((N - pz) % N) * N + (N - py) % N) * M + (N - px);
-      const C a = fphi[m], b = fpi[m];
-      f = mag2v(a);
-      k = mag2v(b);
-      q = dotv(a, b);
-      if (key & KEY_WEIGHT2) {  // exact doubling
-        f += f;
-        k += k;
-        q += q;
-      }
-    }
-    // segmented inclusive scan: a segment is a run of lanes with one bin
-    const int prev = __shfl_up_sync(full, bin, 1);
-    const unsigned heads = __ballot_sync(full, lane == 0 || prev != bin);
-    const int start = 31 - __clz(heads & (full >> (31 - lane)));  // first lane of my segment
+  const int nrows = M * N;
+  // a warp walks whole rows (py, pz) of the mode set, 32 px at a time: the
+  // row's offsets are computed once, px comes from the lane (no 64-bit
+  // division per mode); the loads of UNROLL chunks are issued together
+  constexpr int UNROLL = sizeof(V) == 4 ? 4 : 2;
+  for (int row = blockIdx.x * SPEC_WARPS + warp; row < nrows; row += gridDim.x * SPEC_WARPS) {
+    const int py = row % M, pz = row / M;
+    const long long krow = (long long)row * N;                                         // key index of px = 0
+    const long long direct = ((long long)pz * N + py) * M;                              // + px, px <= N/2
+    const long long mirror = ((long long)((N - pz) % N) * N + (N - py) % N) * M + N;  // - px, px > N/2
+    for (int px0 = 0; px0 < N; px0 += 32 * UNROLL) {
+      unsigned kk[UNROLL];
+      C va[UNROLL], vb[UNROLL];
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const V uf = __shfl_up_sync(full, f, off), uk = __shfl_up_sync(full, k, off), uq = __shfl_up_sync(full, q, off);
-      if (lane - off >= start) {
-        f += uf;
-        k += uk;
-        q += uq;
+      for (int u = 0; u < UNROLL; ++u) {
+        const int px = px0 + 32 * u + lane;
+        kk[u] = 0xffffffffu;  // past the row's end
+        if (px < N) {
+          kk[u] = keys[krow + px];
+          const long long m = px <= h ? direct + px : mirror - px;
+          va[u] = fphi[m];
+          vb[u] = fpi[m];
+        }
       }
-    }
-    // the last lane of each segment holds the segment's sum
-    const int next = __shfl_down_sync(full, bin, 1);
-    const bool tail = (lane == 31 || next != bin) && bin >= 0;
-    const unsigned same = __match_any_sync(full, tail ? bin : -2 - lane);
-    if (!__any_sync(full, tail && __popc(same) > 1)) {
-      if (tail) {  // distinct bins: one store each
-        hF[bin] += (double)f;
-        hK[bin] += (double)k;
-        hQ[bin] += (double)q;
-      }
-    } else {  // runs sharing a bin (the mirror turn at px = N/2, a row change): in lane order
-      for (unsigned tails = __ballot_sync(full, tail); tails; tails &= tails - 1) {
-        if (lane == __ffs(tails) - 1) {
-          hF[bin] += (double)f;
-          hK[bin] += (double)k;
-          hQ[bin] += (double)q;
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        int bin = -1;  // lanes past the end: a segment that is never written
+        V f = 0, k = 0, q = 0;
+        if (kk[u] != 0xffffffffu) {
+          bin = (int)(kk[u] & KEY_BIN);
+          f = mag2v(va[u]);
+          k = mag2v(vb[u]);
+          q = dotv(va[u], vb[u]);
+          if (kk[u] & KEY_WEIGHT2) {  // exact doubling
+            f += f;
+            k += k;
+            q += q;
+          }
+        }
+        // segmented inclusive scan: a segment is a run of lanes with one bin
+        const int prev = __shfl_up_sync(full, bin, 1);
+        const unsigned heads = __ballot_sync(full, lane == 0 || prev != bin);
+        const int start = 31 - __clz(heads & (full >> (31 - lane)));  // first lane of my segment
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const V uf = __shfl_up_sync(full, f, off), uk = __shfl_up_sync(full, k, off),
+                  uq = __shfl_up_sync(full, q, off);
+          if (lane - off >= start) {
+            f += uf;
+            k += uk;
+            q += uq;
+          }
+        }
+        // the last lane of each segment holds the segment's sum
+        const int next = __shfl_down_sync(full, bin, 1);
+        const bool tail = (lane == 31 || next != bin) && bin >= 0;
+        const unsigned same = __match_any_sync(full, tail ? bin : -2 - lane);
+        if (!__any_sync(full, tail && __popc(same) > 1)) {
+          if (tail) {  // distinct bins: one update each
+            hist_add(hF[bin], f);
+            hist_add(hK[bin], k);
+            hist_add(hQ[bin], q);
+          }
+        } else {  // runs sharing a bin (the mirror turn at px = N/2, a row change): in lane order
+          for (unsigned tails = __ballot_sync(full, tail); tails; tails &= tails - 1) {
+            if (lane == __ffs(tails) - 1) {
+              hist_add(hF[bin], f);
+              hist_add(hK[bin], k);
+              hist_add(hQ[bin], q);
+            }
+            __syncwarp();
+          }
         }
         __syncwarp();
       }
     }
-    __syncwarp();
   }
   __syncthreads();
   // fold the warp histograms in warp order; one record per block
   for (int j = threadIdx.x; j < 3 * nbins; j += SPEC_THREADS) {
     double s = 0.0;
-    for (int w = 0; w < SPEC_WARPS; ++w) s += hist[(size_t)w * 3 * nbins + j];
+    for (int w = 0; w < SPEC_WARPS; ++w) s += hist_value(hist[(size_t)w * 3 * nbins + j]);
     partials[(size_t)blockIdx.x * 3 * nbins + j] = s;
   }
 }
