@@ -253,19 +253,24 @@ def measure_gpu(args, dist: Dist):
     hphi, hpi = np.empty_like(phi), np.empty_like(pi)
     for a in (hphi, hpi):
         L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
-    its = []
+    its, phases = [], []
 
     def e2e_iter():
+        t0 = time.perf_counter()
         elat.upload(phi, pi)
+        t1 = time.perf_counter()
         elat.run_loop(TSO_STEPS, 1.0, max_rows=2)
+        t2 = time.perf_counter()
         L.check(lib.phn_download(elat.h, hphi.ctypes.data_as(L._PD), hpi.ctypes.data_as(L._PD)))
+        t3 = time.perf_counter()
+        return t3 - t0, (t1 - t0, t2 - t1, t3 - t2)
 
     def e2e_burst(n):
         dist.barrier()
         for _ in range(n):
-            t0 = time.perf_counter()
-            e2e_iter()
-            its.append(time.perf_counter() - t0)
+            t, ph = e2e_iter()
+            its.append(t)
+            phases.append(ph)
 
     def e2e_close():
         # per-iteration wall times, in three bursts (here, after the other
@@ -276,15 +281,40 @@ def measure_gpu(args, dist: Dist):
                       "h2d_bytes_per_step": int(phi.nbytes + pi.nbytes),
                       "d2h_bytes_per_step": int(hphi.nbytes + hpi.nbytes + 26 * 8),
                       "iteration_s": {"median": float(np.median(its)), "min": float(min(its)),
-                                      "max": float(max(its)), "n": len(its), "all": [round(t, 4) for t in its]},
+                                      "max": float(max(its)), "n": len(its), "all": [round(t, 4) for t in its],
+                                      "upload_steps_download": [[round(x, 4) for x in ph] for ph in phases]},
                       "step": f"upload phi,pi (FP64 reference layout) + {TSO_STEPS} leapfrog steps with one fused "
-                              "SO row + download phi,pi"}
+                              "SO row + download phi,pi",
+                      "f32_host": e2e_f32}
         for a in (phi, pi, hphi, hpi):
             lib.phn_unpin_host(a.ctypes.data)
         elat.close()
 
     e2e_iter()  # warm-up
     e2e_burst(3 if not (args.no_extra and args.quick) else 9)
+
+    # the same with the reference's single-precision host layout (float
+    # arrays, phn_upload_f32 / phn_download_f32): half the bytes on the link
+    phi32, pi32 = phi.astype(np.float32), pi.astype(np.float32)
+    hphi32, hpi32 = np.empty_like(phi32), np.empty_like(pi32)
+    for a in (phi32, pi32, hphi32, hpi32):
+        L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
+    its32 = []
+    for it in range(4):
+        t0 = time.perf_counter()
+        L.check(lib.phn_upload_f32(elat.h, phi32.ctypes.data, pi32.ctypes.data))
+        elat.run_loop(TSO_STEPS, 1.0, max_rows=2)
+        L.check(lib.phn_download_f32(elat.h, hphi32.ctypes.data, hpi32.ctypes.data))
+        if it:
+            its32.append(time.perf_counter() - t0)
+    for a in (phi32, pi32, hphi32, hpi32):
+        lib.phn_unpin_host(a.ctypes.data)
+    e2e_f32 = {"value": sites * TSO_STEPS * dist.world / dist.max(float(np.median(its32))), "unit": METRIC,
+               "h2d_bytes_per_step": int(phi32.nbytes + pi32.nbytes),
+               "d2h_bytes_per_step": int(hphi32.nbytes + hpi32.nbytes + 26 * 8),
+               "iteration_s": [round(t, 4) for t in its32],
+               "step": "as e2e with float host arrays (the reference's doubleprecision -1 build)"}
+    del phi32, pi32, hphi32, hpi32
 
     # ------------------------------------------- the other precisions/sizes
     also = {}

@@ -124,6 +124,12 @@ int phn_destroy(phn_handle *h);
  * slabs, so the caller's values there are left untouched. */
 int phn_upload(phn_handle *h, const double *Phi, const double *Pi);
 int phn_download(phn_handle *h, double *Phi, double *Pi);
+/* The same for the reference's single-precision build (doubleprecision -1,
+ * pseudo_double = float; parameters.cpp:13-16): float arrays in the same
+ * layout, converted on the device to the handle's precision (and back, FP64
+ * handles rounding to float). */
+int phn_upload_f32(phn_handle *h, const float *Phi, const float *Pi);
+int phn_download_f32(phn_handle *h, float *Phi, float *Pi);
 
 /* reset() (dynamics.cpp:28-50): tau = T0, kick/drift clocks = tau, counters 0.
  * The next evolve kicks by dtau/2 (dynamics.cpp:84). */

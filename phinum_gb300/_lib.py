@@ -75,6 +75,8 @@ _SIGS = {
     "phn_destroy": (_I, [ctypes.c_void_p]),
     "phn_upload": (_I, [ctypes.c_void_p, _PD, _PD]),
     "phn_download": (_I, [ctypes.c_void_p, _PD, _PD]),
+    "phn_upload_f32": (_I, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "phn_download_f32": (_I, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "phn_reset": (_I, [ctypes.c_void_p]),
     "phn_evolve": (_I, [ctypes.c_void_p, _I]),
     "phn_time": (_I, [ctypes.c_void_p, _PD, _PI]),

@@ -45,6 +45,13 @@ static void check(int status, const char *what) {
   }
 }
 
+// LocalLattice::Phi/Pi transfers in the build's pseudo_double: double
+// (doubleprecision 0) or float (doubleprecision -1).
+static void upload(const double *Phi, const double *Pi) { check(phn_upload(handle, Phi, Pi), "phn_upload"); }
+static void upload(const float *Phi, const float *Pi) { check(phn_upload_f32(handle, Phi, Pi), "phn_upload_f32"); }
+static void download(double *Phi, double *Pi) { check(phn_download(handle, Phi, Pi), "phn_download"); }
+static void download(float *Phi, float *Pi) { check(phn_download_f32(handle, Phi, Pi), "phn_download_f32"); }
+
 // Mirrors the reference clock (LocalLattice::tau, numeric::Last_*_update,
 // numeric::total_stepcount) from the handle after every call that moves it.
 static void mirror_clock() {
@@ -111,7 +118,7 @@ inline void init() {
   p.precision = prec ? std::atoi(prec) : PHN_FP64;
   if (handle) phn_destroy(handle);
   check(phn_create(&p, &handle), "phn_create");
-  check(phn_upload(handle, LocalLattice::Phi, LocalLattice::Pi), "phn_upload");
+  upload(LocalLattice::Phi, LocalLattice::Pi);
 }
 
 inline void fin() {
@@ -120,7 +127,7 @@ inline void fin() {
 }
 
 // Brings the device fields back into LocalLattice::Phi/Pi.
-inline void to_host() { check(phn_download(handle, LocalLattice::Phi, LocalLattice::Pi), "phn_download"); }
+inline void to_host() { download(LocalLattice::Phi, LocalLattice::Pi); }
 
 // reset() (dynamics.cpp:28-50).
 inline void reset() {

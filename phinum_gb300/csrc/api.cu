@@ -344,42 +344,49 @@ static int ensure_ref_staging(phn_handle *h) {
   return PHN_OK;
 }
 
-int phn_upload(phn_handle *h, const double *Phi, const double *Pi) {
+}  // extern "C"
+
+// phn_upload / phn_download for reference-layout arrays of R (double or float).
+template <typename R>
+static int upload_ref(phn_handle *h, const R *Phi, const R *Pi) {
   if (!h || !Phi || !Pi) return set_error(PHN_ERR_INVALID, "NULL argument");
   int r = ensure_ref_staging(h);
   if (r) return r;
   const int N = h->p.N, Nc = h->p.Nc;
   const size_t n = (size_t)Nc * N * N * (N + 2);
+  R *stage = (R *)h->d_ref;  // n doubles of room
   // phi
-  CK(cudaMemcpyAsync(h->d_ref, Phi, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(stage, Phi, n * sizeof(R), cudaMemcpyHostToDevice, h->stream));
   if (h->p.precision == PHN_FP32_KAHAN)
-    CK(launch_from_ref_kahan(h->d_ref, (float *)h->phi[h->cur], h->cphi, N, Nc, h->stream));
+    CK(launch_from_ref_kahan(stage, (float *)h->phi[h->cur], h->cphi, N, Nc, h->stream));
   else
-    CK(launch_from_ref(h->d_ref, h->phi[h->cur], h->p.precision, N, Nc, h->stream));
+    CK(launch_from_ref(stage, h->phi[h->cur], h->p.precision, N, Nc, h->stream));
   // pi
-  CK(cudaMemcpyAsync(h->d_ref, Pi, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(stage, Pi, n * sizeof(R), cudaMemcpyHostToDevice, h->stream));
   if (h->p.precision == PHN_FP32_KAHAN)
-    CK(launch_from_ref_kahan(h->d_ref, (float *)h->pi, h->cpi, N, Nc, h->stream));
+    CK(launch_from_ref_kahan(stage, (float *)h->pi, h->cpi, N, Nc, h->stream));
   else
-    CK(launch_from_ref(h->d_ref, h->pi, h->p.precision, N, Nc, h->stream));
+    CK(launch_from_ref(stage, h->pi, h->p.precision, N, Nc, h->stream));
   h->launches += 2;
   CK(cudaStreamSynchronize(h->stream));
   return PHN_OK;
 }
 
-int phn_download(phn_handle *h, double *Phi, double *Pi) {
+template <typename R>
+static int download_ref(phn_handle *h, R *Phi, R *Pi) {
   if (!h || (!Phi && !Pi)) return set_error(PHN_ERR_INVALID, "NULL argument");
   int r = ensure_ref_staging(h);
   if (r) return r;
   const int N = h->p.N, Nc = h->p.Nc;
   const size_t n = (size_t)Nc * N * N * (N + 2);
   const bool kahan = h->p.precision == PHN_FP32_KAHAN;
+  R *stage = (R *)h->d_ref;
   if (Phi) {
     if (kahan)
-      CK(launch_to_ref_kahan((const float *)h->phi[h->cur], h->cphi, h->d_ref, N, Nc, h->stream));
+      CK(launch_to_ref_kahan((const float *)h->phi[h->cur], h->cphi, stage, N, Nc, h->stream));
     else
-      CK(launch_to_ref(h->phi[h->cur], h->d_ref, h->p.precision, N, Nc, h->stream));
-    CK(cudaMemcpyAsync(Phi, h->d_ref, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      CK(launch_to_ref(h->phi[h->cur], stage, h->p.precision, N, Nc, h->stream));
+    CK(cudaMemcpyAsync(Phi, stage, n * sizeof(R), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->launches++;
   }
@@ -388,15 +395,22 @@ int phn_download(phn_handle *h, double *Phi, double *Pi) {
     // written by the reference, so only the interior is returned.
     const size_t slab = (size_t)Nc * N * N;
     if (kahan)
-      CK(launch_to_ref_kahan((const float *)h->pi, h->cpi, h->d_ref, N, Nc, h->stream));
+      CK(launch_to_ref_kahan((const float *)h->pi, h->cpi, stage, N, Nc, h->stream));
     else
-      CK(launch_to_ref(h->pi, h->d_ref, h->p.precision, N, Nc, h->stream));
-    CK(cudaMemcpyAsync(Pi + slab, h->d_ref + slab, slab * N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      CK(launch_to_ref(h->pi, stage, h->p.precision, N, Nc, h->stream));
+    CK(cudaMemcpyAsync(Pi + slab, stage + slab, slab * N * sizeof(R), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->launches++;
   }
   return PHN_OK;
 }
+
+extern "C" {
+
+int phn_upload(phn_handle *h, const double *Phi, const double *Pi) { return upload_ref(h, Phi, Pi); }
+int phn_download(phn_handle *h, double *Phi, double *Pi) { return download_ref(h, Phi, Pi); }
+int phn_upload_f32(phn_handle *h, const float *Phi, const float *Pi) { return upload_ref(h, Phi, Pi); }
+int phn_download_f32(phn_handle *h, float *Phi, float *Pi) { return download_ref(h, Phi, Pi); }
 
 int phn_time(const phn_handle *h, double *tau, int *total_stepcount) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");

@@ -167,13 +167,17 @@ int x4_grid(const phn_params &p, int variant);
 cudaError_t launch_step_f32_x4(const Consts &k, int variant, int grid, int mode, const float *phi, float *phi_out,
                                float *pi, float *cphi, float *cpi, StepF s, double *partials, cudaStream_t st);
 
-// Layout conversion between the reference layout (host order, ghosts) and
-// the device SoA layout [a][z][y][x] (layout.cu).
-cudaError_t launch_from_ref(const double *ref, void *dst, int prec, int N, int Nc, cudaStream_t st);
-cudaError_t launch_to_ref(const void *src, double *ref, int prec, int N, int Nc, cudaStream_t st);
-cudaError_t launch_to_ref_kahan(const float *hi, const float *comp, double *ref, int N, int Nc,
-                                cudaStream_t st);
-cudaError_t launch_from_ref_kahan(const double *ref, float *hi, float *comp, int N, int Nc, cudaStream_t st);
+// Layout conversion between the reference layout (host order, ghosts; R =
+// double or float, the reference's pseudo_double) and the device SoA layout
+// [a][z][y][x] (layout.cu).
+template <typename R>
+cudaError_t launch_from_ref(const R *ref, void *dst, int prec, int N, int Nc, cudaStream_t st);
+template <typename R>
+cudaError_t launch_to_ref(const void *src, R *ref, int prec, int N, int Nc, cudaStream_t st);
+template <typename R>
+cudaError_t launch_to_ref_kahan(const float *hi, const float *comp, R *ref, int N, int Nc, cudaStream_t st);
+template <typename R>
+cudaError_t launch_from_ref_kahan(const R *ref, float *hi, float *comp, int N, int Nc, cudaStream_t st);
 
 // Error text for phn_last_error (api.cu).
 int set_error(int code, const char *fmt, ...);

@@ -94,15 +94,27 @@ class Lattice:
 
     # ------------------------------------------------------------- fields
     def upload(self, phi: np.ndarray, pi: np.ndarray):
+        """Reference-layout fields; float32 arrays go through phn_upload_f32
+        (the reference's single-precision build), anything else as float64."""
+        if phi.dtype == np.float32 and pi.dtype == np.float32:
+            phi, pi = np.ascontiguousarray(phi), np.ascontiguousarray(pi)
+            assert phi.size == self.p.field_len and pi.size == self.p.field_len
+            L.check(self.lib.phn_upload_f32(self.h, phi.ctypes.data, pi.ctypes.data))
+            return
         phi = np.ascontiguousarray(phi, dtype=np.float64)
         pi = np.ascontiguousarray(pi, dtype=np.float64)
         assert phi.size == self.p.field_len and pi.size == self.p.field_len
         L.check(self.lib.phn_upload(self.h, _pd(phi), _pd(pi)))
 
-    def download(self):
-        phi = np.zeros(self.p.field_len)
-        pi = np.zeros(self.p.field_len)
-        L.check(self.lib.phn_download(self.h, _pd(phi), _pd(pi)))
+    def download(self, dtype=np.float64):
+        """Reference-layout fields as float64, or as float32 through
+        phn_download_f32."""
+        phi = np.zeros(self.p.field_len, dtype=dtype)
+        pi = np.zeros(self.p.field_len, dtype=dtype)
+        if np.dtype(dtype) == np.float32:
+            L.check(self.lib.phn_download_f32(self.h, phi.ctypes.data, pi.ctypes.data))
+        else:
+            L.check(self.lib.phn_download(self.h, _pd(phi), _pd(pi)))
         return phi, pi
 
     def initial_conditions(self, seed: int = 1, justnoise: int = 0, QS: float = 1.0, scale2: float = 1.0,

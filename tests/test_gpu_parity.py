@@ -442,3 +442,62 @@ def test_compensated_x4_matches_plain_compensated_bit_for_bit(N):
     assert np.array_equal(before[0], after[0]) and np.array_equal(before[1][N * N:-N * N], after[1][N * N:-N * N])
     assert v.value >= -1
     lat.close()
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_islands_fp32_with_a_spanning_cluster(precision):
+    """FP32 (and compensated) fields at 128^3 with a mask over half the
+    lattice, so that one cluster spans the box: labels and sizes equal the
+    oracle's BFS on the same (FP32-valued) fields, energies within FP32
+    rounding (the per-site terms are FP32 for FP32 fields, the per-island sums
+    FP64)."""
+    import inputs
+    PL = gpu()
+    N = 128
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 12)
+    phi32, pi32 = phi_i.astype(np.float32).astype(np.float64), pi_i.astype(np.float32).astype(np.float64)
+    phi, pi = O.to_ref_layout(phi32), O.to_ref_layout(pi32)
+    thr = float(np.quantile(np.sqrt(phi32 ** 2 + pi32 ** 2), 0.5))
+    lat = PL.Lattice(PL.Params(N=N, precision=precision))
+    lat.upload(phi, pi)
+    lab, recs = lat.full_analysis(thr)
+    lat.close()
+    olab, orecs = O.islands(O.Params(N=N), phi, pi, thr)
+    assert np.array_equal(lab, olab)
+    I = {k: i for i, k in enumerate(O.ISLAND_FIELDS)}
+    assert np.array_equal(recs[:, I["size"]], orecs[:, I["size"]])
+    assert recs[:, I["size"]].max() > 0.3 * N ** 3  # the spanning cluster
+    for k in ("pot_en", "kin_en", "grad_en"):
+        np.testing.assert_allclose(recs[:, I[k]], orecs[:, I[k]], rtol=2e-5, atol=1e-6 * np.abs(orecs[:, I[k]]).max())
+    np.testing.assert_allclose(recs[:, I["av_phi"]], orecs[:, I["av_phi"]], rtol=1e-5, atol=1e-6)
+    assert np.array_equal(np.abs(recs[:, I["peak_value"]]), np.abs(orecs[:, I["peak_value"]]))
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_single_precision_host_layout(precision):
+    """phn_upload_f32 / phn_download_f32 (the reference's single-precision
+    build, pseudo_double = float): the same reference layout with float
+    elements.  Float inputs give the device the same state as their double
+    values; the float download is the double download rounded; ghost slabs
+    as phn_download's."""
+    import inputs
+    PL = gpu()
+    N = 32
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 13)
+    phi32 = O.to_ref_layout(phi_i).astype(np.float32)
+    pi32 = O.to_ref_layout(pi_i).astype(np.float32)
+    out = []
+    for host in (np.float32, np.float64):
+        lat = PL.Lattice(PL.Params(N=N, precision=precision))
+        lat.upload(phi32.astype(host), pi32.astype(host))
+        lat.evolve(5)
+        out.append((lat.download(), lat.download(np.float32)))
+        lat.close()
+    (d64_a, d32_a), (d64_b, d32_b) = out
+    for x, y in zip(d64_a, d64_b):
+        assert np.array_equal(x, y)
+    for x, y in zip(d32_a, d32_b):
+        assert np.array_equal(x, y)
+    slab = N * N
+    assert np.array_equal(d32_a[0], d64_a[0].astype(np.float32))
+    assert np.array_equal(d32_a[1][slab:-slab], d64_a[1][slab:-slab].astype(np.float32))
