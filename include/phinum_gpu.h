@@ -171,7 +171,8 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
 int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double *Q, int *counts);
 
 /* SetInitialConditions() (initialconditions.cpp:45-723) for `initialize 3`,
- * static box, no charge, on the device: drand48's stream from srand48(seed)
+ * static or expanding box (the handle's `expanding`, with its T0 and H0), no
+ * charge, on the device: drand48's stream from srand48(seed)
  * (the reference seeds with time(NULL)*(ID+1), initialconditions.cpp:16),
  * consumed in the reference's mode order -- two phases and one polar
  * Box-Muller acceptance per mode and component -- then ensureRealResult and
@@ -343,8 +344,8 @@ int phn_stats(const phn_handle *h, long long *kernel_launches, double *last_evol
  * Many independent lattices (the reference run once per realization, one
  * `main` per seed) evolved together: one persistent kernel per step walks a
  * work list of (member, tile) items, and the step loop runs as a captured CUDA
- * graph.  Members: FP32, Nc = 1, N a multiple of 32, any potential/couplings;
- * they share a, dt and T0 (one clock).  A member's fields are bit-identical to
+ * graph.  Members: FP32, Nc = 1, N a multiple of 32, theory 0 or 1 with any
+ * couplings, static box; they share a, dt and T0 (one clock).  A member's fields are bit-identical to
  * those of a single-lattice handle with the same inputs. */
 typedef struct phn_ensemble phn_ensemble;
 int phn_ensemble_create(const phn_params *members, int n, phn_ensemble **out);
@@ -377,7 +378,8 @@ int phn_ensemble_stats(const phn_ensemble *e, long long *kernel_launches, double
  * step kernels as phn_evolve, checkpoints every `every` steps.  Backward: the
  * discrete adjoint of the implemented leapfrog, reverse time stepping that
  * restarts from each checkpoint (finite-precision reversal drifts).
- * Nc = 1, FP32 or FP64 (the FP64 run is the reference gradient). */
+ * Theory 0 or 1, Nc = 1, static box, FP32 or FP64 (the FP64 run is the
+ * reference gradient). */
 typedef struct phn_adjoint phn_adjoint;
 int phn_adjoint_create(const phn_params *params, int nsteps, int every, double width, phn_adjoint **out);
 int phn_adjoint_destroy(phn_adjoint *a);
