@@ -343,6 +343,9 @@ def measure_gpu(args, dist: Dist):
     if not args.quick:
         also["ensemble_c3"] = measure_ensemble(2000, 100)
         also["analysis"] = analysis_form(N, precisions=("fp32",))["fp32"]
+        adj = adjoint_form(128, 1000, check=False, reps_unchecked=3)
+        also["adjoint_c4_fp32"] = {k: adj[k] for k in ("cost_ratio", "forward_plain_ms", "adjoint_forward_ms",
+                                                       "adjoint_backward_ms", "timing")}
     e2e_burst(3)
     e2e_close()
     out["also"] = also
@@ -481,7 +484,8 @@ def precision_form(N: int, steps: int, check_step: int = 500, tso_steps: int = 5
 
 
 def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: float = 1e-3,
-                 c6_steps=(1e-4, 1e-5, 1e-6, 1e-7), width_cfg: float = 0.1, check: bool = True):
+                 c6_steps=(1e-4, 1e-5, 1e-6, 1e-7), width_cfg: float = 0.1, check: bool = True,
+                 reps_unchecked: int = 1):
     """Adjoint form (config C4): phi^6, N^3, FP32, `steps` steps, checkpoints
     every `every`; J = sum rho sigmoid((rho - 2<rho>)/0.1) of the final state,
     in the configuration's units.  The kernels work in the reference's units
@@ -491,7 +495,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     phi^6 coupling, checked against the FP64 adjoint and against central
     finite differences of the FP64 forward (step h_fd) on `ndir` random unit
     directions; cost = (forward with checkpoints + backward) / plain forward.
-    check=False times the FP32 pair only (one timed solve; for profiling)."""
+    check=False times the FP32 pair only (`reps_unchecked` timed solves)."""
     from phinum_gb300 import lattice as PL
     phi, pi = make_fields(N)
     sl = slice(N * N, -N * N)
@@ -503,7 +507,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     out = {"form": "adjoint", "N": N, "steps": steps, "every": every, "width_config_units": width_cfg,
            "width_reference_units": width}
     res = {}
-    legs = (("fp32", 1, 5), ("fp64", 0, 2)) if check else (("fp32", 1, 1),)
+    legs = (("fp32", 1, 5), ("fp64", 0, 2)) if check else (("fp32", 1, reps_unchecked),)
     for name, prec, reps in legs:
         lat = PL.Lattice(PL.Params(N=N, precision=prec, kappa=kappa))
         plain = []
@@ -532,7 +536,8 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     out["timing"] = ("device events; median of 5 (FP32) / 2 (FP64) solves after one warm-up solve; "
                      "adjoint = forward with checkpoints and J + backward (seed and reverse sweep)")
     if not check:
-        out["timing"] = "device events; one solve after one warm-up solve (profiling run, no checks)"
+        out["timing"] = (f"device events; median of {reps_unchecked} solve(s) after one warm-up solve "
+                         "(no gradient checks)")
         return out
     r64 = res["fp64"]
     d32, d64 = res["fp32"]["dphi"][sl], res["fp64"]["dphi"][sl]
