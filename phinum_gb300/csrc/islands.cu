@@ -147,11 +147,30 @@ __global__ void ccl_init(const T *__restrict__ phi, const float *__restrict__ cp
   }
 }
 
-__device__ __forceinline__ int find_root(const int *parent, int x) {
+// Union-find on site indices.  Every parent pointer points to a smaller or
+// equal index; during the merge a root changes only by atomicCAS(root ->
+// smaller root), and a non-root only by path halving, which stores one of its
+// ancestors.  So concurrent finds may shorten each other's paths but never
+// cut a link.  Halving is for the merge only: ccl_compress must leave every
+// site pointing at its root, so it finds roots without writing (find_root_ro)
+// -- a halving write there could replace a root just stored by another
+// thread with an intermediate ancestor.
+__device__ __forceinline__ int find_root_ro(const int *parent, int x) {
   int p = parent[x];
   while (p != x) {
     x = p;
     p = parent[x];
+  }
+  return x;
+}
+
+__device__ __forceinline__ int find_root(int *parent, int x) {
+  int p = parent[x];
+  while (p != x) {
+    const int gp = parent[p];
+    if (gp != p) parent[x] = gp;  // path halving: x now points two levels up
+    x = p;
+    p = gp;
   }
   return x;
 }
@@ -166,9 +185,8 @@ __device__ void unite(int *parent, int a, int b) {
       a = b;
       b = t;
     }
-    const int old = atomicMin(&parent[a], b);
-    if (old == a) return;
-    a = old;  // a had been linked meanwhile: continue from its new parent
+    // hook the larger root under the smaller; retry if a stopped being a root
+    if (atomicCAS(&parent[a], a, b) == a) return;
   }
 }
 
@@ -195,7 +213,7 @@ __global__ void ccl_compress(int *__restrict__ parent, size_t V, int *__restrict
   if (i < V) {
     const int p = parent[i];
     if (p >= 0) {
-      const int r = find_root(parent, (int)i);
+      const int r = find_root_ro(parent, (int)i);
       parent[i] = r;
       root = (r == (int)i);
     }
