@@ -59,6 +59,9 @@ CASES = {
     "t4_n8": (dict(N=8, Nc=1, **CUBIC), 9, 1.0, 100, 0.25, True, (1, 10, 100)),
     "t4_n16": (dict(N=16, Nc=1, **CUBIC), 10, 1.0, 300, 0.5, False, (1, 100, 300)),
     "t5_n8": (dict(N=8, Nc=1, **POWER), 11, 2.0, 100, 0.25, True, (1, 10, 100)),
+    # three and four field components (O(3) and O(4) models)
+    "t0_n8_nc3": (dict(N=8, Nc=3, **PHI6), 38, SQRT6, 100, 0.25, True, (1, 100)),
+    "t1_n12_nc4": (dict(N=12, Nc=4, **TDW), 39, -SQRT6, 100, 0.25, True, (1, 100)),
     # the radiation-era expanding box (expansion 1) at the reference's H_0
     "e0_n12": (dict(N=12, Nc=1, **PHI6, **EXP), 31, SQRT6, 300, 0.5, True, (1, 100, 300)),
     "e0_n8_nc2": (dict(N=8, Nc=2, **PHI6, **EXP), 32, SQRT6, 100, 0.25, True, (1, 100)),

@@ -160,7 +160,7 @@ def test_spectrum(name, precision):
     lat.close()
 
 
-@pytest.mark.parametrize("name", [n for n in CASES if "nc2" not in n])
+@pytest.mark.parametrize("name", [n for n in CASES if fixtures.load(n)["params"]["Nc"] == 1])
 def test_islands_fp64(name):
     d = fixtures.load(name)
     lat, p = start(d, 0)
