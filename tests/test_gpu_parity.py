@@ -107,7 +107,8 @@ def test_fp64_run_loop_rows(name):
 
 
 @pytest.mark.parametrize("precision,atol", [(1, 2e-4), (2, 2e-5)])
-@pytest.mark.parametrize("name", ["t0_n8", "t1_n8", "t0_n12", "t0_n16_nc2", "t2_n8", "t3_n8", "t4_n8", "t5_n8"])
+@pytest.mark.parametrize("name", ["t0_n8", "t1_n8", "t0_n12", "t0_n16_nc2", "t0_n8_nc3", "t1_n12_nc4", "t2_n8", "t3_n8",
+                                  "t4_n8", "t5_n8"])
 def test_fp32_fields_close(name, precision, atol):
     d = fixtures.load(name)
     lat, p = start(d, precision)
