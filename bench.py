@@ -755,7 +755,7 @@ def main():
                     help="lattice edge (profiling runs use smaller cases); under torchrun spell it --lattice-edge")
     ap.add_argument("--variant", type=int, default=None, help="TMA kernel variant instead of the autotuner's pick")
     ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble", "initial", "io", "analysis"],
-                    help="report one of the north-star forms instead of the benchmark line")
+                    help="report one of the extra forms (or the analysis passes) instead of the benchmark line")
     args = ap.parse_args()
     rank, local, world = env_rank()
     config = {"workload": f"phi^6 oscillon (theory 0, Kappa=sqrt(3)), {args.n}^3 periodic lattice, a=0.25, "

@@ -5,9 +5,9 @@
 #
 # Test infrastructure only.  Flags: no -ffast-math and no FP contraction, so
 # that the reference's FP64 arithmetic is plain IEEE round-to-nearest in
-# source order (the reference's own PBS scripts add -ffast-math, which only
-# reorders).  Exits 0 without building when the reference tree
-# is absent.
+# source order (the reference's own PBS scripts add -ffast-math, which lets
+# the compiler reorder; the parity pin wants the source order).  Exits 0
+# without building when the reference tree is absent.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF_DIR="${REF_DIR:-/root/reference}"
