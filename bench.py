@@ -273,9 +273,9 @@ def measure_gpu(args, dist: Dist):
             phases.append(ph)
 
     def e2e_close():
-        # per-iteration wall times, in three bursts (here, after the other
-        # sizes and after the ensemble): the host link is shared with other
-        # tenants, and the median keeps a disturbed burst from setting the number
+        # per-iteration wall times of nine back-to-back iterations right after
+        # the host buffers are pinned; the median keeps a disturbed iteration
+        # from setting the number
         e2e_s = dist.max(float(np.median(its)))
         out["e2e"] = {"value": sites * TSO_STEPS * dist.world / e2e_s, "unit": METRIC,
                       "h2d_bytes_per_step": int(phi.nbytes + pi.nbytes),
@@ -291,7 +291,7 @@ def measure_gpu(args, dist: Dist):
         elat.close()
 
     e2e_iter()  # warm-up
-    e2e_burst(3 if not (args.no_extra and args.quick) else 9)
+    e2e_burst(9)
 
     # the same with the reference's single-precision host layout (float
     # arrays, phn_upload_f32 / phn_download_f32): half the bytes on the link
@@ -319,7 +319,6 @@ def measure_gpu(args, dist: Dist):
     # ------------------------------------------- the other precisions/sizes
     also = {}
     if args.no_extra:
-        e2e_burst(6 if not args.quick else 0)
         e2e_close()
         out["also"] = also
         return out
@@ -339,14 +338,12 @@ def measure_gpu(args, dist: Dist):
                        "hbm_gbs_algorithmic": BYTES_PER_SITE[prec] * n ** 3 / t / 1e9,
                        "frac_of_measured_hbm": BYTES_PER_SITE[prec] * n ** 3 / t / 1e9 / peak}
         lat.close()
-    e2e_burst(3)
     if not args.quick:
         also["ensemble_c3"] = measure_ensemble(2000, 100)
         also["analysis"] = analysis_form(N, precisions=("fp32",))["fp32"]
         adj = adjoint_form(128, 1000, check=False, reps_unchecked=3)
         also["adjoint_c4_fp32"] = {k: adj[k] for k in ("cost_ratio", "forward_plain_ms", "adjoint_forward_ms",
                                                        "adjoint_backward_ms", "timing")}
-    e2e_burst(3)
     e2e_close()
     out["also"] = also
     return out
