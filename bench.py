@@ -300,7 +300,7 @@ def measure_gpu(args, dist: Dist):
     for a in (phi32, pi32, hphi32, hpi32):
         L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
     its32 = []
-    for it in range(4):
+    for it in range(10):  # a warm-up, then nine timed
         t0 = time.perf_counter()
         L.check(lib.phn_upload_f32(elat.h, phi32.ctypes.data, pi32.ctypes.data))
         elat.run_loop(TSO_STEPS, 1.0, max_rows=2)
