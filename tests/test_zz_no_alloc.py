@@ -60,3 +60,28 @@ def test_noalloc_rejects_lattices_beyond_its_scratch():
     p = PL.Params(N=64, precision=2)
     assert lib.phn_volume_averages_noalloc(ctypes.byref(p.c()), None, None, None, ctypes.byref(out)) == \
         L.ERR_UNSUPPORTED
+
+
+def test_noalloc_expanding_box_uses_the_initial_scale_factor():
+    """For the expanding box the allocation-free averages are those at
+    tau = T0 (scale factor sqrt(1 + 2 H0 T0)): equal to the handle's averages
+    right after upload, whose clock is at T0."""
+    from phinum_gb300 import _lib as L
+    from phinum_gb300 import lattice as PL
+
+    N = 32
+    p = PL.Params(N=N, precision=0, expansion=1, H0=0.05, T0=3.0)
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 32)
+    with PL.Lattice(p) as lat:
+        lat.upload(O.to_ref_layout(phi_i), O.to_ref_layout(pi_i))
+        ref = lat.volume_averages()
+        assert ref[25] == (1.0 + 2.0 * 0.05 * 3.0) ** 0.5
+        d_phi, d_pi, st = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        L.check(lat.lib.phn_device_fields(lat.h, ctypes.byref(d_phi), ctypes.byref(d_pi), ctypes.byref(st)))
+        lat.synchronize()
+        out = L.PhnAverages()
+        L.check(lat.lib.phn_volume_averages_noalloc(ctypes.byref(p.c()), d_phi, d_pi, st, ctypes.byref(out)))
+        got = np.frombuffer(bytes(out), dtype=np.float64)
+        assert np.array_equal(got[EXACT], ref[EXACT])
+        np.testing.assert_allclose(got[SUMS], ref[SUMS], rtol=1e-11, atol=1e-14)
+        assert got[25] == ref[25]
