@@ -1,0 +1,62 @@
+"""Host-side checks of the C ABI, on the CPU: NULL handles and bad
+parameters return PHN_ERR_* status codes (with a message) before any CUDA
+call, so these run without a GPU."""
+import ctypes
+
+import pytest
+
+
+@pytest.fixture(scope="module")
+def L():
+    from phinum_gb300 import build
+    build.build()
+    from phinum_gb300 import _lib
+    _lib.load()
+    return _lib
+
+
+def create_status(L, **kw):
+    from phinum_gb300 import lattice as PL
+    p = PL.Params(**kw)
+    h = ctypes.c_void_p()
+    return L.load().phn_create(ctypes.byref(p.c()), ctypes.byref(h))
+
+
+@pytest.mark.parametrize("kw,code", [
+    (dict(N=1), "ERR_INVALID"),
+    (dict(N=4096), "ERR_INVALID"),
+    (dict(N=8, Nc=9), "ERR_UNSUPPORTED"),
+    (dict(N=8, theory=6), "ERR_INVALID"),
+    (dict(N=8, theory=3, Nc=2), "ERR_UNSUPPORTED"),
+    (dict(N=8, theory=2, m_sqr=0.0), "ERR_INVALID"),
+    (dict(N=8, theory=5, p_mono=0.0), "ERR_INVALID"),
+    (dict(N=8, theory=0, kappa=0.0), "ERR_INVALID"),
+    (dict(N=8, precision=3), "ERR_INVALID"),
+    (dict(N=8, a=0.0), "ERR_INVALID"),
+    (dict(N=8, expansion=2), "ERR_INVALID"),
+    (dict(N=8, expansion=1, H0=0.0), "ERR_INVALID"),
+    (dict(N=8, expansion=1, H0=0.1, T0=-20.0), "ERR_INVALID"),
+])
+def test_create_rejects_bad_parameters(L, kw, code):
+    assert create_status(L, **kw) == getattr(L, code)
+    assert L.load().phn_last_error()  # a message says why
+
+
+def test_null_handles_are_status_codes(L):
+    lib = L.load()
+    d = ctypes.c_double()
+    i = ctypes.c_int()
+    buf = (ctypes.c_double * 8)()
+    calls = [
+        lambda: lib.phn_upload(None, buf, buf),
+        lambda: lib.phn_download(None, buf, buf),
+        lambda: lib.phn_upload_f32(None, None, None),
+        lambda: lib.phn_download_f32(None, None, None),
+        lambda: lib.phn_evolve(None, 1),
+        lambda: lib.phn_reset(None),
+        lambda: lib.phn_time(None, ctypes.byref(d), ctypes.byref(i)),
+        lambda: lib.phn_conformal_time(None, ctypes.byref(d), ctypes.byref(d)),
+    ]
+    for c in calls:
+        assert c() == L.ERR_INVALID
+    assert lib.phn_destroy(None) == L.OK  # like free(NULL)
