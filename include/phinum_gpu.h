@@ -320,8 +320,9 @@ int phn_set_variant(phn_handle *h, int variant);
  * stays usable.  No copy is issued and nothing faults. */
 int phn_wait_selftest(phn_handle *h, long long polls);
 
-/* Self-test of the FP64 kernels' division by a constant (a reciprocal
- * multiply with two residual corrections): n operands a drawn on the device
+/* Self-test of the FP64 kernels' division by a constant (a multiply by a
+ * one- or two-word reciprocal, then one residual correction): n operands a
+ * drawn on the device
  * from `seed` -- half with random significands and exponents in
  * [2^-1000, 2^1000], half placed at ±1-2 ulps around b times a midpoint
  * between two doubles, plus zeros, subnormals, infinities and NaN -- each

@@ -57,13 +57,17 @@ int phn::validate_params(const phn_params *p) {
   return PHN_OK;
 }
 
-// RN(1/b) of every constant divisor the FP64 kernels divide by (div_by), and
-// whether all of them lie in [2^-100, 2^100], where the residual steps cannot
+// RN(1/b) of every constant divisor the FP64 kernels divide by (div_by,
+// div_by_near), the low words RN((1 - b RN(1/b))/b) of div_by's two-word
+// reciprocals (the residual 1 - b RN(1/b) is exact in one fma), and whether
+// all divisors lie in [2^-100, 2^100], where the residual steps cannot
 // underflow or overflow for the operands div_by accepts.
 static void set_reciprocals(Consts &k) {
   const double divisors[] = {k.six_nc, k.kappa, k.c120, k.c24, k.c720, k.a2, k.sqrt_m, k.msq, k.sf, k.sf_sqrtm};
   double *recips[] = {&k.r_six_nc, &k.r_kappa, &k.r_c120, &k.r_c24, &k.r_c720, &k.r_a2, &k.r_sqrtm, &k.r_msq,
                       &k.r_sf, &k.r_sf_sqrtm};
+  double *lows[] = {nullptr, &k.l_kappa, nullptr, nullptr, &k.l_c720, &k.l_a2, &k.l_sqrtm, &k.l_msq,
+                    &k.l_sf, &k.l_sf_sqrtm};
   k.fastdiv = 1;
   for (int i = 0; i < 10; ++i) {
     const double b = divisors[i];
@@ -71,13 +75,15 @@ static void set_reciprocals(Consts &k) {
     // unused divisors (zero couplings of other theories) get no reciprocal
     if (b == 0.0) {
       *recips[i] = 0.0;
+      if (lows[i]) *lows[i] = 0.0;
       continue;
     }
     *recips[i] = 1.0 / b;
+    if (lows[i]) *lows[i] = fma(-b, *recips[i], 1.0) / b;
     if (!(m >= 0x1p-100 && m <= 0x1p100)) k.fastdiv = 0;
   }
-  // the kernels divide by 6 Nc, 24 Nc and 120 Nc^2 with one correction
-  // (div_by<true>): their reciprocals must be within 2^-54 (b * RN(1/b) - 1
+  // the kernels divide by 6 Nc, 24 Nc and 120 Nc^2 from RN(a RN(1/b))
+  // (div_by_near): their reciprocals must be within 2^-54 (b * RN(1/b) - 1
   // is exact in one fma); true for Nc <= 4, checked all the same
   const double near[] = {k.six_nc, k.c24, k.c120};
   for (double b : near)

@@ -28,28 +28,28 @@ namespace phn {
 template <int THEORY>
 __device__ __forceinline__ double force_f64_ext(const Consts &k, double lap, double c, double l) {
   if (THEORY == 3 && k.expansion) {  // sin(phi / (sf sqrt(M))), no phi/|phi| factor
-    const double t = __dmul_rn(k.m3, sin(div_by(k, c, k.sf_sqrtm, k.r_sf_sqrtm)));
+    const double t = __dmul_rn(k.m3, sin(div_by(k, c, k.sf_sqrtm, k.r_sf_sqrtm, k.l_sf_sqrtm)));
     return __dadd_rn(__dadd_rn(lap, -__dmul_rn(k.mmono, c)), -t);
   }
   if (THEORY == 2 || THEORY == 3) {
     const double s = __dsqrt_rn(l);
-    const double arg = k.expansion ? div_by(k, div_by(k, s, k.sf, k.r_sf), k.sqrt_m, k.r_sqrtm)
-                                   : div_by(k, s, k.sqrt_m, k.r_sqrtm);
+    const double arg = k.expansion ? div_by(k, div_by(k, s, k.sf, k.r_sf, k.l_sf), k.sqrt_m, k.r_sqrtm, k.l_sqrtm)
+                                   : div_by(k, s, k.sqrt_m, k.r_sqrtm, k.l_sqrtm);
     const double t = __dmul_rn(__dmul_rn(k.m3, c / s), sin(arg));
     if (THEORY == 2) return __dadd_rn(lap, -t);
     return __dadd_rn(__dadd_rn(lap, -__dmul_rn(k.mmono, c)), -t);
   }
   if (THEORY == 4) {
     const double coef = __dadd_rn(__dadd_rn(k.mmM, -(__dmul_rn(k.g, c) / 2.)),
-                                  __dmul_rn(k.lm, div_by<true>(k, l, k.six_nc, k.r_six_nc)));
+                                  __dmul_rn(k.lm, div_by_near(k, l, k.six_nc, k.r_six_nc)));
     return __dadd_rn(lap, -__dmul_rn(coef, c));
   }
   if (k.expansion)
     return __dadd_rn(lap, -__dmul_rn(__dmul_rn(k.msq_sf2, c),
-                                     pow(__dadd_rn(1., div_by(k, div_by(k, div_by(k, l, k.msq, k.r_msq), k.sf, k.r_sf),
-                                                              k.sf, k.r_sf)),
+                                     pow(__dadd_rn(1., div_by(k, div_by(k, div_by(k, l, k.msq, k.r_msq, k.l_msq), k.sf, k.r_sf, k.l_sf),
+                                                              k.sf, k.r_sf, k.l_sf)),
                                          k.p_mono - 1)));
-  return __dadd_rn(lap, -__dmul_rn(__dmul_rn(k.msq, c), pow(__dadd_rn(1., div_by(k, l, k.msq, k.r_msq)), k.p_mono - 1)));
+  return __dadd_rn(lap, -__dmul_rn(__dmul_rn(k.msq, c), pow(__dadd_rn(1., div_by(k, l, k.msq, k.r_msq, k.l_msq)), k.p_mono - 1)));
 }
 
 // The kick and drift use explicit round-to-nearest intrinsics and IEEE
@@ -97,11 +97,11 @@ __global__ void __launch_bounds__(THREADS) step_f64(const double *__restrict__ p
         double l = 0.0;
 #pragma unroll
         for (int a = 0; a < NC; ++a) l = __dadd_rn(l, __dmul_rn(c[a], c[a]));
-        double coef = __dadd_rn(k.mmM, __dmul_rn(k.lm, div_by<true>(k, l, k.six_nc, k.r_six_nc)));
+        double coef = __dadd_rn(k.mmM, __dmul_rn(k.lm, div_by_near(k, l, k.six_nc, k.r_six_nc)));
         if (THEORY == 0) {
-          double r = div_by(k, l, k.kappa, k.r_kappa);
-          if (k.expansion) r = div_by(k, r, k.sf, k.r_sf);  // sqr(locPhiSqr / Kappa / scale_factor) (dynamics.cpp:90)
-          coef = __dadd_rn(coef, div_by<true>(k, __dmul_rn(r, r), k.c120, k.r_c120));
+          double r = div_by(k, l, k.kappa, k.r_kappa, k.l_kappa);
+          if (k.expansion) r = div_by(k, r, k.sf, k.r_sf, k.l_sf);  // sqr(locPhiSqr / Kappa / scale_factor) (dynamics.cpp:90)
+          coef = __dadd_rn(coef, div_by_near(k, __dmul_rn(r, r), k.c120, k.r_c120));
         }
 #pragma unroll
         for (int a = 0; a < NC; ++a) {

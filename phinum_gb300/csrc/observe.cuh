@@ -146,18 +146,18 @@ __device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c
   A.s[S_PHI6] += __dmul_rn(l2, l);
   // per-site terms (fieldanalysis.cpp:565-617); theories 2-5 have Nc = 1
   if (THEORY == 0) {
-    inter += __dadd_rn(__dmul_rn(k.lm, div_by<true>(k, l2, k.c24, k.r_c24)), div_by(k, __dmul_rn(l2, l), k.c720, k.r_c720));
+    inter += __dadd_rn(__dmul_rn(k.lm, div_by_near(k, l2, k.c24, k.r_c24)), div_by(k, __dmul_rn(l2, l), k.c720, k.r_c720, k.l_c720));
   } else if (THEORY == 1) {
-    inter += __dmul_rn(k.lm, div_by<true>(k, l2, k.c24, k.r_c24));
+    inter += __dmul_rn(k.lm, div_by_near(k, l2, k.c24, k.r_c24));
   } else if (THEORY == 2 || THEORY == 3) {
-    const double arg = k.expansion ? div_by(k, __dsqrt_rn(l), k.sf_sqrtm, k.r_sf_sqrtm)
-                                   : __dsqrt_rn(div_by(k, l, k.msq, k.r_msq));
+    const double arg = k.expansion ? div_by(k, __dsqrt_rn(l), k.sf_sqrtm, k.r_sf_sqrtm, k.l_sf_sqrtm)
+                                   : __dsqrt_rn(div_by(k, l, k.msq, k.r_msq, k.l_msq));
     inter += __dmul_rn(k.msq2, __dsub_rn(1., cos(arg)));
   } else if (THEORY == 4) {
-    inter += __dadd_rn(__dmul_rn(__dmul_rn(-k.g, c[0]), l) / 6.0, __dmul_rn(k.lm, div_by<true>(k, l2, k.c24, k.r_c24)));
+    inter += __dadd_rn(__dmul_rn(__dmul_rn(-k.g, c[0]), l) / 6.0, __dmul_rn(k.lm, div_by_near(k, l2, k.c24, k.r_c24)));
   } else {
-    const double u = k.expansion ? div_by(k, div_by(k, div_by(k, l, k.msq, k.r_msq), k.sf, k.r_sf), k.sf, k.r_sf)
-                                 : div_by(k, l, k.msq, k.r_msq);
+    const double u = k.expansion ? div_by(k, div_by(k, div_by(k, l, k.msq, k.r_msq, k.l_msq), k.sf, k.r_sf, k.l_sf), k.sf, k.r_sf, k.l_sf)
+                                 : div_by(k, l, k.msq, k.r_msq, k.l_msq);
     inter += __dmul_rn(k.t5c, __dsub_rn(pow(__dadd_rn(1., u), k.p_mono), 1.));
   }
   A.s[S_INTER] += inter;

@@ -75,10 +75,13 @@ struct Consts {
   double sf_sqrtm;  // sf * sqrt(M)
   double msq_sf2;   // (M sf) sf
   // reciprocals RN(1/b) of the FP64 kernels' constant divisors (div_by,
-  // div_by_near); fastdiv = 0 when a divisor lies outside [2^-100, 2^100] or
-  // one of 6 Nc, 24 Nc, 120 Nc^2 has a reciprocal further than 2^-54 from 1/b
+  // div_by_near) and, for div_by's divisors, the low word l = RN((1 - b r)/b)
+  // of a two-word reciprocal r + l; fastdiv = 0 when a divisor lies outside
+  // [2^-100, 2^100] or one of 6 Nc, 24 Nc, 120 Nc^2 has a reciprocal further
+  // than 2^-54 from 1/b
   int fastdiv;
   double r_six_nc, r_kappa, r_c120, r_c24, r_c720, r_a2, r_sqrtm, r_msq, r_sf, r_sf_sqrtm;
+  double l_kappa, l_c720, l_a2, l_sqrtm, l_msq, l_sf, l_sf_sqrtm;
 };
 
 // Consts of the expanding box at scale factor sf: every coupling that the
@@ -88,37 +91,47 @@ struct Consts {
 // stays bit-identical; the FP32 constants are folded the same way.
 Consts at_scale_factor(const Consts &k0, double sf);
 
-// a / b, correctly rounded, for a divisor b fixed per launch with rb =
-// RN(1/b) from the host: q = RN(a rb), then residual corrections
-// q <- RN(q + RN(a - b q) rb).  From a faithful q (within one ulp of a/b) and
-// rb = RN(1/b), one correction returns RN(a/b) (Markstein's theorem: P.
+// a / b, correctly rounded, for a divisor b fixed per launch, from its
+// reciprocal rb = RN(1/b) computed on the host.  From a faithful quotient q
+// (within one ulp of a/b) and rb = RN(1/b), one correction
+// q' = RN(q + RN(a - b q) rb) returns RN(a/b) (Markstein's theorem: P.
 // Markstein, IBM J. Res. Dev. 34(1), 1990; M. Cornea-Hasegan, R. Golliver,
 // P. Markstein, ARITH-14, 1999), and the fma residual of a faithful quotient
-// is exact.  RN(a rb) itself is faithful when |b rb - 1| <= 2^-54 (a rb then
-// lies within half an ulp of a/b): NEAR = true, one correction, for the
-// divisors 6 Nc, 24 Nc and 120 Nc^2 (checked on the host); otherwise a first
-// correction makes q faithful and a second one rounds it.  The theorem needs
-// no underflow or overflow in the residuals: operands outside
-// 2^-900 <= |a| < 2^900 (zeros, subnormals, infinities, NaN; an integer test
-// of the exponent) and handles whose divisors leave [2^-100, 2^100]
-// (fastdiv = 0) take IEEE division.  Three or five FP64 operations instead of
-// a full division: the FP64 kernels are bound by GB300's FP64 rate.
-template <bool NEAR = false>
-__device__ __forceinline__ double div_by(const Consts &k, double a, double b, double rb) {
+// is exact.  The faithful q comes from
+//   div_by_near: q = RN(a rb), for divisors with |b rb - 1| <= 2^-54 (a rb is
+//                then within half an ulp of a/b): 6 Nc, 24 Nc, 120 Nc^2,
+//                checked on the host;
+//   div_by:      q = RN(a rb + RN(a rl)) with the two-word reciprocal rb + rl
+//                (rl = RN((1 - b rb)/b), within ~2^-105 of 1/b together), for
+//                every other divisor.
+// The theorem needs no underflow or overflow in the residuals: operands
+// outside 2^-900 <= |a| < 2^900 (zeros, subnormals, infinities, NaN; an
+// integer test of the exponent) and handles whose divisors leave
+// [2^-100, 2^100] (fastdiv = 0) take IEEE division.  Three or four FP64
+// operations instead of a full division: the FP64 kernels are bound by
+// GB300's FP64 rate.
+__device__ __forceinline__ bool div_fast_range(const Consts &k, double a) {
   const unsigned hi = (unsigned)__double2hiint(a) & 0x7fffffffu;
-  if (k.fastdiv && hi >= 0x07b00000u && hi < 0x78300000u) {
-    double q = __dmul_rn(a, rb);
-    if (!NEAR) q = __fma_rn(__fma_rn(-b, q, a), rb, q);
-    return __fma_rn(__fma_rn(-b, q, a), rb, q);
-  }
-  return a / b;
+  return k.fastdiv && hi >= 0x07b00000u && hi < 0x78300000u;
+}
+
+__device__ __forceinline__ double div_by_near(const Consts &k, double a, double b, double rb) {
+  if (!div_fast_range(k, a)) return a / b;
+  const double q = __dmul_rn(a, rb);
+  return __fma_rn(__fma_rn(-b, q, a), rb, q);
+}
+
+__device__ __forceinline__ double div_by(const Consts &k, double a, double b, double rb, double rl) {
+  if (!div_fast_range(k, a)) return a / b;
+  const double q = __fma_rn(a, rb, __dmul_rn(a, rl));
+  return __fma_rn(__fma_rn(-b, q, a), rb, q);
 }
 
 // x / sqr(a_t) in IEEE arithmetic.  When sqr(a_t) is a power of two the
 // quotient is an exact scaling and the product by its reciprocal rounds the
 // same real number the same way (bit-identical, cheaper on the FP64 pipes).
 __device__ __forceinline__ double div_a2(const Consts &k, double x) {
-  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : div_by(k, x, k.a2, k.r_a2);
+  return k.a2_pow2 ? __dmul_rn(x, k.inv_a2) : div_by(k, x, k.a2, k.r_a2, k.l_a2);
 }
 
 // Per-step kick and drift factors: tau - Last_Momenta_update and

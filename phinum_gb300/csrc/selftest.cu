@@ -63,12 +63,12 @@ __device__ double divide_operand(double b, unsigned long long seed, long long i)
   return sign ? -a : a;
 }
 
-__global__ void divide_selftest(const Consts k, double b, double rb, bool near, long long n, unsigned long long seed,
-                                unsigned long long *bad) {
+__global__ void divide_selftest(const Consts k, double b, double rb, double rl, bool near, long long n,
+                                unsigned long long seed, unsigned long long *bad) {
   unsigned long long local = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double a = divide_operand(b, seed, i);
-    const double fast = near ? div_by<true>(k, a, b, rb) : div_by(k, a, b, rb), ieee = a / b;
+    const double fast = near ? div_by_near(k, a, b, rb) : div_by(k, a, b, rb, rl), ieee = a / b;
     const bool same = __double_as_longlong(fast) == __double_as_longlong(ieee) || (fast != fast && ieee != ieee);
     local += same ? 0 : 1;
   }
@@ -86,14 +86,15 @@ extern "C" int phn_divide_selftest(phn_handle *h, double b, long long n, unsigne
   Consts k = h->k;
   const double m = fabs(b);
   k.fastdiv = (m >= 0x1p-100 && m <= 0x1p100) ? 1 : 0;
-  // one correction where the reciprocal is within 2^-54, as for the divisors
-  // the kernels treat so; two otherwise
+  // div_by_near where the reciprocal is within 2^-54, as the kernels use it
+  // for such divisors; div_by with the two-word reciprocal otherwise
   const bool near = fabs(fma(b, 1.0 / b, -1.0)) <= 0x1p-54;
+  const double rb = 1.0 / b, rl = fma(-b, rb, 1.0) / b;
   unsigned long long *d_bad = nullptr;
   cudaError_t e = cudaMalloc((void **)&d_bad, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(unsigned long long), h->stream);
   if (e == cudaSuccess) {
-    divide_selftest<<<152 * 8, 256, 0, h->stream>>>(k, b, 1.0 / b, near, n, seed, d_bad);
+    divide_selftest<<<152 * 8, 256, 0, h->stream>>>(k, b, rb, rl, near, n, seed, d_bad);
     e = cudaGetLastError();
   }
   unsigned long long bad = 0;
