@@ -2,10 +2,14 @@
 //
 // Replaces is_island + BFS + the seeding scan of Full_Analysis
 // (islands.cpp:72-279, 778-840) for a first analysis (empty island history):
-//   1. mask + init: parent[i] = i for mask sites, -1 elsewhere;
-//   2. merge: every mask site unites with its -x, -y (periodic) and -z (open
-//      as on one rank, islands.cpp:224-236, or periodic) mask neighbours,
-//      linking the larger root under the smaller with atomicMin;
+//   1. mask + init: -1 for sites off the mask; a mask site points at the
+//      first site of its run of mask sites along x within its 32-site warp
+//      segment (the x links inside a segment cost no union);
+//   2. merge: every mask site unites with its -x (where init did not link
+//      it), -y (periodic) and -z (open as on one rank, islands.cpp:224-236, or
+//      periodic) mask neighbours, hooking the larger root under the smaller
+//      by atomicCAS; a y or z union is skipped where the -x sites of both
+//      ends are on the mask too (those two are joined already, so are these);
 //   3. compress: parent[i] = root(i).  Links always point to smaller indices,
 //      so each root is the smallest site index of its island;
 //   4. number: islands are numbered by their root in increasing index order,
@@ -17,7 +21,6 @@
 #include <math.h>
 #include <string.h>
 
-#include <vector>
 
 #include <type_traits>
 
@@ -30,23 +33,88 @@ constexpr int CCL_THREADS = 256;
 struct IslState {
   int *parent;     // [V]
   int *ids;        // [V] island id of each root
-  int *blk;        // [nblk] roots per block, then exclusive offsets
-  int nblk;
+  int *blk;        // [nblk] roots per block, then exclusive offsets; [ntile]
+                   // the same per tile of SCAN_TILE blocks; [1] the total
+  int nblk, ntile;
   // per-island arrays, grown on demand
   int cap;
   int *size;
   double *sums;                 // [cap][5]: pot, kin, grad, phi, (unused)
-  unsigned long long *peak2;    // max phi^2 bits
+  unsigned long long *peak2;    // max peak_key per island
   long long *peakpos;           // reference index of the first max site
   double *peakval;
   int *seed;                    // root site (interior linear index)
+  phn_island *rec;              // [cap] the records handed to the caller
 };
+
+// Division of site indices (< 2^31) by the lattice edge N without a divide:
+// q = umulhi(n, m) >> s with s = floor(log2 N), m = ceil(2^(32+s) / N)
+// (Granlund and Montgomery, PLDI 1994).  m < 2^32, and its error e = m N -
+// 2^(32+s) < N <= 2^(s+1) makes n e < 2^(32+s) for n < 2^31, so n m / 2^(32+s)
+// exceeds n / N by less than 1/N and the floor is exact.  Powers of two
+// shift (m = 0).
+struct DivN {
+  unsigned m;
+  int s;
+};
+
+static DivN make_divn(unsigned d) {
+  int s = 0;
+  while ((2u << s) <= d) ++s;  // floor(log2 d)
+  if ((d & (d - 1)) == 0) return DivN{0u, s};
+  const unsigned long long num = 1ull << (32 + s);
+  return DivN{(unsigned)((num + d - 1) / d), s};
+}
+
+__device__ __forceinline__ unsigned div_n(const DivN &q, unsigned n) {
+  return q.m ? __umulhi(n, q.m) >> q.s : n >> q.s;
+}
+
+// x, y, z of site i (i < 2^31)
+__device__ __forceinline__ void site_xyz(const DivN &q, int N, size_t i, int &x, int &y, int &z) {
+  const unsigned row = div_n(q, (unsigned)i), zz = div_n(q, row);
+  x = (int)((unsigned)i - row * (unsigned)N);
+  y = (int)(row - zz * (unsigned)N);
+  z = (int)zz;
+}
 
 template <typename T>
 __device__ __forceinline__ double val(const T *f, const float *comp, size_t i) {
   double v = (double)f[i];
   if (comp) v -= (double)comp[i];
   return v;
+}
+
+// Site values for kernels compiled per storage: KAHAN for compensated FP32
+// fields (value = stored - compensation, in FP64), plain otherwise.  The
+// choice is a template argument: a runtime test on the compensation pointer
+// leaves the FP64 form in the plain kernels (if-converted, it issues for every
+// site on GB300's narrow FP64 pipe).
+template <bool KAHAN, typename T>
+__device__ __forceinline__ double val_k(const T *f, const float *comp, size_t i) {
+  if constexpr (KAHAN) return (double)f[i] - (double)comp[i];
+  else return (double)f[i];
+}
+
+// The same in arithmetic A (FP32 for FP32 storage: no FP64 round trip).
+template <typename A, bool KAHAN, typename T>
+__device__ __forceinline__ A val_as(const T *f, const float *comp, size_t i) {
+  if constexpr (KAHAN) return (A)((double)f[i] - (double)comp[i]);
+  else return (A)f[i];
+}
+
+// Peak key of a site: the FP64 bits of phi^2 (non-negative, so the bits
+// order like the values), or for plain FP32 fields the FP32 bits of |phi| --
+// their squares are exact in FP64, so the two keys order the sites alike and
+// tie alike.  ccl_stats takes the maximum key, ccl_peak the sites that hold it.
+template <bool KAHAN, typename T>
+__device__ __forceinline__ unsigned long long peak_key(const T *phi, const float *cphi, size_t i) {
+  if constexpr (std::is_same<T, float>::value && !KAHAN) {
+    return (unsigned long long)__float_as_uint(fabsf(phi[i]));
+  } else {
+    const double c = val_k<KAHAN>(phi, cphi, i);
+    return (unsigned long long)__double_as_longlong(c * c);
+  }
 }
 
 // Potential of one single-component site, theories 0-5: the BFS PotEn
@@ -113,37 +181,77 @@ __device__ __forceinline__ float site_kinetic(const Consts &k, float c, float p)
 // (fieldanalysis.cpp:437-471,571-579), Nc = 1, in arithmetic A: FP64 for FP64
 // fields, FP32 for FP32 fields (their values carry FP32 rounding already; a
 // site within that of the threshold is on either side).
-template <typename A, typename T>
+template <typename A, bool KAHAN, typename T>
 __device__ A site_rho(const T *phi, const float *cphi, const T *pi, const float *cpi, int N, int x, int y, int z,
                       const Consts k) {
   const size_t NN = (size_t)N * N;
   const size_t i = (size_t)z * NN + (size_t)y * N + x;
-  const A c = (A)val(phi, cphi, i), p = (A)val(pi, cpi, i);
-  const A fx = (A)val(phi, cphi, (size_t)z * NN + (size_t)y * N + (x + 1 == N ? 0 : x + 1));
-  const A fy = (A)val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
-  const A fz = (A)val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
+  const A c = val_as<A, KAHAN>(phi, cphi, i), p = val_as<A, KAHAN>(pi, cpi, i);
+  const A fx = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)y * N + (x + 1 == N ? 0 : x + 1));
+  const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
+  const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
   const A c2 = c * c;
   const A grad = (((fx - c) * (fx - c) + (fy - c) * (fy - c)) + (fz - c) * (fz - c)) * (A)k.inv_a2;
   return site_kinetic(k, c, p) + (A)0.5 * grad + site_potential(k, c, c2);
 }
 
-template <typename T>
+// islands.cpp:76 in FP64; the FP32 form is the rare path of plain FP32 fields
+// (a sum within 2^-19 of the threshold), kept out of line so that it is a
+// branch and not issued for every site.
+__device__ __forceinline__ bool ref_mask(double c, double p, double thr) {
+  return __dadd_rn(__dmul_rn(__dmul_rn(c, c), 0.5), __dmul_rn(__dmul_rn(p, p), 0.5)) > thr;
+}
+
+__device__ __noinline__ bool ref_mask_f64(float c, float p, double thr) { return ref_mask(c, p, thr); }
+
+// The grid-stride loops below advance by whole warps of 32 consecutive
+// sites (blocks are multiples of 32 threads), so site i is always handled by
+// lane i % 32; ccl_merge relies on it to know which x links init made.
+template <typename T, bool KAHAN>
 __global__ void ccl_init(const T *__restrict__ phi, const float *__restrict__ cphi, const T *__restrict__ pi,
-                         const float *__restrict__ cpi, int N, int mode, double thr, const Consts k,
-                         int *__restrict__ parent) {
+                         const float *__restrict__ cpi, int N, const DivN dn, int mode, double thr,
+                         float thr_lo, float thr_hi, const Consts k, int *__restrict__ parent) {
   const size_t V = (size_t)N * N * N;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    bool m;
-    if (mode == PHN_ISLAND_REFERENCE) {
-      // islands.cpp:76: Phi*Phi*0.5 + Pi*Pi*0.5 > thres*thres*0.5 (thr holds the right side)
-      const double c = val(phi, cphi, i), p = val(pi, cpi, i);
-      m = __dadd_rn(__dmul_rn(__dmul_rn(c, c), 0.5), __dmul_rn(__dmul_rn(p, p), 0.5)) > thr;
-    } else {
-      const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((size_t)N * N));
-      using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
-      m = site_rho<A>(phi, cphi, pi, cpi, N, x, y, z, k) > (A)thr;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) & ~(size_t)31; base < V;
+       base += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = base + lane;
+    bool m = false;
+    int x = 0;
+    if (i < V) {
+      int y, z;
+      site_xyz(dn, N, i, x, y, z);
+      if (mode == PHN_ISLAND_REFERENCE) {
+        // islands.cpp:76: Phi*Phi*0.5 + Pi*Pi*0.5 > thres*thres*0.5 (thr
+        // holds the right side), in FP64.  Plain FP32 fields first try FP32:
+        // s = (c c + RN(p p)) / 2 in one fma is within 2^-23 relative of the
+        // exact sum, and thr_lo/thr_hi bracket thr by 2^-19 (both 0 when thr
+        // is outside [2^-100, 2^100]), so a sum outside the bracket decides
+        // the FP64 comparison; sums inside it, and NaN, take FP64.
+        if constexpr (std::is_same<T, float>::value && !KAHAN) {
+          const float cf = phi[i], pf = pi[i];
+          const float sf = 0.5f * fmaf(cf, cf, pf * pf);
+          if (thr_hi > 0.f && (sf > thr_hi || sf < thr_lo)) {
+            m = sf > thr_hi;
+          } else {
+            m = ref_mask_f64(cf, pf, thr);
+          }
+        } else {
+          const double c = val_k<KAHAN>(phi, cphi, i), p = val_k<KAHAN>(pi, cpi, i);
+          m = ref_mask(c, p, thr);
+        }
+      } else {
+        using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+        m = site_rho<A, KAHAN>(phi, cphi, pi, cpi, N, x, y, z, k) > (A)thr;
+      }
     }
-    parent[i] = m ? (int)i : -1;
+    // runs of mask sites along x within this segment: each site points at
+    // the run's first site (a smaller index, as every link must)
+    const unsigned mb = __ballot_sync(full, m);
+    const unsigned joined = __ballot_sync(full, m && x != 0 && lane != 0 && ((mb >> (lane - 1)) & 1u));
+    const unsigned heads = mb & ~joined;
+    if (i < V) parent[i] = m ? (int)(base + (31 - __clz(heads & (full >> (31 - lane))))) : -1;
   }
 }
 
@@ -190,18 +298,27 @@ __device__ void unite(int *parent, int a, int b) {
   }
 }
 
-__global__ void ccl_merge(int *__restrict__ parent, int N, int zper) {
+__global__ void ccl_merge(int *__restrict__ parent, int N, const DivN dn, int zper) {
   const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
     if (parent[i] < 0) continue;
-    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
-    const size_t jx = i - x + (x == 0 ? N - 1 : x - 1);
+    int x, y, z;
+    site_xyz(dn, N, i, x, y, z);
+    // -x: the periodic wrap, and the first lane of a segment (init links the rest)
+    const bool left = x > 0 && parent[i - 1] >= 0;
+    if (x == 0) {
+      if (parent[i + N - 1] >= 0) unite(parent, (int)i, (int)(i + N - 1));
+    } else if (left && (i & 31) == 0) {
+      unite(parent, (int)i, (int)(i - 1));
+    }
+    // -y / -z: i-1 ~ i and j-1 ~ j along x, so with both -x sites on the mask
+    // the pair (i-1, j-1) -- united, or skipped by the same rule further left
+    // -- already joins i and j
     const size_t jy = (y == 0) ? i + (size_t)(N - 1) * N : i - N;
-    if (parent[jx] >= 0) unite(parent, (int)i, (int)jx);
-    if (parent[jy] >= 0) unite(parent, (int)i, (int)jy);
+    if (parent[jy] >= 0 && !(left && parent[jy - 1] >= 0)) unite(parent, (int)i, (int)jy);
     if (z > 0 || zper) {
       const size_t jz = (z == 0) ? i + (size_t)(N - 1) * NN : i - NN;
-      if (parent[jz] >= 0) unite(parent, (int)i, (int)jz);
+      if (parent[jz] >= 0 && !(left && parent[jz - 1] >= 0)) unite(parent, (int)i, (int)jz);
     }
   }
 }
@@ -229,7 +346,41 @@ __global__ void ccl_compress(int *__restrict__ parent, size_t V, int *__restrict
   }
 }
 
-// exclusive scan of the block counts, one block, fixed order
+// Exclusive scan of the block counts in two levels: each block of
+// ccl_scan_tiles scans SCAN_TILE consecutive counts in place (coalesced) and
+// writes the tile's total; ccl_scan then scans the tile totals in one block.
+// ccl_number adds both offsets.
+constexpr int SCAN_TILE = 1024;
+
+__global__ void __launch_bounds__(SCAN_TILE) ccl_scan_tiles(int *__restrict__ blk, int n, int *__restrict__ tile) {
+  __shared__ int wsum[SCAN_TILE / 32];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const size_t b = (size_t)blockIdx.x * SCAN_TILE + t;
+  const int v = b < (size_t)n ? blk[b] : 0;
+  int s = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, s, off);
+    if (lane >= off) s += u;
+  }
+  if (lane == 31) wsum[warp] = s;
+  __syncthreads();
+  if (warp == 0) {
+    int w = wsum[lane];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= off) w += u;
+    }
+    wsum[lane] = w;  // inclusive totals of warps 0..lane
+  }
+  __syncthreads();
+  const int ex = s - v + (warp ? wsum[warp - 1] : 0);
+  if (b < (size_t)n) blk[b] = ex;
+  if (t == SCAN_TILE - 1) tile[blockIdx.x] = wsum[SCAN_TILE / 32 - 1];
+}
+
+// exclusive scan of the tile totals, one block, fixed order
 __global__ void ccl_scan(int *__restrict__ blk, int n, int *__restrict__ total) {
   __shared__ int part[1024];
   const int t = threadIdx.x;
@@ -257,8 +408,8 @@ __global__ void ccl_scan(int *__restrict__ blk, int n, int *__restrict__ total) 
   }
 }
 
-__global__ void ccl_number(const int *__restrict__ parent, size_t V, const int *__restrict__ blk, int *__restrict__ ids,
-                           int *__restrict__ seed, int cap) {
+__global__ void ccl_number(const int *__restrict__ parent, size_t V, const int *__restrict__ blk,
+                           const int *__restrict__ tile, int *__restrict__ ids, int *__restrict__ seed, int cap) {
   const size_t i = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
   const bool root = (i < V) && parent[i] == (int)i;
   __shared__ int cnt[CCL_THREADS / 32];
@@ -267,7 +418,7 @@ __global__ void ccl_number(const int *__restrict__ parent, size_t V, const int *
   if (lane == 0) cnt[warp] = __popc(b);
   __syncthreads();
   if (root) {
-    int off = blk[blockIdx.x];
+    int off = blk[blockIdx.x] + tile[blockIdx.x / SCAN_TILE];
     for (int w = 0; w < warp; ++w) off += cnt[w];
     off += __popc(b & ((1u << lane) - 1u));
     ids[i] = off;
@@ -286,12 +437,46 @@ __global__ void ccl_number(const int *__restrict__ parent, size_t V, const int *
 // same-address atomics from every warp were what bounded this pass.  A run
 // that finds the table full adds to the global sums directly.
 constexpr int STATS_SITES = 8192;
-constexpr int STATS_SLOTS = 1024;  // power of two
+constexpr int STATS_SLOTS = 512;  // power of two; with the run scratch under 48 KB of static shared memory
 
+// One island's sums in a block's table: pot, kin, grad, phi.  FP64 fields
+// add in FP64.  FP32 fields keep each sum as a float pair hi + lo without any
+// FP64 instruction: atomicAdd(hi, v) returns the old value, atom.add.f32
+// rounds to nearest even, so the error of that addition is the TwoSum term
+// (old + v) - RN(old + v) (Knuth, TAOCP vol. 2, 4.2.2), which goes into lo.
+// The pair tracks the exact sum but for lo's own (second-order) rounding.
+template <typename A>
 struct StatsSlot {
-  double pot, kin, grad, phi;
+  double s[4];
   unsigned long long peak2;
   int size, id;
+  __device__ void clear() { s[0] = s[1] = s[2] = s[3] = 0.0; }
+  __device__ void add(int j, double v) { atomicAdd(&s[j], v); }
+  __device__ double sum(int j) const { return s[j]; }
+};
+
+template <>
+struct StatsSlot<float> {
+  float hi[4], lo[4];
+  unsigned long long peak2;
+  int size, id;
+  __device__ void clear() {
+    for (int j = 0; j < 4; ++j) hi[j] = lo[j] = 0.f;
+  }
+  __device__ void add(int j, float v) {
+    const float old = atomicAdd(&hi[j], v);
+    const float s = __fadd_rn(old, v), bb = __fsub_rn(s, old);
+    const float err = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+    if (err != 0.f) atomicAdd(&lo[j], err);
+  }
+  __device__ double sum(int j) const { return (double)hi[j] + (double)lo[j]; }
+};
+
+template <typename A>
+struct RunSums {
+  A pot, kin, grad, cs;
+  unsigned long long pk;
+  int n;
 };
 
 template <typename A>
@@ -305,16 +490,22 @@ __device__ __forceinline__ void stats_global(int id, int n, A pot, A kin, A grad
   atomicMax(&peak2[id], pk);
 }
 
-template <typename T>
+template <typename T, bool KAHAN>
 __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ phi, const float *__restrict__ cphi,
                                                         const T *__restrict__ pi, const float *__restrict__ cpi,
                                                         const int *__restrict__ parent, const int *__restrict__ ids,
-                                                        int N, const Consts k, int *__restrict__ size,
+                                                        int N, const DivN dn, const Consts k,
+                                                        int *__restrict__ size,
                                                         double *__restrict__ sums,
                                                         unsigned long long *__restrict__ peak2) {
-  __shared__ StatsSlot table[STATS_SLOTS];
+  // FP32 fields: per-site terms and the in-warp scan in FP32 (GB300's FP64
+  // rate would otherwise bound the pass); FP64 fields: FP64.  The global
+  // per-island sums are FP64 either way.
+  using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+  __shared__ StatsSlot<A> table[STATS_SLOTS];
+  __shared__ RunSums<A> scratch[CCL_THREADS / 32][32];
   for (int j = threadIdx.x; j < STATS_SLOTS; j += CCL_THREADS) {
-    table[j].pot = table[j].kin = table[j].grad = table[j].phi = 0.0;
+    table[j].clear();
     table[j].peak2 = 0;
     table[j].size = 0;
     table[j].id = -1;
@@ -325,10 +516,6 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ p
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const size_t s0 = (size_t)blockIdx.x * STATS_SITES;
   const size_t s1 = s0 + STATS_SITES < V ? s0 + STATS_SITES : V;
-  // FP32 fields: per-site terms and the in-warp scan in FP32 (GB300's FP64
-  // rate would otherwise bound the pass); FP64 fields: FP64.  The global
-  // per-island sums are FP64 either way.
-  using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
   // chunk loop: uniform per warp, so every lane takes part in the collectives
   for (size_t base = s0 + (size_t)warp * 32; base < s1; base += (size_t)(CCL_THREADS / 32) * 32) {
     const size_t i = base + lane;
@@ -336,23 +523,22 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ p
     A pot = 0, kin = 0, grad = 0, cs = 0;
     unsigned long long pk = 0;
     const int r = i < s1 ? parent[i] : -1;
+    if (__ballot_sync(full, r >= 0) == 0) continue;  // uniform per warp
     if (r >= 0) {
       id = ids[r];
-      const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
-      const double cd = val(phi, cphi, i);
-      const A c = (A)cd, p = (A)val(pi, cpi, i);
-      const A fx = (A)val(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
-      const A fy = (A)val(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
-      const A fz = (A)val(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
+      int x, y, z;
+      site_xyz(dn, N, i, x, y, z);
+      const A c = val_as<A, KAHAN>(phi, cphi, i), p = val_as<A, KAHAN>(pi, cpi, i);
+      const A fx = val_as<A, KAHAN>(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
+      const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
+      const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
       // BFS accumulators (islands.cpp:131-198)
       grad = (A)0.5 * ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) * (A)k.inv_a2;
       kin = site_kinetic(k, c, p);
       pot = site_potential(k, c, c * c);
       cs = c;
       n = 1;
-      // phi^2 >= 0: its bits order like the value; the FP64 square, so that
-      // ccl_peak finds the same maximum
-      pk = (unsigned long long)__double_as_longlong(cd * cd);
+      pk = peak_key<KAHAN>(phi, cphi, i);
     }
     const int prev = __shfl_up_sync(full, id, 1);
     const unsigned heads = __ballot_sync(full, lane == 0 || prev != id);
@@ -373,7 +559,24 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ p
       }
     }
     const int next = __shfl_down_sync(full, id, 1);
-    if ((lane == 31 || next != id) && id >= 0) {
+    const bool end = (lane == 31 || next != id) && id >= 0;
+    // The runs of one island in this chunk (a cluster winding through it)
+    // combine first, in lane order, so that the table takes one update per
+    // island per chunk: updates of one slot serialise, and the FP64 ones on
+    // GB300's narrow FP64 pipe.
+    const unsigned grp = __match_any_sync(full, end ? id : -1 - lane);
+    if (end) scratch[warp][lane] = RunSums<A>{pot, kin, grad, cs, pk, n};
+    __syncwarp();
+    if (end && (grp & ((1u << lane) - 1u)) == 0) {
+      for (unsigned b = grp & (grp - 1u); b; b &= b - 1u) {
+        const RunSums<A> &o = scratch[warp][__ffs(b) - 1];
+        pot += o.pot;
+        kin += o.kin;
+        grad += o.grad;
+        cs += o.cs;
+        n += o.n;
+        pk = o.pk > pk ? o.pk : pk;
+      }
       // open addressing on the island id, linear probing
       unsigned h = ((unsigned)id * 2654435761u) & (STATS_SLOTS - 1);
       int slot = -1;
@@ -387,24 +590,25 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ p
       }
       if (slot >= 0) {
         atomicAdd(&table[slot].size, n);
-        atomicAdd(&table[slot].pot, (double)pot);
-        atomicAdd(&table[slot].kin, (double)kin);
-        atomicAdd(&table[slot].grad, (double)grad);
-        atomicAdd(&table[slot].phi, (double)cs);
+        table[slot].add(0, pot);
+        table[slot].add(1, kin);
+        table[slot].add(2, grad);
+        table[slot].add(3, cs);
         atomicMax(&table[slot].peak2, pk);
       } else {
         stats_global(id, n, pot, kin, grad, cs, pk, size, sums, peak2);
       }
     }
+    __syncwarp();  // scratch is rewritten by the next chunk
   }
   __syncthreads();
   for (int j = threadIdx.x; j < STATS_SLOTS; j += CCL_THREADS) {
-    const StatsSlot &t = table[j];
-    if (t.id >= 0) stats_global(t.id, t.size, t.pot, t.kin, t.grad, t.phi, t.peak2, size, sums, peak2);
+    const StatsSlot<A> &t = table[j];
+    if (t.id >= 0) stats_global(t.id, t.size, t.sum(0), t.sum(1), t.sum(2), t.sum(3), t.peak2, size, sums, peak2);
   }
 }
 
-template <typename T>
+template <typename T, bool KAHAN>
 __global__ void ccl_peak(const T *__restrict__ phi, const float *__restrict__ cphi, const int *__restrict__ parent,
                          const int *__restrict__ ids, int N, const unsigned long long *__restrict__ peak2,
                          long long *__restrict__ peakpos) {
@@ -413,8 +617,7 @@ __global__ void ccl_peak(const T *__restrict__ phi, const float *__restrict__ cp
     const int r = parent[i];
     if (r < 0) continue;
     const int id = ids[r];
-    const double c = val(phi, cphi, i);
-    if ((unsigned long long)__double_as_longlong(c * c) == peak2[id])
+    if (peak_key<KAHAN>(phi, cphi, i) == peak2[id])
       atomicMin(&peakpos[id], (long long)(i + NN));  // reference index (Nc = 1)
   }
 }
@@ -470,6 +673,30 @@ __global__ void ccl_labels_mapped(const int *__restrict__ parent, const int *__r
   }
 }
 
+// The caller's records (islands.cpp:239-262 units), assembled on the device
+// so that one copy returns them.  volume = ((size a) a) a and the energies
+// sum * a^3 as the reference's cV factors; no operation here can contract.
+__global__ void ccl_records(const int *__restrict__ size, const double *__restrict__ sums,
+                            const long long *__restrict__ peakpos, const double *__restrict__ peakval,
+                            const int *__restrict__ seed, int n, double a, double cell, long long NN,
+                            phn_island *__restrict__ out) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    phn_island I;
+    const double sz = (double)size[j];
+    I.index = (double)j;
+    I.size = sz;
+    I.volume = __dmul_rn(__dmul_rn(__dmul_rn(sz, a), a), a);  // cV = NN*a_t*a_t*a_eta (islands.cpp:241)
+    I.pot_en = __dmul_rn(sums[(size_t)j * 4 + 0], cell);
+    I.kin_en = __dmul_rn(sums[(size_t)j * 4 + 1], cell);
+    I.grad_en = __dmul_rn(sums[(size_t)j * 4 + 2], cell);
+    I.av_phi = __ddiv_rn(sums[(size_t)j * 4 + 3], sz);
+    I.peak_pos = (double)peakpos[j];
+    I.peak_value = peakval[j];
+    I.seed_pos = (double)((long long)seed[j] + NN);
+    out[j] = I;
+  }
+}
+
 __global__ void fill_ll(long long *p, long long v, int n) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) p[j] = v;
 }
@@ -481,6 +708,8 @@ static void free_isl_arrays(IslState *s) {
   cudaFree(s->peakpos);
   cudaFree(s->peakval);
   cudaFree(s->seed);
+  cudaFree(s->rec);
+  s->rec = nullptr;
   s->size = nullptr;
   s->sums = nullptr;
   s->peak2 = nullptr;
@@ -520,9 +749,10 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
     memset(s, 0, sizeof(*s));
     h->isl = s;
     s->nblk = (int)((V + CCL_THREADS - 1) / CCL_THREADS);
+    s->ntile = (s->nblk + SCAN_TILE - 1) / SCAN_TILE;
     cudaError_t e = cudaMalloc(&s->parent, V * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&s->ids, V * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&s->blk, ((size_t)s->nblk + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->blk, ((size_t)s->nblk + s->ntile + 1) * sizeof(int));
     if (e != cudaSuccess) {
       islands_release(h);
       return cuda_error(e, "island buffers");
@@ -532,13 +762,24 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
   const double thr = mode == PHN_ISLAND_REFERENCE ? (thres * thres * 0.5) : thres;
   const int gb = grid_blocks(V);
   const Consts k = consts_now(h);
-  ccl_init<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, k, s->parent);
-  ccl_merge<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, zper);
+  const DivN dn = make_divn((unsigned)N);
+  float thr_lo = 0.f, thr_hi = 0.f;  // the FP32 bracket of the reference mask (ccl_init)
+  if (thr >= 0x1p-100 && thr <= 0x1p100) {
+    thr_lo = (float)(thr * (1.0 - 0x1p-19));
+    thr_hi = (float)(thr * (1.0 + 0x1p-19));
+  }
+  if (cphi)
+    ccl_init<T, true><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, dn, mode, thr, thr_lo, thr_hi, k, s->parent);
+  else
+    ccl_init<T, false><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, dn, mode, thr, thr_lo, thr_hi, k, s->parent);
+  ccl_merge<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, dn, zper);
   ccl_compress<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk);
-  ccl_scan<<<1, 1024, 0, st>>>(s->blk, s->nblk, s->blk + s->nblk);
-  h->launches += 4;
+  int *tile = s->blk + s->nblk;
+  ccl_scan_tiles<<<s->ntile, SCAN_TILE, 0, st>>>(s->blk, s->nblk, tile);
+  ccl_scan<<<1, 1024, 0, st>>>(tile, s->ntile, tile + s->ntile);
+  h->launches += 5;
   int count = 0;
-  cudaError_t e = cudaMemcpyAsync(&count, s->blk + s->nblk, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaError_t e = cudaMemcpyAsync(&count, tile + s->ntile, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_error(e, "island count");
   if (count > s->cap) {
@@ -550,22 +791,30 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
     if (e == cudaSuccess) e = cudaMalloc(&s->peakpos, cap * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc(&s->peakval, cap * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&s->seed, cap * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->rec, cap * sizeof(phn_island));
     if (e != cudaSuccess) {
       free_isl_arrays(s);
       return cuda_error(e, "island arrays");
     }
     s->cap = cap;
   }
-  ccl_number<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk, s->ids, s->seed, s->cap);
+  ccl_number<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk, tile, s->ids, s->seed, s->cap);
   h->launches++;
   if (count > 0) {
     cudaMemsetAsync(s->size, 0, count * sizeof(int), st);
     cudaMemsetAsync(s->sums, 0, (size_t)count * 4 * sizeof(double), st);
     cudaMemsetAsync(s->peak2, 0, count * sizeof(unsigned long long), st);
     fill_ll<<<(count + 255) / 256, 256, 0, st>>>(s->peakpos, LLONG_MAX, count);
-    ccl_stats<T><<<(unsigned)((V + STATS_SITES - 1) / STATS_SITES), CCL_THREADS, 0, st>>>(
-        phi, cphi, pi, cpi, s->parent, s->ids, N, k, s->size, s->sums, s->peak2);
-    ccl_peak<T><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
+    const unsigned sb = (unsigned)((V + STATS_SITES - 1) / STATS_SITES);
+    if (cphi) {
+      ccl_stats<T, true><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size, s->sums,
+                                                     s->peak2);
+      ccl_peak<T, true><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
+    } else {
+      ccl_stats<T, false><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
+                                                      s->sums, s->peak2);
+      ccl_peak<T, false><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
+    }
     ccl_peakval<T><<<(count + 255) / 256, 256, 0, st>>>(phi, cphi, N, count, s->peakpos, s->peakval);
     h->launches += 4;
   }
@@ -584,33 +833,14 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
   if (e != cudaSuccess) return cuda_error(e, "island kernels");
   const int n_out = count < max_out ? count : max_out;
   if (out && n_out > 0) {
-    std::vector<int> size(n_out), seed(n_out);
-    std::vector<double> sums((size_t)n_out * 4), pval(n_out);
-    std::vector<long long> ppos(n_out);
-    e = cudaMemcpyAsync(size.data(), s->size, n_out * sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(seed.data(), s->seed, n_out * sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(sums.data(), s->sums, (size_t)n_out * 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(pval.data(), s->peakval, n_out * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(ppos.data(), s->peakpos, n_out * sizeof(long long), cudaMemcpyDeviceToHost, st);
+    const double a = h->p.a, cell = (a * a) * a;
+    ccl_records<<<(n_out + 255) / 256, 256, 0, st>>>(s->size, s->sums, s->peakpos, s->peakval, s->seed, n_out, a,
+                                                     cell, (long long)N * N, s->rec);
+    h->launches++;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, s->rec, (size_t)n_out * sizeof(phn_island), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "island readback");
-    const double a = h->p.a, cell = (a * a) * a;
-    const size_t NN = (size_t)N * N;
-    for (int j = 0; j < n_out; ++j) {
-      phn_island &I = out[j];
-      I.index = j;
-      I.size = size[j];
-      I.volume = size[j] * a * a * a;  // cV = NN*a_t*a_t*a_eta (islands.cpp:241)
-      I.pot_en = sums[(size_t)j * 4 + 0] * cell;
-      I.kin_en = sums[(size_t)j * 4 + 1] * cell;
-      I.grad_en = sums[(size_t)j * 4 + 2] * cell;
-      I.av_phi = sums[(size_t)j * 4 + 3] / (double)size[j];
-      I.peak_pos = (double)ppos[j];
-      I.peak_value = pval[j];
-      I.seed_pos = (double)((size_t)seed[j] + NN);
-    }
   } else {
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "islands");

@@ -474,6 +474,34 @@ def test_islands_fp32_with_a_spanning_cluster(precision):
     assert np.array_equal(np.abs(recs[:, I["peak_value"]]), np.abs(orecs[:, I["peak_value"]]))
 
 
+@pytest.mark.parametrize("N", [24, 47, 100])
+def test_islands_at_edges_that_are_not_powers_of_two(N):
+    """Rows that straddle the 32-site warp segments of the labelling (its
+    run links and x-wrap unions) and index division by an edge that is not a
+    power of two: labels, sizes and seeds equal the oracle's for both masks,
+    z open and periodic, FP64 and (reference mask) FP32 fields."""
+    import inputs
+    PL = gpu()
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 31)
+    phi32, pi32 = phi_i.astype(np.float32).astype(np.float64), pi_i.astype(np.float32).astype(np.float64)
+    op = O.Params(N=N)
+    for precision, (ph, pp) in ((0, (phi_i, pi_i)), (1, (phi32, pi32))):
+        phi, pi = O.to_ref_layout(ph), O.to_ref_layout(pp)
+        thr = float(np.quantile(np.sqrt(ph ** 2 + pp ** 2), 0.45))
+        rho = O.averages(op, phi, pi)[O.AVG["energy"]]
+        lat = PL.Lattice(PL.Params(N=N, precision=precision))
+        lat.upload(phi, pi)
+        for mode, t in ((0, thr), (1, 1.2 * rho)):
+            if precision and mode:
+                continue  # the FP32 energy mask rounds differently near the threshold
+            for zper in (0, 1):
+                lab, recs = lat.full_analysis(t, mode=mode, z_periodic=bool(zper))
+                olab, orecs = O.islands(op, phi, pi, t, mode=mode, zper=zper)
+                assert np.array_equal(lab, olab), (precision, mode, zper)
+                assert np.array_equal(recs[:, 1], orecs[:, 1]) and np.array_equal(recs[:, 9], orecs[:, 9])
+        lat.close()
+
+
 @pytest.mark.parametrize("precision", [0, 1, 2])
 def test_single_precision_host_layout(precision):
     """phn_upload_f32 / phn_download_f32 (the reference's single-precision
