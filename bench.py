@@ -507,17 +507,24 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     out = {"form": "adjoint", "N": N, "steps": steps, "every": every, "width_config_units": width_cfg,
            "width_reference_units": width}
     res = {}
-    legs = (("fp32", 1, 5), ("fp64", 0, 2)) if check else (("fp32", 1, reps_unchecked),)
-    for name, prec, reps in legs:
-        lat = PL.Lattice(PL.Params(N=N, precision=prec, kappa=kappa))
+    # fp32_fwd64: the FP32 adjoint with its forward solve in FP64
+    # (phn_adjoint_set_forward_precision); its plain forward is the FP64 one
+    legs = ((("fp32", 1, 5, None), ("fp64", 0, 2, None), ("fp32_fwd64", 1, 2, 0)) if check
+            else (("fp32", 1, reps_unchecked, None),))
+    for name, prec, reps, fwd_prec in legs:
         plain = []
-        for r in range(reps + 1):
-            lat.upload(phi, pi)
-            lat.evolve(steps)
-            if r:
-                plain.append(lat.stats()[1])
-        lat.close()
-        with PL.Adjoint(PL.Params(N=N, precision=prec, kappa=kappa), steps, every, width) as adj:
+        if fwd_prec is None:
+            lat = PL.Lattice(PL.Params(N=N, precision=prec, kappa=kappa))
+            for r in range(reps + 1):
+                lat.upload(phi, pi)
+                lat.evolve(steps)
+                if r:
+                    plain.append(lat.stats()[1])
+            lat.close()
+        else:
+            plain = [res["fp64"]["plain_ms"]]
+        with PL.Adjoint(PL.Params(N=N, precision=prec, kappa=kappa), steps, every, width,
+                        forward_precision=fwd_prec) as adj:
             fl, bl = [], []
             for r in range(reps + 1):
                 adj.forward(phi, pi)
@@ -549,9 +556,21 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     g32, g64 = res["fp32"]["g"], res["fp64"]["g"]
     out["fp32_vs_fp64_dphi0_rel"] = float(abs(g32[0] - g64[0]) / abs(g64[0]))
     out["fp32_vs_fp64_dc6_rel"] = float(abs(g32[1] - g64[1]) / abs(g64[1]))
+    rm = res["fp32_fwd64"]
+    dm, gm = rm["dphi"][sl], rm["g"]
+    out["fp32_fwd64"] = {
+        "what": "FP32 adjoint (checkpoints, reverse sweep) with an FP64 forward solve",
+        "cost_ratio_vs_fp64_forward": (rm["forward_ms"] + rm["backward_ms"]) / r64["plain_ms"],
+        "cost_ratio_vs_fp32_forward": (rm["forward_ms"] + rm["backward_ms"]) / r32["plain_ms"],
+        "cost_vs_fp64_adjoint": (rm["forward_ms"] + rm["backward_ms"]) / (r64["forward_ms"] + r64["backward_ms"]),
+        "adjoint_forward_ms": rm["forward_ms"], "adjoint_backward_ms": rm["backward_ms"],
+        "J_equals_fp64": rm["J"] == res["fp64"]["J"],
+        "vs_fp64_field_rel_l2": float(np.linalg.norm(dm - d64) / np.linalg.norm(d64)),
+        "vs_fp64_dphi0_rel": float(abs(gm[0] - g64[0]) / abs(g64[0])),
+        "vs_fp64_dc6_rel": float(abs(gm[1] - g64[1]) / abs(g64[1]))}
     # central finite differences of the FP64 forward
     rng = np.random.default_rng(99)
-    errs64, errs32 = [], []
+    errs64, errs32, errsm = [], [], []
     with PL.Adjoint(PL.Params(N=N, precision=0, kappa=kappa), steps, every, width) as adj:
         for _ in range(ndir):
             v = np.zeros_like(phi)
@@ -560,6 +579,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
             fd = (adj.forward(phi + h_fd * v, pi) - adj.forward(phi - h_fd * v, pi)) / (2 * h_fd)
             errs64.append(abs(float(np.dot(d64, v[sl])) - fd) / abs(fd))
             errs32.append(abs(float(np.dot(d32, v[sl])) - fd) / abs(fd))
+            errsm.append(abs(float(np.dot(dm, v[sl])) - fd) / abs(fd))
         # the homogeneous shift moves every site at once: a far smaller step
         # keeps the central difference out of the sigmoid's curvature
         h_s = 1e-7
@@ -583,6 +603,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     out["fp64_adjoint_vs_fd_rel_max"] = float(max(errs64))
     out["fp32_adjoint_vs_fd_rel_max"] = float(max(errs32))
     out["fp32_adjoint_vs_fd_rel_median"] = float(np.median(errs32))
+    out["fp32_fwd64"]["vs_fd_rel_max"] = float(max(errsm))
     out["dphi0"] = {"fp32": float(g32[0]), "fp64": float(g64[0]), "fd": fd_phi0}
     out["dc6"] = {"fp32": float(g32[1]), "fp64": float(g64[1]), "fd": fd_c6}
     # the configuration's units: J = J_ref / 6, phi_ref = sqrt(6) phi, c6 = g / 216

@@ -391,6 +391,13 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
  * of Phi0), dJ/dc6 with c6 = 1/(720 Kappa^2) the phi^6 coefficient of V
  * (theory 0), dJ/dh (theory 1) }. */
 int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *grads);
+/* Precision of the forward solve of an FP32 adjoint: PHN_FP64 runs the
+ * forward with the FP64 step kernels (FP32 checkpoints, rounded; J and the
+ * seed on the FP64 final state), the reverse sweep staying FP32; PHN_FP32
+ * (the default) runs both in FP32.  The gradient's sensitivity to the final
+ * state through the sigmoid makes the forward's precision the one that
+ * matters.  PHN_ERR_UNSUPPORTED for an FP64 adjoint or other precisions. */
+int phn_adjoint_set_forward_precision(phn_adjoint *a, int precision);
 /* J of the last forward and device times (ms) of the last forward and backward. */
 int phn_adjoint_info(const phn_adjoint *a, double *J, double *forward_ms, double *backward_ms);
 

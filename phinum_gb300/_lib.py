@@ -136,6 +136,7 @@ _SIGS = {
     "phn_adjoint_forward": (_I, [ctypes.c_void_p, _PD, _PD, _PD]),
     "phn_adjoint_backward": (_I, [ctypes.c_void_p, _PD, _PD, _PD]),
     "phn_adjoint_info": (_I, [ctypes.c_void_p, _PD, _PD, _PD]),
+    "phn_adjoint_set_forward_precision": (_I, [ctypes.c_void_p, _I]),
     "phn_pin_host": (_I, [ctypes.c_void_p, ctypes.c_size_t]),
     "phn_unpin_host": (_I, [ctypes.c_void_p]),
 }

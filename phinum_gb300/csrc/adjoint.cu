@@ -26,6 +26,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <type_traits>
 #include <vector>
 
 #include "phn_internal.h"
@@ -83,6 +84,40 @@ __device__ __forceinline__ T vpp(const Consts &k, T c) {
   return v;
 }
 
+// force and vpp with their coefficients formed once per thread (the same
+// expressions, so the same values), for the one-site-per-thread reverse step
+// whose FP64 form is bound by GB300's FP64 rate.
+template <typename T>
+struct PotCoef {
+  T inv_a2, l6, c6, mmM, h;
+  int theory;
+  __device__ explicit PotCoef(const Consts &k)
+      : inv_a2((T)1 / (T)k.a2), l6((T)k.lm / (T)k.six_nc),
+        c6((T)1 / ((T)k.kappa * (T)k.kappa * (T)k.c120)), mmM((T)k.mmM), h((T)k.h), theory(k.theory) {}
+  __device__ __forceinline__ T force(T diff_sum, T c) const {
+    const T l = c * c;
+    T coef = mmM + l * l6;
+    if (theory == 0) coef += (l * l) * c6;
+    T f = diff_sum * inv_a2 - coef * c;
+    if (theory == 1) f -= h;
+    return f;
+  }
+  __device__ __forceinline__ T vpp(T c) const {
+    const T l = c * c;
+    T v = mmM + (T)3 * l * l6;
+    if (theory == 0) v += (T)5 * (l * l) * c6;
+    return v;
+  }
+};
+
+// A plain running sum (FP64 partials need no compensation over one column).
+template <typename T>
+struct PSum {
+  T s = 0;
+  __device__ __forceinline__ void add(T v) { s += v; }
+  __device__ __forceinline__ double value() const { return (double)s; }
+};
+
 // Block-level sum of the two per-thread gradient partials into this
 // block's slot (fixed order: warp shuffles, then the warps in order).
 __device__ __forceinline__ void grad_slot_add(double g0, double g1, double *gs, int tid, int nwarps) {
@@ -124,7 +159,12 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
   const int x = blockIdx.x * ADJ_TX + threadIdx.x, y = blockIdx.y * ADJ_TY + threadIdx.y;
   const int z0 = blockIdx.z * cz, z1 = min(z0 + cz, N);
   const size_t NN = (size_t)N * N;
-  KSum<T> k_c6, k_h;
+  // sum_z mu phi^5 and sum_z mu; the step's factors -6 fk and -fk apply once
+  using Sum = typename std::conditional<std::is_same<T, double>::value, PSum<T>, KSum<T>>::type;
+  Sum k_c6, k_h;
+  const PotCoef<T> pc_k(k);
+  static_assert(ADJ_TX == 32, "a warp spans one row segment of 32 sites");
+  const bool warp_rows = (N & 31) == 0;
   if (x < N && y < N && z0 < z1) {
     const int xp = (x + 1 == N) ? 0 : x + 1, xm = (x == 0) ? N - 1 : x - 1;
     const int yp = (y + 1 == N) ? 0 : y + 1, ym = (y == 0) ? N - 1 : y - 1;
@@ -134,34 +174,57 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
     const int zm0 = (z0 == 0) ? N - 1 : z0 - 1;
     T pm = rphi((size_t)zm0 * NN + col), pc = rphi((size_t)z0 * NN + col);
     T mm = rmu((size_t)zm0 * NN + col), mc = rmu((size_t)z0 * NN + col);
-    const T inv_a2 = (T)1 / (T)k.a2;
+    const T inv_a2 = pc_k.inv_a2;
     for (int z = z0; z < z1; ++z) {
       const int zn = (z + 1 == N) ? 0 : z + 1;
       const size_t pl = (size_t)z * NN, i = pl + col;
       const T pn = rphi((size_t)zn * NN + col), mn = rmu((size_t)zn * NN + col);
       const size_t ixp = pl + (size_t)y * N + xp, ixm = pl + (size_t)y * N + xm;
       const size_t iyp = pl + (size_t)yp * N + x, iym = pl + (size_t)ym * N + x;
-      const T dphi = (((rphi(ixp) - pc) + (rphi(ixm) - pc)) + ((rphi(iyp) - pc) + (rphi(iym) - pc))) +
-                     ((pn - pc) + (pm - pc));
-      const T pi_before = AdjOps<T>::fma_(-fk, force<T>(k, dphi, pc), pi1[i]);
-      const T dmu = (((rmu(ixp) - mc) + (rmu(ixm) - mc)) + ((rmu(iyp) - mc) + (rmu(iym) - mc))) +
-                    ((mn - mc) + (mm - mc));
-      const T lphi_before = AdjOps<T>::fma_(fk, dmu * inv_a2 - vpp<T>(k, pc) * mc, lphi[i]);
+      // x neighbours: from the next / previous lane where a warp spans 32
+      // sites of one row (N a multiple of 32: whole warps active), else
+      // reconstructed here -- the same values either way
+      T pxp, pxm, mxp, mxm;
+      if (warp_rows) {
+        const int lane = threadIdx.x;
+        pxp = __shfl_down_sync(0xffffffffu, pc, 1);
+        pxm = __shfl_up_sync(0xffffffffu, pc, 1);
+        mxp = __shfl_down_sync(0xffffffffu, mc, 1);
+        mxm = __shfl_up_sync(0xffffffffu, mc, 1);
+        if (lane == 31) {
+          pxp = rphi(ixp);
+          mxp = rmu(ixp);
+        }
+        if (lane == 0) {
+          pxm = rphi(ixm);
+          mxm = rmu(ixm);
+        }
+      } else {
+        pxp = rphi(ixp);
+        pxm = rphi(ixm);
+        mxp = rmu(ixp);
+        mxm = rmu(ixm);
+      }
+      const T dphi = (((pxp - pc) + (pxm - pc)) + ((rphi(iyp) - pc) + (rphi(iym) - pc))) + ((pn - pc) + (pm - pc));
+      const T pi_before = AdjOps<T>::fma_(-fk, pc_k.force(dphi, pc), pi1[i]);
+      const T dmu = (((mxp - mc) + (mxm - mc)) + ((rmu(iyp) - mc) + (rmu(iym) - mc))) + ((mn - mc) + (mm - mc));
+      const T lphi_before = AdjOps<T>::fma_(fk, dmu * inv_a2 - pc_k.vpp(pc) * mc, lphi[i]);
       phi0[i] = pc;
       pi0[i] = pi_before;
       lphi0[i] = lphi_before;
       lpi0[i] = mc;
       // dF/dc6 = -6 phi^5 ; dF/dh = -1   (kick pi' = pi + fk F)
       const T p2 = pc * pc;
-      k_c6.add(fk * mc * ((T)-6 * (p2 * p2 * pc)));
-      k_h.add(-fk * mc);
+      k_c6.add(mc * (p2 * p2 * pc));
+      k_h.add(mc);
       pm = pc;
       pc = pn;
       mm = mc;
       mc = mn;
     }
   }
-  grad_slot_add(k_c6.value(), k_h.value(), gs, threadIdx.x + ADJ_TX * threadIdx.y, ADJ_THREADS / 32);
+  grad_slot_add(-6.0 * (double)fk * k_c6.value(), -(double)fk * k_h.value(), gs, threadIdx.x + ADJ_TX * threadIdx.y,
+                ADJ_THREADS / 32);
 }
 
 // The same reverse step for FP32, four consecutive x-sites per thread
@@ -399,10 +462,10 @@ __global__ void __launch_bounds__(OBJ_THREADS) obj_seed(const double *__restrict
 //   lam_phi = g (-sum_d (phi(x+d) - phi(x)) / a^2 + V'(phi)) + sum_d g(x-d) (phi(x) - phi(x-d)) / a^2
 // and, in the same pass, block sums of the direct coupling terms
 // dJ/dc6 = sum g phi^6 and dJ/dh = sum g phi into part[0..nb), part[nb..2nb).
-template <typename T>
+template <typename T, typename L>
 __global__ void __launch_bounds__(OBJ_THREADS) obj_adjoint_init(const T *__restrict__ phi, const T *__restrict__ pi,
                                                                 const double *__restrict__ g, const Consts k,
-                                                                T *__restrict__ lphi, T *__restrict__ lpi,
+                                                                L *__restrict__ lphi, L *__restrict__ lpi,
                                                                 double *__restrict__ part, int nb) {
   const int N = k.N;
   const size_t NN = (size_t)N * N, V = NN * N;
@@ -423,8 +486,8 @@ __global__ void __launch_bounds__(OBJ_THREADS) obj_adjoint_init(const T *__restr
     double vp = 2.0 * k.mm_half_M * c + l6 * c2 * c;
     if (k.theory == 0) vp += 6.0 * c2 * c2 * c * i720;
     if (k.theory == 1) vp += k.h;
-    lphi[i] = (T)(gi * (-fwd * ia2 + vp) + bwd * ia2);
-    lpi[i] = (T)(gi * (double)pi[i]);
+    lphi[i] = (L)(gi * (-fwd * ia2 + vp) + bwd * ia2);
+    lpi[i] = (L)(gi * (double)pi[i]);
     a6 += gi * (c2 * c2 * c2);
     ah += gi * c;
   }
@@ -433,6 +496,12 @@ __global__ void __launch_bounds__(OBJ_THREADS) obj_adjoint_init(const T *__restr
     part[blockIdx.x] = s6;
     part[nb + blockIdx.x] = sh;
   }
+}
+
+// FP64 forward state -> FP32 checkpoint (round to nearest)
+__global__ void narrow_f64(const double *__restrict__ src, float *__restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
 }
 
 __global__ void gs_zero(double *gs, size_t n) {
@@ -448,7 +517,8 @@ struct phn_adjoint {
   Consts k;
   int nsteps, every, nseg;
   double w;
-  size_t V, elem;
+  size_t V, elem;          // elem: bytes of a checkpoint / reverse-sweep value
+  size_t fwd_elem;         // bytes of a forward value (8 for an FP64 forward)
   phn_handle *fwd;
   void *ckpt;              // (nseg + 1) x {phi, pi}
   void *rphi[2], *rpi[2], *lphi[2], *lpi[2];
@@ -527,6 +597,7 @@ int phn_adjoint_create(const phn_params *params, int nsteps, int every, double w
   a->w = width;
   a->V = (size_t)params->N * params->N * params->N;
   a->elem = params->precision == PHN_FP64 ? 8 : 4;
+  a->fwd_elem = a->elem;
   r = phn_create(params, &a->fwd);
   if (r) {
     adj_free(a);
@@ -577,9 +648,17 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
   a->fd.clear();
   phn_device_fields(h, &phi, &pi, &stv);
   cudaStream_t st = (cudaStream_t)stv;
+  // an FP64 forward under an FP32 reverse sweep stores FP32 checkpoints
+  const bool narrow = a->fwd_elem == 8 && a->elem == 4;
+  auto store = [&](char *dst, const void *src) -> cudaError_t {
+    if (!narrow) return cudaMemcpyAsync(dst, src, fb, cudaMemcpyDeviceToDevice, st);
+    narrow_f64<<<152 * 4, 256, 0, st>>>((const double *)src, (float *)dst, a->V);
+    h->launches++;
+    return cudaGetLastError();
+  };
   CKA(cudaEventRecord(a->ev0, st));
-  CKA(cudaMemcpyAsync(ck, phi, fb, cudaMemcpyDeviceToDevice, st));
-  CKA(cudaMemcpyAsync(ck + fb, pi, fb, cudaMemcpyDeviceToDevice, st));
+  CKA(store(ck, phi));
+  CKA(store(ck + fb, pi));
   for (int s = 0; s < a->nseg; ++s) {
     // the factors the next `every` steps will use: the clock arithmetic of
     // dynamics.cpp:200-213, as the handle runs it
@@ -595,10 +674,10 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
     r = evolve_async(h, a->every);
     if (r) return r;
     phn_device_fields(h, &phi, &pi, &stv);
-    CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb, phi, fb, cudaMemcpyDeviceToDevice, st));
-    CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb + fb, pi, fb, cudaMemcpyDeviceToDevice, st));
+    CKA(store(ck + (size_t)(s + 1) * 2 * fb, phi));
+    CKA(store(ck + (size_t)(s + 1) * 2 * fb + fb, pi));
   }
-  if (a->elem == 8)
+  if (a->fwd_elem == 8)
     r = objective<double>(a, (const double *)phi, (const double *)pi, st);
   else
     r = objective<float>(a, (const float *)phi, (const float *)pi, st);
@@ -685,12 +764,17 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   CKA(cudaEventRecord(a->ev0, st));
   gs_zero<<<64, 256, 0, st>>>(a->gs, (size_t)gr.nblocks * ADJ_NG);
   // adjoint of the objective, with the direct dependence of rho on the couplings
+  // (on the forward's final state: FP64 when the forward ran in FP64)
   if (dbl)
-    obj_adjoint_init<double><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
-                                                         (double *)a->lphi[0], (double *)a->lpi[0], a->sums, nb);
+    obj_adjoint_init<double, double><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
+                                                                 (double *)a->lphi[0], (double *)a->lpi[0], a->sums,
+                                                                 nb);
+  else if (a->fwd_elem == 8)
+    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
+                                                                (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   else
-    obj_adjoint_init<float><<<nb, OBJ_THREADS, 0, st>>>((const float *)phi, (const float *)pi, a->g, a->k,
-                                                        (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
+    obj_adjoint_init<float, float><<<nb, OBJ_THREADS, 0, st>>>((const float *)phi, (const float *)pi, a->g, a->k,
+                                                               (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   CKA(cudaGetLastError());
   CKA(cudaGraphLaunch(a->sweep, st));
   h->launches += a->nsteps + 2;
@@ -741,6 +825,24 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
     grads[1] = g_c6 + direct_c6;
     grads[2] = g_h + direct_h;
   }
+  return PHN_OK;
+}
+
+int phn_adjoint_set_forward_precision(phn_adjoint *a, int precision) {
+  if (!a) return set_error(PHN_ERR_INVALID, "NULL argument");
+  const int cur = a->fwd_elem == 8 ? PHN_FP64 : PHN_FP32;
+  if (precision == cur) return PHN_OK;
+  if (a->p.precision != PHN_FP32 || (precision != PHN_FP64 && precision != PHN_FP32))
+    return set_error(PHN_ERR_UNSUPPORTED, "forward precision: FP64 or FP32 under an FP32 adjoint");
+  phn_params q = a->p;
+  q.precision = precision;
+  phn_handle *nh = nullptr;
+  const int r = phn_create(&q, &nh);
+  if (r) return r;
+  phn_destroy(a->fwd);
+  a->fwd = nh;
+  a->fwd_elem = precision == PHN_FP64 ? 8 : 4;
+  a->forward_done = false;
   return PHN_OK;
 }
 

@@ -370,13 +370,16 @@ class Adjoint:
     units; the default 0.6 is width 0.1 in the units of the
     phi^2/2 - phi^4/4 + g phi^6/6 form (Phi = sqrt(6) phi, energies 6x)."""
 
-    def __init__(self, p: Params, nsteps: int, every: int = 50, width: float = 0.6):
+    def __init__(self, p: Params, nsteps: int, every: int = 50, width: float = 0.6,
+                 forward_precision: int = None):
         self.p = p
         self.lib = L.load()
         h = ctypes.c_void_p()
         L.check(self.lib.phn_adjoint_create(ctypes.byref(p.c()), int(nsteps), int(every), float(width),
                                             ctypes.byref(h)))
         self.h = h
+        if forward_precision is not None:
+            L.check(self.lib.phn_adjoint_set_forward_precision(self.h, int(forward_precision)))
 
     def close(self):
         if self.h:

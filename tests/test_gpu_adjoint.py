@@ -101,3 +101,38 @@ def test_backward_is_deterministic_and_forward_matches_evolve():
         assert np.array_equal(x, y)
     with pytest.raises(Exception):
         PL.Adjoint(p, 61, 20)
+
+
+def test_fp64_forward_fp32_adjoint_within_1e4_of_fp64_adjoint():
+    """phn_adjoint_set_forward_precision(PHN_FP64) under an FP32 adjoint: the
+    forward runs the FP64 step kernels (J is the FP64 adjoint's, bit for bit),
+    checkpoints and reverse sweep stay FP32; the field gradient is within
+    1e-4 (relative L2) of the FP64 adjoint's.  Back to FP32 it is the plain
+    FP32 adjoint again, bit for bit; an FP64 adjoint refuses the switch."""
+    from phinum_gb300 import lattice as PL
+    from phinum_gb300 import _lib as L
+    N, steps, every = 32, 200, 50
+    kw, phi, pi = setup(N, 23)
+    sl = slice(N * N, -N * N)
+    with PL.Adjoint(PL.Params(N=N, precision=0, **kw), steps, every) as adj:
+        J64 = adj.forward(phi, pi)
+        d64, p64, g64 = adj.backward()
+        with pytest.raises(L.PhnError) as e:
+            L.check(adj.lib.phn_adjoint_set_forward_precision(adj.h, 1))
+        assert e.value.code == L.ERR_UNSUPPORTED
+    with PL.Adjoint(PL.Params(N=N, precision=1, **kw), steps, every, forward_precision=0) as adj:
+        Jm = adj.forward(phi, pi)
+        dm, pm, gm = adj.backward()
+        assert Jm == J64
+        assert np.linalg.norm(dm[sl] - d64[sl]) <= 1e-4 * np.linalg.norm(d64[sl])
+        assert np.linalg.norm(pm[sl] - p64[sl]) <= 1e-4 * np.linalg.norm(p64[sl])
+        assert abs(gm[0] - g64[0]) <= 1e-4 * abs(g64[0])
+        assert abs(gm[1] - g64[1]) <= 1e-4 * abs(g64[1])
+        L.check(adj.lib.phn_adjoint_set_forward_precision(adj.h, 1))
+        adj.forward(phi, pi)
+        back = adj.backward()
+    with PL.Adjoint(PL.Params(N=N, precision=1, **kw), steps, every) as adj:
+        adj.forward(phi, pi)
+        plain = adj.backward()
+    for x, y in zip(back, plain):
+        assert np.array_equal(x, y)
