@@ -9,7 +9,9 @@
 //      it), -y (periodic) and -z (open as on one rank, islands.cpp:224-236, or
 //      periodic) mask neighbours, hooking the larger root under the smaller
 //      by atomicCAS; a y or z union is skipped where the -x sites of both
-//      ends are on the mask too (those two are joined already, so are these);
+//      ends are on the mask too (those two are joined already, so are these).
+//      Edges that are multiples of 32 run steps 1-2 per 32 x 8 x 8 tile in
+//      shared memory (ccl_tile), then unite across tile faces (ccl_border);
 //   3. compress: parent[i] = root(i).  Links always point to smaller indices,
 //      so each root is the smallest site index of its island;
 //   4. number: islands are numbered by their root in increasing index order,
@@ -204,6 +206,33 @@ __device__ __forceinline__ bool ref_mask(double c, double p, double thr) {
 
 __device__ __noinline__ bool ref_mask_f64(float c, float p, double thr) { return ref_mask(c, p, thr); }
 
+// The island mask at site i = (x, y, z).
+template <typename T, bool KAHAN>
+__device__ __forceinline__ bool site_mask(const T *__restrict__ phi, const float *__restrict__ cphi,
+                                          const T *__restrict__ pi, const float *__restrict__ cpi, int N, int mode,
+                                          double thr, float thr_lo, float thr_hi, const Consts &k, size_t i, int x,
+                                          int y, int z) {
+  if (mode == PHN_ISLAND_REFERENCE) {
+    // islands.cpp:76: Phi*Phi*0.5 + Pi*Pi*0.5 > thres*thres*0.5 (thr
+    // holds the right side), in FP64.  Plain FP32 fields first try FP32:
+    // s = (c c + RN(p p)) / 2 in one fma is within 2^-23 relative of the
+    // exact sum, and thr_lo/thr_hi bracket thr by 2^-19 (both 0 when thr
+    // is outside [2^-100, 2^100]), so a sum outside the bracket decides
+    // the FP64 comparison; sums inside it, and NaN, take FP64.
+    if constexpr (std::is_same<T, float>::value && !KAHAN) {
+      const float cf = phi[i], pf = pi[i];
+      const float sf = 0.5f * fmaf(cf, cf, pf * pf);
+      if (thr_hi > 0.f && (sf > thr_hi || sf < thr_lo)) return sf > thr_hi;
+      return ref_mask_f64(cf, pf, thr);
+    } else {
+      const double c = val_k<KAHAN>(phi, cphi, i), p = val_k<KAHAN>(pi, cpi, i);
+      return ref_mask(c, p, thr);
+    }
+  }
+  using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+  return site_rho<A, KAHAN>(phi, cphi, pi, cpi, N, x, y, z, k) > (A)thr;
+}
+
 // The grid-stride loops below advance by whole warps of 32 consecutive
 // sites (blocks are multiples of 32 threads), so site i is always handled by
 // lane i % 32; ccl_merge relies on it to know which x links init made.
@@ -222,29 +251,7 @@ __global__ void ccl_init(const T *__restrict__ phi, const float *__restrict__ cp
     if (i < V) {
       int y, z;
       site_xyz(dn, N, i, x, y, z);
-      if (mode == PHN_ISLAND_REFERENCE) {
-        // islands.cpp:76: Phi*Phi*0.5 + Pi*Pi*0.5 > thres*thres*0.5 (thr
-        // holds the right side), in FP64.  Plain FP32 fields first try FP32:
-        // s = (c c + RN(p p)) / 2 in one fma is within 2^-23 relative of the
-        // exact sum, and thr_lo/thr_hi bracket thr by 2^-19 (both 0 when thr
-        // is outside [2^-100, 2^100]), so a sum outside the bracket decides
-        // the FP64 comparison; sums inside it, and NaN, take FP64.
-        if constexpr (std::is_same<T, float>::value && !KAHAN) {
-          const float cf = phi[i], pf = pi[i];
-          const float sf = 0.5f * fmaf(cf, cf, pf * pf);
-          if (thr_hi > 0.f && (sf > thr_hi || sf < thr_lo)) {
-            m = sf > thr_hi;
-          } else {
-            m = ref_mask_f64(cf, pf, thr);
-          }
-        } else {
-          const double c = val_k<KAHAN>(phi, cphi, i), p = val_k<KAHAN>(pi, cpi, i);
-          m = ref_mask(c, p, thr);
-        }
-      } else {
-        using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
-        m = site_rho<A, KAHAN>(phi, cphi, pi, cpi, N, x, y, z, k) > (A)thr;
-      }
+      m = site_mask<T, KAHAN>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, i, x, y, z);
     }
     // runs of mask sites along x within this segment: each site points at
     // the run's first site (a smaller index, as every link must)
@@ -317,6 +324,129 @@ __global__ void ccl_merge(int *__restrict__ parent, int N, const DivN dn, int zp
     const size_t jy = (y == 0) ? i + (size_t)(N - 1) * N : i - N;
     if (parent[jy] >= 0 && !(left && parent[jy - 1] >= 0)) unite(parent, (int)i, (int)jy);
     if (z > 0 || zper) {
+      const size_t jz = (z == 0) ? i + (size_t)(N - 1) * NN : i - NN;
+      if (parent[jz] >= 0 && !(left && parent[jz - 1] >= 0)) unite(parent, (int)i, (int)jz);
+    }
+  }
+}
+
+// Tiled labelling for edges that are multiples of 32 (x) and 8 (y, z): a
+// block labels a TILE_X x TILE_Y x TILE_Z tile in shared memory first (the
+// same union-find on tile-local indices, whose order is the sites' index
+// order, with the same skip rule), writes each mask site's link to the
+// global index of its tile root, and ccl_border then unites across tile
+// faces only: the -x union at lx = 0, -y at ly = 0, -z at lz = 0 (the skip
+// rule needs the -x pair, which lies on the same face).  Shared-memory
+// unions replace most global root searches.
+constexpr int TILE_X = 32, TILE_Y = 8, TILE_Z = 8, TILE_SITES = TILE_X * TILE_Y * TILE_Z;
+
+__device__ __forceinline__ int find_root_sh(volatile int *lp, int x) {
+  int p = lp[x];
+  while (p != x) {
+    const int gp = lp[p];
+    if (gp != p) lp[x] = gp;  // path halving, as find_root
+    x = p;
+    p = gp;
+  }
+  return x;
+}
+
+__device__ __forceinline__ int find_root_sh_ro(volatile int *lp, int x) {
+  int p = lp[x];
+  while (p != x) {
+    x = p;
+    p = lp[x];
+  }
+  return x;
+}
+
+__device__ void unite_sh(int *lp, int a, int b) {
+  while (true) {
+    a = find_root_sh(lp, a);
+    b = find_root_sh(lp, b);
+    if (a == b) return;
+    if (a < b) {
+      const int t = a;
+      a = b;
+      b = t;
+    }
+    if (atomicCAS(&lp[a], a, b) == a) return;
+  }
+}
+
+template <typename T, bool KAHAN>
+__global__ void __launch_bounds__(TILE_X *TILE_Y) ccl_tile(const T *__restrict__ phi, const float *__restrict__ cphi,
+                                                         const T *__restrict__ pi, const float *__restrict__ cpi,
+                                                         int N, int mode, double thr, float thr_lo, float thr_hi,
+                                                         const Consts k, int *__restrict__ parent) {
+  static_assert(TILE_X == 32, "a tile row is one warp");
+  __shared__ int lp[TILE_SITES];
+  const int lx = threadIdx.x, ly = threadIdx.y;
+  const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y, z0 = blockIdx.z * TILE_Z;
+  const int x = x0 + lx, y = y0 + ly;
+  const size_t NN = (size_t)N * N;
+  // a warp is one tile row: x-runs link to their first site by ballot, as
+  // in ccl_init (the tile row starts the segment, so lx = 0 links nowhere)
+  const unsigned full = 0xffffffffu;
+#pragma unroll 1
+  for (int lz = 0; lz < TILE_Z; ++lz) {
+    const int s = (lz * TILE_Y + ly) * TILE_X + lx;
+    const size_t i = (size_t)(z0 + lz) * NN + (size_t)y * N + x;
+    const bool m = site_mask<T, KAHAN>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, i, x, y, z0 + lz);
+    const unsigned mb = __ballot_sync(full, m);
+    const unsigned heads = mb & ~(mb << 1);
+    lp[s] = m ? s - lx + (31 - __clz(heads & (full >> (31 - lx)))) : -1;
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int lz = 0; lz < TILE_Z; ++lz) {
+    const int s = (lz * TILE_Y + ly) * TILE_X + lx;
+    if (((volatile int *)lp)[s] < 0) continue;
+    const bool left = lx > 0 && ((volatile int *)lp)[s - 1] >= 0;  // linked above
+    if (ly > 0) {
+      const int t = s - TILE_X;
+      if (((volatile int *)lp)[t] >= 0 && !(left && ((volatile int *)lp)[t - 1] >= 0)) unite_sh(lp, s, t);
+    }
+    if (lz > 0) {
+      const int t = s - TILE_X * TILE_Y;
+      if (((volatile int *)lp)[t] >= 0 && !(left && ((volatile int *)lp)[t - 1] >= 0)) unite_sh(lp, s, t);
+    }
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int lz = 0; lz < TILE_Z; ++lz) {
+    const int s = (lz * TILE_Y + ly) * TILE_X + lx;
+    const size_t i = (size_t)(z0 + lz) * NN + (size_t)y * N + x;
+    int g = -1;
+    if (lp[s] >= 0) {
+      const int r = find_root_sh_ro(lp, s);
+      const int rz = r / (TILE_X * TILE_Y), ry = (r / TILE_X) % TILE_Y, rx = r % TILE_X;
+      g = (int)((size_t)(z0 + rz) * NN + (size_t)(y0 + ry) * N + (x0 + rx));
+    }
+    parent[i] = g;
+  }
+}
+
+// Unions across tile faces (see ccl_tile); one thread per site, sites off
+// the faces return at once.
+__global__ void ccl_border(int *__restrict__ parent, int N, const DivN dn, int zper) {
+  const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+    int x, y, z;
+    site_xyz(dn, N, i, x, y, z);
+    const bool fx = (x % TILE_X) == 0, fy = (y % TILE_Y) == 0, fz = (z % TILE_Z) == 0 && (z > 0 || zper);
+    if (!(fx || fy || fz)) continue;
+    if (parent[i] < 0) continue;
+    const bool left = x > 0 && parent[i - 1] >= 0;
+    if (fx) {
+      const size_t jx = x == 0 ? i + N - 1 : i - 1;
+      if (parent[jx] >= 0) unite(parent, (int)i, (int)jx);
+    }
+    if (fy) {
+      const size_t jy = (y == 0) ? i + (size_t)(N - 1) * N : i - N;
+      if (parent[jy] >= 0 && !(left && parent[jy - 1] >= 0)) unite(parent, (int)i, (int)jy);
+    }
+    if (fz) {
       const size_t jz = (z == 0) ? i + (size_t)(N - 1) * NN : i - NN;
       if (parent[jz] >= 0 && !(left && parent[jz - 1] >= 0)) unite(parent, (int)i, (int)jz);
     }
@@ -768,11 +898,22 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
     thr_lo = (float)(thr * (1.0 - 0x1p-19));
     thr_hi = (float)(thr * (1.0 + 0x1p-19));
   }
-  if (cphi)
-    ccl_init<T, true><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, dn, mode, thr, thr_lo, thr_hi, k, s->parent);
-  else
-    ccl_init<T, false><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, dn, mode, thr, thr_lo, thr_hi, k, s->parent);
-  ccl_merge<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, dn, zper);
+  if (N % TILE_X == 0 && N % TILE_Y == 0 && N % TILE_Z == 0) {
+    const dim3 tg(N / TILE_X, N / TILE_Y, N / TILE_Z), tb(TILE_X, TILE_Y);
+    if (cphi)
+      ccl_tile<T, true><<<tg, tb, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, s->parent);
+    else
+      ccl_tile<T, false><<<tg, tb, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, s->parent);
+    ccl_border<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, dn, zper);
+  } else {
+    if (cphi)
+      ccl_init<T, true><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, dn, mode, thr, thr_lo, thr_hi, k,
+                                                   s->parent);
+    else
+      ccl_init<T, false><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, dn, mode, thr, thr_lo, thr_hi, k,
+                                                    s->parent);
+    ccl_merge<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, dn, zper);
+  }
   ccl_compress<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk);
   int *tile = s->blk + s->nblk;
   ccl_scan_tiles<<<s->ntile, SCAN_TILE, 0, st>>>(s->blk, s->nblk, tile);
