@@ -17,7 +17,9 @@
 //   4. number: islands are numbered by their root in increasing index order,
 //      which is the order in which the reference's linear scan seeds BFS, so
 //      the labels equal the reference's b[] labels;
-//   5. statistics per island (size, energies, <phi>, peak) with FP64 atomics.
+//   5. statistics per island (size, energies, <phi>, peak): runs reduced in
+//      the warp, merged per block in shared memory, then added to the FP64
+//      per-island sums once per island per block; 6. the records.
 // Every loop terminates: a root search follows strictly decreasing indices,
 // and a union retry strictly decreases the larger root.
 #include <math.h>
@@ -26,6 +28,7 @@
 
 #include <type_traits>
 
+#include "ccl_math.h"
 #include "phn_internal.h"
 
 namespace phn {
@@ -48,29 +51,6 @@ struct IslState {
   int *seed;                    // root site (interior linear index)
   phn_island *rec;              // [cap] the records handed to the caller
 };
-
-// Division of site indices (< 2^31) by the lattice edge N without a divide:
-// q = umulhi(n, m) >> s with s = floor(log2 N), m = ceil(2^(32+s) / N)
-// (Granlund and Montgomery, PLDI 1994).  m < 2^32, and its error e = m N -
-// 2^(32+s) < N <= 2^(s+1) makes n e < 2^(32+s) for n < 2^31, so n m / 2^(32+s)
-// exceeds n / N by less than 1/N and the floor is exact.  Powers of two
-// shift (m = 0).
-struct DivN {
-  unsigned m;
-  int s;
-};
-
-static DivN make_divn(unsigned d) {
-  int s = 0;
-  while ((2u << s) <= d) ++s;  // floor(log2 d)
-  if ((d & (d - 1)) == 0) return DivN{0u, s};
-  const unsigned long long num = 1ull << (32 + s);
-  return DivN{(unsigned)((num + d - 1) / d), s};
-}
-
-__device__ __forceinline__ unsigned div_n(const DivN &q, unsigned n) {
-  return q.m ? __umulhi(n, q.m) >> q.s : n >> q.s;
-}
 
 // x, y, z of site i (i < 2^31)
 __device__ __forceinline__ void site_xyz(const DivN &q, int N, size_t i, int &x, int &y, int &z) {
@@ -214,16 +194,12 @@ __device__ __forceinline__ bool site_mask(const T *__restrict__ phi, const float
                                           int y, int z) {
   if (mode == PHN_ISLAND_REFERENCE) {
     // islands.cpp:76: Phi*Phi*0.5 + Pi*Pi*0.5 > thres*thres*0.5 (thr
-    // holds the right side), in FP64.  Plain FP32 fields first try FP32:
-    // s = (c c + RN(p p)) / 2 in one fma is within 2^-23 relative of the
-    // exact sum, and thr_lo/thr_hi bracket thr by 2^-19 (both 0 when thr
-    // is outside [2^-100, 2^100]), so a sum outside the bracket decides
-    // the FP64 comparison; sums inside it, and NaN, take FP64.
+    // holds the right side), in FP64.  Plain FP32 fields first try FP32
+    // (ref_mask_f32, ccl_math.h); sums within the bracket, and NaN, take FP64.
     if constexpr (std::is_same<T, float>::value && !KAHAN) {
       const float cf = phi[i], pf = pi[i];
-      const float sf = 0.5f * fmaf(cf, cf, pf * pf);
-      if (thr_hi > 0.f && (sf > thr_hi || sf < thr_lo)) return sf > thr_hi;
-      return ref_mask_f64(cf, pf, thr);
+      const int d = ref_mask_f32(cf, pf, thr_lo, thr_hi);
+      return d >= 0 ? d == 1 : ref_mask_f64(cf, pf, thr);
     } else {
       const double c = val_k<KAHAN>(phi, cphi, i), p = val_k<KAHAN>(pi, cpi, i);
       return ref_mask(c, p, thr);
@@ -893,11 +869,8 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
   const int gb = grid_blocks(V);
   const Consts k = consts_now(h);
   const DivN dn = make_divn((unsigned)N);
-  float thr_lo = 0.f, thr_hi = 0.f;  // the FP32 bracket of the reference mask (ccl_init)
-  if (thr >= 0x1p-100 && thr <= 0x1p100) {
-    thr_lo = (float)(thr * (1.0 - 0x1p-19));
-    thr_hi = (float)(thr * (1.0 + 0x1p-19));
-  }
+  float thr_lo, thr_hi;  // the FP32 bracket of the reference mask (site_mask)
+  mask_bracket(thr, &thr_lo, &thr_hi);
   if (N % TILE_X == 0 && N % TILE_Y == 0 && N % TILE_Z == 0) {
     const dim3 tg(N / TILE_X, N / TILE_Y, N / TILE_Z), tb(TILE_X, TILE_Y);
     if (cphi)
