@@ -56,6 +56,10 @@ def test_null_handles_are_status_codes(L):
         lambda: lib.phn_reset(None),
         lambda: lib.phn_time(None, ctypes.byref(d), ctypes.byref(i)),
         lambda: lib.phn_conformal_time(None, ctypes.byref(d), ctypes.byref(d)),
+        lambda: lib.phn_adjoint_forward(None, buf, buf, ctypes.byref(d)),
+        lambda: lib.phn_adjoint_backward(None, None, None, None),
+        lambda: lib.phn_adjoint_set_forward_precision(None, 0),
+        lambda: lib.phn_adjoint_info(None, None, None, None),
     ]
     for c in calls:
         assert c() == L.ERR_INVALID
