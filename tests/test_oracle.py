@@ -108,7 +108,7 @@ def test_spectrum_counts_cover_every_mode():
 @pytest.mark.parametrize("theory,N,Nc,expansion", [(0, 6, 1, 0), (1, 10, 1, 0), (0, 8, 3, 0), (2, 6, 1, 0),
                                                    (3, 6, 1, 0), (4, 8, 1, 0), (5, 6, 1, 0), (0, 6, 2, 1),
                                                    (1, 8, 1, 1), (2, 6, 1, 1), (3, 6, 1, 1), (4, 6, 1, 1),
-                                                   (5, 6, 1, 1)])
+                                                   (5, 6, 1, 1), (1, 6, 4, 0), (1, 6, 3, 1), (0, 6, 4, 1)])
 def test_oracle_matches_reference_live(theory, N, Nc, expansion, tmp_path):
     """Runs the reference pin in a child process on fresh random inputs."""
     import subprocess
