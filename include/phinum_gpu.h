@@ -413,10 +413,15 @@ int phn_adjoint_info(const phn_adjoint *a, double *J, double *forward_ms, double
  * (kept until the process exits), which limits N to 1024; larger lattices
  * get PHN_ERR_INVALID.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race, so serialise them.  Returns after the result is on the host.  The
- * expanding box's averages are those at tau = T0 (scale factor
- * sqrt(1 + 2 H_0 T0)). */
+ * stream capture.  The address is kept with the ID of the CUDA context it
+ * belongs to and looked up again when the calling thread's current context
+ * is another one (after the device was reset, or under a context the host
+ * created with the driver API), so such a call is a set-up call too.  All
+ * calls share the array: calls that overlap on the GPU race, so serialise
+ * them.  The call synchronises `stream` and returns after the result is on
+ * the host.  out->t is T0: the fields are taken as the state at tau = T0, and
+ * the expanding box's averages use that time's scale factor
+ * sqrt(1 + 2 H_0 T0). */
 int phn_volume_averages_noalloc(const phn_params *params, const void *d_phi, const void *d_pi, void *stream,
                                 phn_averages *out);
 

@@ -15,6 +15,9 @@
 // (leapfrog.cu, observation-only mode), launched with one block per 32x8
 // column of the lattice marching all N planes, so the number of block records
 // is ceil(N/32) * ceil(N/8); the fold is finalize_averages.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <mutex>
 
 #include "phn_internal.h"
@@ -31,26 +34,75 @@ constexpr size_t kScratchDoubles = kOutOffset + 32;            // output record:
 
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
+// The device address of the array belongs to the CUDA context the module was
+// loaded into.  A device reset (cudaDeviceReset, by this or another runtime in
+// the process) or a context the host created with the driver API gives the
+// same device another context, in which the old address means nothing.  So
+// the address is cached per device together with the unique ID of the context
+// it was looked up in (cuCtxGetId: IDs are never reused in a process), and
+// looked up again when the calling thread's current context has another ID.
 constexpr int kMaxDevices = 64;
+struct ScratchSlot {
+  unsigned long long ctx_id;  // 0: no set-up on this device yet
+  double *addr;
+};
 std::mutex g_mu;
-double *g_scratch_addr[kMaxDevices];  // device address of the array, per device
+ScratchSlot g_slot[kMaxDevices];
+
+// cuCtxGetCurrent / cuCtxGetId from the driver through the runtime (the
+// library does not link libcuda); null when the driver lacks them, and then
+// every call looks the address up.
+PFN_cuCtxGetCurrent_v4000 g_ctx_current = nullptr;
+PFN_cuCtxGetId_v12000 g_ctx_id = nullptr;
+std::once_flag g_entry_once;
+
+void load_entry_points() {
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    g_ctx_current = (PFN_cuCtxGetCurrent_v4000)fn;
+  fn = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    g_ctx_id = (PFN_cuCtxGetId_v12000)fn;
+}
+
+// ID of the context current on the calling thread; 0 when none is current yet
+// (a fresh thread, or right after a reset) or the driver cannot tell.
+unsigned long long current_context_id() {
+  if (!g_ctx_current || !g_ctx_id) return 0;
+  CUcontext c = nullptr;
+  if (g_ctx_current(&c) != CUDA_SUCCESS || !c) return 0;
+  unsigned long long id = 0;
+  if (g_ctx_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // The array's name in host code is only a host-side stand-in; the device
-// address comes from cudaGetSymbolAddress, once per device, with that device
-// current (it is the caller's current device here).
+// address comes from cudaGetSymbolAddress, with the device current (it is the
+// caller's current device here), at set-up: the first call on a device, and
+// again whenever that device's context has changed since.
 int scratch_address(double **out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return phn::cuda_error(e, "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return phn::set_error(PHN_ERR_UNSUPPORTED, "device %d >= %d", dev, kMaxDevices);
+  std::call_once(g_entry_once, load_entry_points);
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return phn::cuda_error(e, "cudaGetSymbolAddress(scratch)");
-    g_scratch_addr[dev] = (double *)p;
+  ScratchSlot &s = g_slot[dev];
+  const unsigned long long now = current_context_id();
+  if (s.addr && now != 0 && now == s.ctx_id) {
+    *out = s.addr;
+    return PHN_OK;
   }
-  *out = g_scratch_addr[dev];
+  // set-up (this also makes the runtime's context current when none was)
+  void *p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return phn::cuda_error(e, "cudaGetSymbolAddress(scratch)");
+  s.addr = (double *)p;
+  s.ctx_id = current_context_id();
+  *out = s.addr;
   return PHN_OK;
 }
 
@@ -102,7 +154,7 @@ extern "C" int phn_volume_averages_noalloc(const phn_params *params, const void 
   e = cudaMemcpyAsync(out, d_out, sizeof(phn_averages), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_error(e, "averages readback");
-  out->t = 0.0;
+  out->t = params->T0;  // the state is taken as the one at tau = T0, as a fresh handle stamps it
   if (out->nonfinite > 0) return set_error(PHN_ERR_NONFINITE, "%.0f non-finite field values", out->nonfinite);
   return PHN_OK;
 }

@@ -64,3 +64,19 @@ def test_null_handles_are_status_codes(L):
     for c in calls:
         assert c() == L.ERR_INVALID
     assert lib.phn_destroy(None) == L.OK  # like free(NULL)
+
+
+def test_noalloc_scratch_limit_is_exactly_n_1024(L):
+    """The allocation-free averages hold ceil(N/32) * ceil(N/8) block records
+    in a fixed array of 4096: the size check (host only, before any CUDA call)
+    must pass every N <= 1024 and reject every larger N.  With NULL field
+    pointers an accepted size then fails on the NULL check instead."""
+    from phinum_gb300 import lattice as PL
+    lib = L.load()
+    out = L.PhnAverages()
+    for N in list(range(2, 80)) + list(range(980, 1100)):
+        p = PL.Params(N=N, precision=1)
+        assert lib.phn_volume_averages_noalloc(ctypes.byref(p.c()), None, None, None, ctypes.byref(out)) == \
+            L.ERR_INVALID
+        assert (b"N <= 1024" in lib.phn_last_error()) == (N > 1024), N
+        assert ((N + 31) // 32) * ((N + 7) // 8) <= 4096 or N > 1024
