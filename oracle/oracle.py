@@ -232,6 +232,27 @@ def run_loop(p: Params, phi: np.ndarray, pi: np.ndarray, nsteps: int, tso: float
     return rows[:n], clock
 
 
+def false_vacuum_decayed(interaction: float, theory: int) -> bool:
+    """false_vacuum_decayed() (fieldanalysis.cpp:887-893): for theories 0, 1
+    and 4 the vacuum has decayed when <V> < 0, <V> is NaN, or <V> * 0 != 0
+    (an infinity); the other theories never stop."""
+    v = float(interaction)
+    if theory not in (0, 1, 4):
+        return False
+    return v < 0 or v != v or v * 0.0 != 0.0
+
+
+def stop_step(rows: np.ndarray, theory: int, step_of_row) -> int:
+    """Where main.cpp:77-90 breaks: false_vacuum_decayed() reads the averages
+    of the last row computed, so the loop stops at the first row whose
+    interaction decays it, before that step's evolve().  step_of_row(i) is
+    row i's step count; -1 when no row decays it."""
+    for i in range(rows.shape[0]):
+        if false_vacuum_decayed(rows[i, 15], theory):
+            return int(step_of_row(i))
+    return -1
+
+
 def spectrum_bins(p: Params):
     nb, bs = _I(), _D()
     _load().orc_spectrum_bins(ctypes.byref(_cp(p)), ctypes.byref(nb), ctypes.byref(bs))
@@ -318,6 +339,12 @@ def islands(p: Params, phi: np.ndarray, pi: np.ndarray, thres: float, mode: int 
 
 # ------------------------------------------------------ the reference pin ---
 REF_DIR = os.path.join(HERE, "_ref")
+
+
+def ref_dir() -> str:
+    """The reference tree the pin builds from: REF_DIR, with the default of
+    oracle/build_ref.sh."""
+    return os.environ.get("REF_DIR", "/root/reference")
 
 
 def ref_path(theory: int = 0, precision: str = "f64", expansion: int = 0) -> str:
@@ -438,6 +465,21 @@ class Reference:
         rows = np.zeros((max_rows, AVG_LEN))
         n = self.lib.ref_run_loop(int(nsteps), float(tso), _ptr(rows), max_rows)
         return rows[:n]
+
+    def false_vacuum_decayed(self, interaction: float) -> bool:
+        """The reference's false_vacuum_decayed() with avgInteraction set."""
+        self.lib.ref_false_vacuum_decayed.argtypes = [_D]
+        self.lib.ref_false_vacuum_decayed.restype = _I
+        return bool(self.lib.ref_false_vacuum_decayed(float(interaction)))
+
+    def run_until_decayed(self, nsteps: int, tso: float, max_rows: int = 10000):
+        """main.cpp:77-90 with the false-vacuum break: (rows, stop step or -1)."""
+        self.lib.ref_run_until_decayed.argtypes = [_I, _D, _PD, _I, _PI]
+        self.lib.ref_run_until_decayed.restype = _I
+        rows = np.zeros((max_rows, AVG_LEN))
+        stop = _I()
+        n = self.lib.ref_run_until_decayed(int(nsteps), float(tso), _ptr(rows), max_rows, ctypes.byref(stop))
+        return rows[:n], stop.value
 
     def spectrum(self):
         nb = self.lib.ref_nbins()

@@ -224,6 +224,38 @@ int ref_run_loop(int nsteps, double tso, double *rows, int max_rows) {
   return nrows;
 }
 
+/* The reference's false_vacuum_decayed() (fieldanalysis.cpp:887-893) on an
+ * avgInteraction of v. */
+int ref_false_vacuum_decayed(double v) {
+  LocalLattice::avgInteraction = (pseudo_double)v;
+  return false_vacuum_decayed() ? 1 : 0;
+}
+
+/* main.cpp:77-90 without islands and spectra, with an explicit step cap:
+ * Print_AveragesExtrema(), then the false_vacuum_decayed() break, then
+ * evolve().  Rows as ref_run_loop; *stop receives total_stepcount when the
+ * loop broke, -1 when it ran all nsteps. */
+int ref_run_until_decayed(int nsteps, double tso, double *rows, int max_rows, int *stop) {
+  TSO = (pseudo_double)tso;
+  int nrows = 0;
+  int count = 0;
+  *stop = -1;
+  for (reset(); count < nsteps; evolve(), ++count) {
+    const bool due = !(numeric::total_stepcount > 0 &&
+                       LocalLattice::tau < numeric::LastSOoutput + TSO);
+    Print_AveragesExtrema();
+    if (due && nrows < max_rows) {
+      record((double)numeric::LastSOoutput, rows + (size_t)nrows * REF_AVG_LEN);
+      ++nrows;
+    }
+    if (false_vacuum_decayed()) {
+      *stop = numeric::total_stepcount;
+      break;
+    }
+  }
+  return nrows;
+}
+
 int ref_nbins() { return MomentumSpace::nTBins; }
 double ref_binsize() { return (double)MomentumSpace::binsizeT; }
 

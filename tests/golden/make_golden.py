@@ -200,6 +200,38 @@ def run_filter_case(name: str) -> None:
     print(f"filter/{name}")
 
 
+# The false-vacuum break of main.cpp:85-89: lattice params, input seed, phi0,
+# steps, TSO, a site of Pi set to NaN (-1: none).  The tilted well with a
+# strong tilt rolls from phi0 = 0.8 towards negative phi, and <V> turns
+# negative mid-run; a NaN in Pi reaches phi with the first drift, so the
+# reference stops at its second row.
+FVD_CASES = {
+    "fvd_t1_n16": (dict(N=16, Nc=1, theory=1, mass_mode=-1, lambda_mode=1, m_sqr=1.0, kappa=1.0, h=0.6),
+                   51, 0.8, 400, 0.2, -1),
+    "fvd_t0_n16_nan": (dict(N=16, Nc=1, **PHI6), 52, SQRT6, 100, 0.2, 16 * 16 * 5 + 16 * 3 + 7),
+}
+
+
+def run_fvd_case(name: str) -> None:
+    """The reference's run loop with its false_vacuum_decayed() break: the
+    rows it printed and the step count at the break."""
+    from oracle import oracle as O
+    import inputs
+    pd, seed, phi0, steps, tso, nan_site = FVD_CASES[name]
+    p = O.Params(**{"a": 0.25, "dt": 0.08, "T0": 0.0, **pd})
+    phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, seed, phi0=phi0)
+    Phi, Pi = O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc)
+    if nan_site >= 0:
+        Pi[nan_site] = np.nan
+    R = O.Reference(p)
+    R.set_fields(Phi, Pi)
+    rows, stop = R.run_until_decayed(steps, tso)
+    os.makedirs(os.path.join(HERE, "fvd"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "fvd", f"{name}.npz"), params=json.dumps(pd), seed=seed, phi0=phi0,
+                        steps=steps, tso=tso, nan_site=nan_site, rows=rows, stop=stop)
+    print(f"fvd/{name}: rows={len(rows)} stop={stop}")
+
+
 def run_ic_case(name: str) -> None:
     from oracle import oracle as O
     pd, ic = IC_CASES[name]
@@ -297,6 +329,13 @@ def main() -> None:
         for name in CONFIG_CASES:
             subprocess.run([sys.executable, os.path.abspath(__file__), "--config-case", name], check=True)
         return
+    if len(sys.argv) > 2 and sys.argv[1] == "--fvd-case":
+        run_fvd_case(sys.argv[2])
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "--fvd":
+        for name in FVD_CASES:
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--fvd-case", name], check=True)
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "--ic":
         for name in IC_CASES:
             subprocess.run([sys.executable, os.path.abspath(__file__), "--ic-case", name], check=True)
@@ -319,6 +358,8 @@ def main() -> None:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--config-case", name], check=True)
     for name in FILTER_CASES:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--filter-case", name], check=True)
+    for name in FVD_CASES:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--fvd-case", name], check=True)
 
 
 if __name__ == "__main__":

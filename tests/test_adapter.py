@@ -7,8 +7,10 @@ import subprocess
 
 import pytest
 
+from oracle import oracle as O
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = O.ref_dir()
 
 
 @pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "dynamics.cpp")), reason="reference tree not present")
