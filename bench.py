@@ -13,15 +13,24 @@ phi0 = sqrt(6), vacuum amplitude per mode, modes above pi/(2 dx) zeroed);
 value     site-updates/s over K steps, fields resident in HBM, device time
           (CUDA events on the handle's stream), max over ranks x ranks.
 e2e       the same metric through the C ABI with host buffers: each e2e
-          iteration uploads phi, pi (reference layout, FP64, pinned), runs one
-          TSO interval (50 steps + one SO row) and downloads phi, pi.
-roofline  the plain step kernel: 16 algorithmic bytes per site (read phi, pi;
-          write pi, phi') over its mean launch time, against the measured HBM
-          copy bandwidth in MEASURED_PEAKS.json.
+          iteration uploads phi, pi (reference layout, pinned float arrays as
+          the reference's single-precision build holds them; e2e.f64_host:
+          double arrays, its default build), runs one TSO interval (50 steps +
+          one SO row) and downloads phi, pi.
+roofline  the autotuned step kernel: 16 algorithmic bytes per site (read phi,
+          pi; write pi, phi') over its mean launch time, against the measured
+          HBM copy bandwidth in MEASURED_PEAKS.json; traffic from the kernel's
+          ncu summary when that summary covers the same sources and variant.
+clocks    SM clock and clock-event reasons: nvidia-smi every 200 ms and NVML
+          every millisecond during the timed region.
 cpu_baseline / --impl reference
-          the CPU oracle (C restatement of the reference loop, FP64, the
-          reference's -O3 -ffast-math flags, OpenMP over z-slabs) on a bounded
-          number of steps of the same lattice.
+          the reference loop restated in C (the oracle), compiled with the
+          reference's -O3 -ffast-math flags, OpenMP over z-slabs, all host
+          threads, a bounded number of steps of the same lattice: the float
+          build (doubleprecision -1, pinned bit-identical to the reference's
+          own float build) like for like with this FP32 line, and the double
+          build (cpu_baseline_fp64) for the FP64 GPU line; like_for_like holds
+          both ratios.
 Multi-GPU: replicas only -- every rank evolves its own lattice; no collective
 on the data path.
 
@@ -94,8 +103,10 @@ class ClockSampler:
 
     def __init__(self, gpu_index: int):
         self.idx, self.samples, self.proc = gpu_index, [], None
+        self.nvml = NvmlPoller(gpu_index)
 
     def __enter__(self):
+        self.nvml.start()
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -113,6 +124,7 @@ class ClockSampler:
                 self.samples.append(parts)
 
     def __exit__(self, *exc):
+        self.nvml.stop()
         if self.proc:
             self.proc.terminate()
             try:
@@ -121,14 +133,69 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[j] for s in self.samples for j in range(4) if s[5 + j].lower() == "active"})
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+        reasons = {names[j] for s in self.samples for j in range(4) if s[5 + j].lower() == "active"}
+        # NVML polled every millisecond inside the timed region (nvidia-smi's
+        # 200 ms period misses regions of a few milliseconds)
+        sm += [float(m) for m, _ in self.nvml.samples]
+        reasons |= {n for _, bits in self.nvml.samples for n, b in NvmlPoller.REASONS.items() if bits & b}
+        if self.nvml.max_mhz:
+            mx.append(float(self.nvml.max_mhz))
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples), "samples_nvml": len(self.nvml.samples)}
+
+
+class NvmlPoller:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml, the
+    driver's library) every millisecond on a thread while the timed work runs
+    in ctypes calls, which release the GIL.  Reads only; no setting changes."""
+
+    REASONS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+               "hw_thermal_slowdown": 0x40}
+
+    def __init__(self, index: int):
+        import ctypes
+        self.samples, self.max_mhz, self.h, self.lib = [], None, None, None
+        self._stop = threading.Event()
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(int(index), ctypes.byref(h)) != 0:
+                return
+            self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            mhz = ctypes.c_uint()
+            if lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mhz)) == 0:  # NVML_CLOCK_SM
+                self.max_mhz = mhz.value
+            self.lib, self.h = lib, h
+        except (OSError, AttributeError):
+            self.lib = None
+
+    def _run(self):
+        import ctypes
+        mhz, bits = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self._stop.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.h, ctypes.byref(bits)) == 0:
+                self.samples.append((mhz.value, bits.value))
+            time.sleep(0.001)
+
+    def start(self):
+        if self.lib is not None:
+            self._stop.clear()
+            self.t = threading.Thread(target=self._run, daemon=True)
+            self.t.start()
+
+    def stop(self):
+        if self.lib is not None:
+            self._stop.set()
+            self.t.join(timeout=5)
 
 
 def peaks():
@@ -140,25 +207,49 @@ def peaks():
     return 6800.0, "fallback"
 
 
-PROFILE_OF_PATH = {2: "leapfrog_f32_512.md", 3: "leapfrog_f32_x4_512.md"}  # PHN_PATH_TMA, PHN_PATH_X4
+# ncu summaries of the FP32 step kernels at 512^3 (PHN_PATH_TMA, PHN_PATH_X4)
+# and the sources each kernel is compiled from
+PROFILE_OF_PATH = {2: ("leapfrog_f32_512.md", ("leapfrog_tma.cu", "tma.cuh", "kick.cuh")),
+                   3: ("leapfrog_f32_x4_512.md", ("leapfrog_x4.cu", "kick.cuh"))}
 
 
-def traffic_from_profile(path_kind: int):
-    """DRAM bytes per launch of the FP32 step kernel of the given path at
-    512^3, from its committed ncu summary (line 'traffic_bytes_per_launch: X');
-    None when that kernel has no summary."""
+def source_digest(files) -> str:
+    """SHA-256 (first 16 hex digits) of the kernel's source files, in order."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in files:
+        with open(os.path.join(ROOT, "phinum_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def traffic_from_profile(path_kind: int, variant: int):
+    """DRAM bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)
+    of the FP32 step kernel at 512^3 from its committed ncu summary, which
+    records the traffic, the variant captured and the digest of the sources it
+    was compiled from.  ncu cannot run inside a timed benchmark, so the figure
+    is used only when the summary covers this variant and these exact sources;
+    otherwise (None, why)."""
     if path_kind not in PROFILE_OF_PATH:
-        return None
-    path = os.path.join(ROOT, "profiles", PROFILE_OF_PATH[path_kind])
+        return None, "no ncu summary for this kernel"
+    name, files = PROFILE_OF_PATH[path_kind]
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
-        return None
+        return None, f"profiles/{name} missing"
+    rec = {}
     for line in open(path):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+        if ":" in line and line.split(":", 1)[0].strip() in ("traffic_bytes_per_launch", "source_sha256_16",
+                                                              "variant"):
+            k, v = line.split(":", 1)
+            rec[k.strip()] = v.strip().split()[0] if v.strip() else ""
+    if rec.get("source_sha256_16") != source_digest(files):
+        return None, f"profiles/{name} was captured on other sources (stale)"
+    if rec.get("variant") != str(variant):
+        return None, f"profiles/{name} covers variant {rec.get('variant')}, this run uses {variant}"
+    try:
+        return float(rec["traffic_bytes_per_launch"]), f"profiles/{name} (ncu, same sources and variant)"
+    except (KeyError, ValueError):
+        return None, f"profiles/{name} has no traffic line"
 
 
 _FIELDS = {}
@@ -231,9 +322,10 @@ def measure_gpu(args, dist: Dist):
     t_launch = ms_plain / 1e3 / k_plain
     achieved = BYTES_PER_SITE[1] * sites / t_launch / 1e9
     peak, kind = peaks()
+    traffic, traffic_src = traffic_from_profile(pk.value, tv.value) if N == 512 else (None, "not 512^3")
     out["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                        "frac": round(achieved / peak, 4),
-                       "traffic": traffic_from_profile(pk.value) if N == 512 else None,
+                       "traffic": traffic, "traffic_source": traffic_src,
                        "kernel": kernel_name, "peak_kind": f"{kind} hbm_gbs",
                        "algorithmic_bytes_per_launch": BYTES_PER_SITE[1] * sites,
                        "mean_launch_ms": round(t_launch * 1e3, 4)}
@@ -248,81 +340,59 @@ def measure_gpu(args, dist: Dist):
     elat = PL.Lattice(PL.Params(N=N, precision=L.FP32))
     # the kernel the autotuner chose above
     L.check(lib.phn_set_path(elat.h, L.PATH_PLAIN) if tv.value < 0 else lib.phn_set_variant(elat.h, tv.value))
-    # the host fields as a caller prepares them just before the call: fresh
-    # arrays (the same values), pinned
-    ephi, epi = phi.copy(), pi.copy()
-    for a in (ephi, epi):
-        L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
-    hphi, hpi = np.empty_like(phi), np.empty_like(pi)
-    for a in (hphi, hpi):
-        L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
-    its, phases = [], []
 
-    def e2e_iter():
-        t0 = time.perf_counter()
-        elat.upload(ephi, epi)
-        t1 = time.perf_counter()
-        elat.run_loop(TSO_STEPS, 1.0, max_rows=2)
-        t2 = time.perf_counter()
-        L.check(lib.phn_download(elat.h, hphi.ctypes.data_as(L._PD), hpi.ctypes.data_as(L._PD)))
-        t3 = time.perf_counter()
-        return t3 - t0, (t1 - t0, t2 - t1, t3 - t2)
+    def e2e_leg(host_dtype, upload, download, n=9):
+        """Per iteration: upload phi, pi from pinned host arrays in the
+        reference layout, one TSO interval (50 steps + one fused SO row, the
+        row read back), download phi, pi.  The host fields are fresh arrays
+        (the same values) pinned just before the iterations, as a caller
+        prepares them; one warm-up iteration, then n timed back to back."""
+        hphi, hpi = phi.astype(host_dtype), pi.astype(host_dtype)
+        ophi, opi = np.empty_like(hphi), np.empty_like(hpi)
+        for a in (hphi, hpi, ophi, opi):
+            L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
+        its, phases = [], []
+        try:
+            for it in range(n + 1):
+                dist.barrier()
+                t0 = time.perf_counter()
+                L.check(upload(elat.h, hphi.ctypes.data, hpi.ctypes.data))
+                t1 = time.perf_counter()
+                elat.run_loop(TSO_STEPS, 1.0, max_rows=2)
+                t2 = time.perf_counter()
+                L.check(download(elat.h, ophi.ctypes.data, opi.ctypes.data))
+                t3 = time.perf_counter()
+                if it:
+                    its.append(t3 - t0)
+                    phases.append((t1 - t0, t2 - t1, t3 - t2))
+        finally:
+            for a in (hphi, hpi, ophi, opi):
+                lib.phn_unpin_host(a.ctypes.data)
+        med = dist.max(float(np.median(its)))
+        return {"value": sites * TSO_STEPS * dist.world / med, "unit": METRIC,
+                "h2d_bytes_per_step": int(hphi.nbytes + hpi.nbytes),
+                "d2h_bytes_per_step": int(ophi.nbytes + opi.nbytes + 26 * 8),
+                "iteration_s": {"median": float(np.median(its)), "min": float(min(its)), "max": float(max(its)),
+                                "n": len(its), "all": [round(t, 4) for t in its],
+                                "upload_steps_download": [[round(x, 4) for x in ph] for ph in phases]}}
 
-    def e2e_burst(n):
-        dist.barrier()
-        for _ in range(n):
-            t, ph = e2e_iter()
-            its.append(t)
-            phases.append(ph)
-
-    def e2e_close():
-        # per-iteration wall times of nine back-to-back iterations right after
-        # the host buffers are pinned; the median keeps a disturbed iteration
-        # from setting the number
-        e2e_s = dist.max(float(np.median(its)))
-        out["e2e"] = {"value": sites * TSO_STEPS * dist.world / e2e_s, "unit": METRIC,
-                      "h2d_bytes_per_step": int(ephi.nbytes + epi.nbytes),
-                      "d2h_bytes_per_step": int(hphi.nbytes + hpi.nbytes + 26 * 8),
-                      "iteration_s": {"median": float(np.median(its)), "min": float(min(its)),
-                                      "max": float(max(its)), "n": len(its), "all": [round(t, 4) for t in its],
-                                      "upload_steps_download": [[round(x, 4) for x in ph] for ph in phases]},
-                      "step": f"upload phi,pi (FP64 reference layout) + {TSO_STEPS} leapfrog steps with one fused "
-                              "SO row + download phi,pi",
-                      "f32_host": e2e_f32}
-        for a in (ephi, epi, hphi, hpi):
-            lib.phn_unpin_host(a.ctypes.data)
-        elat.close()
-
-    e2e_iter()  # warm-up
-    e2e_burst(9)
-
-    # the same with the reference's single-precision host layout (float
-    # arrays, phn_upload_f32 / phn_download_f32): half the bytes on the link
-    phi32, pi32 = phi.astype(np.float32), pi.astype(np.float32)
-    hphi32, hpi32 = np.empty_like(phi32), np.empty_like(pi32)
-    for a in (phi32, pi32, hphi32, hpi32):
-        L.check(lib.phn_pin_host(a.ctypes.data, a.nbytes))
-    its32 = []
-    for it in range(10):  # a warm-up, then nine timed
-        t0 = time.perf_counter()
-        L.check(lib.phn_upload_f32(elat.h, phi32.ctypes.data, pi32.ctypes.data))
-        elat.run_loop(TSO_STEPS, 1.0, max_rows=2)
-        L.check(lib.phn_download_f32(elat.h, hphi32.ctypes.data, hpi32.ctypes.data))
-        if it:
-            its32.append(time.perf_counter() - t0)
-    for a in (phi32, pi32, hphi32, hpi32):
-        lib.phn_unpin_host(a.ctypes.data)
-    e2e_f32 = {"value": sites * TSO_STEPS * dist.world / dist.max(float(np.median(its32))), "unit": METRIC,
-               "h2d_bytes_per_step": int(phi32.nbytes + pi32.nbytes),
-               "d2h_bytes_per_step": int(hphi32.nbytes + hpi32.nbytes + 26 * 8),
-               "iteration_s": [round(t, 4) for t in its32],
-               "step": "as e2e with float host arrays (the reference's doubleprecision -1 build)"}
-    del phi32, pi32, hphi32, hpi32
+    # the reference's single-precision build (doubleprecision -1) keeps float
+    # host arrays: phn_upload_f32 / phn_download_f32, like for like with the
+    # FP32 device arithmetic and the FP32 CPU baseline
+    e2e = e2e_leg(np.float32, lib.phn_upload_f32, lib.phn_download_f32)
+    e2e["step"] = (f"upload phi,pi (float host arrays, reference layout: the doubleprecision -1 build) + "
+                   f"{TSO_STEPS} leapfrog steps with one fused SO row + download phi,pi")
+    # its default double build: FP64 host arrays, converted on the device
+    f64 = e2e_leg(np.float64, lambda h, a, b: lib.phn_upload(h, ctypes.cast(a, L._PD), ctypes.cast(b, L._PD)),
+                  lambda h, a, b: lib.phn_download(h, ctypes.cast(a, L._PD), ctypes.cast(b, L._PD)))
+    f64["step"] = "as e2e with FP64 host arrays (the reference's default doubleprecision 0 build)"
+    e2e["f64_host"] = f64
+    out["e2e"] = e2e
+    elat.close()
 
     # ------------------------------------------- the other precisions/sizes
     also = {}
     if args.no_extra:
-        e2e_close()
         out["also"] = also
         return out
     for label, n, prec, k in (("n256_fp32", 256, L.FP32, 400), ("n256_fp64", 256, L.FP64, 40),
@@ -347,7 +417,6 @@ def measure_gpu(args, dist: Dist):
         adj = adjoint_form(128, 1000, check=False, reps_unchecked=3)
         also["adjoint_c4_fp32"] = {k: adj[k] for k in ("cost_ratio", "forward_plain_ms", "adjoint_forward_ms",
                                                        "adjoint_backward_ms", "timing")}
-    e2e_close()
     out["also"] = also
     return out
 
@@ -744,22 +813,39 @@ def io_form(N: int, directory: str):
     return out
 
 
-def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int, warmup: int = 1):
-    """The oracle's reference loop (FP64) on all host threads, bounded."""
+def cpu_reference_rate(N: int, max_seconds: float, steps_cap: int, warmup: int = 1, precision: str = "f32"):
+    """The reference loop restated in the oracle (orc_evolve: the default
+    double build; orc_evolve_f32: the doubleprecision -1 float build, pinned
+    bit-identical to the reference's own float build), compiled with the
+    reference's -O3 -ffast-math flags, on all host threads (OpenMP over
+    z-slabs, the analogue of mpirun -np K), bounded in time."""
     from oracle import oracle as O
     O.build()
     p = O.Params(N=N)
     phi, pi = make_fields(N)
     nt = O.max_threads(True)
-    clock = O.Clock(p, fast=True)
-    O.evolve(p, phi, pi, max(1, warmup), clock, nthreads=nt, fast=True)  # warm-up, page-in
+    if precision == "f32":
+        phi, pi = phi.astype(np.float32), pi.astype(np.float32)
+        clock = O.Clock32(p, fast=True)
+        step = lambda n: O.evolve_f32(p, phi, pi, n, clock, nthreads=nt, fast=True)  # noqa: E731
+    else:
+        phi, pi = phi.copy(), pi.copy()
+        clock = O.Clock(p, fast=True)
+        step = lambda n: O.evolve(p, phi, pi, n, clock, nthreads=nt, fast=True)  # noqa: E731
+    step(max(1, warmup))  # warm-up, page-in
     t0 = time.perf_counter()
     steps = 0
     while steps < steps_cap and time.perf_counter() - t0 < max_seconds:
-        O.evolve(p, phi, pi, 1, clock, nthreads=nt, fast=True)
+        step(1)
         steps += 1
     dt = time.perf_counter() - t0
     return N ** 3 * steps / dt, nt, steps, dt
+
+
+def cpu_sample(N, rate, nt, steps, dt, precision):
+    build = "float (doubleprecision -1)" if precision == "f32" else "double (doubleprecision 0)"
+    return (f"{steps} steps of the {N}^3 lattice ({dt:.1f} s), the reference's {build} loop restated in C, "
+            f"{nt} OpenMP threads over z-slabs, -O3 -ffast-math (reference flags)")
 
 
 def main():
@@ -818,15 +904,19 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        # the reference's single-precision build, like for like with this
+        # benchmark's FP32 arm; its default double build beside it
         warm = max(3, args.warmup)
-        rate, nt, steps, dt = cpu_reference_rate(args.n, 45.0, max(1, args.steps), warm)
+        rate, nt, steps, dt = cpu_reference_rate(args.n, 40.0, max(1, args.steps), warm, "f32")
+        r64, nt64, s64, dt64 = cpu_reference_rate(args.n, 25.0, max(1, args.steps), 1, "f64")
         line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": args.gpus,
                 "steps": steps, "warmup": warm, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": rate, "unit": METRIC, "cores": nt, "kind": "port",
-                                 "sample": f"{steps} steps of the {args.n}^3 lattice, FP64, {nt} OpenMP threads "
-                                           f"over z-slabs, -O3 -ffast-math (reference flags)"},
-                "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                                 "sample": cpu_sample(args.n, rate, nt, steps, dt, "f32")},
+                "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "also": {"f64": {"value": r64, "unit": METRIC, "cores": nt64, "kind": "port",
+                                 "sample": cpu_sample(args.n, r64, nt64, s64, dt64, "f64")}}}
         print(json.dumps(line))
         return
 
@@ -843,10 +933,20 @@ def main():
             "gpu_launches": res["gpu_launches"], "also": res["also"],
             "so_rows": res["rows"], "energy_drift_rel": res["energy_drift"]}
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, nt, steps, dt = cpu_reference_rate(args.n, 15.0, 200, 3)
-        line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": nt, "kind": "port",
-                                "sample": f"{steps} steps of the {args.n}^3 lattice ({dt:.1f} s), FP64, {nt} "
-                                          f"OpenMP threads over z-slabs, -O3 -ffast-math (reference flags)"}
+        # like for like: the reference's float build against this FP32 line,
+        # its double build against the FP64 GPU line (also.n512_fp64)
+        rate, nt, steps, dt = cpu_reference_rate(args.n, 15.0, 200, 3, "f32")
+        line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": nt, "kind": "port", "dtype": "f32",
+                                "sample": cpu_sample(args.n, rate, nt, steps, dt, "f32")}
+        r64, nt64, s64, dt64 = cpu_reference_rate(args.n, 10.0, 200, 1, "f64")
+        line["cpu_baseline_fp64"] = {"value": r64, "unit": METRIC, "cores": nt64, "kind": "port", "dtype": "f64",
+                                     "sample": cpu_sample(args.n, r64, nt64, s64, dt64, "f64")}
+        lfl = {"fp32_gpu_over_fp32_cpu": res["value"] / rate,
+               "fp32_e2e_over_fp32_cpu": res["e2e"]["value"] / rate if res["e2e"] else None}
+        g64 = res["also"].get(f"n{args.n}_fp64")
+        if g64:
+            lfl["fp64_gpu_over_fp64_cpu"] = g64["site_updates_per_s"] / r64
+        line["like_for_like"] = lfl
     if rank == 0:
         print(json.dumps(line))
     dist.close()

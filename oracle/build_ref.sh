@@ -25,6 +25,7 @@ build() {
 build libphinum_ref_t0_f64.so -DPHN_REF_THEORY=0 -DPHN_REF_PRECISION=0 &
 build libphinum_ref_t1_f64.so -DPHN_REF_THEORY=1 -DPHN_REF_PRECISION=0 &
 build libphinum_ref_t0_f32.so -DPHN_REF_THEORY=0 -DPHN_REF_PRECISION=-1 &
+build libphinum_ref_t1_f32.so -DPHN_REF_THEORY=1 -DPHN_REF_PRECISION=-1 &
 for t in 2 3 4 5; do
   build libphinum_ref_t${t}_f64.so -DPHN_REF_THEORY=$t -DPHN_REF_PRECISION=0 &
 done

@@ -66,6 +66,11 @@ class _CClock(ctypes.Structure):
                 ("last_field_c", _D)]
 
 
+class _CClock32(ctypes.Structure):
+    _fields_ = [("tau", ctypes.c_float), ("dtau", ctypes.c_float), ("last_mom", ctypes.c_float),
+                ("last_field", ctypes.c_float), ("steps", _I), ("pad_", _I)]
+
+
 class _CIc(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_long), ("justnoise", _I), ("pad_", _I), ("QS", _D), ("scale2", _D),
                 ("amplitude", _D), ("noise", _D), ("phi0", _D * 2), ("pi0", _D * 2), ("m2_long", _D),
@@ -171,6 +176,9 @@ def _load(fast: bool = False):
                                            ctypes.c_long, _I, _I, _I]
         lib.orc_site_energy_at.restype = _D
         lib.orc_max_threads.restype = _I
+        _PF = ctypes.POINTER(ctypes.c_float)
+        lib.orc_reset_f32.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock32)]
+        lib.orc_evolve_f32.argtypes = [ctypes.POINTER(_CParams), ctypes.POINTER(_CClock32), _PF, _PF, _I, _I]
         _libs[key] = lib
     return _libs[key]
 
@@ -199,6 +207,35 @@ class Clock:
     def sf(self) -> float:
         """Scale factor (1 for the static box)."""
         return self._c.sf
+
+
+class Clock32:
+    """The single-precision build's clock (float tau, dtau, update stamps)."""
+
+    def __init__(self, p: Params, fast: bool = False):
+        self.p, self._c, self.fast = p, _CClock32(), fast
+        _load(fast).orc_reset_f32(ctypes.byref(_cp(p)), ctypes.byref(self._c))
+
+    @property
+    def tau(self) -> float:
+        return self._c.tau
+
+    @property
+    def steps(self) -> int:
+        return self._c.steps
+
+
+def evolve_f32(p: Params, phi: np.ndarray, pi: np.ndarray, nsteps: int, clock: Clock32 | None = None,
+               nthreads: int = 1, fast: bool = False) -> Clock32:
+    """n x evolve() of the reference's single-precision build (theories 0, 1,
+    static box) in place on reference-layout float32 arrays."""
+    assert phi.dtype == np.float32 and pi.dtype == np.float32 and phi.flags.c_contiguous
+    assert phi.size == field_len(p) and pi.size == field_len(p) and p.theory in (0, 1) and not p.expansion
+    clock = clock or Clock32(p, fast)
+    pf = ctypes.POINTER(ctypes.c_float)
+    _load(fast).orc_evolve_f32(ctypes.byref(_cp(p)), ctypes.byref(clock._c), phi.ctypes.data_as(pf),
+                               pi.ctypes.data_as(pf), int(nsteps), int(nthreads))
+    return clock
 
 
 def max_threads(fast: bool = True) -> int:

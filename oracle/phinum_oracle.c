@@ -226,6 +226,85 @@ void orc_evolve(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int 
   }
 }
 
+/* ------------------------------------------- the single-precision build */
+/* With doubleprecision -1 every pseudo_double of the reference is a float
+ * (parameters.cpp:13-16): the fields, the clock (dynamics.cpp:8-50), a_t,
+ * M_sqr, Kappa, h, and util.cpp:20-23's sqr(), which takes and returns a
+ * float.  Literals such as 6. and 120. stay double, so the kick mixes float
+ * and double arithmetic by C's usual conversions, and each += rounds the
+ * double sum back to float.  This restates those types for theories 0 and 1
+ * on the static box. */
+static inline float sqr_f(float x) { return x * x; }
+
+void orc_reset_f32(const orc_params *p, orc_clock_f32 *c) {
+  memset(c, 0, sizeof(*c));
+  c->tau = (float)p->T0;                  /* LocalLattice::tau = T0 (dynamics.cpp:36) */
+  c->dtau = (float)p->dt * (float)p->a;   /* dtBaseTrans * a_t, float * float (:42) */
+  c->last_field = c->tau;
+  c->last_mom = c->tau;
+}
+
+/* updateMomenta() theory 0 (dynamics.cpp:82-87) and 1 (:96-101), slab z. */
+static void update_momenta_slab_f32(const orc_params *p, const float *Phi, float *Pi, float factor, int z) {
+  const int N = p->N, Nc = p->Nc;
+  const float mass = (float)p->m_sqr, kappa = (float)p->kappa, h = (float)p->h, a_t = (float)p->a;
+  long Kooo = pos3(p, 0, 0, z);
+  for (int y = 0; y < N; y++)
+    for (int x = 0; x < N; x++) {
+      float locPhiSqr = 0.0f;
+      for (int a = 0; a < Nc; a++) locPhiSqr += sqr_f(Phi[Kooo + a]);
+      long Kuoo = pos3(p, mod(x + 1, N), y, z);
+      long Kouo = pos3(p, x, mod(y + 1, N), z);
+      long Koou = pos3(p, x, y, z + 1);
+      long Kdoo = pos3(p, mod(x - 1, N), y, z);
+      long Kodo = pos3(p, x, mod(y - 1, N), z);
+      long Kood = pos3(p, x, y, z - 1);
+      for (int a = 0; a < Nc; a++) {
+        /* the six float additions, then a double subtraction and division */
+        float LapPhi = (float)((Phi[Kuoo] + Phi[Kdoo] + Phi[Kouo] + Phi[Kodo] + Phi[Koou] + Phi[Kood] -
+                                6. * Phi[Kooo]) / sqr_f(a_t));
+        double f;
+        if (p->theory == 0)
+          f = LapPhi - (p->mass_mode * mass + p->lambda_mode * (locPhiSqr / (6. * Nc)) +
+                        (sqr_f(locPhiSqr / kappa) / (120. * Nc * Nc))) * Phi[Kooo];
+        else if (a == 0)
+          f = (LapPhi - h) - (p->mass_mode * mass + p->lambda_mode * (locPhiSqr / (6. * Nc))) * Phi[Kooo];
+        else
+          f = LapPhi - (p->mass_mode * mass + p->lambda_mode * (locPhiSqr / (6. * Nc))) * Phi[Kooo];
+        Pi[Kooo] = (float)(Pi[Kooo] + f * factor);
+        Kooo++; Kuoo++; Kouo++; Koou++; Kdoo++; Kodo++; Kood++;
+      }
+    }
+}
+
+/* evolve() (dynamics.cpp:196-237) in the single-precision build. */
+void orc_evolve_f32(const orc_params *p, orc_clock_f32 *c, float *Phi, float *Pi, int nsteps, int nthreads) {
+  const int N = p->N;
+  const long slab = (long)p->Nc * N * N;
+  const long begin = slab, end = slab * (N + 1);
+  if (nthreads < 1) nthreads = 1;
+  (void)nthreads;
+  for (int s = 0; s < nsteps; s++) {
+    c->tau = (float)(c->tau + 0.5 * c->dtau);
+    const float fk = c->tau - c->last_mom;  /* tau - Last_Momenta_update, float */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+    for (int z = 1; z < N + 1; z++) update_momenta_slab_f32(p, Phi, Pi, fk, z);
+    c->last_mom = c->tau;
+    c->tau = (float)(c->tau + 0.5 * c->dtau);
+    const float fd = c->tau - c->last_field;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+    for (long K = begin; K < end; K++) Phi[K] += Pi[K] * fd; /* updateFields, dynamics.cpp:180-183 */
+    c->last_field = c->tau;
+    memcpy(Phi + (long)(N + 1) * slab, Phi + slab, (size_t)slab * sizeof(float)); /* exchange, comm.cpp:63-78 */
+    memcpy(Phi, Phi + (long)N * slab, (size_t)slab * sizeof(float));
+    c->steps++;
+  }
+}
+
 /* ---------------------------------------------------------------- averages */
 /* CalculateExtrema(): fieldanalysis.cpp:319-397 (one rank). */
 static void extrema(const orc_params *p, const double *Phi, orc_row *o) {

@@ -74,6 +74,16 @@ int orc_max_threads(void);
 void orc_reset(const orc_params *p, orc_clock *c);
 void orc_exchange(const orc_params *p, double *f);
 void orc_evolve(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int nsteps, int nthreads);
+
+/* The reference's single-precision build (doubleprecision -1: pseudo_double
+ * = float, parameters.cpp:13-16): clock and fields in float, theories 0 and
+ * 1, static box. */
+typedef struct orc_clock_f32 {
+  float tau, dtau, last_mom, last_field;
+  int steps, pad_;
+} orc_clock_f32;
+void orc_reset_f32(const orc_params *p, orc_clock_f32 *c);
+void orc_evolve_f32(const orc_params *p, orc_clock_f32 *c, float *Phi, float *Pi, int nsteps, int nthreads);
 void orc_averages(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, orc_row *o);
 int orc_run_loop(const orc_params *p, orc_clock *c, double *Phi, double *Pi, int nsteps, double tso,
                  orc_row *rows, int max_rows, int nthreads);

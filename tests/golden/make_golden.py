@@ -232,6 +232,32 @@ def run_fvd_case(name: str) -> None:
     print(f"fvd/{name}: rows={len(rows)} stop={stop}")
 
 
+# The reference's single-precision build (doubleprecision -1): lattice
+# params, input seed, phi0, steps.  Float fields after the steps.
+F32_CASES = {
+    "f32_t0_n12_nc2": (dict(N=12, Nc=2, **PHI6), 61, SQRT6, 100),
+    "f32_t1_n12": (dict(N=12, Nc=1, **TDW), 62, -SQRT6, 100),
+}
+
+
+def run_f32_case(name: str) -> None:
+    from oracle import oracle as O
+    import inputs
+    pd, seed, phi0, steps = F32_CASES[name]
+    p = O.Params(**{"a": 0.25, "dt": 0.08, "T0": 0.0, **pd})
+    phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, seed, phi0=phi0)
+    R = O.Reference(p, "f32")
+    R.set_fields(O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc))
+    R.reset()
+    R.evolve(steps)
+    phi, pi = R.get_fields()
+    tau, n = R.time()
+    os.makedirs(os.path.join(HERE, "f32"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "f32", f"{name}.npz"), params=json.dumps(pd), seed=seed, phi0=phi0,
+                        steps=steps, phi=phi.astype(np.float32), pi=pi.astype(np.float32), tau=tau)
+    print(f"f32/{name}: tau={tau}")
+
+
 def run_ic_case(name: str) -> None:
     from oracle import oracle as O
     pd, ic = IC_CASES[name]
@@ -329,6 +355,13 @@ def main() -> None:
         for name in CONFIG_CASES:
             subprocess.run([sys.executable, os.path.abspath(__file__), "--config-case", name], check=True)
         return
+    if len(sys.argv) > 2 and sys.argv[1] == "--f32-case":
+        run_f32_case(sys.argv[2])
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "--f32":
+        for name in F32_CASES:
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--f32-case", name], check=True)
+        return
     if len(sys.argv) > 2 and sys.argv[1] == "--fvd-case":
         run_fvd_case(sys.argv[2])
         return
@@ -360,6 +393,8 @@ def main() -> None:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--filter-case", name], check=True)
     for name in FVD_CASES:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--fvd-case", name], check=True)
+    for name in F32_CASES:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--f32-case", name], check=True)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,67 @@
+"""The benchmark's own kernels at the benchmark's sizes.
+
+The FP32 step the benchmark times is whatever the project's autotuner picks
+on the live lattice (a TMA or x4 variant; at 512^3 an x4 variant whose item
+decomposition depends on N).  Here that pick, at 256^3 and 512^3, runs the
+benchmark's loop -- 200 leapfrog steps with the averages and extrema fused
+into every 50th step -- against the plain one-site-per-thread kernel of the
+same precision (step_f32, or step_kahan for compensated FP32) on the same
+inputs: fields must be bit-identical (all kernels of a precision compute
+identical bits), extrema exact, and the fused sums equal to FP32-summation
+rounding (1e-6 relative).  Plain and compensated FP32; the phi^6 potential
+(theory 0) and the tilted double well (theory 1, h = sqrt(6) 0.05).
+
+Inputs come from the device initial-condition generator (seeded drand48
+stream, the configuration's spectrum: noise 3 below |p| = 2 pi), which is
+deterministic, so both lattices start from the same bits."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SQRT6 = 6.0 ** 0.5
+THEORY = {0: dict(theory=0), 1: dict(theory=1, mass_mode=-1, lambda_mode=1, h=SQRT6 * 0.05)}
+
+
+def run(N, theory, precision, tuned):
+    from phinum_gb300 import _lib as L
+    from phinum_gb300 import lattice as PL
+    lat = PL.Lattice(PL.Params(N=N, precision=precision, **THEORY[theory]))
+    try:
+        lat.initial_conditions(seed=2026 + theory, noise=3.0, scale2=2 * np.pi,
+                               phi0=((-1) ** theory * SQRT6, 0.0))
+        v, ms, path = ctypes.c_int(-2), ctypes.c_double(), ctypes.c_int()
+        if tuned:
+            L.check(lat.lib.phn_autotune(lat.h, 20, ctypes.byref(v), ctypes.byref(ms)))
+        else:
+            L.check(lat.lib.phn_set_path(lat.h, L.PATH_PLAIN))
+        L.check(lat.lib.phn_get_path(lat.h, ctypes.byref(path)))
+        rows = lat.run_loop(200, 1.0)
+        phi, pi = lat.download()
+        return rows, phi, pi, (v.value, path.value)
+    finally:
+        lat.close()
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("theory", [0, 1])
+@pytest.mark.parametrize("N", [256, 512])
+def test_autotuned_pick_matches_plain_kernel(N, theory, precision):
+    from phinum_gb300 import _lib as L
+    r1, f1, p1, (variant, path) = run(N, theory, precision, tuned=True)
+    r0, f0, p0, (_, path0) = run(N, theory, precision, tuned=False)
+    assert path0 == L.PATH_PLAIN
+    print(f"N={N} theory={theory} precision={precision}: autotuner picked variant {variant} (path {path})")
+    slab = N * N
+    assert rows_equal_shape(r0, r1) and r0.shape[0] == 4
+    assert np.array_equal(f0, f1), f"phi differs (variant {variant}, path {path})"
+    assert np.array_equal(p0[slab:-slab], p1[slab:-slab]), f"pi differs (variant {variant}, path {path})"
+    assert np.array_equal(r0[:, 17:23], r1[:, 17:23])
+    np.testing.assert_allclose(r1[:, 9:17], r0[:, 9:17], rtol=1e-6, atol=1e-9)
+    assert np.isfinite(f1).all() and np.abs(f1).max() > 0
+
+
+def rows_equal_shape(a, b):
+    return a.shape == b.shape

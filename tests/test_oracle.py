@@ -7,6 +7,8 @@ reproduce every FP64 field, SO row and island label bit for bit; spectra use
 a different FFT, so their values agree to rounding and their bin counts
 exactly.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -147,3 +149,33 @@ def test_oracle_matches_reference_live(theory, N, Nc, expansion, tmp_path):
     """)
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
     assert r.returncode == 0 and "ok" in r.stdout, r.stderr
+
+
+F32_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "f32")
+
+
+@pytest.mark.parametrize("name", sorted(f[:-4] for f in os.listdir(F32_DIR)))
+def test_single_precision_port_matches_reference_float_build(name):
+    """orc_evolve_f32, the restatement of the reference's doubleprecision -1
+    build (float fields and clock, double literals), against that build's own
+    output (fixtures from oracle/_ref/libphinum_ref_t{0,1}_f32.so): float
+    fields bit-identical after 100 steps, and the float clock."""
+    import json
+    import inputs
+    with np.load(os.path.join(F32_DIR, name + ".npz")) as z:
+        d = {k: z[k] for k in z.files}
+    pd = json.loads(str(d["params"]))
+    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, int(d["seed"]), phi0=float(d["phi0"]))
+    phi = O.to_ref_layout(phi_i, p.Nc).astype(np.float32)
+    pi = O.to_ref_layout(pi_i, p.Nc).astype(np.float32)
+    clock = O.evolve_f32(p, phi, pi, int(d["steps"]))
+    slab = p.Nc * p.N * p.N
+    assert np.array_equal(phi, d["phi"])
+    assert np.array_equal(pi[slab:-slab], d["pi"][slab:-slab])
+    assert clock.tau == float(d["tau"]) and clock.steps == int(d["steps"])
+    # the timing build (-O3 -ffast-math, the reference's flags) on all threads runs the same steps
+    phi2 = O.to_ref_layout(phi_i, p.Nc).astype(np.float32)
+    pi2 = O.to_ref_layout(pi_i, p.Nc).astype(np.float32)
+    O.evolve_f32(p, phi2, pi2, int(d["steps"]), nthreads=O.max_threads(True), fast=True)
+    np.testing.assert_allclose(phi2, phi, rtol=0, atol=1e-4)
