@@ -94,7 +94,12 @@ inline bool finish(int id) {
 inline int MPI_Init(int *, char ***) { return MPI_SUCCESS; }
 inline int MPI_Finalize() { return MPI_SUCCESS; }
 inline int MPI_Comm_rank(MPI_Comm, int *r) { *r = 0; return MPI_SUCCESS; }
-inline int MPI_Comm_size(MPI_Comm, int *s) { *s = 1; return MPI_SUCCESS; }
+/* PHN_SHIM_NODES > 1 reports more ranks (this process stays rank 0), only to
+ * check that a caller refuses a multi-rank run before any message is sent. */
+#ifndef PHN_SHIM_NODES
+#define PHN_SHIM_NODES 1
+#endif
+inline int MPI_Comm_size(MPI_Comm, int *s) { *s = PHN_SHIM_NODES; return MPI_SUCCESS; }
 inline int MPI_Barrier(MPI_Comm) { return MPI_SUCCESS; }
 inline int MPI_Bcast(void *, int, MPI_Datatype, int, MPI_Comm) { return MPI_SUCCESS; }
 inline int MPI_Reduce(const void *s, void *r, int n, MPI_Datatype t, MPI_Op, int, MPI_Comm) {

@@ -34,6 +34,10 @@
 
 #include "phinum_gpu.h"
 
+#if (withEnergyPS == 1)
+#error "phinum_gpu adapter: withEnergyPS 1 (the energy spectrum and EnergybasedID) has no GPU drop-in"
+#endif
+
 namespace phn_gpu {
 
 static phn_handle *handle = nullptr;
@@ -75,8 +79,19 @@ static void mirror_clock() {
 }
 
 // After LocalLattice::init, fix_tadpole and SetInitialConditions: creates the
-// device lattice from the reference's parameters and uploads Phi/Pi.
+// device lattice from the reference's parameters and uploads Phi/Pi.  The
+// device holds the whole lattice, so the run must be a single rank: with
+// mpirun -np K > 1 each rank's Phi/Pi hold only its z-slab
+// (Nc*N*N*(N_eta_loc+2) values, lattice.cpp:72-78) and are refused here
+// rather than read past their end.
 inline void init() {
+  if (nodes != 1 || LocalLattice::N_eta_loc != N_eta || N_eta != N_t) {
+    std::fprintf(stderr,
+                 "phinum_gpu: the GPU drop-in evolves the whole %d^3 lattice on one rank; this run has %d "
+                 "rank(s) holding %d of %d z-slabs each (run with one MPI rank)\n",
+                 N_t, nodes, LocalLattice::N_eta_loc, N_eta);
+    std::exit(1);
+  }
   phn_params p;
   std::memset(&p, 0, sizeof(p));
   p.N = N_t;
@@ -233,7 +248,10 @@ inline void Calculate_CorrelationFunctions() {
 
 // Print_fp() (momentumspace.cpp:280-384): same cadence; the spectrum comes
 // from the device and the Distrib-<run>-<t>.txt file gets the same columns as
-// the reference's printer (momentumspace.cpp:307-381).
+// the reference's printer (momentumspace.cpp:307-381), the expanding box's
+// scale factor included (:363-365).  The energy spectrum columns of
+// withEnergyPS 1 (:366-371) have no device counterpart: that switch is
+// refused at compile time below.
 inline void Print_fp() {
   using namespace LocalLattice;
   if (numeric::total_stepcount > 0 && tau < numeric::LastMOoutput + TMO) return;
@@ -255,23 +273,32 @@ inline void Print_fp() {
     char fname[256];
     snprintf(fname, 256, "./output/%i/Distrib-%i-%g.txt", LASTRUN, runID, really_double(numeric::LastMOoutput));
     specOut.open(fname);
-    const double NormCorr = 1. / (sqr(N_t * a_t) * N_eta * a_eta);
+    // the printer's locals are pseudo_double, as the reference declares them,
+    // so the single-precision build rounds and prints as it does
+    const pseudo_double NormCorr = 1. / (sqr(N_t * a_t) * N_eta * a_eta);
     for (int k = 0; k < nTBins; k++) {
-      const double norm2 = (TotalBCounts[k] == 0 ? 0 : 1 / (double)(TotalBCounts[k]));
-      const double pabs = binsizeT * k;
+      const pseudo_double norm2 = (TotalBCounts[k] == 0 ? 0 : 1 / (pseudo_double)(TotalBCounts[k]));
+      const pseudo_double pabs = binsizeT * k;
       if (norm2 != 0 && TotalCorrF[k * Nc] != 0) {
         if (k != 0) specOut << std::endl;
         specOut << pabs << " " << TotalBCounts[k] << " ";
-        double FF = 0, KK = 0;
+        pseudo_double FF = 0, KK = 0, QQ = 0;
         for (int a = 0; a < Nc; a++) {
           FF += TotalCorrF[k * Nc + a];
           KK += TotalCorrK[k * Nc + a];
+          QQ += TotalCorrQ[k * Nc + a];
         }
         FF /= Nc;
         KK /= Nc;
-        specOut << sqrt(KK / FF) << ' ' << FF * NormCorr * norm2 << ' ' << KK * NormCorr * norm2 << ' '
-                << sqrt(FF * KK) * NormCorr * norm2 << " "
-                << FF * NormCorr * norm2 * pabs * pabs * pabs / 2. / acos(-1.) / acos(-1.) << ' ';
+        QQ /= Nc;
+        const pseudo_double omg = sqrt(KK / FF);
+        specOut << omg << ' ' << FF * NormCorr * norm2 << ' ' << KK * NormCorr * norm2 << ' '
+                << sqrt(FF * KK) * NormCorr * norm2 << " ";
+#if (expansion == 1)
+        specOut << scale_factor << " ";  // the expanding box's scale-factor column
+#endif
+        specOut << FF * NormCorr * norm2 * pabs * pabs * pabs / 2. / acos(-1.) / acos(-1.) << ' ';
+        if (FF * KK - QQ * QQ < 0) std::cout << "negative at " << k << std::endl;
       }
     }
     specOut.close();

@@ -5,7 +5,9 @@ call sequence of the reference-side adapter.  The loop must stop at the step
 where the reference's own loop stopped (fixtures tests/golden/fvd/: a tilted
 well whose <V> turns negative at step 151, and a NaN in Pi that reaches phi
 with the first drift, stopping at step 10), with the rows of the reference
-(FP64 sums 1e-11 relative, extrema of finite rows exact; FP32 rows 2e-5)."""
+(FP64 sums 1e-11 relative, extrema of finite rows exact; FP32 rows 2e-5 and
+compensated FP32 rows 5e-6 of each column's largest value: the rows' per-site
+terms are FP32 in both)."""
 import numpy as np
 import pytest
 
@@ -15,7 +17,7 @@ from test_false_vacuum import FVD, fvd_case
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("precision,rtol", [(0, 1e-11), (1, 2e-5), (2, 2e-6)])
+@pytest.mark.parametrize("precision,rtol", [(0, 1e-11), (1, 2e-5), (2, 5e-6)])
 @pytest.mark.parametrize("name", FVD)
 def test_library_loop_stops_where_the_reference_loop_stops(name, precision, rtol):
     from phinum_gb300 import lattice as PL
