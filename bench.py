@@ -34,10 +34,11 @@ cpu_baseline / --impl reference
 Multi-GPU: replicas only -- every rank evolves its own lattice; no collective
 on the data path.
 
---form precision|adjoint|ensemble|initial|io|analysis prints one JSON object
-for the compensated-FP32 run, the adjoint, the ensemble, the initial
-conditions, the checkpoint files or the spectrum/island passes instead of the
-benchmark line.
+--form precision|adjoint|ensemble|initial|io|analysis|c1 prints one JSON
+object for the compensated-FP32 run, the adjoint, the ensemble, the initial
+conditions, the checkpoint files, the spectrum/island passes or the 256^3
+drop-in configuration (both potentials, three precisions and the host
+oracle) instead of the benchmark line.
 """
 from __future__ import annotations
 
@@ -681,6 +682,116 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     return out
 
 
+def c1_form(N: int = 256, steps: int = 5000, seed: int = 2027, oracle_threads: int = 0):
+    """The GPU drop-in configuration (C1): 256^3, 5000 steps, dtau = 0.02,
+    a = 0.25, the phi^6 potential (theory 0, Kappa = sqrt(3), phi0 = sqrt(6))
+    and the tilted double well (theory 1, Mass_Mode -1, Lambda_Mode 1,
+    h = sqrt(6) 0.05, phi0 = -sqrt(6)), in FP64, FP32 and compensated FP32 on
+    the same seeded inputs, and the reference's arithmetic on the host (the
+    oracle, FP64, all threads) on the same inputs.
+
+    Inputs: the reference's own initial conditions (SetInitialConditions,
+    initialize 3, drand48 from srand48(seed), the configuration's spectrum:
+    Noise 3 below |p| = 2 pi) generated on the device in FP64.  Each run is
+    the reference loop with SO rows every 50 steps (TSO 1.0) and no
+    false-vacuum break: the tilted well starts at <V> < 0, where the
+    reference's false_vacuum_decayed() would stop at once.  At the end: the
+    spectrum (reference bins), islands with the reference's mask (thres =
+    2.57583 sqrt(<phi^2>) at t = 0, main.cpp:70) and with the configuration's
+    energy mask (rho > 2 <rho>, z periodic), and the fields.
+
+    Reported per potential: device time and rate of each precision; FP64
+    against the oracle (fields bit for bit, rows, spectrum, island labels);
+    FP32 and compensated FP32 against FP64 (energy rows, drift, field L2,
+    per-bin spectrum, island counts and mask agreement)."""
+    import ctypes
+    from oracle import oracle as O
+    from phinum_gb300 import _lib as L
+    from phinum_gb300 import lattice as PL
+    sq6 = 6 ** 0.5
+    pots = {"phi6": (dict(theory=0, kappa=3 ** 0.5), sq6),
+            "tilted_well": (dict(theory=1, mass_mode=-1, lambda_mode=1, h=sq6 * 0.05), -sq6)}
+    out = {"form": "c1", "N": N, "steps": steps, "tso_steps": 50, "seed": seed,
+           "workload": f"{N}^3, {steps} steps, a=0.25, dtau=0.02; phi^6 and tilted double well; "
+                       "the reference's initial conditions (initialize 3, Noise 3 below |p| = 2 pi)"}
+    nt = oracle_threads or O.max_threads(False)
+    lib = L.load()
+    for pname, (kw, phi0) in pots.items():
+        gen = PL.Lattice(PL.Params(N=N, precision=0, **kw))
+        gen.initial_conditions(seed=seed, noise=3.0, scale2=2 * np.pi, phi0=(phi0, 0.0))
+        phi, pi = gen.download()
+        avg0 = gen.volume_averages(allow_nonfinite=True)
+        gen.close()
+        thr = 2.57583 * float(np.sqrt(avg0[O_AVG_PHI2]))
+        runs = {}
+        for name, prec in (("fp64", L.FP64), ("fp32", L.FP32), ("kahan_fp32", L.FP32_KAHAN)):
+            lat = PL.Lattice(PL.Params(N=N, precision=prec, **kw))
+            lat.upload(phi, pi)
+            kernel = tune(lib, lat) if prec != L.FP64 else "step_f64"
+            t0 = time.perf_counter()
+            rows = lat.run_loop(steps, 1.0, max_rows=steps // 50 + 2)
+            wall = time.perf_counter() - t0
+            _, ms, _ = lat.stats()
+            F, K, Q, C = lat.correlation_functions()
+            fphi, fpi = lat.download()
+            if name == "fp64":
+                rho_thr = 2.0 * float(lat.volume_averages(allow_nonfinite=True)[O_AVG_ENERGY])
+            lab_r, rec_r = lat.full_analysis(thr)
+            lab_e, rec_e = lat.full_analysis(rho_thr, mode=L.ISLAND_ENERGY, z_periodic=True)
+            lat.close()
+            runs[name] = dict(rows=rows, F=F, C=C, phi=fphi, lab_r=lab_r, rec_r=rec_r, lab_e=lab_e, rec_e=rec_e,
+                              timing={"device_ms": ms, "wall_s": wall, "kernel": kernel,
+                                      "site_updates_per_s": N ** 3 * steps / (ms / 1e3)})
+        r64 = runs["fp64"]
+        res = {"threshold_reference_mask": thr, "threshold_energy_mask": rho_thr,
+               "timing": {k: v["timing"] for k, v in runs.items()},
+               "islands_fp64": {"reference_mask": int(r64["rec_r"].shape[0]),
+                                "energy_mask": int(r64["rec_e"].shape[0])}}
+        e64 = r64["rows"][:, O_AVG_ENERGY]
+        sl = slice(N * N, -N * N)
+        nz = r64["F"] > 0
+        for name in ("fp32", "kahan_fp32"):
+            r = runs[name]
+            e = r["rows"][:, O_AVG_ENERGY]
+            rel = np.abs(r["F"][nz] - r64["F"][nz]) / r64["F"][nz]
+            res[f"{name}_vs_fp64"] = {
+                "energy_rows_rel_err_max": float(np.max(np.abs(e - e64) / np.abs(e64))),
+                "energy_drift": float(abs(e[-1] - e[0]) / abs(e[0])), "energy_drift_fp64": float(abs(e64[-1] - e64[0])
+                                                                                              / abs(e64[0])),
+                "phi_rel_l2_end": float(np.linalg.norm(r["phi"][sl] - r64["phi"][sl]) / np.linalg.norm(r64["phi"][sl])),
+                "spectrum_rel_err_max": float(rel.max()), "spectrum_rel_err_median": float(np.median(rel)),
+                "spectrum_counts_equal": bool(np.array_equal(r["C"], r64["C"])),
+                "islands_reference_mask": int(r["rec_r"].shape[0]),
+                "islands_energy_mask": int(r["rec_e"].shape[0]),
+                "energy_mask_sites_differing": int(np.count_nonzero((r["lab_e"] >= 0) != (r64["lab_e"] >= 0))),
+                "energy_mask_labels_equal": bool(np.array_equal(r["lab_e"], r64["lab_e"])),
+                "reference_mask_labels_equal": bool(np.array_equal(r["lab_r"], r64["lab_r"]))}
+        # the reference's arithmetic on the host: the oracle on the same inputs
+        p = O.Params(N=N, **kw)
+        ophi, opi = phi.copy(), pi.copy()
+        t0 = time.perf_counter()
+        orows, clock = O.run_loop(p, ophi, opi, steps, 1.0, max_rows=steps // 50 + 2, nthreads=nt)
+        t_or = time.perf_counter() - t0
+        oF, oK, oQ, oC = O.spectrum(p, ophi, opi)
+        olab_r, orec_r = O.islands(p, ophi, opi, thr, clock=clock)
+        olab_e, orec_e = O.islands(p, ophi, opi, rho_thr, mode=1, zper=1, clock=clock)
+        res["fp64_vs_oracle"] = {
+            "oracle_wall_s": t_or, "oracle_threads": nt,
+            "oracle_site_updates_per_s": N ** 3 * steps / t_or,
+            "phi_bit_identical": bool(np.array_equal(r64["phi"], ophi)),
+            "rows": int(orows.shape[0]),
+            "extrema_exact": bool(np.array_equal(r64["rows"][:, 17:23], orows[:, 17:23])),
+            "row_sums_rel_err_max": float(np.max(np.abs(r64["rows"][:, 9:17] - orows[:, 9:17]) /
+                                                 np.maximum(np.abs(orows[:, 9:17]), 1e-300))),
+            "spectrum_counts_equal": bool(np.array_equal(r64["C"], oC)),
+            "spectrum_max_abs_err_over_largest_bin": float(np.max(np.abs(r64["F"] - oF)) / np.max(np.abs(oF))),
+            "reference_mask_labels_equal": bool(np.array_equal(r64["lab_r"], olab_r)),
+            "energy_mask_labels_equal": bool(np.array_equal(r64["lab_e"], olab_e)),
+            "islands_oracle": {"reference_mask": int(orec_r.shape[0]), "energy_mask": int(orec_e.shape[0])}}
+        out[pname] = res
+    return out
+
+
 def initial_form(N: int, n_cpu: int = 128, n_check: int = 64):
     """Initial conditions (SetInitialConditions, initialize 3, the
     configuration's spectrum: Noise 3 below |p| = 2 pi, phi0 = sqrt(6)) on the
@@ -861,7 +972,8 @@ def main():
     ap.add_argument("--n", "--lattice-edge", dest="n", type=int, default=N_MAIN,
                     help="lattice edge (profiling runs use smaller cases); under torchrun spell it --lattice-edge")
     ap.add_argument("--variant", type=int, default=None, help="TMA kernel variant instead of the autotuner's pick")
-    ap.add_argument("--form", default=None, choices=["precision", "adjoint", "ensemble", "initial", "io", "analysis"],
+    ap.add_argument("--form", default=None,
+                    choices=["precision", "adjoint", "ensemble", "initial", "io", "analysis", "c1"],
                     help="report one of the extra forms (or the analysis passes) instead of the benchmark line")
     args = ap.parse_args()
     rank, local, world = env_rank()
@@ -893,6 +1005,10 @@ def main():
         return
     if args.form == "analysis":
         print(json.dumps(analysis_form(args.n)))
+        return
+    if args.form == "c1":
+        n = args.n if args.n != N_MAIN else 256
+        print(json.dumps(c1_form(n, args.steps if args.steps != 1000 else 5000)))
         return
     if args.form == "ensemble":
         out = measure_ensemble(max(args.steps, 100), 100)
