@@ -30,6 +30,16 @@ for t in 2 3 4 5; do
   build libphinum_ref_t${t}_f64.so -DPHN_REF_THEORY=$t -DPHN_REF_PRECISION=0 &
 done
 wait
+# the other initial conditions: initialize 0, 1, 2, 4, and the charged
+# variant (withcharge 1) of initialize 2 and 3
+for i in 0 1 2 4; do
+  build libphinum_ref_t0_f64_ic${i}.so -DPHN_REF_THEORY=0 -DPHN_REF_PRECISION=0 -DPHN_REF_INIT=$i &
+done
+for i in 2 3; do
+  build libphinum_ref_t0_f64_ic${i}q.so -DPHN_REF_THEORY=0 -DPHN_REF_PRECISION=0 -DPHN_REF_INIT=$i \
+    -DPHN_REF_WITHCHARGE=1 &
+done
+wait
 # the expanding box (expansion 1), every theory
 for t in 0 1 2 3 4 5; do
   build libphinum_ref_t${t}_f64_exp.so -DPHN_REF_THEORY=$t -DPHN_REF_PRECISION=0 -DPHN_REF_EXPANSION=1 &

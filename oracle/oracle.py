@@ -74,12 +74,16 @@ class _CClock32(ctypes.Structure):
 class _CIc(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_long), ("justnoise", _I), ("pad_", _I), ("QS", _D), ("scale2", _D),
                 ("amplitude", _D), ("noise", _D), ("phi0", _D * 2), ("pi0", _D * 2), ("m2_long", _D),
-                ("m2_trans", _D)]
+                ("m2_trans", _D), ("initialize", _I), ("withcharge", _I), ("chi", _D), ("famp", _D), ("lambda_", _D),
+                ("temperature", _D), ("phi0s", _D), ("pi0s", _D)]
 
 
-# SetInitialConditions parameters (initialize 3): the reference globals' names
+# SetInitialConditions parameters: the reference globals' names; initialize
+# and withcharge are its compile-time switches (parameters.cpp:205, :51), the
+# last six the globals of initialize 0-2 (phi0s, pi0s: its phi0, pi0)
 IC_DEFAULTS = dict(seed=1, justnoise=0, QS=1.0, scale2=1.0, amplitude=0.0, noise=0.5, phi0=(0.0, 0.0),
-                   pi0=(0.0, 0.0))
+                   pi0=(0.0, 0.0), initialize=3, withcharge=0, chi=1.0, famp=0.5, lambda_=1.0, temperature=1.0,
+                   phi0s=0.0, pi0s=0.0)
 
 
 def _cp(p: Params) -> _CParams:
@@ -317,13 +321,16 @@ def spectrum_uniform(p: Params, phi: np.ndarray, pi: np.ndarray, nbins: int = 64
 
 
 def initial_conditions(p: Params, **kw):
-    """SetInitialConditions (initialize 3) with srand48(seed): Phi, Pi in the
-    reference layout (Pi's ghost slabs zero).  M2_long = M2_trans = M_sqr."""
+    """SetInitialConditions (initialize 0-4, withcharge 0/1; default 3, 0)
+    with srand48(seed): Phi, Pi in the reference layout (Pi's ghost slabs
+    zero).  M2_long = M2_trans = M_sqr."""
     q = dict(IC_DEFAULTS, **kw)
     c = _CIc(int(q["seed"]), int(q["justnoise"]), 0, q["QS"], q["scale2"], q["amplitude"], q["noise"],
-             (_D * 2)(*q["phi0"]), (_D * 2)(*q["pi0"]), p.m_sqr, p.m_sqr)
+             (_D * 2)(*q["phi0"]), (_D * 2)(*q["pi0"]), p.m_sqr, p.m_sqr, int(q["initialize"]),
+             int(q["withcharge"]), q["chi"], q["famp"], q["lambda_"], q["temperature"], q["phi0s"], q["pi0s"])
     phi, pi = np.zeros(field_len(p)), np.zeros(field_len(p))
-    _load().orc_initial_conditions(ctypes.byref(_cp(p)), ctypes.byref(c), _ptr(phi), _ptr(pi))
+    if _load().orc_initial_conditions(ctypes.byref(_cp(p)), ctypes.byref(c), _ptr(phi), _ptr(pi)) != 0:
+        raise ValueError("initialize/withcharge combination the reference does not define")
     return phi, pi
 
 
@@ -384,21 +391,23 @@ def ref_dir() -> str:
     return os.environ.get("REF_DIR", "/root/reference")
 
 
-def ref_path(theory: int = 0, precision: str = "f64", expansion: int = 0) -> str:
-    return os.path.join(REF_DIR, f"libphinum_ref_t{theory}_{precision}{'_exp' if expansion else ''}.so")
+def ref_path(theory: int = 0, precision: str = "f64", expansion: int = 0, variant: str = "") -> str:
+    """variant: "" (initialize 3), "_ic0", "_ic1", "_ic2", "_ic4" (other
+    initialize switches), "_ic2q", "_ic3q" (withcharge 1)."""
+    return os.path.join(REF_DIR, f"libphinum_ref_t{theory}_{precision}{'_exp' if expansion else ''}{variant}.so")
 
 
-def ref_available(theory: int = 0, precision: str = "f64", expansion: int = 0) -> bool:
-    return os.path.exists(ref_path(theory, precision, expansion))
+def ref_available(theory: int = 0, precision: str = "f64", expansion: int = 0, variant: str = "") -> bool:
+    return os.path.exists(ref_path(theory, precision, expansion, variant))
 
 
 class Reference:
     """The reference's own sources (single rank, shims) behind ctypes.  One
     instance per process and variant: the reference keeps global state."""
 
-    def __init__(self, p: Params, precision: str = "f64"):
+    def __init__(self, p: Params, precision: str = "f64", variant: str = ""):
         self.p = p
-        lib = ctypes.CDLL(ref_path(p.theory, precision, p.expansion))
+        lib = ctypes.CDLL(ref_path(p.theory, precision, p.expansion, variant))
         lib.ref_init.argtypes = [_I, _I, _D, _D, _D, _I, _D, _I, _D, _D, _D]
         lib.ref_init.restype = _I
         lib.ref_set_fields.argtypes = [_PD, _PD]
@@ -433,8 +442,11 @@ class Reference:
             raise RuntimeError(f"ref_init failed ({r}); one Reference per process")
 
     def initial_conditions(self, **kw):
-        """The reference's SetInitialConditions with srand48(seed); returns Phi, Pi."""
+        """The reference's SetInitialConditions with srand48(seed) (the
+        build's initialize / withcharge switches); returns Phi, Pi."""
         q = dict(IC_DEFAULTS, **kw)
+        self.lib.ref_set_ic_extra.argtypes = [_D] * 6
+        self.lib.ref_set_ic_extra(q["chi"], q["famp"], q["lambda_"], q["temperature"], q["phi0s"], q["pi0s"])
         r = self.lib.ref_initial_conditions(int(q["seed"]), int(q["justnoise"]), q["QS"], q["scale2"],
                                             q["amplitude"], q["noise"], q["phi0"][0], q["phi0"][1],
                                             q["pi0"][0], q["pi0"][1])

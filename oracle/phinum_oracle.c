@@ -19,7 +19,7 @@
  *                        Calculate_CorrelationFunctions, fftXtoP_direct
  *                                                     momentumspace.cpp:32-278,
  *                                                     clusterfft.cpp:185-225
- *   orc_initial_conditions  SetInitialConditions (initialize 3), ensureRealResult,
+ *   orc_initial_conditions  SetInitialConditions (initialize 0-4, withcharge 0/1), ensureRealResult,
  *                        fftPtoX            initialconditions.cpp:14-723,
  *                                           clusterfft.cpp:10-16,55-182
  *   orc_apply_filter     apply_filter      filter.cpp:11-133
@@ -752,13 +752,92 @@ static void ic_fft_ptox(const orc_params *p, const double *hre, const double *hi
  * initial scale factor squared, E = H0 A and Pi_0 += phi0_0 H0.  Phi/Pi in
  * the reference layout; Phi's ghost slabs exchanged, Pi's left as they
  * were.  Returns 0. */
+/* Occupation and Omega of one mode and component (initialconditions.cpp):
+ * the withcharge 0 branches (:308-508) or the withcharge 1 ones (:160-257),
+ * each with its own comparisons; the expanding box's forms belong to
+ * initialize 3 without charge.  Returns 0, or -1 for initialize 4 with
+ * charge, where the reference sets neither. */
+static int ic_occupation(const orc_params *p, const orc_ic *ic, int a, double pt, double nu, double psqr,
+                         double *occ, double *omega) {
+  const int Nc = p->Nc;
+  const double M = p->m_sqr;
+  double pchisqr;
+  switch (ic->initialize) {
+    case 0: /* parametric resonance (:163-175, :310-321) */
+      if (a == 0) *omega = sqrt(psqr + fabs(M) - 3. * sqr(ic->temperature) * sqr(ic->phi0s) / (6. * Nc));
+      else *omega = sqrt(psqr + fabs(M) - sqr(ic->temperature) * sqr(ic->phi0s) / (6. * Nc));
+      *occ = ic->famp * ic->lambda;
+      return 0;
+    case 1: /* box (:180-206, :326-350) */
+      pchisqr = sqr(pt) + sqr(ic->chi) * sqr(nu);
+      if (sqrt(pchisqr) < ic->QS) *occ = ic->amplitude;
+      else *occ = sqrt(pchisqr) < 2.0 * ic->QS ? ic->noise : 0.0;
+      break;
+    case 2: /* large-Lambda box (:211-251, :357-397) */
+      pchisqr = sqr(pt) + sqr(nu);
+      if (ic->justnoise == 0 && sqrt(pchisqr) < ic->QS) *occ = ic->amplitude + ic->noise;
+      else if (ic->scale2 == 0) *occ = ic->noise;
+      else *occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
+      break;
+    case 3:
+      pchisqr = sqr(pt) + sqr(nu);
+      if (ic->withcharge) { /* :255-291: static forms only */
+        if (ic->justnoise == 0 && sqrt(pchisqr) < ic->QS) *occ = ic->amplitude + ic->noise;
+        else if (ic->scale2 == 0) *occ = ic->noise;
+        else *occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
+        *omega = a == 0 ? sqrt(psqr + ic->m2_long) : sqrt(psqr + ic->m2_trans);
+        return 0;
+      }
+      /* :402-510 */
+      if (ic->justnoise == 0 && p->expansion && psqr > 0. && psqr < (ic->QS * ic->QS)) {
+        const double omegap = sqrt(psqr + (1. + 2. * p->H0 * p->T0) * ic->m2_long);
+        *occ = 2. * acos(-1.) * acos(-1.) * 2.1e-9 * ic->phi0[0] * ic->phi0[0] / psqr / sqrt(psqr) * omegap;
+      } else if (ic->justnoise == 0 && !p->expansion && pchisqr < ic->QS * ic->QS) {
+        *occ = ic->amplitude + ic->noise;
+      } else {
+        if (ic->scale2 == 0) *occ = ic->noise;
+        else *occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
+      }
+      {
+        const double m2 = a == 0 ? ic->m2_long : ic->m2_trans;
+        *omega = p->expansion ? sqrt(psqr + (1. + 2. * p->H0 * p->T0) * m2) : sqrt(psqr + m2);
+      }
+      return 0;
+    case 4: /* :514-556, no charged form */
+      if (ic->withcharge) return -1;
+      pchisqr = sqr(pt) + sqr(nu);
+      if (ic->justnoise == 0 && pchisqr < ic->QS * ic->QS) *occ = ic->temperature / sqrt(psqr + ic->m2_long) + ic->noise;
+      else if (ic->scale2 == 0) *occ = ic->noise;
+      else *occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
+      *omega = a == 0 ? sqrt(psqr + ic->m2_long) : sqrt(psqr + ic->m2_trans);
+      return 0;
+    default:
+      return -1;
+  }
+  /* initialize 1 and 2 (:197-204, :244-249, :343-350, :390-397) */
+  if (a == 0) *omega = sqrt(psqr + fabs(M) - 3. * sqr(ic->phi0s) / (6. * Nc));
+  else *omega = sqrt(psqr + fabs(M) - sqr(ic->phi0s) / (6. * Nc));
+  return 0;
+}
+
+/* SetInitialConditions (initialconditions.cpp:45-723) for initialize 0-4,
+ * withcharge 0 or 1, static or expanding box.  Per mode (pz, px, py <= N/2)
+ * and component: two phases and two |Gaussians| -- except with charge and
+ * Nc = 2 (:132-147), where component 0 takes nothing new and component 1
+ * shifts the previous phase and Gaussian into phase2/gauss2 and draws one of
+ * each, so component 0 of a mode uses component 1's draws of the two modes
+ * before it.  Those are uninitialized locals for the first mode (:72-76);
+ * the reference pin reads them as 0, and so does this restatement. */
 int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, double *Pi) {
   const int N = p->N, Nc = p->Nc, M = N / 2 + 1;
   const long NM = (long)N * N * M, NN = (long)N * N;
   const double a = p->a;
+  if (ic->initialize < 0 || ic->initialize > 4 || (ic->initialize == 4 && ic->withcharge)) return -1;
   double *Are = (double *)calloc((size_t)Nc * NM, sizeof(double)), *Aim = (double *)calloc((size_t)Nc * NM, sizeof(double));
   double *Ere = (double *)calloc((size_t)Nc * NM, sizeof(double)), *Eim = (double *)calloc((size_t)Nc * NM, sizeof(double));
   double *X = (double *)malloc(sizeof(double) * NN * N);
+  const int paired = ic->withcharge && Nc == 2;
+  double phase1 = 0.0, phase2 = 0.0, gauss1 = 0.0, gauss2 = 0.0;
   srand48(ic->seed);
   ic_on = 0;
   for (int pz = 0; pz < N; pz++) {
@@ -776,21 +855,21 @@ int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, d
         const double psqr = sqr(pt) + sqr(nu);
         const long posMom = py + (long)px * M + (long)pz * N * M;
         for (int c = 0; c < Nc; c++) {
-          const double phase1 = 2.0 * acos(-1.) * drand48(), phase2 = 2.0 * acos(-1.) * drand48();
-          const double gauss1 = fabs(ic_gauss()), gauss2 = fabs(ic_gauss());
-          const double pchisqr = sqr(pt) + sqr(nu);
-          double occ;
-          if (ic->justnoise == 0 && p->expansion && psqr > 0. && psqr < (ic->QS * ic->QS)) {
-            const double omegap = sqrt(psqr + (1. + 2. * p->H0 * p->T0) * ic->m2_long);
-            occ = 2. * acos(-1.) * acos(-1.) * 2.1e-9 * ic->phi0[0] * ic->phi0[0] / psqr / sqrt(psqr) * omegap;
-          } else if (ic->justnoise == 0 && !p->expansion && pchisqr < ic->QS * ic->QS) {
-            occ = ic->amplitude + ic->noise;
+          if (paired) {
+            if (c == 1) {
+              phase2 = phase1;
+              phase1 = 2.0 * acos(-1.) * drand48();
+              gauss2 = gauss1;
+              gauss1 = fabs(ic_gauss());
+            }
           } else {
-            if (ic->scale2 == 0) occ = ic->noise;
-            else occ = sqrt(pchisqr) < ic->scale2 ? ic->noise : 0.0;
+            phase1 = 2.0 * acos(-1.) * drand48();
+            phase2 = 2.0 * acos(-1.) * drand48();
+            gauss1 = fabs(ic_gauss());
+            gauss2 = fabs(ic_gauss());
           }
-          const double m2 = c == 0 ? ic->m2_long : ic->m2_trans;
-          const double omega = p->expansion ? sqrt(psqr + (1. + 2. * p->H0 * p->T0) * m2) : sqrt(psqr + m2);
+          double occ = 0.0, omega = 0.0;
+          ic_occupation(p, ic, c, pt, nu, psqr, &occ, &omega);
           const double s1 = sqrt(occ) * gauss1, s2 = sqrt(occ) * gauss2;
           const long o = (long)c * NM + posMom;
           if (fabs(omega) < 1e-8) {
@@ -798,7 +877,7 @@ int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, d
           } else {
             const double so = sqrt(omega);
             Are[o] = s1 * cos(phase1) / so; Aim[o] = s1 * sin(phase1) / so;
-            if (p->expansion) {
+            if (p->expansion && !ic->withcharge) { /* E = A H_0 (:581-583) */
               Ere[o] = Are[o] * p->H0; Eim[o] = Aim[o] * p->H0;
             } else {
               Ere[o] = s2 * cos(phase2) * so; Eim[o] = s2 * sin(phase2) * so;
@@ -813,11 +892,17 @@ int orc_initial_conditions(const orc_params *p, const orc_ic *ic, double *Phi, d
     ic_ensure_real(N, Are + (long)c * NM, Aim + (long)c * NM);
     ic_ensure_real(N, Ere + (long)c * NM, Eim + (long)c * NM);
   }
+  /* the lattice values (:634-690): initialize 3 and 4 add phi0_0/1, pi0_0/1
+   * (+ phi0_0 H_0 to Pi's component 0 in the expanding box), the others
+   * phi0, pi0 to component 0 only */
+  const int own = ic->initialize == 3 || ic->initialize == 4;
   for (int f = 0; f < 2; f++)
     for (int c = 0; c < Nc; c++) {
       ic_fft_ptox(p, (f == 0 ? Are : Ere) + (long)c * NM, (f == 0 ? Aim : Eim) + (long)c * NM, X);
-      const double off = c < 2 ? (f == 0 ? ic->phi0[c] : ic->pi0[c]) : 0.0;
-      const int hubble = p->expansion && f == 1 && c == 0; /* + phi0_0 H0 (:657) */
+      double off;
+      if (own) off = c < 2 ? (f == 0 ? ic->phi0[c] : ic->pi0[c]) : 0.0;
+      else off = c == 0 ? (f == 0 ? ic->phi0s : ic->pi0s) : 0.0;
+      const int hubble = own && p->expansion && f == 1 && c == 0; /* + phi0_0 H0 (:657) */
       double *dst = f == 0 ? Phi : Pi;
       for (int z = 0; z < N; z++)
         for (int y = 0; y < N; y++)

@@ -67,6 +67,11 @@ typedef struct orc_ic {
   double QS, scale2, amplitude, noise;
   double phi0[2], pi0[2];
   double m2_long, m2_trans;
+  /* the `initialize` (0-4) and `withcharge` switches and the globals of
+   * initialize 0-2 (parameters.cpp:207-272): chi, FAmp, Lambda,
+   * Temperature and the homogeneous phi0, pi0 of component 0 */
+  int initialize, withcharge;
+  double chi, famp, lambda, temperature, phi0s, pi0s;
 } orc_ic;
 
 int orc_version(void);

@@ -364,8 +364,20 @@ int ref_apply_filter(double r, int which, const double *table, int n, double dp)
  * and ./moment-<name>.out in the working directory. */
 void ref_save_config(int name) { SaveConfig(name); }
 
-/* SetInitialConditions() (initialize 3) with srand48(seed); the fields land
- * in LocalLattice::Phi/Pi (read them with ref_get_fields). */
+/* The globals of initialize 0-2 and 4 (parameters.cpp:207-272): chi,
+ * FAmp, Lambda, Temperature and the homogeneous phi0, pi0 of component 0. */
+void ref_set_ic_extra(double chi_, double famp, double lambda, double temperature, double phi0_, double pi0_) {
+  chi = (pseudo_double)chi_;
+  FAmp = (pseudo_double)famp;
+  Lambda = (pseudo_double)lambda;
+  Temperature = (pseudo_double)temperature;
+  phi0 = (pseudo_double)phi0_;
+  pi0 = (pseudo_double)pi0_;
+}
+
+/* SetInitialConditions() (the build's `initialize` and `withcharge`) with
+ * srand48(seed); the fields land in LocalLattice::Phi/Pi (read them with
+ * ref_get_fields). */
 int ref_initial_conditions(long seed, int justnoise_, double qs, double scale2_, double amplitude, double noise,
                            double phi00, double phi01, double pi00, double pi01) {
   if (!g_ready) return -1;

@@ -53,7 +53,10 @@
 #define withCorr 1
 #define withBins 1
 #define LAMBDA_MODE 1
-#define withcharge 0
+#ifndef PHN_REF_WITHCHARGE
+#define PHN_REF_WITHCHARGE 0
+#endif
+#define withcharge PHN_REF_WITHCHARGE
 #ifndef PHN_REF_EXPANSION
 #define PHN_REF_EXPANSION 0
 #endif
@@ -64,7 +67,10 @@
 #define EnergybasedID 0
 #define theory PHN_REF_THEORY
 #define adjustDT 0
-#define initialize 3
+#ifndef PHN_REF_INIT
+#define PHN_REF_INIT 3
+#endif
+#define initialize PHN_REF_INIT
 
 int runs = 1;
 int runID = 1;
@@ -111,6 +117,12 @@ pseudo_double Noise = 0.5;
 pseudo_double phi0_0 = 0., phi0_1 = 0.;
 pseudo_double pi0_0 = 0., pi0_1 = 0.;
 pseudo_double M2_long = 0., M2_trans = 0.;
+/* initialize 0-2 (parameters.cpp:207-272): the homogeneous values phi0, pi0
+ * of component 0, FAmp and Temperature (initialize 0; Temperature also in
+ * initialize 4, which parameters.cpp gives no block of its own) */
+pseudo_double phi0 = 0., pi0 = 0.;
+pseudo_double FAmp = 0.5;
+pseudo_double Temperature = 1.;
 
 int LASTRUN = 0;
 

@@ -1,6 +1,6 @@
-// Initial conditions on the GPU: SetInitialConditions for `initialize 3`,
-// static or expanding box, no charge (initialconditions.cpp:45-723,
-// clusterfft.cpp:55-182), with the reference's own random stream.  The
+// Initial conditions on the GPU: SetInitialConditions for `initialize` 0-4,
+// with or without charge, static or expanding box (initialconditions.cpp:
+// 45-723, clusterfft.cpp:55-182), with the reference's own random stream.  The
 // expanding box (:459-465, :504-510, :581-583, :656-658) seeds the
 // scale-invariant occupation 2 pi^2 2.1e-9 phi0_0^2 omega_p / p^3 below QS,
 // uses Omega^2 = p^2 + (1 + 2 H_0 T0) M^2, E = H_0 A, and adds phi0_0 H_0 to
@@ -16,6 +16,12 @@
 // accepted one.  Which pair belongs to which mode is a two-state automaton
 // over the acceptance flags ("next pair is a phase pair" / "a trial pair");
 // it is evaluated with a parallel prefix over chunks of pairs.
+//
+// The charged variant with Nc = 2 (withcharge 1, :132-147) draws one phase
+// and one Gaussian per mode (component 1; component 0 reuses the draws of the
+// two modes before).  Its stream is u_0, then trials up to an accepted pair
+// (whose two Gaussians serve two modes), then u_1 u_2, trials, u_3 u_4, ...:
+// one draw later, the same automaton over pairs, entered in the trial state.
 //
 //   ic_pairs    drand48 by jump-ahead (X <- A^k X + C_k mod 2^48): each thread
 //               one chunk of pairs; stores the pairs (exact doubles X / 2^48),
@@ -156,11 +162,12 @@ __global__ void ic_scan_blocks(const Trans *__restrict__ trans, long long nchunk
   if (threadIdx.x == IC_THREADS - 1) block_total[blockIdx.x] = sh[cur][threadIdx.x];
 }
 
-// Entry state and modes completed before each block, from the start state 0.
-__global__ void ic_scan_top(const Trans *__restrict__ block_total, long long nblocks, unsigned char *__restrict__ bstate,
-                            unsigned long long *__restrict__ bmodes) {
+// Entry state and modes completed before each block, from the start state
+// (0: a phase pair first; 1: a trial first, the charged stream).
+__global__ void ic_scan_top(const Trans *__restrict__ block_total, long long nblocks, int start,
+                            unsigned char *__restrict__ bstate, unsigned long long *__restrict__ bmodes) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  unsigned char s = 0;
+  unsigned char s = (unsigned char)start;
   unsigned long long n = 0;
   for (long long b = 0; b < nblocks; ++b) {
     bstate[b] = s;
@@ -204,10 +211,20 @@ __global__ void ic_assign(const double2 *__restrict__ uv, long long npairs, long
 
 struct IcConsts {
   int N, Nc, justnoise, expansion;
+  int initialize, withcharge;
   double a, QS, scale2, amplitude, noise, m2_long, m2_trans;
   double H0;
   double a0sq;      // 1. + 2.*H_0*T0: the initial scale factor squared
   double spectrum;  // 2.*acos(-1.)*acos(-1.)*2.1e-9*phi0_0*phi0_0
+  // initialize 0-2 and 4 (host values in the reference's order)
+  double abs_m;     // fabs(M_sqr)
+  double w_long, w_trans;  // 3.*sqr(Temperature)*sqr(phi0)/(6.*Nc), sqr(T)*sqr(phi0)/(6.*Nc) (init 0);
+                           // 3.*sqr(phi0)/(6.*Nc), sqr(phi0)/(6.*Nc) (init 1, 2)
+  double occ0;      // FAmp*Lambda (init 0)
+  double chi2;      // sqr(chi) (init 1)
+  double two_qs;    // 2.0*QS (init 1)
+  double temperature;
+  double u0;        // the charged stream's first draw
 };
 
 // Per-axis lattice momentum as initialconditions.cpp:88-113 writes it,
@@ -217,8 +234,111 @@ static double ic_p_host(int n, int N, double a) {
   return -2.0 / (a) * sin(n * acos(-1.) / N);
 }
 
-// One (mode, component): initialconditions.cpp:339-569 (initialize 3,
-// withcharge 0).  A and E are [a][pz][px][py] complex arrays.
+// The chopped plateau of initialize 2-4: Noise below scale2 (everywhere
+// when scale2 == 0), else 0.
+__device__ __forceinline__ double ic_plateau(const IcConsts &k, double root) {
+  return k.scale2 == 0 ? k.noise : (root < k.scale2 ? k.noise : 0.0);
+}
+
+// Occupation and Omega of one mode and component, each `initialize` branch
+// with its own comparisons (initialconditions.cpp:163-257 with charge,
+// :308-556 without); IEEE operations in the reference's order.
+__device__ void ic_occ_omega(const IcConsts &k, int a, double pt, double nu, double psqr, double *occ,
+                             double *omega) {
+  const double m2 = a == 0 ? k.m2_long : k.m2_trans;
+  switch (k.initialize) {
+    case 0:
+      *omega = __dsqrt_rn(__dsub_rn(__dadd_rn(psqr, k.abs_m), a == 0 ? k.w_long : k.w_trans));
+      *occ = k.occ0;
+      return;
+    case 1: {
+      const double pchisqr = __dadd_rn(__dmul_rn(pt, pt), __dmul_rn(k.chi2, __dmul_rn(nu, nu)));
+      const double root = __dsqrt_rn(pchisqr);
+      *occ = root < k.QS ? k.amplitude : (root < k.two_qs ? k.noise : 0.0);
+      *omega = __dsqrt_rn(__dsub_rn(__dadd_rn(psqr, k.abs_m), a == 0 ? k.w_long : k.w_trans));
+      return;
+    }
+    case 2: {
+      const double root = __dsqrt_rn(psqr);  // pchisqr = sqr(pt)+sqr(nu) = psqr
+      *occ = (k.justnoise == 0 && root < k.QS) ? __dadd_rn(k.amplitude, k.noise) : ic_plateau(k, root);
+      *omega = __dsqrt_rn(__dsub_rn(__dadd_rn(psqr, k.abs_m), a == 0 ? k.w_long : k.w_trans));
+      return;
+    }
+    case 3: {
+      const double root = __dsqrt_rn(psqr);
+      if (k.withcharge) {  // :255-291, static forms
+        *occ = (k.justnoise == 0 && root < k.QS) ? __dadd_rn(k.amplitude, k.noise) : ic_plateau(k, root);
+        *omega = __dsqrt_rn(__dadd_rn(psqr, m2));
+        return;
+      }
+      if (k.expansion) {  // :459-465, :504-510
+        if (k.justnoise == 0 && psqr > 0. && psqr < __dmul_rn(k.QS, k.QS)) {
+          const double omegap = __dsqrt_rn(__dadd_rn(psqr, __dmul_rn(k.a0sq, k.m2_long)));
+          *occ = __dmul_rn(__ddiv_rn(__ddiv_rn(k.spectrum, psqr), __dsqrt_rn(psqr)), omegap);
+        } else {
+          *occ = ic_plateau(k, root);
+        }
+        *omega = __dsqrt_rn(__dadd_rn(psqr, __dmul_rn(k.a0sq, m2)));
+      } else {
+        *occ = (k.justnoise == 0 && psqr < __dmul_rn(k.QS, k.QS)) ? __dadd_rn(k.amplitude, k.noise)
+                                                                   : ic_plateau(k, root);
+        *omega = __dsqrt_rn(__dadd_rn(psqr, m2));
+      }
+      return;
+    }
+    default: {  // 4 (:514-556)
+      const double root = __dsqrt_rn(psqr);
+      *occ = (k.justnoise == 0 && psqr < __dmul_rn(k.QS, k.QS))
+                 ? __dadd_rn(__ddiv_rn(k.temperature, __dsqrt_rn(__dadd_rn(psqr, k.m2_long))), k.noise)
+                 : ic_plateau(k, root);
+      *omega = __dsqrt_rn(__dadd_rn(psqr, m2));
+      return;
+    }
+  }
+}
+
+// Box-Muller of an accepted pair (initialconditions.cpp:36-39): gauss1 and
+// the cached gauss2.
+__device__ __forceinline__ void ic_box_muller(double2 g, double *g1, double *g2) {
+  const double x = __dsub_rn(__dmul_rn(2.0, g.x), 1.0), y = __dsub_rn(__dmul_rn(2.0, g.y), 1.0);
+  const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)));
+  const double c = __ddiv_rn(x, r), s = __ddiv_rn(y, r);
+  *g1 = __dmul_rn(c, __dsqrt_rn(__dmul_rn(-2.0, log(__dmul_rn(r, r)))));
+  *g2 = __dmul_rn(__ddiv_rn(s, c), *g1);
+}
+
+// A and E of one mode and component from its phases and |Gaussians|
+// (initialconditions.cpp:563-587): F = sqrt(occ) g (cos th, sin th),
+// A = F1 / sqrt(Omega), E = F2 sqrt(Omega), or E = A H_0 in the expanding
+// box without charge; both 0 where |Omega| < 1e-8.
+__device__ void ic_amplitudes(const IcConsts &k, int a, int pz, int px, int py, const double *__restrict__ ptab,
+                              double phase1, double phase2, double gauss1, double gauss2, double2 *fa_out,
+                              double2 *fe_out) {
+  const double nu = pz == 0 ? 0.0 : ptab[pz];
+  const double ppx = ptab[px];
+  const double ppy = ptab[py];  // py <= N/2: the positive branch
+  const double pt = __dsqrt_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)));
+  const double psqr = __dadd_rn(__dmul_rn(pt, pt), __dmul_rn(nu, nu));
+  double occ, omega;
+  ic_occ_omega(k, a, pt, nu, psqr, &occ, &omega);
+  const double amp1 = __dmul_rn(__dsqrt_rn(occ), gauss1), amp2 = __dmul_rn(__dsqrt_rn(occ), gauss2);
+  double2 fa = make_double2(0.0, 0.0), fe = make_double2(0.0, 0.0);
+  if (!(fabs(omega) < 1e-8)) {
+    const double so = __dsqrt_rn(omega);
+    fa = make_double2(__ddiv_rn(__dmul_rn(amp1, cos(phase1)), so), __ddiv_rn(__dmul_rn(amp1, sin(phase1)), so));
+    if (k.expansion && !k.withcharge)  // EFieldP = AFieldP * H_0 (:581-583)
+      fe = make_double2(__dmul_rn(fa.x, k.H0), __dmul_rn(fa.y, k.H0));
+    else
+      fe = make_double2(__dmul_rn(__dmul_rn(amp2, cos(phase2)), so), __dmul_rn(__dmul_rn(amp2, sin(phase2)), so));
+  }
+  *fa_out = fa;
+  *fe_out = fe;
+}
+
+// One (mode, component) of the uncharged stream (and the charged one for
+// Nc != 2, which draws alike): two phases from its phase pair, two
+// Gaussians from its accepted pair.  A and E are [a][pz][px][py] complex
+// arrays.
 __global__ void ic_modes(const IcConsts k, const double *__restrict__ ptab, const double2 *__restrict__ uv,
                          const long long *__restrict__ phase_pair,
                          const long long *__restrict__ acc_pair, long long nmodes, double2 *__restrict__ A,
@@ -229,54 +349,53 @@ __global__ void ic_modes(const IcConsts k, const double *__restrict__ ptab, cons
   const int a = (int)(m % k.Nc);
   const long long pos = m / k.Nc;  // py + px M + pz N M: the mode loop order
   const int py = (int)(pos % M), px = (int)((pos / M) % N), pz = (int)(pos / ((long long)M * N));
-  const double nu = pz == 0 ? 0.0 : ptab[pz];
-  const double ppx = ptab[px];
-  const double ppy = ptab[py];  // py <= N/2: the positive branch
-  const double pt = __dsqrt_rn(__dadd_rn(__dmul_rn(ppx, ppx), __dmul_rn(ppy, ppy)));
-  const double psqr = __dadd_rn(__dmul_rn(pt, pt), __dmul_rn(nu, nu));
   // phases and Gaussians (initialconditions.cpp:27-41, 344-349)
-  const double2 ph = uv[phase_pair[m]], g = uv[acc_pair[m]];
+  const double2 ph = uv[phase_pair[m]];
   const double two_pi = __dmul_rn(2.0, acos(-1.));
-  const double phase1 = __dmul_rn(two_pi, ph.x), phase2 = __dmul_rn(two_pi, ph.y);
-  const double x = __dsub_rn(__dmul_rn(2.0, g.x), 1.0), y = __dsub_rn(__dmul_rn(2.0, g.y), 1.0);
-  const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)));
-  const double c = __ddiv_rn(x, r), s = __ddiv_rn(y, r);
-  const double g1 = __dmul_rn(c, __dsqrt_rn(__dmul_rn(-2.0, log(__dmul_rn(r, r)))));
-  const double g2 = __dmul_rn(__ddiv_rn(s, c), g1);
-  const double gauss1 = fabs(g1), gauss2 = fabs(g2);
-  // occupation (initialconditions.cpp:442-497) and Omega (:499-505)
-  const double pchisqr = psqr;
-  double occ;
-  const double root = __dsqrt_rn(pchisqr);
-  const double plateau = k.scale2 == 0 ? k.noise : (root < k.scale2 ? k.noise : 0.0);
-  const double m2 = a == 0 ? k.m2_long : k.m2_trans;
-  double omega;
-  if (k.expansion) {  // initialconditions.cpp:459-465, :504-510
-    if (k.justnoise == 0 && psqr > 0. && psqr < __dmul_rn(k.QS, k.QS)) {
-      const double omegap = __dsqrt_rn(__dadd_rn(psqr, __dmul_rn(k.a0sq, k.m2_long)));
-      occ = __dmul_rn(__ddiv_rn(__ddiv_rn(k.spectrum, psqr), __dsqrt_rn(psqr)), omegap);
-    } else {
-      occ = plateau;
-    }
-    omega = __dsqrt_rn(__dadd_rn(psqr, __dmul_rn(k.a0sq, m2)));
-  } else {
-    if (k.justnoise == 0)
-      occ = pchisqr < __dmul_rn(k.QS, k.QS) ? __dadd_rn(k.amplitude, k.noise) : plateau;
-    else
-      occ = plateau;
-    omega = __dsqrt_rn(__dadd_rn(psqr, m2));
-  }
-  // F = sqrt(occ) g (cos th, sin th); A = F1 / sqrt(Omega), E = F2 sqrt(Omega)
-  const double amp1 = __dmul_rn(__dsqrt_rn(occ), gauss1), amp2 = __dmul_rn(__dsqrt_rn(occ), gauss2);
-  double2 fa = make_double2(0.0, 0.0), fe = make_double2(0.0, 0.0);
-  if (!(fabs(omega) < 1e-8)) {
-    const double so = __dsqrt_rn(omega);
-    fa = make_double2(__ddiv_rn(__dmul_rn(amp1, cos(phase1)), so), __ddiv_rn(__dmul_rn(amp1, sin(phase1)), so));
-    if (k.expansion)  // EFieldP = AFieldP * H_0 (:581-583)
-      fe = make_double2(__dmul_rn(fa.x, k.H0), __dmul_rn(fa.y, k.H0));
-    else
-      fe = make_double2(__dmul_rn(__dmul_rn(amp2, cos(phase2)), so), __dmul_rn(__dmul_rn(amp2, sin(phase2)), so));
-  }
+  double g1, g2;
+  ic_box_muller(uv[acc_pair[m]], &g1, &g2);
+  double2 fa, fe;
+  ic_amplitudes(k, a, pz, px, py, ptab, __dmul_rn(two_pi, ph.x), __dmul_rn(two_pi, ph.y), fabs(g1), fabs(g2), &fa,
+                &fe);
+  const size_t o = (size_t)a * N * N * M + ((size_t)pz * N + px) * M + py;
+  A[o] = fa;
+  E[o] = fe;
+}
+
+// The charged stream with Nc = 2: mode m's draw u_m (u_0 the first draw;
+// then u_{2j-1}, u_{2j} the j-th phase pair) and |Gaussian| (the first or
+// the cached second value of accepted pair m/2).  Component 1 of mode m
+// takes (u_m, u_{m-1}) and (g_m, g_{m-1}); component 0 those of m-1 and m-2;
+// values before the stream began are the reference's uninitialized locals,
+// read as 0 (as its pinned build reads them).
+__device__ __forceinline__ double ic_q_phase(const IcConsts &k, const double2 *__restrict__ uv,
+                                             const long long *__restrict__ phase_pair, long long m) {
+  if (m < 0) return 0.0;
+  const double u = m == 0 ? k.u0 : ((m & 1) ? uv[phase_pair[(m + 1) / 2]].x : uv[phase_pair[m / 2]].y);
+  return __dmul_rn(__dmul_rn(2.0, acos(-1.)), u);
+}
+
+__device__ __forceinline__ double ic_q_gauss(const double2 *__restrict__ uv, const long long *__restrict__ acc_pair,
+                                             long long m) {
+  if (m < 0) return 0.0;
+  double g1, g2;
+  ic_box_muller(uv[acc_pair[m / 2]], &g1, &g2);
+  return fabs((m & 1) ? g2 : g1);
+}
+
+__global__ void ic_modes_q(const IcConsts k, const double *__restrict__ ptab, const double2 *__restrict__ uv,
+                           const long long *__restrict__ phase_pair, const long long *__restrict__ acc_pair,
+                           long long nmodes, double2 *__restrict__ A, double2 *__restrict__ E) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= nmodes) return;
+  const int N = k.N, M = N / 2 + 1;
+  const int a = (int)(t & 1);
+  const long long pos = t >> 1;
+  const int py = (int)(pos % M), px = (int)((pos / M) % N), pz = (int)(pos / ((long long)M * N));
+  const long long m = a == 1 ? pos : pos - 1;
+  double2 fa, fe;
+  ic_amplitudes(k, a, pz, px, py, ptab, ic_q_phase(k, uv, phase_pair, m), ic_q_phase(k, uv, phase_pair, m - 1),
+                ic_q_gauss(uv, acc_pair, m), ic_q_gauss(uv, acc_pair, m - 1), &fa, &fe);
   const size_t o = (size_t)a * N * N * M + ((size_t)pz * N + px) * M + py;
   A[o] = fa;
   E[o] = fe;

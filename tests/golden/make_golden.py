@@ -84,6 +84,29 @@ IC_CASES = {
                                                       pi0=(0.1, 0.0))),
     "n16_exp_nc2": (dict(N=16, Nc=2, **PHI6, **EXP, T0=3.0),
                     dict(seed=42, noise=0.5, QS=4.0, scale2=6.0, phi0=(2.0, -0.5), pi0=(0.0, 0.3))),
+    # the other `initialize` switches and the charged variant (withcharge 1),
+    # from the reference builds oracle/_ref/libphinum_ref_t0_f64_ic*.so
+    "n12_ic0": (dict(N=12, Nc=1, **dict(PHI6, m_sqr=0.7)),
+                dict(seed=51, initialize=0, famp=0.5, lambda_=1.7, temperature=0.6, phi0s=0.9, pi0s=0.3,
+                     variant="_ic0")),
+    "n12_ic1_nc2": (dict(N=12, Nc=2, **dict(PHI6, m_sqr=0.7)),
+                    dict(seed=52, initialize=1, QS=5.0, amplitude=0.8, noise=0.4, chi=1.3, phi0s=0.9, pi0s=0.3,
+                         variant="_ic1")),
+    "n12_ic2_nc3": (dict(N=12, Nc=3, **dict(PHI6, m_sqr=0.7)),
+                    dict(seed=53, initialize=2, QS=5.0, scale2=7.0, amplitude=0.8, noise=0.4, phi0s=0.9, pi0s=0.3,
+                         variant="_ic2")),
+    "n12_ic4_nc2": (dict(N=12, Nc=2, **dict(PHI6, m_sqr=0.7)),
+                    dict(seed=54, initialize=4, QS=5.0, scale2=7.0, noise=0.4, temperature=0.6, phi0=(1.0, 0.5),
+                         pi0=(0.2, -0.1), variant="_ic4")),
+    "n12_ic2q_nc2": (dict(N=12, Nc=2, **dict(PHI6, m_sqr=0.7)),
+                     dict(seed=55, initialize=2, withcharge=1, QS=5.0, scale2=7.0, amplitude=0.8, noise=0.4,
+                          phi0s=0.9, pi0s=0.3, variant="_ic2q")),
+    "n16_ic3q_nc2": (dict(N=16, Nc=2, **dict(PHI6, m_sqr=0.7)),
+                     dict(seed=56, initialize=3, withcharge=1, QS=5.0, scale2=7.0, amplitude=0.8, noise=0.4,
+                          phi0=(1.0, 0.5), pi0=(0.2, -0.1), variant="_ic3q")),
+    "n12_ic3q_nc1": (dict(N=12, Nc=1, **dict(PHI6, m_sqr=0.7)),
+                     dict(seed=57, initialize=3, withcharge=1, QS=5.0, scale2=7.0, amplitude=0.8, noise=0.4,
+                          phi0=(1.0, 0.0), variant="_ic3q")),
 }
 
 
@@ -261,8 +284,10 @@ def run_f32_case(name: str) -> None:
 def run_ic_case(name: str) -> None:
     from oracle import oracle as O
     pd, ic = IC_CASES[name]
+    ic = dict(ic)
+    variant = ic.pop("variant", "")
     p = O.Params(**{"a": 0.25, "dt": 0.08, "T0": 0.0, **pd})
-    R = O.Reference(p)
+    R = O.Reference(p, "f64", variant)
     phi, pi = R.initial_conditions(**ic)
     os.makedirs(os.path.join(HERE, "ic"), exist_ok=True)
     np.savez_compressed(os.path.join(HERE, "ic", f"{name}.npz"), params=json.dumps(pd), ic=json.dumps(ic),
