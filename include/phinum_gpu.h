@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PHN_ABI_VERSION 3
+#define PHN_ABI_VERSION 4
 #define PHN_MAX_NC 4
 
 enum {
@@ -192,6 +192,38 @@ typedef struct phn_ic_params {
   double m2_trans;      /* M2_trans (components a >= 1) */
 } phn_ic_params;
 int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic);
+
+/* SetInitialConditions() for the reference's other compile-time choices
+ * (initialconditions.cpp:45-723; parameters.cpp:205-303): `initialize`
+ *   0  parametric resonance: occupation FAmp*Lambda, Omega^2 = p^2 + |M_sqr|
+ *      - 3 Temperature^2 phi0^2 / (6 Nc) (component 0; 1x for the others);
+ *   1  box: occupation Amplitude below QS in sqrt(pt^2 + chi^2 pz^2), Noise
+ *      below 2 QS, Omega^2 = p^2 + |M_sqr| - 3 phi0^2 / (6 Nc) (1x for a > 0);
+ *   2  large-Lambda box: Amplitude + Noise below QS, Noise below scale2,
+ *      Omega as initialize 1;
+ *   3  phn_initial_conditions;
+ *   4  Temperature / sqrt(p^2 + M2_long) + Noise below QS, Noise below
+ *      scale2, Omega as initialize 3 (static forms);
+ * with withcharge 1 the charged variant (:120-291): for Nc = 2 one phase and
+ * one Gaussian per mode, component 0 reusing the draws of the two modes
+ * before (the first mode's are the reference's uninitialized locals, taken as
+ * 0); for other Nc the draws of withcharge 0, with the static forms of
+ * initialize 3.  Initialize 0-2 add phi0, pi0 to component 0 only; 3 and 4
+ * add phi0[], pi0[] of phn_ic_params to components 0 and 1.  phn_ic_params
+ * supplies seed, justnoise, QS, scale2, Amplitude, Noise, M2_long/M2_trans
+ * (and phi0[], pi0[] for 3, 4); M_sqr is the handle's.  Initialize 4 with
+ * charge is PHN_ERR_UNSUPPORTED (the reference sets no occupation there). */
+typedef struct phn_ic_mode {
+  int init_mode;      /* the reference's `initialize` switch, 0-4 */
+  int charged;        /* its `withcharge` switch, 0 or 1 (both named apart because the
+                         reference #defines them in the translation unit that includes this) */
+  double chi;         /* chi: anisotropy of initialize 1 */
+  double famp;        /* FAmp (initialize 0) */
+  double lambda;      /* Lambda (initialize 0) */
+  double temperature; /* Temperature (initialize 0 and 4) */
+  double phi0, pi0;   /* phi0, pi0 of initialize 0-2 */
+} phn_ic_mode;
+int phn_initial_conditions_mode(phn_handle *h, const phn_ic_params *ic, const phn_ic_mode *mode);
 
 /* Full_Analysis() seeding from an empty history (islands.cpp:72-279,778-840):
  * mask (mode), 6-connectivity, x and y periodic, z open as on one rank unless

@@ -25,7 +25,7 @@ _D, _I = ctypes.c_double, ctypes.c_int
 _PD, _PI = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
 
 
-ABI_VERSION = 3  # PHN_ABI_VERSION of include/phinum_gpu.h
+ABI_VERSION = 4  # PHN_ABI_VERSION of include/phinum_gpu.h
 
 
 class PhnParams(ctypes.Structure):
@@ -38,6 +38,11 @@ class PhnParams(ctypes.Structure):
 class PhnIcParams(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_long), ("justnoise", _I), ("QS", _D), ("scale2", _D), ("amplitude", _D),
                 ("noise", _D), ("phi0", _D * 2), ("pi0", _D * 2), ("m2_long", _D), ("m2_trans", _D)]
+
+
+class PhnIcMode(ctypes.Structure):
+    _fields_ = [("init_mode", _I), ("charged", _I), ("chi", _D), ("famp", _D), ("lambda_", _D),
+                ("temperature", _D), ("phi0", _D), ("pi0", _D)]
 
 
 class PhnTrackIsland(ctypes.Structure):
@@ -88,6 +93,7 @@ _SIGS = {
     "phn_spectrum": (_I, [ctypes.c_void_p, _PD, _PD, _PD, _PI, _I]),
     "phn_spectrum_uniform": (_I, [ctypes.c_void_p, _I, _PD, _PD, _PD, _PI]),
     "phn_initial_conditions": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams)]),
+    "phn_initial_conditions_mode": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams), ctypes.POINTER(PhnIcMode)]),
     "phn_islands_lookup": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _I, _PI]),
     "phn_save_config": (_I, [ctypes.c_void_p, ctypes.c_char_p, _I, _I, _I]),
     "phn_apply_filter": (_I, [ctypes.c_void_p, _D, _I, _PD, _I, _D]),

@@ -46,6 +46,7 @@
 // C library's in the last bit, and cuFFT rounds differently from FFTW.
 #include <cufft.h>
 #include <math.h>
+#include <string.h>
 
 #include "phn_internal.h"
 
@@ -453,12 +454,21 @@ using namespace phn;
 
 extern "C" {
 
-int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
-  if (!h || !ic) return set_error(PHN_ERR_INVALID, "NULL argument");
+static int run_initial_conditions(phn_handle *h, const phn_ic_params *ic, const phn_ic_mode *md) {
+  if (!h || !ic || !md) return set_error(PHN_ERR_INVALID, "NULL argument");
   const int N = h->p.N, Nc = h->p.Nc;
   if (N % 2 != 0) return set_error(PHN_ERR_UNSUPPORTED, "initial conditions need an even N");
+  if (md->init_mode < 0 || md->init_mode > 4) return set_error(PHN_ERR_INVALID, "initialize %d", md->init_mode);
+  if (md->charged != 0 && md->charged != 1) return set_error(PHN_ERR_INVALID, "withcharge %d", md->charged);
+  if (md->init_mode == 4 && md->charged)
+    return set_error(PHN_ERR_UNSUPPORTED, "initialize 4 has no charged form (the reference sets no occupation)");
   const int M = N / 2 + 1;
-  const long long nmodes = (long long)N * N * M * Nc;
+  // the charged stream with Nc = 2: one accepted pair per two modes; the
+  // automaton runs one mode further for the last modes' phases
+  const bool paired = md->charged && Nc == 2;
+  const long long nspatial = (long long)N * N * M;
+  const long long nmodes = paired ? nspatial / 2 + 1 : nspatial * Nc;
+  const long long nthreads = paired ? nspatial * 2 : nmodes;
   // pairs: one phase pair per mode plus 4/pi trials on average; 2.5 per mode
   // leaves a margin of thousands of standard deviations
   const long long npairs = nmodes * 5 / 2 + 65536;
@@ -507,14 +517,20 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
       for (int n = 0; n < N; ++n) tab[n] = ic_p_host(n, N, h->p.a);
       ICK(cudaMemcpy(ptab, tab, N * sizeof(double), cudaMemcpyHostToDevice));
     }
-    // srand48(seed): X0 = (seed mod 2^32) 2^16 + 0x330E
-    const unsigned long long x0 = (((unsigned long long)ic->seed & 0xFFFFFFFFULL) << 16) | 0x330EULL;
+    // srand48(seed): X0 = (seed mod 2^32) 2^16 + 0x330E; the charged
+    // stream's pairs start after its first draw
+    unsigned long long x0 = (((unsigned long long)ic->seed & 0xFFFFFFFFULL) << 16) | 0x330EULL;
+    double u0 = 0.0;
+    if (paired) {
+      x0 = (LCG_A * x0 + LCG_C) & LCG_MASK;
+      u0 = (double)x0 * 0x1p-48;
+    }
     const int tb = 128;
     ic_pairs<<<(unsigned)((nchunks + tb - 1) / tb), tb, 0, st>>>(x0, npairs, uv, trans, nchunks);
     ICK(cudaGetLastError());
     ic_scan_blocks<<<(unsigned)nsblocks, IC_THREADS, 0, st>>>(trans, nchunks, excl, btot);
     ICK(cudaGetLastError());
-    ic_scan_top<<<1, 1, 0, st>>>(btot, nsblocks, bstate, bmodes);
+    ic_scan_top<<<1, 1, 0, st>>>(btot, nsblocks, paired ? 1 : 0, bstate, bmodes);
     ICK(cudaGetLastError());
     ICK(cudaMemcpyAsync(&done, bmodes + nsblocks, sizeof(done), cudaMemcpyDeviceToHost, st));
     ICK(cudaStreamSynchronize(st));
@@ -522,6 +538,7 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
       r = set_error(PHN_ERR_INVALID, "random stream too short (%llu of %lld modes)", done, nmodes);
       goto cleanup;
     }
+    ICK(cudaMemsetAsync(phase_pair, 0, nmodes * sizeof(long long), st));
     ic_assign<<<(unsigned)((nchunks + tb - 1) / tb), tb, 0, st>>>(uv, npairs, nchunks, excl, bstate, bmodes, nmodes,
                                                                   phase_pair, acc_pair);
     ICK(cudaGetLastError());
@@ -540,7 +557,29 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
     k.H0 = h->p.H0;
     k.a0sq = 1. + 2. * h->p.H0 * h->p.T0;
     k.spectrum = 2. * acos(-1.) * acos(-1.) * 2.1e-9 * ic->phi0[0] * ic->phi0[0];
-    ic_modes<<<(unsigned)((nmodes + 255) / 256), 256, 0, st>>>(k, ptab, uv, phase_pair, acc_pair, nmodes, A, E);
+    k.initialize = md->init_mode;
+    k.withcharge = md->charged;
+    k.abs_m = fabs(h->p.m_sqr);
+    // the mode-independent parts of Omega and the occupation, in the
+    // reference's order (initialconditions.cpp:166-171, :198-203, :245-248)
+    if (md->init_mode == 0) {
+      k.w_long = 3. * (md->temperature * md->temperature) * (md->phi0 * md->phi0) / (6. * Nc);
+      k.w_trans = (md->temperature * md->temperature) * (md->phi0 * md->phi0) / (6. * Nc);
+    } else {
+      k.w_long = 3. * (md->phi0 * md->phi0) / (6. * Nc);
+      k.w_trans = (md->phi0 * md->phi0) / (6. * Nc);
+    }
+    k.occ0 = md->famp * md->lambda;
+    k.chi2 = md->chi * md->chi;
+    k.two_qs = 2.0 * ic->QS;
+    k.temperature = md->temperature;
+    k.u0 = u0;
+    if (paired)
+      ic_modes_q<<<(unsigned)((nthreads + 255) / 256), 256, 0, st>>>(k, ptab, uv, phase_pair, acc_pair, nthreads, A,
+                                                                     E);
+    else
+      ic_modes<<<(unsigned)((nthreads + 255) / 256), 256, 0, st>>>(k, ptab, uv, phase_pair, acc_pair, nthreads, A,
+                                                                   E);
     ICK(cudaGetLastError());
     const long long nre = 2LL * N * N * Nc;
     ic_reality<<<(unsigned)((nre + 255) / 256), 256, 0, st>>>(A, N, Nc);
@@ -570,9 +609,13 @@ int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
           r = set_error(PHN_ERR_CUDA, "cufftExecZ2D failed");
           goto cleanup;
         }
-        const double off = a < 2 ? (f == 0 ? phi0[a] : pi0[a]) : 0.0;
-        // the expanding box's Pi_0 += phi0_0 H_0 (initialconditions.cpp:657)
-        const double off2 = (h->p.expanding && f == 1 && a == 0) ? phi0[0] * h->p.H0 : 0.0;
+        // initialize 3 and 4 add phi0_0/1, pi0_0/1 (and the expanding box's
+        // Pi_0 += phi0_0 H_0, initialconditions.cpp:657), the others phi0,
+        // pi0 to component 0 only (:673-686)
+        const bool own = md->init_mode == 3 || md->init_mode == 4;
+        const double off = own ? (a < 2 ? (f == 0 ? phi0[a] : pi0[a]) : 0.0)
+                               : (a == 0 ? (f == 0 ? md->phi0 : md->pi0) : 0.0);
+        const double off2 = (own && h->p.expanding && f == 1 && a == 0) ? phi0[0] * h->p.H0 : 0.0;
         void *dst = f == 0 ? h->phi[h->cur] : h->pi;
         if (h->p.precision == PHN_FP64) {
           ic_store<double><<<sg, sb, 0, st>>>(X, (double *)dst + (size_t)a * h->V, N, scale, off, off2);
@@ -604,6 +647,17 @@ cleanup:
   cudaFree(X);
   cudaFree(ptab);
   return r;
+}
+
+int phn_initial_conditions(phn_handle *h, const phn_ic_params *ic) {
+  phn_ic_mode md;
+  memset(&md, 0, sizeof(md));
+  md.init_mode = 3;
+  return run_initial_conditions(h, ic, &md);
+}
+
+int phn_initial_conditions_mode(phn_handle *h, const phn_ic_params *ic, const phn_ic_mode *mode) {
+  return run_initial_conditions(h, ic, mode);
 }
 
 }  // extern "C"

@@ -119,15 +119,24 @@ class Lattice:
 
     def initial_conditions(self, seed: int = 1, justnoise: int = 0, QS: float = 1.0, scale2: float = 1.0,
                            amplitude: float = 0.0, noise: float = 0.5, phi0=(0.0, 0.0), pi0=(0.0, 0.0),
-                           m2_long: float | None = None, m2_trans: float | None = None):
-        """SetInitialConditions (initialize 3) on the device with the
-        reference's drand48 stream from srand48(seed); M2_long and M2_trans
-        default to M_sqr (renormalization.cpp:17-18)."""
+                           m2_long: float | None = None, m2_trans: float | None = None, initialize: int = 3,
+                           withcharge: int = 0, chi: float = 1.0, famp: float = 0.5, lambda_: float = 1.0,
+                           temperature: float = 1.0, phi0s: float = 0.0, pi0s: float = 0.0):
+        """SetInitialConditions on the device with the reference's drand48
+        stream from srand48(seed): initialize 3 without charge through
+        phn_initial_conditions, any other initialize / withcharge through
+        phn_initial_conditions_mode (phi0s, pi0s: the phi0, pi0 of
+        initialize 0-2).  M2_long and M2_trans default to M_sqr
+        (renormalization.cpp:17-18)."""
         m2l = self.p.m_sqr if m2_long is None else m2_long
         m2t = self.p.m_sqr if m2_trans is None else m2_trans
         ic = L.PhnIcParams(int(seed), int(justnoise), QS, scale2, amplitude, noise, (ctypes.c_double * 2)(*phi0),
                            (ctypes.c_double * 2)(*pi0), m2l, m2t)
-        L.check(self.lib.phn_initial_conditions(self.h, ctypes.byref(ic)))
+        if initialize == 3 and not withcharge:
+            L.check(self.lib.phn_initial_conditions(self.h, ctypes.byref(ic)))
+            return
+        md = L.PhnIcMode(int(initialize), int(withcharge), chi, famp, lambda_, temperature, phi0s, pi0s)
+        L.check(self.lib.phn_initial_conditions_mode(self.h, ctypes.byref(ic), ctypes.byref(md)))
 
     def apply_filter(self, r_filter: float, which: int, table=None, dp: float = 0.0):
         """apply_filter (filter.cpp:53-133): 0 top hat, 1 Gaussian, 2 table, 3 sharp cut."""

@@ -58,3 +58,37 @@ def test_gpu_initial_conditions_deterministic_and_seeded():
         with pytest.raises(L.PhnError) as e:
             lat.initial_conditions(seed=1)
         assert e.value.code == L.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("mode", [
+    dict(initialize=0, famp=0.5, lambda_=1.7, temperature=0.6, phi0s=0.9, pi0s=0.3),
+    dict(initialize=1, QS=5.0, amplitude=0.8, noise=0.4, chi=1.3, phi0s=0.9),
+    dict(initialize=2, QS=5.0, scale2=7.0, amplitude=0.8, noise=0.4, phi0s=0.9),
+    dict(initialize=4, QS=5.0, scale2=7.0, noise=0.4, temperature=0.6, phi0=(1.0, 0.5)),
+    dict(initialize=3, withcharge=1, QS=5.0, scale2=7.0, amplitude=0.8, noise=0.4, phi0=(1.0, 0.5)),
+    dict(initialize=2, withcharge=1, QS=5.0, scale2=7.0, amplitude=0.8, noise=0.4, phi0s=0.9),
+])
+def test_gpu_initial_condition_modes_match_oracle_at_48(mode):
+    """The other initialize switches and the charged stream at 48^3, Nc = 2
+    (the charged variant's paired draws), against the oracle's restatement."""
+    N = 48
+    ic = dict(seed=77, **mode)
+    pd = dict(N=N, Nc=2, theory=0, kappa=3 ** 0.5, m_sqr=0.7)
+    phi, pi = gpu_ic(pd, ic)
+    ophi, opi = O.initial_conditions(O.Params(N=N, Nc=2, kappa=3 ** 0.5, m_sqr=0.7), **ic)
+    sl = slice(2 * N * N, -2 * N * N)
+    assert np.abs(phi - ophi).max() <= 1e-12 * np.abs(ophi).max()
+    assert np.abs(pi[sl] - opi[sl]).max() <= 1e-12 * np.abs(opi[sl]).max()
+    assert np.std(ophi[sl]) > 1e-3
+
+
+def test_gpu_initial_conditions_refuse_charged_initialize_4():
+    from phinum_gb300 import lattice as PL
+    from phinum_gb300 import _lib as L
+    with PL.Lattice(PL.Params(N=8, Nc=2)) as lat:
+        with pytest.raises(L.PhnError) as e:
+            lat.initial_conditions(seed=1, initialize=4, withcharge=1)
+        assert e.value.code == L.ERR_UNSUPPORTED
+        with pytest.raises(L.PhnError) as e:
+            lat.initial_conditions(seed=1, initialize=5)
+        assert e.value.code == L.ERR_INVALID
