@@ -415,9 +415,10 @@ def measure_gpu(args, dist: Dist):
     if not args.quick:
         also["ensemble_c3"] = measure_ensemble(2000, 100)
         also["analysis"] = analysis_form(N, precisions=("fp32",))["fp32"]
-        adj = adjoint_form(128, 1000, check=False, reps_unchecked=3)
+        adj = adjoint_form(128, 1000, reps_unchecked=3, light=True)
         also["adjoint_c4_fp32"] = {k: adj[k] for k in ("cost_ratio", "forward_plain_ms", "adjoint_forward_ms",
-                                                       "adjoint_backward_ms", "timing")}
+                                                       "adjoint_backward_ms", "timing", "fp32_vs_fp64_field_rel_l2")}
+        also["adjoint_c4_fp32_pair_forward"] = adj["fp32_pair"]
     out["also"] = also
     return out
 
@@ -555,7 +556,7 @@ def precision_form(N: int, steps: int, check_step: int = 500, tso_steps: int = 5
 
 def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: float = 1e-3,
                  c6_steps=(1e-4, 1e-5, 1e-6, 1e-7), width_cfg: float = 0.1, check: bool = True,
-                 reps_unchecked: int = 1):
+                 reps_unchecked: int = 1, light: bool = False):
     """Adjoint form (config C4): phi^6, N^3, FP32, `steps` steps, checkpoints
     every `every`; J = sum rho sigmoid((rho - 2<rho>)/0.1) of the final state,
     in the configuration's units.  The kernels work in the reference's units
@@ -565,7 +566,11 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     phi^6 coupling, checked against the FP64 adjoint and against central
     finite differences of the FP64 forward (step h_fd) on `ndir` random unit
     directions; cost = (forward with checkpoints + backward) / plain forward.
-    check=False times the FP32 pair only (`reps_unchecked` timed solves)."""
+    The FP32 adjoint runs with three forwards: FP32, FP64, and FP32 pairs
+    (double-float arithmetic on the FP32 pipe).
+    check=False times the all-FP32 adjoint only (`reps_unchecked` timed
+    solves); light=True times the all-FP32 and the pair-forward adjoints and
+    compares both with one FP64 adjoint (no finite differences)."""
     from phinum_gb300 import lattice as PL
     phi, pi = make_fields(N)
     sl = slice(N * N, -N * N)
@@ -579,11 +584,17 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     res = {}
     # fp32_fwd64: the FP32 adjoint with its forward solve in FP64
     # (phn_adjoint_set_forward_precision); its plain forward is the FP64 one
-    legs = ((("fp32", 1, 5, None), ("fp64", 0, 2, None), ("fp32_fwd64", 1, 2, 0)) if check
-            else (("fp32", 1, reps_unchecked, None),))
+    if light:
+        legs = (("fp32", 1, reps_unchecked, None), ("fp32_pair", 1, reps_unchecked, 3), ("fp64", 0, 1, None))
+    elif check:
+        legs = (("fp32", 1, 5, None), ("fp64", 0, 2, None), ("fp32_fwd64", 1, 2, 0), ("fp32_pair", 1, 5, 3))
+    else:
+        legs = (("fp32", 1, reps_unchecked, None),)
     for name, prec, reps, fwd_prec in legs:
         plain = []
-        if fwd_prec is None:
+        if fwd_prec == 3:
+            plain = [res["fp32"]["plain_ms"]]  # its cost against the plain FP32 forward
+        elif fwd_prec is None:
             lat = PL.Lattice(PL.Params(N=N, precision=prec, kappa=kappa))
             for r in range(reps + 1):
                 lat.upload(phi, pi)
@@ -612,6 +623,21 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     out["adjoint_backward_ms"] = r32["backward_ms"]
     out["timing"] = ("device events; median of 5 (FP32) / 2 (FP64) solves after one warm-up solve; "
                      "adjoint = forward with checkpoints and J + backward (seed and reverse sweep)")
+    if light:
+        r64, rp = res["fp64"], res["fp32_pair"]
+        d64 = r64["dphi"][sl]
+        out["timing"] = (f"device events; median of {reps_unchecked} solve(s) after one warm-up solve; "
+                         "errors against one FP64 adjoint")
+        out["fp32_vs_fp64_field_rel_l2"] = float(np.linalg.norm(r32["dphi"][sl] - d64) / np.linalg.norm(d64))
+        out["fp32_pair"] = {
+            "what": "FP32 adjoint with its forward in FP32 pairs (double-float arithmetic on the FP32 pipe)",
+            "cost_ratio": (rp["forward_ms"] + rp["backward_ms"]) / r32["plain_ms"],
+            "adjoint_forward_ms": rp["forward_ms"], "adjoint_backward_ms": rp["backward_ms"],
+            "vs_fp64_field_rel_l2": float(np.linalg.norm(rp["dphi"][sl] - d64) / np.linalg.norm(d64)),
+            "vs_fp64_dphi0_rel": float(abs(rp["g"][0] - r64["g"][0]) / abs(r64["g"][0])),
+            "vs_fp64_dc6_rel": float(abs(rp["g"][1] - r64["g"][1]) / abs(r64["g"][1])),
+            "J_rel_to_fp64": float(abs(rp["J"] - r64["J"]) / abs(r64["J"]))}
+        return out
     if not check:
         out["timing"] = (f"device events; median of {reps_unchecked} solve(s) after one warm-up solve "
                          "(no gradient checks)")
@@ -626,6 +652,16 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     g32, g64 = res["fp32"]["g"], res["fp64"]["g"]
     out["fp32_vs_fp64_dphi0_rel"] = float(abs(g32[0] - g64[0]) / abs(g64[0]))
     out["fp32_vs_fp64_dc6_rel"] = float(abs(g32[1] - g64[1]) / abs(g64[1]))
+    rp = res["fp32_pair"]
+    dpp, gpp = rp["dphi"][sl], rp["g"]
+    out["fp32_pair"] = {
+        "what": "FP32 adjoint with its forward in FP32 pairs (double-float arithmetic on the FP32 pipe)",
+        "cost_ratio": (rp["forward_ms"] + rp["backward_ms"]) / r32["plain_ms"],
+        "adjoint_forward_ms": rp["forward_ms"], "adjoint_backward_ms": rp["backward_ms"],
+        "J_rel_to_fp64": float(abs(rp["J"] - res["fp64"]["J"]) / abs(res["fp64"]["J"])),
+        "vs_fp64_field_rel_l2": float(np.linalg.norm(dpp - d64) / np.linalg.norm(d64)),
+        "vs_fp64_dphi0_rel": float(abs(gpp[0] - g64[0]) / abs(g64[0])),
+        "vs_fp64_dc6_rel": float(abs(gpp[1] - g64[1]) / abs(g64[1]))}
     rm = res["fp32_fwd64"]
     dm, gm = rm["dphi"][sl], rm["g"]
     out["fp32_fwd64"] = {
@@ -640,7 +676,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
         "vs_fp64_dc6_rel": float(abs(gm[1] - g64[1]) / abs(g64[1]))}
     # central finite differences of the FP64 forward
     rng = np.random.default_rng(99)
-    errs64, errs32, errsm = [], [], []
+    errs64, errs32, errsm, errsp = [], [], [], []
     with PL.Adjoint(PL.Params(N=N, precision=0, kappa=kappa), steps, every, width) as adj:
         for _ in range(ndir):
             v = np.zeros_like(phi)
@@ -650,6 +686,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
             errs64.append(abs(float(np.dot(d64, v[sl])) - fd) / abs(fd))
             errs32.append(abs(float(np.dot(d32, v[sl])) - fd) / abs(fd))
             errsm.append(abs(float(np.dot(dm, v[sl])) - fd) / abs(fd))
+            errsp.append(abs(float(np.dot(dpp, v[sl])) - fd) / abs(fd))
         # the homogeneous shift moves every site at once: a far smaller step
         # keeps the central difference out of the sigmoid's curvature
         h_s = 1e-7
@@ -674,6 +711,7 @@ def adjoint_form(N: int, steps: int, every: int = 50, ndir: int = 20, h_fd: floa
     out["fp32_adjoint_vs_fd_rel_max"] = float(max(errs32))
     out["fp32_adjoint_vs_fd_rel_median"] = float(np.median(errs32))
     out["fp32_fwd64"]["vs_fd_rel_max"] = float(max(errsm))
+    out["fp32_pair"]["vs_fd_rel_max"] = float(max(errsp))
     out["dphi0"] = {"fp32": float(g32[0]), "fp64": float(g64[0]), "fd": fd_phi0}
     out["dc6"] = {"fp32": float(g32[1]), "fp64": float(g64[1]), "fd": fd_c6}
     # the configuration's units: J = J_ref / 6, phi_ref = sqrt(6) phi, c6 = g / 216

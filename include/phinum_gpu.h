@@ -46,7 +46,9 @@ enum {
 enum {
   PHN_FP64 = 0,      /* fields and arithmetic in FP64, in the reference's operation order */
   PHN_FP32 = 1,      /* fields in FP32, FP64 reductions */
-  PHN_FP32_KAHAN = 2 /* fields in FP32 with compensated (Kahan) kick and drift, FP64 reductions */
+  PHN_FP32_KAHAN = 2, /* fields in FP32 with compensated (Kahan) kick and drift, FP64 reductions */
+  PHN_FP32_PAIR = 3   /* FP32 pairs: double-float arithmetic on the FP32 pipe (about 48 bits);
+                         the adjoint's forward solve only (phn_adjoint_set_forward_precision) */
 };
 
 enum {
@@ -425,10 +427,13 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
 int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *grads);
 /* Precision of the forward solve of an FP32 adjoint: PHN_FP64 runs the
  * forward with the FP64 step kernels (FP32 checkpoints, rounded; J and the
- * seed on the FP64 final state), the reverse sweep staying FP32; PHN_FP32
- * (the default) runs both in FP32.  The gradient's sensitivity to the final
- * state through the sigmoid makes the forward's precision the one that
- * matters.  PHN_ERR_UNSUPPORTED for an FP64 adjoint or other precisions. */
+ * seed on the FP64 final state), the reverse sweep staying FP32; PHN_FP32_PAIR
+ * runs it in FP32 pairs (double-float arithmetic for the force, the
+ * increments and the updates; FP32 checkpoints; J and the seed on the pair
+ * state widened to FP64) at FP32-pipe speed; PHN_FP32 (the default) runs
+ * both in FP32.  The gradient's sensitivity to the final state through the
+ * sigmoid makes the forward's precision the one that matters.
+ * PHN_ERR_UNSUPPORTED for an FP64 adjoint or other precisions. */
 int phn_adjoint_set_forward_precision(phn_adjoint *a, int precision);
 /* J of the last forward and device times (ms) of the last forward and backward. */
 int phn_adjoint_info(const phn_adjoint *a, double *J, double *forward_ms, double *backward_ms);

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libphinum_gpu.so")
 MAX_NC = 4
 OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NOMEM, ERR_UNSUPPORTED, ERR_TRUNCATED = \
     0, -1, -2, -3, -4, -5, -6, -7
-FP64, FP32, FP32_KAHAN = 0, 1, 2
+FP64, FP32, FP32_KAHAN, FP32_PAIR = 0, 1, 2, 3
 ISLAND_REFERENCE, ISLAND_ENERGY = 0, 1
 PATH_AUTO, PATH_PLAIN, PATH_TMA, PATH_X4 = 0, 1, 2, 3
 TRACK_ALIVE, TRACK_RETIRED, TRACK_BUBBLES = 0, 1, 2

@@ -535,6 +535,12 @@ struct phn_adjoint {
   cudaGraphExec_t sweep;  // the captured reverse sweep
   bool graph_ok;
   int final_cur;          // buffer parity of the adjoint after the sweep
+  // forward in FP32 pairs (phn_adjoint_set_forward_precision(PHN_FP32_PAIR)):
+  // phi (hi, lo) double-buffered, pi (hi, lo), the final state widened to
+  // FP64 for the objective, and an FP64 reference-layout staging buffer
+  bool pair;
+  float *pph[2], *ppl[2], *pqh, *pql;
+  double *pfin, *pstage;
 };
 
 static void adj_free(phn_adjoint *a) {
@@ -552,6 +558,14 @@ static void adj_free(phn_adjoint *a) {
   cudaFree(a->sums);
   if (a->h_res) cudaFreeHost(a->h_res);
   cudaFree(a->gs);
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(a->pph[i]);
+    cudaFree(a->ppl[i]);
+  }
+  cudaFree(a->pqh);
+  cudaFree(a->pql);
+  cudaFree(a->pfin);
+  cudaFree(a->pstage);
   if (a->ev0) cudaEventDestroy(a->ev0);
   if (a->ev1) cudaEventDestroy(a->ev1);
   if (a->graph_ok) cudaGraphExecDestroy(a->sweep);
@@ -634,8 +648,71 @@ int phn_adjoint_destroy(phn_adjoint *a) {
   return PHN_OK;
 }
 
+// The forward solve in FP32 pairs: the clock of dynamics.cpp:28-50,196-213
+// on the host (the factors the handle would use), one pair step per evolve(),
+// FP32 checkpoints from the high words (the pair's rounding to FP32), and J
+// with its seed on the final state widened to FP64.
+static int forward_pair(phn_adjoint *a, const double *Phi0, const double *Pi0) {
+  phn_handle *h = a->fwd;
+  cudaStream_t st = h->stream;
+  const int N = a->p.N;
+  const size_t V = a->V, fb = V * sizeof(float), nref = (size_t)N * N * (N + 2);
+  CKA(cudaMemcpyAsync(a->pstage, Phi0, nref * sizeof(double), cudaMemcpyHostToDevice, st));
+  CKA(launch_pair_from_ref(a->pstage, a->pph[0], a->ppl[0], N, st));
+  CKA(cudaMemcpyAsync(a->pstage, Pi0, nref * sizeof(double), cudaMemcpyHostToDevice, st));
+  CKA(launch_pair_from_ref(a->pstage, a->pqh, a->pql, N, st));
+  h->launches += 2;
+  a->fk.clear();
+  a->fd.clear();
+  double tau = a->p.T0, lm = tau, lf = tau;
+  const double dtau = a->p.dt * a->p.a;
+  int cur = 0;
+  char *ck = (char *)a->ckpt;
+  CKA(cudaEventRecord(a->ev0, st));
+  CKA(cudaMemcpyAsync(ck, a->pph[0], fb, cudaMemcpyDeviceToDevice, st));
+  CKA(cudaMemcpyAsync(ck + fb, a->pqh, fb, cudaMemcpyDeviceToDevice, st));
+  for (int s = 0; s < a->nseg; ++s) {
+    for (int i = 0; i < a->every; ++i) {
+      tau += 0.5 * dtau;
+      const double fk = tau - lm;
+      lm = tau;
+      tau += 0.5 * dtau;
+      const double fd = tau - lf;
+      lf = tau;
+      a->fk.push_back(fk);
+      a->fd.push_back(fd);
+      CKA(launch_step_pair(a->k, fk, fd, a->pph[cur], a->ppl[cur], a->pqh, a->pql, a->pph[1 - cur],
+                           a->ppl[1 - cur], st));
+      cur = 1 - cur;
+    }
+    h->launches += a->every;
+    CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb, a->pph[cur], fb, cudaMemcpyDeviceToDevice, st));
+    CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb + fb, a->pqh, fb, cudaMemcpyDeviceToDevice, st));
+  }
+  CKA(launch_pair_to_f64(a->pph[cur], a->ppl[cur], a->pfin, N, st));
+  CKA(launch_pair_to_f64(a->pqh, a->pql, a->pfin + V, N, st));
+  h->launches += 2;
+  return objective<double>(a, a->pfin, a->pfin + V, st);
+}
+
 int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, double *J) {
   if (!a || !Phi0 || !Pi0) return set_error(PHN_ERR_INVALID, "NULL argument");
+  if (a->pair) {
+    int r = forward_pair(a, Phi0, Pi0);
+    if (r) return r;
+    cudaStream_t st = a->fwd->stream;
+    CKA(cudaEventRecord(a->ev1, st));
+    CKA(cudaEventSynchronize(a->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a->ev0, a->ev1);
+    a->fwd_ms = ms;
+    a->mean = a->h_res[0];
+    a->J = a->h_res[1];
+    a->S = a->h_res[2];
+    a->forward_done = true;
+    if (J) *J = a->J;
+    return PHN_OK;
+  }
   phn_handle *h = a->fwd;
   int r = phn_upload(h, Phi0, Pi0);
   if (r) return r;
@@ -764,11 +841,15 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   CKA(cudaEventRecord(a->ev0, st));
   gs_zero<<<64, 256, 0, st>>>(a->gs, (size_t)gr.nblocks * ADJ_NG);
   // adjoint of the objective, with the direct dependence of rho on the couplings
-  // (on the forward's final state: FP64 when the forward ran in FP64)
+  // (on the forward's final state: FP64 when the forward ran in FP64, the
+  // pair state widened to FP64 when it ran in pairs)
   if (dbl)
     obj_adjoint_init<double, double><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
                                                                  (double *)a->lphi[0], (double *)a->lpi[0], a->sums,
                                                                  nb);
+  else if (a->pair)
+    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>(a->pfin, a->pfin + a->V, a->g, a->k,
+                                                                (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   else if (a->fwd_elem == 8)
     obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
                                                                 (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
@@ -830,10 +911,41 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
 
 int phn_adjoint_set_forward_precision(phn_adjoint *a, int precision) {
   if (!a) return set_error(PHN_ERR_INVALID, "NULL argument");
-  const int cur = a->fwd_elem == 8 ? PHN_FP64 : PHN_FP32;
+  const int cur = a->pair ? PHN_FP32_PAIR : (a->fwd_elem == 8 ? PHN_FP64 : PHN_FP32);
   if (precision == cur) return PHN_OK;
-  if (a->p.precision != PHN_FP32 || (precision != PHN_FP64 && precision != PHN_FP32))
-    return set_error(PHN_ERR_UNSUPPORTED, "forward precision: FP64 or FP32 under an FP32 adjoint");
+  if (a->p.precision != PHN_FP32 ||
+      (precision != PHN_FP64 && precision != PHN_FP32 && precision != PHN_FP32_PAIR))
+    return set_error(PHN_ERR_UNSUPPORTED, "forward precision: FP64, FP32 or FP32 pairs under an FP32 adjoint");
+  if (precision == PHN_FP32_PAIR) {
+    // the pair forward keeps the FP32 internal handle (its stream) and adds
+    // its own buffers
+    if (a->fwd_elem == 8) {
+      const int r = phn_adjoint_set_forward_precision(a, PHN_FP32);
+      if (r) return r;
+    }
+    if (!a->pqh) {
+      const size_t fb = a->V * sizeof(float);
+      const size_t nref = (size_t)a->p.N * a->p.N * (a->p.N + 2);
+      cudaError_t e = cudaSuccess;
+      for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaMalloc(&a->pph[i], fb);
+        if (e == cudaSuccess) e = cudaMalloc(&a->ppl[i], fb);
+      }
+      if (e == cudaSuccess) e = cudaMalloc(&a->pqh, fb);
+      if (e == cudaSuccess) e = cudaMalloc(&a->pql, fb);
+      if (e == cudaSuccess) e = cudaMalloc(&a->pfin, 2 * a->V * sizeof(double));
+      if (e == cudaSuccess) e = cudaMalloc(&a->pstage, nref * sizeof(double));
+      if (e != cudaSuccess) return cuda_error(e, "pair forward buffers");
+    }
+    a->pair = true;
+    a->forward_done = false;
+    return PHN_OK;
+  }
+  a->pair = false;
+  if (precision == (a->fwd_elem == 8 ? PHN_FP64 : PHN_FP32)) {
+    a->forward_done = false;
+    return PHN_OK;
+  }
   phn_params q = a->p;
   q.precision = precision;
   phn_handle *nh = nullptr;

@@ -44,6 +44,8 @@ int phn::validate_params(const phn_params *p) {
     return set_error(PHN_ERR_UNSUPPORTED, "theory %d is provided for Nc = 1", p->potential);
   if (p->potential >= 2 && !(p->m_sqr > 0.0)) return set_error(PHN_ERR_INVALID, "theory %d needs M_sqr > 0", p->potential);
   if (p->potential == 5 && !(p->p_mono != 0.0)) return set_error(PHN_ERR_INVALID, "p_mono must be non-zero");
+  if (p->precision == PHN_FP32_PAIR)
+    return set_error(PHN_ERR_UNSUPPORTED, "FP32 pairs serve the adjoint's forward solve only");
   if (p->precision < PHN_FP64 || p->precision > PHN_FP32_KAHAN)
     return set_error(PHN_ERR_INVALID, "precision %d", p->precision);
   if (!(p->a > 0.0) || !isfinite(p->a)) return set_error(PHN_ERR_INVALID, "a must be positive");

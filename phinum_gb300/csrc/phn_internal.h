@@ -180,6 +180,13 @@ int x4_grid(const phn_params &p, int variant);
 cudaError_t launch_step_f32_x4(const Consts &k, int variant, int grid, int mode, const float *phi, float *phi_out,
                                float *pi, float *cphi, float *cpi, StepF s, double *partials, cudaStream_t st);
 
+// Leapfrog in FP32 pairs (double-float arithmetic; pair.cu), theories 0 and 1,
+// Nc = 1, static box: pi (qh, ql) updated in place, phi (ph, pl) -> (oh, ol).
+cudaError_t launch_step_pair(const Consts &k, double fk, double fd, const float *ph, const float *pl, float *qh,
+                             float *ql, float *oh, float *ol, cudaStream_t st);
+cudaError_t launch_pair_from_ref(const double *ref, float *hi, float *lo, int N, cudaStream_t st);
+cudaError_t launch_pair_to_f64(const float *hi, const float *lo, double *out, int N, cudaStream_t st);
+
 // Layout conversion between the reference layout (host order, ghosts; R =
 // double or float, the reference's pseudo_double) and the device SoA layout
 // [a][z][y][x] (layout.cu).

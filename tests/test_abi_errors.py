@@ -31,7 +31,8 @@ def create_status(L, **kw):
     (dict(N=8, theory=2, m_sqr=0.0), "ERR_INVALID"),
     (dict(N=8, theory=5, p_mono=0.0), "ERR_INVALID"),
     (dict(N=8, theory=0, kappa=0.0), "ERR_INVALID"),
-    (dict(N=8, precision=3), "ERR_INVALID"),
+    (dict(N=8, precision=3), "ERR_UNSUPPORTED"),  # FP32 pairs: the adjoint's forward only
+    (dict(N=8, precision=4), "ERR_INVALID"),
     (dict(N=8, a=0.0), "ERR_INVALID"),
     (dict(N=8, expansion=2), "ERR_INVALID"),
     (dict(N=8, expansion=1, H0=0.0), "ERR_INVALID"),

@@ -136,3 +136,67 @@ def test_fp64_forward_fp32_adjoint_within_1e4_of_fp64_adjoint():
         plain = adj.backward()
     for x, y in zip(back, plain):
         assert np.array_equal(x, y)
+
+
+def test_pair_forward_fp32_adjoint_within_1e4_of_fp64_adjoint():
+    """phn_adjoint_set_forward_precision(PHN_FP32_PAIR): the forward in FP32
+    pairs (double-float arithmetic), FP32 checkpoints and reverse sweep.  J is
+    the FP64 adjoint's to 1e-10 relative (the pair state carries ~48 bits),
+    the gradients within 1e-4 of the FP64 adjoint's; back to FP32 the plain
+    FP32 adjoint returns, bit for bit."""
+    from phinum_gb300 import lattice as PL
+    from phinum_gb300 import _lib as L
+    N, steps, every = 32, 200, 50
+    kw, phi, pi = setup(N, 23)
+    sl = slice(N * N, -N * N)
+    with PL.Adjoint(PL.Params(N=N, precision=0, **kw), steps, every) as adj:
+        J64 = adj.forward(phi, pi)
+        d64, p64, g64 = adj.backward()
+    with PL.Adjoint(PL.Params(N=N, precision=1, **kw), steps, every, forward_precision=L.FP32_PAIR) as adj:
+        Jp = adj.forward(phi, pi)
+        dp, pp, gp = adj.backward()
+        assert abs(Jp - J64) <= 1e-10 * abs(J64)
+        assert np.linalg.norm(dp[sl] - d64[sl]) <= 1e-4 * np.linalg.norm(d64[sl])
+        assert np.linalg.norm(pp[sl] - p64[sl]) <= 1e-4 * np.linalg.norm(p64[sl])
+        assert abs(gp[0] - g64[0]) <= 1e-4 * abs(g64[0])
+        assert abs(gp[1] - g64[1]) <= 1e-4 * abs(g64[1])
+        L.check(adj.lib.phn_adjoint_set_forward_precision(adj.h, 1))
+        adj.forward(phi, pi)
+        back = adj.backward()
+    with PL.Adjoint(PL.Params(N=N, precision=1, **kw), steps, every) as adj:
+        adj.forward(phi, pi)
+        plain = adj.backward()
+    for x, y in zip(back, plain):
+        assert np.array_equal(x, y)
+
+
+def test_adjoint_against_central_differences_20_directions_64():
+    """The gradient check of the adjoint configuration at 64^3 x 200 steps
+    (checkpoints every 50): central differences of the FP64 forward, step
+    h = 1e-3, along 20 seeded random unit directions of the initial phi.  The
+    FP64 adjoint agrees to 1e-5 per direction and the FP32 adjoint with its
+    forward in FP32 pairs to 1e-4; the all-FP32 adjoint's error is reported
+    beside them (its forward's FP32 rounding, amplified by the sigmoid)."""
+    from phinum_gb300 import lattice as PL
+    from phinum_gb300 import _lib as L
+    N, steps, every, h, ndir = 64, 200, 50, 1e-3, 20
+    kw, phi, pi = setup(N, 41)
+    sl = slice(N * N, -N * N)
+    grads = {}
+    for name, prec, fwd in (("fp64", 0, None), ("pair", 1, L.FP32_PAIR), ("fp32", 1, None)):
+        with PL.Adjoint(PL.Params(N=N, precision=prec, **kw), steps, every, forward_precision=fwd) as adj:
+            adj.forward(phi, pi)
+            grads[name] = adj.backward()[0][sl]
+    rng = np.random.default_rng(99)
+    err = {k: [] for k in grads}
+    with PL.Adjoint(PL.Params(N=N, precision=0, **kw), steps, every) as adj:
+        for _ in range(ndir):
+            v = np.zeros_like(phi)
+            v[sl] = rng.standard_normal(N ** 3)
+            v /= np.linalg.norm(v[sl])
+            fd = (adj.forward(phi + h * v, pi) - adj.forward(phi - h * v, pi)) / (2 * h)
+            for k, g in grads.items():
+                err[k].append(abs(float(np.dot(g, v[sl])) - fd) / abs(fd))
+    print({k: max(v) for k, v in err.items()})
+    assert max(err["fp64"]) <= 1e-5
+    assert max(err["pair"]) <= 1e-4
