@@ -881,7 +881,11 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   // fields: lam_phi(0), lam_pi(0) in the reference layout, through the
   // handle's upload/download staging buffer
   const int N = a->p.N;
-  double *ref = h->d_ref;
+  // the reference-layout staging buffer: the handle's (allocated by its
+  // upload) or, for a forward in pairs, which never uploads through the
+  // handle, the pair forward's own
+  double *ref = a->pair ? a->pstage : h->d_ref;
+  if (!ref) return set_error(PHN_ERR_INVALID, "adjoint: no staging buffer (no forward upload)");
   const size_t slab = (size_t)N * N, nref = slab * (N + 2);
   double sum_lphi = 0.0;
   std::vector<double> tmp;
