@@ -321,6 +321,15 @@ def measure_gpu(args, dist: Dist):
     lat.evolve(k_plain)
     _, ms_plain, _ = lat.stats()
     t_launch = ms_plain / 1e3 / k_plain
+    # an observed step: every step of the loop is due a row (TSO = dtau), so
+    # each costs the fused step with the averages, the fold and the row's read
+    k_obs = 50
+    lat.run_loop(k_obs, 0.02, max_rows=k_obs + 2)
+    _, ms_obs, _ = lat.stats()
+    out["observed_step"] = {"ms": ms_obs / k_obs, "plain_ms": t_launch * 1e3,
+                            "ratio": (ms_obs / k_obs) / (t_launch * 1e3),
+                            "what": "run loop with a row due every step (fused averages + fold + row read) "
+                                    "against the plain step, same kernel variant"}
     achieved = BYTES_PER_SITE[1] * sites / t_launch / 1e9
     peak, kind = peaks()
     traffic, traffic_src = traffic_from_profile(pk.value, tv.value) if N == 512 else (None, "not 512^3")
@@ -1084,7 +1093,7 @@ def main():
             "warmup": max(3, args.warmup), "ms_per_step": res["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
             "roofline": res["roofline"], "e2e": res["e2e"], "clocks": res["clocks"],
-            "gpu_launches": res["gpu_launches"], "also": res["also"],
+            "gpu_launches": res["gpu_launches"], "also": res["also"], "observed_step": res.get("observed_step"),
             "so_rows": res["rows"], "energy_drift_rel": res["energy_drift"]}
     if rank == 0 and world == 1 and not args.no_cpu:
         # like for like: the reference's float build against this FP32 line,

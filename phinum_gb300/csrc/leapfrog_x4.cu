@@ -12,8 +12,8 @@
 // operands as the other FP32 kernels, so the fields are bit-identical to
 // theirs.  Items are numbered (z chunk, plane chunk); a variant either walks
 // them with a persistent grid or launches one block per item.  Observation
-// steps always use a persistent variant (few block records to fold) and
-// per-plane FP32 partials with one compensated update per plane.
+// steps run the same variant with the moment sums of ObsX4 (one block record
+// per block).
 //
 // KAHAN: the compensated FP32 step (PHN_FP32_KAHAN) -- phi and pi carry
 // per-site compensation words (read and written as float4, never read by the
@@ -32,6 +32,141 @@ struct X4Variant {
 constexpr X4Variant kX4Variants[] = {{8, 32, true}, {8, 16, true}, {4, 32, true},
                                      {8, 16, false}, {8, 8, false}, {4, 16, false}};
 constexpr int kNumX4Variants = 6;
+
+// Observation sums of the x4 kernel (theories 0 and 1, one component).  The
+// four sites of a thread's plane row add to plain FP32 moments with FMAs --
+// sum phi, pi, phi^2, pi^2, phi pi, phi^4, phi^6 and the squared forward
+// differences -- which enter compensated per-thread totals every OBS_FOLD
+// planes; the FP64 record then takes the gradient's 1/a^2 and the
+// interaction as the linear combination of the moments that theories 0 and
+// 1 make of it (fieldanalysis.cpp:456-579: mmh phi^2 + lm phi^4/(24 Nc)
+// [+ phi^6/(720 Nc^2 Kappa^2)] [+ h phi]).  Extrema: the plane row's
+// maximum, minimum and largest |phi| first (fmaxf/fminf ignore NaN, as the
+// reference's comparisons do), and only when one reaches the running value
+// the site is located and compared by index (ties keep the smaller index).
+// Non-finite values are counted exactly, on the rare rows whose sum of 0 x
+// value is not 0.
+constexpr int OBS_FOLD = 4;
+enum { MOM_PHI, MOM_PI, MOM_PHI2, MOM_PI2, MOM_PHIPI, MOM_PHI4, MOM_PHI6, MOM_GRAD, NMOM };
+
+struct ObsX4 {
+  float part[NMOM];
+  float s[NMOM], c[NMOM];
+  int nplanes;
+  float nonfinite;
+  float maxv, minv, absv;
+  long long maxi, mini, absi;
+
+  __device__ __forceinline__ void init() {
+#pragma unroll
+    for (int j = 0; j < NMOM; ++j) part[j] = s[j] = c[j] = 0.f;
+    nplanes = 0;
+    nonfinite = 0.f;
+    maxv = -10000000.f;  // CalculateExtrema's starting values (fieldanalysis.cpp:324-325)
+    minv = 10000000.f;
+    absv = 0.f;
+    maxi = mini = absi = LLONG_MAX;
+  }
+
+  __device__ __forceinline__ void site(float c, float p, float fx, float fy, float fz) {
+    const float c2 = __fmul_rn(c, c), l2 = __fmul_rn(c2, c2);
+    part[MOM_PHI] += c;
+    part[MOM_PI] += p;
+    part[MOM_PHI2] += c2;
+    part[MOM_PI2] = fmaf(p, p, part[MOM_PI2]);
+    part[MOM_PHIPI] = fmaf(c, p, part[MOM_PHIPI]);
+    part[MOM_PHI4] += l2;
+    part[MOM_PHI6] = fmaf(l2, c2, part[MOM_PHI6]);
+    const float dx = fx - c, dy = fy - c, dz = fz - c;
+    part[MOM_GRAD] = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, part[MOM_GRAD])));
+  }
+
+  __device__ __forceinline__ void fold() {
+#pragma unroll
+    for (int j = 0; j < NMOM; ++j) {
+      const float y = __fsub_rn(part[j], c[j]);
+      const float t = __fadd_rn(s[j], y);
+      c[j] = __fsub_rn(__fsub_rn(t, s[j]), y);
+      s[j] = t;
+      part[j] = 0.f;
+    }
+    nplanes = 0;
+  }
+
+  // One plane row of four sites: v = phi, p = pi, xr = phi right of v.w,
+  // yp, zp = phi at +y, +z; kidx = reference index of v.x.
+  __device__ __forceinline__ void row(float4 v, float4 p, float xr, float4 yp, float4 zp, long long kidx) {
+    site(v.x, p.x, v.y, yp.x, zp.x);
+    site(v.y, p.y, v.z, yp.y, zp.y);
+    site(v.z, p.z, v.w, yp.z, zp.z);
+    site(v.w, p.w, xr, yp.w, zp.w);
+    row_rest(v, p, kidx);
+  }
+
+  // The row's non-finite count, extrema and fold, after its four sites.
+  __device__ __forceinline__ void row_rest(float4 v, float4 p, long long kidx) {
+    const float z0 = fmaf(v.x, 0.f, fmaf(v.y, 0.f, fmaf(v.z, 0.f, fmaf(v.w, 0.f, 0.f))));
+    const float z1 = fmaf(p.x, 0.f, fmaf(p.y, 0.f, fmaf(p.z, 0.f, fmaf(p.w, 0.f, z0))));
+    if (z1 != 0.f) {  // a NaN or an infinity in this row
+      const float a[8] = {v.x, v.y, v.z, v.w, p.x, p.y, p.z, p.w};
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (!isfinite(a[j])) nonfinite += 1.f;
+    }
+    // fmaxf / fminf return one of their operands, so the first site holding
+    // the row's extremum is one of the four
+    const float hi = fmaxf(fmaxf(v.x, v.y), fmaxf(v.z, v.w));
+    if (hi >= maxv && hi > -10000000.f) {
+      const int o = v.x == hi ? 0 : (v.y == hi ? 1 : (v.z == hi ? 2 : 3));
+      if (hi > maxv || kidx + o < maxi) {
+        maxv = hi;
+        maxi = kidx + o;
+      }
+    }
+    const float lo = fminf(fminf(v.x, v.y), fminf(v.z, v.w));
+    if (lo <= minv && lo < 10000000.f) {
+      const int o = v.x == lo ? 0 : (v.y == lo ? 1 : (v.z == lo ? 2 : 3));
+      if (lo < minv || kidx + o < mini) {
+        minv = lo;
+        mini = kidx + o;
+      }
+    }
+    const float ab = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+    if (ab >= absv && ab > 0.f) {  // sqrt(phi^2) of one component
+      const int o = fabsf(v.x) == ab ? 0 : (fabsf(v.y) == ab ? 1 : (fabsf(v.z) == ab ? 2 : 3));
+      if (ab > absv || kidx + o < absi) {
+        absv = ab;
+        absi = kidx + o;
+      }
+    }
+    if (++nplanes == OBS_FOLD) fold();
+  }
+
+  template <int THEORY>
+  __device__ void to_double(Acc &A, const Consts &k) {
+    if (nplanes) fold();
+    A.init();
+    double m[NMOM];
+#pragma unroll
+    for (int j = 0; j < NMOM; ++j) m[j] = (double)s[j] - (double)c[j];
+    A.s[S_PHI] = m[MOM_PHI];
+    A.s[S_PI] = m[MOM_PI];
+    A.s[S_PHI2] = m[MOM_PHI2];
+    A.s[S_PI2] = m[MOM_PI2];
+    A.s[S_PHIPI] = m[MOM_PHIPI];
+    A.s[S_PHI4] = m[MOM_PHI4];
+    A.s[S_PHI6] = m[MOM_PHI6];
+    A.s[S_GRAD] = m[MOM_GRAD] * k.inv_a2;
+    double inter = k.mm_half_M * m[MOM_PHI2] + (k.lm / k.c24) * m[MOM_PHI4];
+    if (THEORY == 0) inter += m[MOM_PHI6] / k.c720;
+    if (THEORY == 1) inter += k.h * m[MOM_PHI];
+    A.s[S_INTER] = inter;
+    A.s[S_NONFINITE] = (double)nonfinite;
+    if (maxi != LLONG_MAX) A.take_max((double)maxv, maxi);
+    if (mini != LLONG_MAX) A.take_min((double)minv, mini);
+    if (absi != LLONG_MAX) A.take_abs((double)absv, absi);
+  }
+};
 
 // The compensated kick and drift of one site (step_kahan's arithmetic).
 __device__ __forceinline__ void kahan_site(float fk, float fd, float f, float c, float ec, float p, float ep,
@@ -54,8 +189,8 @@ __global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const floa
   const int N = k.N, NN = N * N;
   const int tid = threadIdx.x + 32 * threadIdx.y;
   const int chunks = NN / (128 * W);
-  AccF accf;
-  if (MODE != MODE_STEP) accf.init();
+  ObsX4 obs;
+  if (MODE != MODE_STEP) obs.init();
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int zc = it / chunks, qc = it - zc * chunks;
     const int q = qc * (128 * W) + 4 * tid;  // this thread's first site in the plane
@@ -84,20 +219,20 @@ __global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const floa
       if (MODE != MODE_STEP) {
         // observables of the represented values hi - comp (neighbours: hi only)
         const long long kidx = (long long)q + (long long)(z + 1) * NN;
-        PlaneF P;
-        P.clear();
         if (KAHAN) {
-          observe_site<THEORY>(P, accf, k, __fsub_rn(c.x, ec.x), __fsub_rn(p.x, ep.x), c.y, yp.x, cp.x, kidx);
-          observe_site<THEORY>(P, accf, k, __fsub_rn(c.y, ec.y), __fsub_rn(p.y, ep.y), c.z, yp.y, cp.y, kidx + 1);
-          observe_site<THEORY>(P, accf, k, __fsub_rn(c.z, ec.z), __fsub_rn(p.z, ep.z), c.w, yp.z, cp.z, kidx + 2);
-          observe_site<THEORY>(P, accf, k, __fsub_rn(c.w, ec.w), __fsub_rn(p.w, ep.w), xp, yp.w, cp.w, kidx + 3);
+          const float4 v = make_float4(__fsub_rn(c.x, ec.x), __fsub_rn(c.y, ec.y), __fsub_rn(c.z, ec.z),
+                                       __fsub_rn(c.w, ec.w));
+          const float4 pv = make_float4(__fsub_rn(p.x, ep.x), __fsub_rn(p.y, ep.y), __fsub_rn(p.z, ep.z),
+                                        __fsub_rn(p.w, ep.w));
+          // forward x neighbours of the hi words, as the other kernels take them
+          obs.site(v.x, pv.x, c.y, yp.x, cp.x);
+          obs.site(v.y, pv.y, c.z, yp.y, cp.y);
+          obs.site(v.z, pv.z, c.w, yp.z, cp.z);
+          obs.site(v.w, pv.w, xp, yp.w, cp.w);
+          obs.row_rest(v, pv, kidx);
         } else {
-          observe_site<THEORY>(P, accf, k, c.x, p.x, c.y, yp.x, cp.x, kidx);
-          observe_site<THEORY>(P, accf, k, c.y, p.y, c.z, yp.y, cp.y, kidx + 1);
-          observe_site<THEORY>(P, accf, k, c.z, p.z, c.w, yp.z, cp.z, kidx + 2);
-          observe_site<THEORY>(P, accf, k, c.w, p.w, xp, yp.w, cp.w, kidx + 3);
+          obs.row(c, p, xp, yp, cp, kidx);
         }
-        flush_plane(accf, P);
       }
       if (MODE != MODE_OBS) {
         if (KAHAN) {
@@ -136,7 +271,7 @@ __global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const floa
   if (MODE != MODE_STEP) {
     // one record per block, whatever the number of items it walked
     Acc acc;
-    accf.to_double(acc);
+    obs.to_double<THEORY>(acc, k);
     block_store_n(acc, partials, tid, W, (size_t)blockIdx.x);
   }
 }
@@ -148,12 +283,10 @@ bool x4_supported(const phn_params &p) {
 
 int x4_num_variants() { return kNumX4Variants; }
 
-int x4_obs_variant(int variant) {
-  if (kX4Variants[variant].persistent) return variant;
-  for (int v = 0; v < kNumX4Variants; ++v)
-    if (kX4Variants[v].persistent && kX4Variants[v].w == kX4Variants[variant].w) return v;
-  return 0;
-}
+// Observation steps run the plain step's own variant: with the moment sums
+// a block record costs little, so a one-block-per-item grid folds its
+// (many) records in finalize_averages without a persistent grid.
+int x4_obs_variant(int variant) { return variant; }
 
 static int x4_items(int N, const X4Variant &v) {
   const int cz = v.cz < N ? v.cz : N;

@@ -281,7 +281,7 @@ __device__ __forceinline__ void flush_plane(AccF &A, PlaneF &P) {
   P.clear();
 }
 
-constexpr int FIN_THREADS = 128;
+constexpr int FIN_THREADS = 256;  // sh[FIN_THREADS][REC] doubles: the 48 KB of static shared memory
 
 // Folds block records [b0, b1) in a fixed order with one block of FIN_THREADS
 // threads and forms the reference's derived quantities
@@ -293,10 +293,15 @@ __device__ __forceinline__ void fold_records(const double *__restrict__ partials
   const int t = threadIdx.x;
   Acc a;
   a.init();
-  for (int b = b0 + t; b < b1; b += FIN_THREADS) {
-    Acc o;
+  // two records per round, loaded before either is combined (the loads of a
+  // round overlap); combined in record order
+  for (int b = b0 + t; b < b1; b += 2 * FIN_THREADS) {
+    Acc o, o2;
     load_rec(o, partials + (size_t)b * REC);
+    const bool two = b + FIN_THREADS < b1;
+    if (two) load_rec(o2, partials + (size_t)(b + FIN_THREADS) * REC);
     combine(a, o);
+    if (two) combine(a, o2);
   }
   store_rec(sh[t], a);
   __syncthreads();
