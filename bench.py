@@ -1035,7 +1035,7 @@ def main():
         print(json.dumps(precision_form(args.n, max(args.steps, 500))))
         return
     if args.form == "adjoint":
-        kw = dict(check=False) if args.quick else {}
+        kw = dict(light=True, reps_unchecked=1) if args.quick else {}
         print(json.dumps(adjoint_form(args.n, args.steps, **kw)))
         return
     if args.form == "io":

@@ -541,6 +541,8 @@ struct phn_adjoint {
   bool pair;
   float *pph[2], *ppl[2], *pqh, *pql;
   double *pfin, *pstage;
+  cudaGraphExec_t pgraph;  // the pair forward's steps and checkpoints, captured once
+  bool pgraph_ok;
 };
 
 static void adj_free(phn_adjoint *a) {
@@ -566,6 +568,7 @@ static void adj_free(phn_adjoint *a) {
   cudaFree(a->pql);
   cudaFree(a->pfin);
   cudaFree(a->pstage);
+  if (a->pgraph_ok) cudaGraphExecDestroy(a->pgraph);
   if (a->ev0) cudaEventDestroy(a->ev0);
   if (a->ev1) cudaEventDestroy(a->ev1);
   if (a->graph_ok) cudaGraphExecDestroy(a->sweep);
@@ -662,36 +665,54 @@ static int forward_pair(phn_adjoint *a, const double *Phi0, const double *Pi0) {
   CKA(cudaMemcpyAsync(a->pstage, Pi0, nref * sizeof(double), cudaMemcpyHostToDevice, st));
   CKA(launch_pair_from_ref(a->pstage, a->pqh, a->pql, N, st));
   h->launches += 2;
-  a->fk.clear();
-  a->fd.clear();
-  double tau = a->p.T0, lm = tau, lf = tau;
-  const double dtau = a->p.dt * a->p.a;
-  int cur = 0;
-  char *ck = (char *)a->ckpt;
-  CKA(cudaEventRecord(a->ev0, st));
-  CKA(cudaMemcpyAsync(ck, a->pph[0], fb, cudaMemcpyDeviceToDevice, st));
-  CKA(cudaMemcpyAsync(ck + fb, a->pqh, fb, cudaMemcpyDeviceToDevice, st));
-  for (int s = 0; s < a->nseg; ++s) {
-    for (int i = 0; i < a->every; ++i) {
-      tau += 0.5 * dtau;
-      const double fk = tau - lm;
-      lm = tau;
-      tau += 0.5 * dtau;
-      const double fd = tau - lf;
-      lf = tau;
-      a->fk.push_back(fk);
-      a->fd.push_back(fd);
-      CKA(launch_step_pair(a->k, fk, fd, a->pph[cur], a->ppl[cur], a->pqh, a->pql, a->pph[1 - cur],
-                           a->ppl[1 - cur], st));
-      cur = 1 - cur;
+  // The steps and the checkpoint copies depend only on the buffers and the
+  // clock factors (the same for every forward from reset()): captured once as
+  // a CUDA graph, replayed per forward.
+  if (!a->pgraph_ok) {
+    a->fk.clear();
+    a->fd.clear();
+    double tau = a->p.T0, lm = tau, lf = tau;
+    const double dtau = a->p.dt * a->p.a;
+    int cur = 0;
+    char *ck = (char *)a->ckpt;
+    CKA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = cudaMemcpyAsync(ck, a->pph[0], fb, cudaMemcpyDeviceToDevice, st);
+    if (le == cudaSuccess) le = cudaMemcpyAsync(ck + fb, a->pqh, fb, cudaMemcpyDeviceToDevice, st);
+    for (int s = 0; s < a->nseg && le == cudaSuccess; ++s) {
+      for (int i = 0; i < a->every && le == cudaSuccess; ++i) {
+        tau += 0.5 * dtau;
+        const double fk = tau - lm;
+        lm = tau;
+        tau += 0.5 * dtau;
+        const double fd = tau - lf;
+        lf = tau;
+        a->fk.push_back(fk);
+        a->fd.push_back(fd);
+        le = launch_step_pair(a->k, fk, fd, a->pph[cur], a->ppl[cur], a->pqh, a->pql, a->pph[1 - cur],
+                              a->ppl[1 - cur], st);
+        cur = 1 - cur;
+      }
+      if (le == cudaSuccess)
+        le = cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb, a->pph[cur], fb, cudaMemcpyDeviceToDevice, st);
+      if (le == cudaSuccess)
+        le = cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb + fb, a->pqh, fb, cudaMemcpyDeviceToDevice, st);
     }
-    h->launches += a->every;
-    CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb, a->pph[cur], fb, cudaMemcpyDeviceToDevice, st));
-    CKA(cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb + fb, a->pqh, fb, cudaMemcpyDeviceToDevice, st));
+    if (le == cudaSuccess) le = launch_pair_to_f64(a->pph[cur], a->ppl[cur], a->pfin, N, st);
+    if (le == cudaSuccess) le = launch_pair_to_f64(a->pqh, a->pql, a->pfin + V, N, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return cuda_error(le != cudaSuccess ? le : ce, "pair forward capture");
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&a->pgraph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return cuda_error(ie, "cudaGraphInstantiate (pair forward)");
+    a->pgraph_ok = true;
   }
-  CKA(launch_pair_to_f64(a->pph[cur], a->ppl[cur], a->pfin, N, st));
-  CKA(launch_pair_to_f64(a->pqh, a->pql, a->pfin + V, N, st));
-  h->launches += 2;
+  CKA(cudaEventRecord(a->ev0, st));
+  CKA(cudaGraphLaunch(a->pgraph, st));
+  h->launches += a->nsteps + 2;
   return objective<double>(a, a->pfin, a->pfin + V, st);
 }
 
