@@ -62,7 +62,7 @@ typedef struct phn_params {
   int Nc;          /* field components, 1..PHN_MAX_NC */
   int potential;   /* the reference's `theory` (parameters.cpp:86-170): 0 phi^4 + phi^6 (Kappa),
                       1 phi^4 + linear h, 2 cosine, 3 cosine + monodromy mass,
-                      4 cubic (g), 5 power-law monodromy (p_mono); 2-5 with Nc = 1.
+                      4 cubic (g), 5 power-law monodromy (p_mono); every theory for Nc 1-4.
                       Named apart because the reference #defines `theory` in the
                       translation unit that includes this */
   int mass_mode;   /* Mass_Mode */

@@ -40,8 +40,6 @@ int phn::validate_params(const phn_params *p) {
   if (p->N < 2 || p->N > 2048) return set_error(PHN_ERR_INVALID, "N=%d outside [2, 2048]", p->N);
   if (p->Nc < 1 || p->Nc > PHN_MAX_NC) return set_error(PHN_ERR_UNSUPPORTED, "Nc=%d outside [1, %d]", p->Nc, PHN_MAX_NC);
   if (p->potential < 0 || p->potential > 5) return set_error(PHN_ERR_INVALID, "theory %d", p->potential);
-  if (p->potential >= 2 && p->Nc != 1)
-    return set_error(PHN_ERR_UNSUPPORTED, "theory %d is provided for Nc = 1", p->potential);
   if (p->potential >= 2 && !(p->m_sqr > 0.0)) return set_error(PHN_ERR_INVALID, "theory %d needs M_sqr > 0", p->potential);
   if (p->potential == 5 && !(p->p_mono != 0.0)) return set_error(PHN_ERR_INVALID, "p_mono must be non-zero");
   if (p->precision == PHN_FP32_PAIR)

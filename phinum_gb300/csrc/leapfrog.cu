@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(THREADS) step_f32(const float *__restrict__ ph
           // the shared neighbour-difference Laplacian: the TMA kernel computes the same bits
           const float lap = lap_diff_f32(c[a], fxm[a], fxp[a], fym[a], fyp[a], cm[a], cp[a], k.inv_a2_f);
           float f;
-          if (NC == 1) {
+          if (NC == 1 || THEORY >= 2) {  // theories 2-5 take the component sum l as well
             f = force_f32<THEORY>(k, lap, c[a], l);
           } else {
             f = fmaf(-coef, c[a], lap);
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(THREADS) step_kahan(const float *__restrict__ 
           // the shared neighbour-difference Laplacian: the TMA kernel computes the same bits
           const float lap = lap_diff_f32(c[a], fxm[a], fxp[a], fym[a], fyp[a], cm[a], cp[a], k.inv_a2_f);
           float f;
-          if (NC == 1) {
+          if (NC == 1 || THEORY >= 2) {  // theories 2-5 take the component sum l as well
             f = force_f32<THEORY>(k, lap, c[a], l);
           } else {
             f = fmaf(-coef, c[a], lap);
@@ -348,18 +348,16 @@ Grid lattice_grid(int N) {
   if ((THV) == 0) { constexpr int TH_ = 0; __VA_ARGS__; }      \
   else { constexpr int TH_ = 1; __VA_ARGS__; }
 
-// Theories 0 and 1 for every component count; theories 2-5 with Nc = 1.
-#define PHN_DISPATCH_NC_TH(NCV, THV, ...)                                          \
-  if ((THV) <= 1) {                                                                \
-    PHN_DISPATCH_NC(NCV, PHN_DISPATCH_TH(THV, __VA_ARGS__));                       \
-  } else {                                                                         \
-    if ((NCV) != 1) return cudaErrorInvalidValue;                                  \
-    constexpr int NC_ = 1;                                                         \
-    if ((THV) == 2) { constexpr int TH_ = 2; __VA_ARGS__; }                        \
-    else if ((THV) == 3) { constexpr int TH_ = 3; __VA_ARGS__; }                   \
-    else if ((THV) == 4) { constexpr int TH_ = 4; __VA_ARGS__; }                   \
-    else { constexpr int TH_ = 5; __VA_ARGS__; }                                   \
-  }
+// Every theory for every component count.
+#define PHN_DISPATCH_TH6(THV, ...)                                                 \
+  if ((THV) == 0) { constexpr int TH_ = 0; __VA_ARGS__; }                          \
+  else if ((THV) == 1) { constexpr int TH_ = 1; __VA_ARGS__; }                     \
+  else if ((THV) == 2) { constexpr int TH_ = 2; __VA_ARGS__; }                     \
+  else if ((THV) == 3) { constexpr int TH_ = 3; __VA_ARGS__; }                     \
+  else if ((THV) == 4) { constexpr int TH_ = 4; __VA_ARGS__; }                     \
+  else { constexpr int TH_ = 5; __VA_ARGS__; }
+
+#define PHN_DISPATCH_NC_TH(NCV, THV, ...) PHN_DISPATCH_NC(NCV, PHN_DISPATCH_TH6(THV, __VA_ARGS__))
 
 #define PHN_DISPATCH_MODE(MV, ...)                             \
   if ((MV) == MODE_STEP) { constexpr int MD_ = MODE_STEP; __VA_ARGS__; }          \

@@ -118,9 +118,10 @@ template <int NC, int THEORY>
 __device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c, const double *p,
                                         const double *fxp, const double *fyp, const double *fzp,
                                         long long kidx) {
-  double l = 0.0, inter = 0.0;
+  double l = 0.0, inter = 0.0, lphi = 0.0;  // locPhiSqr, Interaction, locPhi (fieldanalysis.cpp:434-443)
 #pragma unroll
   for (int a = 0; a < NC; ++a) {
+    lphi = __dadd_rn(lphi, c[a]);
     A.s[S_PHI + a] += c[a];
     A.s[S_PI + a] += p[a];
     const double c2 = __dmul_rn(c[a], c[a]);
@@ -144,7 +145,7 @@ __device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c
   const double l2 = __dmul_rn(l, l);
   A.s[S_PHI4] += l2;
   A.s[S_PHI6] += __dmul_rn(l2, l);
-  // per-site terms (fieldanalysis.cpp:565-617); theories 2-5 have Nc = 1
+  // per-site terms (fieldanalysis.cpp:565-617)
   if (THEORY == 0) {
     inter += __dadd_rn(__dmul_rn(k.lm, div_by_near(k, l2, k.c24, k.r_c24)), div_by(k, __dmul_rn(l2, l), k.c720, k.r_c720, k.l_c720));
   } else if (THEORY == 1) {
@@ -154,7 +155,7 @@ __device__ __forceinline__ void observe(Acc &A, const Consts &k, const double *c
                                    : __dsqrt_rn(div_by(k, l, k.msq, k.r_msq, k.l_msq));
     inter += __dmul_rn(k.msq2, __dsub_rn(1., cos(arg)));
   } else if (THEORY == 4) {
-    inter += __dadd_rn(__dmul_rn(__dmul_rn(-k.g, c[0]), l) / 6.0, __dmul_rn(k.lm, div_by_near(k, l2, k.c24, k.r_c24)));
+    inter += __dadd_rn(__dmul_rn(__dmul_rn(-k.g, lphi), l) / 6.0, __dmul_rn(k.lm, div_by_near(k, l2, k.c24, k.r_c24)));
   } else {
     const double u = k.expansion ? div_by(k, div_by(k, div_by(k, l, k.msq, k.r_msq, k.l_msq), k.sf, k.r_sf, k.l_sf), k.sf, k.r_sf, k.l_sf)
                                  : div_by(k, l, k.msq, k.r_msq, k.l_msq);
@@ -200,9 +201,10 @@ struct AccF {
 template <int NC, int THEORY>
 __device__ __forceinline__ void observe_f32(AccF &A, const Consts &k, const float *c, const float *p,
                                             const float *fxp, const float *fyp, const float *fzp, long long kidx) {
-  float l = 0.f, inter = 0.f;
+  float l = 0.f, inter = 0.f, lphi = 0.f;
 #pragma unroll
   for (int a = 0; a < NC; ++a) {
+    lphi += c[a];
     A.add(S_PHI + a, c[a]);
     A.add(S_PI + a, p[a]);
     const float c2 = c[a] * c[a];
@@ -229,7 +231,7 @@ __device__ __forceinline__ void observe_f32(AccF &A, const Consts &k, const floa
   if (THEORY == 0 || THEORY == 1 || THEORY == 4) inter = fmaf(k.e4_f, l2, inter);
   if (THEORY == 0) inter = fmaf(k.e6_f, l2 * l, inter);
   if (THEORY == 2 || THEORY == 3) inter = fmaf(k.msq2_f, 1.f - cosf(sqrtf(l * k.inv_m_f)), inter);
-  if (THEORY == 4) inter = fmaf(-k.g6_f * c[0], l, inter);
+  if (THEORY == 4) inter = fmaf(-k.g6_f * lphi, l, inter);
   if (THEORY == 5) inter = fmaf(k.t5c_f, powf(fmaf(l, k.inv_m_f, 1.f), k.p_f) - 1.f, inter);
   A.add(S_INTER, inter);
   const float r = sqrtf(l);

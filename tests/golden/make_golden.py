@@ -62,6 +62,13 @@ CASES = {
     # three and four field components (O(3) and O(4) models)
     "t0_n8_nc3": (dict(N=8, Nc=3, **PHI6), 38, SQRT6, 100, 0.25, True, (1, 100)),
     "t1_n12_nc4": (dict(N=12, Nc=4, **TDW), 39, -SQRT6, 100, 0.25, True, (1, 100)),
+    # theories 2-5 with several components (their forces and averages use the
+    # component sums locPhiSqr and, for theory 4, locPhi)
+    "t2_n8_nc2": (dict(N=8, Nc=2, **COS), 41, 1.5, 100, 0.25, True, (1, 10, 100)),
+    "t3_n8_nc3": (dict(N=8, Nc=3, **MONO), 42, 2.0, 100, 0.25, True, (1, 100)),
+    "t4_n8_nc2": (dict(N=8, Nc=2, **CUBIC), 43, 1.0, 100, 0.25, True, (1, 10, 100)),
+    "t5_n8_nc4": (dict(N=8, Nc=4, **POWER), 44, 2.0, 100, 0.25, True, (1, 100)),
+    "e4_n8_nc2": (dict(N=8, Nc=2, **CUBIC, **EXP), 45, 1.0, 100, 0.25, True, (1, 100)),
     # the radiation-era expanding box (expansion 1) at the reference's H_0
     "e0_n12": (dict(N=12, Nc=1, **PHI6, **EXP), 31, SQRT6, 300, 0.5, True, (1, 100, 300)),
     "e0_n8_nc2": (dict(N=8, Nc=2, **PHI6, **EXP), 32, SQRT6, 100, 0.25, True, (1, 100)),

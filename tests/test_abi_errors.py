@@ -27,7 +27,6 @@ def create_status(L, **kw):
     (dict(N=4096), "ERR_INVALID"),
     (dict(N=8, Nc=9), "ERR_UNSUPPORTED"),
     (dict(N=8, theory=6), "ERR_INVALID"),
-    (dict(N=8, theory=3, Nc=2), "ERR_UNSUPPORTED"),
     (dict(N=8, theory=2, m_sqr=0.0), "ERR_INVALID"),
     (dict(N=8, theory=5, p_mono=0.0), "ERR_INVALID"),
     (dict(N=8, theory=0, kappa=0.0), "ERR_INVALID"),

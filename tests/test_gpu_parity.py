@@ -108,7 +108,7 @@ def test_fp64_run_loop_rows(name):
 
 @pytest.mark.parametrize("precision,atol", [(1, 2e-4), (2, 2e-5)])
 @pytest.mark.parametrize("name", ["t0_n8", "t1_n8", "t0_n12", "t0_n16_nc2", "t0_n8_nc3", "t1_n12_nc4", "t2_n8", "t3_n8",
-                                  "t4_n8", "t5_n8"])
+                                  "t4_n8", "t5_n8", "t2_n8_nc2", "t3_n8_nc3", "t4_n8_nc2", "t5_n8_nc4"])
 def test_fp32_fields_close(name, precision, atol):
     d = fixtures.load(name)
     lat, p = start(d, precision)
@@ -239,9 +239,6 @@ def test_errors_are_status_codes():
     from phinum_gb300 import _lib as L
     with pytest.raises(L.PhnError) as e:
         PL.Lattice(PL.Params(N=8, Nc=9))
-    assert e.value.code == L.ERR_UNSUPPORTED
-    with pytest.raises(L.PhnError) as e:
-        PL.Lattice(PL.Params(N=8, Nc=2, theory=3))  # theories 2-5: Nc = 1
     assert e.value.code == L.ERR_UNSUPPORTED
     with pytest.raises(L.PhnError) as e:
         PL.Lattice(PL.Params(N=8, theory=6))
