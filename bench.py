@@ -919,6 +919,7 @@ def analysis_form(N: int, reps: int = 5, steps: int = 200, precisions=("fp32", "
         n_rho = lat.full_analysis(rho_thr, mode=L.ISLAND_ENERGY, z_periodic=True, labels=False,
                                   max_out=1 << 23)[1].shape[0]
         ms_isl, isl = timed(lambda: lat.full_analysis(thr, labels=False, max_out=n_isl))
+        ms_isl_dev, _ = timed(lambda: lat.full_analysis_device(thr))
         ms_rho, rho = timed(lambda: lat.full_analysis(rho_thr, mode=L.ISLAND_ENERGY, z_periodic=True, labels=False,
                                                       max_out=n_rho))
         elem = 8 if prec == L.FP32 else 16  # complex bytes
@@ -927,6 +928,7 @@ def analysis_form(N: int, reps: int = 5, steps: int = 200, precisions=("fp32", "
                      "spectrum_uniform64_ms": ms_uni,
                      "spectrum_halfspectra_bytes": 2 * half,
                      "islands_reference_mask_ms": ms_isl, "islands_reference_mask_count": int(isl[1].shape[0]),
+                     "islands_reference_mask_device_records_ms": ms_isl_dev,
                      "islands_reference_mask_sites": int(isl[1][:, 1].sum()),
                      "islands_energy_mask_ms": ms_rho, "islands_energy_mask_count": int(rho[1].shape[0]),
                      "islands_energy_mask_sites": int(rho[1][:, 1].sum()),

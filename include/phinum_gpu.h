@@ -262,6 +262,15 @@ int phn_write_config_file(const char *path, const double *Phi, const double *Pi,
                           int nthreads);
 int phn_read_config_file(const char *path, double *Phi, double *Pi, int N, int Nc, int nthreads);
 
+/* phn_islands without the host copies: every island's record is assembled
+ * in a device buffer held by the handle, *d_records points at it (NULL when
+ * there is no island) and *n_islands receives the count.  The records stay
+ * valid until the next island call on the handle or its destruction; the
+ * labels stay on the device for phn_islands_lookup.  The same records as
+ * phn_islands writes, for callers that consume them on the GPU. */
+int phn_islands_device(phn_handle *h, double thres, int mode, int z_periodic, const phn_island **d_records,
+                       int *n_islands);
+
 /* After phn_islands: the island (numbered as phn_islands numbers them) that
  * holds each queried site, reference-layout indices; -1 outside the mask. */
 int phn_islands_lookup(phn_handle *h, const long long *pos, int n, int *island);

@@ -114,6 +114,7 @@ _SIGS = {
     "phn_tracker_oscillons": (_I, [ctypes.c_void_p, _I, _D, _D, _PD]),
     "phn_tracker_add_stat": (_I, [ctypes.c_void_p, _D, _D, _PI, _PI]),
     "phn_islands": (_I, [ctypes.c_void_p, _D, _I, _I, _PI, _PD, _I, _PI]),
+    "phn_islands_device": (_I, [ctypes.c_void_p, _D, _I, _I, ctypes.POINTER(ctypes.c_void_p), _PI]),
     "phn_set_path": (_I, [ctypes.c_void_p, _I]),
     "phn_get_path": (_I, [ctypes.c_void_p, _PI]),
     "phn_autotune": (_I, [ctypes.c_void_p, _I, _PI, _PD]),

@@ -1,25 +1,31 @@
 // Island detection as connected-component labelling on the GPU.
 //
 // Replaces is_island + BFS + the seeding scan of Full_Analysis
-// (islands.cpp:72-279, 778-840) for a first analysis (empty island history):
-//   1. mask + init: -1 for sites off the mask; a mask site points at the
-//      first site of its run of mask sites along x within its 32-site warp
-//      segment (the x links inside a segment cost no union);
-//   2. merge: every mask site unites with its -x (where init did not link
-//      it), -y (periodic) and -z (open as on one rank, islands.cpp:224-236, or
-//      periodic) mask neighbours, hooking the larger root under the smaller
-//      by atomicCAS; a y or z union is skipped where the -x sites of both
-//      ends are on the mask too (those two are joined already, so are these).
-//      Edges that are multiples of 32 run steps 1-2 per 32 x 8 x 8 tile in
-//      shared memory (ccl_tile), then unite across tile faces (ccl_border);
-//   3. compress: parent[i] = root(i).  Links always point to smaller indices,
-//      so each root is the smallest site index of its island;
-//   4. number: islands are numbered by their root in increasing index order,
+// (islands.cpp:72-279, 778-840) for a first analysis (empty island history).
+// Edges that are multiples of 32 (x) and 8 (y, z) take the tiled labelling:
+//   1. ccl_tile: per 32 x 8 x 8 tile in shared memory, the mask, x-runs
+//      linked by ballot and the -y/-z unions (union-find on tile-local
+//      indices); every mask site links to its tile root, and the tile roots
+//      are marked in a bit per site;
+//   2. ccl_border_tiles: unions across tile faces only, each hooking the
+//      larger root under the smaller by atomicCAS; a y or z union is skipped
+//      where the -x sites of both ends are on the mask too (those two are
+//      joined already, so are these);
+//   3. ccl_resolve: each tile root's final root, root bits and counts.  Links
+//      always point to smaller indices, so each root is the smallest site
+//      index of its island;
+// other edges link every site in global memory: ccl_init (mask, x-runs
+// inside 32-site warp segments), ccl_merge (the unions, same skip rule),
+// ccl_compress (parent = root, root bits), ccl_count_bits.  Then
+//   4. ccl_number: islands numbered by their root in increasing index order,
 //      which is the order in which the reference's linear scan seeds BFS, so
-//      the labels equal the reference's b[] labels;
+//      the labels equal the reference's b[] labels; tile roots take their
+//      root's number (ccl_troot_ids), so ids[parent[i]] is the island of
+//      every mask site;
 //   5. statistics per island (size, energies, <phi>, peak): runs reduced in
 //      the warp, merged per block in shared memory, then added to the FP64
-//      per-island sums once per island per block; 6. the records.
+//      per-island sums once per island per block (ccl_stats4, four sites per
+//      lane; ccl_stats for edges that are not a multiple of 4); 6. records.
 // Every loop terminates: a root search follows strictly decreasing indices,
 // and a union retry strictly decreases the larger root.
 #include <math.h>
@@ -37,9 +43,12 @@ constexpr int CCL_THREADS = 256;
 
 struct IslState {
   int *parent;     // [V]
-  int *ids;        // [V] island id of each root
-  int *blk;        // [nblk] roots per block, then exclusive offsets; [ntile]
-                   // the same per tile of SCAN_TILE blocks; [1] the total
+  int *ids;        // [V] island id of each root (and, tiled, of each tile root)
+  unsigned *tbits; // [W] tile roots, one bit per site (tiled labelling)
+  unsigned *bits;  // [W] roots, one bit per site
+  int *blk;        // [nblk] roots per block of CCL_THREADS words, then exclusive
+                   // offsets; [ntile] the same per tile of SCAN_TILE blocks; [1] the total
+  size_t W;        // 32-site words
   int nblk, ntile;
   // per-island arrays, grown on demand
   int cap;
@@ -310,7 +319,7 @@ __global__ void ccl_merge(int *__restrict__ parent, int N, const DivN dn, int zp
 // block labels a TILE_X x TILE_Y x TILE_Z tile in shared memory first (the
 // same union-find on tile-local indices, whose order is the sites' index
 // order, with the same skip rule), writes each mask site's link to the
-// global index of its tile root, and ccl_border then unites across tile
+// global index of its tile root, and ccl_border_tiles then unites across tile
 // faces only: the -x union at lx = 0, -y at ly = 0, -z at lz = 0 (the skip
 // rule needs the -x pair, which lies on the same face).  Shared-memory
 // unions replace most global root searches.
@@ -354,24 +363,50 @@ template <typename T, bool KAHAN>
 __global__ void __launch_bounds__(TILE_X *TILE_Y) ccl_tile(const T *__restrict__ phi, const float *__restrict__ cphi,
                                                          const T *__restrict__ pi, const float *__restrict__ cpi,
                                                          int N, int mode, double thr, float thr_lo, float thr_hi,
-                                                         const Consts k, int *__restrict__ parent) {
+                                                         const Consts k, int *__restrict__ parent,
+                                                         unsigned *__restrict__ tbits) {
   static_assert(TILE_X == 32, "a tile row is one warp");
   __shared__ int lp[TILE_SITES];
   const int lx = threadIdx.x, ly = threadIdx.y;
   const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y, z0 = blockIdx.z * TILE_Z;
   const int x = x0 + lx, y = y0 + ly;
   const size_t NN = (size_t)N * N;
+  // the mask of the thread's TILE_Z sites, their loads issued together
+  bool mk[TILE_Z];
+  bool done = false;
+  if constexpr (std::is_same<T, float>::value && !KAHAN) {
+    if (mode == PHN_ISLAND_REFERENCE) {
+      float cf[TILE_Z], pf[TILE_Z];
+#pragma unroll
+      for (int lz = 0; lz < TILE_Z; ++lz) {
+        const size_t i = (size_t)(z0 + lz) * NN + (size_t)y * N + x;
+        cf[lz] = phi[i];
+        pf[lz] = pi[i];
+      }
+#pragma unroll
+      for (int lz = 0; lz < TILE_Z; ++lz) {
+        const int d = ref_mask_f32(cf[lz], pf[lz], thr_lo, thr_hi);
+        mk[lz] = d >= 0 ? d == 1 : ref_mask_f64(cf[lz], pf[lz], thr);
+      }
+      done = true;
+    }
+  }
+  if (!done) {
+#pragma unroll
+    for (int lz = 0; lz < TILE_Z; ++lz) {
+      const size_t i = (size_t)(z0 + lz) * NN + (size_t)y * N + x;
+      mk[lz] = site_mask<T, KAHAN>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, i, x, y, z0 + lz);
+    }
+  }
   // a warp is one tile row: x-runs link to their first site by ballot, as
   // in ccl_init (the tile row starts the segment, so lx = 0 links nowhere)
   const unsigned full = 0xffffffffu;
-#pragma unroll 1
+#pragma unroll
   for (int lz = 0; lz < TILE_Z; ++lz) {
     const int s = (lz * TILE_Y + ly) * TILE_X + lx;
-    const size_t i = (size_t)(z0 + lz) * NN + (size_t)y * N + x;
-    const bool m = site_mask<T, KAHAN>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, i, x, y, z0 + lz);
-    const unsigned mb = __ballot_sync(full, m);
+    const unsigned mb = __ballot_sync(full, mk[lz]);
     const unsigned heads = mb & ~(mb << 1);
-    lp[s] = m ? s - lx + (31 - __clz(heads & (full >> (31 - lx)))) : -1;
+    lp[s] = mk[lz] ? s - lx + (31 - __clz(heads & (full >> (31 - lx)))) : -1;
   }
   __syncthreads();
 #pragma unroll 1
@@ -389,48 +424,100 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) ccl_tile(const T *__restrict__
     }
   }
   __syncthreads();
-#pragma unroll 1
+  // each mask site links to its tile root's global index; the tile roots'
+  // bits (one 32-bit word per tile row: N is a multiple of 32) let the
+  // later passes visit the roots only
+#pragma unroll
   for (int lz = 0; lz < TILE_Z; ++lz) {
     const int s = (lz * TILE_Y + ly) * TILE_X + lx;
     const size_t i = (size_t)(z0 + lz) * NN + (size_t)y * N + x;
     int g = -1;
-    if (lp[s] >= 0) {
+    const int l = lp[s];
+    if (l >= 0) {
       const int r = find_root_sh_ro(lp, s);
       const int rz = r / (TILE_X * TILE_Y), ry = (r / TILE_X) % TILE_Y, rx = r % TILE_X;
       g = (int)((size_t)(z0 + rz) * NN + (size_t)(y0 + ry) * N + (x0 + rx));
     }
     parent[i] = g;
+    const unsigned tb = __ballot_sync(full, l == s);
+    if (lx == 0) tbits[i >> 5] = tb;
   }
 }
 
-// Unions across tile faces (see ccl_tile); one thread per site, sites off
-// the faces return at once.
-__global__ void ccl_border(int *__restrict__ parent, int N, const DivN dn, int zper) {
-  const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    int x, y, z;
-    site_xyz(dn, N, i, x, y, z);
-    const bool fx = (x % TILE_X) == 0, fy = (y % TILE_Y) == 0, fz = (z % TILE_Z) == 0 && (z > 0 || zper);
-    if (!(fx || fy || fz)) continue;
-    if (parent[i] < 0) continue;
-    const bool left = x > 0 && parent[i - 1] >= 0;
-    if (fx) {
-      const size_t jx = x == 0 ? i + N - 1 : i - 1;
-      if (parent[jx] >= 0) unite(parent, (int)i, (int)jx);
-    }
-    if (fy) {
-      const size_t jy = (y == 0) ? i + (size_t)(N - 1) * N : i - N;
-      if (parent[jy] >= 0 && !(left && parent[jy - 1] >= 0)) unite(parent, (int)i, (int)jy);
-    }
-    if (fz) {
-      const size_t jz = (z == 0) ? i + (size_t)(N - 1) * NN : i - NN;
-      if (parent[jz] >= 0 && !(left && parent[jz - 1] >= 0)) unite(parent, (int)i, (int)jz);
-    }
+// Unions across tile faces (see ccl_tile), one block per tile: warp w takes
+// the -y face's row at lz = w and the -z face's row at ly = w, threads
+// 0-63 the -x face's column.  parent[] of a mask site is a tile root (or an
+// ancestor of one, after a path-halving write), and every union hooks one
+// tile root under another, so after this pass the tile roots alone carry
+// the cross-tile structure.
+__device__ __forceinline__ void face_union(int *parent, size_t i, size_t j, bool skip_rule) {
+  if (parent[i] < 0 || parent[j] < 0) return;
+  // the skip rule of ccl_merge: with i-1 and j-1 on the mask too, the pair
+  // (i-1, j-1) -- united here or skipped by the same rule -- joins i and j
+  if (skip_rule && parent[i - 1] >= 0 && parent[j - 1] >= 0) return;
+  unite(parent, (int)i, (int)j);
+}
+
+__global__ void __launch_bounds__(CCL_THREADS) ccl_border_tiles(int *__restrict__ parent, int N, int zper) {
+  static_assert(CCL_THREADS == TILE_X * TILE_Y && TILE_Y == TILE_Z, "one row of each face per warp");
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y, z0 = blockIdx.z * TILE_Z;
+  const size_t NN = (size_t)N * N;
+  const int x = x0 + lane;
+  {  // -y face, periodic
+    const size_t i = (size_t)(z0 + w) * NN + (size_t)y0 * N + x;
+    face_union(parent, i, y0 == 0 ? i + (size_t)(N - 1) * N : i - N, x > 0);
+  }
+  if (z0 > 0 || zper) {  // -z face, open on one rank unless asked periodic
+    const size_t i = (size_t)z0 * NN + (size_t)(y0 + w) * N + x;
+    face_union(parent, i, z0 == 0 ? i + (size_t)(N - 1) * NN : i - NN, x > 0);
+  }
+  if (t < TILE_Y * TILE_Z) {  // -x face, periodic
+    const size_t i = (size_t)(z0 + t / TILE_Y) * NN + (size_t)(y0 + t % TILE_Y) * N + x0;
+    face_union(parent, i, x0 == 0 ? i + N - 1 : i - 1, false);
   }
 }
 
-// compress and count roots per block of CCL_THREADS sites
-__global__ void ccl_compress(int *__restrict__ parent, size_t V, int *__restrict__ blk) {
+// Roots per block of CCL_THREADS threads, into blk[blockIdx.x].
+__device__ __forceinline__ void block_count(int c, int *blk) {
+  __shared__ int cnt[CCL_THREADS / 32];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+  if ((threadIdx.x & 31) == 0) cnt[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < CCL_THREADS / 32; ++w) s += cnt[w];
+    blk[blockIdx.x] = s;
+  }
+}
+
+// Tiled labelling: every tile root's final root.  One thread per 32-site
+// word of the tile-root bits; a tile root that is not a root gets its root
+// written (root searches of other threads still end at the same root), a
+// root sets its bit in bits[].  Counts the roots per block of CCL_THREADS
+// words for the numbering scan.
+__global__ void __launch_bounds__(CCL_THREADS) ccl_resolve(int *__restrict__ parent, const unsigned *__restrict__ tbits,
+                                                          size_t W, unsigned *__restrict__ bits, int *__restrict__ blk) {
+  const size_t w = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
+  unsigned rb = 0;
+  if (w < W) {
+    for (unsigned b = tbits[w]; b; b &= b - 1u) {
+      const int kb = __ffs(b) - 1;
+      const int tr = (int)(w * 32 + kb);
+      const int r = find_root_ro(parent, tr);
+      if (r == tr) rb |= 1u << kb;
+      else parent[tr] = r;
+    }
+    bits[w] = rb;
+  }
+  block_count(__popc(rb), blk);
+}
+
+// Untiled labelling: parent[i] = root(i) for every mask site, and the roots'
+// bits (a warp covers one aligned 32-site word).
+__global__ void __launch_bounds__(CCL_THREADS) ccl_compress(int *__restrict__ parent, size_t V,
+                                                           unsigned *__restrict__ bits) {
   const size_t i = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
   bool root = false;
   if (i < V) {
@@ -441,15 +528,15 @@ __global__ void ccl_compress(int *__restrict__ parent, size_t V, int *__restrict
       root = (r == (int)i);
     }
   }
-  __shared__ int cnt[CCL_THREADS / 32];
   const unsigned b = __ballot_sync(0xffffffffu, root);
-  if ((threadIdx.x & 31) == 0) cnt[threadIdx.x >> 5] = __popc(b);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int s = 0;
-    for (int w = 0; w < CCL_THREADS / 32; ++w) s += cnt[w];
-    blk[blockIdx.x] = s;
-  }
+  if ((threadIdx.x & 31) == 0 && i < V) bits[i >> 5] = b;
+}
+
+// roots per block of CCL_THREADS words (untiled labelling)
+__global__ void __launch_bounds__(CCL_THREADS) ccl_count_bits(const unsigned *__restrict__ bits, size_t W,
+                                                             int *__restrict__ blk) {
+  const size_t w = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
+  block_count(w < W ? __popc(bits[w]) : 0, blk);
 }
 
 // Exclusive scan of the block counts in two levels: each block of
@@ -514,21 +601,45 @@ __global__ void ccl_scan(int *__restrict__ blk, int n, int *__restrict__ total) 
   }
 }
 
-__global__ void ccl_number(const int *__restrict__ parent, size_t V, const int *__restrict__ blk,
-                           const int *__restrict__ tile, int *__restrict__ ids, int *__restrict__ seed, int cap) {
-  const size_t i = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
-  const bool root = (i < V) && parent[i] == (int)i;
-  __shared__ int cnt[CCL_THREADS / 32];
-  const unsigned b = __ballot_sync(0xffffffffu, root);
+// Islands are numbered by their root in increasing site order: the rank of
+// each root bit, from the scanned block counts and a scan of the popcounts
+// inside the block.
+__global__ void __launch_bounds__(CCL_THREADS) ccl_number(const unsigned *__restrict__ bits, size_t W,
+                                                         const int *__restrict__ blk, const int *__restrict__ tile,
+                                                         int *__restrict__ ids, int *__restrict__ seed, int cap) {
+  __shared__ int wsum[CCL_THREADS / 32];
+  const size_t w = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) cnt[warp] = __popc(b);
+  unsigned b = w < W ? bits[w] : 0u;
+  const int c = __popc(b);
+  int incl = c;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += u;
+  }
+  if (lane == 31) wsum[warp] = incl;
   __syncthreads();
-  if (root) {
-    int off = blk[blockIdx.x] + tile[blockIdx.x / SCAN_TILE];
-    for (int w = 0; w < warp; ++w) off += cnt[w];
-    off += __popc(b & ((1u << lane) - 1u));
-    ids[i] = off;
-    if (off < cap) seed[off] = (int)i;
+  int off = blk[blockIdx.x] + tile[blockIdx.x / SCAN_TILE] + incl - c;
+  for (int v = 0; v < warp; ++v) off += wsum[v];
+  for (; b; b &= b - 1u) {
+    const int r = (int)(w * 32 + (__ffs(b) - 1));
+    ids[r] = off;
+    if (off < cap) seed[off] = r;
+    ++off;
+  }
+}
+
+// Tiled labelling: each tile root that is not a root takes its root's
+// island number, so that ids[parent[i]] is the island of every mask site.
+__global__ void __launch_bounds__(CCL_THREADS) ccl_troot_ids(const unsigned *__restrict__ tbits, size_t W,
+                                                            const int *__restrict__ parent, int *__restrict__ ids) {
+  const size_t w = blockIdx.x * (size_t)CCL_THREADS + threadIdx.x;
+  if (w >= W) return;
+  for (unsigned b = tbits[w]; b; b &= b - 1u) {
+    const int tr = (int)(w * 32 + (__ffs(b) - 1));
+    const int r = parent[tr];
+    if (r != tr) ids[tr] = ids[r];
   }
 }
 
@@ -596,6 +707,54 @@ __device__ __forceinline__ void stats_global(int id, int n, A pot, A kin, A grad
   atomicMax(&peak2[id], pk);
 }
 
+// One run's sums into the block's table: open addressing on the island id,
+// linear probing; a full table sends the run to the global sums.
+template <typename A>
+__device__ __forceinline__ void table_update(StatsSlot<A> *table, int id, const RunSums<A> &r, int *size,
+                                             double *sums, unsigned long long *peak2) {
+  unsigned h = ((unsigned)id * 2654435761u) & (STATS_SLOTS - 1);
+  int slot = -1;
+  for (int probe = 0; probe < STATS_SLOTS; ++probe) {
+    const int old = atomicCAS(&table[h].id, -1, id);
+    if (old == -1 || old == id) {
+      slot = (int)h;
+      break;
+    }
+    h = (h + 1) & (STATS_SLOTS - 1);
+  }
+  if (slot >= 0) {
+    atomicAdd(&table[slot].size, r.n);
+    table[slot].add(0, r.pot);
+    table[slot].add(1, r.kin);
+    table[slot].add(2, r.grad);
+    table[slot].add(3, r.cs);
+    atomicMax(&table[slot].peak2, r.pk);
+  } else {
+    stats_global(id, r.n, r.pot, r.kin, r.grad, r.cs, r.pk, size, sums, peak2);
+  }
+}
+
+template <typename A>
+__device__ __forceinline__ void table_clear(StatsSlot<A> *table) {
+  for (int j = threadIdx.x; j < STATS_SLOTS; j += CCL_THREADS) {
+    table[j].clear();
+    table[j].peak2 = 0;
+    table[j].size = 0;
+    table[j].id = -1;
+  }
+}
+
+template <typename A>
+__device__ __forceinline__ void table_flush(const StatsSlot<A> *table, int *size, double *sums,
+                                            unsigned long long *peak2) {
+  for (int j = threadIdx.x; j < STATS_SLOTS; j += CCL_THREADS) {
+    const StatsSlot<A> &t = table[j];
+    if (t.id >= 0) stats_global(t.id, t.size, t.sum(0), t.sum(1), t.sum(2), t.sum(3), t.peak2, size, sums, peak2);
+  }
+}
+
+// The statistics for any edge, one site per lane (edges that are not a
+// multiple of 4).
 template <typename T, bool KAHAN>
 __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ phi, const float *__restrict__ cphi,
                                                         const T *__restrict__ pi, const float *__restrict__ cpi,
@@ -610,12 +769,7 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ p
   using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
   __shared__ StatsSlot<A> table[STATS_SLOTS];
   __shared__ RunSums<A> scratch[CCL_THREADS / 32][32];
-  for (int j = threadIdx.x; j < STATS_SLOTS; j += CCL_THREADS) {
-    table[j].clear();
-    table[j].peak2 = 0;
-    table[j].size = 0;
-    table[j].id = -1;
-  }
+  table_clear(table);
   __syncthreads();
   const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
   const unsigned full = 0xffffffffu;
@@ -683,35 +837,229 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ p
         n += o.n;
         pk = o.pk > pk ? o.pk : pk;
       }
-      // open addressing on the island id, linear probing
-      unsigned h = ((unsigned)id * 2654435761u) & (STATS_SLOTS - 1);
-      int slot = -1;
-      for (int probe = 0; probe < STATS_SLOTS; ++probe) {
-        const int old = atomicCAS(&table[h].id, -1, id);
-        if (old == -1 || old == id) {
-          slot = (int)h;
-          break;
-        }
-        h = (h + 1) & (STATS_SLOTS - 1);
-      }
-      if (slot >= 0) {
-        atomicAdd(&table[slot].size, n);
-        table[slot].add(0, pot);
-        table[slot].add(1, kin);
-        table[slot].add(2, grad);
-        table[slot].add(3, cs);
-        atomicMax(&table[slot].peak2, pk);
-      } else {
-        stats_global(id, n, pot, kin, grad, cs, pk, size, sums, peak2);
-      }
+      table_update(table, id, RunSums<A>{pot, kin, grad, cs, pk, n}, size, sums, peak2);
     }
     __syncwarp();  // scratch is rewritten by the next chunk
   }
   __syncthreads();
-  for (int j = threadIdx.x; j < STATS_SLOTS; j += CCL_THREADS) {
-    const StatsSlot<A> &t = table[j];
-    if (t.id >= 0) stats_global(t.id, t.size, t.sum(0), t.sum(1), t.sum(2), t.sum(3), t.peak2, size, sums, peak2);
+  table_flush(table, size, sums, peak2);
+}
+
+// ---------------------------------------------------------------------------
+// The statistics with four consecutive x-sites per lane (edges that are a
+// multiple of 4): a warp covers 128 sites, so the warp collectives -- the
+// segmented scan, the grouping of runs by island, the table updates -- run
+// once per 128 sites instead of once per 32, and every field is read as
+// 16-byte vectors.
+//
+// Mask sites adjacent along x in one row belong to one island, so the runs
+// are found from the mask alone and the island number is looked up once per
+// run.  A lane splits its four sites at their gaps: L, the run through its
+// first site; R, the run through its last; M, a run between two gaps (at most
+// one in four sites).  A lane whose four sites are all on the mask passes L
+// on.  The carry C (the run through the lane's last site, summed over the
+// lanes it spans) is a segmented inclusive scan over the lanes; a segment
+// starts at every lane that does not continue the previous lane's run (its
+// first site off the mask, the previous lane's last site off it, or a new
+// row).  Closed runs: L plus the previous lane's carry, at a lane with a gap;
+// M; and C where the next lane does not continue it.
+//
+// Plain FP32 fields pack the peak as (|phi| bits, ~index): the maximum is
+// the largest |phi| and, among equal ones, the smallest index, which is the
+// peak position itself -- no second pass over the sites.
+template <typename A>
+__device__ __forceinline__ void run_zero(RunSums<A> &r) {
+  r.pot = r.kin = r.grad = r.cs = (A)0;
+  r.pk = 0;
+  r.n = 0;
+}
+
+template <typename A>
+__device__ __forceinline__ void run_add(RunSums<A> &r, const RunSums<A> &o) {
+  r.pot += o.pot;
+  r.kin += o.kin;
+  r.grad += o.grad;
+  r.cs += o.cs;
+  r.n += o.n;
+  r.pk = o.pk > r.pk ? o.pk : r.pk;
+}
+
+template <typename A>
+__device__ __forceinline__ RunSums<A> run_shfl_up(const RunSums<A> &r, int off) {
+  const unsigned full = 0xffffffffu;
+  return RunSums<A>{__shfl_up_sync(full, r.pot, off), __shfl_up_sync(full, r.kin, off),
+                    __shfl_up_sync(full, r.grad, off), __shfl_up_sync(full, r.cs, off),
+                    __shfl_up_sync(full, r.pk, off),  __shfl_up_sync(full, r.n, off)};
+}
+
+// One round of table updates: the lanes with u set offer (id, r); the offers
+// of one island combine in lane order first, so that the table takes one
+// update per island per round.
+template <typename A>
+__device__ __forceinline__ void table_round(bool u, int id, RunSums<A> r, StatsSlot<A> *table, RunSums<A> *scratch,
+                                            int lane, int *size, double *sums, unsigned long long *peak2) {
+  const unsigned full = 0xffffffffu;
+  if (!__any_sync(full, u)) return;
+  const unsigned grp = __match_any_sync(full, u ? id : -1 - lane);
+  if (u) scratch[lane] = r;
+  __syncwarp();
+  if (u && (grp & ((1u << lane) - 1u)) == 0) {
+    for (unsigned b = grp & (grp - 1u); b; b &= b - 1u) run_add(r, scratch[__ffs(b) - 1]);
+    table_update(table, id, r, size, sums, peak2);
   }
+  __syncwarp();  // scratch is rewritten by the next round
+}
+
+// Four consecutive values of a field in arithmetic A (16-byte loads; i0 is a
+// multiple of 4).
+template <typename A, bool KAHAN, typename T>
+__device__ __forceinline__ void load4(const T *__restrict__ f, const float *__restrict__ comp, size_t i0, A v[4]) {
+  if constexpr (std::is_same<T, double>::value) {
+    const double2 a = *(const double2 *)(f + i0), b = *(const double2 *)(f + i0 + 2);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+  } else {
+    const float4 a = *(const float4 *)(f + i0);
+    if constexpr (KAHAN) {
+      const float4 c = *(const float4 *)(comp + i0);
+      v[0] = (A)((double)a.x - (double)c.x);
+      v[1] = (A)((double)a.y - (double)c.y);
+      v[2] = (A)((double)a.z - (double)c.z);
+      v[3] = (A)((double)a.w - (double)c.w);
+    } else {
+      v[0] = a.x;
+      v[1] = a.y;
+      v[2] = a.z;
+      v[3] = a.w;
+    }
+  }
+}
+
+template <typename T, bool KAHAN>
+__global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ phi, const float *__restrict__ cphi,
+                                                         const T *__restrict__ pi, const float *__restrict__ cpi,
+                                                         const int *__restrict__ parent, const int *__restrict__ ids,
+                                                         int N, const DivN dn, const Consts k,
+                                                         int *__restrict__ size, double *__restrict__ sums,
+                                                         unsigned long long *__restrict__ peak2) {
+  using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+  constexpr bool PACKED = std::is_same<T, float>::value && !KAHAN;
+  constexpr int WARP_SITES = 32 * 4;
+  __shared__ StatsSlot<A> table[STATS_SLOTS];
+  __shared__ RunSums<A> scratch[CCL_THREADS / 32][32];
+  table_clear(table);
+  __syncthreads();
+  const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t s0 = (size_t)blockIdx.x * STATS_SITES;
+  const size_t s1 = s0 + STATS_SITES < V ? s0 + STATS_SITES : V;
+  // chunk loop: uniform per warp, so every lane takes part in the collectives
+  for (size_t base = s0 + (size_t)warp * WARP_SITES; base < s1; base += (size_t)(CCL_THREADS / 32) * WARP_SITES) {
+    const size_t i0 = base + 4 * (size_t)lane;  // V is a multiple of 4: all four sites or none
+    int4 pr = make_int4(-1, -1, -1, -1);
+    if (i0 < s1) pr = *(const int4 *)(parent + i0);
+    const int prv[4] = {pr.x, pr.y, pr.z, pr.w};
+    const bool any = pr.x >= 0 || pr.y >= 0 || pr.z >= 0 || pr.w >= 0;
+    if (__ballot_sync(full, any) == 0) continue;  // uniform per warp
+    int x0 = 0, y = 0, z = 0;
+    if (i0 < s1) site_xyz(dn, N, i0, x0, y, z);
+    RunSums<A> L, M, R;
+    run_zero(L);
+    run_zero(M);
+    run_zero(R);
+    int mpar = -1, rpar = -1;  // the parent of a site of M and of R, for the island lookup
+    if (any) {
+      A c[4], p[4], fy[4], fz[4];
+      const size_t row = (size_t)z * NN + (size_t)y * N;
+      load4<A, KAHAN>(phi, cphi, i0, c);
+      load4<A, KAHAN>(pi, cpi, i0, p);
+      load4<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x0, fy);
+      load4<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x0, fz);
+      const A fx3 = val_as<A, KAHAN>(phi, cphi, row + (x0 + 4 == N ? 0 : x0 + 4));
+      bool gap = false;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (prv[j] < 0) {
+          if (gap && R.n > 0) {
+            M = R;
+            mpar = rpar;
+          }
+          run_zero(R);
+          gap = true;
+        } else {
+          const A cj = c[j], fx = j < 3 ? c[j + 1] : fx3;
+          RunSums<A> t;
+          // BFS accumulators (islands.cpp:131-198)
+          t.grad = (A)0.5 * ((fx - cj) * (fx - cj) + (fy[j] - cj) * (fy[j] - cj) + (fz[j] - cj) * (fz[j] - cj)) *
+                   (A)k.inv_a2;
+          t.kin = site_kinetic(k, cj, p[j]);
+          t.pot = site_potential(k, cj, cj * cj);
+          t.cs = cj;
+          t.n = 1;
+          if constexpr (PACKED) {
+            t.pk = ((unsigned long long)__float_as_uint(fabsf(cj)) << 32) |
+                   (unsigned long long)(0xffffffffu - (unsigned)(i0 + j));
+          } else {
+            t.pk = peak_key<KAHAN>(phi, cphi, i0 + j);
+          }
+          if (!gap) {
+            run_add(L, t);
+          } else {
+            run_add(R, t);
+            rpar = prv[j];
+          }
+        }
+      }
+    }
+    const bool m0 = pr.x >= 0, m3 = pr.w >= 0;
+    const bool through = pr.x >= 0 && pr.y >= 0 && pr.z >= 0 && pr.w >= 0;
+    const bool m3prev = __shfl_up_sync(full, m3, 1);
+    const bool conn = lane > 0 && m0 && m3prev && x0 != 0;
+    // segmented inclusive scan of the carries
+    RunSums<A> C = through ? L : R;
+    const unsigned heads = __ballot_sync(full, !(through && conn));
+    const int start = 31 - __clz(heads & (full >> (31 - lane)));
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const RunSums<A> u = run_shfl_up(C, off);
+      if (lane - off >= start) run_add(C, u);
+    }
+    const RunSums<A> Cp = run_shfl_up(C, 1);
+    const bool conn_next = __shfl_down_sync(full, conn, 1);
+    bool u1 = C.n > 0 && (lane == 31 || !conn_next);  // the carry closes here
+    bool u2 = !through && m0;                        // L closes at the lane's first gap
+    bool u3 = M.n > 0;
+    if (u2 && conn) run_add(L, Cp);
+    const int id1 = u1 ? ids[pr.w] : -1, id2 = u2 ? ids[pr.x] : -1, id3 = u3 ? ids[mpar] : -1;
+    // a lane's own closed runs of one island combine first
+    if (u3 && u2 && id3 == id2) {
+      run_add(L, M);
+      u3 = false;
+    }
+    if (u1 && u2 && id1 == id2) {
+      run_add(L, C);
+      u1 = false;
+    }
+    if (u1 && u3 && id1 == id3) {
+      run_add(M, C);
+      u1 = false;
+    }
+    table_round(u2, id2, L, table, scratch[warp], lane, size, sums, peak2);
+    table_round(u3, id3, M, table, scratch[warp], lane, size, sums, peak2);
+    table_round(u1, id1, C, table, scratch[warp], lane, size, sums, peak2);
+  }
+  __syncthreads();
+  table_flush(table, size, sums, peak2);
+}
+
+// Plain FP32 fields: the peak position from the packed key (ccl_stats4).
+__global__ void ccl_peak_unpack(const unsigned long long *__restrict__ peak2, int n, long long NN,
+                                long long *__restrict__ peakpos) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    peakpos[j] = (long long)(0xffffffffu - (unsigned)(peak2[j] & 0xffffffffull)) + NN;
 }
 
 template <typename T, bool KAHAN>
@@ -830,6 +1178,8 @@ void islands_release(phn_handle *h) {
   if (!s) return;
   cudaFree(s->parent);
   cudaFree(s->ids);
+  cudaFree(s->tbits);
+  cudaFree(s->bits);
   cudaFree(s->blk);
   free_isl_arrays(s);
   delete s;
@@ -844,7 +1194,7 @@ static int grid_blocks(size_t n) {
 
 template <typename T>
 static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, int mode, int zper, int *labels,
-                       phn_island *out, int max_out, int *n_islands) {
+                       phn_island *out, int max_out, int *n_islands, const phn_island **d_out = nullptr) {
   const int N = h->p.N;
   const size_t V = h->V;
   cudaStream_t st = h->stream;
@@ -854,10 +1204,13 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
     IslState *s = new IslState();
     memset(s, 0, sizeof(*s));
     h->isl = s;
-    s->nblk = (int)((V + CCL_THREADS - 1) / CCL_THREADS);
+    s->W = (V + 31) / 32;
+    s->nblk = (int)((s->W + CCL_THREADS - 1) / CCL_THREADS);
     s->ntile = (s->nblk + SCAN_TILE - 1) / SCAN_TILE;
     cudaError_t e = cudaMalloc(&s->parent, V * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&s->ids, V * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->tbits, s->W * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&s->bits, s->W * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc(&s->blk, ((size_t)s->nblk + s->ntile + 1) * sizeof(int));
     if (e != cudaSuccess) {
       islands_release(h);
@@ -871,13 +1224,16 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
   const DivN dn = make_divn((unsigned)N);
   float thr_lo, thr_hi;  // the FP32 bracket of the reference mask (site_mask)
   mask_bracket(thr, &thr_lo, &thr_hi);
-  if (N % TILE_X == 0 && N % TILE_Y == 0 && N % TILE_Z == 0) {
+  const bool tiled = N % TILE_X == 0 && N % TILE_Y == 0 && N % TILE_Z == 0;
+  if (tiled) {
+    // tile labels, face unions, then the tile roots' roots and the root bits
     const dim3 tg(N / TILE_X, N / TILE_Y, N / TILE_Z), tb(TILE_X, TILE_Y);
     if (cphi)
-      ccl_tile<T, true><<<tg, tb, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, s->parent);
+      ccl_tile<T, true><<<tg, tb, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, s->parent, s->tbits);
     else
-      ccl_tile<T, false><<<tg, tb, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, s->parent);
-    ccl_border<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, dn, zper);
+      ccl_tile<T, false><<<tg, tb, 0, st>>>(phi, cphi, pi, cpi, N, mode, thr, thr_lo, thr_hi, k, s->parent, s->tbits);
+    ccl_border_tiles<<<tg, CCL_THREADS, 0, st>>>(s->parent, N, zper);
+    ccl_resolve<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, s->tbits, s->W, s->bits, s->blk);
   } else {
     if (cphi)
       ccl_init<T, true><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, dn, mode, thr, thr_lo, thr_hi, k,
@@ -886,12 +1242,13 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
       ccl_init<T, false><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, N, dn, mode, thr, thr_lo, thr_hi, k,
                                                     s->parent);
     ccl_merge<<<gb, CCL_THREADS, 0, st>>>(s->parent, N, dn, zper);
+    ccl_compress<<<(unsigned)((V + CCL_THREADS - 1) / CCL_THREADS), CCL_THREADS, 0, st>>>(s->parent, V, s->bits);
+    ccl_count_bits<<<s->nblk, CCL_THREADS, 0, st>>>(s->bits, s->W, s->blk);
   }
-  ccl_compress<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk);
   int *tile = s->blk + s->nblk;
   ccl_scan_tiles<<<s->ntile, SCAN_TILE, 0, st>>>(s->blk, s->nblk, tile);
   ccl_scan<<<1, 1024, 0, st>>>(tile, s->ntile, tile + s->ntile);
-  h->launches += 5;
+  h->launches += tiled ? 5 : 6;
   int count = 0;
   cudaError_t e = cudaMemcpyAsync(&count, tile + s->ntile, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -912,25 +1269,50 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
     }
     s->cap = cap;
   }
-  ccl_number<<<s->nblk, CCL_THREADS, 0, st>>>(s->parent, V, s->blk, tile, s->ids, s->seed, s->cap);
+  ccl_number<<<s->nblk, CCL_THREADS, 0, st>>>(s->bits, s->W, s->blk, tile, s->ids, s->seed, s->cap);
   h->launches++;
+  if (tiled) {
+    ccl_troot_ids<<<s->nblk, CCL_THREADS, 0, st>>>(s->tbits, s->W, s->parent, s->ids);
+    h->launches++;
+  }
   if (count > 0) {
+    // four sites per lane where rows hold whole groups of four; plain FP32
+    // fields then take the peak from the packed key, the others in a
+    // second pass over the sites
+    const bool x4 = N % 4 == 0;
+    const bool packed = x4 && std::is_same<T, float>::value && !cphi;
     cudaMemsetAsync(s->size, 0, count * sizeof(int), st);
     cudaMemsetAsync(s->sums, 0, (size_t)count * 4 * sizeof(double), st);
     cudaMemsetAsync(s->peak2, 0, count * sizeof(unsigned long long), st);
-    fill_ll<<<(count + 255) / 256, 256, 0, st>>>(s->peakpos, LLONG_MAX, count);
+    if (!packed) {
+      fill_ll<<<(count + 255) / 256, 256, 0, st>>>(s->peakpos, LLONG_MAX, count);
+      h->launches++;
+    }
     const unsigned sb = (unsigned)((V + STATS_SITES - 1) / STATS_SITES);
-    if (cphi) {
-      ccl_stats<T, true><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size, s->sums,
-                                                     s->peak2);
+    if (x4) {
+      if (cphi)
+        ccl_stats4<T, true><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
+                                                        s->sums, s->peak2);
+      else
+        ccl_stats4<T, false><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
+                                                         s->sums, s->peak2);
+    } else {
+      if (cphi)
+        ccl_stats<T, true><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
+                                                       s->sums, s->peak2);
+      else
+        ccl_stats<T, false><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
+                                                        s->sums, s->peak2);
+    }
+    if (packed) {
+      ccl_peak_unpack<<<(count + 255) / 256, 256, 0, st>>>(s->peak2, count, (long long)N * N, s->peakpos);
+    } else if (cphi) {
       ccl_peak<T, true><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
     } else {
-      ccl_stats<T, false><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
-                                                      s->sums, s->peak2);
       ccl_peak<T, false><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
     }
     ccl_peakval<T><<<(count + 255) / 256, 256, 0, st>>>(phi, cphi, N, count, s->peakpos, s->peakval);
-    h->launches += 4;
+    h->launches += 3;
   }
   if (labels) {
     const size_t total = (size_t)N * N * (N + 2);
@@ -945,6 +1327,22 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "island kernels");
+  if (d_out) {  // every record, left in the handle's device buffer
+    *d_out = nullptr;
+    if (count > 0) {
+      const double a = h->p.a, cell = (a * a) * a;
+      ccl_records<<<(count + 255) / 256, 256, 0, st>>>(s->size, s->sums, s->peakpos, s->peakval, s->seed, count, a,
+                                                       cell, (long long)N * N, s->rec);
+      h->launches++;
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return cuda_error(e, "island records");
+      *d_out = s->rec;
+    }
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "islands");
+    if (n_islands) *n_islands = count;
+    return PHN_OK;
+  }
   const int n_out = count < max_out ? count : max_out;
   if (out && n_out > 0) {
     const double a = h->p.a, cell = (a * a) * a;
@@ -1027,4 +1425,17 @@ extern "C" int phn_islands(phn_handle *h, double thres, int mode, int z_periodic
                                labels, out, max_out, n_islands);
   return run_islands<float>(h, (const float *)h->phi[h->cur], (const float *)h->pi, thres, mode, z_periodic, labels,
                             out, max_out, n_islands);
+}
+
+extern "C" int phn_islands_device(phn_handle *h, double thres, int mode, int z_periodic,
+                                  const phn_island **d_records, int *n_islands) {
+  if (!h || !d_records || !n_islands) return set_error(PHN_ERR_INVALID, "bad argument");
+  if (h->p.Nc != 1) return set_error(PHN_ERR_UNSUPPORTED, "islands need Nc == 1");
+  if (mode != PHN_ISLAND_REFERENCE && mode != PHN_ISLAND_ENERGY) return set_error(PHN_ERR_INVALID, "mode %d", mode);
+  if (h->V > (size_t)0x7fffffff) return set_error(PHN_ERR_UNSUPPORTED, "lattice too large for 32-bit labels");
+  if (h->p.precision == PHN_FP64)
+    return run_islands<double>(h, (const double *)h->phi[h->cur], (const double *)h->pi, thres, mode, z_periodic,
+                               nullptr, nullptr, 0, n_islands, d_records);
+  return run_islands<float>(h, (const float *)h->phi[h->cur], (const float *)h->pi, thres, mode, z_periodic,
+                            nullptr, nullptr, 0, n_islands, d_records);
 }

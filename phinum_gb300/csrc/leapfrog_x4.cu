@@ -142,13 +142,131 @@ struct ObsX4 {
     if (++nplanes == OBS_FOLD) fold();
   }
 
-  template <int THEORY>
-  __device__ void to_double(Acc &A, const Consts &k) {
-    if (nplanes) fold();
-    A.init();
-    double m[NMOM];
+  // (h, l) += (h2, l2), both unevaluated sums: TwoSum of the high words, the
+  // low words into the error, Fast2Sum.
+  __device__ static __forceinline__ void pair_add(float &h, float &l, float h2, float l2) {
+    const float t = __fadd_rn(h, h2);
+    const float bb = __fsub_rn(t, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bb)), __fsub_rn(h2, bb));
+    const float lo = __fadd_rn(e, __fadd_rn(l, l2));
+    h = __fadd_rn(t, lo);
+    l = __fsub_rn(lo, __fsub_rn(h, t));
+  }
+
+  // Combines another thread's totals: moments as FP32 pairs, extrema by the
+  // comparisons of Acc::take_* (ties keep the smaller index).
+  __device__ __forceinline__ void merge(const float *h2, const float *l2, float nf2, float mx, long long ix,
+                                        float mn, long long in, float ab, long long ia, float *h, float *l) {
 #pragma unroll
-    for (int j = 0; j < NMOM; ++j) m[j] = (double)s[j] - (double)c[j];
+    for (int j = 0; j < NMOM; ++j) pair_add(h[j], l[j], h2[j], l2[j]);
+    nonfinite += nf2;
+    if (ix != LLONG_MAX && (mx > maxv || (mx == maxv && ix < maxi && mx > -10000000.f))) {
+      maxv = mx;
+      maxi = ix;
+    }
+    if (in != LLONG_MAX && (mn < minv || (mn == minv && in < mini && mn < 10000000.f))) {
+      minv = mn;
+      mini = in;
+    }
+    if (ia != LLONG_MAX && (ab > absv || (ab == absv && ia < absi && ab > 0.f))) {
+      absv = ab;
+      absi = ia;
+    }
+  }
+
+  __device__ __forceinline__ void shfl_merge(float *h, float *l, int off) {
+    const unsigned full = 0xffffffffu;
+    float h2[NMOM], l2[NMOM];
+#pragma unroll
+    for (int j = 0; j < NMOM; ++j) {
+      h2[j] = __shfl_down_sync(full, h[j], off);
+      l2[j] = __shfl_down_sync(full, l[j], off);
+    }
+    const float nf2 = __shfl_down_sync(full, nonfinite, off);
+    const float mx = __shfl_down_sync(full, maxv, off), mn = __shfl_down_sync(full, minv, off),
+                ab = __shfl_down_sync(full, absv, off);
+    const long long ix = __shfl_down_sync(full, maxi, off), in = __shfl_down_sync(full, mini, off),
+                    ia = __shfl_down_sync(full, absi, off);
+    merge(h2, l2, nf2, mx, ix, mn, in, ab, ia, h, l);
+  }
+
+  // The block's record: the threads' compensated totals summed as FP32 pairs
+  // over the warp and then over the block's W warps in a fixed tree (no FP64
+  // instruction per thread: with one block per item a 512^3 lattice has
+  // 16384 blocks, and per-thread FP64 trees on GB300's narrow FP64 pipe cost
+  // more than the step); one thread widens the pairs to FP64 and stores the
+  // record in record()'s form.
+  template <int THEORY, int W>
+  __device__ void block_store(const Consts &k, double *partials, int tid, size_t slot) {
+    struct WarpTotals {
+      float h[NMOM], l[NMOM];
+      float nf, mx, mn, ab;
+      long long ix, in, ia;
+    };
+    __shared__ WarpTotals sh[W];
+    if (nplanes) fold();
+    float h[NMOM], l[NMOM];
+#pragma unroll
+    for (int j = 0; j < NMOM; ++j) {
+      h[j] = s[j];
+      l[j] = -c[j];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) shfl_merge(h, l, off);
+    const int lane = tid & 31, warp = tid >> 5;
+    if (lane == 0) {
+      WarpTotals &t = sh[warp];
+#pragma unroll
+      for (int j = 0; j < NMOM; ++j) {
+        t.h[j] = h[j];
+        t.l[j] = l[j];
+      }
+      t.nf = nonfinite;
+      t.mx = maxv;
+      t.mn = minv;
+      t.ab = absv;
+      t.ix = maxi;
+      t.in = mini;
+      t.ia = absi;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // lanes past the block's warps carry empty totals
+      init();
+#pragma unroll
+      for (int j = 0; j < NMOM; ++j) h[j] = l[j] = 0.f;
+      if (lane < W) {
+        const WarpTotals &t = sh[lane];
+#pragma unroll
+        for (int j = 0; j < NMOM; ++j) {
+          h[j] = t.h[j];
+          l[j] = t.l[j];
+        }
+        nonfinite = t.nf;
+        maxv = t.mx;
+        minv = t.mn;
+        absv = t.ab;
+        maxi = t.ix;
+        mini = t.in;
+        absi = t.ia;
+      }
+#pragma unroll
+      for (int off = W / 2; off > 0; off >>= 1) shfl_merge(h, l, off);
+      if (lane == 0) {
+        Acc A;
+        A.init();
+        double m[NMOM];
+#pragma unroll
+        for (int j = 0; j < NMOM; ++j) m[j] = (double)h[j] + (double)l[j];
+        record<THEORY>(A, k, m);
+        store_rec(partials + slot * REC, A);
+      }
+    }
+  }
+
+  // The record from the moment totals m[] (FP64) and the extrema.
+  template <int THEORY>
+  __device__ __forceinline__ void record(Acc &A, const Consts &k, const double *m) const {
     A.s[S_PHI] = m[MOM_PHI];
     A.s[S_PI] = m[MOM_PI];
     A.s[S_PHI2] = m[MOM_PHI2];
@@ -268,12 +386,7 @@ __global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const floa
       c = cp;
     }
   }
-  if (MODE != MODE_STEP) {
-    // one record per block, whatever the number of items it walked
-    Acc acc;
-    obs.to_double<THEORY>(acc, k);
-    block_store_n(acc, partials, tid, W, (size_t)blockIdx.x);
-  }
+  if (MODE != MODE_STEP) obs.block_store<THEORY, W>(k, partials, tid, (size_t)blockIdx.x);  // one record per block
 }
 
 bool x4_supported(const phn_params &p) {

@@ -216,6 +216,14 @@ class Lattice:
         L.check(r)
         return lab, recs if n.value == max_out else recs[:n.value].copy()
 
+    def full_analysis_device(self, thres: float, mode: int = L.ISLAND_REFERENCE, z_periodic: bool = False):
+        """phn_islands_device: (number of islands, device address of their
+        records); the records live in the handle until its next island call."""
+        n, d = ctypes.c_int(), ctypes.c_void_p()
+        L.check(self.lib.phn_islands_device(self.h, float(thres), int(mode), int(bool(z_periodic)), ctypes.byref(d),
+                                            ctypes.byref(n)))
+        return n.value, d.value
+
     def stats(self):
         n, ms, st = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_int()
         L.check(self.lib.phn_stats(self.h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(st)))

@@ -15,10 +15,14 @@ Tolerances
       relative 2e-5.  Compensated FP32: absolute 2e-5.
   Islands: labels, counts and sizes exact; island sums relative 1e-11.
 """
+import ctypes
+import os
+
 import numpy as np
 import pytest
 
 import fixtures
+from rows import assert_fp32_sums_close
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -331,7 +335,7 @@ def test_tma_path_matches_plain_path_bit_for_bit(N, theory):
     for key, (r1, f1, p1) in out.items():
         assert np.array_equal(f0, f1) and np.array_equal(p0[N * N:-N * N], p1[N * N:-N * N]), key
         assert np.array_equal(r0[:, 17:23], r1[:, 17:23]), key
-        np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
+        assert_fp32_sums_close(r1, r0)
 
 
 def test_autotune_keeps_state_and_picks_a_variant():
@@ -392,8 +396,8 @@ def test_x4_path_matches_plain_path_bit_for_bit(N, theory):
         assert np.array_equal(f0, f1) and np.array_equal(p0[N * N:-N * N], p1[N * N:-N * N]), key
         assert np.array_equal(r0[:, 17:23], r1[:, 17:23]), key
         assert np.array_equal(a0[17:23], a1[17:23]), key
-        np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
-        np.testing.assert_allclose(a0[9:17], a1[9:17], rtol=1e-6, atol=1e-9)
+        assert_fp32_sums_close(r1, r0)
+        assert_fp32_sums_close(a1, a0)
 
 
 @pytest.mark.parametrize("N", [64, 128])
@@ -429,7 +433,7 @@ def test_compensated_x4_matches_plain_compensated_bit_for_bit(N):
     for key, (r1, f1, p1) in out.items():
         assert np.array_equal(f0, f1) and np.array_equal(p0[N * N:-N * N], p1[N * N:-N * N]), key
         assert np.array_equal(r0[:, 17:23], r1[:, 17:23]), key
-        np.testing.assert_allclose(r0[:, 9:17], r1[:, 9:17], rtol=1e-6, atol=1e-9)
+        assert_fp32_sums_close(r1, r0)
     lat = PL.Lattice(PL.Params(N=N, precision=2))
     lat.upload(phi, pi)
     lat.evolve(3)
@@ -469,6 +473,50 @@ def test_islands_fp32_with_a_spanning_cluster(precision):
         np.testing.assert_allclose(recs[:, I[k]], orecs[:, I[k]], rtol=2e-5, atol=1e-6 * np.abs(orecs[:, I[k]]).max())
     np.testing.assert_allclose(recs[:, I["av_phi"]], orecs[:, I["av_phi"]], rtol=1e-5, atol=1e-6)
     assert np.array_equal(np.abs(recs[:, I["peak_value"]]), np.abs(orecs[:, I["peak_value"]]))
+
+
+def _cudart():
+    import ctypes.util
+    for name in ("libcudart.so.13", "libcudart.so", ctypes.util.find_library("cudart")):
+        if not name:
+            continue
+        for cand in (name, os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64", name)):
+            try:
+                return ctypes.CDLL(cand)
+            except OSError:
+                pass
+    pytest.skip("libcudart not found for the device-to-host check")
+
+
+@pytest.mark.parametrize("precision,N", [(1, 128), (0, 64), (2, 96), (1, 100)])
+def test_islands_device_records_equal_host_records(precision, N):
+    """phn_islands_device leaves the same records on the device that
+    phn_islands copies to the host (tiled and untiled labellings, FP32, FP64
+    and compensated fields), and the labels it leaves behind answer lookups
+    like phn_islands'."""
+    import inputs
+    from phinum_gb300 import _lib as L
+    PL = gpu()
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 12)
+    phi, pi = O.to_ref_layout(phi_i), O.to_ref_layout(pi_i)
+    thr = float(np.quantile(np.sqrt(phi_i ** 2 + pi_i ** 2), 0.6))
+    lat = PL.Lattice(PL.Params(N=N, precision=precision))
+    lat.upload(phi, pi)
+    lab, recs = lat.full_analysis(thr)
+    n, dptr = lat.full_analysis_device(thr)
+    assert n == recs.shape[0] and n > 0 and dptr
+    got = np.zeros_like(recs)
+    rt = _cudart()
+    rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    assert rt.cudaMemcpy(got.ctypes.data, ctypes.c_void_p(dptr), got.nbytes, 2) == 0  # device to host
+    assert np.array_equal(got[:, :2], recs[:, :2]) and np.array_equal(got[:, 8:], recs[:, 8:])
+    np.testing.assert_allclose(got[:, 2:8], recs[:, 2:8], rtol=1e-12, atol=1e-300)
+    pos = np.flatnonzero(lab >= 0)[:: max(1, (lab >= 0).sum() // 1000)].astype(np.int64)
+    isl = np.zeros(pos.size, dtype=np.int32)
+    L.check(lat.lib.phn_islands_lookup(lat.h, pos.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), pos.size,
+                                       isl.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+    assert np.array_equal(isl, lab[pos])
+    lat.close()
 
 
 @pytest.mark.parametrize("N", [24, 47, 100])
