@@ -40,6 +40,16 @@ for i in 2 3; do
     -DPHN_REF_WITHCHARGE=1 &
 done
 wait
+# the energy-density analysis (withEnergyPS 1, EnergybasedID 1): the
+# theories for which the reference compiles it (its theory 0 and 1 forms
+# name the monodromy mass, which only theory 3 defines)
+for t in 2 3 4 5; do
+  build libphinum_ref_t${t}_f64_eps.so -DPHN_REF_THEORY=$t -DPHN_REF_PRECISION=0 -DPHN_REF_ENERGYPS=1 \
+    -DPHN_REF_ENERGYID=1 &
+done
+build libphinum_ref_t3_f64_exp_eps.so -DPHN_REF_THEORY=3 -DPHN_REF_PRECISION=0 -DPHN_REF_EXPANSION=1 \
+  -DPHN_REF_ENERGYPS=1 -DPHN_REF_ENERGYID=1 &
+wait
 # the expanding box (expansion 1), every theory
 for t in 0 1 2 3 4 5; do
   build libphinum_ref_t${t}_f64_exp.so -DPHN_REF_THEORY=$t -DPHN_REF_PRECISION=0 -DPHN_REF_EXPANSION=1 &

@@ -376,9 +376,42 @@ def islands(p: Params, phi: np.ndarray, pi: np.ndarray, thres: float, mode: int 
     n = _load().orc_islands_at(ctypes.byref(_cp(p)), ctypes.byref(clock._c) if clock else None, _ptr(phi),
                                _ptr(pi), float(thres), int(mode), int(zper), _ptr(labels, _PI), _ptr(recs),
                                max_islands)
+    if n == -2:
+        raise ValueError(f"no Delta mask for theory {p.theory}")
     if n < 0:
         raise MemoryError("oracle islands: allocation failed")
     return labels, recs[:min(n, max_islands)]
+
+
+def delta(p: Params, phi: np.ndarray, pi: np.ndarray, clock: Clock | None = None) -> np.ndarray:
+    """Delta of every component of every interior site (withEnergyPS 1,
+    fieldanalysis.cpp:446-560), the reference layout's interior: Nc N^3
+    values.  Theories 2-5 only, as the reference compiles them."""
+    lib = _load()
+    lib.orc_delta_at.restype = ctypes.c_int
+    out = np.zeros(p.Nc * p.N ** 3)
+    r = lib.orc_delta_at(ctypes.byref(_cp(p)), ctypes.byref(clock._c) if clock else None, _ptr(phi), _ptr(pi),
+                         _ptr(out))
+    if r:
+        raise ValueError(f"no Delta for theory {p.theory} (the reference's withEnergyPS forms need theory 2-5)")
+    return out
+
+
+def spectrum_energy(p: Params, phi: np.ndarray, pi: np.ndarray, clock: Clock | None = None):
+    """The density-contrast spectrum (momentumspace.cpp:165-183, 233-270):
+    (D[bin*Nc + a], counts)."""
+    lib = _load()
+    lib.orc_spectrum_energy_at.restype = ctypes.c_int
+    nb, _ = spectrum_bins(p)
+    D = np.zeros(nb * p.Nc)
+    C = np.zeros(nb, dtype=np.int32)
+    r = lib.orc_spectrum_energy_at(ctypes.byref(_cp(p)), ctypes.byref(clock._c) if clock else None, _ptr(phi),
+                                   _ptr(pi), _ptr(D), _ptr(C, _PI))
+    if r == -2:
+        raise ValueError(f"no Delta for theory {p.theory}")
+    if r < 0:
+        raise MemoryError("oracle energy spectrum: allocation failed")
+    return D, C
 
 
 # ------------------------------------------------------ the reference pin ---
@@ -542,3 +575,22 @@ class Reference:
         stats = np.zeros((max_islands, 8))
         n = self.lib.ref_islands(float(thres), _ptr(labels, _PI), _ptr(stats), max_islands)
         return labels, stats[:min(n, max_islands)]
+
+    def island_thres(self) -> float:
+        """The threshold of the last Full_Analysis (EnergybasedID: 4 <rho>)."""
+        self.lib.ref_island_thres.restype = _D
+        return self.lib.ref_island_thres()
+
+    def delta(self) -> np.ndarray:
+        """withEnergyPS builds: Delta of the current fields (interior)."""
+        out = np.zeros(self.p.Nc * self.p.N ** 3)
+        self.lib.ref_delta(_ptr(out))
+        return out
+
+    def spectrum_energy(self):
+        """withEnergyPS builds: Calculate_CorrelationFunctions' TotalCorrD
+        (note: the reference turns Delta into the density contrast in place)."""
+        F, K, Q, C = self.spectrum()
+        D = np.zeros(self.lib.ref_nbins() * self.p.Nc)
+        self.lib.ref_spectrum_d(_ptr(D))
+        return D, C

@@ -1054,8 +1054,75 @@ double orc_site_energy(const orc_params *p, const double *Phi, const double *Pi,
 /* Mask: mode 0 is is_island() (islands.cpp:76): the first component at the
  * site satisfies Phi^2/2 + Pi^2/2 > thres^2/2; mode 1 is the energy-density
  * mask rho(x) > thres. */
+/* Delta, the per-site energy density of CalculateVolumeAverages with
+ * withEnergyPS 1 (fieldanalysis.cpp:446-560): for every component of every
+ * interior site, 0.5 Pi^2 plus the full squared forward differences (no 1/2)
+ * plus the potential in Delta's own forms, static or expanding box.  out[]
+ * holds the reference layout's interior (Nc N^3 values, index K - N^2 Nc).
+ * The reference compiles these forms for theories 2-5 only (its theory 0 and
+ * 1 forms name the monodromy mass, which only theory 3 defines): -1 for 0, 1. */
+int orc_delta_at(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, double *out) {
+  if (p->theory < 2) return -1;
+  const int N = p->N, Nc = p->Nc;
+  const double mass = p->m_sqr, a2 = sqr(p->a);
+  const double sf = p->expansion ? clock_sf(p, c) : 1.0;
+  const long off = pos3(p, 0, 0, 1);
+  for (int z = 1; z < N + 1; z++)
+    for (int y = 0; y < N; y++)
+      for (int x = 0; x < N; x++) {
+        const long K0 = pos3(p, x, y, z), Ku = pos3(p, mod(x + 1, N), y, z), Kv = pos3(p, x, mod(y + 1, N), z),
+                   Kw = pos3(p, x, y, z + 1);
+        for (int a = 0; a < Nc; a++) {
+          const long K = K0 + a;
+          const double ph = Phi[K];
+          double d = (0.5 * sqr(Pi[K]) + sqr(Phi[Ku + a] - ph) / a2 + sqr(Phi[Kv + a] - ph) / a2 +
+                      sqr(Phi[Kw + a] - ph) / a2);
+          if (p->expansion) {
+            d += (0.5 * sqr(p->H0 / sf) * sqr(ph) - ph * Pi[K] * p->H0 / sf);
+            switch (p->theory) { /* fieldanalysis.cpp:536-558 */
+              case 2:
+                d += sqr(sf * sf * mass) * (1. - cos(ph / (sf * sqrt(mass))));
+                break;
+              case 3:
+                d += (0.5 * p->m_mono_sqr * (sqr(sf)) * sqr(ph));
+                d += sqr(sf * sf * mass) * (1. - cos(ph / (sf * sqrt(mass))));
+                break;
+              case 4:
+                d += (double)(p->mass_mode) * 0.5 * mass * sf * sf * sqr(ph);
+                d += (((-p->g * sf * sqr(ph) * ph) / (6.0)) + (double)(p->lambda_mode) * (sqr(sqr(ph)) / (24.0 * Nc)));
+                break;
+              default:
+                d += sqr(sf * sf * mass) * 0.5 / p->p_mono * (pow((1. + ph * ph / mass / sf / sf), p->p_mono) - 1.);
+            }
+          } else {
+            switch (p->theory) { /* fieldanalysis.cpp:511-535 */
+              case 2:
+                d += sqr(mass) * (1. - cos(ph / (sqrt(mass))));
+                break;
+              case 3:
+                d += 0.5 * p->m_mono_sqr * sqr(ph);
+                d += sqr(mass) * (1. - cos(ph / (sqrt(mass))));
+                break;
+              case 4:
+                d += (double)(p->mass_mode) * 0.5 * mass * sqr(ph);
+                d += (((-p->g * sqr(ph) * ph) / (6.0)) + (double)(p->lambda_mode) * (sqr(sqr(ph)) / (24.0 * Nc)));
+                break;
+              default:
+                d += sqr(mass) * 0.5 / p->p_mono * (pow((1. + ph * ph / mass), p->p_mono) - 1.);
+            }
+          }
+          out[K - off] = d;
+        }
+      }
+  return 0;
+}
+
+int orc_delta(const orc_params *p, const double *Phi, const double *Pi, double *out) {
+  return orc_delta_at(p, NULL, Phi, Pi, out);
+}
+
 static unsigned char *make_mask(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi,
-                                double thres, int mode) {
+                                double thres, int mode, const double *delta) {
   const int N = p->N;
   const long n = field_len(p);
   unsigned char *m = (unsigned char *)calloc((size_t)n, 1);
@@ -1065,6 +1132,8 @@ static unsigned char *make_mask(const orc_params *p, const orc_clock *c, const d
         long K = pos3(p, x, y, z);
         if (mode == 0)
           m[K] = (Phi[K] * Phi[K] * 0.5 + Pi[K] * Pi[K] * 0.5 > thres * thres * 0.5);
+        else if (mode == 2) /* EnergybasedID: Delta[K] > thres (islands.cpp:82-83) */
+          m[K] = delta[K - pos3(p, 0, 0, 1)] > thres;
         else
           m[K] = orc_site_energy_at(p, c, Phi, Pi, K, x, y, z) > thres;
       }
@@ -1108,7 +1177,8 @@ static void bfs_expanded(const orc_params *p, double phi, double pi, double sf, 
  * the expanding box's energies.  z is open (1..N) as on one rank (:224-236)
  * unless zper. */
 static void bfs(const orc_params *p, const double *Phi, const double *Pi, const unsigned char *mask, int *b,
-                long *queue, long P, int flag, int zper, orc_island *B, double sf) {
+                long *queue, long P, int flag, int zper, orc_island *B, double sf, const double *delta) {
+  const long doff = pos3(p, 0, 0, 1);
   const int N = p->N, Nc = p->Nc;
   const double mass = p->m_sqr;
   int NN = 0;
@@ -1119,7 +1189,11 @@ static void bfs(const orc_params *p, const double *Phi, const double *Pi, const 
   queue[tail++] = P;
   while (head < tail) {
     long Kooo = queue[head++];
-    if (Phi[Kooo] * Phi[Kooo] > Phi[cnt] * Phi[cnt]) cnt = Kooo;
+    if (delta) { /* EnergybasedID: the peak of Delta (islands.cpp:113-114) */
+      if (delta[Kooo - doff] > delta[cnt - doff]) cnt = Kooo;
+    } else if (Phi[Kooo] * Phi[Kooo] > Phi[cnt] * Phi[cnt]) {
+      cnt = Kooo;
+    }
     int z = (int)(Kooo / ((long)Nc * N * N));
     int y = (int)((Kooo - (long)Nc * N * N * z) / ((long)Nc * N));
     int x = (int)((Kooo - (long)Nc * N * N * z - (long)Nc * N * y) / Nc);
@@ -1179,7 +1253,7 @@ static void bfs(const orc_params *p, const double *Phi, const double *Pi, const 
   B->grad_en = cGradEn * cell;
   B->av_phi = cavPhi;
   B->peak_pos = (double)cnt;
-  B->peak_value = Phi[cnt];
+  B->peak_value = delta ? delta[cnt - doff] : Phi[cnt]; /* islands.cpp:256-261 */
   B->seed_pos = (double)P;
 }
 
@@ -1193,7 +1267,16 @@ int orc_islands_at(const orc_params *p, const orc_clock *c, const double *Phi, c
   const int N = p->N, Nc = p->Nc;
   const long n = field_len(p);
   const double sf = p->expansion ? clock_sf(p, c) : 0.0;
-  unsigned char *mask = make_mask(p, c, Phi, Pi, thres, mode);
+  double *delta = NULL;
+  if (mode == 2) {
+    delta = (double *)malloc(sizeof(double) * (size_t)Nc * N * N * N);
+    if (!delta) return -1;
+    if (orc_delta_at(p, c, Phi, Pi, delta)) {
+      free(delta);
+      return -2;
+    }
+  }
+  unsigned char *mask = make_mask(p, c, Phi, Pi, thres, mode, delta);
   int *b = labels ? labels : (int *)malloc(sizeof(int) * (size_t)n);
   long *queue = (long *)malloc(sizeof(long) * (size_t)n);
   if (!mask || !b || !queue) return -1;
@@ -1203,13 +1286,58 @@ int orc_islands_at(const orc_params *p, const orc_clock *c, const double *Phi, c
   for (long K = pos3(p, 0, 0, 1); K < (long)Nc * N * N * (N + 1); K++)
     if (mask[K] && b[K] == -1) {
       orc_island *B = count < max_islands ? &islands[count] : &scratch;
-      bfs(p, Phi, Pi, mask, b, queue, K, count, zper, B, sf);
+      bfs(p, Phi, Pi, mask, b, queue, K, count, zper, B, sf, delta);
       count++;
     }
   free(mask);
   free(queue);
+  free(delta);
   if (!labels) free(b);
   return count;
+}
+
+/* The density-contrast spectrum of Calculate_CorrelationFunctions with
+ * withEnergyPS 1 (momentumspace.cpp:165-183, 191, 233-270): Delta, its mean
+ * Aavden = (sum over every component of every site) / N^3, the contrast
+ * (Delta - Aavden) / Aavden per component, and its binned power
+ * D[bin*Nc + a] with orc_spectrum's modes, weights and a^3 factors (the
+ * reference transforms Delta with the same fftXtoP_direct as Phi).  Returns
+ * the bin count as orc_spectrum does, -2 for the theories without Delta. */
+int orc_spectrum_energy_at(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, double *D,
+                           int *counts) {
+  const int N = p->N, Nc = p->Nc;
+  const long nint = (long)Nc * N * N * N, off = pos3(p, 0, 0, 1);
+  double *delta = (double *)malloc(sizeof(double) * (size_t)nint);
+  double *field = (double *)calloc((size_t)field_len(p), sizeof(double));
+  if (!delta || !field) {
+    free(delta);
+    free(field);
+    return -1;
+  }
+  if (orc_delta_at(p, c, Phi, Pi, delta)) {
+    free(delta);
+    free(field);
+    return -2;
+  }
+  double aavden = 0.;
+  for (long k = 0; k < nint; k++) aavden += delta[k];
+  const double Aavden = aavden / ((double)N * N * N);
+  for (long k = 0; k < nint; k++) {
+    double v = delta[k];
+    v -= Aavden;
+    v /= Aavden;
+    field[off + k] = v;
+  }
+  int nb;
+  double binsize;
+  orc_spectrum_bins(p, &nb, &binsize);
+  double *K = (double *)malloc(sizeof(double) * (size_t)nb * Nc), *Q = (double *)malloc(sizeof(double) * (size_t)nb * Nc);
+  const int r = (K && Q) ? orc_spectrum(p, field, field, D, K, Q, counts) : -1;
+  free(K);
+  free(Q);
+  free(delta);
+  free(field);
+  return r;
 }
 
 int orc_islands(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode, int zper,

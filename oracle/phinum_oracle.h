@@ -109,6 +109,13 @@ double orc_site_energy_at(const orc_params *p, const orc_clock *c, const double 
                           int x, int y, int z);
 int orc_islands(const orc_params *p, const double *Phi, const double *Pi, double thres, int mode, int zper,
                 int *labels, orc_island *islands, int max_islands);
+/* withEnergyPS 1: Delta per component (interior, Nc N^3), the island mask
+ * mode 2 (Delta > thres, peak and Peak_value by Delta) and the contrast
+ * spectrum; theories 2-5 as the reference compiles them. */
+int orc_delta_at(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, double *out);
+int orc_delta(const orc_params *p, const double *Phi, const double *Pi, double *out);
+int orc_spectrum_energy_at(const orc_params *p, const orc_clock *c, const double *Phi, const double *Pi, double *D,
+                           int *counts);
 
 #ifdef __cplusplus
 }

@@ -271,6 +271,27 @@ void ref_spectrum(double *F, double *K, double *Q, int *counts) {
   for (int k = 0; k < MomentumSpace::nTBins; ++k) counts[k] = MomentumSpace::TotalBCounts[k];
 }
 
+/* The threshold the last Full_Analysis used: the caller's, or with
+ * EnergybasedID 4 <rho> (islands.cpp:783-786). */
+double ref_island_thres() { return (double)island_analysis::thres; }
+
+#if (withEnergyPS == 1)
+/* CalculateVolumeAverages (fieldanalysis.cpp:399-699) on the current fields
+ * and its per-site energy density Delta (fieldanalysis.cpp:446-560), the
+ * reference layout's interior. */
+void ref_delta(double *out) {
+  CalculateVolumeAverages();
+  const size_t slab = (size_t)Nc * N_t * N_t;
+  for (size_t k = 0; k < slab * (size_t)LocalLattice::N_eta_loc; ++k) out[k] = (double)LocalLattice::Delta[slab + k];
+}
+
+/* After ref_spectrum: TotalCorrD[bin*Nc + a], the binned power of the
+ * density contrast (momentumspace.cpp:165-183, 233-270). */
+void ref_spectrum_d(double *D) {
+  for (int k = 0; k < MomentumSpace::nTBins * Nc; ++k) D[k] = (double)MomentumSpace::TotalCorrD[k];
+}
+#endif
+
 /* One Full_Analysis (islands.cpp:778-840) from an empty island history with
  * the given threshold.  labels[] receives the reference's b[] array (the
  * reference layout, -1 outside islands); stats[i*8 + ...] = index, V, PotEn,

@@ -62,9 +62,15 @@
 #endif
 #define expansion PHN_REF_EXPANSION
 #define finebin 0
-#define withEnergyPS 0
+#ifndef PHN_REF_ENERGYPS
+#define PHN_REF_ENERGYPS 0
+#endif
+#define withEnergyPS PHN_REF_ENERGYPS
 #define islanddetect 1
-#define EnergybasedID 0
+#ifndef PHN_REF_ENERGYID
+#define PHN_REF_ENERGYID 0
+#endif
+#define EnergybasedID PHN_REF_ENERGYID
 #define theory PHN_REF_THEORY
 #define adjustDT 0
 #ifndef PHN_REF_INIT

@@ -243,10 +243,7 @@ __device__ __forceinline__ void f4set(float4 &v, int e, float x) {
   else v.w = x;
 }
 
-// At least four blocks per SM (64 registers a thread): at 128^3 the reverse
-// step is latency-bound, and the resident warps, not the issue rate, set its
-// time.
-__global__ void __launch_bounds__(ADJ_THREADS, 4) adjoint_step_x4(const float *__restrict__ phi1,
+__global__ void __launch_bounds__(ADJ_THREADS) adjoint_step_x4(const float *__restrict__ phi1,
                                                                const float *__restrict__ pi1,
                                                                const float *__restrict__ lphi,
                                                                const float *__restrict__ lpi, float *__restrict__ phi0,
@@ -314,9 +311,10 @@ __global__ void __launch_bounds__(ADJ_THREADS, 4) adjoint_step_x4(const float *_
 
 // Grid of the reverse kernel (x4: a block covers 128 x-sites).  Cost model:
 // whole waves of the resident capacity times the planes a block handles
-// plus its fixed overhead (two z-halo planes, the gradient reduction); every
-// plane count from 1 to 64 is a candidate, so that the grid can fill one
-// wave (at 128^3 with four blocks per SM: 4 planes, 512 blocks).
+// plus its fixed overhead (two z-halo planes, the gradient reduction).  A
+// 64-register cap (four blocks per SM) with one-wave plane counts measured
+// slower at 128^3 (18.0 ms against 14.5 ms per 1000 reverse steps): the
+// spills and the shorter z-runs cost more than the extra warps hide.
 // PHN_ADJ_CZ overrides the planes per block (tuning).
 static Grid adjoint_grid(int N, bool x4) {
   Grid g;
@@ -333,7 +331,7 @@ static Grid adjoint_grid(int N, bool x4) {
   const long long resident = (long long)sms * (occ > 0 ? occ : 1);
   int best_cz = 8;
   double best_cost = 1e300;
-  for (int cz = 1; cz <= 64 && cz <= N; ++cz) {
+  for (int cz = 1; cz <= 64 && cz <= N; cz *= 2) {
     const long long blocks = (long long)gx * gy * ((N + cz - 1) / cz);
     const double cost = (double)((blocks + resident - 1) / resident) * (cz + 2.0);
     if (cost < best_cost) {

@@ -201,6 +201,7 @@ static void free_all(phn_handle *h) {
   cudaFree(h->cphi);
   cudaFree(h->cpi);
   cudaFree(h->partials);
+  cudaFree(h->fold_groups);
   cudaFree(h->d_avg);
   cudaFree(h->d_ref);
   cudaFree(h->d_err);
@@ -323,6 +324,8 @@ int phn_create(const phn_params *params, phn_handle **out) {
       }
     h->partial_cap = recs;
     CKF(cudaMalloc(&h->partials, (size_t)recs * REC * sizeof(double)));
+    h->fold_cap = (recs + FIN_GROUP - 1) / FIN_GROUP;
+    CKF(cudaMalloc(&h->fold_groups, (size_t)h->fold_cap * REC * sizeof(double)));
   }
   CKF(cudaMalloc(&h->d_err, sizeof(int)));
   CKF(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
@@ -571,8 +574,8 @@ int phn_evolve(phn_handle *h, int nsteps) {
 
 static int fetch_avg(phn_handle *h, phn_averages *dst_host_slot) {
   CK(launch_finalize(h->p.expanding ? at_scale_factor(h->k, h->obs_sf) : h->k, h->partials, h->obs_records,
-                     h->d_avg, h->stream));
-  h->launches++;
+                     h->d_avg, h->stream, h->fold_groups, h->fold_cap));
+  h->launches += (h->obs_records > 4 * FIN_GROUP && (h->obs_records + FIN_GROUP - 1) / FIN_GROUP <= h->fold_cap) ? 2 : 1;
   CK(cudaMemcpyAsync(dst_host_slot, h->d_avg, sizeof(phn_averages), cudaMemcpyDeviceToHost, h->stream));
   return PHN_OK;
 }

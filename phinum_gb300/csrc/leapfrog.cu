@@ -310,6 +310,17 @@ __global__ void __launch_bounds__(FIN_THREADS) finalize_averages(const double *_
   fold_records(partials, 0, nblocks, k, out);
 }
 
+// First level of a two-level fold: block g folds records [g FIN_GROUP,
+// (g+1) FIN_GROUP) into group record g.
+__global__ void __launch_bounds__(FIN_THREADS) fold_groups(const double *__restrict__ partials, int nblocks,
+                                                           double *__restrict__ groups) {
+  __shared__ double sh[FIN_THREADS][REC];
+  const int b0 = blockIdx.x * FIN_GROUP, b1 = min(nblocks, b0 + FIN_GROUP);
+  fold_acc(partials, b0, b1, sh);
+  if (threadIdx.x == 0)
+    for (int j = 0; j < REC; ++j) groups[(size_t)blockIdx.x * REC + j] = sh[0][j];
+}
+
 // ----------------------------------------------------------- launchers
 Grid lattice_grid(int N) {
   Grid g;
@@ -390,9 +401,18 @@ cudaError_t launch_step_kahan(const Consts &k, const Grid &g, int mode, const fl
   return cudaGetLastError();
 }
 
+// Many records (one block per item at 512^3: 16384) fold in two levels, so
+// that one block does not walk them all: groups of FIN_GROUP records into
+// groups[], then those.  Both levels keep a fixed order.
 cudaError_t launch_finalize(const Consts &k, const double *partials, int nblocks, phn_averages *out,
-                            cudaStream_t st) {
-  finalize_averages<<<1, FIN_THREADS, 0, st>>>(partials, nblocks, k, out);
+                            cudaStream_t st, double *groups, int groups_cap) {
+  const int ng = (nblocks + FIN_GROUP - 1) / FIN_GROUP;
+  if (groups && nblocks > 4 * FIN_GROUP && ng <= groups_cap) {
+    fold_groups<<<ng, FIN_THREADS, 0, st>>>(partials, nblocks, groups);
+    finalize_averages<<<1, FIN_THREADS, 0, st>>>(groups, ng, k, out);
+  } else {
+    finalize_averages<<<1, FIN_THREADS, 0, st>>>(partials, nblocks, k, out);
+  }
   return cudaGetLastError();
 }
 

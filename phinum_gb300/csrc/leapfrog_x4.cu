@@ -49,9 +49,13 @@ constexpr int kNumX4Variants = 6;
 constexpr int OBS_FOLD = 4;
 enum { MOM_PHI, MOM_PI, MOM_PHI2, MOM_PI2, MOM_PHIPI, MOM_PHI4, MOM_PHI6, MOM_GRAD, NMOM };
 
+// COMP: the thread's totals are compensated (s - c, Kahan), for grids whose
+// threads walk many items; with one item per block a thread adds only
+// 4 x cz sites and its plain FP32 sums go straight into the block's pair tree.
+template <bool COMP>
 struct ObsX4 {
   float part[NMOM];
-  float s[NMOM], c[NMOM];
+  float s[COMP ? NMOM : 1], c[COMP ? NMOM : 1];
   int nplanes;
   float nonfinite;
   float maxv, minv, absv;
@@ -59,7 +63,11 @@ struct ObsX4 {
 
   __device__ __forceinline__ void init() {
 #pragma unroll
-    for (int j = 0; j < NMOM; ++j) part[j] = s[j] = c[j] = 0.f;
+    for (int j = 0; j < NMOM; ++j) part[j] = 0.f;
+    if constexpr (COMP) {
+#pragma unroll
+      for (int j = 0; j < NMOM; ++j) s[j] = c[j] = 0.f;
+    }
     nplanes = 0;
     nonfinite = 0.f;
     maxv = -10000000.f;  // CalculateExtrema's starting values (fieldanalysis.cpp:324-325)
@@ -82,13 +90,15 @@ struct ObsX4 {
   }
 
   __device__ __forceinline__ void fold() {
+    if constexpr (COMP) {
 #pragma unroll
-    for (int j = 0; j < NMOM; ++j) {
-      const float y = __fsub_rn(part[j], c[j]);
-      const float t = __fadd_rn(s[j], y);
-      c[j] = __fsub_rn(__fsub_rn(t, s[j]), y);
-      s[j] = t;
-      part[j] = 0.f;
+      for (int j = 0; j < NMOM; ++j) {
+        const float y = __fsub_rn(part[j], c[j]);
+        const float t = __fadd_rn(s[j], y);
+        c[j] = __fsub_rn(__fsub_rn(t, s[j]), y);
+        s[j] = t;
+        part[j] = 0.f;
+      }
     }
     nplanes = 0;
   }
@@ -208,8 +218,8 @@ struct ObsX4 {
     float h[NMOM], l[NMOM];
 #pragma unroll
     for (int j = 0; j < NMOM; ++j) {
-      h[j] = s[j];
-      l[j] = -c[j];
+      h[j] = COMP ? s[j] : part[j];
+      l[j] = COMP ? -c[j] : 0.f;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) shfl_merge(h, l, off);
@@ -297,8 +307,11 @@ __device__ __forceinline__ void kahan_site(float fk, float fd, float f, float c,
   ed = __fsub_rn(__fsub_rn(td, c), yd);
 }
 
-template <int W, int MODE, int THEORY, bool KAHAN>
-__global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const float *__restrict__ phi,
+// A fused observation step with one item per block keeps 4 blocks of 8
+// warps per SM (64 registers): it streams the fields like the plain step and
+// needs its warps for the same latency hiding.
+template <int W, int MODE, int THEORY, bool KAHAN, bool COMP>
+__global__ void __launch_bounds__(32 * W, (MODE == MODE_STEP_OBS && !COMP && !KAHAN) ? 32 / W : 1) step_f32_x4(const Consts k, const float *__restrict__ phi,
                                                       float *__restrict__ phi_out, float *__restrict__ pi,
                                                       float *__restrict__ cphi, float *__restrict__ cpi, StepF s,
                                                       int cz, int nitems, double *__restrict__ partials) {
@@ -307,7 +320,7 @@ __global__ void __launch_bounds__(32 * W) step_f32_x4(const Consts k, const floa
   const int N = k.N, NN = N * N;
   const int tid = threadIdx.x + 32 * threadIdx.y;
   const int chunks = NN / (128 * W);
-  ObsX4 obs;
+  ObsX4<COMP> obs;
   if (MODE != MODE_STEP) obs.init();
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int zc = it / chunks, qc = it - zc * chunks;
@@ -408,7 +421,8 @@ static int x4_items(int N, const X4Variant &v) {
 
 template <int W>
 static const void *x4_fn(bool kahan) {
-  return kahan ? (const void *)step_f32_x4<W, MODE_STEP, 0, true> : (const void *)step_f32_x4<W, MODE_STEP, 0, false>;
+  return kahan ? (const void *)step_f32_x4<W, MODE_STEP, 0, true, false>
+               : (const void *)step_f32_x4<W, MODE_STEP, 0, false, false>;
 }
 
 int x4_grid(const phn_params &p, int variant) {
@@ -427,23 +441,41 @@ int x4_grid(const phn_params &p, int variant) {
   return g < items ? g : items;
 }
 
+template <int W, int MODE, bool COMP>
+static void x4_launch_c(const Consts &k, int theory, int grid, int cz, int nitems, const float *phi,
+                        float *phi_out, float *pi, float *cphi, float *cpi, StepF s, double *partials,
+                        cudaStream_t st) {
+  const dim3 b(32, W);
+  if (cphi) {
+    if (theory == 0)
+      step_f32_x4<W, MODE, 0, true, COMP><<<grid, b, 0, st>>>(k, phi, phi_out, pi, cphi, cpi, s, cz, nitems,
+                                                              partials);
+    else
+      step_f32_x4<W, MODE, 1, true, COMP><<<grid, b, 0, st>>>(k, phi, phi_out, pi, cphi, cpi, s, cz, nitems,
+                                                              partials);
+  } else {
+    if (theory == 0)
+      step_f32_x4<W, MODE, 0, false, COMP><<<grid, b, 0, st>>>(k, phi, phi_out, pi, nullptr, nullptr, s, cz, nitems,
+                                                               partials);
+    else
+      step_f32_x4<W, MODE, 1, false, COMP><<<grid, b, 0, st>>>(k, phi, phi_out, pi, nullptr, nullptr, s, cz, nitems,
+                                                               partials);
+  }
+}
+
+// Observation kernels compensate the threads' totals only where a block
+// walks more than one item.
 template <int W, int MODE>
 static cudaError_t x4_launch_t(const Consts &k, int theory, int grid, int cz, int nitems, const float *phi,
                                float *phi_out, float *pi, float *cphi, float *cpi, StepF s, double *partials,
                                cudaStream_t st) {
-  const dim3 b(32, W);
-  if (cphi) {
-    if (theory == 0)
-      step_f32_x4<W, MODE, 0, true><<<grid, b, 0, st>>>(k, phi, phi_out, pi, cphi, cpi, s, cz, nitems, partials);
-    else
-      step_f32_x4<W, MODE, 1, true><<<grid, b, 0, st>>>(k, phi, phi_out, pi, cphi, cpi, s, cz, nitems, partials);
+  if constexpr (MODE == MODE_STEP) {
+    x4_launch_c<W, MODE, false>(k, theory, grid, cz, nitems, phi, phi_out, pi, cphi, cpi, s, partials, st);
   } else {
-    if (theory == 0)
-      step_f32_x4<W, MODE, 0, false><<<grid, b, 0, st>>>(k, phi, phi_out, pi, nullptr, nullptr, s, cz, nitems,
-                                                          partials);
+    if (grid < nitems)
+      x4_launch_c<W, MODE, true>(k, theory, grid, cz, nitems, phi, phi_out, pi, cphi, cpi, s, partials, st);
     else
-      step_f32_x4<W, MODE, 1, false><<<grid, b, 0, st>>>(k, phi, phi_out, pi, nullptr, nullptr, s, cz, nitems,
-                                                          partials);
+      x4_launch_c<W, MODE, false>(k, theory, grid, cz, nitems, phi, phi_out, pi, cphi, cpi, s, partials, st);
   }
   return cudaGetLastError();
 }

@@ -289,9 +289,11 @@ constexpr int FIN_THREADS = 256;  // sh[FIN_THREADS][REC] doubles: the 48 KB of 
 // threads and forms the reference's derived quantities
 // (fieldanalysis.cpp:619-638): Energy, Charge, Interaction and the per-volume
 // moments of a lattice of k.N^3 sites.
-__device__ __forceinline__ void fold_records(const double *__restrict__ partials, int b0, int b1, const Consts &k,
-                             phn_averages *__restrict__ out) {
-  __shared__ double sh[FIN_THREADS][REC];
+// The fold of records [b0, b1) by one block of FIN_THREADS threads: strided
+// per thread (two records per round, combined in record order), then a fixed
+// tree; the total is left in sh[0].
+__device__ __forceinline__ void fold_acc(const double *__restrict__ partials, int b0, int b1,
+                                         double (*sh)[REC]) {
   const int t = threadIdx.x;
   Acc a;
   a.init();
@@ -317,7 +319,13 @@ __device__ __forceinline__ void fold_records(const double *__restrict__ partials
     }
     __syncthreads();
   }
-  if (t == 0) {
+}
+
+__device__ __forceinline__ void fold_records(const double *__restrict__ partials, int b0, int b1, const Consts &k,
+                             phn_averages *__restrict__ out) {
+  __shared__ double sh[FIN_THREADS][REC];
+  fold_acc(partials, b0, b1, sh);
+  if (threadIdx.x == 0) {
     Acc r;
     load_rec(r, sh[0]);
     const double vol = (double)k.N * (double)k.N * (double)k.N;

@@ -36,6 +36,8 @@ enum {
   E_ABS_I,
   REC = 24     // doubles per block record (padded)
 };
+constexpr int FIN_GROUP = 256;  // block records per first-level fold (launch_finalize)
+
 
 // Coefficients of the kick, the volume averages and the energy density,
 // evaluated on the host with the reference's own expressions so that the FP64
@@ -158,7 +160,7 @@ cudaError_t launch_step_kahan(const Consts &k, const Grid &g, int mode, const fl
                               const float *cphi, float *cphi_out, float *pi, float *cpi, StepF s,
                               double *partials, cudaStream_t st);
 cudaError_t launch_finalize(const Consts &k, const double *partials, int nblocks, phn_averages *out,
-                            cudaStream_t st);
+                            cudaStream_t st, double *groups = nullptr, int groups_cap = 0);
 
 // TMA-pipelined FP32 step (leapfrog_tma.cu): Nc = 1, N in {128,256,384,512,768,1024};
 // variants are tile heights / stage counts, all bit-identical.
@@ -233,6 +235,8 @@ struct phn_handle {
   double obs_sf;       // scale factor of the state the last observation read
   int *d_err;          // device error word of bounded waits (0: none)
   double *partials;    // block records of the fused observation
+  double *fold_groups; // first-level folds of many records (launch_finalize)
+  int fold_cap;        // group records fold_groups holds
   phn_averages *d_avg; // finalize output (device)
   phn_averages *h_avg; // pinned host mirror, one per row slot
   int h_avg_cap;

@@ -56,6 +56,7 @@ struct SpecState {
   double binsize;
   std::vector<int> h_counts;
   bool counts_ok;
+  bool mono, u_mono;       // the key tables' rows are monotone per half (bin_runs applies)
   // uniform-bin (configuration) mode, allocated on first use
   int u_nbins;
   double *u_partials, *u_bins;
@@ -249,13 +250,185 @@ __global__ void __launch_bounds__(SPEC_THREADS) bin_sums(const C *__restrict__ f
   }
 }
 
-__global__ void fold_blocks(const double *__restrict__ partials, int nblocks, int nbins, double scale,
-                            double *__restrict__ out) {
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 3 * nbins; j += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += partials[(size_t)b * 3 * nbins + j];
-    out[j] = s * scale;
+// Per-call sums, FP32 spectra, by runs: the bins of a row (py, pz) are
+// monotone in px on each half -- non-decreasing on [0, N/2) where |p_x|
+// grows, non-increasing on [N/2, N) where it falls (checked per key table by
+// keys_monotone; bin_sums serves a table that fails the check).  A warp walks
+// a half row in chunks of 32 lanes x RUN_Q consecutive modes: the chunk's
+// modes are loaded coalesced into shared memory (|Phi|^2, |Pi|^2,
+// Re(Phi Pi*) and the bin of each), then every lane sums the runs of equal
+// bins in its RUN_Q modes in registers.  A run inside a lane's modes has a
+// bin no other lane of the chunk holds (monotone bins), so it adds to the
+// warp histogram without a conflict; the runs that cross lanes join in one
+// segmented scan per chunk (once per 256 modes, against once per 32 in
+// bin_sums), and each closes in one lane.  The order of every addition is
+// fixed, so the sums are the same run to run.
+constexpr int RUN_Q = 8;
+constexpr int RUN_WARPS = 4;  // 128 threads: the histograms of up to 1024 bins and the stage fit twice per SM
+constexpr int RUN_THREADS = 32 * RUN_WARPS;
+
+__device__ __forceinline__ void run_flush(CompF *hF, CompF *hK, CompF *hQ, int bin, float f, float k, float q) {
+  hist_add(hF[bin], f);
+  hist_add(hK[bin], k);
+  hist_add(hQ[bin], q);
+}
+
+__global__ void __launch_bounds__(RUN_THREADS) bin_runs(const float2 *__restrict__ fphi, const float2 *__restrict__ fpi,
+                                                       const unsigned short *__restrict__ keys, int N, int nbins,
+                                                       double *__restrict__ partials) {
+  extern __shared__ double run_mem[];
+  CompF *hist = (CompF *)run_mem;                                  // [RUN_WARPS][3][nbins]
+  float4 *stage_all = (float4 *)(run_mem + RUN_WARPS * 3 * nbins);  // [RUN_WARPS][32][RUN_Q + 1]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < RUN_WARPS * 3 * nbins; i += RUN_THREADS) hist_zero(hist[i]);
+  __syncthreads();
+  CompF *hF = hist + (size_t)warp * 3 * nbins, *hK = hF + nbins, *hQ = hK + nbins;
+  float4 *stage = stage_all + (size_t)warp * 32 * (RUN_Q + 1);
+  const unsigned full = 0xffffffffu;
+  const int h = N / 2, M = N / 2 + 1;
+  const int nrows = M * N;
+  for (int row = blockIdx.x * RUN_WARPS + warp; row < nrows; row += gridDim.x * RUN_WARPS) {
+    const int py = row % M, pz = row / M;
+    const long long krow = (long long)row * N;
+    const long long direct = ((long long)pz * N + py) * M;
+    const long long mirror = ((long long)((N - pz) % N) * N + (N - py) % N) * M + N;
+    for (int half = 0; half < 2; ++half) {
+      const int x1 = half ? N : h;
+      for (int c0 = half ? h : 0; c0 < x1; c0 += 32 * RUN_Q) {
+        const int cn = min(32 * RUN_Q, x1 - c0);
+        // the chunk's modes, coalesced, into lane-contiguous stage slots
+#pragma unroll
+        for (int u = 0; u < RUN_Q; ++u) {
+          const int j = u * 32 + lane;
+          if (j < cn) {
+            const int px = c0 + j;
+            const unsigned kk = keys[krow + px];
+            const long long m = px <= h ? direct + px : mirror - px;
+            const float2 va = fphi[m], vb = fpi[m];
+            float f = mag2v(va), k = mag2v(vb), q = dotv(va, vb);
+            if (kk & KEY_WEIGHT2) {  // exact doubling
+              f += f;
+              k += k;
+              q += q;
+            }
+            stage[(j / RUN_Q) * (RUN_Q + 1) + (j % RUN_Q)] = make_float4(f, k, q, __int_as_float((int)(kk & KEY_BIN)));
+          }
+        }
+        __syncwarp();
+        // runs of the lane's modes: the first (fb), the interior ones
+        // (flushed here), the last (lb; the whole segment when through)
+        const int nm = max(0, min(RUN_Q, cn - lane * RUN_Q));
+        int fb = -1, cur = -1;
+        float F0 = 0.f, F1 = 0.f, F2 = 0.f, a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        bool first_open = true;
+#pragma unroll
+        for (int m = 0; m < RUN_Q; ++m) {
+          if (m < nm) {
+            const float4 e = stage[lane * (RUN_Q + 1) + m];
+            const int b = __float_as_int(e.w);
+            if (b != cur) {
+              if (cur >= 0) {
+                if (first_open) {
+                  fb = cur;
+                  F0 = a0;
+                  F1 = a1;
+                  F2 = a2;
+                  first_open = false;
+                } else {
+                  run_flush(hF, hK, hQ, cur, a0, a1, a2);
+                }
+              }
+              cur = b;
+              a0 = e.x;
+              a1 = e.y;
+              a2 = e.z;
+            } else {
+              a0 += e.x;
+              a1 += e.y;
+              a2 += e.z;
+            }
+          }
+        }
+        const int lb = cur;
+        const bool through = nm > 0 && first_open;
+        if (through) fb = lb;
+        __syncwarp();  // interior runs added; the stage is free for the next chunk after this one
+        // runs across lanes: carry C = the run through the lane's last mode
+        const int lb_prev = __shfl_up_sync(full, lb, 1);
+        const bool conn = lane > 0 && nm > 0 && lb_prev >= 0 && fb == lb_prev;
+        const unsigned heads = __ballot_sync(full, !(through && conn));
+        const int start = 31 - __clz(heads & (full >> (31 - lane)));
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const float u0 = __shfl_up_sync(full, a0, off), u1 = __shfl_up_sync(full, a1, off),
+                      u2 = __shfl_up_sync(full, a2, off);
+          if (lane - off >= start) {
+            a0 += u0;
+            a1 += u1;
+            a2 += u2;
+          }
+        }
+        const float p0 = __shfl_up_sync(full, a0, 1), p1 = __shfl_up_sync(full, a1, 1),
+                    p2 = __shfl_up_sync(full, a2, 1);
+        const bool conn_next = __shfl_down_sync(full, conn, 1) && lane < 31;
+        if (nm > 0 && !through) {  // the first run closes at the lane's first bin change
+          if (conn) {
+            F0 += p0;
+            F1 += p1;
+            F2 += p2;
+          }
+          run_flush(hF, hK, hQ, fb, F0, F1, F2);
+        }
+        __syncwarp();
+        if (nm > 0 && !conn_next) run_flush(hF, hK, hQ, lb, a0, a1, a2);
+        __syncwarp();
+      }
+    }
   }
+  __syncthreads();
+  for (int j = threadIdx.x; j < 3 * nbins; j += RUN_THREADS) {
+    double s = 0.0;
+    for (int w = 0; w < RUN_WARPS; ++w) s += hist_value(hist[(size_t)w * 3 * nbins + j]);
+    partials[(size_t)blockIdx.x * 3 * nbins + j] = s;
+  }
+}
+
+// Whether every row's bins are monotone on each half (bin_runs' condition):
+// one thread per row and half.  Sets bit 1 of *flag on a violation.
+__global__ void keys_monotone(const unsigned short *__restrict__ keys, int N, int *__restrict__ flag) {
+  const int h = N / 2, M = N / 2 + 1;
+  const long long n = 2LL * M * N;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const long long row = t >> 1;
+    const int half = (int)(t & 1);
+    const unsigned short *k = keys + row * N;
+    int prev = half ? 0x7fffffff : -1;
+    bool ok = true;
+    for (int px = half ? h : 0; px < (half ? N : h); ++px) {
+      const int b = (int)(k[px] & KEY_BIN);
+      if (half ? b > prev : b < prev) ok = false;
+      prev = b;
+    }
+    if (!ok) atomicOr(flag, 2);
+  }
+}
+
+// The per-bin totals over the blocks' partials: one block per entry (F, K, Q
+// of a bin), a strided sum per thread and a fixed tree, so the result does
+// not depend on timing.
+__global__ void __launch_bounds__(256) fold_blocks(const double *__restrict__ partials, int nblocks, int nbins,
+                                                   double scale, double *__restrict__ out) {
+  __shared__ double sh[256];
+  const int j = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += 256) s += partials[(size_t)b * 3 * nbins + j];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[j] = sh[0] * scale;
 }
 
 void spectrum_release(phn_handle *h) {
@@ -290,7 +463,7 @@ static size_t n_modes(int N) { return (size_t)N * (N / 2 + 1) * N; }
 
 // Key table and mode counts of one rule (bin_keys), counts copied to host.
 static int build_keys(phn_handle *h, unsigned short *keys, int *counts, int nbins, double binsize, int rule,
-                      std::vector<int> &h_counts) {
+                      std::vector<int> &h_counts, bool *mono) {
   SpecState *s = (SpecState *)h->spec;
   cudaError_t e = cudaMemsetAsync(counts, 0, nbins * sizeof(int), h->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->flag, 0, sizeof(int), h->stream);
@@ -299,15 +472,24 @@ static int build_keys(phn_handle *h, unsigned short *keys, int *counts, int nbin
                                                                           counts, s->flag);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "bin_keys");
-  h->launches++;
+  keys_monotone<<<s->nblocks, SPEC_THREADS, 0, h->stream>>>(keys, h->p.N, s->flag);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "keys_monotone");
+  h->launches += 2;
   h_counts.resize(nbins);
   int flag = 0;
   e = cudaMemcpyAsync(h_counts.data(), counts, nbins * sizeof(int), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return cuda_error(e, "mode counts");
-  if (flag) return set_error(PHN_ERR_INVALID, "bin array too small (momentumspace.cpp:128)");
+  if (flag & 1) return set_error(PHN_ERR_INVALID, "bin array too small (momentumspace.cpp:128)");
+  *mono = (flag & 2) == 0;
   return PHN_OK;
+}
+
+// Shared memory of bin_runs: the warp histograms and the mode stages.
+static size_t run_smem(int nbins) {
+  return (size_t)RUN_WARPS * 3 * nbins * sizeof(double) + (size_t)RUN_WARPS * 32 * (RUN_Q + 1) * sizeof(float4);
 }
 
 static int spec_init(phn_handle *h) {
@@ -347,15 +529,16 @@ static int spec_init(phn_handle *h) {
   CKS(cudaFuncSetAttribute(bin_sums<float2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
   CKS(cudaFuncSetAttribute(bin_sums<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
   CKS(cudaFuncSetAttribute(bin_keys, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(maxb * sizeof(int))));
+  CKS(cudaFuncSetAttribute(bin_runs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem(maxb)));
 #undef CKS
   // keys and mode counts of the reference rule (InitBCounts): field independent
-  return build_keys(h, s->keys, s->counts, s->nbins, s->binsize, RULE_REFERENCE, s->h_counts);
+  return build_keys(h, s->keys, s->counts, s->nbins, s->binsize, RULE_REFERENCE, s->h_counts, &s->mono);
 }
 
 // One component: R2C of phi and pi, the binned sums, the three bin arrays
 // into hb ([3][nbins], scaled by a^3 a^3).
 static int spectrum_component(phn_handle *h, int a, const unsigned short *keys, int nbins, double *partials,
-                              double *bins, double scale, std::vector<double> &hb) {
+                              double *bins, double scale, bool mono, std::vector<double> &hb) {
   SpecState *s = (SpecState *)h->spec;
   const int N = h->p.N;
   const bool dbl = h->p.precision == PHN_FP64;
@@ -374,12 +557,15 @@ static int spectrum_component(phn_handle *h, int a, const unsigned short *keys, 
   if (dbl)
     bin_sums<double2, double><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
         (const double2 *)s->fphi, (const double2 *)s->fpi, keys, N, nbins, partials);
+  else if (mono)
+    bin_runs<<<s->nblocks, RUN_THREADS, run_smem(nbins), h->stream>>>((const float2 *)s->fphi, (const float2 *)s->fpi,
+                                                                     keys, N, nbins, partials);
   else
     bin_sums<float2, float><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
         (const float2 *)s->fphi, (const float2 *)s->fpi, keys, N, nbins, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "bin_sums");
-  fold_blocks<<<(3 * nbins + 255) / 256, 256, 0, h->stream>>>(partials, s->nblocks, nbins, scale, bins);
+  fold_blocks<<<3 * nbins, 256, 0, h->stream>>>(partials, s->nblocks, nbins, scale, bins);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "fold_blocks");
   h->launches += 2;
@@ -424,7 +610,7 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
     if (Q) Q[k] = 0.0;
   }
   for (int a = 0; a < Nc; ++a) {
-    r = spectrum_component(h, a, s->keys, s->nbins, s->partials, s->bins, f3 * f3, hb);
+    r = spectrum_component(h, a, s->keys, s->nbins, s->partials, s->bins, f3 * f3, s->mono, hb);
     if (r) return r;
     for (int b = 0; b < s->nbins; ++b) {
       if (F) F[b * Nc + a] = hb[b];
@@ -464,14 +650,14 @@ int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double 
     if (e == cudaSuccess) e = cudaMalloc(&s->u_counts, (size_t)nbins * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&s->u_keys, n_modes(N) * sizeof(unsigned short));
     if (e != cudaSuccess) return cuda_error(e, "uniform spectrum buffers");
-    r = build_keys(h, s->u_keys, s->u_counts, nbins, pmax / nbins, RULE_UNIFORM, s->u_h_counts);
+    r = build_keys(h, s->u_keys, s->u_counts, nbins, pmax / nbins, RULE_UNIFORM, s->u_h_counts, &s->u_mono);
     if (r) return r;
     s->u_nbins = nbins;
   }
   const double f3 = (h->p.a * h->p.a) * h->p.a;
   std::vector<double> hb;
   for (int a = 0; a < Nc; ++a) {
-    r = spectrum_component(h, a, s->u_keys, nbins, s->u_partials, s->u_bins, f3 * f3, hb);
+    r = spectrum_component(h, a, s->u_keys, nbins, s->u_partials, s->u_bins, f3 * f3, s->u_mono, hb);
     if (r) return r;
     for (int b = 0; b < nbins; ++b) {
       if (F) F[b * Nc + a] = hb[b];

@@ -288,6 +288,42 @@ def run_f32_case(name: str) -> None:
     print(f"f32/{name}: tau={tau}")
 
 
+# The energy-density analysis (withEnergyPS 1, EnergybasedID 1) of the
+# reference builds that compile it: lattice params, input seed, phi0, steps
+# before the analysis.  Delta, the island labels and records of a first
+# Full_Analysis (threshold 4 <rho>, set by the reference itself) and the
+# density-contrast spectrum.
+EPS_CASES = {
+    "eps_t2_n12": (dict(N=12, Nc=1, **COS), 71, 1.0, 40),
+    "eps_t3_n12": (dict(N=12, Nc=1, **MONO), 72, 0.0, 40),
+    "eps_t4_n12": (dict(N=12, Nc=1, **CUBIC), 73, 0.5, 40),
+    "eps_t5_n12": (dict(N=12, Nc=1, **POWER), 74, 1.0, 40),
+    "eps_t3_n12_exp": (dict(N=12, Nc=1, **MONO, **EXP), 75, 0.0, 40),
+}
+
+
+def run_eps_case(name: str) -> None:
+    from oracle import oracle as O
+    import inputs
+    pd, seed, phi0, steps = EPS_CASES[name]
+    p = O.Params(**{"a": 0.25, "dt": 0.08, "T0": 0.0, **pd})
+    phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, seed, phi0=phi0)
+    R = O.Reference(p, "f64", "_eps")
+    R.set_fields(O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc))
+    R.reset()
+    R.evolve(steps)
+    phi, pi = R.get_fields()
+    delta = R.delta()
+    labels, stats = R.islands(0.0)  # Full_Analysis replaces the threshold by 4 <rho>
+    thres = R.island_thres()
+    D, C = R.spectrum_energy()
+    os.makedirs(os.path.join(HERE, "eps"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "eps", f"{name}.npz"), params=json.dumps(pd), seed=seed, phi0=phi0,
+                        steps=steps, phi=phi, pi=pi, delta=delta, labels=labels, stats=stats, thres=thres, D=D,
+                        counts=C)
+    print(f"eps/{name}: thres={thres:.6g} islands={len(stats)} D[1]={D[1]:.6g}")
+
+
 def run_ic_case(name: str) -> None:
     from oracle import oracle as O
     pd, ic = IC_CASES[name]
@@ -387,6 +423,13 @@ def main() -> None:
         for name in CONFIG_CASES:
             subprocess.run([sys.executable, os.path.abspath(__file__), "--config-case", name], check=True)
         return
+    if len(sys.argv) > 2 and sys.argv[1] == "--eps-case":
+        run_eps_case(sys.argv[2])
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "--eps":
+        for name in EPS_CASES:
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--eps-case", name], check=True)
+        return
     if len(sys.argv) > 2 and sys.argv[1] == "--f32-case":
         run_f32_case(sys.argv[2])
         return
@@ -427,6 +470,8 @@ def main() -> None:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--fvd-case", name], check=True)
     for name in F32_CASES:
         subprocess.run([sys.executable, os.path.abspath(__file__), "--f32-case", name], check=True)
+    for name in EPS_CASES:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--eps-case", name], check=True)
 
 
 if __name__ == "__main__":

@@ -179,3 +179,49 @@ def test_single_precision_port_matches_reference_float_build(name):
     pi2 = O.to_ref_layout(pi_i, p.Nc).astype(np.float32)
     O.evolve_f32(p, phi2, pi2, int(d["steps"]), nthreads=O.max_threads(True), fast=True)
     np.testing.assert_allclose(phi2, phi, rtol=0, atol=1e-4)
+
+
+EPS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "eps")
+EPS = sorted(n[:-4] for n in os.listdir(EPS_DIR) if n.endswith(".npz")) if os.path.isdir(EPS_DIR) else []
+
+
+@pytest.mark.parametrize("name", EPS)
+def test_energy_density_analysis_matches_reference_fixture(name):
+    """withEnergyPS 1 with EnergybasedID 1, the reference builds that compile
+    it (theories 2-5, static and expanding): Delta bit-exact, the threshold
+    4 <rho> that Full_Analysis sets, the Delta mask's labels and records (peak
+    and Peak_value by Delta) bit-exact, the density-contrast spectrum within
+    the rounding of the two FFTs."""
+    import json
+    import inputs
+    d = np.load(os.path.join(EPS_DIR, name + ".npz"))
+    pd = json.loads(str(d["params"]))
+    p = O.Params(a=0.25, dt=0.08, T0=0.0, **pd)
+    phi_i, pi_i = inputs.lattice_fields(p.N, p.Nc, int(d["seed"]), phi0=float(d["phi0"]))
+    phi, pi = O.to_ref_layout(phi_i, p.Nc), O.to_ref_layout(pi_i, p.Nc)
+    clock = O.Clock(p)
+    O.evolve(p, phi, pi, int(d["steps"]), clock)
+    slab = p.Nc * p.N * p.N
+    assert np.array_equal(phi[slab:-slab], d["phi"][slab:-slab]) and np.array_equal(pi[slab:-slab], d["pi"][slab:-slab])
+    delta = O.delta(p, phi, pi, clock)
+    assert np.array_equal(delta, d["delta"])
+    thr = 4.0 * O.averages(p, phi, pi, clock)[O.AVG["energy"]]
+    assert thr == float(d["thres"])
+    labels, recs = O.islands(p, phi, pi, thr, mode=2, clock=clock)
+    assert np.array_equal(labels, d["labels"])
+    st = d["stats"]
+    assert recs.shape[0] == st.shape[0] > 0
+    cols = [O.ISL[k] for k in ("index", "volume", "pot_en", "kin_en", "grad_en", "av_phi", "peak_pos", "peak_value")]
+    assert np.array_equal(recs[:, cols], st)
+    D, C = O.spectrum_energy(p, phi, pi, clock)
+    assert np.array_equal(C, d["counts"])
+    np.testing.assert_allclose(D, d["D"], rtol=1e-10, atol=1e-12 * np.abs(d["D"]).max())
+
+
+def test_energy_density_analysis_is_refused_where_the_reference_does_not_compile_it():
+    p = O.Params(N=8, theory=0)
+    phi = O.to_ref_layout(np.ones((8, 8, 8)))
+    with pytest.raises(ValueError):
+        O.delta(p, phi, phi.copy())
+    with pytest.raises(ValueError):
+        O.islands(p, phi, phi.copy(), 1.0, mode=2)
