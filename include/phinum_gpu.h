@@ -53,7 +53,12 @@ enum {
 
 enum {
   PHN_ISLAND_REFERENCE = 0, /* is_island(): phi^2/2 + pi^2/2 > thres^2/2 (islands.cpp:76) */
-  PHN_ISLAND_ENERGY = 1     /* energy density rho(x) > thres, rho the summand of <E> */
+  PHN_ISLAND_ENERGY = 1,    /* energy density rho(x) > thres, rho the summand of <E> */
+  PHN_ISLAND_DELTA = 2      /* EnergybasedID 1 (islands.cpp:82-83): Delta(x) > thres, Delta the per-site
+                               energy density of withEnergyPS 1 (fieldanalysis.cpp:446-560: 0.5 Pi^2, the
+                               full squared forward differences, the potential); the peak and its value by
+                               Delta (islands.cpp:113-114, 259-260).  Theories 2-5, as the reference compiles
+                               it; the reference's Full_Analysis takes thres = 4 <rho> (islands.cpp:783-786) */
 };
 
 /* Run parameters, in the reference's own terms (parameters.cpp:84-201). */
@@ -165,6 +170,16 @@ int phn_spectrum_bins(const phn_handle *h, int *nbins, double *binsize);
  * momentumspace.cpp:140-278) on the current state: TotalCorrF/K/Q[bin*Nc+a]
  * and TotalBCounts[bin].  Arrays hold nbins*Nc (F, K, Q) and nbins (counts). */
 int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, int nbins);
+/* The density-contrast spectrum of Calculate_CorrelationFunctions with
+ * withEnergyPS 1 (momentumspace.cpp:165-183, 191, 233-270): Delta of every
+ * component at every site (fieldanalysis.cpp:446-560), Aavden = its sum over
+ * components and sites / N^3, the contrast (Delta - Aavden) / Aavden, and
+ * its binned power D[bin*Nc + a] = TotalCorrD with phn_spectrum's modes,
+ * weights and a^3 a^3 factor; counts as phn_spectrum's.  Theories 2-5, for
+ * which the reference compiles it.  The fields are not changed (the reference
+ * overwrites its Delta array with the contrast). */
+int phn_spectrum_energy(phn_handle *h, double *D, int *counts, int nbins);
+
 /* The configuration's radial spectrum (no reference counterpart): the modes,
  * weights and sums of phn_spectrum, binned uniformly in the lattice momentum
  * |p| on [0, p_max], p_max = 2 sqrt(3) / a (pTmax of momentumspace.cpp:43):

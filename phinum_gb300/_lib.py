@@ -16,7 +16,7 @@ MAX_NC = 4
 OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_NOMEM, ERR_UNSUPPORTED, ERR_TRUNCATED = \
     0, -1, -2, -3, -4, -5, -6, -7
 FP64, FP32, FP32_KAHAN, FP32_PAIR = 0, 1, 2, 3
-ISLAND_REFERENCE, ISLAND_ENERGY = 0, 1
+ISLAND_REFERENCE, ISLAND_ENERGY, ISLAND_DELTA = 0, 1, 2
 PATH_AUTO, PATH_PLAIN, PATH_TMA, PATH_X4 = 0, 1, 2, 3
 TRACK_ALIVE, TRACK_RETIRED, TRACK_BUBBLES = 0, 1, 2
 FILTER_TOPHAT, FILTER_GAUSSIAN, FILTER_TABLE, FILTER_KTOPHAT = 0, 1, 2, 3
@@ -92,6 +92,7 @@ _SIGS = {
     "phn_spectrum_bins": (_I, [ctypes.c_void_p, _PI, _PD]),
     "phn_spectrum": (_I, [ctypes.c_void_p, _PD, _PD, _PD, _PI, _I]),
     "phn_spectrum_uniform": (_I, [ctypes.c_void_p, _I, _PD, _PD, _PD, _PI]),
+    "phn_spectrum_energy": (_I, [ctypes.c_void_p, _PD, _PI, _I]),
     "phn_initial_conditions": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams)]),
     "phn_initial_conditions_mode": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams), ctypes.POINTER(PhnIcMode)]),
     "phn_islands_lookup": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _I, _PI]),

@@ -36,6 +36,7 @@
 
 #include "ccl_math.h"
 #include "phn_internal.h"
+#include "site_terms.cuh"
 
 namespace phn {
 
@@ -69,31 +70,6 @@ __device__ __forceinline__ void site_xyz(const DivN &q, int N, size_t i, int &x,
   z = (int)zz;
 }
 
-template <typename T>
-__device__ __forceinline__ double val(const T *f, const float *comp, size_t i) {
-  double v = (double)f[i];
-  if (comp) v -= (double)comp[i];
-  return v;
-}
-
-// Site values for kernels compiled per storage: KAHAN for compensated FP32
-// fields (value = stored - compensation, in FP64), plain otherwise.  The
-// choice is a template argument: a runtime test on the compensation pointer
-// leaves the FP64 form in the plain kernels (if-converted, it issues for every
-// site on GB300's narrow FP64 pipe).
-template <bool KAHAN, typename T>
-__device__ __forceinline__ double val_k(const T *f, const float *comp, size_t i) {
-  if constexpr (KAHAN) return (double)f[i] - (double)comp[i];
-  else return (double)f[i];
-}
-
-// The same in arithmetic A (FP32 for FP32 storage: no FP64 round trip).
-template <typename A, bool KAHAN, typename T>
-__device__ __forceinline__ A val_as(const T *f, const float *comp, size_t i) {
-  if constexpr (KAHAN) return (A)((double)f[i] - (double)comp[i]);
-  else return (A)f[i];
-}
-
 // Peak key of a site: the FP64 bits of phi^2 (non-negative, so the bits
 // order like the values), or for plain FP32 fields the FP32 bits of |phi| --
 // their squares are exact in FP64, so the two keys order the sites alike and
@@ -108,82 +84,14 @@ __device__ __forceinline__ unsigned long long peak_key(const T *phi, const float
   }
 }
 
-// Potential of one single-component site, theories 0-5: the BFS PotEn
-// summand (islands.cpp:137-196), which is also the Interaction summand of
-// CalculateVolumeAverages (fieldanalysis.cpp:456-617) for Nc = 1.  The
-// expanding box's couplings come folded with the scale factor
-// (at_scale_factor); the cosine and power arguments carry it per site.
-// (FP64; the constant divisors as products by their reciprocals: these sums
-// are compared to the reference's within rounding, not bitwise.)
-__device__ __forceinline__ double site_potential(const Consts &k, double c, double c2) {
-  const double l2 = c2 * c2;
-  const double cos_arg = k.expansion ? sqrt(c2) * k.r_sf_sqrtm : sqrt(c2 * k.r_msq);
-  switch (k.theory) {
-    case 0:
-      return k.mm_half_M * c2 + k.lm * (l2 * k.r_c24) + (l2 * c2 * k.r_c720);
-    case 1:
-      return k.h * c + k.mm_half_M * c2 + k.lm * (l2 * k.r_c24);
-    case 2:
-      return k.msq2 * (1. - cos(cos_arg));
-    case 3:
-      return 0.5 * k.mmono * c2 + k.msq2 * (1. - cos(cos_arg));
-    case 4:
-      return k.mm_half_M * c2 - k.g * c2 * c * (1.0 / 6.0) + k.lm * (l2 * k.r_c24);
-    default:
-      return k.t5c * (pow(1. + (k.expansion ? c2 / k.msq_sf2 : c2 * k.r_msq), k.p_mono) - 1.);
-  }
+// Keys that order like the values for every sign (the peak of Delta).
+__device__ __forceinline__ unsigned ordered_key(float v) {
+  const unsigned u = __float_as_uint(v);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
-
-// The same in FP32, from the FP32 forms of the couplings (those of the FP32
-// observation): island statistics of FP32 fields.
-__device__ __forceinline__ float site_potential(const Consts &k, float c, float c2) {
-  const float l2 = c2 * c2;
-  switch (k.theory) {
-    case 0:
-      return fmaf(k.e6_f, l2 * c2, fmaf(k.e4_f, l2, k.mmh_f * c2));
-    case 1:
-      return fmaf(k.h_f, c, fmaf(k.e4_f, l2, k.mmh_f * c2));
-    case 2:
-      return k.msq2_f * (1.f - cosf(sqrtf(c2 * k.inv_m_f)));
-    case 3:
-      return fmaf(k.mono_half_f, c2, k.msq2_f * (1.f - cosf(sqrtf(c2 * k.inv_m_f))));
-    case 4:
-      return fmaf(-k.g6_f * c, c2, fmaf(k.e4_f, l2, k.mmh_f * c2));
-    default:
-      return k.t5c_f * (powf(fmaf(c2, k.inv_m_f, 1.f), k.p_f) - 1.f);
-  }
-}
-
-// Kinetic summand, with the expanding box's H0/sf terms (islands.cpp:133-138,
-// fieldanalysis.cpp:626-629).
-__device__ __forceinline__ double site_kinetic(const Consts &k, double c, double p) {
-  if (!k.expansion) return 0.5 * (p * p);
-  const double hub = k.H0 / k.sf;
-  return (0.5 * (p * p) + 0.5 * (hub * hub) * (c * c) - c * p * k.H0 / k.sf);
-}
-
-__device__ __forceinline__ float site_kinetic(const Consts &k, float c, float p) {
-  if (!k.expansion) return 0.5f * (p * p);
-  const float hub = (float)(k.H0 / k.sf);
-  return fmaf(0.5f * (hub * hub) * c, c, fmaf(0.5f * p, p, -c * p * hub));
-}
-
-// Per-site energy density: the summand of the reference's Energy
-// (fieldanalysis.cpp:437-471,571-579), Nc = 1, in arithmetic A: FP64 for FP64
-// fields, FP32 for FP32 fields (their values carry FP32 rounding already; a
-// site within that of the threshold is on either side).
-template <typename A, bool KAHAN, typename T>
-__device__ A site_rho(const T *phi, const float *cphi, const T *pi, const float *cpi, int N, int x, int y, int z,
-                      const Consts k) {
-  const size_t NN = (size_t)N * N;
-  const size_t i = (size_t)z * NN + (size_t)y * N + x;
-  const A c = val_as<A, KAHAN>(phi, cphi, i), p = val_as<A, KAHAN>(pi, cpi, i);
-  const A fx = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)y * N + (x + 1 == N ? 0 : x + 1));
-  const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
-  const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
-  const A c2 = c * c;
-  const A grad = (((fx - c) * (fx - c) + (fy - c) * (fy - c)) + (fz - c) * (fz - c)) * (A)k.inv_a2;
-  return site_kinetic(k, c, p) + (A)0.5 * grad + site_potential(k, c, c2);
+__device__ __forceinline__ unsigned long long ordered_key(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
 // islands.cpp:76 in FP64; the FP32 form is the rare path of plain FP32 fields
@@ -215,6 +123,7 @@ __device__ __forceinline__ bool site_mask(const T *__restrict__ phi, const float
     }
   }
   using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+  if (mode == PHN_ISLAND_DELTA) return site_delta<A, KAHAN>(phi, cphi, pi, cpi, N, x, y, z, k) > (A)thr;
   return site_rho<A, KAHAN>(phi, cphi, pi, cpi, N, x, y, z, k) > (A)thr;
 }
 
@@ -759,7 +668,7 @@ template <typename T, bool KAHAN>
 __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ phi, const float *__restrict__ cphi,
                                                         const T *__restrict__ pi, const float *__restrict__ cpi,
                                                         const int *__restrict__ parent, const int *__restrict__ ids,
-                                                        int N, const DivN dn, const Consts k,
+                                                        int N, const DivN dn, const Consts k, int dpeak,
                                                         int *__restrict__ size,
                                                         double *__restrict__ sums,
                                                         unsigned long long *__restrict__ peak2) {
@@ -793,12 +702,12 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ p
       const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
       const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
       // BFS accumulators (islands.cpp:131-198)
-      grad = (A)0.5 * ((fx - c) * (fx - c) + (fy - c) * (fy - c) + (fz - c) * (fz - c)) * (A)k.inv_a2;
+      grad = grad_half(c, fx, fy, fz, (A)k.inv_a2);
       kin = site_kinetic(k, c, p);
       pot = site_potential(k, c, c * c);
       cs = c;
       n = 1;
-      pk = peak_key<KAHAN>(phi, cphi, i);
+      pk = dpeak ? ordered_key((double)delta_of<A>(kin, grad, pot)) : peak_key<KAHAN>(phi, cphi, i);
     }
     const int prev = __shfl_up_sync(full, id, 1);
     const unsigned heads = __ballot_sync(full, lane == 0 || prev != id);
@@ -941,7 +850,7 @@ template <typename T, bool KAHAN>
 __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ phi, const float *__restrict__ cphi,
                                                          const T *__restrict__ pi, const float *__restrict__ cpi,
                                                          const int *__restrict__ parent, const int *__restrict__ ids,
-                                                         int N, const DivN dn, const Consts k,
+                                                         int N, const DivN dn, const Consts k, int dpeak,
                                                          int *__restrict__ size, double *__restrict__ sums,
                                                          unsigned long long *__restrict__ peak2) {
   using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
@@ -993,17 +902,16 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ 
           const A cj = c[j], fx = j < 3 ? c[j + 1] : fx3;
           RunSums<A> t;
           // BFS accumulators (islands.cpp:131-198)
-          t.grad = (A)0.5 * ((fx - cj) * (fx - cj) + (fy[j] - cj) * (fy[j] - cj) + (fz[j] - cj) * (fz[j] - cj)) *
-                   (A)k.inv_a2;
+          t.grad = grad_half(cj, fx, fy[j], fz[j], (A)k.inv_a2);
           t.kin = site_kinetic(k, cj, p[j]);
           t.pot = site_potential(k, cj, cj * cj);
           t.cs = cj;
           t.n = 1;
           if constexpr (PACKED) {
-            t.pk = ((unsigned long long)__float_as_uint(fabsf(cj)) << 32) |
-                   (unsigned long long)(0xffffffffu - (unsigned)(i0 + j));
+            const unsigned key = dpeak ? ordered_key(delta_of<A>(t.kin, t.grad, t.pot)) : __float_as_uint(fabsf(cj));
+            t.pk = ((unsigned long long)key << 32) | (unsigned long long)(0xffffffffu - (unsigned)(i0 + j));
           } else {
-            t.pk = peak_key<KAHAN>(phi, cphi, i0 + j);
+            t.pk = dpeak ? ordered_key((double)delta_of<A>(t.kin, t.grad, t.pot)) : peak_key<KAHAN>(phi, cphi, i0 + j);
           }
           if (!gap) {
             run_add(L, t);
@@ -1062,26 +970,49 @@ __global__ void ccl_peak_unpack(const unsigned long long *__restrict__ peak2, in
     peakpos[j] = (long long)(0xffffffffu - (unsigned)(peak2[j] & 0xffffffffull)) + NN;
 }
 
+// Delta of site i from the BFS summands, as the statistics kernels form it.
 template <typename T, bool KAHAN>
-__global__ void ccl_peak(const T *__restrict__ phi, const float *__restrict__ cphi, const int *__restrict__ parent,
-                         const int *__restrict__ ids, int N, const unsigned long long *__restrict__ peak2,
-                         long long *__restrict__ peakpos) {
+__device__ __forceinline__ double site_delta_stats(const T *phi, const float *cphi, const T *pi, const float *cpi,
+                                                   int N, const DivN &dn, const Consts &k, size_t i) {
+  using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+  int x, y, z;
+  site_xyz(dn, N, i, x, y, z);
+  const size_t NN = (size_t)N * N;
+  const A c = val_as<A, KAHAN>(phi, cphi, i), p = val_as<A, KAHAN>(pi, cpi, i);
+  const A fx = val_as<A, KAHAN>(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
+  const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
+  const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
+  return (double)delta_of<A>(site_kinetic(k, c, p), grad_half(c, fx, fy, fz, (A)k.inv_a2),
+                             site_potential(k, c, c * c));
+}
+
+// The sites that hold each island's peak key; dpeak: the key of Delta.
+template <typename T, bool KAHAN>
+__global__ void ccl_peak(const T *__restrict__ phi, const float *__restrict__ cphi, const T *__restrict__ pi,
+                         const float *__restrict__ cpi, const int *__restrict__ parent, const int *__restrict__ ids,
+                         int N, const DivN dn, const Consts k, int dpeak,
+                         const unsigned long long *__restrict__ peak2, long long *__restrict__ peakpos) {
   const size_t V = (size_t)N * N * N, NN = (size_t)N * N;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
     const int r = parent[i];
     if (r < 0) continue;
     const int id = ids[r];
-    if (peak_key<KAHAN>(phi, cphi, i) == peak2[id])
-      atomicMin(&peakpos[id], (long long)(i + NN));  // reference index (Nc = 1)
+    const unsigned long long key =
+        dpeak ? ordered_key(site_delta_stats<T, KAHAN>(phi, cphi, pi, cpi, N, dn, k, i)) : peak_key<KAHAN>(phi, cphi, i);
+    if (key == peak2[id]) atomicMin(&peakpos[id], (long long)(i + NN));  // reference index (Nc = 1)
   }
 }
 
-template <typename T>
-__global__ void ccl_peakval(const T *__restrict__ phi, const float *__restrict__ cphi, int N, int n,
+// Peak_value: phi at the peak (islands.cpp:256-258), or Delta there (:259-260).
+template <typename T, bool KAHAN>
+__global__ void ccl_peakval(const T *__restrict__ phi, const float *__restrict__ cphi, const T *__restrict__ pi,
+                            const float *__restrict__ cpi, int N, const DivN dn, const Consts k, int dpeak, int n,
                             const long long *__restrict__ peakpos, double *__restrict__ peakval) {
   const size_t NN = (size_t)N * N;
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-    peakval[j] = val(phi, cphi, (size_t)peakpos[j] - NN);
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const size_t i = (size_t)peakpos[j] - NN;
+    peakval[j] = dpeak ? site_delta_stats<T, KAHAN>(phi, cphi, pi, cpi, N, dn, k, i) : val(phi, cphi, i);
+  }
 }
 
 // labels in the reference layout: ghost slabs -1, interior island ids
@@ -1289,29 +1220,37 @@ static int run_islands(phn_handle *h, const T *phi, const T *pi, double thres, i
       h->launches++;
     }
     const unsigned sb = (unsigned)((V + STATS_SITES - 1) / STATS_SITES);
+    const int dpeak = mode == PHN_ISLAND_DELTA;
     if (x4) {
       if (cphi)
-        ccl_stats4<T, true><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
-                                                        s->sums, s->peak2);
+        ccl_stats4<T, true><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, dpeak,
+                                                        s->size, s->sums, s->peak2);
       else
-        ccl_stats4<T, false><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
-                                                         s->sums, s->peak2);
+        ccl_stats4<T, false><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, dpeak,
+                                                         s->size, s->sums, s->peak2);
     } else {
       if (cphi)
-        ccl_stats<T, true><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
-                                                       s->sums, s->peak2);
+        ccl_stats<T, true><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, dpeak,
+                                                       s->size, s->sums, s->peak2);
       else
-        ccl_stats<T, false><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, s->size,
-                                                        s->sums, s->peak2);
+        ccl_stats<T, false><<<sb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, dpeak,
+                                                        s->size, s->sums, s->peak2);
     }
     if (packed) {
       ccl_peak_unpack<<<(count + 255) / 256, 256, 0, st>>>(s->peak2, count, (long long)N * N, s->peakpos);
     } else if (cphi) {
-      ccl_peak<T, true><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
+      ccl_peak<T, true><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, dpeak, s->peak2,
+                                                    s->peakpos);
     } else {
-      ccl_peak<T, false><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, s->parent, s->ids, N, s->peak2, s->peakpos);
+      ccl_peak<T, false><<<gb, CCL_THREADS, 0, st>>>(phi, cphi, pi, cpi, s->parent, s->ids, N, dn, k, dpeak, s->peak2,
+                                                     s->peakpos);
     }
-    ccl_peakval<T><<<(count + 255) / 256, 256, 0, st>>>(phi, cphi, N, count, s->peakpos, s->peakval);
+    if (cphi)
+      ccl_peakval<T, true><<<(count + 255) / 256, 256, 0, st>>>(phi, cphi, pi, cpi, N, dn, k, dpeak, count,
+                                                                s->peakpos, s->peakval);
+    else
+      ccl_peakval<T, false><<<(count + 255) / 256, 256, 0, st>>>(phi, cphi, pi, cpi, N, dn, k, dpeak, count,
+                                                                 s->peakpos, s->peakval);
     h->launches += 3;
   }
   if (labels) {
@@ -1417,7 +1356,11 @@ extern "C" int phn_islands(phn_handle *h, double thres, int mode, int z_periodic
                            int max_out, int *n_islands) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
   if (h->p.Nc != 1) return set_error(PHN_ERR_UNSUPPORTED, "islands need Nc == 1");
-  if (mode != PHN_ISLAND_REFERENCE && mode != PHN_ISLAND_ENERGY) return set_error(PHN_ERR_INVALID, "mode %d", mode);
+  if (mode != PHN_ISLAND_REFERENCE && mode != PHN_ISLAND_ENERGY && mode != PHN_ISLAND_DELTA)
+    return set_error(PHN_ERR_INVALID, "mode %d", mode);
+  if (mode == PHN_ISLAND_DELTA && h->p.potential < 2)
+    return set_error(PHN_ERR_UNSUPPORTED, "the Delta mask has no form for theory %d (the reference's withEnergyPS "
+                     "build compiles for theories 2-5)", h->p.potential);
   if (h->V > (size_t)0x7fffffff) return set_error(PHN_ERR_UNSUPPORTED, "lattice too large for 32-bit labels");
   if (max_out < 0) return set_error(PHN_ERR_INVALID, "max_out < 0");
   if (h->p.precision == PHN_FP64)
@@ -1431,7 +1374,10 @@ extern "C" int phn_islands_device(phn_handle *h, double thres, int mode, int z_p
                                   const phn_island **d_records, int *n_islands) {
   if (!h || !d_records || !n_islands) return set_error(PHN_ERR_INVALID, "bad argument");
   if (h->p.Nc != 1) return set_error(PHN_ERR_UNSUPPORTED, "islands need Nc == 1");
-  if (mode != PHN_ISLAND_REFERENCE && mode != PHN_ISLAND_ENERGY) return set_error(PHN_ERR_INVALID, "mode %d", mode);
+  if (mode != PHN_ISLAND_REFERENCE && mode != PHN_ISLAND_ENERGY && mode != PHN_ISLAND_DELTA)
+    return set_error(PHN_ERR_INVALID, "mode %d", mode);
+  if (mode == PHN_ISLAND_DELTA && h->p.potential < 2)
+    return set_error(PHN_ERR_UNSUPPORTED, "the Delta mask has no form for theory %d", h->p.potential);
   if (h->V > (size_t)0x7fffffff) return set_error(PHN_ERR_UNSUPPORTED, "lattice too large for 32-bit labels");
   if (h->p.precision == PHN_FP64)
     return run_islands<double>(h, (const double *)h->phi[h->cur], (const double *)h->pi, thres, mode, z_periodic,

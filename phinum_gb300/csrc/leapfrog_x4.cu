@@ -29,9 +29,9 @@ struct X4Variant {
   int w, cz;
   bool persistent;
 };
-constexpr X4Variant kX4Variants[] = {{8, 32, true}, {8, 16, true}, {4, 32, true},
-                                     {8, 16, false}, {8, 8, false}, {4, 16, false}};
-constexpr int kNumX4Variants = 6;
+constexpr X4Variant kX4Variants[] = {{8, 32, true}, {8, 16, true}, {4, 32, true}, {8, 16, false},
+                                     {8, 8, false},  {4, 16, false}, {8, 32, false}};
+constexpr int kNumX4Variants = 7;
 
 // Observation sums of the x4 kernel (theories 0 and 1, one component).  The
 // four sites of a thread's plane row add to plain FP32 moments with FMAs --
@@ -409,10 +409,19 @@ bool x4_supported(const phn_params &p) {
 
 int x4_num_variants() { return kNumX4Variants; }
 
-// Observation steps run the plain step's own variant: with the moment sums
-// a block record costs little, so a one-block-per-item grid folds its
-// (many) records in finalize_averages without a persistent grid.
-int x4_obs_variant(int variant) { return variant; }
+// Observation steps run a one-item-per-block grid of the plain variant's
+// width with the most planes per item: every block ends in one record (a
+// block tree), so the fewer and longer the items, the less that costs (at
+// 512^3: 4096 records of 32 planes against 16384 of 8), and the threads'
+// totals need no compensation (128 sites each).
+int x4_obs_variant(int variant) {
+  int best = -1;
+  for (int v = 0; v < kNumX4Variants; ++v)
+    if (!kX4Variants[v].persistent && kX4Variants[v].w == kX4Variants[variant].w &&
+        (best < 0 || kX4Variants[v].cz > kX4Variants[best].cz))
+      best = v;
+  return best >= 0 ? best : variant;
+}
 
 static int x4_items(int N, const X4Variant &v) {
   const int cz = v.cz < N ? v.cz : N;

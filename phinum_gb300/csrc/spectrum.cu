@@ -32,10 +32,12 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <type_traits>
 #include <vector>
 
 #include "phn_internal.h"
+#include "site_terms.cuh"
 
 namespace phn {
 
@@ -53,10 +55,14 @@ struct SpecState {
   int *flag;               // bin overflow flag (device)
   unsigned short *keys;    // [N][N/2+1][N] bin | weight bit per mode (reference rule)
   int nblocks, nbins;
+  int rblocks;             // bin_runs' grid (more, smaller blocks than bin_sums')
   double binsize;
   std::vector<int> h_counts;
   bool counts_ok;
   bool mono, u_mono;       // the key tables' rows are monotone per half (bin_runs applies)
+  // density-contrast spectrum (phn_spectrum_energy), allocated on first use
+  void *dfield;            // [Nc][V] Delta, then its contrast (the field's precision)
+  double *dsum;            // [nblocks] per-block sums of Delta, then [nblocks] the mean
   // uniform-bin (configuration) mode, allocated on first use
   int u_nbins;
   double *u_partials, *u_bins;
@@ -254,18 +260,19 @@ __global__ void __launch_bounds__(SPEC_THREADS) bin_sums(const C *__restrict__ f
 // monotone in px on each half -- non-decreasing on [0, N/2) where |p_x|
 // grows, non-increasing on [N/2, N) where it falls (checked per key table by
 // keys_monotone; bin_sums serves a table that fails the check).  A warp walks
-// a half row in chunks of 32 lanes x RUN_Q consecutive modes: the chunk's
-// modes are loaded coalesced into shared memory (|Phi|^2, |Pi|^2,
-// Re(Phi Pi*) and the bin of each), then every lane sums the runs of equal
-// bins in its RUN_Q modes in registers.  A run inside a lane's modes has a
-// bin no other lane of the chunk holds (monotone bins), so it adds to the
-// warp histogram without a conflict; the runs that cross lanes join in one
-// segmented scan per chunk (once per 256 modes, against once per 32 in
-// bin_sums), and each closes in one lane.  The order of every addition is
-// fixed, so the sums are the same run to run.
+// a half row in chunks of 32 lanes x RUN_Q consecutive modes; each lane
+// loads its own RUN_Q modes (keys and both spectra: 3 RUN_Q independent
+// loads in flight, contiguous per lane, so the lines the warp touches serve
+// it from L1) and sums the runs of equal bins in registers.  A run inside a
+// lane's modes has a bin no other lane of the chunk holds (monotone bins),
+// so it adds to the warp histogram without a conflict; the runs that cross
+// lanes join in one segmented scan per chunk (once per 256 modes, against
+// once per 32 in bin_sums), and each closes in one lane.  The order of every
+// addition is fixed, so the sums are the same run to run.
 constexpr int RUN_Q = 8;
-constexpr int RUN_WARPS = 4;  // 128 threads: the histograms of up to 1024 bins and the stage fit twice per SM
+constexpr int RUN_WARPS = 4;  // 128 threads: histograms of up to 1024 bins
 constexpr int RUN_THREADS = 32 * RUN_WARPS;
+constexpr int RUN_BLOCKS_PER_SM = 6;  // the resident blocks at 80 registers
 
 __device__ __forceinline__ void run_flush(CompF *hF, CompF *hK, CompF *hQ, int bin, float f, float k, float q) {
   hist_add(hF[bin], f);
@@ -273,17 +280,15 @@ __device__ __forceinline__ void run_flush(CompF *hF, CompF *hK, CompF *hQ, int b
   hist_add(hQ[bin], q);
 }
 
-__global__ void __launch_bounds__(RUN_THREADS) bin_runs(const float2 *__restrict__ fphi, const float2 *__restrict__ fpi,
+__global__ void __launch_bounds__(RUN_THREADS, 6) bin_runs(const float2 *__restrict__ fphi, const float2 *__restrict__ fpi,
                                                        const unsigned short *__restrict__ keys, int N, int nbins,
                                                        double *__restrict__ partials) {
   extern __shared__ double run_mem[];
-  CompF *hist = (CompF *)run_mem;                                  // [RUN_WARPS][3][nbins]
-  float4 *stage_all = (float4 *)(run_mem + RUN_WARPS * 3 * nbins);  // [RUN_WARPS][32][RUN_Q + 1]
+  CompF *hist = (CompF *)run_mem;  // [RUN_WARPS][3][nbins]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < RUN_WARPS * 3 * nbins; i += RUN_THREADS) hist_zero(hist[i]);
   __syncthreads();
   CompF *hF = hist + (size_t)warp * 3 * nbins, *hK = hF + nbins, *hQ = hK + nbins;
-  float4 *stage = stage_all + (size_t)warp * 32 * (RUN_Q + 1);
   const unsigned full = 0xffffffffu;
   const int h = N / 2, M = N / 2 + 1;
   const int nrows = M * N;
@@ -296,36 +301,36 @@ __global__ void __launch_bounds__(RUN_THREADS) bin_runs(const float2 *__restrict
       const int x1 = half ? N : h;
       for (int c0 = half ? h : 0; c0 < x1; c0 += 32 * RUN_Q) {
         const int cn = min(32 * RUN_Q, x1 - c0);
-        // the chunk's modes, coalesced, into lane-contiguous stage slots
+        // the lane's modes, loaded together
+        const int nm = max(0, min(RUN_Q, cn - lane * RUN_Q));
+        const int px0 = c0 + lane * RUN_Q;
+        unsigned kk[RUN_Q];
+        float2 va[RUN_Q], vb[RUN_Q];
 #pragma unroll
-        for (int u = 0; u < RUN_Q; ++u) {
-          const int j = u * 32 + lane;
-          if (j < cn) {
-            const int px = c0 + j;
-            const unsigned kk = keys[krow + px];
-            const long long m = px <= h ? direct + px : mirror - px;
-            const float2 va = fphi[m], vb = fpi[m];
-            float f = mag2v(va), k = mag2v(vb), q = dotv(va, vb);
-            if (kk & KEY_WEIGHT2) {  // exact doubling
-              f += f;
-              k += k;
-              q += q;
-            }
-            stage[(j / RUN_Q) * (RUN_Q + 1) + (j % RUN_Q)] = make_float4(f, k, q, __int_as_float((int)(kk & KEY_BIN)));
+        for (int m = 0; m < RUN_Q; ++m) {
+          if (m < nm) {
+            const int px = px0 + m;
+            kk[m] = keys[krow + px];
+            const long long mi = px <= h ? direct + px : mirror - px;
+            va[m] = fphi[mi];
+            vb[m] = fpi[mi];
           }
         }
-        __syncwarp();
         // runs of the lane's modes: the first (fb), the interior ones
         // (flushed here), the last (lb; the whole segment when through)
-        const int nm = max(0, min(RUN_Q, cn - lane * RUN_Q));
         int fb = -1, cur = -1;
         float F0 = 0.f, F1 = 0.f, F2 = 0.f, a0 = 0.f, a1 = 0.f, a2 = 0.f;
         bool first_open = true;
 #pragma unroll
         for (int m = 0; m < RUN_Q; ++m) {
           if (m < nm) {
-            const float4 e = stage[lane * (RUN_Q + 1) + m];
-            const int b = __float_as_int(e.w);
+            float f = mag2v(va[m]), k = mag2v(vb[m]), q = dotv(va[m], vb[m]);
+            if (kk[m] & KEY_WEIGHT2) {  // exact doubling
+              f += f;
+              k += k;
+              q += q;
+            }
+            const int b = (int)(kk[m] & KEY_BIN);
             if (b != cur) {
               if (cur >= 0) {
                 if (first_open) {
@@ -339,20 +344,20 @@ __global__ void __launch_bounds__(RUN_THREADS) bin_runs(const float2 *__restrict
                 }
               }
               cur = b;
-              a0 = e.x;
-              a1 = e.y;
-              a2 = e.z;
+              a0 = f;
+              a1 = k;
+              a2 = q;
             } else {
-              a0 += e.x;
-              a1 += e.y;
-              a2 += e.z;
+              a0 += f;
+              a1 += k;
+              a2 += q;
             }
           }
         }
         const int lb = cur;
         const bool through = nm > 0 && first_open;
         if (through) fb = lb;
-        __syncwarp();  // interior runs added; the stage is free for the next chunk after this one
+        __syncwarp();  // interior runs added
         // runs across lanes: carry C = the run through the lane's last mode
         const int lb_prev = __shfl_up_sync(full, lb, 1);
         const bool conn = lane > 0 && nm > 0 && lb_prev >= 0 && fb == lb_prev;
@@ -431,6 +436,59 @@ __global__ void __launch_bounds__(256) fold_blocks(const double *__restrict__ pa
   if (threadIdx.x == 0) out[j] = sh[0] * scale;
 }
 
+// Delta of component a at every site (site_delta: kinetic, the full squared
+// forward differences, Delta's potential), into out[], and per block the FP64
+// sum of the block's values (each thread's values summed in FP32 pairs
+// first).  A thread walks sites i = t, t + T, ... of the grid's T threads.
+template <typename T, bool KAHAN>
+__global__ void __launch_bounds__(SPEC_THREADS) delta_field(const T *__restrict__ phi, const float *__restrict__ cphi,
+                                                           const T *__restrict__ pi, const float *__restrict__ cpi,
+                                                           int N, const Consts k, T *__restrict__ out,
+                                                           double *__restrict__ bsum) {
+  using A = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+  const size_t NN = (size_t)N * N, V = NN * N;
+  A hi = 0, lo = 0;
+  for (size_t i = blockIdx.x * (size_t)SPEC_THREADS + threadIdx.x; i < V; i += (size_t)gridDim.x * SPEC_THREADS) {
+    const int z = (int)(i / NN), y = (int)((i - (size_t)z * NN) / N), x = (int)(i - (size_t)z * NN - (size_t)y * N);
+    const A d = site_delta<A, KAHAN>(phi, cphi, pi, cpi, N, x, y, z, k);
+    out[i] = (T)d;
+    const A t = hi + d, bb = t - hi;  // TwoSum
+    lo += (hi - (t - bb)) + (d - bb);
+    hi = t;
+  }
+  __shared__ double sh[SPEC_THREADS];
+  sh[threadIdx.x] = (double)hi + (double)lo;
+  __syncthreads();
+  for (int w = SPEC_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < (unsigned)w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) bsum[blockIdx.x] += sh[0];
+}
+
+// Aavden = (sum of Delta over every component and site) / N^3
+// (momentumspace.cpp:165-176), in a fixed order; into *mean.
+__global__ void delta_mean(const double *__restrict__ bsum, int nblocks, int N, double *__restrict__ mean) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += bsum[b];
+    *mean = s / ((double)N * (double)N * (double)N);
+  }
+}
+
+// The density contrast (Delta - Aavden) / Aavden in the field's precision
+// (momentumspace.cpp:177-181).
+template <typename T>
+__global__ void delta_contrast(T *__restrict__ f, size_t n, const double *__restrict__ mean) {
+  const T m = (T)*mean;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    T v = f[i];
+    v -= m;
+    v /= m;
+    f[i] = v;
+  }
+}
+
 void spectrum_release(phn_handle *h) {
   SpecState *s = (SpecState *)h->spec;
   if (!s) return;
@@ -447,6 +505,8 @@ void spectrum_release(phn_handle *h) {
   cudaFree(s->u_bins);
   cudaFree(s->u_counts);
   cudaFree(s->u_keys);
+  cudaFree(s->dfield);
+  cudaFree(s->dsum);
   delete s;
   h->spec = nullptr;
 }
@@ -487,10 +547,8 @@ static int build_keys(phn_handle *h, unsigned short *keys, int *counts, int nbin
   return PHN_OK;
 }
 
-// Shared memory of bin_runs: the warp histograms and the mode stages.
-static size_t run_smem(int nbins) {
-  return (size_t)RUN_WARPS * 3 * nbins * sizeof(double) + (size_t)RUN_WARPS * 32 * (RUN_Q + 1) * sizeof(float4);
-}
+// Shared memory of bin_runs: the warp histograms.
+static size_t run_smem(int nbins) { return (size_t)RUN_WARPS * 3 * nbins * sizeof(double); }
 
 static int spec_init(phn_handle *h) {
   if (h->spec) return PHN_OK;
@@ -499,6 +557,7 @@ static int spec_init(phn_handle *h) {
   const int N = h->p.N;
   bin_geometry(h->p, &s->nbins, &s->binsize);
   s->nblocks = 152 * 4;
+  s->rblocks = 152 * RUN_BLOCKS_PER_SM;
   const size_t ncomplex = (size_t)N * N * (N / 2 + 1);
   const bool dbl = h->p.precision == PHN_FP64;
   const size_t csize = dbl ? sizeof(double2) : sizeof(float2);
@@ -511,7 +570,7 @@ static int spec_init(phn_handle *h) {
   CKS(cudaMalloc(&s->fphi, ncomplex * csize));
   CKS(cudaMalloc(&s->fpi, ncomplex * csize));
   CKS(cudaMalloc(&s->ptab, N * sizeof(double)));
-  CKS(cudaMalloc(&s->partials, (size_t)s->nblocks * 3 * s->nbins * sizeof(double)));
+  CKS(cudaMalloc(&s->partials, (size_t)std::max(s->nblocks, s->rblocks) * 3 * s->nbins * sizeof(double)));
   CKS(cudaMalloc(&s->bins, (size_t)3 * s->nbins * sizeof(double)));
   CKS(cudaMalloc(&s->counts, (size_t)s->nbins * sizeof(int)));
   CKS(cudaMalloc(&s->flag, sizeof(int)));
@@ -537,6 +596,9 @@ static int spec_init(phn_handle *h) {
 
 // One component: R2C of phi and pi, the binned sums, the three bin arrays
 // into hb ([3][nbins], scaled by a^3 a^3).
+static int bin_spectra(phn_handle *h, const void *fa, const void *fb, const unsigned short *keys, int nbins,
+                       double *partials, double *bins, double scale, bool mono, std::vector<double> &hb);
+
 static int spectrum_component(phn_handle *h, int a, const unsigned short *keys, int nbins, double *partials,
                               double *bins, double scale, bool mono, std::vector<double> &hb) {
   SpecState *s = (SpecState *)h->spec;
@@ -553,19 +615,30 @@ static int spectrum_component(phn_handle *h, int a, const unsigned short *keys, 
     if (fr == CUFFT_SUCCESS) fr = cufftExecR2C(s->plan, pi, (cufftComplex *)s->fpi);
   }
   if (fr != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cuFFT exec failed (%d)", (int)fr);
+  return bin_spectra(h, s->fphi, s->fpi, keys, nbins, partials, bins, scale, mono, hb);
+}
+
+// The binned sums of two half-spectra (F from the first, K from the second,
+// Q from both) into hb ([3][nbins], scaled).
+static int bin_spectra(phn_handle *h, const void *fa, const void *fb, const unsigned short *keys, int nbins,
+                       double *partials, double *bins, double scale, bool mono, std::vector<double> &hb) {
+  SpecState *s = (SpecState *)h->spec;
+  const int N = h->p.N;
+  const bool dbl = h->p.precision == PHN_FP64;
   const size_t smem = (size_t)SPEC_WARPS * 3 * nbins * sizeof(double);
   if (dbl)
     bin_sums<double2, double><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-        (const double2 *)s->fphi, (const double2 *)s->fpi, keys, N, nbins, partials);
+        (const double2 *)fa, (const double2 *)fb, keys, N, nbins, partials);
   else if (mono)
-    bin_runs<<<s->nblocks, RUN_THREADS, run_smem(nbins), h->stream>>>((const float2 *)s->fphi, (const float2 *)s->fpi,
-                                                                     keys, N, nbins, partials);
+    bin_runs<<<s->rblocks, RUN_THREADS, run_smem(nbins), h->stream>>>((const float2 *)fa, (const float2 *)fb, keys, N,
+                                                                     nbins, partials);
   else
     bin_sums<float2, float><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
-        (const float2 *)s->fphi, (const float2 *)s->fpi, keys, N, nbins, partials);
+        (const float2 *)fa, (const float2 *)fb, keys, N, nbins, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "bin_sums");
-  fold_blocks<<<3 * nbins, 256, 0, h->stream>>>(partials, s->nblocks, nbins, scale, bins);
+  fold_blocks<<<3 * nbins, 256, 0, h->stream>>>(partials, (!dbl && mono) ? s->rblocks : s->nblocks, nbins, scale,
+                                                  bins);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "fold_blocks");
   h->launches += 2;
@@ -623,6 +696,83 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
   return PHN_OK;
 }
 
+int phn_spectrum_energy(phn_handle *h, double *D, int *counts, int nbins) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  if (h->p.potential < 2)
+    return set_error(PHN_ERR_UNSUPPORTED, "Delta has no form for theory %d (the reference's withEnergyPS build "
+                     "compiles for theories 2-5)", h->p.potential);
+  int r = spec_init(h);
+  if (r) {
+    spectrum_release(h);
+    return r;
+  }
+  SpecState *s = (SpecState *)h->spec;
+  if (nbins < s->nbins) return set_error(PHN_ERR_TRUNCATED, "nbins=%d < %d", nbins, s->nbins);
+  const int N = h->p.N, Nc = h->p.Nc;
+  const bool dbl = h->p.precision == PHN_FP64;
+  const size_t V = h->V, esize = dbl ? sizeof(double) : sizeof(float);
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaSuccess;
+  if (!s->dfield) {
+    e = cudaMalloc(&s->dfield, (size_t)Nc * V * esize);
+    if (e == cudaSuccess) e = cudaMalloc(&s->dsum, (size_t)(s->nblocks + 1) * sizeof(double));
+    if (e != cudaSuccess) {
+      cudaFree(s->dfield);
+      s->dfield = nullptr;
+      return cuda_error(e, "energy spectrum buffers");
+    }
+  }
+  // Delta of every component, its mean over them all, the contrast
+  const Consts k = consts_now(h);
+  const bool kahan = h->p.precision == PHN_FP32_KAHAN;
+  e = cudaMemsetAsync(s->dsum, 0, (size_t)s->nblocks * sizeof(double), st);
+  if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
+  for (int a = 0; a < Nc; ++a) {
+    const size_t o = (size_t)a * V;
+    if (dbl)
+      delta_field<double, false><<<s->nblocks, SPEC_THREADS, 0, st>>>(
+          (const double *)h->phi[h->cur] + o, nullptr, (const double *)h->pi + o, nullptr, N, k,
+          (double *)s->dfield + o, s->dsum);
+    else if (kahan)
+      delta_field<float, true><<<s->nblocks, SPEC_THREADS, 0, st>>>(
+          (const float *)h->phi[h->cur] + o, h->cphi + o, (const float *)h->pi + o, h->cpi + o, N, k,
+          (float *)s->dfield + o, s->dsum);
+    else
+      delta_field<float, false><<<s->nblocks, SPEC_THREADS, 0, st>>>(
+          (const float *)h->phi[h->cur] + o, nullptr, (const float *)h->pi + o, nullptr, N, k,
+          (float *)s->dfield + o, s->dsum);
+  }
+  double *mean = s->dsum + s->nblocks;
+  delta_mean<<<1, 32, 0, st>>>(s->dsum, s->nblocks, N, mean);
+  if (dbl)
+    delta_contrast<double><<<s->nblocks, SPEC_THREADS, 0, st>>>((double *)s->dfield, (size_t)Nc * V, mean);
+  else
+    delta_contrast<float><<<s->nblocks, SPEC_THREADS, 0, st>>>((float *)s->dfield, (size_t)Nc * V, mean);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "Delta kernels");
+  h->launches += Nc + 2;
+  // per component: R2C of the contrast and its binned power (the F sum of
+  // the binning with the same spectrum in both slots)
+  const double f3 = (h->p.a * h->p.a) * h->p.a;
+  std::vector<double> hb;
+  for (int a = 0; a < Nc; ++a) {
+    const size_t o = (size_t)a * V;
+    cufftResult fr;
+    if (dbl)
+      fr = cufftExecD2Z(s->plan, (double *)s->dfield + o, (cufftDoubleComplex *)s->fphi);
+    else
+      fr = cufftExecR2C(s->plan, (float *)s->dfield + o, (cufftComplex *)s->fphi);
+    if (fr != CUFFT_SUCCESS) return set_error(PHN_ERR_CUDA, "cuFFT exec failed (%d)", (int)fr);
+    r = bin_spectra(h, s->fphi, s->fphi, s->keys, s->nbins, s->partials, s->bins, f3 * f3, s->mono, hb);
+    if (r) return r;
+    for (int b = 0; b < s->nbins; ++b)
+      if (D) D[b * Nc + a] = hb[b];
+  }
+  if (counts)
+    for (int b = 0; b < s->nbins; ++b) counts[b] = s->h_counts[b];
+  return PHN_OK;
+}
+
 int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double *Q, int *counts) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
   if (nbins < 1 || nbins > SPEC_MAX_UNIFORM_BINS)
@@ -645,7 +795,7 @@ int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double 
     s->u_counts = nullptr;
     s->u_keys = nullptr;
     s->u_nbins = 0;
-    cudaError_t e = cudaMalloc(&s->u_partials, (size_t)s->nblocks * 3 * nbins * sizeof(double));
+    cudaError_t e = cudaMalloc(&s->u_partials, (size_t)std::max(s->nblocks, s->rblocks) * 3 * nbins * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&s->u_bins, (size_t)3 * nbins * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&s->u_counts, (size_t)nbins * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&s->u_keys, n_modes(N) * sizeof(unsigned short));

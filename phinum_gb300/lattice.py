@@ -206,6 +206,15 @@ class Lattice:
         L.check(self.lib.phn_spectrum_uniform(self.h, int(nbins), _pd(F), _pd(K), _pd(Q), _pi(C)))
         return F, K, Q, C
 
+    def spectrum_energy(self):
+        """The density-contrast spectrum (withEnergyPS 1): (D[bin*Nc + a], counts)."""
+        nb, bs = ctypes.c_int(), ctypes.c_double()
+        L.check(self.lib.phn_spectrum_bins(self.h, ctypes.byref(nb), ctypes.byref(bs)))
+        D = np.zeros(nb.value * self.p.Nc)
+        C = np.zeros(nb.value, dtype=np.int32)
+        L.check(self.lib.phn_spectrum_energy(self.h, _pd(D), _pi(C), nb.value))
+        return D, C
+
     def full_analysis(self, thres: float, mode: int = L.ISLAND_REFERENCE, z_periodic: bool = False,
                       labels: bool = True, max_out: int = 1 << 20):
         lab = np.zeros(self.p.N * self.p.N * (self.p.N + 2), dtype=np.int32) if labels else None
