@@ -311,11 +311,13 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step_x4(const float *__re
 
 // Grid of the reverse kernel (x4: a block covers 128 x-sites).  Cost model:
 // whole waves of the resident capacity times the planes a block handles
-// plus its fixed overhead (two z-halo planes, the gradient reduction).  A
-// 64-register cap (four blocks per SM) with one-wave plane counts measured
-// slower at 128^3 (18.0 ms against 14.5 ms per 1000 reverse steps): the
-// spills and the shorter z-runs cost more than the extra warps hide.
-// PHN_ADJ_CZ overrides the planes per block (tuning).
+// plus its fixed overhead (two z-halo planes, the gradient reduction); every
+// plane count from 1 to 64 is a candidate, so that the grid can fill one wave
+// of resident blocks.  At 128^3 (three blocks of 8 warps per SM) that is 5
+// planes, 416 blocks: 13.3 ms per 1000 reverse steps, against 14.8 ms for 8
+// planes (256 blocks, 0.56 of a wave), 14.7 ms for 6 and 17.1 ms for 4 (512
+// blocks, a second wave).  A 64-register cap for four blocks per SM measured
+// slower (spills).  PHN_ADJ_CZ overrides the planes per block (tuning).
 static Grid adjoint_grid(int N, bool x4) {
   Grid g;
   g.block = dim3(ADJ_TX, ADJ_TY, 1);
@@ -331,7 +333,7 @@ static Grid adjoint_grid(int N, bool x4) {
   const long long resident = (long long)sms * (occ > 0 ? occ : 1);
   int best_cz = 8;
   double best_cost = 1e300;
-  for (int cz = 1; cz <= 64 && cz <= N; cz *= 2) {
+  for (int cz = 1; cz <= 64 && cz <= N; ++cz) {
     const long long blocks = (long long)gx * gy * ((N + cz - 1) / cz);
     const double cost = (double)((blocks + resident - 1) / resident) * (cz + 2.0);
     if (cost < best_cost) {

@@ -6,9 +6,11 @@
 // products use the FMA error of the high words (Dekker's product with an
 // FMA, T. J. Dekker, Numer. Math. 18, 1971; Knuth, TAOCP vol. 2, 4.2.2), and
 // every result is renormalised with Fast2Sum.  GB300's FP64 rate is a small
-// fraction of its FP32 rate; a pair step costs about 130 FP32 operations per
-// site and reaches FP64-class accuracy (a 32^3 phi^6 run of 1000 steps stays
-// within 2e-9 of FP64, against 5e-7 for plain FP32).
+// fraction of its FP32 rate; a pair step costs about 110 FP32 operations per
+// site.  On a 32^3 phi^6 run of 1000 steps its phi is 1.7e-6 (relative L2)
+// from FP64's, against 4.7e-5 for plain FP32: the trajectory differences of a
+// chaotic field grow over the run, and the pair's come mostly from the
+// Laplacian's high-word differences (see pair_force_w).
 //
 // It serves the adjoint's forward solve: the sigmoid objective amplifies a
 // change of the final state some 400-fold into the gradient, and compensated
@@ -65,6 +67,14 @@ __device__ __forceinline__ F2 f2_madd(F2 c, F2 a, F2 b) {
   return f2_fast(s, e);
 }
 
+// a^2: the FMA error of hi^2 plus the cross term 2 hi lo.
+__device__ __forceinline__ F2 f2_sqr(F2 a) {
+  const float p = __fmul_rn(a.hi, a.hi);
+  float e = __fmaf_rn(a.hi, a.hi, -p);
+  e = __fmaf_rn(__fadd_rn(a.hi, a.hi), a.lo, e);
+  return f2_fast(p, e);
+}
+
 // The pair of a double: hi = RN(x), lo = RN(x - hi).
 __host__ __device__ inline F2 f2_of(double x) {
   F2 r;
@@ -86,7 +96,7 @@ struct PairConsts {
 // multiply-adds.
 __device__ __forceinline__ F2 pair_potential_force(const PairConsts &k, F2 c, F2 s) {
   const F2 lap = k.a2_pow2 ? F2{__fmul_rn(s.hi, k.inv_a2.hi), __fmul_rn(s.lo, k.inv_a2.hi)} : f2_mul(s, k.inv_a2);
-  const F2 l = f2_mul(c, c);
+  const F2 l = f2_sqr(c);
   F2 coef = k.c4;
   if (k.theory == 0) coef = f2_madd(k.c4, l, k.c6);
   coef = f2_madd(k.mmM, coef, l);
@@ -109,34 +119,62 @@ __device__ __forceinline__ F2 pair_force(const PairConsts &k, F2 c, const F2 nb[
 
 // The same force with the Laplacian's six differences taken word by word:
 // the high words of neighbouring sites subtract exactly (Sterbenz) wherever
-// phi keeps its sign between them, and their sum is accumulated with TwoSum;
-// the low words' differences add plainly (they are ~2^-24 of the high
-// words').  A 32^3 phi^6 run of 1000 steps stays as close to FP64 as with
-// full pair differences (1.5e-9), at a third of the Laplacian's cost.
+// phi keeps its sign between them and their differences add plainly (small
+// numbers on one grid of ulps: exact unless the partial sums outgrow it), the
+// low words' differences add plainly, and one TwoSum joins the two.  Against
+// a TwoSum per high-word difference this is 5x further from FP64 on a 32^3
+// phi^6 run of 1000 steps (1.7e-6 against 3.3e-7 relative in phi; FP32:
+// 4.7e-5) for 30 fewer operations per site: the adjoint's gradient error
+// stays well inside its 1e-4 target.
 __device__ __forceinline__ F2 pair_force_w(const PairConsts &k, F2 c, const F2 nb[6]) {
-  float acc = 0.f, err = 0.f, lo = 0.f;
+  float acc = 0.f, lo = 0.f;
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    const float d = __fsub_rn(nb[j].hi, c.hi);
-    const float t = __fadd_rn(acc, d);
-    const float bb = __fsub_rn(t, acc);
-    err = __fadd_rn(err, __fadd_rn(__fsub_rn(acc, __fsub_rn(t, bb)), __fsub_rn(d, bb)));
-    acc = t;
+    acc = __fadd_rn(acc, __fsub_rn(nb[j].hi, c.hi));
     lo = __fadd_rn(lo, __fsub_rn(nb[j].lo, c.lo));
   }
-  const F2 s = f2_fast(acc, __fadd_rn(err, lo));
+  const float sh = __fadd_rn(acc, lo), bb = __fsub_rn(sh, acc);  // TwoSum(acc, lo)
+  const F2 s = F2{sh, __fadd_rn(__fsub_rn(acc, __fsub_rn(sh, bb)), __fsub_rn(lo, bb))};
   return pair_potential_force(k, c, s);
 }
 
 // Four consecutive x-sites per thread, one plane: pi += fk F(phi) in place,
 // phi' = phi + fd pi'.  Both words of phi and pi move as float4; the x
 // neighbours outside the four come as scalars.  N a multiple of 4.
-__global__ void __launch_bounds__(256, 4) step_pair_x4(const PairConsts k, const float *__restrict__ ph,
-                                                    const float *__restrict__ pl, float *__restrict__ qh,
-                                                    float *__restrict__ ql, float *__restrict__ oh,
-                                                    float *__restrict__ ol) {
+template <int XS>
+struct PairVec;
+template <>
+struct PairVec<4> {
+  using T = float4;
+  __device__ static void unpack(const T &v, float *o) {
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+  }
+  __device__ static T pack(const float *o) { return make_float4(o[0], o[1], o[2], o[3]); }
+};
+template <>
+struct PairVec<2> {
+  using T = float2;
+  __device__ static void unpack(const T &v, float *o) {
+    o[0] = v.x;
+    o[1] = v.y;
+  }
+  __device__ static T pack(const float *o) { return make_float2(o[0], o[1]); }
+};
+
+// XS consecutive x-sites per thread (4: float4 words, 2: float2), one plane
+// per thread; a warp covers 32 XS sites of a row.
+template <int XS>
+__global__ void __launch_bounds__(256, XS == 4 ? 4 : 1) step_pair_xs(const PairConsts k, const float *__restrict__ ph,
+                                                                  const float *__restrict__ pl,
+                                                                  float *__restrict__ qh, float *__restrict__ ql,
+                                                                  float *__restrict__ oh, float *__restrict__ ol) {
+  using PV = PairVec<XS>;
+  using V = typename PV::T;
   const int N = k.N;
-  const int x0 = 4 * (blockIdx.x * 32 + threadIdx.x), y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+  const int x0 = XS * (blockIdx.x * 32 + threadIdx.x), y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
   if (x0 >= N || y >= N) return;
   const size_t NN = (size_t)N * N;
   const size_t plane = (size_t)z * NN, row = plane + (size_t)y * N;
@@ -145,26 +183,29 @@ __global__ void __launch_bounds__(256, 4) step_pair_x4(const PairConsts k, const
   const size_t iym = plane + (size_t)(y == 0 ? N - 1 : y - 1) * N + x0;
   const size_t izp = (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x0;
   const size_t izm = (size_t)(z == 0 ? N - 1 : z - 1) * NN + (size_t)y * N + x0;
-  const size_t ixl = row + (x0 == 0 ? N - 1 : x0 - 1), ixr = row + (x0 + 4 == N ? 0 : x0 + 4);
-  const float4 ch = *(const float4 *)(ph + i), cl = *(const float4 *)(pl + i);
-  const float4 yph = *(const float4 *)(ph + iyp), ypl = *(const float4 *)(pl + iyp);
-  const float4 ymh = *(const float4 *)(ph + iym), yml = *(const float4 *)(pl + iym);
-  const float4 zph = *(const float4 *)(ph + izp), zpl = *(const float4 *)(pl + izp);
-  const float4 zmh = *(const float4 *)(ph + izm), zml = *(const float4 *)(pl + izm);
+  const size_t ixl = row + (x0 == 0 ? N - 1 : x0 - 1), ixr = row + (x0 + XS == N ? 0 : x0 + XS);
+  auto ld = [](const float *f, size_t j) { return *(const V *)(f + j); };
+  float chv[XS], clv[XS], yphv[XS], yplv[XS], ymhv[XS], ymlv[XS], zphv[XS], zplv[XS], zmhv[XS], zmlv[XS], qhv[XS],
+      qlv[XS];
+  PV::unpack(ld(ph, i), chv);
+  PV::unpack(ld(pl, i), clv);
+  PV::unpack(ld(ph, iyp), yphv);
+  PV::unpack(ld(pl, iyp), yplv);
+  PV::unpack(ld(ph, iym), ymhv);
+  PV::unpack(ld(pl, iym), ymlv);
+  PV::unpack(ld(ph, izp), zphv);
+  PV::unpack(ld(pl, izp), zplv);
+  PV::unpack(ld(ph, izm), zmhv);
+  PV::unpack(ld(pl, izm), zmlv);
   const F2 xl = F2{ph[ixl], pl[ixl]}, xr = F2{ph[ixr], pl[ixr]};
-  const float4 pqh = *(const float4 *)(qh + i), pql = *(const float4 *)(ql + i);
-  const float chv[4] = {ch.x, ch.y, ch.z, ch.w}, clv[4] = {cl.x, cl.y, cl.z, cl.w};
-  const float yphv[4] = {yph.x, yph.y, yph.z, yph.w}, yplv[4] = {ypl.x, ypl.y, ypl.z, ypl.w};
-  const float ymhv[4] = {ymh.x, ymh.y, ymh.z, ymh.w}, ymlv[4] = {yml.x, yml.y, yml.z, yml.w};
-  const float zphv[4] = {zph.x, zph.y, zph.z, zph.w}, zplv[4] = {zpl.x, zpl.y, zpl.z, zpl.w};
-  const float zmhv[4] = {zmh.x, zmh.y, zmh.z, zmh.w}, zmlv[4] = {zml.x, zml.y, zml.z, zml.w};
-  const float qhv[4] = {pqh.x, pqh.y, pqh.z, pqh.w}, qlv[4] = {pql.x, pql.y, pql.z, pql.w};
-  float nqh[4], nql[4], nph[4], npl[4];
+  PV::unpack(ld(qh, i), qhv);
+  PV::unpack(ld(ql, i), qlv);
+  float nqh[XS], nql[XS], nph[XS], npl[XS];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < XS; ++j) {
     const F2 c = F2{chv[j], clv[j]};
     const F2 left = j == 0 ? xl : F2{chv[j - 1], clv[j - 1]};
-    const F2 right = j == 3 ? xr : F2{chv[j + 1], clv[j + 1]};
+    const F2 right = j == XS - 1 ? xr : F2{chv[j + 1], clv[j + 1]};
     const F2 nb[6] = {right, left, F2{yphv[j], yplv[j]}, F2{ymhv[j], ymlv[j]}, F2{zphv[j], zplv[j]},
                       F2{zmhv[j], zmlv[j]}};
     const F2 f = pair_force_w(k, c, nb);
@@ -175,10 +216,10 @@ __global__ void __launch_bounds__(256, 4) step_pair_x4(const PairConsts k, const
     nph[j] = p.hi;
     npl[j] = p.lo;
   }
-  *(float4 *)(qh + i) = make_float4(nqh[0], nqh[1], nqh[2], nqh[3]);
-  *(float4 *)(ql + i) = make_float4(nql[0], nql[1], nql[2], nql[3]);
-  *(float4 *)(oh + i) = make_float4(nph[0], nph[1], nph[2], nph[3]);
-  *(float4 *)(ol + i) = make_float4(npl[0], npl[1], npl[2], npl[3]);
+  *(V *)(qh + i) = PV::pack(nqh);
+  *(V *)(ql + i) = PV::pack(nql);
+  *(V *)(oh + i) = PV::pack(nph);
+  *(V *)(ol + i) = PV::pack(npl);
 }
 
 // One leapfrog step on pairs: pi += fk F(phi) in place, phi' = phi + fd pi'.
@@ -261,9 +302,15 @@ cudaError_t launch_step_pair(const Consts &k, double fk, double fd, const float 
   c.fk = f2_of(fk);
   c.fd = f2_of(fd);
   const int N = k.N;
+  // four sites per thread where rows hold whole float4 words; two (float2)
+  // measured 22% slower at 128^3 (more loads per site), so they serve only
+  // edges that are even but not multiples of 4
   if (N % 4 == 0) {  // float4 rows (16-byte aligned: N a multiple of 4, cudaMalloc'd arrays)
     const dim3 grid((N + 127) / 128, (N + 7) / 8, N), block(32, 8);
-    step_pair_x4<<<grid, block, 0, st>>>(c, ph, pl, qh, ql, oh, ol);
+    step_pair_xs<4><<<grid, block, 0, st>>>(c, ph, pl, qh, ql, oh, ol);
+  } else if (N % 2 == 0) {
+    const dim3 grid((N + 63) / 64, (N + 7) / 8, N), block(32, 8);
+    step_pair_xs<2><<<grid, block, 0, st>>>(c, ph, pl, qh, ql, oh, ol);
   } else {
     const dim3 grid((N + 31) / 32, (N + 7) / 8, (N + PAIR_CZ - 1) / PAIR_CZ), block(32, 8);
     step_pair<<<grid, block, 0, st>>>(c, PAIR_CZ, ph, pl, qh, ql, oh, ol);

@@ -4,7 +4,8 @@ EnergybasedID 1) against fixtures from the reference builds that compile it
 oracle.
 
 Tolerances:
-  FP64 fields: island labels, sizes and peak positions exact; the threshold
+  FP64 fields (the reference's own, uploaded after the same number of steps
+  sets the clock): island labels, sizes and peak positions exact; the threshold
   4 <rho>, the island energies and Peak_value (Delta at the peak) within
   1e-11 relative (theories 2, 3 and 5 evaluate cos and pow with CUDA's
   functions, so FP64 agrees to rounding, not bitwise); the density-contrast
@@ -35,7 +36,8 @@ def load(name):
 
 def lattice(pd, precision, seed, phi0, steps):
     """A lattice of params pd with the fixture's inputs evolved `steps` steps
-    on the GPU (FP64: the reference's fields bit for bit)."""
+    on the GPU (FP64: the reference's fields bit for bit for theory 4, to
+    rounding for the sin/cos/pow theories)."""
     import inputs
     from phinum_gb300 import lattice as PL
     p = PL.Params(precision=precision, a=0.25, dt=0.08, T0=0.0, **pd)
@@ -53,7 +55,15 @@ def test_delta_islands_and_contrast_spectrum_match_reference(name):
     N = pd["N"]
     slab = N * N
     phi, pi = lat.download()
-    assert np.array_equal(phi[slab:-slab], d["phi"][slab:-slab]) and np.array_equal(pi[slab:-slab], d["pi"][slab:-slab])
+    # the evolution: bit-exact for theory 4, to rounding for 2, 3, 5 (CUDA's
+    # sin, cos and pow); the analysis then starts from the reference's own
+    # fields (the clock stays where the steps left it)
+    for got, want in ((phi, d["phi"]), (pi, d["pi"])):
+        if pd["theory"] == 4:
+            assert np.array_equal(got[slab:-slab], want[slab:-slab])
+        else:
+            np.testing.assert_allclose(got[slab:-slab], want[slab:-slab], rtol=0, atol=1e-12)
+    lat.upload(d["phi"], d["pi"])
     # Full_Analysis' threshold, 4 <rho> (islands.cpp:783-786)
     thr = 4.0 * lat.volume_averages()[O.AVG["energy"]]
     np.testing.assert_allclose(thr, float(d["thres"]), rtol=1e-11)
