@@ -36,14 +36,16 @@ constexpr int kNumX4Variants = 7;
 // Observation sums of the x4 kernel (theories 0 and 1, one component).  The
 // four sites of a thread's plane row add to plain FP32 moments with FMAs --
 // sum phi, pi, phi^2, pi^2, phi pi, phi^4, phi^6 and the squared forward
-// differences -- which enter compensated per-thread totals every OBS_FOLD
-// planes; the FP64 record then takes the gradient's 1/a^2 and the
-// interaction as the linear combination of the moments that theories 0 and
-// 1 make of it (fieldanalysis.cpp:456-579: mmh phi^2 + lm phi^4/(24 Nc)
-// [+ phi^6/(720 Nc^2 Kappa^2)] [+ h phi]).  Extrema: the plane row's
-// maximum, minimum and largest |phi| first (fmaxf/fminf ignore NaN, as the
-// reference's comparisons do), and only when one reaches the running value
-// the site is located and compared by index (ties keep the smaller index).
+// differences -- which (on grids whose threads walk many items) enter
+// compensated per-thread totals every OBS_FOLD planes; the FP64 record then
+// takes the gradient's 1/a^2 and the interaction as the linear combination
+// of the moments that theories 0 and 1 make of it (fieldanalysis.cpp:456-579:
+// mmh phi^2 + lm phi^4/(24 Nc) [+ phi^6/(720 Nc^2 Kappa^2)] [+ h phi]).
+// Extrema: the plane row's maximum, minimum and largest |phi| first
+// (fmaxf/fminf ignore NaN, as the reference's comparisons do), kept when
+// strictly beyond the thread's running value -- a thread visits its rows in
+// index order, so that keeps the first site -- with the site inside the row
+// found once at the end; the block tree breaks ties by the smaller index.
 // Non-finite values are counted exactly, on the rare rows whose sum of 0 x
 // value is not 0.
 constexpr int OBS_FOLD = 4;
@@ -78,15 +80,15 @@ struct ObsX4 {
 
   __device__ __forceinline__ void site(float c, float p, float fx, float fy, float fz) {
     const float c2 = __fmul_rn(c, c), l2 = __fmul_rn(c2, c2);
-    part[MOM_PHI] += c;
-    part[MOM_PI] += p;
-    part[MOM_PHI2] += c2;
-    part[MOM_PI2] = fmaf(p, p, part[MOM_PI2]);
-    part[MOM_PHIPI] = fmaf(c, p, part[MOM_PHIPI]);
-    part[MOM_PHI4] += l2;
-    part[MOM_PHI6] = fmaf(l2, c2, part[MOM_PHI6]);
-    const float dx = fx - c, dy = fy - c, dz = fz - c;
-    part[MOM_GRAD] = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, part[MOM_GRAD])));
+    part[MOM_PHI] = __fadd_rn(part[MOM_PHI], c);
+    part[MOM_PI] = __fadd_rn(part[MOM_PI], p);
+    part[MOM_PHI2] = __fadd_rn(part[MOM_PHI2], c2);
+    part[MOM_PI2] = __fmaf_rn(p, p, part[MOM_PI2]);
+    part[MOM_PHIPI] = __fmaf_rn(c, p, part[MOM_PHIPI]);
+    part[MOM_PHI4] = __fadd_rn(part[MOM_PHI4], l2);
+    part[MOM_PHI6] = __fmaf_rn(l2, c2, part[MOM_PHI6]);
+    const float dx = __fsub_rn(fx, c), dy = __fsub_rn(fy, c), dz = __fsub_rn(fz, c);
+    part[MOM_GRAD] = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, part[MOM_GRAD])));
   }
 
   __device__ __forceinline__ void fold() {
@@ -110,10 +112,14 @@ struct ObsX4 {
     site(v.y, p.y, v.z, yp.y, zp.y);
     site(v.z, p.z, v.w, yp.z, zp.z);
     site(v.w, p.w, xr, yp.w, zp.w);
-    row_rest(v, p, kidx);
+    row_rest<false>(v, p, kidx);
   }
 
   // The row's non-finite count, extrema and fold, after its four sites.
+  // EAGER: the site inside a row is found at once (compensated fields, whose
+  // compensation words the step rewrites in place); otherwise only the row is
+  // kept and resolve_sites finds the site at the end.
+  template <bool EAGER>
   __device__ __forceinline__ void row_rest(float4 v, float4 p, long long kidx) {
     const float z0 = fmaf(v.x, 0.f, fmaf(v.y, 0.f, fmaf(v.z, 0.f, fmaf(v.w, 0.f, 0.f))));
     const float z1 = fmaf(p.x, 0.f, fmaf(p.y, 0.f, fmaf(p.z, 0.f, fmaf(p.w, 0.f, z0))));
@@ -123,31 +129,25 @@ struct ObsX4 {
       for (int j = 0; j < 8; ++j)
         if (!isfinite(a[j])) nonfinite += 1.f;
     }
-    // fmaxf / fminf return one of their operands, so the first site holding
-    // the row's extremum is one of the four
+    // the row's extrema (fmaxf / fminf ignore NaN, as the reference's
+    // comparisons do); a thread visits its rows in increasing index order, so
+    // a strictly larger value (smaller for the minimum) keeps the first site
+    // of the thread holding it.  Only the row is kept here: the site inside it
+    // is found once, in block_store.
     const float hi = fmaxf(fmaxf(v.x, v.y), fmaxf(v.z, v.w));
-    if (hi >= maxv && hi > -10000000.f) {
-      const int o = v.x == hi ? 0 : (v.y == hi ? 1 : (v.z == hi ? 2 : 3));
-      if (hi > maxv || kidx + o < maxi) {
-        maxv = hi;
-        maxi = kidx + o;
-      }
+    if (hi > maxv) {
+      maxv = hi;
+      maxi = EAGER ? first_of(v, hi, kidx) : kidx;
     }
     const float lo = fminf(fminf(v.x, v.y), fminf(v.z, v.w));
-    if (lo <= minv && lo < 10000000.f) {
-      const int o = v.x == lo ? 0 : (v.y == lo ? 1 : (v.z == lo ? 2 : 3));
-      if (lo < minv || kidx + o < mini) {
-        minv = lo;
-        mini = kidx + o;
-      }
+    if (lo < minv) {
+      minv = lo;
+      mini = EAGER ? first_of(v, lo, kidx) : kidx;
     }
     const float ab = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
-    if (ab >= absv && ab > 0.f) {  // sqrt(phi^2) of one component
-      const int o = fabsf(v.x) == ab ? 0 : (fabsf(v.y) == ab ? 1 : (fabsf(v.z) == ab ? 2 : 3));
-      if (ab > absv || kidx + o < absi) {
-        absv = ab;
-        absi = kidx + o;
-      }
+    if (ab > absv) {  // sqrt(phi^2) of one component
+      absv = ab;
+      absi = EAGER ? first_of(make_float4(fabsf(v.x), fabsf(v.y), fabsf(v.z), fabsf(v.w)), ab, kidx) : kidx;
     }
     if (++nplanes == OBS_FOLD) fold();
   }
@@ -206,6 +206,24 @@ struct ObsX4 {
   // 16384 blocks, and per-thread FP64 trees on GB300's narrow FP64 pipe cost
   // more than the step); one thread widens the pairs to FP64 and stores the
   // record in record()'s form.
+  // The first site of a kept row that holds the row's extremum (the row's
+  // values v: those the step observed).
+  __device__ static __forceinline__ long long first_of(float4 v, float x, long long row) {
+    return row + (v.x == x ? 0 : (v.y == x ? 1 : (v.z == x ? 2 : 3)));
+  }
+
+  // Plain FP32 fields: the site of each kept row (the input phi is not
+  // written during the step).
+  __device__ __forceinline__ void resolve_sites(const float *phi, long long NN) {
+    auto at = [&](long long row) { return *(const float4 *)(phi + (row - NN)); };
+    if (maxi != LLONG_MAX) maxi = first_of(at(maxi), maxv, maxi);
+    if (mini != LLONG_MAX) mini = first_of(at(mini), minv, mini);
+    if (absi != LLONG_MAX) {
+      const float4 v = at(absi);
+      absi = first_of(make_float4(fabsf(v.x), fabsf(v.y), fabsf(v.z), fabsf(v.w)), absv, absi);
+    }
+  }
+
   template <int THEORY, int W>
   __device__ void block_store(const Consts &k, double *partials, int tid, size_t slot) {
     struct WarpTotals {
@@ -360,7 +378,7 @@ __global__ void __launch_bounds__(32 * W, (MODE == MODE_STEP_OBS && !COMP && !KA
           obs.site(v.y, pv.y, c.z, yp.y, cp.y);
           obs.site(v.z, pv.z, c.w, yp.z, cp.z);
           obs.site(v.w, pv.w, xp, yp.w, cp.w);
-          obs.row_rest(v, pv, kidx);
+          obs.template row_rest<true>(v, pv, kidx);
         } else {
           obs.row(c, p, xp, yp, cp, kidx);
         }
@@ -399,7 +417,10 @@ __global__ void __launch_bounds__(32 * W, (MODE == MODE_STEP_OBS && !COMP && !KA
       c = cp;
     }
   }
-  if (MODE != MODE_STEP) obs.block_store<THEORY, W>(k, partials, tid, (size_t)blockIdx.x);  // one record per block
+  if (MODE != MODE_STEP) {  // one record per block
+    if (!KAHAN) obs.resolve_sites(phi, (long long)NN);
+    obs.template block_store<THEORY, W>(k, partials, tid, (size_t)blockIdx.x);
+  }
 }
 
 bool x4_supported(const phn_params &p) {
