@@ -237,20 +237,22 @@ def traffic_from_profile(path_kind: int, variant: int):
     path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None, f"profiles/{name} missing"
-    rec = {}
+    digest, per_variant = None, {}
     for line in open(path):
-        if ":" in line and line.split(":", 1)[0].strip() in ("traffic_bytes_per_launch", "source_sha256_16",
-                                                              "variant"):
-            k, v = line.split(":", 1)
-            rec[k.strip()] = v.strip().split()[0] if v.strip() else ""
-    if rec.get("source_sha256_16") != source_digest(files):
+        key, _, val = line.partition(":")
+        key, val = key.strip(), val.split()
+        if key == "source_sha256_16" and val:
+            digest = val[0]
+        elif key == "variant_traffic_bytes_per_launch" and len(val) >= 2:
+            per_variant[val[0]] = val[1]  # "<variant> <bytes>"
+    if digest != source_digest(files):
         return None, f"profiles/{name} was captured on other sources (stale)"
-    if rec.get("variant") != str(variant):
-        return None, f"profiles/{name} covers variant {rec.get('variant')}, this run uses {variant}"
+    if str(variant) not in per_variant:
+        return None, f"profiles/{name} covers variants {sorted(per_variant)}, this run uses {variant}"
     try:
-        return float(rec["traffic_bytes_per_launch"]), f"profiles/{name} (ncu, same sources and variant)"
-    except (KeyError, ValueError):
-        return None, f"profiles/{name} has no traffic line"
+        return float(per_variant[str(variant)]), f"profiles/{name} (ncu, same sources and variant)"
+    except ValueError:
+        return None, f"profiles/{name} has no traffic line for variant {variant}"
 
 
 _FIELDS = {}

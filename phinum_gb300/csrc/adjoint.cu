@@ -29,6 +29,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "ccl_math.h"
 #include "phn_internal.h"
 
 namespace phn {
@@ -393,16 +394,26 @@ __device__ double obj_fold(const double *part, int n) {
 
 // Pass 1: rho(x) from T fields (the summand of the reference's Energy:
 // pi^2/2 + forward-difference gradient energy + V) and block sums of rho.
+// x, y, z of site i (i < 2^31) by multiply-high division (ccl_math.h), not
+// 64-bit divisions.
+__device__ __forceinline__ void obj_xyz(const DivN &q, int N, size_t i, int &x, int &y, int &z) {
+  const unsigned row = div_n(q, (unsigned)i), zz = div_n(q, row);
+  x = (int)((unsigned)i - row * (unsigned)N);
+  y = (int)(row - zz * (unsigned)N);
+  z = (int)zz;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(OBJ_THREADS) obj_rho(const T *__restrict__ phi, const T *__restrict__ pi,
-                                                       const Consts k, double *__restrict__ rho,
+                                                       const Consts k, const DivN dn, double *__restrict__ rho,
                                                        double *__restrict__ part) {
   const int N = k.N;
   const size_t NN = (size_t)N * N, V = NN * N;
   const double ia2 = 1.0 / k.a2, i24 = 1.0 / k.c24, i720 = 1.0 / k.c720;
   double acc = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
+    int x, y, z;
+    obj_xyz(dn, N, i, x, y, z);
     const double c = phi[i], p = pi[i];
     const double fx = phi[i - x + (x + 1 == N ? 0 : x + 1)];
     const double fy = phi[(size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x];
@@ -470,14 +481,16 @@ __global__ void __launch_bounds__(OBJ_THREADS) obj_seed(const double *__restrict
 template <typename T, typename L>
 __global__ void __launch_bounds__(OBJ_THREADS) obj_adjoint_init(const T *__restrict__ phi, const T *__restrict__ pi,
                                                                 const double *__restrict__ g, const Consts k,
-                                                                L *__restrict__ lphi, L *__restrict__ lpi,
-                                                                double *__restrict__ part, int nb) {
+                                                                const DivN dn, L *__restrict__ lphi,
+                                                                L *__restrict__ lpi, double *__restrict__ part,
+                                                                int nb) {
   const int N = k.N;
   const size_t NN = (size_t)N * N, V = NN * N;
   const double ia2 = 1.0 / k.a2, i720 = 1.0 / k.c720, l6 = k.lm * (24.0 / k.c24) / 6.0;
   double a6 = 0.0, ah = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / NN);
+    int x, y, z;
+    obj_xyz(dn, N, i, x, y, z);
     const size_t ixp = i - x + (x + 1 == N ? 0 : x + 1), ixm = i - x + (x == 0 ? N - 1 : x - 1);
     const size_t iyp = (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x;
     const size_t iym = (size_t)z * NN + (size_t)(y == 0 ? N - 1 : y - 1) * N + x;
@@ -592,7 +605,7 @@ template <typename T>
 static int objective(phn_adjoint *a, const T *phi, const T *pi, cudaStream_t st) {
   const int nb = a->sum_blocks;
   double *res = a->sums + 3 * nb;
-  obj_rho<T><<<nb, OBJ_THREADS, 0, st>>>(phi, pi, a->k, a->rho, a->sums);
+  obj_rho<T><<<nb, OBJ_THREADS, 0, st>>>(phi, pi, a->k, make_divn((unsigned)a->k.N), a->rho, a->sums);
   obj_sigmoid<<<nb, OBJ_THREADS, 0, st>>>(a->rho, a->V, a->w, a->g, a->sums, nb);
   obj_seed<<<nb, OBJ_THREADS, 0, st>>>(a->rho, a->V, a->w, a->g, a->sums, nb, res);
   CKA(cudaGetLastError());
@@ -869,18 +882,19 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   // adjoint of the objective, with the direct dependence of rho on the couplings
   // (on the forward's final state: FP64 when the forward ran in FP64, the
   // pair state widened to FP64 when it ran in pairs)
+  const DivN dn = make_divn((unsigned)a->k.N);
   if (dbl)
-    obj_adjoint_init<double, double><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
+    obj_adjoint_init<double, double><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k, dn,
                                                                  (double *)a->lphi[0], (double *)a->lpi[0], a->sums,
                                                                  nb);
   else if (a->pair)
-    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>(a->pfin, a->pfin + a->V, a->g, a->k,
+    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>(a->pfin, a->pfin + a->V, a->g, a->k, dn,
                                                                 (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   else if (a->fwd_elem == 8)
-    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k,
+    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k, dn,
                                                                 (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   else
-    obj_adjoint_init<float, float><<<nb, OBJ_THREADS, 0, st>>>((const float *)phi, (const float *)pi, a->g, a->k,
+    obj_adjoint_init<float, float><<<nb, OBJ_THREADS, 0, st>>>((const float *)phi, (const float *)pi, a->g, a->k, dn,
                                                                (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   CKA(cudaGetLastError());
   CKA(cudaGraphLaunch(a->sweep, st));

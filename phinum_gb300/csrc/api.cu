@@ -172,6 +172,7 @@ Consts phn::at_scale_factor(const Consts &k0, double sf) {
   k.msq2 = m2 * m2;
   k.t5c = k0.theory == 5 ? k.msq2 * 0.5 / k0.p_mono : 0.0;
   // FP32 forms
+  k.hub_f = (float)(k0.H0 / sf);
   k.mmM_f = (float)k.mmM;
   k.c6_f = k0.theory == 0 ? (float)(1.0 / (k0.kappa * k0.kappa * k0.c120 * sf * sf)) : 0.f;
   k.h_f = (float)k.h;

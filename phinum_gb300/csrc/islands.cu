@@ -702,7 +702,7 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats(const T *__restrict__ p
       const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
       const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
       // BFS accumulators (islands.cpp:131-198)
-      grad = grad_half(c, fx, fy, fz, (A)k.inv_a2);
+      grad = grad_half(c, fx, fy, fz, inv_a2_of<A>(k));
       kin = site_kinetic(k, c, p);
       pot = site_potential(k, c, c * c);
       cs = c;
@@ -902,7 +902,7 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ 
           const A cj = c[j], fx = j < 3 ? c[j + 1] : fx3;
           RunSums<A> t;
           // BFS accumulators (islands.cpp:131-198)
-          t.grad = grad_half(cj, fx, fy[j], fz[j], (A)k.inv_a2);
+          t.grad = grad_half(cj, fx, fy[j], fz[j], inv_a2_of<A>(k));
           t.kin = site_kinetic(k, cj, p[j]);
           t.pot = site_potential(k, cj, cj * cj);
           t.cs = cj;
@@ -982,7 +982,7 @@ __device__ __forceinline__ double site_delta_stats(const T *phi, const float *cp
   const A fx = val_as<A, KAHAN>(phi, cphi, i - x + (x + 1 == N ? 0 : x + 1));
   const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
   const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
-  return (double)delta_of<A>(site_kinetic(k, c, p), grad_half(c, fx, fy, fz, (A)k.inv_a2),
+  return (double)delta_of<A>(site_kinetic(k, c, p), grad_half(c, fx, fy, fz, inv_a2_of<A>(k)),
                              site_potential(k, c, c * c));
 }
 

@@ -327,9 +327,11 @@ __device__ __forceinline__ void kahan_site(float fk, float fd, float f, float c,
 
 // A fused observation step with one item per block keeps 4 blocks of 8
 // warps per SM (64 registers): it streams the fields like the plain step and
-// needs its warps for the same latency hiding.
+// needs its warps for the same latency hiding.  The other kernels give no
+// minimum (0): an explicit minimum of one block raised the plain step from 48
+// to 64 registers.
 template <int W, int MODE, int THEORY, bool KAHAN, bool COMP>
-__global__ void __launch_bounds__(32 * W, (MODE == MODE_STEP_OBS && !COMP && !KAHAN) ? 32 / W : 1) step_f32_x4(const Consts k, const float *__restrict__ phi,
+__global__ void __launch_bounds__(32 * W, (MODE == MODE_STEP_OBS && !COMP && !KAHAN) ? 32 / W : 0) step_f32_x4(const Consts k, const float *__restrict__ phi,
                                                       float *__restrict__ phi_out, float *__restrict__ pi,
                                                       float *__restrict__ cphi, float *__restrict__ cpi, StepF s,
                                                       int cz, int nitems, double *__restrict__ partials) {

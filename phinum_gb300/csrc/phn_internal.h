@@ -58,6 +58,7 @@ struct Consts {
   double c720;       // 720.0*Nc*Nc*Kappa*Kappa
   // FP32 forms of the kick
   float inv_a2_f, mmM_f, c4_f, c6_f, h_f;
+  float hub_f;  // H0 / scale factor (the expanding box's kinetic terms; 0 for the static box)
   // FP32 forms of the energy density
   float mmh_f, e4_f, e6_f;
   // theories 2-5 (Nc = 1): M = BareM_sqr, as the reference writes the terms

@@ -37,6 +37,14 @@ __device__ __forceinline__ A val_as(const T *f, const float *comp, size_t i) {
   else return (A)f[i];
 }
 
+// 1/a^2 in arithmetic A: the FP32 kernels take the FP32 constant, so that no
+// site converts the FP64 one (a conversion on GB300's narrow FP64 pipe).
+template <typename A>
+__device__ __forceinline__ A inv_a2_of(const Consts &k) {
+  if constexpr (std::is_same<A, float>::value) return k.inv_a2_f;
+  else return k.inv_a2;
+}
+
 // Potential of one single-component site, theories 0-5: the BFS PotEn
 // summand (islands.cpp:137-196), which is also the Interaction summand of
 // CalculateVolumeAverages (fieldanalysis.cpp:456-617) for Nc = 1.  The
@@ -93,7 +101,7 @@ __device__ __forceinline__ double site_kinetic(const Consts &k, double c, double
 
 __device__ __forceinline__ float site_kinetic(const Consts &k, float c, float p) {
   if (!k.expansion) return 0.5f * (p * p);
-  const float hub = (float)(k.H0 / k.sf);
+  const float hub = k.hub_f;  // no FP64 per site
   return fmaf(0.5f * (hub * hub) * c, c, fmaf(0.5f * p, p, -c * p * hub));
 }
 
@@ -111,7 +119,7 @@ __device__ A site_rho(const T *phi, const float *cphi, const T *pi, const float 
   const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
   const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
   const A c2 = c * c;
-  const A grad = (((fx - c) * (fx - c) + (fy - c) * (fy - c)) + (fz - c) * (fz - c)) * (A)k.inv_a2;
+  const A grad = (((fx - c) * (fx - c) + (fy - c) * (fy - c)) + (fz - c) * (fz - c)) * inv_a2_of<A>(k);
   return site_kinetic(k, c, p) + (A)0.5 * grad + site_potential(k, c, c2);
 }
 
@@ -152,7 +160,7 @@ __device__ A site_delta(const T *phi, const float *cphi, const T *pi, const floa
   const A fx = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)y * N + (x + 1 == N ? 0 : x + 1));
   const A fy = val_as<A, KAHAN>(phi, cphi, (size_t)z * NN + (size_t)(y + 1 == N ? 0 : y + 1) * N + x);
   const A fz = val_as<A, KAHAN>(phi, cphi, (size_t)(z + 1 == N ? 0 : z + 1) * NN + (size_t)y * N + x);
-  return delta_of<A>(site_kinetic(k, c, p), grad_half(c, fx, fy, fz, (A)k.inv_a2), site_potential(k, c, c * c));
+  return delta_of<A>(site_kinetic(k, c, p), grad_half(c, fx, fy, fz, inv_a2_of<A>(k)), site_potential(k, c, c * c));
 }
 
 }  // namespace phn
