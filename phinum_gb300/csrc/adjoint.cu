@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "ccl_math.h"
+#include "kick.cuh"
 #include "phn_internal.h"
 
 namespace phn {
@@ -145,6 +146,51 @@ __device__ __forceinline__ void grad_slot_add(double g0, double g1, double *gs, 
   }
 }
 
+// (h, l) += (h2, l2) for unevaluated sums of two floats: TwoSum of the high
+// words, the low words into the error, Fast2Sum.
+__device__ __forceinline__ void fpair_add(float &h, float &l, float h2, float l2) {
+  const float t = __fadd_rn(h, h2);
+  const float bb = __fsub_rn(t, h);
+  const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bb)), __fsub_rn(h2, bb));
+  const float lo = __fadd_rn(e, __fadd_rn(l, l2));
+  h = __fadd_rn(t, lo);
+  l = __fsub_rn(lo, __fsub_rn(h, t));
+}
+
+// grad_slot_add for two per-thread compensated FP32 sums (value s - c): the
+// warp shuffles and the sum over the warps add float pairs, and FP64 is used
+// by the one thread that adds to the block's slots.  The FP64 form cost the
+// FP32 reverse step a tenth of its time at 128^3: every block of the single
+// wave reaches its reduction at the same moment, on GB300's narrow FP64 pipe.
+__device__ __forceinline__ void grad_slot_add_f32(const KSum<float> &a, const KSum<float> &b, double *gs, int tid,
+                                                  int nwarps) {
+  __shared__ float sh[4][32];
+  float h0 = a.s, l0 = -a.c, h1 = b.s, l1 = -b.c;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float h0n = __shfl_down_sync(0xffffffffu, h0, off), l0n = __shfl_down_sync(0xffffffffu, l0, off);
+    const float h1n = __shfl_down_sync(0xffffffffu, h1, off), l1n = __shfl_down_sync(0xffffffffu, l1, off);
+    fpair_add(h0, l0, h0n, l0n);
+    fpair_add(h1, l1, h1n, l1n);
+  }
+  if ((tid & 31) == 0) {
+    sh[0][tid >> 5] = h0;
+    sh[1][tid >> 5] = l0;
+    sh[2][tid >> 5] = h1;
+    sh[3][tid >> 5] = l1;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 1; w < nwarps; ++w) {
+      fpair_add(h0, l0, sh[0][w], sh[1][w]);
+      fpair_add(h1, l1, sh[2][w], sh[3][w]);
+    }
+    const size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
+    gs[blk * ADJ_NG + 0] += (double)h0 + (double)l0;
+    gs[blk * ADJ_NG + 1] += (double)h1 + (double)l1;
+  }
+}
+
 // One reverse step, one site per thread (any N; the FP64 path).
 // phi1, pi1: state after the step; lphi, lpi: adjoints at that time.  Writes
 // phi0, pi0 (state before) and lphi0, lpi0 (adjoints before).  Gradient slots:
@@ -230,7 +276,10 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
 
 // The same reverse step for FP32, four consecutive x-sites per thread
 // (N a multiple of 4): 16-byte loads and stores, x neighbours inside the
-// thread plus one scalar per side, y rows and z planes as float4.
+// thread plus one scalar per side, y rows and z planes as float4.  The
+// reconstruction pi = pi' - fk F(phi) uses the forward kick's own FP32 force
+// (kick.cuh) and coefficients; the theory is a template parameter, and
+// theory 0 is held to 80 registers (three blocks of 8 warps per SM).
 __device__ __forceinline__ float4 f4fma(float a, float4 b, float4 c) {
   return make_float4(fmaf(a, b.x, c.x), fmaf(a, b.y, c.y), fmaf(a, b.z, c.z), fmaf(a, b.w, c.w));
 }
@@ -244,7 +293,8 @@ __device__ __forceinline__ void f4set(float4 &v, int e, float x) {
   else v.w = x;
 }
 
-__global__ void __launch_bounds__(ADJ_THREADS) adjoint_step_x4(const float *__restrict__ phi1,
+template <int THEORY>
+__global__ void __launch_bounds__(ADJ_THREADS, THEORY == 0 ? 3 : 0) adjoint_step_x4(const float *__restrict__ phi1,
                                                                const float *__restrict__ pi1,
                                                                const float *__restrict__ lphi,
                                                                const float *__restrict__ lpi, float *__restrict__ phi0,
@@ -269,7 +319,9 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step_x4(const float *__re
     float4 pm = rphi4((size_t)zm0 * NN + col), mm = rmu4((size_t)zm0 * NN + col);
     size_t ic = (size_t)z0 * NN + col;
     float4 pc = rphi4(ic), mc = rmu4(ic), pic = ld4(pi1, ic), lphic = ld4(lphi, ic);
-    const float inv_a2 = 1.f / (float)k.a2;
+    // V''(phi) = mmM + 3 c4 phi^2 [+ 5 c6 phi^4] with the forward kick's FP32
+    // coefficients (parameter-space constants: no per-site FP64 conversion)
+    const float c4x3 = 3.f * k.c4_f, c6x5 = 5.f * k.c6_f;
     for (int z = z0; z < z1; ++z) {
       const int zn = (z + 1 == N) ? 0 : z + 1;
       const size_t pl = (size_t)z * NN, i = pl + col, in = (size_t)zn * NN + col;
@@ -284,14 +336,15 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step_x4(const float *__re
         const float c = f4get(pc, e), m = f4get(mc, e);
         const float cxm = e == 0 ? pxl : f4get(pc, e - 1), cxp = e == 3 ? pxr : f4get(pc, e + 1);
         const float mxm = e == 0 ? mxl : f4get(mc, e - 1), mxp = e == 3 ? mxr : f4get(mc, e + 1);
-        const float dphi = (((cxp - c) + (cxm - c)) + ((f4get(pyp, e) - c) + (f4get(pym, e) - c))) +
-                           ((f4get(pn, e) - c) + (f4get(pm, e) - c));
-        const float dmu = (((mxp - m) + (mxm - m)) + ((f4get(myp, e) - m) + (f4get(mym, e) - m))) +
-                          ((f4get(mn, e) - m) + (f4get(mm, e) - m));
+        const float lap = lap_diff_f32(c, cxm, cxp, f4get(pym, e), f4get(pyp, e), f4get(pm, e), f4get(pn, e),
+                                       k.inv_a2_f);
+        const float lmu = lap_diff_f32(m, mxm, mxp, f4get(mym, e), f4get(myp, e), f4get(mm, e), f4get(mn, e),
+                                       k.inv_a2_f);
+        const float c2 = __fmul_rn(c, c);
+        const float vpp = THEORY == 0 ? fmaf(c2, fmaf(c2, c6x5, c4x3), k.mmM_f) : fmaf(c2, c4x3, k.mmM_f);
         f4set(o_phi, e, c);
-        f4set(o_pi, e, fmaf(-fk, force<float>(k, dphi, c), f4get(pic, e)));
-        f4set(o_lphi, e, fmaf(fk, dmu * inv_a2 - vpp<float>(k, c) * m, f4get(lphic, e)));
-        const float c2 = c * c;
+        f4set(o_pi, e, fmaf(-fk, force_f32<THEORY>(k, lap, c, c2), f4get(pic, e)));
+        f4set(o_lphi, e, fmaf(fk, fmaf(-vpp, m, lmu), f4get(lphic, e)));
         k_c6.add(fk * m * (-6.f * (c2 * c2 * c)));
         k_h.add(-fk * m);
       }
@@ -307,7 +360,7 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step_x4(const float *__re
       lphic = lphin;
     }
   }
-  grad_slot_add(k_c6.value(), k_h.value(), gs, threadIdx.x + ADJ_TX * threadIdx.y, ADJ_THREADS / 32);
+  grad_slot_add_f32(k_c6, k_h, gs, threadIdx.x + ADJ_TX * threadIdx.y, ADJ_THREADS / 32);
 }
 
 // Grid of the reverse kernel (x4: a block covers 128 x-sites).  Cost model:
@@ -328,7 +381,7 @@ static Grid adjoint_grid(int N, bool x4) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (x4)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step_x4, ADJ_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step_x4<0>, ADJ_THREADS, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step<double>, ADJ_THREADS, 0);
   const long long resident = (long long)sms * (occ > 0 ? occ : 1);
@@ -848,7 +901,7 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
               (double *)phi0, (double *)pi0, (double *)a->lphi[1 - cur], (double *)a->lpi[1 - cur], a->k,
               a->fk[n], a->fd[n], gr.cz, a->gs);
         else if (x4)
-          adjoint_step_x4<<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
+          (a->k.theory == 0 ? adjoint_step_x4<0> : adjoint_step_x4<1>)<<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
               (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
               (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
               (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
