@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "ccl_math.h"
+#include "float_pair.cuh"
 #include "kick.cuh"
 #include "phn_internal.h"
 
@@ -144,17 +145,6 @@ __device__ __forceinline__ void grad_slot_add(double g0, double g1, double *gs, 
     gs[b * ADJ_NG + 0] += s0;
     gs[b * ADJ_NG + 1] += s1;
   }
-}
-
-// (h, l) += (h2, l2) for unevaluated sums of two floats: TwoSum of the high
-// words, the low words into the error, Fast2Sum.
-__device__ __forceinline__ void fpair_add(float &h, float &l, float h2, float l2) {
-  const float t = __fadd_rn(h, h2);
-  const float bb = __fsub_rn(t, h);
-  const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bb)), __fsub_rn(h2, bb));
-  const float lo = __fadd_rn(e, __fadd_rn(l, l2));
-  h = __fadd_rn(t, lo);
-  l = __fsub_rn(lo, __fsub_rn(h, t));
 }
 
 // grad_slot_add for two per-thread compensated FP32 sums (value s - c): the

@@ -254,7 +254,7 @@ __device__ __forceinline__ int find_root_sh_ro(volatile int *lp, int x) {
   return x;
 }
 
-__device__ void unite_sh(int *lp, int a, int b) {
+__device__ __forceinline__ void unite_sh(int *lp, int a, int b) {
   while (true) {
     a = find_root_sh(lp, a);
     b = find_root_sh(lp, b);
@@ -308,47 +308,74 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) ccl_tile(const T *__restrict__
     }
   }
   // a warp is one tile row: x-runs link to their first site by ballot, as
-  // in ccl_init (the tile row starts the segment, so lx = 0 links nowhere)
+  // in ccl_init (the tile row starts the segment, so lx = 0 links nowhere);
+  // the rows' mask words go to shared memory for the union rule
+  __shared__ unsigned mrow[TILE_Z][TILE_Y];
   const unsigned full = 0xffffffffu;
+  unsigned mbs[TILE_Z];
 #pragma unroll
   for (int lz = 0; lz < TILE_Z; ++lz) {
     const int s = (lz * TILE_Y + ly) * TILE_X + lx;
     const unsigned mb = __ballot_sync(full, mk[lz]);
     const unsigned heads = mb & ~(mb << 1);
+    mbs[lz] = mb;
+    if (lx == 0) mrow[lz][ly] = mb;
     lp[s] = mk[lz] ? s - lx + (31 - __clz(heads & (full >> (31 - lx)))) : -1;
   }
   __syncthreads();
-#pragma unroll 1
-  for (int lz = 0; lz < TILE_Z; ++lz) {
-    const int s = (lz * TILE_Y + ly) * TILE_X + lx;
-    if (((volatile int *)lp)[s] < 0) continue;
-    const bool left = lx > 0 && ((volatile int *)lp)[s - 1] >= 0;  // linked above
-    if (ly > 0) {
-      const int t = s - TILE_X;
-      if (((volatile int *)lp)[t] >= 0 && !(left && ((volatile int *)lp)[t - 1] >= 0)) unite_sh(lp, s, t);
+  // -y and -z unions by the skip rule, from the mask words: site s unites
+  // with t when both are on the mask and not both of s-1, t-1 are
+  // (b & ~(b << 1), b = the two rows' common mask).  A union joins the first
+  // sites of the two x-runs (their links' targets), found from the words too.
+  // Each warp first lists the unions of its eight rows (at most 16 per pair
+  // of rows), then runs them with every lane busy: unions per row are few,
+  // and a loop over the rows left most lanes idle in the root searches.
+  __shared__ unsigned edges[TILE_Y][2 * TILE_Z * 16];
+  {
+    const unsigned le = full >> (31 - lx), lt = le >> 1;  // lanes 0..lx, 0..lx-1
+    int ne = 0;                                           // uniform per warp
+#pragma unroll
+    for (int lz = 0; lz < TILE_Z; ++lz) {
+      const unsigned me = mbs[lz];
+      const unsigned wy = ly > 0 ? mrow[lz][ly - 1] : 0u, wz = lz > 0 ? mbs[lz - 1] : 0u;
+      const unsigned by = me & wy, bz = me & wz;
+      const unsigned uy = by & ~(by << 1), uz = bz & ~(bz << 1);
+      const int row = (lz * TILE_Y + ly) * TILE_X;
+      const unsigned hs = (unsigned)(row + 31 - __clz(me & ~(me << 1) & le));
+      if ((uy >> lx) & 1u)
+        edges[ly][ne + __popc(uy & lt)] = hs << 16 | (unsigned)(row - TILE_X + 31 - __clz(wy & ~(wy << 1) & le));
+      ne += __popc(uy);
+      if ((uz >> lx) & 1u)
+        edges[ly][ne + __popc(uz & lt)] =
+            hs << 16 | (unsigned)(row - TILE_X * TILE_Y + 31 - __clz(wz & ~(wz << 1) & le));
+      ne += __popc(uz);
     }
-    if (lz > 0) {
-      const int t = s - TILE_X * TILE_Y;
-      if (((volatile int *)lp)[t] >= 0 && !(left && ((volatile int *)lp)[t - 1] >= 0)) unite_sh(lp, s, t);
+    __syncwarp();
+    for (int e = lx; e < ne; e += TILE_X) {
+      const unsigned ab = edges[ly][e];
+      unite_sh(lp, (int)(ab >> 16), (int)(ab & 0xffffu));
     }
   }
   __syncthreads();
-  // each mask site links to its tile root's global index; the tile roots'
-  // bits (one 32-bit word per tile row: N is a multiple of 32) let the
-  // later passes visit the roots only
+  // each mask site links to its tile root's global index: the first site of
+  // each x-run finds the root, the run's other sites take it by shuffle; the
+  // tile roots' bits (one 32-bit word per tile row: N is a multiple of 32)
+  // let the later passes visit the roots only
 #pragma unroll
   for (int lz = 0; lz < TILE_Z; ++lz) {
     const int s = (lz * TILE_Y + ly) * TILE_X + lx;
     const size_t i = (size_t)(z0 + lz) * NN + (size_t)y * N + x;
+    const unsigned mb = mbs[lz], heads = mb & ~(mb << 1);
+    const bool m = (mb >> lx) & 1u;
+    const int r0 = ((heads >> lx) & 1u) ? find_root_sh_ro(lp, s) : 0;
+    const int r = __shfl_sync(full, r0, m ? 31 - __clz(heads & (full >> (31 - lx))) : lx);
     int g = -1;
-    const int l = lp[s];
-    if (l >= 0) {
-      const int r = find_root_sh_ro(lp, s);
+    if (m) {
       const int rz = r / (TILE_X * TILE_Y), ry = (r / TILE_X) % TILE_Y, rx = r % TILE_X;
       g = (int)((size_t)(z0 + rz) * NN + (size_t)(y0 + ry) * N + (x0 + rx));
     }
     parent[i] = g;
-    const unsigned tb = __ballot_sync(full, l == s);
+    const unsigned tb = __ballot_sync(full, m && r == s);
     if (lx == 0) tbits[i >> 5] = tb;
   }
 }
@@ -359,32 +386,50 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) ccl_tile(const T *__restrict__
 // ancestor of one, after a path-halving write), and every union hooks one
 // tile root under another, so after this pass the tile roots alone carry
 // the cross-tile structure.
-__device__ __forceinline__ void face_union(int *parent, size_t i, size_t j, bool skip_rule) {
-  if (parent[i] < 0 || parent[j] < 0) return;
-  // the skip rule of ccl_merge: with i-1 and j-1 on the mask too, the pair
-  // (i-1, j-1) -- united here or skipped by the same rule -- joins i and j
-  if (skip_rule && parent[i - 1] >= 0 && parent[j - 1] >= 0) return;
-  unite(parent, (int)i, (int)j);
+
+// Whether the face pair (i, j) needs a union: both on the mask, and not
+// dropped by the skip rule of ccl_merge (with i-1 and j-1 on the mask too,
+// the pair (i-1, j-1) -- united here or skipped by the same rule -- joins i
+// and j).
+__device__ __forceinline__ bool face_pair(const int *parent, size_t i, size_t j, bool skip_rule) {
+  if (parent[i] < 0 || parent[j] < 0) return false;
+  return !(skip_rule && parent[i - 1] >= 0 && parent[j - 1] >= 0);
 }
 
 __global__ void __launch_bounds__(CCL_THREADS) ccl_border_tiles(int *__restrict__ parent, int N, int zper) {
   static_assert(CCL_THREADS == TILE_X * TILE_Y && TILE_Y == TILE_Z, "one row of each face per warp");
+  // each warp lists its faces' unions, then runs them with every lane busy
+  // (a face row holds a few; the root searches are global-memory latency)
+  __shared__ int2 pairs[CCL_THREADS / 32][3 * 32];
+  const unsigned full = 0xffffffffu;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y, z0 = blockIdx.z * TILE_Z;
   const size_t NN = (size_t)N * N;
   const int x = x0 + lane;
+  const unsigned lt = (1u << lane) - 1u;
+  int np = 0;  // uniform per warp
+  auto offer = [&](bool want, size_t i, size_t j) {
+    const unsigned b = __ballot_sync(full, want);
+    if (want) pairs[w][np + __popc(b & lt)] = make_int2((int)i, (int)j);
+    np += __popc(b);
+  };
   {  // -y face, periodic
     const size_t i = (size_t)(z0 + w) * NN + (size_t)y0 * N + x;
-    face_union(parent, i, y0 == 0 ? i + (size_t)(N - 1) * N : i - N, x > 0);
+    const size_t j = y0 == 0 ? i + (size_t)(N - 1) * N : i - N;
+    offer(face_pair(parent, i, j, x > 0), i, j);
   }
-  if (z0 > 0 || zper) {  // -z face, open on one rank unless asked periodic
+  if (z0 > 0 || zper) {  // -z face, open on one rank unless asked periodic (uniform per block)
     const size_t i = (size_t)z0 * NN + (size_t)(y0 + w) * N + x;
-    face_union(parent, i, z0 == 0 ? i + (size_t)(N - 1) * NN : i - NN, x > 0);
+    const size_t j = z0 == 0 ? i + (size_t)(N - 1) * NN : i - NN;
+    offer(face_pair(parent, i, j, x > 0), i, j);
   }
-  if (t < TILE_Y * TILE_Z) {  // -x face, periodic
+  if (w < TILE_Y * TILE_Z / 32) {  // -x face, periodic (warps 0 and 1)
     const size_t i = (size_t)(z0 + t / TILE_Y) * NN + (size_t)(y0 + t % TILE_Y) * N + x0;
-    face_union(parent, i, x0 == 0 ? i + N - 1 : i - 1, false);
+    const size_t j = x0 == 0 ? i + N - 1 : i - 1;
+    offer(face_pair(parent, i, j, false), i, j);
   }
+  __syncwarp();
+  for (int e = lane; e < np; e += 32) unite(parent, pairs[w][e].x, pairs[w][e].y);
 }
 
 // Roots per block of CCL_THREADS threads, into blk[blockIdx.x].
@@ -599,7 +644,7 @@ struct StatsSlot<float> {
 };
 
 template <typename A>
-struct RunSums {
+struct alignas(16) RunSums {  // 16-byte aligned: the scratch copies move as vectors
   A pot, kin, grad, cs;
   unsigned long long pk;
   int n;
@@ -801,14 +846,36 @@ __device__ __forceinline__ RunSums<A> run_shfl_up(const RunSums<A> &r, int off) 
                     __shfl_up_sync(full, r.pk, off),  __shfl_up_sync(full, r.n, off)};
 }
 
+template <typename A>
+__device__ __forceinline__ RunSums<A> run_shfl_down(const RunSums<A> &r, int off) {
+  const unsigned full = 0xffffffffu;
+  return RunSums<A>{__shfl_down_sync(full, r.pot, off), __shfl_down_sync(full, r.kin, off),
+                    __shfl_down_sync(full, r.grad, off), __shfl_down_sync(full, r.cs, off),
+                    __shfl_down_sync(full, r.pk, off),  __shfl_down_sync(full, r.n, off)};
+}
+
 // One round of table updates: the lanes with u set offer (id, r); the offers
-// of one island combine in lane order first, so that the table takes one
-// update per island per round.
+// of one island combine first, so that the table takes one update per island
+// per round.  When every offer is of one island (runs of the spanning
+// cluster, most often) they combine by a shuffle tree over the lanes from the
+// first to the last offer, the others in lane order through the scratch row.
 template <typename A>
 __device__ __forceinline__ void table_round(bool u, int id, RunSums<A> r, StatsSlot<A> *table, RunSums<A> *scratch,
                                             int lane, int *size, double *sums, unsigned long long *peak2) {
   const unsigned full = 0xffffffffu;
-  if (!__any_sync(full, u)) return;
+  const unsigned um = __ballot_sync(full, u);
+  if (um == 0u) return;
+  const int first = __ffs(um) - 1, last = 31 - __clz(um);
+  const int id0 = __shfl_sync(full, id, first);
+  if (__all_sync(full, !u || id == id0)) {
+    if (!u) run_zero(r);
+    for (int off = 1; first + off <= last; off <<= 1) {  // uniform per warp
+      const RunSums<A> o = run_shfl_down(r, off);
+      if (((lane - first) & (2 * off - 1)) == 0 && lane + off <= last) run_add(r, o);
+    }
+    if (lane == first) table_update(table, id0, r, size, sums, peak2);
+    return;
+  }
   const unsigned grp = __match_any_sync(full, u ? id : -1 - lane);
   if (u) scratch[lane] = r;
   __syncwarp();
@@ -926,21 +993,26 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ 
     const bool through = pr.x >= 0 && pr.y >= 0 && pr.z >= 0 && pr.w >= 0;
     const bool m3prev = __shfl_up_sync(full, m3, 1);
     const bool conn = lane > 0 && m0 && m3prev && x0 != 0;
-    // segmented inclusive scan of the carries
+    // segmented inclusive scan of the carries; it stops at the first step
+    // that no lane's segment reaches back to (the longest segment sets the
+    // number of steps)
     RunSums<A> C = through ? L : R;
     const unsigned heads = __ballot_sync(full, !(through && conn));
     const int start = 31 - __clz(heads & (full >> (31 - lane)));
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
+      if (!__any_sync(full, lane - off >= start)) break;  // uniform per warp
       const RunSums<A> u = run_shfl_up(C, off);
       if (lane - off >= start) run_add(C, u);
     }
-    const RunSums<A> Cp = run_shfl_up(C, 1);
     const bool conn_next = __shfl_down_sync(full, conn, 1);
     bool u1 = C.n > 0 && (lane == 31 || !conn_next);  // the carry closes here
     bool u2 = !through && m0;                        // L closes at the lane's first gap
     bool u3 = M.n > 0;
-    if (u2 && conn) run_add(L, Cp);
+    if (__any_sync(full, u2 && conn)) {
+      const RunSums<A> Cp = run_shfl_up(C, 1);
+      if (u2 && conn) run_add(L, Cp);
+    }
     const int id1 = u1 ? ids[pr.w] : -1, id2 = u2 ? ids[pr.x] : -1, id3 = u3 ? ids[mpar] : -1;
     // a lane's own closed runs of one island combine first
     if (u3 && u2 && id3 == id2) {
@@ -955,9 +1027,14 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ 
       run_add(M, C);
       u1 = false;
     }
-    table_round(u2, id2, L, table, scratch[warp], lane, size, sums, peak2);
-    table_round(u3, id3, M, table, scratch[warp], lane, size, sums, peak2);
-    table_round(u1, id1, C, table, scratch[warp], lane, size, sums, peak2);
+    // the lane's closed runs in order (L, M, C, whichever close here): the
+    // first round takes every lane's first, so the later rounds are short or
+    // skipped
+    const bool w1 = (u2 && u3) || (u1 && (u2 || u3)), w2 = u2 && u3 && u1;
+    table_round(u2 || u3 || u1, u2 ? id2 : (u3 ? id3 : id1), u2 ? L : (u3 ? M : C), table, scratch[warp], lane, size,
+                sums, peak2);
+    table_round(w1, (u2 && u3) ? id3 : id1, (u2 && u3) ? M : C, table, scratch[warp], lane, size, sums, peak2);
+    table_round(w2, id1, C, table, scratch[warp], lane, size, sums, peak2);
   }
   __syncthreads();
   table_flush(table, size, sums, peak2);
@@ -1008,9 +1085,15 @@ template <typename T, bool KAHAN>
 __global__ void ccl_peakval(const T *__restrict__ phi, const float *__restrict__ cphi, const T *__restrict__ pi,
                             const float *__restrict__ cpi, int N, const DivN dn, const Consts k, int dpeak, int n,
                             const long long *__restrict__ peakpos, double *__restrict__ peakval) {
-  const size_t NN = (size_t)N * N;
+  const size_t NN = (size_t)N * N, V = NN * N;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    // every island has a site, so its peak lies on the lattice; a position
+    // off it (an island whose statistics were never written) reads nothing
     const size_t i = (size_t)peakpos[j] - NN;
+    if (i >= V) {
+      peakval[j] = __longlong_as_double(0x7ff8000000000000ll);
+      continue;
+    }
     peakval[j] = dpeak ? site_delta_stats<T, KAHAN>(phi, cphi, pi, cpi, N, dn, k, i) : val(phi, cphi, i);
   }
 }

@@ -36,6 +36,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "float_pair.cuh"
 #include "phn_internal.h"
 #include "site_terms.cuh"
 
@@ -261,16 +262,20 @@ __global__ void __launch_bounds__(SPEC_THREADS) bin_sums(const C *__restrict__ f
 // grows, non-increasing on [N/2, N) where it falls (checked per key table by
 // keys_monotone; bin_sums serves a table that fails the check).  A warp walks
 // a half row in chunks of 32 lanes x RUN_Q consecutive modes; each lane
-// loads its own RUN_Q modes (keys and both spectra: 3 RUN_Q independent
-// loads in flight, contiguous per lane, so the lines the warp touches serve
-// it from L1) and sums the runs of equal bins in registers.  A run inside a
-// lane's modes has a bin no other lane of the chunk holds (monotone bins),
-// so it adds to the warp histogram without a conflict; the runs that cross
-// lanes join in one segmented scan per chunk (once per 256 modes, against
-// once per 32 in bin_sums), and each closes in one lane.  The order of every
-// addition is fixed, so the sums are the same run to run.
-constexpr int RUN_Q = 8;
-constexpr int RUN_WARPS = 4;  // 128 threads: histograms of up to 1024 bins
+// loads its own RUN_Q modes (keys as one 16-byte word where the edge is a
+// multiple of 16, both spectra at fixed offsets from one address per lane)
+// and sums the runs of equal bins in registers.  Within a chunk the bins are
+// monotone, so every run has a bin no other run of the chunk has: the runs
+// inside a lane's modes are staged in shared memory as they close (one
+// 16-byte store, no branch around a histogram update per mode) and added to
+// the warp histogram after the loop, all lanes at once; the runs that cross
+// lanes join in one segmented scan per chunk (it stops at the longest
+// segment), and each closes in one lane.  Each histogram cell takes at most
+// one addition per chunk, in chunk order, so the sums are the same run to
+// run.
+constexpr int RUN_Q = 4;
+constexpr int RUN_STAGE = RUN_Q - 2;  // runs strictly inside a lane's modes
+constexpr int RUN_WARPS = 4;          // 128 threads: histograms of up to 1024 bins
 constexpr int RUN_THREADS = 32 * RUN_WARPS;
 constexpr int RUN_BLOCKS_PER_SM = 6;  // the resident blocks at 80 registers
 
@@ -280,121 +285,166 @@ __device__ __forceinline__ void run_flush(CompF *hF, CompF *hK, CompF *hQ, int b
   hist_add(hQ[bin], q);
 }
 
-__global__ void __launch_bounds__(RUN_THREADS, 6) bin_runs(const float2 *__restrict__ fphi, const float2 *__restrict__ fpi,
-                                                       const unsigned short *__restrict__ keys, int N, int nbins,
-                                                       double *__restrict__ partials) {
+// One chunk of a half row: MIRROR = 0 for px in [0, N/2) (modes at
+// direct + px), 1 for [N/2, N) (px = N/2 at direct + N/2, the others at
+// mirror - px).
+template <int MIRROR>
+__device__ __forceinline__ void run_chunk(const float2 *__restrict__ fphi, const float2 *__restrict__ fpi,
+                                          const unsigned short *__restrict__ keys, long long krow, long long direct,
+                                          long long mirror, int h, int c0, int x1, bool vkeys, int lane, CompF *hF,
+                                          CompF *hK, CompF *hQ, float4 *stage) {
+  const unsigned full = 0xffffffffu;
+  const int cn = min(32 * RUN_Q, x1 - c0);
+  const int nm = max(0, min(RUN_Q, cn - lane * RUN_Q));
+  const int px0 = c0 + lane * RUN_Q;
+  // the lane's modes, loaded together
+  unsigned kk[RUN_Q];
+  float2 va[RUN_Q], vb[RUN_Q];
+  const unsigned short *pk = keys + krow + px0;
+  if (vkeys && nm == RUN_Q) {  // one aligned word: krow and px0 are multiples of RUN_Q
+    unsigned ww[RUN_Q / 2];
+    if constexpr (RUN_Q == 8) {
+      const uint4 w = *(const uint4 *)pk;
+      ww[0] = w.x;
+      ww[1] = w.y;
+      ww[2] = w.z;
+      ww[3] = w.w;
+    } else {
+      const uint2 w = *(const uint2 *)pk;
+      ww[0] = w.x;
+      ww[1] = w.y;
+    }
+#pragma unroll
+    for (int m = 0; m < RUN_Q; m += 2) {
+      kk[m] = ww[m / 2] & 0xffffu;
+      kk[m + 1] = ww[m / 2] >> 16;
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < RUN_Q; ++m) kk[m] = m < nm ? pk[m] : 0u;
+  }
+  const long long base = MIRROR ? mirror - px0 : direct + px0;
+  const float2 *pa = fphi + base, *pb = fpi + base;
+#pragma unroll
+  for (int m = 0; m < RUN_Q; ++m) {
+    if (m < nm) {
+      va[m] = MIRROR ? pa[-m] : pa[m];
+      vb[m] = MIRROR ? pb[-m] : pb[m];
+    }
+  }
+  if (MIRROR && px0 == h && nm > 0) {  // px = N/2 is a direct mode
+    va[0] = fphi[direct + h];
+    vb[0] = fpi[direct + h];
+  }
+  // runs of the lane's modes: the first (fb, F), the ones strictly inside
+  // (staged), the last (cur, a: the whole of them when through)
+  int fb = -1, cur = -1, ns = 0;
+  float F0 = 0.f, F1 = 0.f, F2 = 0.f, a0 = 0.f, a1 = 0.f, a2 = 0.f;
+  bool first_open = true;
+#pragma unroll
+  for (int m = 0; m < RUN_Q; ++m) {
+    if (m < nm) {
+      float f = mag2v(va[m]), k = mag2v(vb[m]), q = dotv(va[m], vb[m]);
+      if (kk[m] & KEY_WEIGHT2) {  // exact doubling
+        f += f;
+        k += k;
+        q += q;
+      }
+      const int b = (int)(kk[m] & KEY_BIN);
+      const bool nw = b != cur;  // a run starts at m
+      const bool close = nw && cur >= 0;
+      if (close && first_open) {
+        fb = cur;
+        F0 = a0;
+        F1 = a1;
+        F2 = a2;
+      }
+      if (close && !first_open) stage[ns++ * 32 + lane] = make_float4(__int_as_float(cur), a0, a1, a2);
+      first_open = first_open && !close;
+      cur = b;
+      a0 = nw ? f : a0 + f;
+      a1 = nw ? k : a1 + k;
+      a2 = nw ? q : a2 + q;
+    }
+  }
+  const int lb = cur;
+  const bool through = nm > 0 && first_open;
+  if (through) fb = lb;
+  // runs across lanes: carry C = the run through the lane's last mode
+  const int lb_prev = __shfl_up_sync(full, lb, 1);
+  const bool conn = lane > 0 && nm > 0 && lb_prev >= 0 && fb == lb_prev;
+  const unsigned heads = __ballot_sync(full, !(through && conn));
+  const int start = 31 - __clz(heads & (full >> (31 - lane)));
+  // the scan stops at the first step that no lane's segment reaches back to
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    if (!__any_sync(full, lane - off >= start)) break;  // uniform per warp
+    const float u0 = __shfl_up_sync(full, a0, off), u1 = __shfl_up_sync(full, a1, off),
+                u2 = __shfl_up_sync(full, a2, off);
+    if (lane - off >= start) {
+      a0 += u0;
+      a1 += u1;
+      a2 += u2;
+    }
+  }
+  const float p0 = __shfl_up_sync(full, a0, 1), p1 = __shfl_up_sync(full, a1, 1), p2 = __shfl_up_sync(full, a2, 1);
+  const bool conn_next = __shfl_down_sync(full, conn, 1) && lane < 31;
+  // every run of the chunk has its own bin: the closing adds touch distinct
+  // cells and go in any order
+  if (nm > 0 && !through) {  // the first run closes at the lane's first bin change
+    if (conn) {
+      F0 += p0;
+      F1 += p1;
+      F2 += p2;
+    }
+    run_flush(hF, hK, hQ, fb, F0, F1, F2);
+  }
+  if (nm > 0 && !conn_next) run_flush(hF, hK, hQ, lb, a0, a1, a2);
+  const int nsmax = __reduce_max_sync(full, (unsigned)ns);
+  for (int j = 0; j < nsmax; ++j) {
+    if (j < ns) {
+      const float4 v = stage[j * 32 + lane];
+      run_flush(hF, hK, hQ, __float_as_int(v.x), v.y, v.z, v.w);
+    }
+  }
+  __syncwarp();  // the histogram and the stage are read by the next chunk
+}
+
+__global__ void __launch_bounds__(RUN_THREADS, RUN_BLOCKS_PER_SM)
+    bin_runs(const float2 *__restrict__ fphi, const float2 *__restrict__ fpi, const unsigned short *__restrict__ keys,
+             int N, int nbins, double *__restrict__ partials) {
   extern __shared__ double run_mem[];
-  CompF *hist = (CompF *)run_mem;  // [RUN_WARPS][3][nbins]
+  CompF *hist = (CompF *)run_mem;                                      // [RUN_WARPS][3][nbins]
+  float4 *stage_all = (float4 *)(run_mem + (size_t)RUN_WARPS * 3 * nbins);  // [RUN_WARPS][RUN_STAGE][32]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < RUN_WARPS * 3 * nbins; i += RUN_THREADS) hist_zero(hist[i]);
   __syncthreads();
   CompF *hF = hist + (size_t)warp * 3 * nbins, *hK = hF + nbins, *hQ = hK + nbins;
-  const unsigned full = 0xffffffffu;
+  float4 *stage = stage_all + (size_t)warp * RUN_STAGE * 32;
   const int h = N / 2, M = N / 2 + 1;
   const int nrows = M * N;
+  const bool vkeys = N % (2 * RUN_Q) == 0;  // every chunk's keys start on a RUN_Q-mode boundary
   for (int row = blockIdx.x * RUN_WARPS + warp; row < nrows; row += gridDim.x * RUN_WARPS) {
     const int py = row % M, pz = row / M;
     const long long krow = (long long)row * N;
     const long long direct = ((long long)pz * N + py) * M;
     const long long mirror = ((long long)((N - pz) % N) * N + (N - py) % N) * M + N;
-    for (int half = 0; half < 2; ++half) {
-      const int x1 = half ? N : h;
-      for (int c0 = half ? h : 0; c0 < x1; c0 += 32 * RUN_Q) {
-        const int cn = min(32 * RUN_Q, x1 - c0);
-        // the lane's modes, loaded together
-        const int nm = max(0, min(RUN_Q, cn - lane * RUN_Q));
-        const int px0 = c0 + lane * RUN_Q;
-        unsigned kk[RUN_Q];
-        float2 va[RUN_Q], vb[RUN_Q];
-#pragma unroll
-        for (int m = 0; m < RUN_Q; ++m) {
-          if (m < nm) {
-            const int px = px0 + m;
-            kk[m] = keys[krow + px];
-            const long long mi = px <= h ? direct + px : mirror - px;
-            va[m] = fphi[mi];
-            vb[m] = fpi[mi];
-          }
-        }
-        // runs of the lane's modes: the first (fb), the interior ones
-        // (flushed here), the last (lb; the whole segment when through)
-        int fb = -1, cur = -1;
-        float F0 = 0.f, F1 = 0.f, F2 = 0.f, a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        bool first_open = true;
-#pragma unroll
-        for (int m = 0; m < RUN_Q; ++m) {
-          if (m < nm) {
-            float f = mag2v(va[m]), k = mag2v(vb[m]), q = dotv(va[m], vb[m]);
-            if (kk[m] & KEY_WEIGHT2) {  // exact doubling
-              f += f;
-              k += k;
-              q += q;
-            }
-            const int b = (int)(kk[m] & KEY_BIN);
-            if (b != cur) {
-              if (cur >= 0) {
-                if (first_open) {
-                  fb = cur;
-                  F0 = a0;
-                  F1 = a1;
-                  F2 = a2;
-                  first_open = false;
-                } else {
-                  run_flush(hF, hK, hQ, cur, a0, a1, a2);
-                }
-              }
-              cur = b;
-              a0 = f;
-              a1 = k;
-              a2 = q;
-            } else {
-              a0 += f;
-              a1 += k;
-              a2 += q;
-            }
-          }
-        }
-        const int lb = cur;
-        const bool through = nm > 0 && first_open;
-        if (through) fb = lb;
-        __syncwarp();  // interior runs added
-        // runs across lanes: carry C = the run through the lane's last mode
-        const int lb_prev = __shfl_up_sync(full, lb, 1);
-        const bool conn = lane > 0 && nm > 0 && lb_prev >= 0 && fb == lb_prev;
-        const unsigned heads = __ballot_sync(full, !(through && conn));
-        const int start = 31 - __clz(heads & (full >> (31 - lane)));
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          const float u0 = __shfl_up_sync(full, a0, off), u1 = __shfl_up_sync(full, a1, off),
-                      u2 = __shfl_up_sync(full, a2, off);
-          if (lane - off >= start) {
-            a0 += u0;
-            a1 += u1;
-            a2 += u2;
-          }
-        }
-        const float p0 = __shfl_up_sync(full, a0, 1), p1 = __shfl_up_sync(full, a1, 1),
-                    p2 = __shfl_up_sync(full, a2, 1);
-        const bool conn_next = __shfl_down_sync(full, conn, 1) && lane < 31;
-        if (nm > 0 && !through) {  // the first run closes at the lane's first bin change
-          if (conn) {
-            F0 += p0;
-            F1 += p1;
-            F2 += p2;
-          }
-          run_flush(hF, hK, hQ, fb, F0, F1, F2);
-        }
-        __syncwarp();
-        if (nm > 0 && !conn_next) run_flush(hF, hK, hQ, lb, a0, a1, a2);
-        __syncwarp();
-      }
-    }
+    for (int c0 = 0; c0 < h; c0 += 32 * RUN_Q)
+      run_chunk<0>(fphi, fpi, keys, krow, direct, mirror, h, c0, h, vkeys, lane, hF, hK, hQ, stage);
+    for (int c0 = h; c0 < N; c0 += 32 * RUN_Q)
+      run_chunk<1>(fphi, fpi, keys, krow, direct, mirror, h, c0, N, vkeys, lane, hF, hK, hQ, stage);
   }
   __syncthreads();
+  // the warps' cells (value s - c) fold in float pairs and widen once: the
+  // grid is one wave, so every block reaches this fold at the same moment,
+  // and FP64 here queued on GB300's narrow FP64 pipe
   for (int j = threadIdx.x; j < 3 * nbins; j += RUN_THREADS) {
-    double s = 0.0;
-    for (int w = 0; w < RUN_WARPS; ++w) s += hist_value(hist[(size_t)w * 3 * nbins + j]);
-    partials[(size_t)blockIdx.x * 3 * nbins + j] = s;
+    float sh = 0.f, sl = 0.f;
+    for (int w = 0; w < RUN_WARPS; ++w) {
+      const CompF c = hist[(size_t)w * 3 * nbins + j];
+      fpair_add(sh, sl, c.s, -c.c);
+    }
+    partials[(size_t)blockIdx.x * 3 * nbins + j] = (double)sh + (double)sl;
   }
 }
 
@@ -547,8 +597,11 @@ static int build_keys(phn_handle *h, unsigned short *keys, int *counts, int nbin
   return PHN_OK;
 }
 
-// Shared memory of bin_runs: the warp histograms.
-static size_t run_smem(int nbins) { return (size_t)RUN_WARPS * 3 * nbins * sizeof(double); }
+// Shared memory of bin_runs: the warp histograms, then the warps' stages of
+// runs inside a lane (16 bytes each).
+static size_t run_smem(int nbins) {
+  return (size_t)RUN_WARPS * 3 * nbins * sizeof(double) + (size_t)RUN_WARPS * RUN_STAGE * 32 * sizeof(float4);
+}
 
 static int spec_init(phn_handle *h) {
   if (h->spec) return PHN_OK;
@@ -602,7 +655,6 @@ static int bin_spectra(phn_handle *h, const void *fa, const void *fb, const unsi
 static int spectrum_component(phn_handle *h, int a, const unsigned short *keys, int nbins, double *partials,
                               double *bins, double scale, bool mono, std::vector<double> &hb) {
   SpecState *s = (SpecState *)h->spec;
-  const int N = h->p.N;
   const bool dbl = h->p.precision == PHN_FP64;
   cufftResult fr;
   if (dbl) {
