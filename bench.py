@@ -914,6 +914,7 @@ def analysis_form(N: int, reps: int = 5, steps: int = 200, precisions=("fp32", "
         lat.correlation_functions()  # warm-up: cuFFT plan, key tables
         lat.spectrum_uniform(64)
         ms_spec, spec = timed(lat.correlation_functions)
+        t_fft, t_bin = lat.spectrum_timing()  # device time of the last call
         ms_uni, _ = timed(lambda: lat.spectrum_uniform(64))
         rho_thr = 2.0 * avg[O_AVG_ENERGY]
         # warm-up calls size the record buffers to the island counts
@@ -921,16 +922,42 @@ def analysis_form(N: int, reps: int = 5, steps: int = 200, precisions=("fp32", "
         n_rho = lat.full_analysis(rho_thr, mode=L.ISLAND_ENERGY, z_periodic=True, labels=False,
                                   max_out=1 << 23)[1].shape[0]
         ms_isl, isl = timed(lambda: lat.full_analysis(thr, labels=False, max_out=n_isl))
+        # the same with the records copied into a page-locked host buffer
+        pinned = np.zeros((n_isl, len(L.ISLAND_FIELDS)))
+        L.check(lat.lib.phn_pin_host(pinned.ctypes.data, pinned.nbytes))
+        try:
+            ms_isl_pin, isl_pin = timed(lambda: lat.full_analysis(thr, labels=False, out=pinned))
+            # the same islands (index, size, volume, peak and seed positions
+            # exact; the FP64 sums add block partials in arrival order, so they
+            # agree to rounding from call to call)
+            a, b = isl_pin[1], isl[1]
+            exact = [0, 1, 2, 7, 8, 9]  # index, size, volume, peak position and value, seed
+            pin_equal = bool(a.shape == b.shape and np.array_equal(a[:, exact], b[:, exact]) and
+                             np.allclose(a, b, rtol=1e-12, atol=0))
+        finally:
+            lat.lib.phn_unpin_host(pinned.ctypes.data)
         ms_isl_dev, _ = timed(lambda: lat.full_analysis_device(thr))
         ms_rho, rho = timed(lambda: lat.full_analysis(rho_thr, mode=L.ISLAND_ENERGY, z_periodic=True, labels=False,
                                                       max_out=n_rho))
         elem = 8 if prec == L.FP32 else 16  # complex bytes
         half = N * N * (N // 2 + 1) * elem
+        # the binning pass reads both half-spectra and the key table once:
+        # its roofline against the measured copy bandwidth
+        bin_bytes = 2 * half + 2 * N * N * (N // 2 + 1)
+        peak, peak_kind = peaks()
         out[name] = {"spectrum_ms": ms_spec, "spectrum_bins": int(spec[3].size),
+                     "spectrum_transforms_device_ms": t_fft, "spectrum_binning_device_ms": t_bin,
+                     "spectrum_binning_bytes": bin_bytes,
+                     "spectrum_binning_gbs": bin_bytes / (t_bin * 1e-3) / 1e9 if t_bin > 0 else None,
+                     "spectrum_binning_frac_of_measured_hbm":
+                         (bin_bytes / (t_bin * 1e-3) / 1e9 / peak) if t_bin > 0 else None,
+                     "hbm_peak_gbs": peak, "hbm_peak_kind": peak_kind,
                      "spectrum_uniform64_ms": ms_uni,
                      "spectrum_halfspectra_bytes": 2 * half,
                      "islands_reference_mask_ms": ms_isl, "islands_reference_mask_count": int(isl[1].shape[0]),
                      "islands_reference_mask_device_records_ms": ms_isl_dev,
+                     "islands_reference_mask_pinned_records_ms": ms_isl_pin,
+                     "islands_pinned_records_equal": pin_equal,
                      "islands_reference_mask_sites": int(isl[1][:, 1].sum()),
                      "islands_energy_mask_ms": ms_rho, "islands_energy_mask_count": int(rho[1].shape[0]),
                      "islands_energy_mask_sites": int(rho[1][:, 1].sum()),

@@ -187,6 +187,14 @@ int phn_spectrum_energy(phn_handle *h, double *D, int *counts, int nbins);
  * 1 <= nbins <= 1024; F, K, Q hold nbins*Nc, counts nbins. */
 int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double *Q, int *counts);
 
+/* Device time of the last phn_spectrum, phn_spectrum_uniform or
+ * phn_spectrum_energy call on this handle (no reference counterpart; CUDA
+ * events on the handle's stream): transform_ms, the R2C transforms of phi
+ * and pi summed over the components (0 for phn_spectrum_energy, whose
+ * contrast field is transformed with it); binning_ms, the binning and
+ * per-bin fold kernels.  PHN_ERR_INVALID before the first spectrum call. */
+int phn_spectrum_timing(const phn_handle *h, double *transform_ms, double *binning_ms);
+
 /* SetInitialConditions() (initialconditions.cpp:45-723) for `initialize 3`,
  * static or expanding box (the handle's `expanding`, with its T0 and H0), no
  * charge, on the device: drand48's stream from srand48(seed)

@@ -93,6 +93,7 @@ _SIGS = {
     "phn_spectrum": (_I, [ctypes.c_void_p, _PD, _PD, _PD, _PI, _I]),
     "phn_spectrum_uniform": (_I, [ctypes.c_void_p, _I, _PD, _PD, _PD, _PI]),
     "phn_spectrum_energy": (_I, [ctypes.c_void_p, _PD, _PI, _I]),
+    "phn_spectrum_timing": (_I, [ctypes.c_void_p, _PD, _PD]),
     "phn_initial_conditions": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams)]),
     "phn_initial_conditions_mode": (_I, [ctypes.c_void_p, ctypes.POINTER(PhnIcParams), ctypes.POINTER(PhnIcMode)]),
     "phn_islands_lookup": (_I, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), _I, _PI]),

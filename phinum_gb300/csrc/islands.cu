@@ -940,13 +940,18 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ 
     const int prv[4] = {pr.x, pr.y, pr.z, pr.w};
     const bool any = pr.x >= 0 || pr.y >= 0 || pr.z >= 0 || pr.w >= 0;
     if (__ballot_sync(full, any) == 0) continue;  // uniform per warp
+    // the island numbers of the four sites, fetched with the fields (a run
+    // that closes in this lane takes its number from one of its sites)
+    int idv[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) idv[j] = prv[j] >= 0 ? ids[prv[j]] : -1;
     int x0 = 0, y = 0, z = 0;
     if (i0 < s1) site_xyz(dn, N, i0, x0, y, z);
     RunSums<A> L, M, R;
     run_zero(L);
     run_zero(M);
     run_zero(R);
-    int mpar = -1, rpar = -1;  // the parent of a site of M and of R, for the island lookup
+    int mid = -1, rid = -1;  // the island of M and of R
     if (any) {
       A c[4], p[4], fy[4], fz[4];
       const size_t row = (size_t)z * NN + (size_t)y * N;
@@ -961,7 +966,7 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ 
         if (prv[j] < 0) {
           if (gap && R.n > 0) {
             M = R;
-            mpar = rpar;
+            mid = rid;
           }
           run_zero(R);
           gap = true;
@@ -984,7 +989,7 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ 
             run_add(L, t);
           } else {
             run_add(R, t);
-            rpar = prv[j];
+            rid = idv[j];
           }
         }
       }
@@ -1013,7 +1018,7 @@ __global__ void __launch_bounds__(CCL_THREADS) ccl_stats4(const T *__restrict__ 
       const RunSums<A> Cp = run_shfl_up(C, 1);
       if (u2 && conn) run_add(L, Cp);
     }
-    const int id1 = u1 ? ids[pr.w] : -1, id2 = u2 ? ids[pr.x] : -1, id3 = u3 ? ids[mpar] : -1;
+    const int id1 = u1 ? idv[3] : -1, id2 = u2 ? idv[0] : -1, id3 = u3 ? mid : -1;
     // a lane's own closed runs of one island combine first
     if (u3 && u2 && id3 == id2) {
       run_add(L, M);

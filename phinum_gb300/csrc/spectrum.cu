@@ -70,6 +70,11 @@ struct SpecState {
   int *u_counts;
   unsigned short *u_keys;
   std::vector<int> u_h_counts;
+  // device time of the last spectrum call (phn_spectrum_timing): events
+  // around the transforms and around the binning of each component
+  cudaEvent_t ev[3];
+  bool ev_ok, pending_transform;
+  double t_transform, t_binning;
 };
 
 constexpr unsigned KEY_WEIGHT2 = 0x8000u;  // the mode is counted twice (py not 0 or N/2)
@@ -325,11 +330,28 @@ __device__ __forceinline__ void run_chunk(const float2 *__restrict__ fphi, const
   }
   const long long base = MIRROR ? mirror - px0 : direct + px0;
   const float2 *pa = fphi + base, *pb = fpi + base;
+  // the lane's RUN_Q modes are consecutive: as 16-byte words where the
+  // lowest one starts on a 16-byte boundary (the row's parity, uniform per
+  // warp), else one mode per load
+  const long long lo = MIRROR ? base - (RUN_Q - 1) : base;
+  if (nm == RUN_Q && (lo & 1) == 0) {
+    const float4 *qa = (const float4 *)(fphi + lo), *qb = (const float4 *)(fpi + lo);
 #pragma unroll
-  for (int m = 0; m < RUN_Q; ++m) {
-    if (m < nm) {
-      va[m] = MIRROR ? pa[-m] : pa[m];
-      vb[m] = MIRROR ? pb[-m] : pb[m];
+    for (int w = 0; w < RUN_Q / 2; ++w) {
+      const float4 xa = qa[w], xb = qb[w];
+      const int m0 = MIRROR ? RUN_Q - 1 - 2 * w : 2 * w, m1 = MIRROR ? m0 - 1 : m0 + 1;
+      va[m0] = make_float2(xa.x, xa.y);
+      va[m1] = make_float2(xa.z, xa.w);
+      vb[m0] = make_float2(xb.x, xb.y);
+      vb[m1] = make_float2(xb.z, xb.w);
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < RUN_Q; ++m) {
+      if (m < nm) {
+        va[m] = MIRROR ? pa[-m] : pa[m];
+        vb[m] = MIRROR ? pb[-m] : pb[m];
+      }
     }
   }
   if (MIRROR && px0 == h && nm > 0) {  // px = N/2 is a direct mode
@@ -557,6 +579,8 @@ void spectrum_release(phn_handle *h) {
   cudaFree(s->u_keys);
   cudaFree(s->dfield);
   cudaFree(s->dsum);
+  if (s->ev_ok)
+    for (int j = 0; j < 3; ++j) cudaEventDestroy(s->ev[j]);
   delete s;
   h->spec = nullptr;
 }
@@ -628,6 +652,8 @@ static int spec_init(phn_handle *h) {
   CKS(cudaMalloc(&s->counts, (size_t)s->nbins * sizeof(int)));
   CKS(cudaMalloc(&s->flag, sizeof(int)));
   CKS(cudaMalloc(&s->keys, n_modes(N) * sizeof(unsigned short)));
+  for (int j = 0; j < 3; ++j) CKS(cudaEventCreate(&s->ev[j]));
+  s->ev_ok = true;
   std::vector<double> tab(N);
   for (int n = 0; n < N; ++n) tab[n] = lattice_p(n, N, h->p.a);
   CKS(cudaMemcpy(s->ptab, tab.data(), N * sizeof(double), cudaMemcpyHostToDevice));
@@ -657,6 +683,8 @@ static int spectrum_component(phn_handle *h, int a, const unsigned short *keys, 
   SpecState *s = (SpecState *)h->spec;
   const bool dbl = h->p.precision == PHN_FP64;
   cufftResult fr;
+  cudaEventRecord(s->ev[0], h->stream);
+  s->pending_transform = true;  // bin_spectra adds the transforms' time
   if (dbl) {
     double *phi = (double *)h->phi[h->cur] + (size_t)a * h->V, *pi = (double *)h->pi + (size_t)a * h->V;
     fr = cufftExecD2Z(s->plan, phi, (cufftDoubleComplex *)s->fphi);
@@ -678,6 +706,9 @@ static int bin_spectra(phn_handle *h, const void *fa, const void *fb, const unsi
   const int N = h->p.N;
   const bool dbl = h->p.precision == PHN_FP64;
   const size_t smem = (size_t)SPEC_WARPS * 3 * nbins * sizeof(double);
+  const bool transformed = s->pending_transform;  // spectrum_component recorded ev[0]
+  s->pending_transform = false;
+  cudaEventRecord(s->ev[1], h->stream);
   if (dbl)
     bin_sums<double2, double><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
         (const double2 *)fa, (const double2 *)fb, keys, N, nbins, partials);
@@ -694,10 +725,14 @@ static int bin_spectra(phn_handle *h, const void *fa, const void *fb, const unsi
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "fold_blocks");
   h->launches += 2;
+  cudaEventRecord(s->ev[2], h->stream);
   hb.resize((size_t)3 * nbins);
   e = cudaMemcpyAsync(hb.data(), bins, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return cuda_error(e, "spectrum readback");
+  float ms = 0.f;
+  if (transformed && cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]) == cudaSuccess) s->t_transform += ms;
+  if (cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]) == cudaSuccess) s->t_binning += ms;
   return PHN_OK;
 }
 
@@ -725,6 +760,8 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
     return r;
   }
   SpecState *s = (SpecState *)h->spec;
+  s->t_transform = s->t_binning = 0.0;
+  s->pending_transform = false;
   if (nbins < s->nbins) return set_error(PHN_ERR_TRUNCATED, "nbins=%d < %d", nbins, s->nbins);
   const int Nc = h->p.Nc;
   const double f3 = (h->p.a * h->p.a) * h->p.a;  // fftXtoP_direct's a^3 (clusterfft.cpp:187,222)
@@ -748,6 +785,15 @@ int phn_spectrum(phn_handle *h, double *F, double *K, double *Q, int *counts, in
   return PHN_OK;
 }
 
+int phn_spectrum_timing(const phn_handle *h, double *transform_ms, double *binning_ms) {
+  if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
+  const SpecState *s = (const SpecState *)h->spec;
+  if (!s) return set_error(PHN_ERR_INVALID, "no spectrum call on this handle");
+  if (transform_ms) *transform_ms = s->t_transform;
+  if (binning_ms) *binning_ms = s->t_binning;
+  return PHN_OK;
+}
+
 int phn_spectrum_energy(phn_handle *h, double *D, int *counts, int nbins) {
   if (!h) return set_error(PHN_ERR_INVALID, "handle is NULL");
   if (h->p.potential < 2)
@@ -759,6 +805,8 @@ int phn_spectrum_energy(phn_handle *h, double *D, int *counts, int nbins) {
     return r;
   }
   SpecState *s = (SpecState *)h->spec;
+  s->t_transform = s->t_binning = 0.0;
+  s->pending_transform = false;
   if (nbins < s->nbins) return set_error(PHN_ERR_TRUNCATED, "nbins=%d < %d", nbins, s->nbins);
   const int N = h->p.N, Nc = h->p.Nc;
   const bool dbl = h->p.precision == PHN_FP64;
@@ -835,6 +883,8 @@ int phn_spectrum_uniform(phn_handle *h, int nbins, double *F, double *K, double 
     return r;
   }
   SpecState *s = (SpecState *)h->spec;
+  s->t_transform = s->t_binning = 0.0;
+  s->pending_transform = false;
   const int N = h->p.N, Nc = h->p.Nc;
   // p_max = pTmax of momentumspace.cpp:43, the largest lattice |p|
   const double pmax = sqrt(3.0 * (4.0 / (h->p.a * h->p.a)));

@@ -206,6 +206,12 @@ class Lattice:
         L.check(self.lib.phn_spectrum_uniform(self.h, int(nbins), _pd(F), _pd(K), _pd(Q), _pi(C)))
         return F, K, Q, C
 
+    def spectrum_timing(self):
+        """Device time of the last spectrum call: (transforms ms, binning ms)."""
+        t, b = ctypes.c_double(), ctypes.c_double()
+        L.check(self.lib.phn_spectrum_timing(self.h, ctypes.byref(t), ctypes.byref(b)))
+        return t.value, b.value
+
     def spectrum_energy(self):
         """The density-contrast spectrum (withEnergyPS 1): (D[bin*Nc + a], counts)."""
         nb, bs = ctypes.c_int(), ctypes.c_double()
@@ -216,13 +222,25 @@ class Lattice:
         return D, C
 
     def full_analysis(self, thres: float, mode: int = L.ISLAND_REFERENCE, z_periodic: bool = False,
-                      labels: bool = True, max_out: int = 1 << 20):
+                      labels: bool = True, max_out: int = 1 << 20, out=None):
+        """phn_islands: (labels or None, records).  `out`, a caller-owned
+        C-contiguous float64 array of shape (rows, 10) (page-locked with
+        phn_pin_host for a DMA copy), receives the records in place of a new
+        array; the result is then a view of its first rows."""
         lab = np.zeros(self.p.N * self.p.N * (self.p.N + 2), dtype=np.int32) if labels else None
-        recs = np.zeros((max_out, len(L.ISLAND_FIELDS)))
+        if out is not None:
+            if out.dtype != np.float64 or out.ndim != 2 or out.shape[1] != len(L.ISLAND_FIELDS) or \
+                    not out.flags["C_CONTIGUOUS"]:
+                raise ValueError("out: a C-contiguous float64 array of shape (rows, %d)" % len(L.ISLAND_FIELDS))
+            recs, max_out = out, out.shape[0]
+        else:
+            recs = np.zeros((max_out, len(L.ISLAND_FIELDS)))
         n = ctypes.c_int()
         r = self.lib.phn_islands(self.h, float(thres), int(mode), int(bool(z_periodic)),
                                  _pi(lab) if labels else None, _pd(recs), max_out, ctypes.byref(n))
         L.check(r)
+        if out is not None:
+            return lab, recs[:n.value]
         return lab, recs if n.value == max_out else recs[:n.value].copy()
 
     def full_analysis_device(self, thres: float, mode: int = L.ISLAND_REFERENCE, z_periodic: bool = False):
