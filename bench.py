@@ -933,7 +933,7 @@ def analysis_form(N: int, reps: int = 5, steps: int = 200, precisions=("fp32", "
             a, b = isl_pin[1], isl[1]
             exact = [0, 1, 2, 7, 8, 9]  # index, size, volume, peak position and value, seed
             pin_equal = bool(a.shape == b.shape and np.array_equal(a[:, exact], b[:, exact]) and
-                             np.allclose(a, b, rtol=1e-12, atol=0))
+                             np.all(np.abs(a - b) <= 1e-12 * np.abs(b).max(axis=0)))
         finally:
             lat.lib.phn_unpin_host(pinned.ctypes.data)
         ms_isl_dev, _ = timed(lambda: lat.full_analysis_device(thr))

@@ -60,6 +60,7 @@ def test_null_handles_are_status_codes(L):
         lambda: lib.phn_adjoint_backward(None, None, None, None),
         lambda: lib.phn_adjoint_set_forward_precision(None, 0),
         lambda: lib.phn_adjoint_info(None, None, None, None),
+        lambda: lib.phn_spectrum_timing(None, ctypes.byref(d), ctypes.byref(d)),
     ]
     for c in calls:
         assert c() == L.ERR_INVALID

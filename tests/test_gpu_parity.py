@@ -519,6 +519,43 @@ def test_islands_device_records_equal_host_records(precision, N):
     lat.close()
 
 
+def test_records_into_a_caller_buffer_and_spectrum_timing():
+    """full_analysis(out=...) writes the records into a caller-owned,
+    page-locked buffer (phn_pin_host): the same islands as a fresh array
+    (ids, sizes, peaks exact; the FP64 sums add block partials in arrival
+    order, so they agree to rounding); phn_spectrum_timing reports the device
+    time of the last spectrum call's transforms and binning."""
+    import inputs
+    from phinum_gb300 import _lib as L
+    PL = gpu()
+    N = 64
+    phi_i, pi_i = inputs.lattice_fields(N, 1, 12)
+    phi, pi = O.to_ref_layout(phi_i), O.to_ref_layout(pi_i)
+    thr = float(np.quantile(np.sqrt(phi_i ** 2 + pi_i ** 2), 0.6))
+    lat = PL.Lattice(PL.Params(N=N, precision=1))
+    lat.upload(phi, pi)
+    _, recs = lat.full_analysis(thr, labels=False)
+    buf = np.zeros((recs.shape[0] + 5, len(L.ISLAND_FIELDS)))
+    L.check(lat.lib.phn_pin_host(buf.ctypes.data, buf.nbytes))
+    try:
+        _, got = lat.full_analysis(thr, labels=False, out=buf)
+        assert got.shape == recs.shape and np.shares_memory(got, buf)
+        exact = [0, 1, 2, 7, 8, 9]
+        assert np.array_equal(got[:, exact], recs[:, exact])
+        assert np.all(np.abs(got - recs) <= 1e-12 * np.abs(recs).max(axis=0))
+        with pytest.raises(ValueError):
+            lat.full_analysis(thr, labels=False, out=np.zeros((4, 3)))
+    finally:
+        lat.lib.phn_unpin_host(buf.ctypes.data)
+    lat.correlation_functions()
+    t, b = lat.spectrum_timing()
+    assert t > 0 and b > 0
+    lat.spectrum_uniform(64)
+    t, b = lat.spectrum_timing()
+    assert t > 0 and b > 0
+    lat.close()
+
+
 @pytest.mark.parametrize("N", [24, 47, 100])
 def test_islands_at_edges_that_are_not_powers_of_two(N):
     """Rows that straddle the 32-site warp segments of the labelling (its
