@@ -412,8 +412,10 @@ int phn_stats(const phn_handle *h, long long *kernel_launches, double *last_evol
  * `main` per seed) evolved together: one persistent kernel per step walks a
  * work list of (member, tile) items, and the step loop runs as a captured CUDA
  * graph.  Members: FP32, Nc = 1, N a multiple of 32, theory 0 or 1 with any
- * couplings, static box; they share a, dt and T0 (one clock).  A member's fields are bit-identical to
- * those of a single-lattice handle with the same inputs. */
+ * couplings; they share a, dt, T0 and the box (all static, or all expanding
+ * with one H0): one clock, whose kick factor, drift factor and scale factor
+ * per step the graph reads from a device table.  A member's fields are
+ * bit-identical to those of a single-lattice handle with the same inputs. */
 typedef struct phn_ensemble phn_ensemble;
 int phn_ensemble_create(const phn_params *members, int n, phn_ensemble **out);
 int phn_ensemble_destroy(phn_ensemble *e);

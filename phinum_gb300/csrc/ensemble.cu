@@ -17,6 +17,7 @@
 // the live ensemble.  Steps run in chunks of kGraphSteps captured once as a
 // CUDA graph; the chunk's kick/drift factors are read from a device table
 // refilled before each launch, so one graph serves the whole run.
+#include <math.h>
 #include <string.h>
 
 #include <vector>
@@ -49,21 +50,43 @@ constexpr EnsTile kEnsTiles[] = {{8, 16, false}, {4, 16, false}, {8, 8, false}, 
 constexpr int kNumEnsTiles = 11;
 constexpr int kGraphSteps = 50;
 
+// The FP32 couplings of theories 0 and 1 at scale factor sf, for an
+// expanding member: the fields of at_scale_factor (api.cu) that the FP32 kick
+// and observation read, by the same FP64 expressions, so that a member gets
+// the bits a single lattice gets (dynamics.cpp:88-104, fieldanalysis.cpp:
+// 461-615).  Once per work item: a few FP64 operations against the item's
+// thousands of sites.
+__device__ __forceinline__ void couplings_at(Consts &k, double sf) {
+  k.sf = sf;
+  k.mmM_f = (float)(k.mmM * sf * sf);
+  k.h_f = (float)(k.h * sf * sf * sf);
+  k.mmh_f = (float)(k.mm_half_M * sf * sf);
+  if (k.theory == 0) {
+    k.c6_f = (float)(1.0 / (k.kappa * k.kappa * k.c120 * sf * sf));
+    k.e6_f = (float)(1.0 / (k.c720 * sf * sf));
+  }
+  k.hub_f = (float)(k.H0 / sf);
+}
+
+// factors: [3 per step] kick factor, drift factor, the kick's scale factor;
+// sf_obs: the scale factor of an observation (MODE_OBS).
 template <int TY, int MODE>
 __global__ void __launch_bounds__(32 * TY) ens_step(const EnsMember *__restrict__ members,
                                                     const EnsItem *__restrict__ items, int nitems,
                                                     const float *__restrict__ phi, float *__restrict__ phi_out,
                                                     float *__restrict__ pi, const double *__restrict__ factors,
-                                                    int slot, double *__restrict__ partials) {
-  const float fk = MODE == MODE_OBS ? 0.f : (float)factors[2 * slot];
-  const float fd = MODE == MODE_OBS ? 0.f : (float)factors[2 * slot + 1];
+                                                    int slot, double sf_obs, double *__restrict__ partials) {
+  const float fk = MODE == MODE_OBS ? 0.f : (float)factors[3 * slot];
+  const float fd = MODE == MODE_OBS ? 0.f : (float)factors[3 * slot + 1];
+  const double sf = MODE == MODE_OBS ? sf_obs : factors[3 * slot + 2];
   const int tid = threadIdx.x + 32 * threadIdx.y;
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const EnsItem I = items[it];
     const int N = members[I.member].N;
     const int theory = members[I.member].theory;
     const long long off = members[I.member].off;
-    const Consts k = members[I.member].k;
+    Consts k = members[I.member].k;
+    if (k.expansion) couplings_at(k, sf);  // uniform per item
     const float *f = phi + off;
     float *fo = phi_out + off;
     float *pp = pi + off;
@@ -126,16 +149,18 @@ __global__ void __launch_bounds__(32 * W) ens_step_x4(const EnsMember *__restric
                                                       const EnsItem *__restrict__ items, int nitems,
                                                       const float *__restrict__ phi, float *__restrict__ phi_out,
                                                       float *__restrict__ pi, const double *__restrict__ factors,
-                                                      int slot, double *__restrict__ partials) {
-  const float fk = MODE == MODE_OBS ? 0.f : (float)factors[2 * slot];
-  const float fd = MODE == MODE_OBS ? 0.f : (float)factors[2 * slot + 1];
+                                                      int slot, double sf_obs, double *__restrict__ partials) {
+  const float fk = MODE == MODE_OBS ? 0.f : (float)factors[3 * slot];
+  const float fd = MODE == MODE_OBS ? 0.f : (float)factors[3 * slot + 1];
+  const double sf = MODE == MODE_OBS ? sf_obs : factors[3 * slot + 2];
   const int tid = threadIdx.x + 32 * threadIdx.y;
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const EnsItem I = items[it];
     const int N = members[I.member].N;
     const int theory = members[I.member].theory;
     const long long off = members[I.member].off;
-    const Consts k = members[I.member].k;
+    Consts k = members[I.member].k;
+    if (k.expansion) couplings_at(k, sf);  // uniform per item
     const float *f = phi + off;
     float *fo = phi_out + off;
     float *pp = pi + off;
@@ -203,35 +228,39 @@ __global__ void __launch_bounds__(32 * W) ens_step_x4(const EnsMember *__restric
 // One block per member folds that member's item records, in item order.
 __global__ void __launch_bounds__(FIN_THREADS) ens_fold(const double *__restrict__ partials,
                                                         const int *__restrict__ item_begin,
-                                                        const EnsMember *__restrict__ members,
+                                                        const EnsMember *__restrict__ members, double sf_obs,
                                                         phn_averages *__restrict__ out) {
   const int m = blockIdx.x;
-  fold_records(partials, item_begin[m], item_begin[m + 1], members[m].k, out + m);
+  Consts k = members[m].k;
+  if (k.expansion) k.sf = sf_obs;  // the fold's expanding-box terms read H0 / sf
+  fold_records(partials, item_begin[m], item_begin[m + 1], k, out + m);
 }
 
 template <int TY, int MODE>
 static cudaError_t ens_launch_t(int grid, const EnsMember *members, const EnsItem *items, int nitems, const float *phi,
-                                float *phi_out, float *pi, const double *factors, int slot, double *partials,
-                                cudaStream_t st) {
-  ens_step<TY, MODE><<<grid, dim3(32, TY), 0, st>>>(members, items, nitems, phi, phi_out, pi, factors, slot, partials);
+                                float *phi_out, float *pi, const double *factors, int slot, double sf_obs,
+                                double *partials, cudaStream_t st) {
+  ens_step<TY, MODE><<<grid, dim3(32, TY), 0, st>>>(members, items, nitems, phi, phi_out, pi, factors, slot, sf_obs,
+                                                    partials);
   return cudaGetLastError();
 }
 
 template <int W, int MODE>
 static cudaError_t ens_launch_x4_t(int grid, const EnsMember *members, const EnsItem *items, int nitems,
                                    const float *phi, float *phi_out, float *pi, const double *factors, int slot,
-                                   double *partials, cudaStream_t st) {
-  ens_step_x4<W, MODE><<<grid, dim3(32, W), 0, st>>>(members, items, nitems, phi, phi_out, pi, factors, slot,
+                                   double sf_obs, double *partials, cudaStream_t st) {
+  ens_step_x4<W, MODE><<<grid, dim3(32, W), 0, st>>>(members, items, nitems, phi, phi_out, pi, factors, slot, sf_obs,
                                                      partials);
   return cudaGetLastError();
 }
 
 static cudaError_t ens_launch(const EnsTile &T, int mode, int grid, const EnsMember *members, const EnsItem *items,
                               int nitems, const float *phi, float *phi_out, float *pi, const double *factors,
-                              int slot, double *partials, cudaStream_t st) {
+                              int slot, double sf_obs, double *partials, cudaStream_t st) {
   const int ty = T.ty;
   if (T.x4) {
-#define PHN_ENS4(WV, MD) return ens_launch_x4_t<WV, MD>(grid, members, items, nitems, phi, phi_out, pi, factors, slot, partials, st)
+#define PHN_ENS4(WV, MD) \
+  return ens_launch_x4_t<WV, MD>(grid, members, items, nitems, phi, phi_out, pi, factors, slot, sf_obs, partials, st)
     if (ty == 8) {
       if (mode == MODE_STEP) PHN_ENS4(8, MODE_STEP);
       if (mode == MODE_STEP_OBS) PHN_ENS4(8, MODE_STEP_OBS);
@@ -247,7 +276,8 @@ static cudaError_t ens_launch(const EnsTile &T, int mode, int grid, const EnsMem
     PHN_ENS4(2, MODE_OBS);
 #undef PHN_ENS4
   }
-#define PHN_ENS(TYV, MD) return ens_launch_t<TYV, MD>(grid, members, items, nitems, phi, phi_out, pi, factors, slot, partials, st)
+#define PHN_ENS(TYV, MD) \
+  return ens_launch_t<TYV, MD>(grid, members, items, nitems, phi, phi_out, pi, factors, slot, sf_obs, partials, st)
   if (ty == 8) {
     if (mode == MODE_STEP) PHN_ENS(8, MODE_STEP);
     if (mode == MODE_STEP_OBS) PHN_ENS(8, MODE_STEP_OBS);
@@ -297,11 +327,14 @@ struct phn_ensemble {
   double *partials;
   int partial_cap;
   phn_averages *d_avg;
-  // clock shared by all members (dynamics.cpp:28-50)
+  // clock shared by all members (dynamics.cpp:28-50); the expanding box's
+  // conformal times and scale factor (dynamics.cpp:196-213)
   double tau, dtau, last_mom, last_field;
+  bool expanding;
+  double H0, tau_c, sf, last_mom_c, last_field_c;
   int steps;
   // factor table and graph
-  double *d_factors;   // [2 * kGraphSteps]
+  double *d_factors;   // [3 * kGraphSteps]: kick, drift, the kick's scale factor
   double *h_factors;   // pinned, grows
   size_t h_factors_cap;
   cudaGraphExec_t graph[2];  // by the parity of cur at launch
@@ -398,7 +431,7 @@ static int ens_set_tile(phn_ensemble *e, int t) {
 
 static int ens_launch_step(phn_ensemble *e, int mode, int slot, int cur) {
   CKE(ens_launch(kEnsTiles[e->tile], mode, e->grid, e->d_members, e->d_items, e->nitems, e->phi[cur],
-                 e->phi[1 - cur], e->pi, e->d_factors, slot, e->partials, e->stream));
+                 e->phi[1 - cur], e->pi, e->d_factors, slot, e->sf, e->partials, e->stream));
   e->launches++;
   return PHN_OK;
 }
@@ -424,14 +457,38 @@ static int ens_build_graph(phn_ensemble *e, int cur) {
   return PHN_OK;
 }
 
-// Host clock for one step (dynamics.cpp:200-236); writes the factors.
-static void ens_clock_step(phn_ensemble *e, double *fk, double *fd) {
+// The expanding box's conformal time and scale factor at tau (the handle's
+// clock, dynamics.cpp:28-50).
+static void ens_conformal(phn_ensemble *e) {
+  e->tau_c = (sqrt(1. + 2. * e->H0 * e->tau) - 1.) / e->H0;
+  e->sf = sqrt(1. + 2. * e->H0 * e->tau);
+}
+
+// Host clock for one step (dynamics.cpp:196-237, as the handle's step):
+// writes f[0] the kick factor, f[1] the drift factor (conformal-time
+// differences in the expanding box), f[2] the scale factor of the kick.
+static void ens_clock_step(phn_ensemble *e, double *f) {
   e->tau += 0.5 * e->dtau;
-  *fk = e->tau - e->last_mom;
+  if (e->expanding) {
+    ens_conformal(e);
+    f[0] = e->tau_c - e->last_mom_c;
+    f[2] = e->sf;
+  } else {
+    f[0] = e->tau - e->last_mom;
+    f[2] = 1.0;
+  }
   e->last_mom = e->tau;
+  e->last_mom_c = e->expanding ? e->tau_c : e->tau;
   e->tau += 0.5 * e->dtau;
-  *fd = e->tau - e->last_field;
+  if (e->expanding) {
+    ens_conformal(e);
+    f[1] = e->tau_c - e->last_field_c;
+  } else {
+    f[1] = e->tau - e->last_field;
+    e->tau_c = e->tau;
+  }
   e->last_field = e->tau;
+  e->last_field_c = e->tau_c;
   e->steps++;
 }
 
@@ -444,11 +501,13 @@ int phn_ensemble_create(const phn_params *members, int n, phn_ensemble **out) {
     int r = validate_params(&members[m]);
     if (r) return r;
     const phn_params &q = members[m];
-    if (q.precision != PHN_FP32 || q.Nc != 1 || q.N % 32 != 0 || q.potential > 1 || q.expanding)
+    if (q.precision != PHN_FP32 || q.Nc != 1 || q.N % 32 != 0 || q.potential > 1)
       return set_error(PHN_ERR_UNSUPPORTED,
-                       "member %d: ensembles take FP32, Nc = 1, N a multiple of 32, theory 0 or 1, static box", m);
-    if (q.a != members[0].a || q.dt != members[0].dt || q.T0 != members[0].T0)
-      return set_error(PHN_ERR_INVALID, "member %d: members share a, dt and T0 (one clock)", m);
+                       "member %d: ensembles take FP32, Nc = 1, N a multiple of 32, theory 0 or 1", m);
+    if (q.a != members[0].a || q.dt != members[0].dt || q.T0 != members[0].T0 ||
+        (q.expanding != 0) != (members[0].expanding != 0) || (q.expanding && q.H0 != members[0].H0))
+      return set_error(PHN_ERR_INVALID, "member %d: members share a, dt, T0 and the box (expanding, H0): one clock",
+                       m);
   }
   phn_ensemble *e = new phn_ensemble();
   e->n = n;
@@ -491,7 +550,7 @@ int phn_ensemble_create(const phn_params *members, int n, phn_ensemble **out) {
   CKC(cudaMemset(e->pi, 0, total * sizeof(float)));
   CKC(cudaMalloc(&e->d_item_begin, (n + 1) * sizeof(int)));
   CKC(cudaMalloc(&e->d_avg, n * sizeof(phn_averages)));
-  CKC(cudaMalloc(&e->d_factors, 2 * kGraphSteps * sizeof(double)));
+  CKC(cudaMalloc(&e->d_factors, 3 * kGraphSteps * sizeof(double)));
   const size_t refn = (size_t)e->maxN * e->maxN * (e->maxN + 2);
   CKC(cudaMalloc(&e->d_ref, refn * sizeof(double)));
 #undef CKC
@@ -500,11 +559,8 @@ int phn_ensemble_create(const phn_params *members, int n, phn_ensemble **out) {
     ens_free(e);
     return r;
   }
-  e->tau = members[0].T0;
-  e->dtau = members[0].dt * members[0].a;
-  e->last_mom = e->last_field = e->tau;
   *out = e;
-  return PHN_OK;
+  return phn_ensemble_reset(e);
 }
 
 int phn_ensemble_destroy(phn_ensemble *e) {
@@ -519,6 +575,15 @@ int phn_ensemble_reset(phn_ensemble *e) {
   e->tau = e->p[0].T0;
   e->dtau = e->p[0].dt * e->p[0].a;
   e->last_mom = e->last_field = e->tau;
+  e->expanding = e->p[0].expanding != 0;
+  e->H0 = e->p[0].H0;
+  if (e->expanding) {
+    ens_conformal(e);
+  } else {
+    e->tau_c = e->tau;
+    e->sf = 1.0;
+  }
+  e->last_mom_c = e->last_field_c = e->tau_c;
   e->steps = 0;
   return PHN_OK;
 }
@@ -555,20 +620,20 @@ int phn_ensemble_download(phn_ensemble *e, int m, double *Phi, double *Pi) {
 
 int phn_ensemble_evolve(phn_ensemble *e, int nsteps) {
   if (!e || nsteps < 0) return set_error(PHN_ERR_INVALID, "bad argument");
-  if ((size_t)2 * nsteps > e->h_factors_cap) {
+  if ((size_t)3 * nsteps > e->h_factors_cap) {
     if (e->h_factors) cudaFreeHost(e->h_factors);
     e->h_factors = nullptr;
-    e->h_factors_cap = 2 * (size_t)(nsteps + kGraphSteps);
+    e->h_factors_cap = 3 * (size_t)(nsteps + kGraphSteps);
     CKE(cudaHostAlloc((void **)&e->h_factors, e->h_factors_cap * sizeof(double), cudaHostAllocDefault));
   }
   // the whole call's factors are written before any copy reads them
-  for (int s = 0; s < nsteps; ++s) ens_clock_step(e, &e->h_factors[2 * s], &e->h_factors[2 * s + 1]);
+  for (int s = 0; s < nsteps; ++s) ens_clock_step(e, &e->h_factors[3 * s]);
   CKE(cudaEventRecord(e->ev0, e->stream));
   int done = 0;
   while (nsteps - done >= kGraphSteps) {
     int r = ens_build_graph(e, e->cur);
     if (r) return r;
-    CKE(cudaMemcpyAsync(e->d_factors, e->h_factors + 2 * done, 2 * kGraphSteps * sizeof(double),
+    CKE(cudaMemcpyAsync(e->d_factors, e->h_factors + 3 * done, 3 * kGraphSteps * sizeof(double),
                         cudaMemcpyHostToDevice, e->stream));
     CKE(cudaGraphLaunch(e->graph[e->cur], e->stream));
     e->launches += kGraphSteps;
@@ -576,7 +641,7 @@ int phn_ensemble_evolve(phn_ensemble *e, int nsteps) {
   }
   if (done < nsteps) {
     const int rest = nsteps - done;
-    CKE(cudaMemcpyAsync(e->d_factors, e->h_factors + 2 * done, 2 * rest * sizeof(double), cudaMemcpyHostToDevice,
+    CKE(cudaMemcpyAsync(e->d_factors, e->h_factors + 3 * done, 3 * rest * sizeof(double), cudaMemcpyHostToDevice,
                         e->stream));
     for (int i = 0; i < rest; ++i) {
       int r = ens_launch_step(e, MODE_STEP, i, e->cur);
@@ -597,7 +662,7 @@ int phn_ensemble_averages(phn_ensemble *e, phn_averages *out) {
   if (!e || !out) return set_error(PHN_ERR_INVALID, "bad argument");
   int r = ens_launch_step(e, MODE_OBS, 0, e->cur);
   if (r) return r;
-  ens_fold<<<e->n, FIN_THREADS, 0, e->stream>>>(e->partials, e->d_item_begin, e->d_members, e->d_avg);
+  ens_fold<<<e->n, FIN_THREADS, 0, e->stream>>>(e->partials, e->d_item_begin, e->d_members, e->sf, e->d_avg);
   CKE(cudaGetLastError());
   e->launches++;
   CKE(cudaMemcpyAsync(out, e->d_avg, e->n * sizeof(phn_averages), cudaMemcpyDeviceToHost, e->stream));
@@ -624,6 +689,9 @@ int phn_ensemble_islands(phn_ensemble *e, int m, double thres, int mode, int z_p
   v.phi[0] = e->phi[e->cur] + e->off[m];
   v.pi = e->pi + e->off[m];
   v.stream = e->stream;
+  v.tau = e->tau;  // the expanding box's island terms read the scale factor
+  v.tau_c = e->tau_c;
+  v.sf = e->sf;
   const int r = phn_islands(&v, thres, mode, z_periodic, labels, out, max_out, n_islands);
   e->launches += v.launches;
   v.launches = 0;
@@ -637,7 +705,7 @@ int phn_ensemble_autotune(phn_ensemble *e, int steps, int *tile, double *best_ms
   float *save = nullptr;
   CKE(cudaMallocAsync((void **)&save, e->total * sizeof(float), e->stream));
   CKE(cudaMemcpyAsync(save, e->pi, e->total * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
-  const double f[2] = {e->dtau, e->dtau};
+  const double f[3] = {e->dtau, e->dtau, e->sf};
   CKE(cudaMemcpyAsync(e->d_factors, f, sizeof(f), cudaMemcpyHostToDevice, e->stream));
   double best = 1e30;
   int best_t = e->tile;

@@ -63,6 +63,44 @@ def test_members_match_single_lattice_runs(tile):
                     assert np.array_equal(lab, olab) and orecs.shape[0] == n_ens
 
 
+@pytest.mark.parametrize("tile", [0, 6])  # a scalar tile and an x4 tile
+def test_expanding_members_match_single_lattice_runs(tile):
+    """The expanding box (one H0, one clock): a member's fields equal a
+    single expanding lattice's bit for bit (the kick's couplings scaled by
+    the step's scale factor with the handle's expressions), the averages'
+    extrema exactly and their sums to FP32 summation order, the time and
+    scale-factor columns exactly; island counts equal."""
+    from phinum_gb300 import lattice as PL
+    ms, fields = members()
+    ms, fields = ms[:3], fields[:3]
+    for p in ms:
+        p.expansion, p.H0, p.T0 = 1, 0.05, 2.0
+    steps = 137
+    with PL.Ensemble(ms) as ens:
+        ens.set_tile(tile)
+        for m, (phi, pi) in enumerate(fields):
+            ens.upload(m, phi, pi)
+        ens.evolve(steps)
+        avg = ens.averages()
+        for m, p in enumerate(ms):
+            with PL.Lattice(p) as lat:
+                lat.upload(*fields[m])
+                lat.evolve(steps)
+                sphi, spi = lat.download()
+                savg = lat.volume_averages()
+                ephi, epi = ens.download(m)
+                N = p.N
+                assert np.array_equal(ephi, sphi), m
+                assert np.array_equal(epi[N * N:-N * N], spi[N * N:-N * N]), m
+                assert avg[m, 0] == savg[0] and avg[m, 25] == savg[25] and savg[25] > 1.0, m
+                assert np.array_equal(avg[m, 17:23], savg[17:23]), m
+                np.testing.assert_allclose(avg[m, 9:17], savg[9:17], rtol=1e-6, atol=1e-9)
+                thr = float(np.quantile(np.sqrt(sphi[N * N:-N * N] ** 2 + spi[N * N:-N * N] ** 2), 0.9))
+                n_ens, _ = ens.islands(m, thr)
+                _, recs = lat.full_analysis(thr, labels=False)
+                assert n_ens == recs.shape[0], m
+
+
 def test_autotune_keeps_state():
     from phinum_gb300 import lattice as PL
     ms, fields = members()
@@ -90,3 +128,11 @@ def test_ensemble_validation():
     with pytest.raises(L.PhnError) as e:
         PL.Ensemble([PL.Params(N=48, precision=1)])
     assert e.value.code == L.ERR_UNSUPPORTED
+    # one clock: every member expanding with one H0, or none
+    with pytest.raises(L.PhnError) as e:
+        PL.Ensemble([PL.Params(N=32, precision=1, expansion=1), PL.Params(N=32, precision=1)])
+    assert e.value.code == L.ERR_INVALID
+    with pytest.raises(L.PhnError) as e:
+        PL.Ensemble([PL.Params(N=32, precision=1, expansion=1, H0=0.05),
+                     PL.Params(N=32, precision=1, expansion=1, H0=0.06)])
+    assert e.value.code == L.ERR_INVALID
