@@ -447,8 +447,11 @@ int phn_ensemble_stats(const phn_ensemble *e, long long *kernel_launches, double
  * step kernels as phn_evolve, checkpoints every `every` steps.  Backward: the
  * discrete adjoint of the implemented leapfrog, reverse time stepping that
  * restarts from each checkpoint (finite-precision reversal drifts).
- * Theory 0 or 1, Nc = 1, static box, FP32 or FP64 (the FP64 run is the
- * reference gradient). */
+ * Theory 0 or 1, Nc = 1, static or expanding box, FP32 or FP64 (the FP64
+ * run is the reference gradient).  In the expanding box rho carries the
+ * kinetic terms of fieldanalysis.cpp:626-629 and the couplings at the final
+ * scale factor, each reverse step the couplings of its kick; dJ/dc6 and dJ/dh
+ * stay derivatives by the unscaled couplings. */
 typedef struct phn_adjoint phn_adjoint;
 int phn_adjoint_create(const phn_params *params, int nsteps, int every, double width, phn_adjoint **out);
 int phn_adjoint_destroy(phn_adjoint *a);

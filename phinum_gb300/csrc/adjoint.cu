@@ -50,22 +50,6 @@ struct AdjOps<double> {
   __device__ static double fma_(double a, double b, double c) { return fma(a, b, c); }
 };
 
-// Potential pieces for one component (Nc = 1), in T arithmetic.
-//   V'(phi)  = (mmM + lm phi^2/6 [+ phi^4 / (120 Kappa^2)]) phi [+ h]
-//   V''(phi) =  mmM + lm phi^2/2 [+ 5 phi^4 / (120 Kappa^2)]
-// F = Lap(phi) - V'(phi), the Laplacian given as the sum of the six
-// neighbour differences (phi_nb - phi), as in the FP32 forward kernels.
-template <typename T>
-__device__ __forceinline__ T force(const Consts &k, T diff_sum, T c) {
-  const T inv_a2 = (T)1 / (T)k.a2;
-  const T l = c * c;
-  T coef = (T)k.mmM + l * ((T)k.lm / (T)k.six_nc);
-  if (k.theory == 0) coef += (l * l) * ((T)1 / ((T)k.kappa * (T)k.kappa * (T)k.c120));
-  T f = diff_sum * inv_a2 - coef * c;
-  if (k.theory == 1) f -= (T)k.h;
-  return f;
-}
-
 // Per-thread compensated sum (Kahan) in T; FP64 only once per thread.
 template <typename T>
 struct KSum {
@@ -79,24 +63,23 @@ struct KSum {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-template <typename T>
-__device__ __forceinline__ T vpp(const Consts &k, T c) {
-  const T l = c * c;
-  T v = (T)k.mmM + (T)3 * l * ((T)k.lm / (T)k.six_nc);
-  if (k.theory == 0) v += (T)5 * (l * l) * ((T)1 / ((T)k.kappa * (T)k.kappa * (T)k.c120));
-  return v;
-}
-
-// force and vpp with their coefficients formed once per thread (the same
-// expressions, so the same values), for the one-site-per-thread reverse step
-// whose FP64 form is bound by GB300's FP64 rate.
+// The potential's pieces for one component (Nc = 1), coefficients formed
+// once per thread, for the one-site-per-thread reverse step (its FP64 form is
+// bound by GB300's FP64 rate):
+//   V'(phi)  = (mmM + lm phi^2/6 [+ phi^4 / (120 Kappa^2)]) phi [+ h]
+//   V''(phi) =  mmM + lm phi^2/2 [+ 5 phi^4 / (120 Kappa^2)]
+// F = Lap(phi) - V'(phi), the Laplacian given as the sum of the six
+// neighbour differences (phi_nb - phi), as in the FP32 forward kernels.
 template <typename T>
 struct PotCoef {
   T inv_a2, l6, c6, mmM, h;
   int theory;
+  // the expanding box's couplings come scaled (at_scale_factor: mmM sf^2,
+  // h sf^3) but for c6, scaled here by 1/sf^2 (sf = 1 for the static box)
   __device__ explicit PotCoef(const Consts &k)
       : inv_a2((T)1 / (T)k.a2), l6((T)k.lm / (T)k.six_nc),
-        c6((T)1 / ((T)k.kappa * (T)k.kappa * (T)k.c120)), mmM((T)k.mmM), h((T)k.h), theory(k.theory) {}
+        c6((T)1 / ((T)k.kappa * (T)k.kappa * (T)k.c120 * (T)k.sf * (T)k.sf)), mmM((T)k.mmM), h((T)k.h),
+        theory(k.theory) {}
   __device__ __forceinline__ T force(T diff_sum, T c) const {
     const T l = c * c;
     T coef = mmM + l * l6;
@@ -190,8 +173,8 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
                                                             const T *__restrict__ lphi, const T *__restrict__ lpi,
                                                             T *__restrict__ phi0, T *__restrict__ pi0,
                                                             T *__restrict__ lphi0, T *__restrict__ lpi0,
-                                                            const Consts k, const T fk, const T fd, const int cz,
-                                                            double *__restrict__ gs) {
+                                                            const Consts k, const T fk, const T fd, const double gk6,
+                                                            const double gkh, const int cz, double *__restrict__ gs) {
   const int N = k.N;
   const int x = blockIdx.x * ADJ_TX + threadIdx.x, y = blockIdx.y * ADJ_TY + threadIdx.y;
   const int z0 = blockIdx.z * cz, z1 = min(z0 + cz, N);
@@ -260,7 +243,7 @@ __global__ void __launch_bounds__(ADJ_THREADS) adjoint_step(const T *__restrict_
       mc = mn;
     }
   }
-  grad_slot_add(-6.0 * (double)fk * k_c6.value(), -(double)fk * k_h.value(), gs, threadIdx.x + ADJ_TX * threadIdx.y,
+  grad_slot_add(-6.0 * gk6 * k_c6.value(), -gkh * k_h.value(), gs, threadIdx.x + ADJ_TX * threadIdx.y,
                 ADJ_THREADS / 32);
 }
 
@@ -290,7 +273,8 @@ __global__ void __launch_bounds__(ADJ_THREADS, THEORY == 0 ? 3 : 0) adjoint_step
                                                                const float *__restrict__ lpi, float *__restrict__ phi0,
                                                                float *__restrict__ pi0, float *__restrict__ lphi0,
                                                                float *__restrict__ lpi0, const Consts k, const float fk,
-                                                               const float fd, const int cz, double *__restrict__ gs) {
+                                                               const float fd, const float gk6, const float gkh,
+                                                               const int cz, double *__restrict__ gs) {
   const int N = k.N;
   const int x0 = (blockIdx.x * ADJ_TX + threadIdx.x) * 4, y = blockIdx.y * ADJ_TY + threadIdx.y;
   const int z0 = blockIdx.z * cz, z1 = min(z0 + cz, N);
@@ -335,8 +319,8 @@ __global__ void __launch_bounds__(ADJ_THREADS, THEORY == 0 ? 3 : 0) adjoint_step
         f4set(o_phi, e, c);
         f4set(o_pi, e, fmaf(-fk, force_f32<THEORY>(k, lap, c, c2), f4get(pic, e)));
         f4set(o_lphi, e, fmaf(fk, fmaf(-vpp, m, lmu), f4get(lphic, e)));
-        k_c6.add(fk * m * (-6.f * (c2 * c2 * c)));
-        k_h.add(-fk * m);
+        k_c6.add(gk6 * m * (-6.f * (c2 * c2 * c)));
+        k_h.add(-gkh * m);
       }
       *(float4 *)(phi0 + i) = o_phi;
       *(float4 *)(pi0 + i) = o_pi;
@@ -466,7 +450,12 @@ __global__ void __launch_bounds__(OBJ_THREADS) obj_rho(const T *__restrict__ phi
     double v = k.mm_half_M * c2 + k.lm * (c4 * i24);
     if (k.theory == 0) v += c4 * c2 * i720;
     if (k.theory == 1) v += k.h * c;
-    const double r = 0.5 * p * p + 0.5 * grad + v;
+    double kin = 0.5 * p * p;
+    if (k.expansion) {  // fieldanalysis.cpp:626-629: + (H0/sf)^2 phi^2 / 2 - phi pi H0/sf
+      const double hub = k.H0 / k.sf;
+      kin += 0.5 * (hub * hub) * c2 - c * p * hub;
+    }
+    const double r = kin + 0.5 * grad + v;
     rho[i] = r;
     acc += r;
   }
@@ -547,8 +536,14 @@ __global__ void __launch_bounds__(OBJ_THREADS) obj_adjoint_init(const T *__restr
     double vp = 2.0 * k.mm_half_M * c + l6 * c2 * c;
     if (k.theory == 0) vp += 6.0 * c2 * c2 * c * i720;
     if (k.theory == 1) vp += k.h;
-    lphi[i] = (L)(gi * (-fwd * ia2 + vp) + bwd * ia2);
-    lpi[i] = (L)(gi * (double)pi[i]);
+    double dk_phi = 0.0, dk_pi = (double)pi[i];  // the kinetic term's derivatives
+    if (k.expansion) {
+      const double hub = k.H0 / k.sf;
+      dk_phi = (hub * hub) * c - (double)pi[i] * hub;
+      dk_pi -= c * hub;
+    }
+    lphi[i] = (L)(gi * (-fwd * ia2 + vp + dk_phi) + bwd * ia2);
+    lpi[i] = (L)(gi * dk_pi);
     a6 += gi * (c2 * c2 * c2);
     ah += gi * c;
   }
@@ -589,6 +584,8 @@ struct phn_adjoint {
   double *gs;              // gradient slots [blocks][ADJ_NG]
   int sum_blocks;
   std::vector<double> fk, fd;  // clock factors of each forward step
+  std::vector<double> sfk;     // the scale factor of each step's kick (1 for the static box)
+  double sf_fin;               // the scale factor of the final state (J's)
   bool forward_done;
   double J, mean, S;
   cudaEvent_t ev0, ev1;
@@ -644,11 +641,51 @@ static void adj_free(phn_adjoint *a) {
 
 // J and its seed g on the current forward state (phi, pi device pointers);
 // <rho>, J, S are copied to the pinned h_res (read after the stream syncs).
+// The clock of one evolve() as the handle runs it (dynamics.cpp:196-237):
+// the kick factor, the drift factor and the kick's scale factor (conformal
+// times and sqrt(1 + 2 H0 tau) in the expanding box, 1 in the static one).
+struct AdjClock {
+  double tau, dtau, lm, lf, lmc, lfc, tc, H0;
+  bool ex;
+  void step(double &fk, double &fd, double &sfk) {
+    tau += 0.5 * dtau;
+    if (ex) {
+      tc = (sqrt(1. + 2. * H0 * tau) - 1.) / H0;
+      sfk = sqrt(1. + 2. * H0 * tau);
+      fk = tc - lmc;
+    } else {
+      sfk = 1.0;
+      fk = tau - lm;
+    }
+    lm = tau;
+    lmc = ex ? tc : tau;
+    tau += 0.5 * dtau;
+    if (ex) {
+      tc = (sqrt(1. + 2. * H0 * tau) - 1.) / H0;
+      fd = tc - lfc;
+    } else {
+      fd = tau - lf;
+      tc = tau;
+    }
+    lf = tau;
+    lfc = tc;
+  }
+  double sf() const { return ex ? sqrt(1. + 2. * H0 * tau) : 1.0; }
+};
+
+// The couplings of the final state (J) and of step n's kick.
+static Consts final_consts(const phn_adjoint *a) {
+  return a->p.expanding ? at_scale_factor(a->k, a->sf_fin) : a->k;
+}
+static Consts step_consts(const phn_adjoint *a, int n) {
+  return a->p.expanding ? at_scale_factor(a->k, a->sfk[n]) : a->k;
+}
+
 template <typename T>
 static int objective(phn_adjoint *a, const T *phi, const T *pi, cudaStream_t st) {
   const int nb = a->sum_blocks;
   double *res = a->sums + 3 * nb;
-  obj_rho<T><<<nb, OBJ_THREADS, 0, st>>>(phi, pi, a->k, make_divn((unsigned)a->k.N), a->rho, a->sums);
+  obj_rho<T><<<nb, OBJ_THREADS, 0, st>>>(phi, pi, final_consts(a), make_divn((unsigned)a->k.N), a->rho, a->sums);
   obj_sigmoid<<<nb, OBJ_THREADS, 0, st>>>(a->rho, a->V, a->w, a->g, a->sums, nb);
   obj_seed<<<nb, OBJ_THREADS, 0, st>>>(a->rho, a->V, a->w, a->g, a->sums, nb, res);
   CKA(cudaGetLastError());
@@ -664,8 +701,8 @@ int phn_adjoint_create(const phn_params *params, int nsteps, int every, double w
   *out = nullptr;
   int r = validate_params(params);
   if (r) return r;
-  if (params->Nc != 1 || params->precision == PHN_FP32_KAHAN || params->potential > 1 || params->expanding)
-    return set_error(PHN_ERR_UNSUPPORTED, "adjoint: theories 0 and 1, Nc = 1, FP32 or FP64, static box");
+  if (params->Nc != 1 || params->precision == PHN_FP32_KAHAN || params->potential > 1)
+    return set_error(PHN_ERR_UNSUPPORTED, "adjoint: theories 0 and 1, Nc = 1, FP32 or FP64");
   phn_adjoint *a = new phn_adjoint();
   a->p = *params;
   a->k = make_consts(params);
@@ -732,8 +769,10 @@ static int forward_pair(phn_adjoint *a, const double *Phi0, const double *Pi0) {
   if (!a->pgraph_ok) {
     a->fk.clear();
     a->fd.clear();
-    double tau = a->p.T0, lm = tau, lf = tau;
-    const double dtau = a->p.dt * a->p.a;
+    a->sfk.clear();
+    AdjClock ck_{a->p.T0, a->p.dt * a->p.a, a->p.T0, a->p.T0, 0.0, 0.0, a->p.T0, a->p.H0, a->p.expanding != 0};
+    if (ck_.ex) ck_.tc = (sqrt(1. + 2. * ck_.H0 * ck_.tau) - 1.) / ck_.H0;  // phn_reset's conformal time
+    ck_.lmc = ck_.lfc = ck_.tc;
     int cur = 0;
     char *ck = (char *)a->ckpt;
     CKA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -741,16 +780,13 @@ static int forward_pair(phn_adjoint *a, const double *Phi0, const double *Pi0) {
     if (le == cudaSuccess) le = cudaMemcpyAsync(ck + fb, a->pqh, fb, cudaMemcpyDeviceToDevice, st);
     for (int s = 0; s < a->nseg && le == cudaSuccess; ++s) {
       for (int i = 0; i < a->every && le == cudaSuccess; ++i) {
-        tau += 0.5 * dtau;
-        const double fk = tau - lm;
-        lm = tau;
-        tau += 0.5 * dtau;
-        const double fd = tau - lf;
-        lf = tau;
+        double fk, fd, sfk;
+        ck_.step(fk, fd, sfk);
         a->fk.push_back(fk);
         a->fd.push_back(fd);
-        le = launch_step_pair(a->k, fk, fd, a->pph[cur], a->ppl[cur], a->pqh, a->pql, a->pph[1 - cur],
-                              a->ppl[1 - cur], st);
+        a->sfk.push_back(sfk);
+        le = launch_step_pair(step_consts(a, (int)a->sfk.size() - 1), fk, fd, a->pph[cur], a->ppl[cur], a->pqh,
+                              a->pql, a->pph[1 - cur], a->ppl[1 - cur], st);
         cur = 1 - cur;
       }
       if (le == cudaSuccess)
@@ -758,6 +794,7 @@ static int forward_pair(phn_adjoint *a, const double *Phi0, const double *Pi0) {
       if (le == cudaSuccess)
         le = cudaMemcpyAsync(ck + (size_t)(s + 1) * 2 * fb + fb, a->pqh, fb, cudaMemcpyDeviceToDevice, st);
     }
+    a->sf_fin = ck_.sf();
     if (le == cudaSuccess) le = launch_pair_to_f64(a->pph[cur], a->ppl[cur], a->pfin, N, st);
     if (le == cudaSuccess) le = launch_pair_to_f64(a->pqh, a->pql, a->pfin + V, N, st);
     cudaGraph_t g = nullptr;
@@ -805,6 +842,7 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
   char *ck = (char *)a->ckpt;
   a->fk.clear();
   a->fd.clear();
+  a->sfk.clear();
   phn_device_fields(h, &phi, &pi, &stv);
   cudaStream_t st = (cudaStream_t)stv;
   // an FP64 forward under an FP32 reverse sweep stores FP32 checkpoints
@@ -820,15 +858,15 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
   CKA(store(ck + fb, pi));
   for (int s = 0; s < a->nseg; ++s) {
     // the factors the next `every` steps will use: the clock arithmetic of
-    // dynamics.cpp:200-213, as the handle runs it
-    double tau = h->tau, lm = h->last_mom, lf = h->last_field;
+    // dynamics.cpp:196-237, as the handle runs it
+    AdjClock ck_{h->tau, h->dtau, h->last_mom, h->last_field, h->last_mom_c, h->last_field_c, h->tau_c,
+                 a->p.H0, a->p.expanding != 0};
     for (int i = 0; i < a->every; ++i) {
-      tau += 0.5 * h->dtau;
-      a->fk.push_back(tau - lm);
-      lm = tau;
-      tau += 0.5 * h->dtau;
-      a->fd.push_back(tau - lf);
-      lf = tau;
+      double fk, fd, sfk;
+      ck_.step(fk, fd, sfk);
+      a->fk.push_back(fk);
+      a->fd.push_back(fd);
+      a->sfk.push_back(sfk);
     }
     r = evolve_async(h, a->every);
     if (r) return r;
@@ -836,6 +874,7 @@ int phn_adjoint_forward(phn_adjoint *a, const double *Phi0, const double *Pi0, d
     CKA(store(ck + (size_t)(s + 1) * 2 * fb, phi));
     CKA(store(ck + (size_t)(s + 1) * 2 * fb + fb, pi));
   }
+  a->sf_fin = h->sf;
   if (a->fwd_elem == 8)
     r = objective<double>(a, (const double *)phi, (const double *)pi, st);
   else
@@ -885,21 +924,26 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
       for (int i = a->every - 1; i >= 0 && le == cudaSuccess; --i) {
         const int n = s * a->every + i;
         void *phi0 = a->rphi[sbuf], *pi0 = a->rpi[sbuf];
+        // step n's couplings and its coupling-gradient factors: the kick's
+        // V' holds c6 / sf^2 and h sf^3 in the expanding box (1 when static)
+        const Consts kn = step_consts(a, n);
+        const double sfk = a->sfk[n], s6 = 1.0 / (sfk * sfk), sh = sfk * sfk * sfk;
+        const double fkT = dbl ? a->fk[n] : (double)(float)a->fk[n];
         if (dbl)
           adjoint_step<double><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
               (const double *)phi1, (const double *)pi1, (const double *)a->lphi[cur], (const double *)a->lpi[cur],
-              (double *)phi0, (double *)pi0, (double *)a->lphi[1 - cur], (double *)a->lpi[1 - cur], a->k,
-              a->fk[n], a->fd[n], gr.cz, a->gs);
+              (double *)phi0, (double *)pi0, (double *)a->lphi[1 - cur], (double *)a->lpi[1 - cur], kn,
+              a->fk[n], a->fd[n], fkT * s6, fkT * sh, gr.cz, a->gs);
         else if (x4)
           (a->k.theory == 0 ? adjoint_step_x4<0> : adjoint_step_x4<1>)<<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
               (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
-              (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
-              (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
+              (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], kn,
+              (float)a->fk[n], (float)a->fd[n], (float)(fkT * s6), (float)(fkT * sh), gr.cz, a->gs);
         else
           adjoint_step<float><<<gr.grid, dim3(ADJ_TX, ADJ_TY), 0, st>>>(
               (const float *)phi1, (const float *)pi1, (const float *)a->lphi[cur], (const float *)a->lpi[cur],
-              (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], a->k,
-              (float)a->fk[n], (float)a->fd[n], gr.cz, a->gs);
+              (float *)phi0, (float *)pi0, (float *)a->lphi[1 - cur], (float *)a->lpi[1 - cur], kn,
+              (float)a->fk[n], (float)a->fd[n], fkT * s6, fkT * sh, gr.cz, a->gs);
         le = cudaGetLastError();
         cur = 1 - cur;
         phi1 = phi0;
@@ -926,18 +970,19 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
   // (on the forward's final state: FP64 when the forward ran in FP64, the
   // pair state widened to FP64 when it ran in pairs)
   const DivN dn = make_divn((unsigned)a->k.N);
+  const Consts kf = final_consts(a);
   if (dbl)
-    obj_adjoint_init<double, double><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k, dn,
+    obj_adjoint_init<double, double><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, kf, dn,
                                                                  (double *)a->lphi[0], (double *)a->lpi[0], a->sums,
                                                                  nb);
   else if (a->pair)
-    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>(a->pfin, a->pfin + a->V, a->g, a->k, dn,
+    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>(a->pfin, a->pfin + a->V, a->g, kf, dn,
                                                                 (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   else if (a->fwd_elem == 8)
-    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, a->k, dn,
+    obj_adjoint_init<double, float><<<nb, OBJ_THREADS, 0, st>>>((const double *)phi, (const double *)pi, a->g, kf, dn,
                                                                 (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   else
-    obj_adjoint_init<float, float><<<nb, OBJ_THREADS, 0, st>>>((const float *)phi, (const float *)pi, a->g, a->k, dn,
+    obj_adjoint_init<float, float><<<nb, OBJ_THREADS, 0, st>>>((const float *)phi, (const float *)pi, a->g, kf, dn,
                                                                (float *)a->lphi[0], (float *)a->lpi[0], a->sums, nb);
   CKA(cudaGetLastError());
   CKA(cudaGraphLaunch(a->sweep, st));
@@ -989,9 +1034,12 @@ int phn_adjoint_backward(phn_adjoint *a, double *dPhi0, double *dPi0, double *gr
     CKA(cudaStreamSynchronize(st));
   }
   if (grads) {
+    // J's own coupling terms: the final state's V holds c6 / sf^2 and h sf^3
+    // in the expanding box
+    const double sf = a->p.expanding ? a->sf_fin : 1.0;
     grads[0] = sum_lphi;
-    grads[1] = g_c6 + direct_c6;
-    grads[2] = g_h + direct_h;
+    grads[1] = g_c6 + (a->p.expanding ? direct_c6 / (sf * sf) : direct_c6);
+    grads[2] = g_h + (a->p.expanding ? direct_h * (sf * sf * sf) : direct_h);
   }
   return PHN_OK;
 }

@@ -17,7 +17,7 @@
 // FP32 does not help there, because the increments dt F and dt pi are
 // themselves rounded to FP32 every step (an error correlated from step to
 // step, which grows linearly).  Here force, increments and updates are all
-// pair arithmetic.  Theories 0 and 1, Nc = 1, static box.
+// pair arithmetic.  Theories 0 and 1, Nc = 1, static or expanding box.
 #include "phn_internal.h"
 
 namespace phn {
@@ -305,7 +305,9 @@ PairConsts pair_consts(const Consts &k) {
   }
   c.mmM = f2_of(k.mmM);
   c.c4 = f2_of(k.lm / k.six_nc);
-  c.c6 = f2_of(k.theory == 0 ? 1.0 / (k.kappa * k.kappa * k.c120) : 0.0);
+  // the expanding box's couplings at the step's scale factor: mmM and h come
+  // scaled (at_scale_factor), c6 is divided by sf^2 here (sf = 1 when static)
+  c.c6 = f2_of(k.theory == 0 ? 1.0 / (k.kappa * k.kappa * k.c120 * k.sf * k.sf) : 0.0);
   c.h = f2_of(k.h);
   c.fk = c.fd = F2{0.f, 0.f};
   return c;

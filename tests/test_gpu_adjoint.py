@@ -30,11 +30,16 @@ def direction(N, seed):
     return v / np.linalg.norm(v[N * N:-N * N])
 
 
+@pytest.mark.parametrize("expansion", [0, 1])
 @pytest.mark.parametrize("theory", [0, 1])
-def test_fp64_adjoint_matches_finite_differences(theory):
+def test_fp64_adjoint_matches_finite_differences(theory, expansion):
+    """Static and expanding box (H0 = 0.05 from T0 = 2: the scale factor
+    grows from 1.095 to 1.105 over the run)."""
     from phinum_gb300 import lattice as PL
     N, steps, every = 16, 40, 10
     kw, phi, pi = setup(N, 7 + theory, theory)
+    if expansion:
+        kw = dict(kw, expansion=1, H0=0.05, T0=2.0)
     p = PL.Params(N=N, precision=0, **kw)
     with PL.Adjoint(p, steps, every) as adj:
         J0 = adj.forward(phi, pi)
@@ -68,10 +73,13 @@ def test_fp64_adjoint_matches_finite_differences(theory):
     assert abs(ad - fd) <= 2e-6 * abs(fd), (ad, fd)
 
 
-def test_fp32_adjoint_close_to_fp64_adjoint():
+@pytest.mark.parametrize("expansion", [0, 1])
+def test_fp32_adjoint_close_to_fp64_adjoint(expansion):
     from phinum_gb300 import lattice as PL
     N, steps, every = 32, 100, 50
     kw, phi, pi = setup(N, 21)
+    if expansion:
+        kw = dict(kw, expansion=1, H0=0.05, T0=2.0)
     out = {}
     for prec in (0, 1):
         with PL.Adjoint(PL.Params(N=N, precision=prec, **kw), steps, every) as adj:
@@ -138,7 +146,8 @@ def test_fp64_forward_fp32_adjoint_within_1e4_of_fp64_adjoint():
         assert np.array_equal(x, y)
 
 
-def test_pair_forward_fp32_adjoint_within_1e4_of_fp64_adjoint():
+@pytest.mark.parametrize("expansion", [0, 1])
+def test_pair_forward_fp32_adjoint_within_1e4_of_fp64_adjoint(expansion):
     """phn_adjoint_set_forward_precision(PHN_FP32_PAIR): the forward in FP32
     pairs (double-float arithmetic), FP32 checkpoints and reverse sweep.  J is
     the FP64 adjoint's to 1e-8 relative (the pair state carries ~48 bits; its
@@ -150,6 +159,8 @@ def test_pair_forward_fp32_adjoint_within_1e4_of_fp64_adjoint():
     from phinum_gb300 import _lib as L
     N, steps, every = 32, 200, 50
     kw, phi, pi = setup(N, 23)
+    if expansion:  # the pair step takes each step's scale factor like the FP64 one
+        kw = dict(kw, expansion=1, H0=0.05, T0=2.0)
     sl = slice(N * N, -N * N)
     with PL.Adjoint(PL.Params(N=N, precision=0, **kw), steps, every) as adj:
         J64 = adj.forward(phi, pi)

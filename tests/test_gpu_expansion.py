@@ -110,7 +110,9 @@ def test_fast_paths_match_plain_under_expansion(N, theory, precision):
 
 
 def test_expanding_box_errors_are_status_codes():
-    """The ensemble and the adjoint are static-box forms; bad H_0 is refused."""
+    """Bad H_0, expansion switch or T0 is refused; the ensemble and the adjoint
+    take the expanding box (their own tests compare them with single lattices
+    and finite differences), the ensemble only with one clock."""
     from phinum_gb300 import lattice as PL
     from phinum_gb300 import _lib as L
     for kw, code in ((dict(expansion=1, H0=0.0), L.ERR_INVALID), (dict(expansion=2), L.ERR_INVALID),
@@ -119,9 +121,8 @@ def test_expanding_box_errors_are_status_codes():
             PL.Lattice(PL.Params(N=8, **kw))
         assert e.value.code == code
     p = PL.Params(N=32, precision=1, expansion=1)
+    PL.Ensemble([p, p]).close()
+    PL.Adjoint(PL.Params(N=16, precision=0, expansion=1), 10, 5).close()
     with pytest.raises(L.PhnError) as e:
-        PL.Ensemble([p, p])
-    assert e.value.code == L.ERR_UNSUPPORTED
-    with pytest.raises(L.PhnError) as e:
-        PL.Adjoint(PL.Params(N=16, precision=0, expansion=1), 10, 5)
-    assert e.value.code == L.ERR_UNSUPPORTED
+        PL.Ensemble([p, PL.Params(N=32, precision=1)])
+    assert e.value.code == L.ERR_INVALID
