@@ -430,6 +430,13 @@ def measure_gpu(args, dist: Dist):
         also["adjoint_c4_fp32"] = {k: adj[k] for k in ("cost_ratio", "forward_plain_ms", "adjoint_forward_ms",
                                                        "adjoint_backward_ms", "timing", "fp32_vs_fp64_field_rel_l2")}
         also["adjoint_c4_fp32_pair_forward"] = adj["fp32_pair"]
+        # the form held to "at most 3x a forward solve at a gradient error
+        # below 1e-4" (both figures from the same solve)
+        pf = adj["fp32_pair"]
+        also["adjoint_c4_target"] = {
+            "form": "FP32 reverse sweep, forward in FP32 pairs", "cost_ratio": pf["cost_ratio"],
+            "field_gradient_rel_l2_vs_fp64": pf["vs_fp64_field_rel_l2"],
+            "met": bool(pf["cost_ratio"] <= 3.0 and pf["vs_fp64_field_rel_l2"] < 1e-4)}
     out["also"] = also
     return out
 
