@@ -282,22 +282,22 @@ constexpr int RUN_Q = 4;
 constexpr int RUN_STAGE = RUN_Q - 2;  // runs strictly inside a lane's modes
 constexpr int RUN_WARPS = 4;          // 128 threads: histograms of up to 1024 bins
 constexpr int RUN_THREADS = 32 * RUN_WARPS;
-constexpr int RUN_BLOCKS_PER_SM = 6;  // the resident blocks at 80 registers
+constexpr int RUN_BLOCKS_PER_SM = 7;  // resident blocks: 71 registers, 31 KB of shared memory at 284 bins
 
-__device__ __forceinline__ void run_flush(CompF *hF, CompF *hK, CompF *hQ, int bin, float f, float k, float q) {
+__device__ __forceinline__ void run_flush(CompF *hF, int nbins, int bin, float f, float k, float q) {
   hist_add(hF[bin], f);
-  hist_add(hK[bin], k);
-  hist_add(hQ[bin], q);
+  hist_add(hF[nbins + bin], k);
+  hist_add(hF[2 * nbins + bin], q);
 }
 
 // One chunk of a half row: MIRROR = 0 for px in [0, N/2) (modes at
 // direct + px), 1 for [N/2, N) (px = N/2 at direct + N/2, the others at
 // mirror - px).
-template <int MIRROR>
+template <int MIRROR, typename I>
 __device__ __forceinline__ void run_chunk(const float2 *__restrict__ fphi, const float2 *__restrict__ fpi,
-                                          const unsigned short *__restrict__ keys, long long krow, long long direct,
-                                          long long mirror, int h, int c0, int x1, bool vkeys, int lane, CompF *hF,
-                                          CompF *hK, CompF *hQ, float4 *stage) {
+                                          const unsigned short *__restrict__ keys, I krow, I direct, I mirror, int h,
+                                          int c0, int x1, bool vkeys, int lane, CompF *hF, int nbins,
+                                          float4 *stage) {
   const unsigned full = 0xffffffffu;
   const int cn = min(32 * RUN_Q, x1 - c0);
   const int nm = max(0, min(RUN_Q, cn - lane * RUN_Q));
@@ -328,12 +328,12 @@ __device__ __forceinline__ void run_chunk(const float2 *__restrict__ fphi, const
 #pragma unroll
     for (int m = 0; m < RUN_Q; ++m) kk[m] = m < nm ? pk[m] : 0u;
   }
-  const long long base = MIRROR ? mirror - px0 : direct + px0;
+  const I base = MIRROR ? mirror - (I)px0 : direct + (I)px0;
   const float2 *pa = fphi + base, *pb = fpi + base;
   // the lane's RUN_Q modes are consecutive: as 16-byte words where the
   // lowest one starts on a 16-byte boundary (the row's parity, uniform per
   // warp), else one mode per load
-  const long long lo = MIRROR ? base - (RUN_Q - 1) : base;
+  const I lo = MIRROR ? base - (I)(RUN_Q - 1) : base;
   if (nm == RUN_Q && (lo & 1) == 0) {
     const float4 *qa = (const float4 *)(fphi + lo), *qb = (const float4 *)(fpi + lo);
 #pragma unroll
@@ -419,19 +419,22 @@ __device__ __forceinline__ void run_chunk(const float2 *__restrict__ fphi, const
       F1 += p1;
       F2 += p2;
     }
-    run_flush(hF, hK, hQ, fb, F0, F1, F2);
+    run_flush(hF, nbins, fb, F0, F1, F2);
   }
-  if (nm > 0 && !conn_next) run_flush(hF, hK, hQ, lb, a0, a1, a2);
+  if (nm > 0 && !conn_next) run_flush(hF, nbins, lb, a0, a1, a2);
   const int nsmax = __reduce_max_sync(full, (unsigned)ns);
   for (int j = 0; j < nsmax; ++j) {
     if (j < ns) {
       const float4 v = stage[j * 32 + lane];
-      run_flush(hF, hK, hQ, __float_as_int(v.x), v.y, v.z, v.w);
+      run_flush(hF, nbins, __float_as_int(v.x), v.y, v.z, v.w);
     }
   }
   __syncwarp();  // the histogram and the stage are read by the next chunk
 }
 
+// I: the index type of the modes, 32-bit where N^2 (N/2 + 1) fits (fewer
+// registers), else 64-bit.
+template <typename I>
 __global__ void __launch_bounds__(RUN_THREADS, RUN_BLOCKS_PER_SM)
     bin_runs(const float2 *__restrict__ fphi, const float2 *__restrict__ fpi, const unsigned short *__restrict__ keys,
              int N, int nbins, double *__restrict__ partials) {
@@ -441,20 +444,20 @@ __global__ void __launch_bounds__(RUN_THREADS, RUN_BLOCKS_PER_SM)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < RUN_WARPS * 3 * nbins; i += RUN_THREADS) hist_zero(hist[i]);
   __syncthreads();
-  CompF *hF = hist + (size_t)warp * 3 * nbins, *hK = hF + nbins, *hQ = hK + nbins;
+  CompF *hF = hist + (size_t)warp * 3 * nbins;
   float4 *stage = stage_all + (size_t)warp * RUN_STAGE * 32;
   const int h = N / 2, M = N / 2 + 1;
   const int nrows = M * N;
   const bool vkeys = N % (2 * RUN_Q) == 0;  // every chunk's keys start on a RUN_Q-mode boundary
   for (int row = blockIdx.x * RUN_WARPS + warp; row < nrows; row += gridDim.x * RUN_WARPS) {
     const int py = row % M, pz = row / M;
-    const long long krow = (long long)row * N;
-    const long long direct = ((long long)pz * N + py) * M;
-    const long long mirror = ((long long)((N - pz) % N) * N + (N - py) % N) * M + N;
+    const I krow = (I)row * (I)N;
+    const I direct = ((I)pz * (I)N + (I)py) * (I)M;
+    const I mirror = ((I)((N - pz) % N) * (I)N + (I)((N - py) % N)) * (I)M + (I)N;
     for (int c0 = 0; c0 < h; c0 += 32 * RUN_Q)
-      run_chunk<0>(fphi, fpi, keys, krow, direct, mirror, h, c0, h, vkeys, lane, hF, hK, hQ, stage);
+      run_chunk<0, I>(fphi, fpi, keys, krow, direct, mirror, h, c0, h, vkeys, lane, hF, nbins, stage);
     for (int c0 = h; c0 < N; c0 += 32 * RUN_Q)
-      run_chunk<1>(fphi, fpi, keys, krow, direct, mirror, h, c0, N, vkeys, lane, hF, hK, hQ, stage);
+      run_chunk<1, I>(fphi, fpi, keys, krow, direct, mirror, h, c0, N, vkeys, lane, hF, nbins, stage);
   }
   __syncthreads();
   // the warps' cells (value s - c) fold in float pairs and widen once: the
@@ -667,7 +670,8 @@ static int spec_init(phn_handle *h) {
   CKS(cudaFuncSetAttribute(bin_sums<float2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
   CKS(cudaFuncSetAttribute(bin_sums<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
   CKS(cudaFuncSetAttribute(bin_keys, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(maxb * sizeof(int))));
-  CKS(cudaFuncSetAttribute(bin_runs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem(maxb)));
+  CKS(cudaFuncSetAttribute(bin_runs<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem(maxb)));
+  CKS(cudaFuncSetAttribute(bin_runs<size_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem(maxb)));
 #undef CKS
   // keys and mode counts of the reference rule (InitBCounts): field independent
   return build_keys(h, s->keys, s->counts, s->nbins, s->binsize, RULE_REFERENCE, s->h_counts, &s->mono);
@@ -713,8 +717,9 @@ static int bin_spectra(phn_handle *h, const void *fa, const void *fb, const unsi
     bin_sums<double2, double><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
         (const double2 *)fa, (const double2 *)fb, keys, N, nbins, partials);
   else if (mono)
-    bin_runs<<<s->rblocks, RUN_THREADS, run_smem(nbins), h->stream>>>((const float2 *)fa, (const float2 *)fb, keys, N,
-                                                                     nbins, partials);
+    (n_modes(N) < ((size_t)1 << 31) ? bin_runs<unsigned> : bin_runs<size_t>)<<<s->rblocks, RUN_THREADS,
+                                                                                  run_smem(nbins), h->stream>>>(
+        (const float2 *)fa, (const float2 *)fb, keys, N, nbins, partials);
   else
     bin_sums<float2, float><<<s->nblocks, SPEC_THREADS, smem, h->stream>>>(
         (const float2 *)fa, (const float2 *)fb, keys, N, nbins, partials);
