@@ -284,7 +284,15 @@ constexpr int RUN_WARPS = 4;          // 128 threads: histograms of up to 1024 b
 constexpr int RUN_THREADS = 32 * RUN_WARPS;
 constexpr int RUN_BLOCKS_PER_SM = 7;  // resident blocks: 71 registers, 31 KB of shared memory at 284 bins
 
-__device__ __forceinline__ void run_flush(CompF *hF, int nbins, int bin, float f, float k, float q) {
+// w2: the chunk's modes count twice (their row's py is neither 0 nor N/2,
+// so the weight is one per row): the doubling of each run's sums is exact,
+// and so the same bits as doubling every mode.
+__device__ __forceinline__ void run_flush(CompF *hF, int nbins, int bin, float f, float k, float q, bool w2) {
+  if (w2) {
+    f += f;
+    k += k;
+    q += q;
+  }
   hist_add(hF[bin], f);
   hist_add(hF[nbins + bin], k);
   hist_add(hF[2 * nbins + bin], q);
@@ -358,6 +366,7 @@ __device__ __forceinline__ void run_chunk(const float2 *__restrict__ fphi, const
     va[0] = fphi[direct + h];
     vb[0] = fpi[direct + h];
   }
+  const bool w2 = (kk[0] & KEY_WEIGHT2) != 0;  // one weight per row (lanes with modes)
   // runs of the lane's modes: the first (fb, F), the ones strictly inside
   // (staged), the last (cur, a: the whole of them when through)
   int fb = -1, cur = -1, ns = 0;
@@ -366,12 +375,7 @@ __device__ __forceinline__ void run_chunk(const float2 *__restrict__ fphi, const
 #pragma unroll
   for (int m = 0; m < RUN_Q; ++m) {
     if (m < nm) {
-      float f = mag2v(va[m]), k = mag2v(vb[m]), q = dotv(va[m], vb[m]);
-      if (kk[m] & KEY_WEIGHT2) {  // exact doubling
-        f += f;
-        k += k;
-        q += q;
-      }
+      const float f = mag2v(va[m]), k = mag2v(vb[m]), q = dotv(va[m], vb[m]);
       const int b = (int)(kk[m] & KEY_BIN);
       const bool nw = b != cur;  // a run starts at m
       const bool close = nw && cur >= 0;
@@ -419,14 +423,14 @@ __device__ __forceinline__ void run_chunk(const float2 *__restrict__ fphi, const
       F1 += p1;
       F2 += p2;
     }
-    run_flush(hF, nbins, fb, F0, F1, F2);
+    run_flush(hF, nbins, fb, F0, F1, F2, w2);
   }
-  if (nm > 0 && !conn_next) run_flush(hF, nbins, lb, a0, a1, a2);
+  if (nm > 0 && !conn_next) run_flush(hF, nbins, lb, a0, a1, a2, w2);
   const int nsmax = __reduce_max_sync(full, (unsigned)ns);
   for (int j = 0; j < nsmax; ++j) {
     if (j < ns) {
       const float4 v = stage[j * 32 + lane];
-      run_flush(hF, nbins, __float_as_int(v.x), v.y, v.z, v.w);
+      run_flush(hF, nbins, __float_as_int(v.x), v.y, v.z, v.w, w2);
     }
   }
   __syncwarp();  // the histogram and the stage are read by the next chunk
