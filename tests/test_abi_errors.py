@@ -81,3 +81,26 @@ def test_noalloc_scratch_limit_is_exactly_n_1024(L):
             L.ERR_INVALID
         assert (b"N <= 1024" in lib.phn_last_error()) == (N > 1024), N
         assert ((N + 31) // 32) * ((N + 7) // 8) <= 4096 or N > 1024
+
+
+def test_ensemble_and_adjoint_parameter_checks_on_the_host(L):
+    """The one-clock rule of the ensemble (a, dt, T0 and the box shared:
+    all static, or all expanding with one H0) and the adjoint's theory/Nc
+    rules are checked on the host before any CUDA call."""
+    from phinum_gb300 import lattice as PL
+    lib = L.load()
+
+    def ens(*ps):
+        arr = (L.PhnParams * len(ps))(*[p.c() for p in ps])
+        h = ctypes.c_void_p()
+        return lib.phn_ensemble_create(arr, len(ps), ctypes.byref(h))
+
+    static, exp1 = PL.Params(N=32, precision=1), PL.Params(N=32, precision=1, expansion=1, H0=0.05)
+    assert ens(static, exp1) == L.ERR_INVALID
+    assert ens(exp1, PL.Params(N=32, precision=1, expansion=1, H0=0.06)) == L.ERR_INVALID
+    assert ens(static, PL.Params(N=32, precision=1, T0=1.0)) == L.ERR_INVALID
+    assert ens(PL.Params(N=32, precision=1, theory=2, m_sqr=1.0)) == L.ERR_UNSUPPORTED
+    h = ctypes.c_void_p()
+    for p in (PL.Params(N=16, precision=0, Nc=2), PL.Params(N=16, precision=0, theory=3, m_sqr=1.0)):
+        assert lib.phn_adjoint_create(ctypes.byref(p.c()), 10, 5, 0.6, ctypes.byref(h)) == L.ERR_UNSUPPORTED
+    assert lib.phn_adjoint_create(ctypes.byref(static.c()), 10, 3, 0.6, ctypes.byref(h)) == L.ERR_INVALID
